@@ -1,0 +1,205 @@
+/*
+ * rheocell_gb300 -- C ABI of the GB300 multi-phase-field time-step engine.
+ *
+ * This is the drop-in boundary for RheoCell's time-step hot path.  In the
+ * reference, SimManager::run (src/Managers/SimManager.cpp:131-178) drives a
+ * backend chosen by BackendFactory::make_backend
+ * (src/Backends/BackendFactory.cpp:12-113, which already reserves the
+ * `backend = CUDA` / `backend_precision` slot at :37-65).  A CUDA backend
+ * class written on top of this header replaces FD_CPUBackend
+ * (src/Backends/FD_CPUBackend.cpp) and the force evaluation of the selected
+ * interaction (src/Interactions/{SimpleMultiField,ActiveNematic,
+ * WetPolarModel,WetModel}.cpp); the C++ caller above it is unchanged.
+ *
+ * Conventions
+ *  - Plain C types only; no exception crosses the ABI.  Every function that
+ *    can fail returns 0 on success and a negative rc_status otherwise;
+ *    rc_last_error() then holds a message.  The C++ caller turns a non-zero
+ *    status into RCexception(rc_last_error(e)), as the reference's main()
+ *    catches RCexception (src/rheoCell.cpp:40-43).
+ *  - Ownership: the device owns the simulation state between calls.  Host
+ *    memory handed to a call is borrowed for the duration of that call.
+ *  - Threading: one host thread per engine; the engine issues all its work
+ *    on one CUDA stream (its own, or the one given to rc_set_stream).
+ *  - All state is FP64, as the reference's `number` (src/Utilities/LR_vector.h:7-11).
+ */
+#ifndef RHEOCELL_GB300_H
+#define RHEOCELL_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RC_ABI_VERSION 1
+
+typedef enum rc_status {
+	RC_OK = 0,
+	RC_ERR_INVALID = -1,      /* bad argument or inconsistent input        */
+	RC_ERR_CUDA = -2,         /* a CUDA call failed                        */
+	RC_ERR_OOM = -3,          /* device allocation failed                  */
+	RC_ERR_OVERLAP = -4,      /* more than 20 patches cover one box site   */
+	RC_ERR_NONFINITE = -5,    /* NaN/Inf in the state                      */
+	RC_ERR_CG = -6,           /* the viscous solve failed (max iterations) */
+	RC_ERR_CAPACITY = -7,     /* a patch outgrew the engine's capacity     */
+	RC_ERR_UNSUPPORTED = -8   /* feature not provided by this build        */
+} rc_status;
+
+/* interaction_type values (src/Interactions/InteractionFactory.cpp:13-58). */
+typedef enum rc_model {
+	RC_SIMPLEFIELD = 0,   /* "simplefield"    */
+	RC_ACTIVENEMATIC = 1, /* "activenematic"  */
+	RC_WETPOLARMODEL = 2, /* "wetpolarmodel"  */
+	RC_WETMODEL = 3       /* "wetmodel"       */
+} rc_model;
+
+/* backend_precision values (src/Backends/BackendFactory.cpp:14-16,38-63). */
+typedef enum rc_precision {
+	RC_PRECISION_DOUBLE = 0, /* FP64 everywhere; the parity path                    */
+	RC_PRECISION_MIXED = 1   /* FP64 fields; FP32 viscous-solve inner iterations,
+	                            FP64 dots and FP64 true-residual refinement        */
+} rc_precision;
+
+/*
+ * Interaction and integrator parameters.  Arrays of two hold the value in
+ * force before interaction->apply_changes_after_equilibration() ([0], the
+ * values the interaction's constructor sets) and after it ([1], the input-file
+ * values); see e.g. WetModel.cpp:4-21 and :88-96.  The C++ caller fills both
+ * from the input file and the constructor defaults.
+ */
+typedef struct rc_params {
+	int model;             /* rc_model                                          */
+	int precision;         /* rc_precision                                      */
+	int R;                 /* cell radius (int, as BaseInteraction::R)          */
+	int border;            /* patch growth border, 4 (src/Fields/BaseField.cpp:5) */
+	double dt;             /* FDBackend dt                                      */
+	double J0;             /* FD_CPUBackend J0 (default 1)                      */
+	double gamma, lambda, omega, mu, kappa;
+	double passive_alpha;  /* wet models                                        */
+	double cg_tolerance;   /* CGtolerance; <= 0 means Eigen's default (epsilon) */
+	int cg_restart_every;  /* warm solves between cold restarts: 100 (wetmodel), 10 (wetpolarmodel) */
+	int anchoring;         /* reserved; must be 0 (walls are out of scope)      */
+	double friction[2];    /* xi                                               */
+	double friction_cell[2]; /* eta; 0 selects the dry path v = f / xi         */
+	double zetaQ_self[2];
+	double zetaQ_inter[2];
+	double J_Q[2];
+	double beta[2];        /* wetpolarmodel perimeter term                      */
+	/* drand48 state (48 bits) and Utils::gaussian's cached deviate, as left by
+	 * the host after reading the topology and configuration. */
+	unsigned long long rng_state;
+	int rng_has_cached;
+	double rng_cached;
+} rc_params;
+
+typedef struct rc_box {
+	int Lx, Ly;            /* periodic square box (src/Boxes/SquareBox.cpp) */
+} rc_box;
+
+/*
+ * One phase-field patch (src/Fields/BaseField.h:121-224).  Scalars are copied
+ * in on create/upload and out on download.  Per-site arrays are host pointers
+ * of at least `capacity` elements (storage order, LsubX fastest); a NULL
+ * pointer skips that array.
+ */
+typedef struct rc_cell_host {
+	int lsub_x, lsub_y;      /* LsubX, LsubY                                  */
+	int offset_x, offset_y;  /* offset[0..1]                                  */
+	int corner;              /* sub_corner_bottom_left (box site index)       */
+	int type;                /* topology type                                  */
+	double com_x, com_y;     /* CoM                                            */
+	double unrap_x, unrap_y; /* unrap_sub_corner_bottom_left_x/_y              */
+	double q00, q01;         /* Q00, Q01                                       */
+	double theta_q, theta_q_old;
+	double nemq_x, nemq_y, nemq_old_x, nemq_old_y;
+	double area, sum_f, perimeter, s00, s01;
+	double force_rep_x, force_rep_y;  /* total_force_repulsion_x/_y           */
+	int capacity;            /* elements available behind each pointer below  */
+	double *phi;             /* fieldScalar                                    */
+	double *vx, *vy;         /* velocity (interaction->get_velocity_x/_y)      */
+	double *mu;              /* freeEnergy                                     */
+	double *dx, *dy;         /* fieldDX, fieldDY                               */
+	int *box_index;          /* map_sub_to_box (download only)                 */
+} rc_cell_host;
+
+/* rc_download / rc_upload field mask. */
+#define RC_FIELD_SCALARS 0x01u  /* per-cell scalars and patch geometry */
+#define RC_FIELD_PHI     0x02u
+#define RC_FIELD_VEL     0x04u
+#define RC_FIELD_MU      0x08u
+#define RC_FIELD_GRAD    0x10u
+#define RC_FIELD_MAP     0x20u
+#define RC_FIELD_ALL     0x3fu
+
+typedef struct rc_step_stats {
+	long long steps_done;    /* sim_step calls completed by this rc_step      */
+	int cg_solves;           /* viscous solves run (x and y counted apart)    */
+	int cg_iterations;       /* CG iterations summed over those solves        */
+	int cg_max_iterations;   /* largest iteration count of one solve          */
+	double cg_max_rel_residual; /* largest |r|/|b| at exit                    */
+	int resized_cells;       /* patches that changed size                     */
+	int refinements;         /* mixed precision: outer refinement sweeps      */
+} rc_step_stats;
+
+typedef struct rc_engine rc_engine;
+
+/* Version of this ABI (RC_ABI_VERSION). */
+int rc_abi_version(void);
+
+/*
+ * Create an engine from a loaded configuration.  Replaces
+ * FD_CPUBackend::init (src/Backends/FD_CPUBackend.cpp:19-42): uploads the
+ * patches and performs the first force evaluation with the phase-0
+ * parameters, as the reference does before apply_changes_after_equilibration.
+ * `device` is the CUDA ordinal; cells[i].phi must hold lsub_x*lsub_y values.
+ */
+int rc_create(const rc_params *params, const rc_box *box, int n_cells,
+              const rc_cell_host *cells, int device, rc_engine **out);
+
+/*
+ * Advance n_steps time steps (FD_CPUBackend::sim_step,
+ * src/Backends/FD_CPUBackend.cpp:134-160, called n_steps times).  stats may
+ * be NULL.  Returns after the work is complete on the device.
+ */
+int rc_step(rc_engine *e, int n_steps, rc_step_stats *stats);
+
+/*
+ * Select the parameter set: 0 before, 1 after
+ * apply_simulation_changes_after_equilibration (src/Backends/SimBackend.cpp:316-325).
+ */
+int rc_set_phase(rc_engine *e, int active);
+
+/* Number of cells and, if the pointers are non-NULL, each patch's size. */
+int rc_get_sizes(const rc_engine *e, int *n_cells, int *lsub_x, int *lsub_y);
+
+/*
+ * Copy device state into host mirrors (SimBackend::apply_simulation_data_changes,
+ * src/Backends/SimBackend.cpp:327-329, which the reference calls before every
+ * print).  Velocities, mu and gradients are those of the last force
+ * evaluation.  Fails with RC_ERR_INVALID if a capacity is too small.
+ */
+int rc_download(rc_engine *e, rc_cell_host *cells, unsigned fields_mask);
+
+/*
+ * Copy host edits into device state (SimBackend::apply_changes_to_simulation_data,
+ * src/Backends/SimBackend.cpp:331-333).  Patch sizes cannot change here.  After
+ * an upload of RC_FIELD_PHI the forces are re-evaluated with the current
+ * parameters, so the next step sees consistent forces.
+ */
+int rc_upload(rc_engine *e, const rc_cell_host *cells, unsigned fields_mask);
+
+/* Issue the engine's work on this cudaStream_t (NULL: the engine's own). */
+int rc_set_stream(rc_engine *e, void *cuda_stream);
+
+/* Sites (sum of LsubX*LsubY) in the current configuration. */
+long long rc_site_count(const rc_engine *e);
+
+/* Message of the last failure on this engine (or of the last failed create). */
+const char *rc_last_error(const rc_engine *e);
+
+void rc_destroy(rc_engine *e);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RHEOCELL_GB300_H */

@@ -1,0 +1,125 @@
+"""ctypes mirror of include/rheocell_gb300.h.
+
+The engine is a C-ABI shared library; this module declares its structs and
+function signatures for Python callers (tests, bench, scripts).  Struct layouts
+must match the header field for field.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+RC_OK = 0
+RC_ERR_INVALID = -1
+RC_ERR_CUDA = -2
+RC_ERR_OOM = -3
+RC_ERR_OVERLAP = -4
+RC_ERR_NONFINITE = -5
+RC_ERR_CG = -6
+RC_ERR_CAPACITY = -7
+RC_ERR_UNSUPPORTED = -8
+
+RC_SIMPLEFIELD = 0
+RC_ACTIVENEMATIC = 1
+RC_WETPOLARMODEL = 2
+RC_WETMODEL = 3
+
+MODEL_NAMES = {"simplefield": RC_SIMPLEFIELD, "activenematic": RC_ACTIVENEMATIC,
+               "wetpolarmodel": RC_WETPOLARMODEL, "wetmodel": RC_WETMODEL}
+
+RC_PRECISION_DOUBLE = 0
+RC_PRECISION_MIXED = 1
+
+RC_FIELD_SCALARS = 0x01
+RC_FIELD_PHI = 0x02
+RC_FIELD_VEL = 0x04
+RC_FIELD_MU = 0x08
+RC_FIELD_GRAD = 0x10
+RC_FIELD_MAP = 0x20
+RC_FIELD_ALL = 0x3F
+
+D2 = C.c_double * 2
+
+
+class RcParams(C.Structure):
+    _fields_ = [
+        ("model", C.c_int), ("precision", C.c_int), ("R", C.c_int), ("border", C.c_int),
+        ("dt", C.c_double), ("J0", C.c_double),
+        ("gamma", C.c_double), ("lambda_", C.c_double), ("omega", C.c_double),
+        ("mu", C.c_double), ("kappa", C.c_double),
+        ("passive_alpha", C.c_double), ("cg_tolerance", C.c_double),
+        ("cg_restart_every", C.c_int), ("anchoring", C.c_int),
+        ("friction", D2), ("friction_cell", D2), ("zetaQ_self", D2), ("zetaQ_inter", D2),
+        ("J_Q", D2), ("beta", D2),
+        ("rng_state", C.c_ulonglong), ("rng_has_cached", C.c_int), ("rng_cached", C.c_double),
+    ]
+
+
+class RcBox(C.Structure):
+    _fields_ = [("Lx", C.c_int), ("Ly", C.c_int)]
+
+
+DP = C.POINTER(C.c_double)
+IP = C.POINTER(C.c_int)
+
+
+class RcCellHost(C.Structure):
+    _fields_ = [
+        ("lsub_x", C.c_int), ("lsub_y", C.c_int), ("offset_x", C.c_int), ("offset_y", C.c_int),
+        ("corner", C.c_int), ("type", C.c_int),
+        ("com_x", C.c_double), ("com_y", C.c_double), ("unrap_x", C.c_double), ("unrap_y", C.c_double),
+        ("q00", C.c_double), ("q01", C.c_double), ("theta_q", C.c_double), ("theta_q_old", C.c_double),
+        ("nemq_x", C.c_double), ("nemq_y", C.c_double), ("nemq_old_x", C.c_double), ("nemq_old_y", C.c_double),
+        ("area", C.c_double), ("sum_f", C.c_double), ("perimeter", C.c_double),
+        ("s00", C.c_double), ("s01", C.c_double), ("force_rep_x", C.c_double), ("force_rep_y", C.c_double),
+        ("capacity", C.c_int),
+        ("phi", DP), ("vx", DP), ("vy", DP), ("mu", DP), ("dx", DP), ("dy", DP), ("box_index", IP),
+    ]
+
+
+class RcStepStats(C.Structure):
+    _fields_ = [
+        ("steps_done", C.c_longlong), ("cg_solves", C.c_int), ("cg_iterations", C.c_int),
+        ("cg_max_iterations", C.c_int), ("cg_max_rel_residual", C.c_double),
+        ("resized_cells", C.c_int), ("refinements", C.c_int),
+    ]
+
+
+def declare(lib: C.CDLL, prefix: str) -> C.CDLL:
+    """Declare the argument/return types of the rc_*-style API under ``prefix``
+    ("rc" for the engine, "orc" for the oracle)."""
+    vp = C.c_void_p
+    f = lambda name: getattr(lib, "%s_%s" % (prefix, name))
+    f("create").argtypes = ([C.POINTER(RcParams), C.POINTER(RcBox), C.c_int, C.POINTER(RcCellHost)]
+                            + ([C.c_int] if prefix == "rc" else []) + [C.POINTER(vp)])
+    f("create").restype = C.c_int
+    f("step").argtypes = [vp, C.c_int, C.POINTER(RcStepStats)]
+    f("step").restype = C.c_int
+    f("set_phase").argtypes = [vp, C.c_int]
+    f("set_phase").restype = C.c_int
+    f("get_sizes").argtypes = [vp, IP, IP, IP]
+    f("get_sizes").restype = C.c_int
+    f("download").argtypes = [vp, C.POINTER(RcCellHost), C.c_uint]
+    f("download").restype = C.c_int
+    f("site_count").argtypes = [vp]
+    f("site_count").restype = C.c_longlong
+    f("last_error").argtypes = [vp]
+    f("last_error").restype = C.c_char_p
+    f("destroy").argtypes = [vp]
+    f("destroy").restype = None
+    if prefix == "rc":
+        lib.rc_upload.argtypes = [vp, C.POINTER(RcCellHost), C.c_uint]
+        lib.rc_upload.restype = C.c_int
+        lib.rc_set_stream.argtypes = [vp, vp]
+        lib.rc_set_stream.restype = C.c_int
+        lib.rc_abi_version.argtypes = []
+        lib.rc_abi_version.restype = C.c_int
+    else:
+        lib.orc_rng_state.argtypes = [vp]
+        lib.orc_rng_state.restype = C.c_ulonglong
+    return lib
+
+
+# Every symbol the header declares (checked by the CPU test suite).
+EXPORTED = ["rc_abi_version", "rc_create", "rc_step", "rc_set_phase", "rc_get_sizes",
+            "rc_download", "rc_upload", "rc_set_stream", "rc_site_count", "rc_last_error",
+            "rc_destroy"]
