@@ -1,0 +1,155 @@
+// Shared device-side definitions of the GB300 multi-phase-field engine.
+//
+// State layout in HBM (all FP64 unless noted):
+//   * per-site arrays, "flat": the patches of all cells concatenated in cell
+//     order, each patch in storage order (LsubX fastest).  This is exactly the
+//     order of the reference's stacked viscous-solve unknowns
+//     (field_start_index, src/Interactions/WetModel.cpp:203-209), so the
+//     solver's warm start has the same meaning as the reference's.
+//   * per-cell records (CellDev, one 288-byte struct per cell);
+//   * box arrays of L*L entries (phi^2 sum, phi*Q sums, patch counts) and the
+//     cover lists of the wet models, slot-major ([slot][box site]) so that
+//     consecutive box sites read consecutive addresses.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace rc {
+
+constexpr int STORE_MAX = 20;        // store_max_size (src/Interactions/WetModel.cpp:58)
+constexpr int MAX_TABLE_SIDE = 128;  // patch sides with precomputed trig tables
+constexpr int MAX_PATCH_SITES = 16384;
+constexpr int BIN_X = 32, BIN_Y = 8; // box bins for the cover search (one CTA each)
+constexpr int BIN_CAP = 128;         // cells listed per bin
+constexpr int CELL_THREADS = 256;
+constexpr int OVERFLOW_SLOTS = 64;   // cells per launch whose patch exceeds shared memory
+
+enum Model { M_SIMPLE = 0, M_NEMATIC = 1, M_POLAR = 2, M_WET = 3 };
+
+// Error bits accumulated on the device and reported by rc_step.
+enum ErrBits {
+	ERR_OVERLAP = 1,    // > STORE_MAX patches on one box site (WetModel.cpp:475-480)
+	ERR_CAPACITY = 2,   // patch or site capacity exceeded
+	ERR_NONFINITE = 4,  // NaN/Inf in a cell's sums
+	ERR_BIN = 8,        // bin list overflow
+	ERR_BARRIER = 16,   // a grid barrier timed out
+	ERR_TYPE = 32,      // activenematic type other than 0/1
+};
+
+// Phase-dependent parameters (see rc_params in the C header).
+struct PhaseParams {
+	double friction, friction_cell, zs, zi, JQ, beta;
+};
+
+struct DevParams {
+	int model, L, border, pad;
+	double dt, J0, gamma, lambda, omega, mu, kappa, passive_alpha, a0, cg_tol;
+};
+
+struct CellDev {
+	int lx, ly, offx, offy;
+	int corner, type, start, n;
+	int xl, yb, resized, old_lx;
+	int old_ly, old_offx, old_offy, old_corner;
+	double comx, comy, com_oldx, com_oldy;
+	double unrapx, unrapy, q00, q01;
+	double thq, thq_old, nqx, nqy;
+	double nq_oldx, nq_oldy, area, area_old;
+	double sumf, sumf_old, perim, s00;
+	double s01, trx, try_, tfx;
+	double tfy, gauss, pad0, pad1;
+};
+
+// Device status word block (one per engine).
+struct DevStatus {
+	int err;
+	int err_where;
+	int resized;      // patches resized by the last corrector
+	int max_n;        // largest patch (sites) after the last corrector
+	long long S;      // sites = sum of patch sizes (= viscous unknowns)
+	long long S_rows; // size_rows of the last evaluation (solver bookkeeping)
+	int restart;      // restart_solver
+	int cg_cold;      // the next solve starts from zero
+	int cg_solves;
+	int cg_iters;
+	int cg_max_iters;
+	double cg_max_rel;
+	int refinements;
+	int overflow_used;
+	unsigned long long rng_state;
+	int rng_has;
+	int pad2;
+	double rng_cached;
+};
+
+__host__ __device__ inline int wrapi(int v, int L) {
+	v %= L;
+	return v < 0 ? v + L : v;
+}
+
+// Box site of patch storage site (sx, sy) (GetSubIndex, MultiPhaseField.cpp:348-350).
+__device__ inline int box_site(const CellDev &c, int sx, int sy, int L) {
+	int lx = sx + c.offx;
+	if(lx >= c.lx) lx -= c.lx;
+	int ly = sy + c.offy;
+	if(ly >= c.ly) ly -= c.ly;
+	int x = c.corner % L + lx;
+	if(x >= L) x -= L;
+	int y = c.corner / L + ly;
+	if(y >= L) y -= L;
+	return x + y * L;
+}
+
+// Trig table index of patch side l (tables for sides 1..MAX_TABLE_SIDE packed).
+__host__ __device__ inline int table_base(int l) { return (l * (l - 1)) / 2; }
+
+// Deterministic block-wide sum of NV doubles per thread (fixed shuffle tree).
+// `scratch` holds NV * (blockDim/32) doubles.  Result valid in every thread.
+template<int NV>
+__device__ inline void block_sum(double (&v)[NV], double *scratch) {
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+	for(int i = 0; i < NV; i++) {
+#pragma unroll
+		for(int o = 16; o > 0; o >>= 1) v[i] += __shfl_down_sync(0xffffffffu, v[i], o);
+	}
+	__syncthreads();
+	if(lane == 0) {
+#pragma unroll
+		for(int i = 0; i < NV; i++) scratch[i * nw + warp] = v[i];
+	}
+	__syncthreads();
+#pragma unroll
+	for(int i = 0; i < NV; i++) {
+		double s = 0.0;
+		for(int w = 0; w < nw; w++) s += scratch[i * nw + w];
+		v[i] = s;
+	}
+	__syncthreads();
+}
+
+template<int NV>
+__device__ inline void block_min(int (&v)[NV], int *scratch) {
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+	for(int i = 0; i < NV; i++) {
+#pragma unroll
+		for(int o = 16; o > 0; o >>= 1) v[i] = min(v[i], __shfl_down_sync(0xffffffffu, v[i], o));
+	}
+	__syncthreads();
+	if(lane == 0) {
+#pragma unroll
+		for(int i = 0; i < NV; i++) scratch[i * nw + warp] = v[i];
+	}
+	__syncthreads();
+#pragma unroll
+	for(int i = 0; i < NV; i++) {
+		int s = scratch[i * nw];
+		for(int w = 1; w < nw; w++) s = min(s, scratch[i * nw + w]);
+		v[i] = s;
+	}
+	__syncthreads();
+}
+
+}  // namespace rc

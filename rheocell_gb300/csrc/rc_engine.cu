@@ -1,0 +1,702 @@
+// Engine object and C ABI (include/rheocell_gb300.h).
+//
+// One engine advances one monolayer on one GPU.  Per time step it issues, on
+// one stream, the kernels that replace FD_CPUBackend::sim_step
+// (src/Backends/FD_CPUBackend.cpp:134-160):
+//
+//   dry evaluation (xi-only velocity; simplefield, activenematic, and the wet
+//   models while friction_cell = 0):
+//     [rng] -> cell(eval phi^n + predictor) -> gather(phi*) -> cell(eval phi* +
+//     corrector + set_positions) -> [repack] -> gather(phi^{n+1})
+//   The force evaluation at phi^{n+1} that closes the reference's step is
+//   carried into the next step's first kernel ("pending"), where it is fused
+//   with the predictor; its parameters are those in force when the reference
+//   would have run it (eval_phase), so the first step after
+//   apply_changes_after_equilibration uses the passive forces, as the
+//   reference does (FD_CPUBackend.cpp:23-24 vs SimManager.cpp:144).
+//
+//   wet evaluation (friction_cell > 0):
+//     [rng] -> cell(predictor) -> gather(phi*) -> cell(forces, rhs) -> CG ->
+//     cell(corrector) -> [repack] -> gather(phi^{n+1}) -> cell(forces, rhs) -> CG
+#include "rc_kernels.cuh"
+#include "../../include/rheocell_gb300.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace rc;
+
+#define RC_PI_F 3.141592653589793238462643f
+
+struct rc_engine {
+	int device = 0;
+	cudaStream_t stream = nullptr;
+	cudaStream_t own_stream = nullptr;
+	rc_params hp;
+	DevParams P;
+	PhaseParams ph[2];
+	int phase = 0;
+	int eval_phase = 0;
+	bool pending = false;
+	int L = 0, N = 0;
+	long long S = 0, S_cap = 0;
+	int smem_n = 0;
+	int max_n_host = 0;
+	int rep_on = 0;
+	int cg_blocks = 0;
+	int nbx = 0, nby = 0;
+
+	CellDev *cells = nullptr;
+	double *phiA = nullptr, *phiB = nullptr, *dphi_old = nullptr, *mu = nullptr, *dxg = nullptr, *dyg = nullptr;
+	double *vx = nullptr, *vy = nullptr, *fx = nullptr, *fy = nullptr, *rep = nullptr;
+	int *mapg = nullptr;
+	double *phi2 = nullptr, *sq00 = nullptr, *sq01 = nullptr;
+	int *cnt = nullptr, *cover = nullptr;
+	int *bin_count = nullptr, *bin_cells = nullptr;
+	double *tab_cos = nullptr, *tab_sin = nullptr;
+	DevStatus *st = nullptr;
+	DevStatus *st_host = nullptr;
+	double *rx = nullptr, *ry = nullptr, *px = nullptr, *py = nullptr, *Px = nullptr, *Py = nullptr;
+	double *partials = nullptr, *scalars = nullptr;
+	unsigned *bar = nullptr;
+	double *scratch_phi = nullptr, *scratch_rep = nullptr;
+	std::vector<void *> allocs;
+	std::string err;
+	std::string launch_error;  // first failed cooperative launch
+};
+
+static std::string g_create_error;
+
+static int set_err(rc_engine *e, int code, const char *fmt, ...) {
+	char buf[1024];
+	va_list ap;
+	va_start(ap, fmt);
+	vsnprintf(buf, sizeof(buf), fmt, ap);
+	va_end(ap);
+	if(e) e->err = buf;
+	else g_create_error = buf;
+	return code;
+}
+
+#define CUDA_TRY(e, call)                                                                                    \
+	do {                                                                                                     \
+		cudaError_t _c = (call);                                                                             \
+		if(_c != cudaSuccess) return set_err((e), RC_ERR_CUDA, "%s failed: %s", #call, cudaGetErrorString(_c)); \
+	} while(0)
+
+template<typename T>
+static int dalloc(rc_engine *e, T **p, size_t count) {
+	void *q = nullptr;
+	cudaError_t c = cudaMalloc(&q, sizeof(T) * (count ? count : 1));
+	if(c != cudaSuccess) return set_err(e, RC_ERR_OOM, "cudaMalloc of %zu bytes failed: %s", sizeof(T) * count, cudaGetErrorString(c));
+	e->allocs.push_back(q);
+	*p = (T *) q;
+	cudaMemset(q, 0, sizeof(T) * (count ? count : 1));
+	return RC_OK;
+}
+
+static bool wet_phase(const rc_engine *e, int phase) {
+	return (e->P.model == M_POLAR || e->P.model == M_WET) && e->ph[phase].friction_cell != 0.0;
+}
+
+static CellArgs cell_args(rc_engine *e) {
+	CellArgs a;
+	memset(&a, 0, sizeof(a));
+	a.cells = e->cells;
+	a.N = e->N;
+	a.smem_n = e->smem_n;
+	a.dphi_old = e->dphi_old;
+	a.mu = e->mu;
+	a.dxg = e->dxg;
+	a.dyg = e->dyg;
+	a.vxg = e->vx;
+	a.vyg = e->vy;
+	a.fxg = e->fx;
+	a.fyg = e->fy;
+	a.mapg = e->mapg;
+	a.rep = e->rep;
+	a.phi2 = e->phi2;
+	a.sq00 = e->sq00;
+	a.sq01 = e->sq01;
+	a.tab_cos = e->tab_cos;
+	a.tab_sin = e->tab_sin;
+	a.bin_count = e->bin_count;
+	a.bin_cells = e->bin_cells;
+	a.nbx = e->nbx;
+	a.nby = e->nby;
+	a.st = e->st;
+	a.P = e->P;
+	a.rep_on = e->rep_on;
+	a.accumulate_rep = 1;
+	return a;
+}
+
+static void gather(rc_engine *e, const double *phi, int phase) {
+	BoxArgs b;
+	memset(&b, 0, sizeof(b));
+	b.cells = e->cells;
+	b.phi = phi;
+	b.phi2 = e->phi2;
+	b.sq00 = e->sq00;
+	b.sq01 = e->sq01;
+	b.cnt = e->cnt;
+	b.cover = e->cover;
+	b.bin_count = e->bin_count;
+	b.bin_cells = e->bin_cells;
+	b.nbx = e->nbx;
+	b.nby = e->nby;
+	b.want_q = (e->P.model == M_NEMATIC || e->P.model == M_WET);
+	b.want_cover = wet_phase(e, phase);
+	b.check_overlap = (e->P.model == M_POLAR || e->P.model == M_WET);
+	b.bookkeeping = (e->P.model == M_POLAR || e->P.model == M_WET);
+	b.restart_every = e->hp.cg_restart_every;
+	b.solve_follows = wet_phase(e, phase);
+	b.st = e->st;
+	b.L = e->L;
+	launch_box_gather(b, e->stream);
+}
+
+static void solve(rc_engine *e, int phase) {
+	CGArgs g;
+	memset(&g, 0, sizeof(g));
+	g.cells = e->cells;
+	g.mapg = e->mapg;
+	g.cnt = e->cnt;
+	g.cover = e->cover;
+	g.fx = e->fx;
+	g.fy = e->fy;
+	g.vx = e->vx;
+	g.vy = e->vy;
+	g.rx = e->rx;
+	g.ry = e->ry;
+	g.px = e->px;
+	g.py = e->py;
+	g.Px = e->Px;
+	g.Py = e->Py;
+	g.partials = e->partials;
+	g.scalars = e->scalars;
+	g.bar = e->bar;
+	g.st = e->st;
+	g.L = e->L;
+	g.restart_every = e->hp.cg_restart_every;
+	g.xi = e->ph[phase].friction;
+	g.eta = e->ph[phase].friction_cell;
+	g.tol = e->hp.cg_tolerance > 0 ? e->hp.cg_tolerance : 2.220446049250313e-16;
+	const cudaError_t c = launch_cg(g, e->cg_blocks, e->stream);
+	if(c != cudaSuccess && e->launch_error.empty()) e->launch_error = cudaGetErrorString(c);
+}
+
+// Forces (and the viscous solve) at phi^n for the current phase, run at its
+// logical time; the dry path leaves it pending for the next predictor.
+static void evaluate_end(rc_engine *e, const double *phi, int phase) {
+	gather(e, phi, phase);
+	if(wet_phase(e, phase)) {
+		CellArgs a = cell_args(e);
+		a.phi_eval = phi;
+		a.pe = e->ph[phase];
+		a.pu = e->ph[phase];
+		launch_cell_kernel(e->P.model, EV_WET_RHS, UP_NONE, a, e->stream);
+		solve(e, phase);
+		e->pending = false;
+	}
+	else {
+		e->pending = true;
+	}
+	e->eval_phase = phase;
+}
+
+static void one_step(rc_engine *e) {
+	const int cur = e->phase;
+	cudaStream_t s = e->stream;
+	if(e->P.model == M_POLAR) launch_rng(e->cells, e->N, e->st, s);
+	CellArgs a = cell_args(e);
+	a.phi_eval = e->phiA;
+	a.phi_out = e->phiB;
+	a.pu = e->ph[cur];
+	if(e->pending) {
+		a.pe = e->ph[e->eval_phase];
+		launch_cell_kernel(e->P.model, EV_LOCAL, UP_PRED, a, s);
+	}
+	else {
+		a.pe = e->ph[cur];
+		launch_cell_kernel(e->P.model, EV_NONE, UP_PRED, a, s);
+	}
+	gather(e, e->phiB, cur);
+	cudaMemsetAsync(e->bin_count, 0, sizeof(int) * (size_t) e->nbx * e->nby, s);
+	CellArgs c = cell_args(e);
+	c.phi_old = e->phiA;
+	c.phi_out = e->phiA;
+	c.pe = e->ph[cur];
+	c.pu = e->ph[cur];
+	if(!wet_phase(e, cur)) {
+		c.phi_eval = e->phiB;
+		launch_cell_kernel(e->P.model, EV_LOCAL, UP_CORR, c, s);
+	}
+	else {
+		CellArgs f = cell_args(e);
+		f.phi_eval = e->phiB;
+		f.pe = e->ph[cur];
+		f.pu = e->ph[cur];
+		launch_cell_kernel(e->P.model, EV_WET_RHS, UP_NONE, f, s);
+		solve(e, cur);
+		c.phi_eval = e->phiB;
+		launch_cell_kernel(e->P.model, EV_NONE, UP_CORR, c, s);
+	}
+	CellArgs r = cell_args(e);
+	r.phi_out = e->phiA;
+	launch_repack(r, e->scratch_phi, e->scratch_rep, e->S_cap, s);
+	evaluate_end(e, e->phiA, cur);
+}
+
+// Materialise a pending dry evaluation into mu, v, gradients and the map.
+static void materialise(rc_engine *e, int accumulate) {
+	if(!e->pending) return;
+	CellArgs a = cell_args(e);
+	a.phi_eval = e->phiA;
+	a.pe = e->ph[e->eval_phase];
+	a.pu = e->ph[e->eval_phase];
+	a.accumulate_rep = accumulate;
+	launch_cell_kernel(e->P.model, EV_STORE, UP_NONE, a, e->stream);
+	if(accumulate) e->pending = false;
+}
+
+static int choose_smem(rc_engine *e) {
+	int want = std::max(256, (e->max_n_host * 3 + 1) / 2);
+	want = ((want + 255) / 256) * 256;
+	const int per_site = (e->P.model == M_POLAR || e->P.model == M_WET) ? 24 : 16;
+	const int cap = (200 * 1024) / per_site;
+	if(e->max_n_host > cap) return set_err(e, RC_ERR_CAPACITY, "patch of %d sites exceeds shared memory", e->max_n_host);
+	e->smem_n = std::min(want, cap);
+	return RC_OK;
+}
+
+static int check_status(rc_engine *e, rc_step_stats *stats) {
+	CUDA_TRY(e, cudaMemcpyAsync(e->st_host, e->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, e->stream));
+	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+	CUDA_TRY(e, cudaGetLastError());
+	if(!e->launch_error.empty()) {
+		std::string m = e->launch_error;
+		e->launch_error.clear();
+		return set_err(e, RC_ERR_CUDA, "viscous solve launch failed: %s", m.c_str());
+	}
+	const DevStatus &h = *e->st_host;
+	e->S = h.S;
+	e->max_n_host = std::max(e->max_n_host, h.max_n);
+	if(stats) {
+		stats->cg_solves = h.cg_solves;
+		stats->cg_iterations = h.cg_iters;
+		stats->cg_max_iterations = h.cg_max_iters;
+		stats->cg_max_rel_residual = h.cg_max_rel;
+		stats->refinements = h.refinements;
+	}
+	if(h.err) {
+		if(h.err & ERR_OVERLAP) return set_err(e, RC_ERR_OVERLAP, "Too many field patches overlap (box site %d)", h.err_where);
+		if(h.err & ERR_CAPACITY) return set_err(e, RC_ERR_CAPACITY, "capacity exceeded (cell %d): patch or site storage", h.err_where);
+		if(h.err & ERR_BIN) return set_err(e, RC_ERR_CAPACITY, "box bin capacity exceeded");
+		if(h.err & ERR_NONFINITE) return set_err(e, RC_ERR_NONFINITE, "non-finite state in cell %d", h.err_where);
+		if(h.err & ERR_BARRIER) return set_err(e, RC_ERR_CG, "viscous solve: grid barrier timed out");
+		if(h.err & ERR_TYPE) return set_err(e, RC_ERR_INVALID, "Too many field types (cell %d)", h.err_where);
+		return set_err(e, RC_ERR_INVALID, "device error 0x%x", h.err);
+	}
+	return RC_OK;
+}
+
+static void host_cell(const rc_cell_host &h, CellDev &c, int start) {
+	memset(&c, 0, sizeof(c));
+	c.lx = h.lsub_x;
+	c.ly = h.lsub_y;
+	c.offx = h.offset_x;
+	c.offy = h.offset_y;
+	c.corner = h.corner;
+	c.type = h.type;
+	c.start = start;
+	c.n = h.lsub_x * h.lsub_y;
+	c.xl = h.lsub_x;
+	c.yb = h.lsub_y;
+	c.comx = c.com_oldx = h.com_x;
+	c.comy = c.com_oldy = h.com_y;
+	c.unrapx = h.unrap_x;
+	c.unrapy = h.unrap_y;
+	c.q00 = h.q00;
+	c.q01 = h.q01;
+	c.thq = h.theta_q;
+	c.thq_old = h.theta_q_old;
+	c.nqx = h.nemq_x;
+	c.nqy = h.nemq_y;
+	c.nq_oldx = h.nemq_old_x;
+	c.nq_oldy = h.nemq_old_y;
+}
+
+// Initial per-cell sums, in the reference's sequential order so they are
+// bit-identical: area = sum phi^2 and sumF = sum phi of the loaded field
+// (SimBackend.cpp:289-296) and the shape tensor of begin_energy_computation()
+// (e.g. WetModel.cpp:126-164; only visible in a download before the first step).
+__global__ void init_sums_kernel(CellDev *cells, const double *phi, int N) {
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if(i >= N) return;
+	CellDev &c = cells[i];
+	const int lx = c.lx, ly = c.ly, n = c.n, st = c.start;
+	double area = 0, sumf = 0, s00 = 0, s01 = 0;
+	for(int q = 0; q < n; q++) {
+		const double p = phi[st + q];
+		area += p * p;
+		sumf += p;
+		const int y = q / lx, x = q - y * lx;
+		const int r = (x == lx - 1) ? q - (lx - 1) : q + 1, l = (x == 0) ? q + (lx - 1) : q - 1;
+		const int u = (y == ly - 1) ? q - (ly - 1) * lx : q + lx, d = (y == 0) ? q + (ly - 1) * lx : q - lx;
+		const double dx = .5 * (phi[st + r] - phi[st + l]), dy = .5 * (phi[st + u] - phi[st + d]);
+		s00 += -0.5 * (dx * dx - dy * dy);
+		s01 += -dx * dy;
+	}
+	c.area = area;
+	c.sumf = sumf;
+	c.s00 = s00;
+	c.s01 = s01;
+}
+
+extern "C" {
+
+int rc_abi_version(void) { return RC_ABI_VERSION; }
+
+int rc_create(const rc_params *params, const rc_box *box, int n_cells, const rc_cell_host *cells, int device,
+              rc_engine **out) {
+	if(!out) return set_err(nullptr, RC_ERR_INVALID, "out is NULL");
+	*out = nullptr;
+	if(!params || !box || (n_cells > 0 && !cells) || n_cells < 0)
+		return set_err(nullptr, RC_ERR_INVALID, "invalid arguments");
+	if(box->Lx != box->Ly || box->Lx < 3 || box->Lx > 46340)
+		return set_err(nullptr, RC_ERR_INVALID, "The box in the configuration file is not a square (%dx%d)", box->Lx, box->Ly);
+	if(params->model < RC_SIMPLEFIELD || params->model > RC_WETMODEL)
+		return set_err(nullptr, RC_ERR_INVALID, "unknown interaction model %d", params->model);
+	if(params->anchoring) return set_err(nullptr, RC_ERR_UNSUPPORTED, "anchoring is not provided");
+	if(params->precision != RC_PRECISION_DOUBLE && params->precision != RC_PRECISION_MIXED)
+		return set_err(nullptr, RC_ERR_INVALID, "unknown precision %d", params->precision);
+	const int L = box->Lx;
+	long long S = 0;
+	int max_n = 0;
+	for(int i = 0; i < n_cells; i++) {
+		const rc_cell_host &h = cells[i];
+		if(h.lsub_x <= 0 || h.lsub_y <= 0 || h.lsub_x > L || h.lsub_y > L || h.lsub_x > MAX_TABLE_SIDE ||
+		   h.lsub_y > MAX_TABLE_SIDE)
+			return set_err(nullptr, RC_ERR_INVALID, "cell %d: patch %dx%d does not fit the box/tables", i, h.lsub_x, h.lsub_y);
+		if(h.offset_x < 0 || h.offset_x >= h.lsub_x || h.offset_y < 0 || h.offset_y >= h.lsub_y)
+			return set_err(nullptr, RC_ERR_INVALID, "cell %d: offset out of range", i);
+		if(h.corner < 0 || h.corner >= L * L) return set_err(nullptr, RC_ERR_INVALID, "cell %d: corner out of box", i);
+		if(!h.phi) return set_err(nullptr, RC_ERR_INVALID, "cell %d: phi is NULL", i);
+		S += (long long) h.lsub_x * h.lsub_y;
+		max_n = std::max(max_n, h.lsub_x * h.lsub_y);
+	}
+	if(S >= (1LL << 31) - (1LL << 24)) return set_err(nullptr, RC_ERR_CAPACITY, "too many sites (%lld)", S);
+
+	rc_engine *e = new rc_engine();
+	e->device = device;
+	e->hp = *params;
+	e->L = L;
+	e->N = n_cells;
+	e->S = S;
+	e->S_cap = std::min((1LL << 31) - 1, S + std::max(S / 4, 65536LL));
+	e->max_n_host = max_n;
+	int rc;
+	cudaError_t ce = cudaSetDevice(device);
+	if(ce != cudaSuccess) {
+		set_err(nullptr, RC_ERR_CUDA, "cudaSetDevice(%d): %s", device, cudaGetErrorString(ce));
+		delete e;
+		return RC_ERR_CUDA;
+	}
+	auto bail = [&](int code) {
+		g_create_error = e->err;
+		*out = e;  // caller may read rc_last_error(e) then destroy
+		return code;
+	};
+	if(cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+		return bail(set_err(e, RC_ERR_CUDA, "stream creation failed"));
+	e->stream = e->own_stream;
+
+	DevParams &P = e->P;
+	memset(&P, 0, sizeof(P));
+	P.model = params->model;
+	P.L = L;
+	P.border = params->border > 0 ? params->border : 4;
+	P.dt = params->dt;
+	P.J0 = params->J0;
+	P.gamma = params->gamma;
+	P.lambda = params->lambda;
+	P.omega = params->omega;
+	P.mu = params->mu;
+	P.kappa = params->kappa;
+	P.passive_alpha = params->passive_alpha;
+	{
+		float a0 = RC_PI_F * (float) params->R * (float) params->R;  // PI is a float literal (defs.h:4)
+		P.a0 = (double) a0;
+	}
+	P.cg_tol = params->cg_tolerance;
+	for(int k = 0; k < 2; k++) {
+		e->ph[k].friction = params->friction[k];
+		e->ph[k].friction_cell = params->friction_cell[k];
+		e->ph[k].zs = params->zetaQ_self[k];
+		e->ph[k].zi = params->zetaQ_inter[k];
+		e->ph[k].JQ = params->J_Q[k];
+		e->ph[k].beta = params->beta[k];
+	}
+	e->rep_on = (P.model == M_POLAR) && (params->J_Q[0] != 0.0 || params->J_Q[1] != 0.0);
+	e->nbx = (L + BIN_X - 1) / BIN_X;
+	e->nby = (L + BIN_Y - 1) / BIN_Y;
+	const size_t L2 = (size_t) L * L;
+	const size_t cap = (size_t) e->S_cap;
+	const bool wet = (P.model == M_POLAR || P.model == M_WET);
+	if((rc = dalloc(e, &e->cells, (size_t) std::max(n_cells, 1))) ||
+	   (rc = dalloc(e, &e->phiA, cap)) || (rc = dalloc(e, &e->phiB, cap)) || (rc = dalloc(e, &e->dphi_old, cap)) ||
+	   (rc = dalloc(e, &e->mu, cap)) || (rc = dalloc(e, &e->dxg, cap)) || (rc = dalloc(e, &e->dyg, cap)) ||
+	   (rc = dalloc(e, &e->vx, cap)) || (rc = dalloc(e, &e->vy, cap)) || (rc = dalloc(e, &e->mapg, cap)) ||
+	   (rc = dalloc(e, &e->phi2, L2)) || (rc = dalloc(e, &e->sq00, L2)) || (rc = dalloc(e, &e->sq01, L2)) ||
+	   (rc = dalloc(e, &e->cnt, L2)) ||
+	   (rc = dalloc(e, &e->bin_count, (size_t) e->nbx * e->nby)) ||
+	   (rc = dalloc(e, &e->bin_cells, (size_t) e->nbx * e->nby * BIN_CAP)) ||
+	   (rc = dalloc(e, &e->tab_cos, (size_t) table_base(MAX_TABLE_SIDE + 1))) ||
+	   (rc = dalloc(e, &e->tab_sin, (size_t) table_base(MAX_TABLE_SIDE + 1))) ||
+	   (rc = dalloc(e, &e->st, 1)) ||
+	   (rc = dalloc(e, &e->scratch_phi, cap + (size_t) n_cells / 2 + 8)) ||
+	   (rc = dalloc(e, &e->rep, e->rep_on ? cap : 1)) || (rc = dalloc(e, &e->scratch_rep, e->rep_on ? cap : 1)))
+		return bail(rc);
+	if(wet) {
+		if((rc = dalloc(e, &e->fx, cap)) || (rc = dalloc(e, &e->fy, cap)) || (rc = dalloc(e, &e->cover, L2 * STORE_MAX)) ||
+		   (rc = dalloc(e, &e->rx, cap)) || (rc = dalloc(e, &e->ry, cap)) || (rc = dalloc(e, &e->px, cap)) ||
+		   (rc = dalloc(e, &e->py, cap)) || (rc = dalloc(e, &e->Px, L2)) || (rc = dalloc(e, &e->Py, L2)) ||
+		   (rc = dalloc(e, &e->partials, 8 * 4096)) || (rc = dalloc(e, &e->scalars, 64)) || (rc = dalloc(e, &e->bar, 2)))
+			return bail(rc);
+		e->cg_blocks = cg_grid_blocks(device);
+	}
+	if(cudaMallocHost(&e->st_host, sizeof(DevStatus)) != cudaSuccess) return bail(set_err(e, RC_ERR_OOM, "pinned alloc failed"));
+
+	// trig tables for the centre of mass, computed like the reference's
+	// (MultiPhaseField.cpp:54-65: float argument, double cos/sin)
+	{
+		std::vector<double> tc(table_base(MAX_TABLE_SIDE + 1)), ts(tc.size());
+		for(int l = 1; l <= MAX_TABLE_SIDE; l++)
+			for(int i = 0; i < l; i++) {
+				volatile float a = (2.0f * RC_PI_F * (float) i);
+				volatile float b = a / (float) l;
+				tc[table_base(l) + i] = cos((double) b);
+				ts[table_base(l) + i] = sin((double) b);
+			}
+		CUDA_TRY(e, cudaMemcpy(e->tab_cos, tc.data(), sizeof(double) * tc.size(), cudaMemcpyHostToDevice));
+		CUDA_TRY(e, cudaMemcpy(e->tab_sin, ts.data(), sizeof(double) * ts.size(), cudaMemcpyHostToDevice));
+	}
+	// cells and fields
+	{
+		std::vector<CellDev> hc((size_t) std::max(n_cells, 1));
+		std::vector<double> phi((size_t) S);
+		long long start = 0;
+		for(int i = 0; i < n_cells; i++) {
+			host_cell(cells[i], hc[i], (int) start);
+			memcpy(&phi[(size_t) start], cells[i].phi, sizeof(double) * (size_t) hc[i].n);
+			start += hc[i].n;
+		}
+		CUDA_TRY(e, cudaMemcpy(e->cells, hc.data(), sizeof(CellDev) * (size_t) std::max(n_cells, 1), cudaMemcpyHostToDevice));
+		if(S) CUDA_TRY(e, cudaMemcpy(e->phiA, phi.data(), sizeof(double) * (size_t) S, cudaMemcpyHostToDevice));
+		DevStatus h;
+		memset(&h, 0, sizeof(h));
+		h.S = S;
+		h.S_rows = 0;
+		h.restart = 0;
+		h.max_n = max_n;
+		h.rng_state = params->rng_state & ((1ULL << 48) - 1);
+		h.rng_has = params->rng_has_cached;
+		h.rng_cached = params->rng_cached;
+		CUDA_TRY(e, cudaMemcpy(e->st, &h, sizeof(h), cudaMemcpyHostToDevice));
+	}
+	if((rc = choose_smem(e))) return bail(rc);
+	if(n_cells > 0) {
+		init_sums_kernel<<<(n_cells + 63) / 64, 64, 0, e->stream>>>(e->cells, e->phiA, n_cells);
+		launch_bins(e->cells, n_cells, L, e->bin_count, e->bin_cells, e->nbx, e->nby, e->st, e->stream);
+		// FD_CPUBackend::init: first force evaluation with the phase-0 parameters
+		evaluate_end(e, e->phiA, 0);
+	}
+	if((rc = check_status(e, nullptr))) return bail(rc);
+	*out = e;
+	return RC_OK;
+}
+
+int rc_step(rc_engine *e, int n_steps, rc_step_stats *stats) {
+	if(!e) return RC_ERR_INVALID;
+	if(n_steps < 0) return set_err(e, RC_ERR_INVALID, "n_steps < 0");
+	if(stats) memset(stats, 0, sizeof(*stats));
+	CUDA_TRY(e, cudaSetDevice(e->device));
+	// reset the per-call counters
+	{
+		DevStatus z;
+		memset(&z, 0, sizeof(z));
+		CUDA_TRY(e, cudaMemcpyAsync(e->st_host, e->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, e->stream));
+		CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+		DevStatus h = *e->st_host;
+		h.cg_solves = h.cg_iters = h.cg_max_iters = 0;
+		h.cg_max_rel = 0;
+		h.refinements = 0;
+		*e->st_host = h;
+		CUDA_TRY(e, cudaMemcpyAsync(e->st, e->st_host, sizeof(DevStatus), cudaMemcpyHostToDevice, e->stream));
+	}
+	const int chunk = 16;
+	int done = 0;
+	int rc = RC_OK;
+	while(done < n_steps) {
+		if((rc = choose_smem(e))) return rc;
+		const int m = std::min(chunk, n_steps - done);
+		for(int i = 0; i < m; i++) one_step(e);
+		rc = check_status(e, stats);
+		if(rc) break;
+		done += m;
+	}
+	if(stats) stats->steps_done = done;
+	return rc;
+}
+
+int rc_set_phase(rc_engine *e, int active) {
+	if(!e) return RC_ERR_INVALID;
+	e->phase = active ? 1 : 0;
+	return RC_OK;
+}
+
+int rc_get_sizes(const rc_engine *e, int *n_cells, int *lsub_x, int *lsub_y) {
+	if(!e) return RC_ERR_INVALID;
+	if(n_cells) *n_cells = e->N;
+	if(lsub_x || lsub_y) {
+		std::vector<CellDev> hc((size_t) std::max(e->N, 1));
+		if(cudaMemcpy(hc.data(), e->cells, sizeof(CellDev) * (size_t) std::max(e->N, 1), cudaMemcpyDeviceToHost) != cudaSuccess)
+			return RC_ERR_CUDA;
+		for(int i = 0; i < e->N; i++) {
+			if(lsub_x) lsub_x[i] = hc[i].lx;
+			if(lsub_y) lsub_y[i] = hc[i].ly;
+		}
+	}
+	return RC_OK;
+}
+
+int rc_download(rc_engine *e, rc_cell_host *cells, unsigned mask) {
+	if(!e || (!cells && e->N > 0)) return RC_ERR_INVALID;
+	CUDA_TRY(e, cudaSetDevice(e->device));
+	materialise(e, 0);
+	std::vector<CellDev> hc((size_t) std::max(e->N, 1));
+	CUDA_TRY(e, cudaMemcpyAsync(hc.data(), e->cells, sizeof(CellDev) * (size_t) std::max(e->N, 1), cudaMemcpyDeviceToHost, e->stream));
+	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+	const bool dry_vel = !wet_phase(e, e->eval_phase);
+	(void) dry_vel;
+	for(int i = 0; i < e->N; i++) {
+		const CellDev &c = hc[i];
+		rc_cell_host &h = cells[i];
+		if(mask & RC_FIELD_SCALARS) {
+			h.lsub_x = c.lx;
+			h.lsub_y = c.ly;
+			h.offset_x = c.offx;
+			h.offset_y = c.offy;
+			h.corner = c.corner;
+			h.type = c.type;
+			h.com_x = c.comx;
+			h.com_y = c.comy;
+			h.unrap_x = c.unrapx;
+			h.unrap_y = c.unrapy;
+			h.q00 = c.q00;
+			h.q01 = c.q01;
+			h.theta_q = c.thq;
+			h.theta_q_old = c.thq_old;
+			h.nemq_x = c.nqx;
+			h.nemq_y = c.nqy;
+			h.nemq_old_x = c.nq_oldx;
+			h.nemq_old_y = c.nq_oldy;
+			h.area = c.area;
+			h.sum_f = c.sumf;
+			h.perimeter = c.perim;
+			h.s00 = c.s00;
+			h.s01 = c.s01;
+			h.force_rep_x = c.trx;
+			h.force_rep_y = c.try_;
+		}
+		if(mask & ~RC_FIELD_SCALARS) {
+			if(h.capacity < c.n) return set_err(e, RC_ERR_INVALID, "cell %d: capacity %d < %d sites", i, h.capacity, c.n);
+			const size_t nb = sizeof(double) * (size_t) c.n;
+			if((mask & RC_FIELD_PHI) && h.phi) CUDA_TRY(e, cudaMemcpyAsync(h.phi, e->phiA + c.start, nb, cudaMemcpyDeviceToHost, e->stream));
+			if(mask & RC_FIELD_VEL) {
+				if(h.vx) CUDA_TRY(e, cudaMemcpyAsync(h.vx, e->vx + c.start, nb, cudaMemcpyDeviceToHost, e->stream));
+				if(h.vy) CUDA_TRY(e, cudaMemcpyAsync(h.vy, e->vy + c.start, nb, cudaMemcpyDeviceToHost, e->stream));
+			}
+			if((mask & RC_FIELD_MU) && h.mu) CUDA_TRY(e, cudaMemcpyAsync(h.mu, e->mu + c.start, nb, cudaMemcpyDeviceToHost, e->stream));
+			if(mask & RC_FIELD_GRAD) {
+				if(h.dx) CUDA_TRY(e, cudaMemcpyAsync(h.dx, e->dxg + c.start, nb, cudaMemcpyDeviceToHost, e->stream));
+				if(h.dy) CUDA_TRY(e, cudaMemcpyAsync(h.dy, e->dyg + c.start, nb, cudaMemcpyDeviceToHost, e->stream));
+			}
+			if((mask & RC_FIELD_MAP) && h.box_index)
+				CUDA_TRY(e, cudaMemcpyAsync(h.box_index, e->mapg + c.start, sizeof(int) * (size_t) c.n, cudaMemcpyDeviceToHost, e->stream));
+		}
+	}
+	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+	return RC_OK;
+}
+
+int rc_upload(rc_engine *e, const rc_cell_host *cells, unsigned mask) {
+	if(!e || (!cells && e->N > 0)) return RC_ERR_INVALID;
+	CUDA_TRY(e, cudaSetDevice(e->device));
+	// the forces of the last evaluation belong to the state before the edit,
+	// as on the CPU backend: make them concrete first
+	materialise(e, 1);
+	std::vector<CellDev> hc((size_t) std::max(e->N, 1));
+	CUDA_TRY(e, cudaMemcpyAsync(hc.data(), e->cells, sizeof(CellDev) * (size_t) std::max(e->N, 1), cudaMemcpyDeviceToHost, e->stream));
+	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+	for(int i = 0; i < e->N; i++) {
+		CellDev &c = hc[i];
+		const rc_cell_host &h = cells[i];
+		if(mask & RC_FIELD_SCALARS) {
+			if(h.lsub_x != c.lx || h.lsub_y != c.ly) return set_err(e, RC_ERR_INVALID, "cell %d: patch size cannot change on upload", i);
+			CellDev n;
+			host_cell(h, n, c.start);
+			n.area = h.area;
+			n.sumf = h.sum_f;
+			n.perim = h.perimeter;
+			n.s00 = h.s00;
+			n.s01 = h.s01;
+			n.trx = h.force_rep_x;
+			n.try_ = h.force_rep_y;
+			n.area_old = c.area_old;
+			n.sumf_old = c.sumf_old;
+			n.com_oldx = c.com_oldx;
+			n.com_oldy = c.com_oldy;
+			c = n;
+		}
+		if((mask & RC_FIELD_PHI) && h.phi)
+			CUDA_TRY(e, cudaMemcpyAsync(e->phiA + c.start, h.phi, sizeof(double) * (size_t) c.n, cudaMemcpyHostToDevice, e->stream));
+	}
+	if(mask & RC_FIELD_SCALARS) {
+		CUDA_TRY(e, cudaMemcpyAsync(e->cells, hc.data(), sizeof(CellDev) * (size_t) std::max(e->N, 1), cudaMemcpyHostToDevice, e->stream));
+		launch_bins(e->cells, e->N, e->L, e->bin_count, e->bin_cells, e->nbx, e->nby, e->st, e->stream);
+	}
+	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+	return RC_OK;
+}
+
+int rc_set_stream(rc_engine *e, void *cuda_stream) {
+	if(!e) return RC_ERR_INVALID;
+	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+	e->stream = cuda_stream ? (cudaStream_t) cuda_stream : e->own_stream;
+	return RC_OK;
+}
+
+long long rc_site_count(const rc_engine *e) { return e ? e->S : 0; }
+
+const char *rc_last_error(const rc_engine *e) { return e ? e->err.c_str() : g_create_error.c_str(); }
+
+void rc_destroy(rc_engine *e) {
+	if(!e) return;
+	cudaSetDevice(e->device);
+	if(e->stream) cudaStreamSynchronize(e->stream);
+	for(void *p : e->allocs) cudaFree(p);
+	if(e->st_host) cudaFreeHost(e->st_host);
+	if(e->own_stream) cudaStreamDestroy(e->own_stream);
+	delete e;
+}
+
+}  // extern "C"

@@ -1,0 +1,80 @@
+// Host-visible launch interface of the engine's kernels (implemented in
+// rc_cells.cu, rc_box.cu and rc_cg.cu).
+#pragma once
+
+#include "rc_common.cuh"
+
+namespace rc {
+
+enum EvalMode { EV_NONE = 0, EV_STORE = 1, EV_WET_RHS = 2, EV_LOCAL = 3 };
+enum UpdMode { UP_NONE = 0, UP_PRED = 1, UP_CORR = 2 };
+
+struct CellArgs {
+	CellDev *cells;
+	int N;
+	int smem_n;            // per-site capacity of the dynamic shared memory
+	const double *phi_eval;  // phi at which forces are evaluated; PRED update also reads phi^n here
+	const double *phi_old;   // CORR: phi^n
+	double *phi_out;         // PRED: phi*; CORR: phi^{n+1}
+	double *dphi_old;
+	double *mu, *dxg, *dyg, *vxg, *vyg, *fxg, *fyg;
+	int *mapg;
+	double *rep;
+	const double *phi2, *sq00, *sq01;
+	const double *tab_cos, *tab_sin;
+	int *bin_count, *bin_cells;
+	int nbx, nby;
+	DevStatus *st;
+	DevParams P;
+	PhaseParams pe;        // parameters of the evaluation
+	PhaseParams pu;        // parameters of the update (directed active forces)
+	int rep_on;            // track the polar Repulsion accumulator
+	int accumulate_rep;    // this evaluation adds to it (not a re-evaluation for download)
+};
+
+struct BoxArgs {
+	const CellDev *cells;
+	const double *phi;
+	double *phi2, *sq00, *sq01;
+	int *cnt, *cover;      // cover[slot * L*L + k]
+	const int *bin_count, *bin_cells;
+	int nbx, nby;
+	int want_q, want_cover, check_overlap;
+	int bookkeeping;       // wet models: size_rows / restart bookkeeping of this evaluation
+	int restart_every;
+	int solve_follows;     // a viscous solve follows this evaluation
+	DevStatus *st;
+	int L;
+};
+
+struct CGArgs {
+	const CellDev *cells;
+	const int *mapg;
+	const int *cnt, *cover;
+	const double *fx, *fy;   // right-hand sides
+	double *vx, *vy;         // solution; warm start
+	double *rx, *ry, *px, *py;
+	double *Px, *Py;         // box-grid sums of p
+	double *partials;        // per-block partial sums
+	double *scalars;         // solver scalars (see rc_cg.cu)
+	unsigned *bar;           // barrier counter and generation
+	DevStatus *st;
+	int L;
+	int restart_every;
+	double xi, eta, tol;
+	int mixed;               // inner iterations in FP32
+	float *rxf, *ryf, *pxf, *pyf, *Pxf, *Pyf;
+	double *ex, *ey;         // mixed: correction accumulators
+};
+
+void launch_cell_kernel(int model, int eval, int upd, const CellArgs &a, cudaStream_t s);
+size_t cell_smem_bytes(int model, int smem_n);
+void launch_rng(CellDev *cells, int N, DevStatus *st, cudaStream_t s);
+void launch_bins(CellDev *cells, int N, int L, int *bin_count, int *bin_cells, int nbx, int nby, DevStatus *st,
+                 cudaStream_t s);
+void launch_repack(CellArgs a, double *scratch_phi, double *scratch_rep, long long cap, cudaStream_t s);
+void launch_box_gather(const BoxArgs &a, cudaStream_t s);
+int cg_grid_blocks(int device);
+cudaError_t launch_cg(const CGArgs &a, int blocks, cudaStream_t s);
+
+}  // namespace rc

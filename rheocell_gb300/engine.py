@@ -1,0 +1,116 @@
+"""Python handle on the GB300 engine's C ABI (librheocell_gb300.so).
+
+This is a thin caller: every step, force evaluation and solve runs in the
+CUDA library.  There is no CPU fallback -- if the library cannot be loaded the
+constructor raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Dict, List, Optional
+
+import numpy as np
+
+from . import abi, build as _build
+from .host import HostCells
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def lib() -> C.CDLL:
+    """Load (building first if needed) the engine library."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_build.LIB):
+            _build.build()
+        if not os.path.exists(_build.LIB):
+            raise RuntimeError("GB300 engine library %s is missing" % _build.LIB)
+        _lib = abi.declare(C.CDLL(_build.LIB), "rc")
+    return _lib
+
+
+class EngineError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__("rc error %d: %s" % (code, msg))
+        self.code = code
+
+
+SCALARS = ["lsub_x", "lsub_y", "offset_x", "offset_y", "corner", "type", "com_x", "com_y",
+           "unrap_x", "unrap_y", "q00", "q01", "theta_q", "nemq_x", "nemq_y", "area", "sum_f",
+           "perimeter", "s00", "s01", "force_rep_x", "force_rep_y"]
+
+
+class Engine:
+    """One monolayer on one GPU (rc_create / rc_step / rc_download ...)."""
+
+    def __init__(self, params: abi.RcParams, L: int, cells: HostCells, device: int = 0):
+        self._lib = lib()
+        self.h = C.c_void_p()
+        box = abi.RcBox(L, L)
+        rc = self._lib.rc_create(C.byref(params), C.byref(box), cells.n, cells.arr, device, C.byref(self.h))
+        if rc != 0:
+            msg = self._lib.rc_last_error(self.h).decode()
+            if self.h:
+                self._lib.rc_destroy(self.h)
+            self.h = None
+            raise EngineError(rc, msg)
+        self.n = cells.n
+        self.L = L
+        self.stats = abi.RcStepStats()
+
+    def _check(self, rc: int, what: str):
+        if rc != 0:
+            raise EngineError(rc, "%s: %s" % (what, self._lib.rc_last_error(self.h).decode()))
+
+    def step(self, n: int = 1) -> abi.RcStepStats:
+        self._check(self._lib.rc_step(self.h, n, C.byref(self.stats)), "rc_step")
+        return self.stats
+
+    def set_phase(self, active: int) -> None:
+        self._check(self._lib.rc_set_phase(self.h, active), "rc_set_phase")
+
+    def set_stream(self, stream_ptr: int) -> None:
+        self._check(self._lib.rc_set_stream(self.h, C.c_void_p(stream_ptr)), "rc_set_stream")
+
+    def site_count(self) -> int:
+        return int(self._lib.rc_site_count(self.h))
+
+    def sizes(self):
+        lx = (C.c_int * self.n)()
+        ly = (C.c_int * self.n)()
+        self._check(self._lib.rc_get_sizes(self.h, None, lx, ly), "rc_get_sizes")
+        return list(lx), list(ly)
+
+    def state(self, mask: int = abi.RC_FIELD_ALL) -> Dict[str, np.ndarray]:
+        lx, ly = self.sizes()
+        sizes = [a * b for a, b in zip(lx, ly)]
+        hc = HostCells(self.n)
+        for i in range(self.n):
+            hc.attach(i, sizes[i])
+        self._check(self._lib.rc_download(self.h, hc.arr, mask), "rc_download")
+        out = {k: hc.scalar(k) for k in SCALARS}
+        for nm in ("phi", "vx", "vy", "mu", "dx", "dy", "box_index"):
+            out[nm] = hc.site_array(nm, sizes)
+        return out
+
+    def download(self, hc: HostCells, mask: int) -> None:
+        self._check(self._lib.rc_download(self.h, hc.arr, mask), "rc_download")
+
+    def upload(self, hc: HostCells, mask: int) -> None:
+        self._check(self._lib.rc_upload(self.h, hc.arr, mask), "rc_upload")
+
+    def close(self):
+        if self.h:
+            self._lib.rc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

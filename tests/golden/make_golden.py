@@ -1,0 +1,118 @@
+"""Generate the golden fixtures in this directory from the reference itself.
+
+Runs the unmodified reference (compiled out of tree by oracle/Makefile into
+oracle/_ref/ref_driver_exact; the wet models use the project's Eigen-API
+shim) on small seeded cases written by rheocell_gb300.generator, and stores
+its state dumps as compressed .npz files:
+
+  * per recorded step: every per-cell scalar of the dump;
+  * phi at the first and the last recorded step after step 0;
+  * at the last recorded step also vx, vy, mu and the box map.
+
+Run from the repository root:  python tests/golden/make_golden.py
+(needs oracle/_ref, i.e. `make -C oracle`; only this container has the
+reference sources).
+"""
+from __future__ import annotations
+
+import json
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from rheocell_gb300 import generator as g  # noqa: E402
+from oracle import refdump  # noqa: E402
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+SMALL = dict(R=5, lam=1.5, patch=27)
+DRY_POLAR_S = dict(g.DRY_POLAR, R=5)
+NEMATIC_S = dict(interaction_type="activenematic", R=5, dt=0.1, gamma=0.06, mu=45, kappa=0.1,
+                 **{"lambda": 1.5}, friction=1, zetaQ_self=0.1, zetaQ_inter=0.05, J_Q=0.5, omega=0.004)
+WET_S = dict(g.WET_NEMATIC, R=5, **{"lambda": 1.5}, omega=0.004, zetaQ_inter=0.02)
+WETPOLAR_S = dict(DRY_POLAR_S, friction_cell=1, CGtolerance=1e-8, J_Q=0.3, zetaQ_inter=0.1)
+SIMPLE_S = dict(interaction_type="simplefield", R=5, dt=0.1, gamma=0.06, mu=45, kappa=0.1, omega=0)
+
+# name: (monolayer kwargs, params, dump steps, seed, equilibration steps)
+CASES = {
+    "polar_dry": (dict(L=48, n=9, seed=3, **SMALL), DRY_POLAR_S, [0, 1, 2, 10], 11, 0),
+    "polar_noise": (dict(L=36, n=4, seed=4, **SMALL), dict(DRY_POLAR_S, zetaQ_inter=0.2, J_Q=0.5), [0, 1, 5], 12, 0),
+    "nematic": (dict(L=48, n=9, seed=5, types=[0, 1, 1, 0, 1, 1, 0, 1, 1], **SMALL), NEMATIC_S, [0, 1, 10], 13, 0),
+    "simple": (dict(L=36, n=4, seed=6, **SMALL), SIMPLE_S, [0, 1, 5], 14, 0),
+    "wet": (dict(L=48, n=9, seed=7, **SMALL), WET_S, [0, 1, 4], 15, 0),
+    "wetpolar": (dict(L=36, n=4, seed=8, **SMALL), WETPOLAR_S, [0, 1, 4], 16, 0),
+    "wet_equil": (dict(L=36, n=4, seed=9, **SMALL), WET_S, [0, 2], 17, 3),
+    "polar41": (dict(L=64, n=4, seed=10), g.DRY_POLAR, [0, 1, 3], 18, 0),
+    "resize": (dict(L=64, n=4, seed=11, R=5, lam=1.5, patch=27, aspect=2.2), DRY_POLAR_S, [0, 1, 2], 19, 0),
+}
+
+
+def monolayer(kw):
+    kw = dict(kw)
+    return g.make_monolayer(kw.pop("L"), kw.pop("n"), kw.pop("seed"), **kw)
+
+
+def record(name):
+    mkw, params, steps, seed, eq = CASES[name]
+    m = monolayer(mkw)
+    d = tempfile.mkdtemp(prefix="rc_golden_")
+    try:
+        g.write_case(d, m, params, steps=max(steps), seed=seed, equilibration_steps=eq)
+        recs = refdump.run_reference(d, steps, flavour="exact")
+        conf = open(os.path.join(d, "start_conf.dat")).read()
+        topo = open(os.path.join(d, "topology.top")).read()
+        inp = open(os.path.join(d, "input")).read()
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    out = {"conf": np.array(conf), "topology": np.array(topo), "input": np.array(inp),
+           "steps": np.array([r["step"] for r in recs], dtype=np.int64)}
+    for i, r in enumerate(recs):
+        s = r["step"]
+        for k in refdump.CELL_I32 + refdump.CELL_F64:
+            out["s%d_%s" % (s, k)] = r[k]
+        if s > 0 and (i == 1 or i == len(recs) - 1):
+            out["s%d_phi" % s] = r["phi"]
+    last = recs[-1]
+    for k in ("vx", "vy", "mu", "map"):
+        out["last_%s" % k] = last[k]
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    return recs
+
+
+def record_overlap():
+    """21 patches on one spot: the reference aborts (WetModel.cpp:475-480)."""
+    pos = np.tile([[24.3, 24.7]], (21, 1))
+    m = g.make_monolayer(48, 21, seed=1, R=5, lam=1.5, patch=27, positions=pos)
+    d = tempfile.mkdtemp(prefix="rc_golden_")
+    try:
+        g.write_case(d, m, DRY_POLAR_S, steps=1, seed=1)
+        res = subprocess.run([refdump.driver_path("exact"), "dump", os.path.join(d, "x.bin"), "1", "input"],
+                             cwd=d, capture_output=True, text=True)
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    info = {"returncode": res.returncode, "overlap_error": "Too many field patches overlap" in res.stderr}
+    with open(os.path.join(HERE, "overlap.json"), "w") as f:
+        json.dump(info, f, indent=1)
+    return info
+
+
+def main():
+    if not refdump.have_reference("exact"):
+        subprocess.check_call(["make", "-C", os.path.join(ROOT, "oracle"), "-j8"])
+    for name in CASES:
+        recs = record(name)
+        sz = os.path.getsize(os.path.join(HERE, name + ".npz"))
+        print("%-12s steps %s  cells %d  sizes %s  %.0f KB" % (name, [r["step"] for r in recs], recs[0]["N"],
+                                                                sorted(set(zip(recs[-1]["lx"], recs[-1]["ly"]))), sz / 1024))
+    print("overlap", record_overlap())
+
+
+if __name__ == "__main__":
+    main()

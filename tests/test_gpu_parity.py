@@ -1,0 +1,120 @@
+"""Parity of the CUDA engine (through its C ABI) with the reference's golden
+dumps and with the CPU restatement.
+
+Tolerances: the engine sums per-cell quantities (area, sums for the centre of
+mass, shape tensor, force totals) with a fixed tree instead of the reference's
+sequential loop, and the viscous solve reduces in a different order; every
+other operation is the reference's IEEE FP64 arithmetic in its order.  So
+per-step results agree to ~1e-15 and the stated bar, 1e-10 relative over 100
+steps, is checked on the dry models at the 140x140 / 100-cell workload."""
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+from rheocell_gb300 import abi, engine, generator as g
+from tests.common import (build_inputs, case_from_monolayer, case_from_texts, compare_to_golden, golden,
+                          rel_err, run)
+
+pytestmark = pytest.mark.gpu
+
+ALL = ["polar_dry", "polar_noise", "nematic", "simple", "polar41", "resize", "wet", "wetpolar", "wet_equil"]
+EQ = {"wet_equil": 3}
+TOL = 1e-10
+
+
+@pytest.mark.parametrize("name", ALL)
+def test_engine_matches_reference_golden(name):
+    gd = golden(name)
+    keys, m = case_from_texts(str(gd["input"]), str(gd["conf"]), str(gd["topology"]))
+    _, states = run(engine.Engine, keys, m, [int(s) for s in gd["steps"]], eq=EQ.get(name, 0))
+    errs = compare_to_golden(gd, states)
+    bad = {k: v for k, v in errs.items() if v > TOL}
+    assert not bad, bad
+
+
+def _pair(keys, m, steps, eq=0):
+    _, a = run(engine.Engine, keys, m, steps, eq=eq)
+    _, b = run(orc.OracleSim, keys, m, steps, eq=eq)
+    return a, b
+
+
+FIELDS = ["phi", "vx", "vy", "mu", "area", "com_x", "com_y", "q00", "q01", "nemq_x", "s00", "s01"]
+
+
+def _check(a, b, steps, tol=TOL, fields=FIELDS):
+    worst = {}
+    for s in steps:
+        for f in fields:
+            worst[(s, f)] = rel_err(a[s][f], b[s][f])
+        for f in ("lsub_x", "lsub_y", "corner", "offset_x", "offset_y"):
+            assert np.array_equal(a[s][f], b[s][f]), (s, f)
+        assert np.array_equal(a[s]["box_index"], b[s]["box_index"]), s
+    bad = {k: v for k, v in worst.items() if v > tol}
+    assert not bad, bad
+    return worst
+
+
+def test_dry_polar_140_100cells_100_steps():
+    """The CPU-runnable workload: 140x140, 100 cells, 41x41 patches, dry polar."""
+    m = g.make_monolayer(140, 100, seed=1)
+    keys, m2 = case_from_monolayer(m, g.DRY_POLAR, seed=1)
+    a, b = _pair(keys, m2, [1, 10, 100])
+    _check(a, b, [1, 10, 100])
+
+
+@pytest.mark.parametrize("model", ["activenematic", "simplefield"])
+def test_dry_models_vs_oracle(model):
+    m = g.make_monolayer(96, 36, seed=2, types=[i % 2 for i in range(36)])
+    params = dict(g.DRY_POLAR, interaction_type=model, zetaQ_self=0.1, zetaQ_inter=0.05, J_Q=0.2, omega=0.004)
+    keys, m2 = case_from_monolayer(m, params, seed=3)
+    a, b = _pair(keys, m2, [1, 30])
+    _check(a, b, [1, 30])
+
+
+def test_polar_noise_and_torque_vs_oracle():
+    m = g.make_monolayer(96, 36, seed=4)
+    params = dict(g.DRY_POLAR, zetaQ_inter=0.3, J_Q=0.5, beta=0.5, omega=0.004)
+    keys, m2 = case_from_monolayer(m, params, seed=5)
+    a, b = _pair(keys, m2, [1, 20], eq=2)
+    _check(a, b, [1, 20], fields=FIELDS + ["theta_q", "force_rep_x", "perimeter"])
+
+
+@pytest.mark.parametrize("model", ["wetmodel", "wetpolarmodel"])
+def test_wet_vs_oracle(model):
+    m = g.make_monolayer(64, 9, seed=6)
+    params = dict(g.WET_NEMATIC, interaction_type=model, beta=0, zetaQ_inter=0.02, omega=0.004)
+    keys, m2 = case_from_monolayer(m, params, seed=7)
+    a, b = _pair(keys, m2, [1, 12])
+    _check(a, b, [1, 12], tol=1e-9)
+
+
+def test_deterministic_bitwise():
+    m = g.make_monolayer(96, 36, seed=8)
+    keys, m2 = case_from_monolayer(m, dict(g.WET_NEMATIC, zetaQ_inter=0.02), seed=9)
+    _, a = run(engine.Engine, keys, m2, [5])
+    _, b = run(engine.Engine, keys, m2, [5])
+    for k in ("phi", "vx", "vy", "area", "com_x"):
+        assert np.array_equal(a[5][k], b[5][k]), k
+
+
+def test_overlap_is_an_error():
+    pos = np.tile([[24.3, 24.7]], (21, 1))
+    m = g.make_monolayer(48, 21, seed=1, R=5, lam=1.5, patch=27, positions=pos)
+    keys, m2 = case_from_monolayer(m, dict(g.DRY_POLAR, R=5))
+    p, cells = build_inputs(keys, m2)
+    with pytest.raises(engine.EngineError) as ei:
+        engine.Engine(p, m2.L, cells)
+    assert ei.value.code == abi.RC_ERR_OVERLAP
+
+
+def test_cg_residual_and_stats():
+    """Every solve stops at |r| < tol |b| (Eigen's criterion)."""
+    m = g.make_monolayer(128, 64, seed=10)
+    keys, m2 = case_from_monolayer(m, g.WET_NEMATIC, seed=11)
+    p, cells = build_inputs(keys, m2)
+    e = engine.Engine(p, m2.L, cells)
+    e.set_phase(1)
+    st = e.step(3)
+    assert st.steps_done == 3 and st.cg_solves == 3 * 2 * 2
+    assert 0 < st.cg_max_rel_residual < 1e-8
+    assert st.cg_iterations > 0

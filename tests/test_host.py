@@ -1,0 +1,97 @@
+"""Host-side logic: drand48 / gaussian stream, input keys and constructor
+defaults per model, and the configuration file format."""
+import ctypes
+import math
+import os
+
+import numpy as np
+import pytest
+
+from rheocell_gb300 import abi, generator as g, host
+
+
+def test_drand48_matches_libc():
+    libc = ctypes.CDLL(None)
+    libc.drand48.restype = ctypes.c_double
+    for seed in (1, 4982, 123456789, -5):
+        libc.srand48(ctypes.c_long(seed))
+        r = host.Drand48(seed)
+        for _ in range(200):
+            assert r.drand48() == libc.drand48()
+
+
+def test_gaussian_pairs_and_cache():
+    r = host.Drand48(7)
+    a = r.gaussian()
+    assert r.has_cached == 1
+    b = r.gaussian()
+    assert r.has_cached == 0 and b == r.cached and a != b
+
+
+def test_params_defaults_per_model():
+    base = dict(R=8, dt=0.1, zetaQ_self=0.1, zetaQ_inter=0, J_Q=0, friction=1, friction_cell=0, beta=0)
+    p = host.make_params(dict(base, interaction_type="simplefield", **{"lambda": 2.0}))
+    assert p.lambda_ == 2.5, "SimpleMultiField::get_settings does not read lambda"
+    p = host.make_params(dict(base, interaction_type="activenematic", friction=3))
+    assert list(p.friction) == [3.0, 3.0] and list(p.zetaQ_self) == [0.0, 0.1]
+    p = host.make_params(dict(base, interaction_type="wetpolarmodel", friction=2, friction_cell=1))
+    assert list(p.friction) == [1.0, 2.0] and list(p.friction_cell) == [0.0, 1.0]
+    assert p.cg_restart_every == 10 and p.cg_tolerance == 1e-4
+    p = host.make_params(dict(base, interaction_type="wetmodel", CGtolerance=1e-8))
+    assert p.cg_restart_every == 100 and p.cg_tolerance == 1e-8 and p.gamma == 0.01
+
+
+def test_params_reject_unprovided():
+    base = dict(R=8, dt=0.1, zetaQ_self=0, zetaQ_inter=0, J_Q=0, friction=1, friction_cell=0, beta=0,
+                interaction_type="wetpolarmodel")
+    with pytest.raises(ValueError):
+        host.make_params(dict(base, interaction_type="lebcwetmodel"))
+    with pytest.raises(ValueError):
+        host.make_params(dict(base, box="channel"))
+    with pytest.raises(ValueError):
+        host.make_params(dict(base, wall_slip=0))
+    with pytest.raises(ValueError):
+        host.make_params({k: v for k, v in base.items() if k != "friction_cell"})
+
+
+def test_nemq_seeding_order():
+    m = g.make_monolayer(64, 4, seed=1)
+    keys = dict(interaction_type="wetmodel", seed="5")
+    cells, rng = host.make_cells(m, keys, 5)
+    r = host.Drand48(5)
+    for i in range(4):
+        th = float(np.float32(math.pi)) * (1 - 2 * r.drand48())
+        q0 = math.cos(2 * th)
+        assert cells.arr[i].nemq_x == math.sqrt((1 + q0 / math.hypot(q0, math.sin(2 * th))) / 2)
+    polar = dict(keys, interaction_type="wetpolarmodel")
+    _, rng2 = host.make_cells(m, polar, 5)
+    assert rng2.state != rng.state  # read_topology draws once per cell first
+
+
+def test_conf_roundtrip(tmp_path):
+    m = g.make_monolayer(64, 4, seed=2)
+    p = tmp_path / "c.dat"
+    g.write_conf(str(p), m)
+    m2 = g.read_conf(str(p))
+    assert m2.L == 64 and m2.n == 4
+    for a, b in zip(m.cells, m2.cells):
+        assert (a.lx, a.ly, a.corner, a.offset) == (b.lx, b.ly, b.corner, b.offset)
+        np.testing.assert_array_equal(a.box_index, b.box_index)
+        np.testing.assert_allclose(a.phi, b.phi, rtol=1e-14, atol=1e-300)
+    g.write_conf(str(p) + "2", m2)
+    assert open(str(p)).read() == open(str(p) + "2").read()
+
+
+def test_generator_shapes():
+    m = g.make_monolayer(140, 100, seed=1)
+    assert m.sites == 100 * 41 * 41
+    assert all(c.lx == 41 and 0 <= c.com[0] < 140 for c in m.cells)
+    phi = np.concatenate([c.phi for c in m.cells])
+    assert phi.max() < 1.0 and phi.min() > 0.0
+
+
+def test_read_input(tmp_path):
+    p = tmp_path / "input"
+    p.write_text("a = 1 # c\n# full\nb=  x y \n a = 2\n")
+    k = host.read_input(str(p), {"c": 3})
+    assert k == {"a": "2", "b": "x y", "c": "3"}

@@ -1,0 +1,64 @@
+"""The CPU restatement (oracle/rc_oracle.c) against the unmodified reference's
+own outputs (tests/golden, produced by tests/golden/make_golden.py).
+
+Dry models must match bit for bit; the wet models' viscous solve sums its dot
+products and operator rows in a different order than the reference's Eigen
+(shim) CG, so they are held to 1e-12 relative."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+from tests.common import GOLDEN, build_inputs, case_from_texts, compare_to_golden, golden, run
+
+DRY = ["polar_dry", "polar_noise", "nematic", "simple", "polar41", "resize"]
+WET = ["wet", "wetpolar", "wet_equil"]
+EQ = {"wet_equil": 3}
+
+
+def _run_oracle(name):
+    gd = golden(name)
+    keys, m = case_from_texts(str(gd["input"]), str(gd["conf"]), str(gd["topology"]))
+    _, states = run(orc.OracleSim, keys, m, [int(s) for s in gd["steps"]], eq=EQ.get(name, 0))
+    return gd, states
+
+
+@pytest.mark.parametrize("name", DRY)
+def test_oracle_matches_reference_bitwise(name):
+    gd, states = _run_oracle(name)
+    errs = compare_to_golden(gd, states)
+    bad = {k: v for k, v in errs.items() if v != 0.0}
+    assert not bad, bad
+
+
+@pytest.mark.parametrize("name", WET)
+def test_oracle_matches_reference_wet(name):
+    gd, states = _run_oracle(name)
+    errs = compare_to_golden(gd, states)
+    bad = {k: v for k, v in errs.items() if v > 1e-12}
+    assert not bad, bad
+
+
+def test_resize_case_resizes():
+    gd = golden("resize")
+    last = int(gd["steps"][-1])
+    sizes = set(zip(gd["s%d_lx" % last].tolist(), gd["s%d_ly" % last].tolist()))
+    assert sizes != {(27, 27)}, "fixture must exercise MultiPhaseField::set_positions' resize branch"
+    _, states = _run_oracle("resize")
+    assert set(zip(states[last]["lsub_x"].tolist(), states[last]["lsub_y"].tolist())) == sizes
+
+
+def test_overlap_error_like_reference():
+    info = json.load(open(os.path.join(GOLDEN, "overlap.json")))
+    assert info["returncode"] != 0 and info["overlap_error"]
+    from rheocell_gb300 import generator as g
+    from tests.common import case_from_monolayer
+    from tests.golden.make_golden import DRY_POLAR_S
+    pos = np.tile([[24.3, 24.7]], (21, 1))
+    m = g.make_monolayer(48, 21, seed=1, R=5, lam=1.5, patch=27, positions=pos)
+    keys, m2 = case_from_monolayer(m, DRY_POLAR_S)
+    p, cells = build_inputs(keys, m2)
+    with pytest.raises(RuntimeError, match="overlap"):
+        orc.OracleSim(p, m2.L, cells)
