@@ -1,0 +1,351 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 multi-phase-field time step.
+
+Default workload (the configuration the headline metric is quoted on): the wet
+multi-phase-field monolayer, periodic 256x256 box, 400 cells of radius 8 on
+41x41 patches, wetmodel (Brinkman viscous solve, xi = eta = 1, CG rtol 1e-8),
+FP64, seeded synthetic initial condition (jittered triangular lattice, tanh
+interfaces) -- synthetic data with the workload's shapes, no dataset exists.
+A "step" is one FD_CPUBackend::sim_step (Heun predictor + corrector, two
+force evaluations, four viscous solves).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--workload wet256|dry140] [--precision double|mixed]
+
+Prints one JSON line (rank 0).  `value` is site-updates/s over all ranks with
+the state resident on the device, timed with CUDA events per step on the
+engine's stream, the L2 cache flushed (256 MiB write) before every timed
+step.  `e2e` is the same metric through the C ABI with host buffers: each
+step uploads phi from pinned memory, steps, and downloads phi.  Under
+torchrun every rank runs an independent replica on its own GPU (a monolayer
+does not shard; replicas only).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MPF steps/s + site-updates/s; wet-step CG time, learned-PCG vs plain @ rtol 1e-8"
+
+
+def workload(name):
+    from rheocell_gb300 import generator as g
+    if name == "wet256":
+        return dict(name="wet MPF 256x256, 400 cells, R=8, 41x41 patches, wetmodel xi=eta=1, CG rtol 1e-8",
+                    L=256, n=400, params=g.WET_NEMATIC, seed=1)
+    if name == "dry140":
+        return dict(name="dry polar MPF 140x140, 100 cells, R=8, 41x41 patches, wetpolarmodel friction_cell=0",
+                    L=140, n=100, params=g.DRY_POLAR, seed=1)
+    raise SystemExit("unknown workload %s" % name)
+
+
+def make_case(w):
+    from rheocell_gb300 import generator as g
+    from tests.common import build_inputs, case_from_monolayer
+    m = g.make_monolayer(w["L"], w["n"], seed=w["seed"])
+    keys, m2 = case_from_monolayer(m, w["params"], seed=w["seed"])
+    return keys, m2
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.proc = None
+        self.lines = []
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax = float(f[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cg_bytes_per_launch(S, L2, iters_per_launch, setup_reads=68.0):
+    """Algorithmic bytes of one viscous-solve launch (both components):
+    setup S*68 B (b, x, r, map); per component-iteration S*78 B (p, r, x reads
+    and writes, cover indices, map) + L2*28 B (box sums of p)."""
+    return S * setup_reads + iters_per_launch * (S * 78.0 + L2 * 28.0)
+
+
+def fused_bytes_per_site(model):
+    """Algorithmic HBM bytes per site of the dry fused predictor+corrector pair:
+    predictor reads phi^n, writes phi*, dphi^n (24 B); corrector reads phi*,
+    phi^n, dphi^n, writes phi^{n+1} (32 B); two box gathers read phi (16 B)."""
+    return 72.0
+
+
+def run_gb300(args, rank, world):
+    import torch
+    from rheocell_gb300 import abi, engine
+    from tests.common import build_inputs
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    w = workload(args.workload)
+    keys, m = make_case(w)
+    prec = abi.RC_PRECISION_MIXED if args.precision == "mixed" else abi.RC_PRECISION_DOUBLE
+    p, cells = build_inputs(keys, m, precision=prec)
+    stream = torch.cuda.current_stream(dev)
+    eng = engine.Engine(p, m.L, cells, device=dev)
+    eng.set_stream(stream.cuda_stream)
+    eng.set_phase(1)
+    lib = eng._lib
+    S = eng.site_count()
+    L2 = m.L * m.L
+    # warm-up
+    eng.step(max(args.warmup, 3) if args.warmup >= 0 else 3)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    lib.rc_set_timing(eng.h, 1)
+    lib.rc_timers(eng.h, None, None, 1)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(dev)
+    evs = []
+    for _ in range(args.steps):
+        flush.zero_()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        rc = lib.rc_step_async(eng.h, 1)
+        if rc != 0:
+            raise RuntimeError(lib.rc_last_error(eng.h).decode())
+        b.record(stream)
+        evs.append((a, b))
+    torch.cuda.synchronize()
+    st = abi.RcStepStats()
+    rc = lib.rc_wait(eng.h, C.byref(st))
+    if rc != 0:
+        raise RuntimeError(lib.rc_last_error(eng.h).decode())
+    clk = clocks.stop()
+    ms = sum(a.elapsed_time(b) for a, b in evs)
+    tms = (C.c_double * 6)()
+    tn = (C.c_longlong * 6)()
+    lib.rc_timers(eng.h, tms, tn, 1)
+    lib.rc_set_timing(eng.h, 0)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+
+    # end-to-end through the C ABI with host buffers
+    import numpy as np
+    host = torch.empty(S, dtype=torch.float64, pin_memory=True)
+    hp = C.cast(host.data_ptr(), abi.DP)
+    lib.rc_download_phi(eng.h, hp, S)
+    e2e_steps = max(1, min(args.steps, 10))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        if lib.rc_upload_phi(eng.h, hp, S) != 0 or lib.rc_step(eng.h, 1, None) != 0 or lib.rc_download_phi(eng.h, hp, S) != 0:
+            raise RuntimeError(lib.rc_last_error(eng.h).decode())
+    e2e_s = time.perf_counter() - t0
+    S_after = eng.site_count()
+    eng.close()
+
+    total_sites = S * args.steps * world
+    value = total_sites / (ms / 1e3)
+    names = abi.TIMER_NAMES
+    stage = {names[i]: {"ms": round(tms[i], 3), "launches": int(tn[i])} for i in range(6) if tn[i]}
+    peak, peak_kind = measured_peaks()
+    dom = max(range(6), key=lambda i: tms[i])
+    dom_avg_s = tms[dom] / max(tn[dom], 1) / 1e3
+    if names[dom] == "solve":
+        it_per_launch = st.cg_iterations / max(tn[dom], 1)
+        bytes_launch = cg_bytes_per_launch(S, L2, it_per_launch)
+        unit_desc = "viscous solve: %.1f component-iterations per launch" % it_per_launch
+    else:
+        bytes_launch = fused_bytes_per_site(w["params"]["interaction_type"]) / 2 * S
+        unit_desc = "per-cell update kernel: 36 B/site per launch"
+    achieved = bytes_launch / dom_avg_s / 1e9
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "traffic_%s.json" % args.workload)
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get(names[dom])
+        except Exception:
+            traffic = None
+    out = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "site-updates/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms / args.steps,
+        "steps_per_s": args.steps / (ms / 1e3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64" if args.precision == "double" else "f64 fields, f32 solve inner iterations",
+        "data": "synthetic (seeded jittered lattice, tanh interfaces)",
+        "config": {"workload": w["name"], "L": m.L, "cells": m.n, "sites": S, "precision": args.precision,
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "flushed (256 MiB write) before every timed step"},
+        "cg": {"solves": st.cg_solves, "iterations": st.cg_iterations, "max_iterations": st.cg_max_iterations,
+               "max_rel_residual": st.cg_max_rel_residual,
+               "ms_per_step": tms[3] / args.steps if tn[3] else 0.0},
+        "stages_ms": stage,
+        "gpu_launches": int(st.kernel_launches),
+        "clocks": clk,
+        "e2e": {"value": S * e2e_steps / e2e_s * world, "unit": "site-updates/s",
+                "h2d_bytes_per_step": 8 * S, "d2h_bytes_per_step": 8 * S,
+                "how": "rc_upload_phi (pinned) + rc_step(1) + rc_download_phi (pinned), wall clock, %d steps" % e2e_steps},
+        "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                     "algorithmic_bytes_per_launch": bytes_launch, "launch_ms": dom_avg_s * 1e3,
+                     "units": unit_desc, "traffic": traffic},
+    }
+    if S_after != S:
+        out["config"]["sites_after"] = S_after
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(args, w, keys, m)
+    return out
+
+
+def cpu_baseline(args, w, keys, m, budget_s=25.0, max_steps=None):
+    """The CPU restatement (oracle/, serial FP64, the reference's algorithm)
+    on the same workload, timed on this host for a bounded number of steps."""
+    from oracle import oracle as orc
+    from tests.common import build_inputs
+    orc.build()
+    p, cells = build_inputs(keys, m)
+    sim = orc.OracleSim(p, m.L, cells)
+    sim.set_phase(1)
+    steps = 0
+    t0 = time.perf_counter()
+    while True:
+        sim.step(1)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or (max_steps and steps >= max_steps):
+            break
+        if el / steps * (steps + 1) > budget_s * 1.5:
+            break
+    S = sim.site_count() if hasattr(sim, "site_count") else m.sites
+    sim.close()
+    return {"value": m.sites * steps / el, "unit": "site-updates/s", "cores": 1, "kind": "port",
+            "sample": "%d main-loop step(s) of the same workload, %.1f s wall" % (steps, el)}
+
+
+def run_reference(args, rank, world):
+    """Reference arm: the reference's CPU implementation of the path.  The
+    compiled reference (oracle/_ref) is an x86 build made where the reference
+    sources are; it does not exist on the GPU host, so this times the CPU
+    restatement (bit-identical to the reference on the dry models), which is
+    single-threaded as the reference's stepping is."""
+    if rank != 0:
+        return None
+    w = workload(args.workload)
+    keys, m = make_case(w)
+    from oracle import refdump
+    kind = "port"
+    budget = 90.0
+    base = cpu_baseline(args, w, keys, m, budget_s=budget, max_steps=max(1, args.steps))
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": base["value"],
+        "unit": "site-updates/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded jittered lattice, tanh interfaces)",
+        "config": {"workload": w["name"], "L": m.L, "cells": m.n, "sites": m.sites, "precision": "double"},
+        "cpu_baseline": dict(base, kind=kind),
+        "e2e": {"value": base["value"], "unit": "site-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    return line
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="wet256", choices=["wet256", "dry140"])
+    ap.add_argument("--precision", default="double", choices=["double", "mixed"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+    else:
+        from rheocell_gb300 import build
+        build.build()
+        out = run_gb300(args, rank, world)
+    if rank == 0 and out is not None:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -138,6 +138,7 @@ typedef struct rc_step_stats {
 	double cg_max_rel_residual; /* largest |r|/|b| at exit                    */
 	int resized_cells;       /* patches that changed size                     */
 	int refinements;         /* mixed precision: outer refinement sweeps      */
+	long long kernel_launches; /* engine kernels launched by the call         */
 } rc_step_stats;
 
 typedef struct rc_engine rc_engine;
@@ -163,6 +164,19 @@ int rc_create(const rc_params *params, const rc_box *box, int n_cells,
 int rc_step(rc_engine *e, int n_steps, rc_step_stats *stats);
 
 /*
+ * Enqueue n_steps time steps on the engine's stream and return at once.
+ * Errors raised on the device are reported by the next rc_wait.  Patch sizes
+ * are not re-examined between the steps of one call, so a patch that grows
+ * past the engine's current shared-memory sizing is reported as
+ * RC_ERR_CAPACITY; rc_step does that check every 16 steps.
+ */
+int rc_step_async(rc_engine *e, int n_steps);
+
+/* Wait for enqueued work; report device errors and the statistics
+ * accumulated since the last rc_wait / rc_step (stats may be NULL). */
+int rc_wait(rc_engine *e, rc_step_stats *stats);
+
+/*
  * Select the parameter set: 0 before, 1 after
  * apply_simulation_changes_after_equilibration (src/Backends/SimBackend.cpp:316-325).
  */
@@ -182,10 +196,38 @@ int rc_download(rc_engine *e, rc_cell_host *cells, unsigned fields_mask);
 /*
  * Copy host edits into device state (SimBackend::apply_changes_to_simulation_data,
  * src/Backends/SimBackend.cpp:331-333).  Patch sizes cannot change here.  After
- * an upload of RC_FIELD_PHI the forces are re-evaluated with the current
- * parameters, so the next step sees consistent forces.
+ * upload the next step uses the forces of the last evaluation (computed
+ * before the edit), as the reference's CPU backend does.
  */
 int rc_upload(rc_engine *e, const rc_cell_host *cells, unsigned fields_mask);
+
+/*
+ * Flat transfers of phi: the patches of all cells concatenated in cell order,
+ * each in storage order (the layout of the reference's stacked solver
+ * unknowns, field_start_index, WetModel.cpp:203-209).  n must equal
+ * rc_site_count(e).  One copy each way; host memory may be pinned.  The
+ * upload follows rc_upload's semantics for RC_FIELD_PHI.
+ */
+int rc_download_phi(rc_engine *e, double *phi, long long n);
+int rc_upload_phi(rc_engine *e, const double *phi, long long n);
+
+/*
+ * Stage timers (CUDA events on the engine's stream), the device-side
+ * counterpart of the reference's TimingManager stages "First Step" and
+ * "Forces" (src/Backends/FDBackend.cpp:41-43).  While enabled, every stage
+ * launch is bracketed by two events; rc_timers() adds up the elapsed times of
+ * the completed ones (it synchronises) and reports, per stage, the total
+ * milliseconds and the number of launches.  reset != 0 zeroes the totals.
+ */
+#define RC_TIMER_UPDATE 0   /* per-cell kernels: update (and fused dry forces) */
+#define RC_TIMER_GATHER 1   /* box gather (and solver bookkeeping)            */
+#define RC_TIMER_FORCES 2   /* wet force / right-hand-side evaluation         */
+#define RC_TIMER_SOLVE  3   /* viscous solve                                  */
+#define RC_TIMER_REPACK 4   /* patch resize repack                            */
+#define RC_TIMER_RNG    5   /* polar noise stream                             */
+#define RC_NUM_TIMERS   6
+int rc_set_timing(rc_engine *e, int enable);
+int rc_timers(rc_engine *e, double *ms, long long *launches, int reset);
 
 /* Issue the engine's work on this cudaStream_t (NULL: the engine's own). */
 int rc_set_stream(rc_engine *e, void *cuda_stream);

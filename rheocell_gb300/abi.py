@@ -80,7 +80,7 @@ class RcStepStats(C.Structure):
     _fields_ = [
         ("steps_done", C.c_longlong), ("cg_solves", C.c_int), ("cg_iterations", C.c_int),
         ("cg_max_iterations", C.c_int), ("cg_max_rel_residual", C.c_double),
-        ("resized_cells", C.c_int), ("refinements", C.c_int),
+        ("resized_cells", C.c_int), ("refinements", C.c_int), ("kernel_launches", C.c_longlong),
     ]
 
 
@@ -113,6 +113,18 @@ def declare(lib: C.CDLL, prefix: str) -> C.CDLL:
         lib.rc_set_stream.restype = C.c_int
         lib.rc_abi_version.argtypes = []
         lib.rc_abi_version.restype = C.c_int
+        lib.rc_step_async.argtypes = [vp, C.c_int]
+        lib.rc_step_async.restype = C.c_int
+        lib.rc_wait.argtypes = [vp, C.POINTER(RcStepStats)]
+        lib.rc_wait.restype = C.c_int
+        lib.rc_download_phi.argtypes = [vp, DP, C.c_longlong]
+        lib.rc_download_phi.restype = C.c_int
+        lib.rc_upload_phi.argtypes = [vp, DP, C.c_longlong]
+        lib.rc_upload_phi.restype = C.c_int
+        lib.rc_set_timing.argtypes = [vp, C.c_int]
+        lib.rc_set_timing.restype = C.c_int
+        lib.rc_timers.argtypes = [vp, DP, C.POINTER(C.c_longlong), C.c_int]
+        lib.rc_timers.restype = C.c_int
     else:
         lib.orc_rng_state.argtypes = [vp]
         lib.orc_rng_state.restype = C.c_ulonglong
@@ -120,6 +132,8 @@ def declare(lib: C.CDLL, prefix: str) -> C.CDLL:
 
 
 # Every symbol the header declares (checked by the CPU test suite).
-EXPORTED = ["rc_abi_version", "rc_create", "rc_step", "rc_set_phase", "rc_get_sizes",
-            "rc_download", "rc_upload", "rc_set_stream", "rc_site_count", "rc_last_error",
-            "rc_destroy"]
+EXPORTED = ["rc_abi_version", "rc_create", "rc_step", "rc_step_async", "rc_wait", "rc_set_phase",
+            "rc_get_sizes", "rc_download", "rc_upload", "rc_download_phi", "rc_upload_phi", "rc_set_stream",
+            "rc_set_timing", "rc_timers", "rc_site_count", "rc_last_error", "rc_destroy"]
+
+TIMER_NAMES = ["update", "gather", "forces", "solve", "repack", "rng"]

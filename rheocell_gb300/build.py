@@ -18,6 +18,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "librheocell_gb300.so")
+CLI = os.path.join(BUILD, "rheocell")
+HOST_SRC = os.path.join(HERE, "host", "rheocell.cpp")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
                      "-Xptxas", "-O3"]
@@ -42,10 +44,10 @@ def _deps():
 
 
 def up_to_date() -> bool:
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(CLI):
         return False
-    t = os.path.getmtime(LIB)
-    return all(os.path.getmtime(d) <= t for d in _deps())
+    t = min(os.path.getmtime(LIB), os.path.getmtime(CLI))
+    return all(os.path.getmtime(d) <= t for d in _deps() + [HOST_SRC])
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
@@ -73,6 +75,13 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
     os.replace(tmp, LIB)
+    # the command-line driver (C++ host above the C ABI)
+    cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-ffp-contract=off", HOST_SRC, "-o", CLI + ".tmp",
+           "-L" + BUILD, "-lrheocell_gb300", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("host driver build failed:\n%s%s" % (r.stdout, r.stderr))
+    os.replace(CLI + ".tmp", CLI)
     return LIB
 
 

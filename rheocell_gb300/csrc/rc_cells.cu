@@ -161,6 +161,7 @@ __device__ void set_positions_dev(CellDev &c, const DevParams &P, DevStatus *st,
 	c.comx = (int) (site - (int) (site / L) * L);
 	c.resized = 1;
 	atomicAdd(&st->resized, 1);
+	atomicAdd(&st->resized_total, 1);
 }
 
 __device__ void directed_forces_dev(CellDev &c, const DevParams &P, const PhaseParams &pu, int store, DevStatus *st,

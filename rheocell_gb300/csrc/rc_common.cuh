@@ -71,11 +71,13 @@ struct DevStatus {
 	long long S_rows; // size_rows of the last evaluation (solver bookkeeping)
 	int restart;      // restart_solver
 	int cg_cold;      // the next solve starts from zero
+	// counters since the last status read (zeroed together, one memset)
 	int cg_solves;
 	int cg_iters;
 	int cg_max_iters;
-	double cg_max_rel;
 	int refinements;
+	double cg_max_rel;
+	int resized_total;
 	int overflow_used;
 	unsigned long long rng_state;
 	int rng_has;

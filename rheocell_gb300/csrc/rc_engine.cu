@@ -27,6 +27,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstddef>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -70,7 +71,62 @@ struct rc_engine {
 	std::vector<void *> allocs;
 	std::string err;
 	std::string launch_error;  // first failed cooperative launch
+	long long launches = 0;    // engine kernels enqueued since the last status read
+	long long async_steps = 0;
+	// stage timers
+	bool timing = false;
+	struct Mark {
+		int stage;
+		cudaEvent_t a, b;
+	};
+	std::vector<Mark> marks;
+	std::vector<cudaEvent_t> event_pool;
+	double timer_ms[RC_NUM_TIMERS] = {0};
+	long long timer_n[RC_NUM_TIMERS] = {0};
 };
+
+static cudaEvent_t get_event(rc_engine *e) {
+	if(!e->event_pool.empty()) {
+		cudaEvent_t v = e->event_pool.back();
+		e->event_pool.pop_back();
+		return v;
+	}
+	cudaEvent_t v;
+	cudaEventCreate(&v);
+	return v;
+}
+
+// Brackets one stage launch with events when timing is enabled.
+struct StageMark {
+	rc_engine *e;
+	rc_engine::Mark m;
+	StageMark(rc_engine *e_, int stage) : e(e_) {
+		if(!e->timing) return;
+		m.stage = stage;
+		m.a = get_event(e);
+		m.b = get_event(e);
+		cudaEventRecord(m.a, e->stream);
+	}
+	~StageMark() {
+		if(!e->timing) return;
+		cudaEventRecord(m.b, e->stream);
+		e->marks.push_back(m);
+	}
+};
+
+// Add up completed marks (the stream must be idle).
+static void collect_marks(rc_engine *e) {
+	for(auto &m : e->marks) {
+		float ms = 0;
+		if(cudaEventElapsedTime(&ms, m.a, m.b) == cudaSuccess) {
+			e->timer_ms[m.stage] += ms;
+			e->timer_n[m.stage] += 1;
+		}
+		e->event_pool.push_back(m.a);
+		e->event_pool.push_back(m.b);
+	}
+	e->marks.clear();
+}
 
 static std::string g_create_error;
 
@@ -160,7 +216,9 @@ static void gather(rc_engine *e, const double *phi, int phase) {
 	b.solve_follows = wet_phase(e, phase);
 	b.st = e->st;
 	b.L = e->L;
+	StageMark sm(e, RC_TIMER_GATHER);
 	launch_box_gather(b, e->stream);
+	e->launches += b.bookkeeping ? 2 : 1;
 }
 
 static void solve(rc_engine *e, int phase) {
@@ -189,7 +247,9 @@ static void solve(rc_engine *e, int phase) {
 	g.xi = e->ph[phase].friction;
 	g.eta = e->ph[phase].friction_cell;
 	g.tol = e->hp.cg_tolerance > 0 ? e->hp.cg_tolerance : 2.220446049250313e-16;
+	StageMark sm(e, RC_TIMER_SOLVE);
 	const cudaError_t c = launch_cg(g, e->cg_blocks, e->stream);
+	e->launches += 1;
 	if(c != cudaSuccess && e->launch_error.empty()) e->launch_error = cudaGetErrorString(c);
 }
 
@@ -202,7 +262,11 @@ static void evaluate_end(rc_engine *e, const double *phi, int phase) {
 		a.phi_eval = phi;
 		a.pe = e->ph[phase];
 		a.pu = e->ph[phase];
-		launch_cell_kernel(e->P.model, EV_WET_RHS, UP_NONE, a, e->stream);
+		{
+			StageMark sm(e, RC_TIMER_FORCES);
+			launch_cell_kernel(e->P.model, EV_WET_RHS, UP_NONE, a, e->stream);
+		}
+		e->launches += 1;
 		solve(e, phase);
 		e->pending = false;
 	}
@@ -215,19 +279,27 @@ static void evaluate_end(rc_engine *e, const double *phi, int phase) {
 static void one_step(rc_engine *e) {
 	const int cur = e->phase;
 	cudaStream_t s = e->stream;
-	if(e->P.model == M_POLAR) launch_rng(e->cells, e->N, e->st, s);
+	if(e->P.model == M_POLAR) {
+		StageMark sm(e, RC_TIMER_RNG);
+		launch_rng(e->cells, e->N, e->st, s);
+		e->launches += 1;
+	}
 	CellArgs a = cell_args(e);
 	a.phi_eval = e->phiA;
 	a.phi_out = e->phiB;
 	a.pu = e->ph[cur];
-	if(e->pending) {
-		a.pe = e->ph[e->eval_phase];
-		launch_cell_kernel(e->P.model, EV_LOCAL, UP_PRED, a, s);
+	{
+		StageMark sm(e, RC_TIMER_UPDATE);
+		if(e->pending) {
+			a.pe = e->ph[e->eval_phase];
+			launch_cell_kernel(e->P.model, EV_LOCAL, UP_PRED, a, s);
+		}
+		else {
+			a.pe = e->ph[cur];
+			launch_cell_kernel(e->P.model, EV_NONE, UP_PRED, a, s);
+		}
 	}
-	else {
-		a.pe = e->ph[cur];
-		launch_cell_kernel(e->P.model, EV_NONE, UP_PRED, a, s);
-	}
+	e->launches += 1;
 	gather(e, e->phiB, cur);
 	cudaMemsetAsync(e->bin_count, 0, sizeof(int) * (size_t) e->nbx * e->nby, s);
 	CellArgs c = cell_args(e);
@@ -237,21 +309,34 @@ static void one_step(rc_engine *e) {
 	c.pu = e->ph[cur];
 	if(!wet_phase(e, cur)) {
 		c.phi_eval = e->phiB;
+		StageMark sm(e, RC_TIMER_UPDATE);
 		launch_cell_kernel(e->P.model, EV_LOCAL, UP_CORR, c, s);
+		e->launches += 1;
 	}
 	else {
 		CellArgs f = cell_args(e);
 		f.phi_eval = e->phiB;
 		f.pe = e->ph[cur];
 		f.pu = e->ph[cur];
-		launch_cell_kernel(e->P.model, EV_WET_RHS, UP_NONE, f, s);
+		{
+			StageMark sm(e, RC_TIMER_FORCES);
+			launch_cell_kernel(e->P.model, EV_WET_RHS, UP_NONE, f, s);
+		}
 		solve(e, cur);
 		c.phi_eval = e->phiB;
-		launch_cell_kernel(e->P.model, EV_NONE, UP_CORR, c, s);
+		{
+			StageMark sm(e, RC_TIMER_UPDATE);
+			launch_cell_kernel(e->P.model, EV_NONE, UP_CORR, c, s);
+		}
+		e->launches += 2;
 	}
 	CellArgs r = cell_args(e);
 	r.phi_out = e->phiA;
-	launch_repack(r, e->scratch_phi, e->scratch_rep, e->S_cap, s);
+	{
+		StageMark sm(e, RC_TIMER_REPACK);
+		launch_repack(r, e->scratch_phi, e->scratch_rep, e->S_cap, s);
+	}
+	e->launches += 5;
 	evaluate_end(e, e->phiA, cur);
 }
 
@@ -264,6 +349,7 @@ static void materialise(rc_engine *e, int accumulate) {
 	a.pu = e->ph[e->eval_phase];
 	a.accumulate_rep = accumulate;
 	launch_cell_kernel(e->P.model, EV_STORE, UP_NONE, a, e->stream);
+	e->launches += 1;
 	if(accumulate) e->pending = false;
 }
 
@@ -290,11 +376,19 @@ static int check_status(rc_engine *e, rc_step_stats *stats) {
 	e->S = h.S;
 	e->max_n_host = std::max(e->max_n_host, h.max_n);
 	if(stats) {
-		stats->cg_solves = h.cg_solves;
-		stats->cg_iterations = h.cg_iters;
-		stats->cg_max_iterations = h.cg_max_iters;
-		stats->cg_max_rel_residual = h.cg_max_rel;
-		stats->refinements = h.refinements;
+		stats->cg_solves += h.cg_solves;
+		stats->cg_iterations += h.cg_iters;
+		stats->cg_max_iterations = std::max(stats->cg_max_iterations, h.cg_max_iters);
+		stats->cg_max_rel_residual = std::max(stats->cg_max_rel_residual, h.cg_max_rel);
+		stats->refinements += h.refinements;
+		stats->resized_cells += h.resized_total;
+		stats->kernel_launches += e->launches;
+	}
+	e->launches = 0;
+	{
+		const size_t off = offsetof(DevStatus, cg_solves);
+		const size_t len = offsetof(DevStatus, overflow_used) - off;
+		CUDA_TRY(e, cudaMemsetAsync(reinterpret_cast<char *>(e->st) + off, 0, len, e->stream));
 	}
 	if(h.err) {
 		if(h.err & ERR_OVERLAP) return set_err(e, RC_ERR_OVERLAP, "Too many field patches overlap (box site %d)", h.err_where);
@@ -529,22 +623,10 @@ int rc_step(rc_engine *e, int n_steps, rc_step_stats *stats) {
 	if(n_steps < 0) return set_err(e, RC_ERR_INVALID, "n_steps < 0");
 	if(stats) memset(stats, 0, sizeof(*stats));
 	CUDA_TRY(e, cudaSetDevice(e->device));
-	// reset the per-call counters
-	{
-		DevStatus z;
-		memset(&z, 0, sizeof(z));
-		CUDA_TRY(e, cudaMemcpyAsync(e->st_host, e->st, sizeof(DevStatus), cudaMemcpyDeviceToHost, e->stream));
-		CUDA_TRY(e, cudaStreamSynchronize(e->stream));
-		DevStatus h = *e->st_host;
-		h.cg_solves = h.cg_iters = h.cg_max_iters = 0;
-		h.cg_max_rel = 0;
-		h.refinements = 0;
-		*e->st_host = h;
-		CUDA_TRY(e, cudaMemcpyAsync(e->st, e->st_host, sizeof(DevStatus), cudaMemcpyHostToDevice, e->stream));
-	}
+	int rc = check_status(e, nullptr);  // errors of earlier async work; resets the counters
+	if(rc) return rc;
 	const int chunk = 16;
 	int done = 0;
-	int rc = RC_OK;
 	while(done < n_steps) {
 		if((rc = choose_smem(e))) return rc;
 		const int m = std::min(chunk, n_steps - done);
@@ -555,6 +637,46 @@ int rc_step(rc_engine *e, int n_steps, rc_step_stats *stats) {
 	}
 	if(stats) stats->steps_done = done;
 	return rc;
+}
+
+int rc_step_async(rc_engine *e, int n_steps) {
+	if(!e) return RC_ERR_INVALID;
+	if(n_steps < 0) return set_err(e, RC_ERR_INVALID, "n_steps < 0");
+	CUDA_TRY(e, cudaSetDevice(e->device));
+	int rc = choose_smem(e);
+	if(rc) return rc;
+	for(int i = 0; i < n_steps; i++) one_step(e);
+	e->async_steps += n_steps;
+	return RC_OK;
+}
+
+int rc_wait(rc_engine *e, rc_step_stats *stats) {
+	if(!e) return RC_ERR_INVALID;
+	if(stats) memset(stats, 0, sizeof(*stats));
+	CUDA_TRY(e, cudaSetDevice(e->device));
+	const int rc = check_status(e, stats);
+	if(stats) stats->steps_done = e->async_steps;
+	e->async_steps = 0;
+	return rc;
+}
+
+int rc_download_phi(rc_engine *e, double *phi, long long n) {
+	if(!e || (!phi && n > 0)) return RC_ERR_INVALID;
+	if(n != e->S) return set_err(e, RC_ERR_INVALID, "rc_download_phi: n = %lld but the state has %lld sites", n, e->S);
+	CUDA_TRY(e, cudaSetDevice(e->device));
+	if(n) CUDA_TRY(e, cudaMemcpyAsync(phi, e->phiA, sizeof(double) * (size_t) n, cudaMemcpyDeviceToHost, e->stream));
+	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+	return RC_OK;
+}
+
+int rc_upload_phi(rc_engine *e, const double *phi, long long n) {
+	if(!e || (!phi && n > 0)) return RC_ERR_INVALID;
+	if(n != e->S) return set_err(e, RC_ERR_INVALID, "rc_upload_phi: n = %lld but the state has %lld sites", n, e->S);
+	CUDA_TRY(e, cudaSetDevice(e->device));
+	materialise(e, 1);
+	if(n) CUDA_TRY(e, cudaMemcpyAsync(e->phiA, phi, sizeof(double) * (size_t) n, cudaMemcpyHostToDevice, e->stream));
+	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+	return RC_OK;
 }
 
 int rc_set_phase(rc_engine *e, int active) {
@@ -678,6 +800,27 @@ int rc_upload(rc_engine *e, const rc_cell_host *cells, unsigned mask) {
 	return RC_OK;
 }
 
+int rc_set_timing(rc_engine *e, int enable) {
+	if(!e) return RC_ERR_INVALID;
+	e->timing = enable != 0;
+	return RC_OK;
+}
+
+int rc_timers(rc_engine *e, double *ms, long long *launches, int reset) {
+	if(!e) return RC_ERR_INVALID;
+	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+	collect_marks(e);
+	for(int i = 0; i < RC_NUM_TIMERS; i++) {
+		if(ms) ms[i] = e->timer_ms[i];
+		if(launches) launches[i] = e->timer_n[i];
+		if(reset) {
+			e->timer_ms[i] = 0;
+			e->timer_n[i] = 0;
+		}
+	}
+	return RC_OK;
+}
+
 int rc_set_stream(rc_engine *e, void *cuda_stream) {
 	if(!e) return RC_ERR_INVALID;
 	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
@@ -695,6 +838,8 @@ void rc_destroy(rc_engine *e) {
 	if(e->stream) cudaStreamSynchronize(e->stream);
 	for(void *p : e->allocs) cudaFree(p);
 	if(e->st_host) cudaFreeHost(e->st_host);
+	collect_marks(e);
+	for(cudaEvent_t v : e->event_pool) cudaEventDestroy(v);
 	if(e->own_stream) cudaStreamDestroy(e->own_stream);
 	delete e;
 }

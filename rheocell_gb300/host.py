@@ -195,7 +195,8 @@ def make_cells(m: Monolayer, keys: Dict[str, object], seed: int) -> Tuple[HostCe
         h.corner = c.corner
         h.type = int(m.types[i]) if i < len(m.types) else 0
         h.com_x, h.com_y = c.com
-        h.unrap_x, h.unrap_y = c.unrap
+        # SimBackend.cpp:276 passes the unwrapped corner through (int)
+        h.unrap_x, h.unrap_y = float(int(c.unrap[0])), float(int(c.unrap[1]))
         h.q00, h.q01 = c.q00, c.q01
         h.theta_q = 0.5 * math.atan2(2 * c.q01, 2 * c.q00)
         h.theta_q_old = h.theta_q

@@ -1,0 +1,431 @@
+// rheocell -- command-line driver of the GB300 engine, a drop-in for the
+// reference's `rheoCell input [key=value ...]` (src/rheoCell.cpp:13-49).
+//
+// It keeps the reference's input keys, topology and configuration formats and
+// run loop, and replaces the backend: FD_CUDABackend below plays the role of
+// the slot BackendFactory reserves for `backend = CUDA`
+// (src/Backends/BackendFactory.cpp:37-65) and calls the engine through its C
+// ABI (include/rheocell_gb300.h).  Host-side pieces mirrored here:
+//   input file ........ key = value lines, '#' comments, command-line
+//                       overrides (src/Utilities/parse_input/parse_input.cpp:117-160)
+//   run loop .......... SimManager::load_options / init / run
+//                       (src/Managers/SimManager.cpp:53-178)
+//   RNG seeding ....... srand48(seed) then the draws of read_topology and
+//                       MultiPhaseField::init (WetPolarModel.cpp:191,
+//                       Fields/MultiPhaseField.cpp:79-95), with the C library's drand48
+//   configuration ..... SimBackend::read_next_configuration (SimBackend.cpp:220-314)
+//                       and Configuration::headers/field (Observables/Configuration.cpp:36-56)
+//   output ............ trajectory (appended), last_conf (overwritten),
+//                       equilibrated_conf (ObservableOutput.cpp:86-190,
+//                       SimBackend.cpp:398-410)
+#include "../../include/rheocell_gb300.h"
+
+#include <cmath>
+#include <csignal>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <map>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace {
+
+const float PI_F = 3.141592653589793238462643f;
+volatile std::sig_atomic_t g_stop = 0;
+void on_signal(int) { g_stop = 1; }
+
+struct RCexception : std::runtime_error {
+	using std::runtime_error::runtime_error;
+};
+
+std::string trim(const std::string &s) {
+	size_t a = s.find_first_not_of(" \t\r\n"), b = s.find_last_not_of(" \t\r\n");
+	return a == std::string::npos ? std::string() : s.substr(a, b - a + 1);
+}
+
+// ---------------------------------------------------------------- input ---
+class InputFile {
+public:
+	void add_line(std::string line) {
+		size_t c = line.find('#');
+		if(c != std::string::npos) line.erase(c);
+		size_t eq = line.find('=');
+		if(eq == std::string::npos) return;
+		std::string k = trim(line.substr(0, eq)), v = trim(line.substr(eq + 1));
+		if(!k.empty()) keys_[k] = v;
+	}
+	void load(const std::string &path) {
+		std::ifstream f(path);
+		if(!f.good()) throw RCexception("Input file '" + path + "' not found");
+		std::string line;
+		while(std::getline(f, line)) add_line(line);
+	}
+	bool has(const std::string &k) const { return keys_.count(k) > 0; }
+	std::string str(const std::string &k, const std::string &def = "", bool required = false) const {
+		auto it = keys_.find(k);
+		if(it == keys_.end()) {
+			if(required) throw RCexception("Mandatory key `" + k + "' not found");
+			return def;
+		}
+		return it->second;
+	}
+	double num(const std::string &k, double def = 0, bool required = false) const {
+		return has(k) ? std::stod(str(k)) : (required ? (str(k, "", true), 0.0) : def);
+	}
+	long long integer(const std::string &k, long long def = 0, bool required = false) const {
+		return has(k) ? (long long) std::llround(std::stod(str(k))) : (required ? (str(k, "", true), 0LL) : def);
+	}
+	bool boolean(const std::string &k, bool def = false) const {
+		if(!has(k)) return def;
+		std::string v = str(k);
+		for(auto &ch : v) ch = (char) tolower(ch);
+		return v == "1" || v == "true" || v == "yes" || v == "yup" || v == "of course";
+	}
+
+private:
+	std::map<std::string, std::string> keys_;
+};
+
+// --------------------------------------------------------------- fields ---
+struct Field {  // host mirror of one patch (BaseField's public state)
+	rc_cell_host h;
+	std::vector<double> phi;
+	std::vector<int> map;
+};
+
+// ------------------------------------------------------------- backend ---
+class FD_CUDABackend {
+public:
+	~FD_CUDABackend() {
+		if(engine_) rc_destroy(engine_);
+	}
+
+	void get_settings(const InputFile &inp) {
+		std::string backend = inp.str("backend", "", true);
+		if(backend != "CUDA" && backend != "CPU")
+			throw RCexception("Backend '" + backend + "' not supported");
+		std::string sim_type = inp.str("sim_type", "FD_CPU");
+		if(sim_type != "FD_CPU") throw RCexception("sim_type '" + sim_type + "' is not provided by the GB300 engine");
+		std::string prec = inp.str("backend_precision", "double");
+		if(prec == "double") params_.precision = RC_PRECISION_DOUBLE;
+		else if(prec == "mixed") params_.precision = RC_PRECISION_MIXED;
+		else throw RCexception("Backend precision '" + prec + "' is not allowed");
+		if(inp.str("box", "square") != "square") throw RCexception("only the periodic square box is provided");
+		if(inp.integer("external_forces", 0) != 0) throw RCexception("external forces are not provided");
+		if(inp.has("wall_slip") && inp.num("wall_slip") <= 0) throw RCexception("wall stencils are not provided");
+		if(inp.boolean("anchoring")) throw RCexception("anchoring is not provided");
+
+		interaction_ = inp.str("interaction_type", "", true);
+		struct D {
+			double gamma, lambda, omega, mu, kappa;
+		} d;
+		if(interaction_ == "simplefield") {
+			params_.model = RC_SIMPLEFIELD;
+			d = {0.01, 2.5, 0.0, 3.0, 0.1};
+		}
+		else if(interaction_ == "activenematic") {
+			params_.model = RC_ACTIVENEMATIC;
+			d = {0.01, 2.5, 0.004, 3.0, 0.1};
+		}
+		else if(interaction_ == "wetpolarmodel") {
+			params_.model = RC_WETPOLARMODEL;
+			d = {0.06, 2.5, 0.004, 20.0, 0.1};
+		}
+		else if(interaction_ == "wetmodel") {
+			params_.model = RC_WETMODEL;
+			d = {0.01, 2.5, 0.004, 3.0, 0.1};
+		}
+		else throw RCexception("interaction_type '" + interaction_ + "' is not provided by the GB300 engine");
+		params_.R = (int) inp.integer("R", 8, true);
+		params_.border = 4;
+		params_.dt = inp.num("dt", 0, true);
+		params_.J0 = inp.num("J0", 1.0);
+		params_.gamma = inp.num("gamma", d.gamma);
+		params_.lambda = interaction_ == "simplefield" ? d.lambda : inp.num("lambda", d.lambda);
+		params_.omega = inp.num("omega", d.omega);
+		params_.mu = inp.num("mu", d.mu);
+		params_.kappa = inp.num("kappa", d.kappa);
+		const bool wet = params_.model == RC_WETMODEL || params_.model == RC_WETPOLARMODEL;
+		params_.passive_alpha = wet ? inp.num("passive_alpha", 1.0) : 1.0;
+		params_.cg_tolerance = wet ? inp.num("CGtolerance", 0.0001) : 0.0;
+		params_.cg_restart_every = params_.model == RC_WETPOLARMODEL ? 10 : 100;
+		auto both = [](double *a, double p, double q) {
+			a[0] = p;
+			a[1] = q;
+		};
+		if(params_.model == RC_SIMPLEFIELD) {
+			both(params_.friction, 1, 1);
+		}
+		else if(params_.model == RC_ACTIVENEMATIC) {
+			double fr = inp.num("friction", 2.0);
+			both(params_.friction, fr, fr);
+			both(params_.zetaQ_self, 0, inp.num("zetaQ_self", 0, true));
+			both(params_.zetaQ_inter, 0, inp.num("zetaQ_inter", 0, true));
+			both(params_.J_Q, 0, inp.num("J_Q", 0, true));
+		}
+		else {
+			both(params_.friction, 1.0, inp.num("friction", 0, true));
+			both(params_.friction_cell, 0.0, inp.num("friction_cell", 0, true));
+			both(params_.zetaQ_self, 0, inp.num("zetaQ_self", 0, true));
+			both(params_.zetaQ_inter, 0, inp.num("zetaQ_inter", 0, true));
+			both(params_.J_Q, 0, inp.num("J_Q", 0, true));
+			if(params_.model == RC_WETPOLARMODEL) both(params_.beta, 0, inp.num("beta", 0, true));
+		}
+		topology_ = inp.str("topology", "", true);
+		conf_file_ = inp.str("conf_file", "", true);
+		if(inp.integer("confs_to_skip", 0) != 0) throw RCexception("confs_to_skip is not provided");
+		restart_step_counter_ = inp.boolean("restart_step_counter", false);
+		device_ = (int) inp.integer("CUDA_device", 0);
+	}
+
+	// SimBackend::init + FD_CPUBackend::init
+	void init() {
+		read_topology();
+		read_configuration();
+		params_.rng_state = 0;
+		// drand48's state after the draws above, carried to the device stream
+		unsigned short probe[3];
+		unsigned short *cur = seed48(probe);  // returns the previous state, sets probe
+		memcpy(probe, cur, sizeof(probe));
+		seed48(probe);                        // restore it
+		params_.rng_state = (unsigned long long) probe[0] | ((unsigned long long) probe[1] << 16) |
+		                    ((unsigned long long) probe[2] << 32);
+		params_.rng_has_cached = 0;
+		params_.rng_cached = 0;
+		rc_box box = {L_, L_};
+		std::vector<rc_cell_host> hc;
+		for(auto &f : fields_) hc.push_back(f.h);
+		int rc = rc_create(&params_, &box, (int) hc.size(), hc.data(), device_, &engine_);
+		if(rc) throw RCexception(std::string("GB300 engine: ") + rc_last_error(engine_));
+	}
+
+	void sim_step() { check(rc_step(engine_, 1, &stats_)); }
+	void sim_steps(int n) { check(rc_step(engine_, n, &stats_)); }
+	void apply_simulation_changes_after_equilibration() { check(rc_set_phase(engine_, 1)); }
+
+	// device state -> host mirrors (SimBackend::apply_simulation_data_changes)
+	void apply_simulation_data_changes() {
+		std::vector<int> lx(fields_.size()), ly(fields_.size());
+		check(rc_get_sizes(engine_, nullptr, lx.data(), ly.data()));
+		std::vector<rc_cell_host> hc(fields_.size());
+		for(size_t i = 0; i < fields_.size(); i++) {
+			Field &f = fields_[i];
+			const size_t n = (size_t) lx[i] * ly[i];
+			f.phi.resize(n);
+			f.map.resize(n);
+			memset(&hc[i], 0, sizeof(rc_cell_host));
+			hc[i].capacity = (int) n;
+			hc[i].phi = f.phi.data();
+			hc[i].box_index = f.map.data();
+		}
+		check(rc_download(engine_, hc.data(), RC_FIELD_SCALARS | RC_FIELD_PHI | RC_FIELD_MAP));
+		for(size_t i = 0; i < fields_.size(); i++) {
+			hc[i].phi = fields_[i].phi.data();
+			hc[i].box_index = fields_[i].map.data();
+			fields_[i].h = hc[i];
+		}
+	}
+
+	std::string configuration(long long step) const {
+		std::stringstream conf;
+		conf.precision(15);
+		conf << "t = " << step << std::endl;
+		conf << "b = " << L_ << " " << L_ << std::endl;
+		for(size_t i = 0; i < fields_.size(); i++) {
+			const rc_cell_host &h = fields_[i].h;
+			if(i > 0) conf << std::endl;
+			conf << h.lsub_x << " " << h.lsub_y << " " << h.com_x << " " << h.com_y << " " << h.offset_x << " "
+			     << h.offset_y << " " << h.corner << " " << h.unrap_x << " " << h.unrap_y << " " << h.q00 << " "
+			     << h.q01 << " ";
+			for(size_t q = 0; q < fields_[i].phi.size(); q++) conf << fields_[i].map[q] << " " << fields_[i].phi[q] << " ";
+		}
+		conf << std::endl;
+		return conf.str();
+	}
+
+	long long start_step() const { return restart_step_counter_ ? 0 : conf_step_; }
+	const rc_step_stats &stats() const { return stats_; }
+
+private:
+	void check(int rc) {
+		if(rc) throw RCexception(std::string("GB300 engine: ") + rc_last_error(engine_));
+	}
+
+	void read_topology() {
+		std::ifstream t(topology_);
+		if(!t.good()) throw RCexception("Can't read topology file '" + topology_ + "'. Aborting");
+		int n = 0;
+		t >> n;
+		std::string rest;
+		std::getline(t, rest);
+		std::string line2;
+		std::getline(t, line2);
+		std::stringstream ss(line2);
+		types_.assign((size_t) n, 0);
+		for(int i = 0; i < n && (ss >> types_[(size_t) i]); i++) {
+		}
+		fields_.resize((size_t) n);
+		if(params_.model == RC_WETPOLARMODEL)
+			for(int i = 0; i < n; i++) (void) drand48();  // run_clock draw of read_topology
+	}
+
+	void read_configuration() {
+		std::ifstream c(conf_file_);
+		if(!c.good()) throw RCexception("Can't read configuration file '" + conf_file_ + "'");
+		std::string line;
+		std::getline(c, line);
+		if(sscanf(line.c_str(), "t = %lld", &conf_step_) != 1) throw RCexception("Malformed headers found in an input configuration");
+		std::getline(c, line);
+		double Lx = 0, Ly = 0;
+		if(sscanf(line.c_str(), "b = %lf %lf", &Lx, &Ly) != 2) throw RCexception("Malformed headers found in an input configuration");
+		if(Lx != Ly) throw RCexception("The box in the configuration file is not a square");
+		L_ = (int) Lx;
+		size_t i = 0;
+		while(i < fields_.size() && std::getline(c, line)) {
+			std::vector<double> v;
+			const char *p = line.c_str();
+			char *end = nullptr;
+			for(;;) {
+				double x = strtod(p, &end);
+				if(end == p) break;
+				v.push_back(x);
+				p = end;
+			}
+			if(v.size() < 11) continue;
+			Field &f = fields_[i];
+			rc_cell_host &h = f.h;
+			memset(&h, 0, sizeof(h));
+			// MultiPhaseField::init(Lx, Ly): one draw seeds the nematic director
+			double theta = (double) PI_F * (1 - 2 * drand48());
+			double q00 = cos(2 * theta), q01 = sin(2 * theta);
+			double mod = sqrt(q00 * q00 + q01 * q01);
+			double sgn = q01 > 0 ? 1 : (q01 < 0 ? -1 : 0);
+			h.nemq_x = h.nemq_old_x = sqrt((1 + q00 / mod) / 2);
+			h.nemq_y = h.nemq_old_y = sgn * sqrt((1 - q00 / mod) / 2);
+			h.lsub_x = (int) v[0];
+			h.lsub_y = (int) v[1];
+			h.com_x = v[2];
+			h.com_y = v[3];
+			h.offset_x = (int) v[4];
+			h.offset_y = (int) v[5];
+			h.corner = (int) v[6];
+			h.unrap_x = (int) v[7];
+			h.unrap_y = (int) v[8];
+			h.q00 = v[9];
+			h.q01 = v[10];
+			h.theta_q = h.theta_q_old = 0.5 * atan2(2 * h.q01, 2 * h.q00);
+			h.type = types_[i];
+			const size_t n = (size_t) h.lsub_x * h.lsub_y;
+			if(v.size() < 11 + 2 * n) throw RCexception("configuration line too short");
+			f.phi.resize(n);
+			f.map.resize(n);
+			for(size_t q = 0; q < n; q++) {
+				f.map[q] = (int) v[11 + 2 * q];
+				f.phi[q] = v[11 + 2 * q + 1];
+			}
+			h.capacity = (int) n;
+			h.phi = f.phi.data();
+			i++;
+		}
+		if(i != fields_.size())
+			throw RCexception("The number of lines found in configuration file doesn't match the parsed number of particles");
+	}
+
+	rc_params params_ = {};
+	rc_engine *engine_ = nullptr;
+	rc_step_stats stats_ = {};
+	std::string interaction_, topology_, conf_file_;
+	std::vector<int> types_;
+	std::vector<Field> fields_;
+	int L_ = 0;
+	long long conf_step_ = 0;
+	bool restart_step_counter_ = false;
+	int device_ = 0;
+};
+
+void write_file(const std::string &path, const std::string &text, bool append) {
+	std::ofstream f(path, append ? std::ios::app : std::ios::trunc);
+	if(!f.good()) throw RCexception("Stream " + path + " not writable");
+	f << text;
+}
+
+}  // namespace
+
+int main(int argc, char *argv[]) {
+	try {
+		if(argc < 2) throw RCexception(std::string("Usage is '") + argv[0] + " input_file'");
+		InputFile input;
+		input.load(argv[1]);
+		for(int i = 2; i < argc; i++) input.add_line(argv[i]);
+
+		// SimManager::load_options
+		const long long steps = input.integer("steps", 0, true);
+		const long long eq_steps = input.integer("equilibration_steps", 0);
+		if(!input.boolean("restart_step_counter") && eq_steps > 0)
+			throw RCexception("if equilibration_steps > 0, restart_step_counter must be set to true");
+		if(eq_steps < 0) throw RCexception("Equilibration steps can not be < 0. Aborting");
+		if(!input.has("seed")) throw RCexception("seed must be given (the GB300 driver does not draw one)");
+		const int seed = (int) input.integer("seed");
+		const std::string ts = input.str("time_scale", "", true);
+		if(ts != "linear") throw RCexception("Time scale '" + ts + "' not supported");
+		const long long interval = input.integer("print_conf_interval", 0, true);
+		const std::string traj = input.str("trajectory_file", "", true);
+		const std::string last_conf = input.str("lastconf_file", "last_conf.dat");
+		const std::string eq_conf = input.str("equilibratedconf_file", "equilibrated_conf.dat");
+
+		// SimManager::init
+		srand48(seed);
+		FD_CUDABackend backend;
+		backend.get_settings(input);
+		signal(SIGTERM, on_signal);
+		signal(SIGINT, on_signal);
+		signal(SIGUSR2, on_signal);
+		backend.init();
+		long long cur = backend.start_step();
+		long long next_print = cur + interval - (cur % interval);
+		write_file(traj, "", false);
+
+		// SimManager::run
+		for(long long s = 0; s < eq_steps && !g_stop; s++) backend.sim_step();
+		backend.apply_simulation_data_changes();
+		write_file(eq_conf, backend.configuration(cur), false);
+		backend.apply_simulation_changes_after_equilibration();
+		long long run = 0;
+		while(run < steps && !g_stop) {
+			if(cur == next_print) {
+				if(run > 0) {
+					backend.apply_simulation_data_changes();
+					const std::string c = backend.configuration(cur);
+					write_file(traj, c, true);
+					write_file(last_conf, c, false);
+				}
+				next_print += interval;
+			}
+			// advance to the next print point in one call
+			long long chunk = std::min(steps - run, next_print - cur);
+			if(chunk < 1) chunk = 1;
+			backend.sim_steps((int) chunk);
+			cur += chunk;
+			run += chunk;
+		}
+		if(cur == next_print && run > 0) {
+			backend.apply_simulation_data_changes();
+			const std::string c = backend.configuration(cur);
+			write_file(traj, c, true);
+			write_file(last_conf, c, false);
+		}
+		backend.apply_simulation_data_changes();
+		write_file(last_conf, backend.configuration(cur), false);
+		fprintf(stderr, "INFO: END OF THE SIMULATION, everything went OK! (%lld steps)\n", run);
+	}
+	catch(std::exception &e) {
+		fprintf(stderr, "ERROR: %s\n", e.what());
+		return 1;
+	}
+	return 0;
+}

@@ -103,6 +103,28 @@ def record_overlap():
     return info
 
 
+def record_cli():
+    """The reference's own executable (rheoCell input) on a small dry polar
+    case with equilibration and periodic printing: its output files are the
+    goldens of the stand-alone driver (rheocell_gb300/_build/rheocell)."""
+    m = g.make_monolayer(48, 9, seed=21, **SMALL)
+    d = tempfile.mkdtemp(prefix="rc_golden_")
+    try:
+        g.write_case(d, m, dict(DRY_POLAR_S, J_Q=0.2, zetaQ_inter=0.1), steps=20, seed=23, equilibration_steps=3,
+                     extra=dict(print_conf_interval=10))
+        res = subprocess.run([os.path.join(refdump.REF_DIR, "rheoCell_exact"), "input"], cwd=d,
+                             capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(res.stderr[-2000:])
+        out = {}
+        for f in ("input", "topology.top", "start_conf.dat", "trajectory.dat", "last_conf.dat",
+                  "equilibrated_conf.dat"):
+            out[f.replace(".", "_")] = np.array(open(os.path.join(d, f)).read())
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    np.savez_compressed(os.path.join(HERE, "cli_polar.npz"), **out)
+
+
 def main():
     if not refdump.have_reference("exact"):
         subprocess.check_call(["make", "-C", os.path.join(ROOT, "oracle"), "-j8"])
@@ -112,6 +134,8 @@ def main():
         print("%-12s steps %s  cells %d  sizes %s  %.0f KB" % (name, [r["step"] for r in recs], recs[0]["N"],
                                                                 sorted(set(zip(recs[-1]["lx"], recs[-1]["ly"]))), sz / 1024))
     print("overlap", record_overlap())
+    record_cli()
+    print("cli_polar %.0f KB" % (os.path.getsize(os.path.join(HERE, "cli_polar.npz")) / 1024))
 
 
 if __name__ == "__main__":
