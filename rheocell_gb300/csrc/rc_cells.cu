@@ -481,6 +481,21 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 		}
 	}
 
+	// Sums whose terms cancel and whose direction drives the dynamics -- the
+	// shape tensor of the nematic models (director alignment) and the polar
+	// repulsion-force totals (torque when J_Q != 0) -- are formed sequentially
+	// in storage order, as the reference's loops form them; a tree order
+	// changes them by more than the 1e-10 parity bar.  Well-conditioned sums
+	// (area, sums of phi, centre-of-mass sums) use the block tree.
+	const bool seq_shape = (MODEL == M_NEMATIC || MODEL == M_WET) && UPD != UP_NONE;
+	const bool seq_rep = (MODEL == M_POLAR) && (EVAL != EV_NONE) && a.rep_on;
+	if(seq_shape && EVAL == EV_NONE) {
+		// gradients of the last evaluation into shared memory (sphi / smu are free here)
+		for(int q = threadIdx.x; q < n; q += blockDim.x) {
+			sphi[q] = a.dxg[start + q];
+			smu[q] = a.dyg[start + q];
+		}
+	}
 	if(UPD != UP_NONE) {
 		block_sum<12>(acc, red);
 		if(UPD == UP_CORR) block_min<2>(imin, ired);
@@ -492,6 +507,49 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 		acc[9] = v4[1];
 		acc[10] = v4[2];
 		acc[11] = v4[3];
+	}
+	if(seq_shape || seq_rep) {
+		__shared__ double s_seq[4];
+		if(threadIdx.x < 4) {
+			const int which = threadIdx.x;
+			double sum = 0.0;
+			if(seq_shape && which < 2) {
+				for(int q = 0; q < n; q++) {
+					double dx, dy;
+					if(EVAL != EV_NONE) {
+						const int y = q / lx, x = q - y * lx;
+						const Nb nb = patch_nb(q, x, y, lx, ly);
+						dx = .5 * (sphi[nb.r] - sphi[nb.l]);
+						dy = .5 * (sphi[nb.u] - sphi[nb.d]);
+					}
+					else {
+						dx = sphi[q];
+						dy = smu[q];
+					}
+					sum += (which == 0) ? -0.5 * (dx * dx - dy * dy) : -dx * dy;
+				}
+			}
+			else if(seq_rep && which >= 2) {
+				for(int q = 0; q < n; q++) {
+					const int y = q / lx, x = q - y * lx;
+					const Nb nb = patch_nb(q, x, y, lx, ly);
+					sum += (which == 2) ? (-1) * 0.5 * (saux[nb.r] - saux[nb.l]) * sphi[q]
+					                    : (-1) * 0.5 * (saux[nb.u] - saux[nb.d]) * sphi[q];
+				}
+			}
+			s_seq[which] = sum;
+		}
+		__syncthreads();
+		if(threadIdx.x == 0) {
+			if(seq_shape) {
+				acc[6] = s_seq[0];
+				acc[7] = s_seq[1];
+			}
+			if(seq_rep) {
+				acc[8] = s_seq[2];
+				acc[9] = s_seq[3];
+			}
+		}
 	}
 
 	if(threadIdx.x == 0) {

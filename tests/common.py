@@ -89,8 +89,9 @@ CELL_KEYS = {"lx": "lsub_x", "ly": "lsub_y", "offx": "offset_x", "offy": "offset
 INT_KEYS = ("lx", "ly", "offx", "offy", "corner")
 
 
-def compare_to_golden(gd, states: Dict[int, Dict[str, np.ndarray]], skip=(), site_tol=0.0, cell_tol=0.0):
-    """Max relative error of each compared quantity (0.0 means bit-identical)."""
+def compare_to_golden(gd, states: Dict[int, Dict[str, np.ndarray]], skip=(), absolute=()):
+    """Max relative error of each compared quantity (0.0 means bit-identical);
+    keys in `absolute` report the max absolute error instead."""
     errs = {}
     steps = [int(s) for s in gd["steps"]]
     for s in steps:
@@ -103,6 +104,8 @@ def compare_to_golden(gd, states: Dict[int, Dict[str, np.ndarray]], skip=(), sit
                 continue
             if k in INT_KEYS:
                 errs[(s, k)] = 0.0 if np.array_equal(gd[key], st[sk]) else float("inf")
+            elif k in absolute:
+                errs[(s, k)] = float(np.max(np.abs(np.asarray(st[sk], float) - gd[key]))) if len(gd[key]) else 0.0
             else:
                 errs[(s, k)] = rel_err(st[sk], gd[key])
         if "s%d_phi" % s in gd:
