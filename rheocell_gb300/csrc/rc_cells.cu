@@ -240,9 +240,12 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 		}
 		return;
 	}
+	// shared layout: phi | mu | aux (Repulsion or f_d) | ext (second chain of
+	// the sequential polar totals); cell_smem_bytes sizes it per model
 	double *sphi = smem;
 	double *smu = smem + a.smem_n;
 	double *saux = smem + 2 * a.smem_n;
+	double *sext = smem + 3 * a.smem_n;
 	const DevParams &P = a.P;
 	const PhaseParams &pe = a.pe;
 	const double gamma = P.gamma, lambda = P.lambda, mu_c = P.mu, kappa = P.kappa, omega = P.omega, a0 = P.a0;
@@ -487,13 +490,41 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 	// in storage order, as the reference's loops form them; a tree order
 	// changes them by more than the 1e-10 parity bar.  Well-conditioned sums
 	// (area, sums of phi, centre-of-mass sums) use the block tree.
-	const bool seq_shape = (MODEL == M_NEMATIC || MODEL == M_WET) && UPD != UP_NONE;
+	// (Only needed when J_Q != 0: otherwise neither sum affects the dynamics.)
+	// On GB300 an FP64 warp instruction occupies the FP64 pipe for tens of
+	// cycles, so all threads first form the terms into shared memory, and one
+	// warp instruction per term then carries both dependent add chains.
+	const bool seq_shape = (MODEL == M_NEMATIC || MODEL == M_WET) && UPD != UP_NONE && pu.JQ != 0.0;
 	const bool seq_rep = (MODEL == M_POLAR) && (EVAL != EV_NONE) && a.rep_on;
-	if(seq_shape && EVAL == EV_NONE) {
-		// gradients of the last evaluation into shared memory (sphi / smu are free here)
+	double *chain0 = saux, *chain1 = smu;  // terms of the two chains (free after stage 2)
+	if(seq_shape || seq_rep) __syncthreads();
+	if(seq_shape) {
 		for(int q = threadIdx.x; q < n; q += blockDim.x) {
-			sphi[q] = a.dxg[start + q];
-			smu[q] = a.dyg[start + q];
+			double dx, dy;
+			if(EVAL != EV_NONE) {
+				const int y = q / lx, x = q - y * lx;
+				const Nb nb = patch_nb(q, x, y, lx, ly);
+				dx = .5 * (sphi[nb.r] - sphi[nb.l]);
+				dy = .5 * (sphi[nb.u] - sphi[nb.d]);
+			}
+			else {
+				dx = a.dxg[start + q];
+				dy = a.dyg[start + q];
+			}
+			chain0[q] = -0.5 * (dx * dx - dy * dy);
+			chain1[q] = -dx * dy;
+		}
+	}
+	if(seq_rep) {
+		// saux holds the Repulsion accumulator (read at neighbours): terms go to
+		// smu and the fourth array
+		chain0 = smu;
+		chain1 = sext;
+		for(int q = threadIdx.x; q < n; q += blockDim.x) {
+			const int y = q / lx, x = q - y * lx;
+			const Nb nb = patch_nb(q, x, y, lx, ly);
+			chain0[q] = (-1) * 0.5 * (saux[nb.r] - saux[nb.l]) * sphi[q];
+			chain1[q] = (-1) * 0.5 * (saux[nb.u] - saux[nb.d]) * sphi[q];
 		}
 	}
 	if(UPD != UP_NONE) {
@@ -509,35 +540,13 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 		acc[11] = v4[3];
 	}
 	if(seq_shape || seq_rep) {
-		__shared__ double s_seq[4];
-		if(threadIdx.x < 4) {
-			const int which = threadIdx.x;
+		__shared__ double s_seq[2];
+		__syncthreads();
+		if(threadIdx.x < 2) {
+			const double *terms = (threadIdx.x == 0) ? chain0 : chain1;
 			double sum = 0.0;
-			if(seq_shape && which < 2) {
-				for(int q = 0; q < n; q++) {
-					double dx, dy;
-					if(EVAL != EV_NONE) {
-						const int y = q / lx, x = q - y * lx;
-						const Nb nb = patch_nb(q, x, y, lx, ly);
-						dx = .5 * (sphi[nb.r] - sphi[nb.l]);
-						dy = .5 * (sphi[nb.u] - sphi[nb.d]);
-					}
-					else {
-						dx = sphi[q];
-						dy = smu[q];
-					}
-					sum += (which == 0) ? -0.5 * (dx * dx - dy * dy) : -dx * dy;
-				}
-			}
-			else if(seq_rep && which >= 2) {
-				for(int q = 0; q < n; q++) {
-					const int y = q / lx, x = q - y * lx;
-					const Nb nb = patch_nb(q, x, y, lx, ly);
-					sum += (which == 2) ? (-1) * 0.5 * (saux[nb.r] - saux[nb.l]) * sphi[q]
-					                    : (-1) * 0.5 * (saux[nb.u] - saux[nb.d]) * sphi[q];
-				}
-			}
-			s_seq[which] = sum;
+			for(int q = 0; q < n; q++) sum += terms[q];
+			s_seq[threadIdx.x] = sum;
 		}
 		__syncthreads();
 		if(threadIdx.x == 0) {
@@ -545,9 +554,9 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 				acc[6] = s_seq[0];
 				acc[7] = s_seq[1];
 			}
-			if(seq_rep) {
-				acc[8] = s_seq[2];
-				acc[9] = s_seq[3];
+			else {
+				acc[8] = s_seq[0];
+				acc[9] = s_seq[1];
 			}
 		}
 	}
@@ -602,20 +611,39 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 	}
 }
 
+int cell_smem_arrays(int model) {
+	switch(model) {
+		case M_SIMPLE: return 2;
+		case M_NEMATIC: return 3;  // phi, mu, and the shape-tensor chain
+		case M_POLAR: return 4;    // phi, mu, Repulsion, and the second torque chain
+		default: return 3;         // phi, mu, f_d
+	}
+}
+
 size_t cell_smem_bytes(int model, int smem_n) {
-	const int arrays = (model == M_POLAR || model == M_WET) ? 3 : 2;
-	return sizeof(double) * (size_t) arrays * (size_t) smem_n;
+	return sizeof(double) * (size_t) cell_smem_arrays(model) * (size_t) smem_n;
 }
 
 template<int MODEL, int EVAL, int UPD>
 static void launch_t(const CellArgs &a, cudaStream_t s) {
 	const size_t smem = cell_smem_bytes(MODEL, a.smem_n);
-	static bool configured = false;
-	if(!configured) {
-		cudaFuncSetAttribute(cell_kernel<MODEL, EVAL, UPD>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-		configured = true;
-	}
 	cell_kernel<MODEL, EVAL, UPD><<<a.N, CELL_THREADS, smem, s>>>(a);
+}
+
+template<int MODEL>
+static cudaError_t configure_m() {
+	cudaError_t e = cudaSuccess, c;
+#define RC_CFG(EV, UP)                                                                                             \
+	c = cudaFuncSetAttribute(cell_kernel<MODEL, EV, UP>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024); \
+	if(c != cudaSuccess) e = c;
+	RC_CFG(EV_STORE, UP_NONE)
+	RC_CFG(EV_WET_RHS, UP_NONE)
+	RC_CFG(EV_LOCAL, UP_PRED)
+	RC_CFG(EV_LOCAL, UP_CORR)
+	RC_CFG(EV_NONE, UP_PRED)
+	RC_CFG(EV_NONE, UP_CORR)
+#undef RC_CFG
+	return e;
 }
 
 template<int MODEL>
@@ -725,21 +753,28 @@ __global__ void __launch_bounds__(CELL_THREADS) rng_kernel(CellDev *cells, int N
 }
 
 void launch_rng(CellDev *cells, int N, DevStatus *st, cudaStream_t s) {
-	static bool init = false;
-	if(!init) {
-		unsigned long long A[2 * CELL_THREADS + 1], Cc[2 * CELL_THREADS + 1];
-		const unsigned long long a = 0x5DEECE66DULL, c = 0xBULL, M = (1ULL << 48) - 1;
-		A[0] = 1;
-		Cc[0] = 0;
-		for(int k = 1; k <= 2 * CELL_THREADS; k++) {
-			A[k] = (A[k - 1] * a) & M;
-			Cc[k] = (Cc[k - 1] * a + c) & M;
-		}
-		cudaMemcpyToSymbol(c_jumpA, A, sizeof(A));
-		cudaMemcpyToSymbol(c_jumpC, Cc, sizeof(Cc));
-		init = true;
-	}
 	rng_kernel<<<1, CELL_THREADS, 0, s>>>(cells, N, st);
+}
+
+// One-time, per-device set-up that must not happen inside stream capture:
+// shared-memory limits of the cell kernels and the LCG jump-ahead table.
+cudaError_t configure_kernels() {
+	cudaError_t e = cudaSuccess, c;
+	if((c = configure_m<M_SIMPLE>()) != cudaSuccess) e = c;
+	if((c = configure_m<M_NEMATIC>()) != cudaSuccess) e = c;
+	if((c = configure_m<M_POLAR>()) != cudaSuccess) e = c;
+	if((c = configure_m<M_WET>()) != cudaSuccess) e = c;
+	unsigned long long A[2 * CELL_THREADS + 1], Cc[2 * CELL_THREADS + 1];
+	const unsigned long long a = 0x5DEECE66DULL, cc = 0xBULL, M = (1ULL << 48) - 1;
+	A[0] = 1;
+	Cc[0] = 0;
+	for(int k = 1; k <= 2 * CELL_THREADS; k++) {
+		A[k] = (A[k - 1] * a) & M;
+		Cc[k] = (Cc[k - 1] * a + cc) & M;
+	}
+	if((c = cudaMemcpyToSymbol(c_jumpA, A, sizeof(A))) != cudaSuccess) e = c;
+	if((c = cudaMemcpyToSymbol(c_jumpC, Cc, sizeof(Cc))) != cudaSuccess) e = c;
+	return e;
 }
 
 // ----------------------------------------------------------------- bins ---

@@ -103,39 +103,35 @@ __device__ __forceinline__ int box_deg(const int *cnt, int k, int L) {
 	return cnt[kd] + cnt[kl] + cnt[kr] + cnt[ku];
 }
 
-__device__ __forceinline__ double box_n4(const double *P, int k, int L) {
+template<typename T>
+__device__ __forceinline__ double box_n4(const T *P, int k, int L) {
 	const int x = k % L, y = k / L;
 	const int kr = (x == L - 1) ? k - (L - 1) : k + 1;
 	const int kl = (x == 0) ? k + (L - 1) : k - 1;
 	const int ku = (y == L - 1) ? k - (L - 1) * L : k + L;
 	const int kd = (y == 0) ? k + (L - 1) * L : k - L;
-	return P[kd] + P[kl] + P[kr] + P[ku];
+	return (double) P[kd] + (double) P[kl] + (double) P[kr] + (double) P[ku];
 }
 
-__global__ void __launch_bounds__(CG_THREADS) cg_kernel(const CGArgs a) {
-	__shared__ double T[CG_MAX_D + 1], iT[CG_MAX_D + 1];
-	__shared__ double red[8 * (CG_THREADS / 32)];
-	__shared__ double tot[8];
-	__shared__ double s_rz[2], s_thr[2], s_bn2[2], s_rn2[2], s_alpha[2], s_beta[2];
-	__shared__ int s_act[2], s_it[2], s_first, s_zero[2];
-	if(threadIdx.x < 2) s_beta[threadIdx.x] = 0.0;
+struct CGShared {
+	double T[CG_MAX_D + 1], iT[CG_MAX_D + 1];
+	double red[8 * (CG_THREADS / 32)];
+	double tot[8];
+	double rz[2], thr[2], bn2[2], rn2[2], alpha[2], beta[2];
+	int act[2], it[2], first, zero[2];
+};
+
+// r = b - A x for both components (x = 0 when `x_zero`), written in FP64 and,
+// for the mixed path, also rounded to FP32.  Reduces |b|^2, |r|^2 and r.M^-1 r
+// (the latter on the stored precision of r) into sh.tot[0..5].
+__device__ bool true_residual(const CGArgs &a, CGShared &sh, bool x_zero, bool to_float) {
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
 	const long long S = a.st->S;
-	const int cold = a.st->cg_cold;
-	const double eta = a.eta;
-	const double neta = -eta * 1.0;
+	const double neta = -a.eta * 1.0;
 	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
 	const long long gstride = (long long) gridDim.x * blockDim.x;
-	if(threadIdx.x == 0) {
-		T[0] = a.xi;
-		for(int d = 1; d <= CG_MAX_D; d++) T[d] = T[d - 1] + eta * 1.0;
-		for(int d = 0; d <= CG_MAX_D; d++) iT[d] = T[d] != 0.0 ? 1.0 / T[d] : 1.0;
-	}
-	__syncthreads();
-
-	// r = b - A x
-	if(!cold) {
+	if(!x_zero) {
 		for(long long k = gtid; k < L2; k += gstride) {
 			const int n = a.cnt[k];
 			double sx = 0.0, sy = 0.0;
@@ -147,174 +143,283 @@ __global__ void __launch_bounds__(CG_THREADS) cg_kernel(const CGArgs a) {
 			a.Px[k] = sx;
 			a.Py[k] = sy;
 		}
-		if(!grid_reduce(a, 0, nullptr, tot, red)) return;
+		if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
 	}
-	{
-		double v[6] = {0, 0, 0, 0, 0, 0};
-		for(long long j = gtid; j < S; j += gstride) {
-			const int k = a.mapg[j];
-			const int D = box_deg(a.cnt, k, L);
-			const double bx = a.fx[j], by = a.fy[j];
-			double rx, ry;
-			if(cold) {
-				a.vx[j] = 0.0;
-				a.vy[j] = 0.0;
-				rx = bx - 0.0;
-				ry = by - 0.0;
-			}
-			else {
-				const double ax = T[D] * a.vx[j] + neta * box_n4(a.Px, k, L);
-				const double ay = T[D] * a.vy[j] + neta * box_n4(a.Py, k, L);
-				rx = bx - ax;
-				ry = by - ay;
-			}
-			a.rx[j] = rx;
-			a.ry[j] = ry;
-			v[0] += bx * bx;
-			v[1] += by * by;
-			v[2] += rx * rx;
-			v[3] += ry * ry;
-			v[4] += rx * (iT[D] * rx);
-			v[5] += ry * (iT[D] * ry);
+	double v[6] = {0, 0, 0, 0, 0, 0};
+	for(long long j = gtid; j < S; j += gstride) {
+		const int k = a.mapg[j];
+		const int D = box_deg(a.cnt, k, L);
+		const double bx = a.fx[j], by = a.fy[j];
+		double rx, ry;
+		if(x_zero) {
+			rx = bx - 0.0;
+			ry = by - 0.0;
 		}
-		block_sum<6>(v, red);
-		if(!grid_reduce(a, 6, v, tot, red)) return;
-	}
-	if(threadIdx.x == 0) {
-		for(int c = 0; c < 2; c++) {
-			s_bn2[c] = tot[c];
-			s_rn2[c] = tot[2 + c];
-			s_rz[c] = tot[4 + c];
-			s_it[c] = 0;
-			s_zero[c] = 0;
-			s_thr[c] = fmax(a.tol * a.tol * s_bn2[c], DBL_MIN);
-			if(s_bn2[c] == 0.0) {
-				s_act[c] = 0;
-				s_zero[c] = 1;
-			}
-			else s_act[c] = (s_rn2[c] < s_thr[c]) ? 0 : 1;
+		else {
+			const double ax = sh.T[D] * a.vx[j] + neta * box_n4(a.Px, k, L);
+			const double ay = sh.T[D] * a.vy[j] + neta * box_n4(a.Py, k, L);
+			rx = bx - ax;
+			ry = by - ay;
 		}
-		s_first = 1;
-	}
-	__syncthreads();
-	if(s_zero[0] || s_zero[1]) {
-		for(long long j = gtid; j < S; j += gstride) {
-			if(s_zero[0]) a.vx[j] = 0.0;
-			if(s_zero[1]) a.vy[j] = 0.0;
+		a.rx[j] = rx;
+		a.ry[j] = ry;
+		v[0] += bx * bx;
+		v[1] += by * by;
+		v[2] += rx * rx;
+		v[3] += ry * ry;
+		if(to_float) {
+			const float fx = (float) rx, fy = (float) ry;
+			a.rxf[j] = fx;
+			a.ryf[j] = fy;
+			a.exf[j] = 0.0f;
+			a.eyf[j] = 0.0f;
+			v[4] += (double) fx * (sh.iT[D] * (double) fx);
+			v[5] += (double) fy * (sh.iT[D] * (double) fy);
+		}
+		else {
+			v[4] += rx * (sh.iT[D] * rx);
+			v[5] += ry * (sh.iT[D] * ry);
 		}
 	}
+	block_sum<6>(v, sh.red);
+	return grid_reduce(a, 6, v, sh.tot, sh.red);
+}
 
-	const long long max_it = 2 * S;
-	while(s_act[0] || s_act[1]) {
-		const int ax = s_act[0], ay = s_act[1], first = s_first;
-		const double bx = s_beta[0], by = s_beta[1];
-		// Phase A: p = z + beta p (p = z on the first sweep), P = S p
+// Jacobi-preconditioned CG iterations from the state in sh (act, rz, thr) and
+// the residual in (rx, ry): Eigen's loop.  T is the storage type of r, p and
+// the box sums, U that of the solution accumulator; dot products are FP64.
+template<typename T, typename U>
+__device__ bool cg_iterate(const CGArgs &a, CGShared &sh, T *rx, T *ry, T *px, T *py, T *Pbx, T *Pby, U *ux, U *uy,
+                           long long max_it) {
+	const int L = a.L;
+	const long long L2 = (long long) L * L;
+	const long long S = a.st->S;
+	const double neta = -a.eta * 1.0;
+	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+	const long long gstride = (long long) gridDim.x * blockDim.x;
+	if(threadIdx.x == 0) sh.first = 1;
+	__syncthreads();
+	while(sh.act[0] || sh.act[1]) {
+		const int ax = sh.act[0], ay = sh.act[1], first = sh.first;
+		const double bx = sh.beta[0], by = sh.beta[1];
+		// Phase A: p = z + beta p (p = z on the first sweep), box sums P = S p
 		for(long long k = gtid; k < L2; k += gstride) {
 			const int n = a.cnt[k];
 			if(n == 0) {
-				if(ax) a.Px[k] = 0.0;
-				if(ay) a.Py[k] = 0.0;
+				if(ax) Pbx[k] = (T) 0;
+				if(ay) Pby[k] = (T) 0;
 				continue;
 			}
-			const double id = iT[box_deg(a.cnt, k, L)];
+			const double id = sh.iT[box_deg(a.cnt, k, L)];
 			double sx = 0.0, sy = 0.0;
 			for(int i = 0; i < n; i++) {
 				const int j = a.cover[(size_t) i * L2 + k];
 				if(ax) {
-					const double z = id * a.rx[j];
-					const double p = first ? z : z + bx * a.px[j];
-					a.px[j] = p;
-					sx += p;
+					const double z = id * (double) rx[j];
+					const T p = (T) (first ? z : z + bx * (double) px[j]);
+					px[j] = p;
+					sx += (double) p;
 				}
 				if(ay) {
-					const double z = id * a.ry[j];
-					const double p = first ? z : z + by * a.py[j];
-					a.py[j] = p;
-					sy += p;
+					const double z = id * (double) ry[j];
+					const T p = (T) (first ? z : z + by * (double) py[j]);
+					py[j] = p;
+					sy += (double) p;
 				}
 			}
-			if(ax) a.Px[k] = sx;
-			if(ay) a.Py[k] = sy;
+			if(ax) Pbx[k] = (T) sx;
+			if(ay) Pby[k] = (T) sy;
 		}
-		if(!grid_reduce(a, 0, nullptr, tot, red)) return;
+		if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
 		// Phase B: p.Ap
 		{
 			double v[2] = {0, 0};
 			for(long long j = gtid; j < S; j += gstride) {
 				const int k = a.mapg[j];
-				const double d = T[box_deg(a.cnt, k, L)];
+				const double d = sh.T[box_deg(a.cnt, k, L)];
 				if(ax) {
-					const double p = a.px[j];
-					v[0] += p * (d * p + neta * box_n4(a.Px, k, L));
+					const double p = (double) px[j];
+					v[0] += p * (d * p + neta * (double) box_n4(Pbx, k, L));
 				}
 				if(ay) {
-					const double p = a.py[j];
-					v[1] += p * (d * p + neta * box_n4(a.Py, k, L));
+					const double p = (double) py[j];
+					v[1] += p * (d * p + neta * (double) box_n4(Pby, k, L));
 				}
 			}
-			block_sum<2>(v, red);
-			if(!grid_reduce(a, 2, v, tot, red)) return;
+			block_sum<2>(v, sh.red);
+			if(!grid_reduce(a, 2, v, sh.tot, sh.red)) return false;
 		}
 		if(threadIdx.x == 0) {
-			if(ax) s_alpha[0] = s_rz[0] / tot[0];
-			if(ay) s_alpha[1] = s_rz[1] / tot[1];
+			if(ax) sh.alpha[0] = sh.rz[0] / sh.tot[0];
+			if(ay) sh.alpha[1] = sh.rz[1] / sh.tot[1];
 		}
 		__syncthreads();
-		// Phase C: x += alpha p; r -= alpha Ap; |r|^2 and r.z
+		// Phase C: u += alpha p; r -= alpha Ap; |r|^2 and r.z
 		{
-			const double alx = s_alpha[0], aly = s_alpha[1];
+			const double alx = sh.alpha[0], aly = sh.alpha[1];
 			double v[4] = {0, 0, 0, 0};
 			for(long long j = gtid; j < S; j += gstride) {
 				const int k = a.mapg[j];
 				const int D = box_deg(a.cnt, k, L);
-				const double d = T[D], id = iT[D];
+				const double d = sh.T[D], id = sh.iT[D];
 				if(ax) {
-					const double p = a.px[j];
-					const double ap = d * p + neta * box_n4(a.Px, k, L);
-					a.vx[j] = a.vx[j] + alx * p;
-					const double r = a.rx[j] - alx * ap;
-					a.rx[j] = r;
-					v[0] += r * r;
-					v[2] += r * (id * r);
+					const double p = (double) px[j];
+					const double ap = d * p + neta * (double) box_n4(Pbx, k, L);
+					ux[j] = (U) ((double) ux[j] + alx * p);
+					const T r = (T) ((double) rx[j] - alx * ap);
+					rx[j] = r;
+					const double rd = (double) r;
+					v[0] += rd * rd;
+					v[2] += rd * (id * rd);
 				}
 				if(ay) {
-					const double p = a.py[j];
-					const double ap = d * p + neta * box_n4(a.Py, k, L);
-					a.vy[j] = a.vy[j] + aly * p;
-					const double r = a.ry[j] - aly * ap;
-					a.ry[j] = r;
-					v[1] += r * r;
-					v[3] += r * (id * r);
+					const double p = (double) py[j];
+					const double ap = d * p + neta * (double) box_n4(Pby, k, L);
+					uy[j] = (U) ((double) uy[j] + aly * p);
+					const T r = (T) ((double) ry[j] - aly * ap);
+					ry[j] = r;
+					const double rd = (double) r;
+					v[1] += rd * rd;
+					v[3] += rd * (id * rd);
 				}
 			}
-			block_sum<4>(v, red);
-			if(!grid_reduce(a, 4, v, tot, red)) return;
+			block_sum<4>(v, sh.red);
+			if(!grid_reduce(a, 4, v, sh.tot, sh.red)) return false;
 		}
 		if(threadIdx.x == 0) {
 			for(int c = 0; c < 2; c++) {
-				if(!s_act[c]) continue;
-				s_rn2[c] = tot[c];
-				if(s_rn2[c] < s_thr[c]) {
-					s_act[c] = 0;
+				if(!sh.act[c]) continue;
+				sh.rn2[c] = sh.tot[c];
+				if(sh.rn2[c] < sh.thr[c]) {
+					sh.act[c] = 0;
 					continue;
 				}
-				const double rz_new = tot[2 + c];
-				s_beta[c] = rz_new / s_rz[c];
-				s_rz[c] = rz_new;
-				s_it[c]++;
-				if(s_it[c] >= max_it) s_act[c] = 0;
+				const double rz_new = sh.tot[2 + c];
+				sh.beta[c] = rz_new / sh.rz[c];
+				sh.rz[c] = rz_new;
+				sh.it[c]++;
+				if(sh.it[c] >= max_it) sh.act[c] = 0;
 			}
-			s_first = 0;
+			sh.first = 0;
 		}
 		__syncthreads();
+	}
+	return true;
+}
+
+__global__ void __launch_bounds__(CG_THREADS) cg_kernel(const CGArgs a) {
+	__shared__ CGShared sh;
+	const long long S = a.st->S;
+	const int cold = a.st->cg_cold;
+	const double eta = a.eta;
+	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+	const long long gstride = (long long) gridDim.x * blockDim.x;
+	if(threadIdx.x == 0) {
+		sh.T[0] = a.xi;
+		for(int d = 1; d <= CG_MAX_D; d++) sh.T[d] = sh.T[d - 1] + eta * 1.0;
+		for(int d = 0; d <= CG_MAX_D; d++) sh.iT[d] = sh.T[d] != 0.0 ? 1.0 / sh.T[d] : 1.0;
+		sh.beta[0] = sh.beta[1] = 0.0;
+	}
+	__syncthreads();
+	if(cold) {
+		for(long long j = gtid; j < S; j += gstride) {
+			a.vx[j] = 0.0;
+			a.vy[j] = 0.0;
+		}
+	}
+	const bool mixed = a.mixed != 0;
+	if(!true_residual(a, sh, cold != 0, mixed)) return;
+	if(threadIdx.x == 0) {
+		for(int c = 0; c < 2; c++) {
+			sh.bn2[c] = sh.tot[c];
+			sh.rn2[c] = sh.tot[2 + c];
+			sh.rz[c] = sh.tot[4 + c];
+			sh.it[c] = 0;
+			sh.zero[c] = 0;
+			sh.thr[c] = fmax(a.tol * a.tol * sh.bn2[c], DBL_MIN);
+			if(sh.bn2[c] == 0.0) {
+				sh.act[c] = 0;
+				sh.zero[c] = 1;
+			}
+			else sh.act[c] = (sh.rn2[c] < sh.thr[c]) ? 0 : 1;
+		}
+	}
+	__syncthreads();
+	if(sh.zero[0] || sh.zero[1]) {
+		for(long long j = gtid; j < S; j += gstride) {
+			if(sh.zero[0]) a.vx[j] = 0.0;
+			if(sh.zero[1]) a.vy[j] = 0.0;
+		}
+	}
+	const long long max_it = 2 * S;
+	int refinements = 0;
+	if(!mixed) {
+		if(!cg_iterate<double, double>(a, sh, a.rx, a.ry, a.px, a.py, a.Px, a.Py, a.vx, a.vy, max_it)) return;
+	}
+	else {
+		// Iterative refinement: FP32 Jacobi-PCG for the correction A e = r,
+		// stopped at inner_tol * |r|, then x += e and r = b - A x in FP64.
+		// A sweep that fails to reduce |r| by 2x hands over to FP64 CG.
+		__shared__ double s_goal[2], s_prev[2];
+		__shared__ int s_fallback;
+		if(threadIdx.x == 0) {
+			for(int c = 0; c < 2; c++) s_goal[c] = sh.thr[c];
+			s_fallback = 0;
+		}
+		__syncthreads();
+		for(int sweep = 0; sweep < 64 && (sh.act[0] || sh.act[1]); sweep++) {
+			if(threadIdx.x == 0) {
+				for(int c = 0; c < 2; c++) {
+					s_prev[c] = sh.rn2[c];
+					if(sh.act[c]) sh.thr[c] = fmax(a.inner_tol * a.inner_tol * sh.rn2[c], s_goal[c]);
+				}
+			}
+			__syncthreads();
+			if(!cg_iterate<float, float>(a, sh, a.rxf, a.ryf, a.pxf, a.pyf, a.Pxf, a.Pyf, a.exf, a.eyf, max_it)) return;
+			for(long long j = gtid; j < S; j += gstride) {
+				a.vx[j] += (double) a.exf[j];
+				a.vy[j] += (double) a.eyf[j];
+			}
+			refinements++;
+			if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return;
+			if(!true_residual(a, sh, false, true)) return;
+			if(threadIdx.x == 0) {
+				for(int c = 0; c < 2; c++) {
+					sh.rn2[c] = sh.tot[2 + c];
+					sh.rz[c] = sh.tot[4 + c];
+					sh.beta[c] = 0.0;
+					if(sh.zero[c]) continue;
+					sh.act[c] = (sh.rn2[c] < s_goal[c]) ? 0 : 1;
+					if(sh.act[c] && sh.rn2[c] > 0.25 * s_prev[c]) s_fallback = 1;
+				}
+			}
+			__syncthreads();
+			if(s_fallback) break;
+		}
+		if(s_fallback || sh.act[0] || sh.act[1]) {
+			// plain FP64 CG from the current x (the residual is in rx, ry)
+			if(!true_residual(a, sh, false, false)) return;
+			if(threadIdx.x == 0) {
+				for(int c = 0; c < 2; c++) {
+					sh.rn2[c] = sh.tot[2 + c];
+					sh.rz[c] = sh.tot[4 + c];
+					sh.thr[c] = s_goal[c];
+					sh.beta[c] = 0.0;
+					sh.act[c] = (!sh.zero[c] && sh.rn2[c] >= s_goal[c]) ? 1 : 0;
+				}
+			}
+			__syncthreads();
+			if(!cg_iterate<double, double>(a, sh, a.rx, a.ry, a.px, a.py, a.Px, a.Py, a.vx, a.vy, max_it)) return;
+		}
 	}
 	if(blockIdx.x == 0 && threadIdx.x == 0) {
 		DevStatus *st = a.st;
 		st->cg_solves += 2;
-		st->cg_iters += s_it[0] + s_it[1];
-		st->cg_max_iters = max(st->cg_max_iters, max(s_it[0], s_it[1]));
+		st->cg_iters += sh.it[0] + sh.it[1];
+		st->cg_max_iters = max(st->cg_max_iters, max(sh.it[0], sh.it[1]));
+		st->refinements += refinements;
 		for(int c = 0; c < 2; c++) {
-			const double rel = s_bn2[c] > 0 ? sqrt(s_rn2[c] / s_bn2[c]) : 0.0;
+			const double rel = sh.bn2[c] > 0 ? sqrt(sh.rn2[c] / sh.bn2[c]) : 0.0;
 			st->cg_max_rel = fmax(st->cg_max_rel, rel);
 		}
 		if(cold) st->restart = 0;
@@ -332,8 +437,19 @@ int cg_grid_blocks(int device) {
 }
 
 cudaError_t launch_cg(const CGArgs &a, int blocks, cudaStream_t s) {
-	void *args[] = {(void *) &a};
-	return cudaLaunchCooperativeKernel((const void *) cg_kernel, dim3(blocks), dim3(CG_THREADS), args, 0, s);
+	// cooperative launch (all blocks co-resident, required by the grid
+	// barriers); cudaLaunchKernelEx form so that it can be captured in a graph
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = dim3(blocks);
+	cfg.blockDim = dim3(CG_THREADS);
+	cfg.dynamicSmemBytes = 0;
+	cfg.stream = s;
+	cudaLaunchAttribute attr[1];
+	attr[0].id = cudaLaunchAttributeCooperative;
+	attr[0].val.cooperative = 1;
+	cfg.attrs = attr;
+	cfg.numAttrs = 1;
+	return cudaLaunchKernelEx(&cfg, cg_kernel, a);
 }
 
 }  // namespace rc

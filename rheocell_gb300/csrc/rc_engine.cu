@@ -67,6 +67,8 @@ struct rc_engine {
 	double *rx = nullptr, *ry = nullptr, *px = nullptr, *py = nullptr, *Px = nullptr, *Py = nullptr;
 	double *partials = nullptr, *scalars = nullptr;
 	unsigned *bar = nullptr;
+	float *rxf = nullptr, *ryf = nullptr, *pxf = nullptr, *pyf = nullptr, *Pxf = nullptr, *Pyf = nullptr;
+	float *exf = nullptr, *eyf = nullptr;
 	double *scratch_phi = nullptr, *scratch_rep = nullptr;
 	std::vector<void *> allocs;
 	std::string err;
@@ -83,6 +85,16 @@ struct rc_engine {
 	std::vector<cudaEvent_t> event_pool;
 	double timer_ms[RC_NUM_TIMERS] = {0};
 	long long timer_n[RC_NUM_TIMERS] = {0};
+	// CUDA graphs of one step, keyed by the host-side step state
+	struct StepGraph {
+		int pending, eval_phase, phase, smem_n;
+		cudaStream_t stream;
+		cudaGraphExec_t exec;
+		int next_pending, next_eval_phase;
+		long long launches;
+	};
+	std::vector<StepGraph> graphs;
+	bool use_graphs = true;
 };
 
 static cudaEvent_t get_event(rc_engine *e) {
@@ -247,6 +259,16 @@ static void solve(rc_engine *e, int phase) {
 	g.xi = e->ph[phase].friction;
 	g.eta = e->ph[phase].friction_cell;
 	g.tol = e->hp.cg_tolerance > 0 ? e->hp.cg_tolerance : 2.220446049250313e-16;
+	g.mixed = e->hp.precision == RC_PRECISION_MIXED;
+	g.inner_tol = 1e-4;
+	g.rxf = e->rxf;
+	g.ryf = e->ryf;
+	g.pxf = e->pxf;
+	g.pyf = e->pyf;
+	g.Pxf = e->Pxf;
+	g.Pyf = e->Pyf;
+	g.exf = e->exf;
+	g.eyf = e->eyf;
 	StageMark sm(e, RC_TIMER_SOLVE);
 	const cudaError_t c = launch_cg(g, e->cg_blocks, e->stream);
 	e->launches += 1;
@@ -340,6 +362,68 @@ static void one_step(rc_engine *e) {
 	evaluate_end(e, e->phiA, cur);
 }
 
+// One step, replayed from a captured CUDA graph when possible.  A graph is
+// captured per distinct host-side state (pending evaluation, its phase, the
+// current phase, shared-memory sizing, stream); the data-dependent solver
+// iteration counts are handled inside the cooperative kernel.
+static void run_step(rc_engine *e) {
+	if(!e->use_graphs || e->timing || e->stream == nullptr || e->stream == cudaStreamLegacy) {
+		one_step(e);
+		return;
+	}
+	for(auto &g : e->graphs) {
+		if(g.pending == (int) e->pending && g.eval_phase == e->eval_phase && g.phase == e->phase &&
+		   g.smem_n == e->smem_n && g.stream == e->stream) {
+			if(cudaGraphLaunch(g.exec, e->stream) != cudaSuccess) {
+				if(e->launch_error.empty()) e->launch_error = "graph launch failed";
+				return;
+			}
+			e->pending = g.next_pending != 0;
+			e->eval_phase = g.next_eval_phase;
+			e->launches += g.launches;
+			return;
+		}
+	}
+	rc_engine::StepGraph g;
+	g.pending = (int) e->pending;
+	g.eval_phase = e->eval_phase;
+	g.phase = e->phase;
+	g.smem_n = e->smem_n;
+	g.stream = e->stream;
+	const bool was_pending = e->pending;
+	const int was_eval_phase = e->eval_phase;
+	const long long l0 = e->launches;
+	cudaGraph_t graph = nullptr;
+	if(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+		cudaGetLastError();
+		e->use_graphs = false;
+		one_step(e);
+		return;
+	}
+	one_step(e);
+	cudaError_t ce = cudaStreamEndCapture(e->stream, &graph);
+	cudaGraphExec_t exec = nullptr;
+	if(ce == cudaSuccess && e->launch_error.empty()) ce = cudaGraphInstantiate(&exec, graph, 0);
+	if(graph) cudaGraphDestroy(graph);
+	if(ce != cudaSuccess || !e->launch_error.empty()) {
+		// capture not possible here: run this and later steps directly
+		cudaGetLastError();
+		e->launch_error.clear();
+		e->use_graphs = false;
+		e->pending = was_pending;
+		e->eval_phase = was_eval_phase;
+		e->launches = l0;
+		one_step(e);
+		return;
+	}
+	g.exec = exec;
+	g.next_pending = (int) e->pending;
+	g.next_eval_phase = e->eval_phase;
+	g.launches = e->launches - l0;
+	e->graphs.push_back(g);
+	if(cudaGraphLaunch(exec, e->stream) != cudaSuccess && e->launch_error.empty()) e->launch_error = "graph launch failed";
+}
+
 // Materialise a pending dry evaluation into mu, v, gradients and the map.
 static void materialise(rc_engine *e, int accumulate) {
 	if(!e->pending) return;
@@ -356,7 +440,7 @@ static void materialise(rc_engine *e, int accumulate) {
 static int choose_smem(rc_engine *e) {
 	int want = std::max(256, (e->max_n_host * 3 + 1) / 2);
 	want = ((want + 255) / 256) * 256;
-	const int per_site = (e->P.model == M_POLAR || e->P.model == M_WET) ? 24 : 16;
+	const int per_site = 8 * cell_smem_arrays(e->P.model);
 	const int cap = (200 * 1024) / per_site;
 	if(e->max_n_host > cap) return set_err(e, RC_ERR_CAPACITY, "patch of %d sites exceeds shared memory", e->max_n_host);
 	e->smem_n = std::min(want, cap);
@@ -511,6 +595,10 @@ int rc_create(const rc_params *params, const rc_box *box, int n_cells, const rc_
 	};
 	if(cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking) != cudaSuccess)
 		return bail(set_err(e, RC_ERR_CUDA, "stream creation failed"));
+	{
+		const cudaError_t c = configure_kernels();
+		if(c != cudaSuccess) return bail(set_err(e, RC_ERR_CUDA, "kernel configuration failed: %s", cudaGetErrorString(c)));
+	}
 	e->stream = e->own_stream;
 
 	DevParams &P = e->P;
@@ -565,6 +653,12 @@ int rc_create(const rc_params *params, const rc_box *box, int n_cells, const rc_
 		   (rc = dalloc(e, &e->py, cap)) || (rc = dalloc(e, &e->Px, L2)) || (rc = dalloc(e, &e->Py, L2)) ||
 		   (rc = dalloc(e, &e->partials, 8 * 4096)) || (rc = dalloc(e, &e->scalars, 64)) || (rc = dalloc(e, &e->bar, 2)))
 			return bail(rc);
+		if(params->precision == RC_PRECISION_MIXED) {
+			if((rc = dalloc(e, &e->rxf, cap)) || (rc = dalloc(e, &e->ryf, cap)) || (rc = dalloc(e, &e->pxf, cap)) ||
+			   (rc = dalloc(e, &e->pyf, cap)) || (rc = dalloc(e, &e->exf, cap)) || (rc = dalloc(e, &e->eyf, cap)) ||
+			   (rc = dalloc(e, &e->Pxf, L2)) || (rc = dalloc(e, &e->Pyf, L2)))
+				return bail(rc);
+		}
 		e->cg_blocks = cg_grid_blocks(device);
 	}
 	if(cudaMallocHost(&e->st_host, sizeof(DevStatus)) != cudaSuccess) return bail(set_err(e, RC_ERR_OOM, "pinned alloc failed"));
@@ -630,7 +724,7 @@ int rc_step(rc_engine *e, int n_steps, rc_step_stats *stats) {
 	while(done < n_steps) {
 		if((rc = choose_smem(e))) return rc;
 		const int m = std::min(chunk, n_steps - done);
-		for(int i = 0; i < m; i++) one_step(e);
+		for(int i = 0; i < m; i++) run_step(e);
 		rc = check_status(e, stats);
 		if(rc) break;
 		done += m;
@@ -645,7 +739,7 @@ int rc_step_async(rc_engine *e, int n_steps) {
 	CUDA_TRY(e, cudaSetDevice(e->device));
 	int rc = choose_smem(e);
 	if(rc) return rc;
-	for(int i = 0; i < n_steps; i++) one_step(e);
+	for(int i = 0; i < n_steps; i++) run_step(e);
 	e->async_steps += n_steps;
 	return RC_OK;
 }
@@ -839,6 +933,7 @@ void rc_destroy(rc_engine *e) {
 	for(void *p : e->allocs) cudaFree(p);
 	if(e->st_host) cudaFreeHost(e->st_host);
 	collect_marks(e);
+	for(auto &g : e->graphs) cudaGraphExecDestroy(g.exec);
 	for(cudaEvent_t v : e->event_pool) cudaEventDestroy(v);
 	if(e->own_stream) cudaStreamDestroy(e->own_stream);
 	delete e;

@@ -62,13 +62,16 @@ struct CGArgs {
 	int L;
 	int restart_every;
 	double xi, eta, tol;
-	int mixed;               // inner iterations in FP32
+	int mixed;               // FP32 inner iterations inside FP64 refinement
+	double inner_tol;        // mixed: relative residual reduction per refinement sweep
 	float *rxf, *ryf, *pxf, *pyf, *Pxf, *Pyf;
-	double *ex, *ey;         // mixed: correction accumulators
+	float *exf, *eyf;        // mixed: correction of one refinement sweep
 };
 
+cudaError_t configure_kernels();
 void launch_cell_kernel(int model, int eval, int upd, const CellArgs &a, cudaStream_t s);
 size_t cell_smem_bytes(int model, int smem_n);
+int cell_smem_arrays(int model);
 void launch_rng(CellDev *cells, int N, DevStatus *st, cudaStream_t s);
 void launch_bins(CellDev *cells, int N, int L, int *bin_count, int *bin_cells, int nbx, int nby, DevStatus *st,
                  cudaStream_t s);
