@@ -39,6 +39,18 @@ __device__ inline int box_el(int site, int dx, int dy, int L) {
 	return wrapi(site % L + dx, L) + wrapi(site / L + dy, L) * L;
 }
 
+// Correctly rounded x / b from rb = RN(1/b): q = RN(x rb), the exact
+// remainder x - q b by FMA, and one correction q + rem rb (Markstein's
+// reciprocal-based division, P. Markstein, IBM J. Res. Dev. 34 (1990) 111-119).
+// Three FP64 instructions instead of a full division; the result equals the
+// IEEE quotient, which tests/test_gpu_parity.py checks bitwise against the
+// CPU restatement's divisions on whole force evaluations.
+__device__ __forceinline__ double div_rn(double x, double b, double rb) {
+	const double q = x * rb;
+	const double rem = __fma_rn(-q, b, x);
+	return __fma_rn(rem, rb, q);
+}
+
 struct Nb {
 	int r, l, u, d;
 };
@@ -251,11 +263,27 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 	const double gamma = P.gamma, lambda = P.lambda, mu_c = P.mu, kappa = P.kappa, omega = P.omega, a0 = P.a0;
 	const bool dry = (MODEL == M_NEMATIC) || (MODEL == M_SIMPLE) || pe.friction_cell == 0;
 
+	// Per-cell constant factors of the reference's left-to-right products
+	// (hoisting a leading sub-product leaves every rounding unchanged).
+	const double rlambda = 1.0 / lambda;
+	const double two_lambda = 2 * lambda;
+	double A_c, Rep_c, Ad_c = 0.0, CHd_c = 0.0, gl_c = gamma * lambda;
+	if(MODEL == M_SIMPLE || MODEL == M_NEMATIC) {
+		A_c = -4 * mu_c / a0 * (1 - c.area / a0);
+		Rep_c = 4 * kappa / lambda;
+	}
+	else {
+		A_c = -4 * (mu_c / a0) * (1 - c.area / a0);
+		Rep_c = 4 * (kappa / lambda);
+		Ad_c = -mu_c / a0;
+		CHd_c = (gamma / lambda) * 4;
+	}
+	const double kl_c = kappa / lambda;
 	double perim = 0.0;
 	if(EVAL != EV_NONE) {
 		for(int q = threadIdx.x; q < n; q += blockDim.x) sphi[q] = a.phi_eval[start + q];
 		__syncthreads();
-		if(MODEL == M_POLAR) {
+		if(MODEL == M_POLAR && (pe.beta != 0.0 || EVAL == EV_STORE || EVAL == EV_WET_RHS)) {
 			double v[1] = {0.0};
 			for(int q = threadIdx.x; q < n; q += blockDim.x) {
 				const int y = q / lx, x = q - y * lx;
@@ -284,16 +312,16 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 			double mu = 0.0;
 			if(MODEL == M_SIMPLE) {
 				const double lap = pu_ + pd + pr + pl - 4 * phi;
-				const double CH = gamma * (8 * phi * (1 - phi) * (1 - 2 * phi) / lambda - 2 * lambda * lap);
-				const double A = -4 * mu_c / a0 * (1 - c.area / a0) * phi;
-				const double Rep = 4 * kappa / lambda * phi * (p2 - phi * phi);
+				const double CH = gamma * (div_rn(8 * phi * (1 - phi) * (1 - 2 * phi), lambda, rlambda) - two_lambda * lap);
+				const double A = A_c * phi;
+				const double Rep = Rep_c * phi * (p2 - phi * phi);
 				mu = CH + A + Rep + 0.;
 			}
 			else if(MODEL == M_NEMATIC) {
 				const double lap = pr + pu_ + pl + pd - 4. * phi;
-				const double CH = +gamma * (8 * phi * (1 - phi) * (1 - 2 * phi) / lambda - 2 * lambda * lap);
-				const double A = -4 * mu_c / a0 * (1 - c.area / a0) * phi;
-				const double Rep = +4 * kappa / lambda * phi * (p2 - phi * phi);
+				const double CH = +gamma * (div_rn(8 * phi * (1 - phi) * (1 - 2 * phi), lambda, rlambda) - two_lambda * lap);
+				const double A = A_c * phi;
+				const double Rep = Rep_c * phi * (p2 - phi * phi);
 				double V = CH + A + Rep;
 				if(omega != 0.0) {
 					const double lsq = 2 * phi * lap + 2 * (dx * dx + dy * dy);
@@ -304,9 +332,9 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 			}
 			else {
 				const double lap = pu_ + pd + pr + pl - 4 * phi;
-				const double CH = gamma * (8 * phi * (1 - phi) * (1 - 2 * phi) / lambda - 2 * lambda * lap);
-				const double A = -4 * (mu_c / a0) * (1 - c.area / a0) * phi;
-				const double Rep = 4 * (kappa / lambda) * phi * (p2 - phi * phi);
+				const double CH = gamma * (div_rn(8 * phi * (1 - phi) * (1 - 2 * phi), lambda, rlambda) - two_lambda * lap);
+				const double A = A_c * phi;
+				const double Rep = Rep_c * phi * (p2 - phi * phi);
 				double V = CH + A + Rep;
 				if(omega != 0.0) {
 					const double lsq = 2 * phi * lap + 2 * (dx * dx + dy * dy);
@@ -325,9 +353,9 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 					}
 				}
 				else {
-					const double CHd = (gamma / lambda) * 4 * phi * phi * (1 - phi) * (1 - phi) + gamma * lambda * (dx * dx + dy * dy);
-					const double Ad = -mu_c / a0 * phi * phi;
-					const double Repd = (kappa / lambda) * phi * phi * (p2 - phi * phi);
+					const double CHd = CHd_c * phi * phi * (1 - phi) * (1 - phi) + gl_c * (dx * dx + dy * dy);
+					const double Ad = Ad_c * phi * phi;
+					const double Repd = kl_c * phi * phi * (p2 - phi * phi);
 					saux[q] = CHd + Ad + Repd;
 				}
 				mu = V;
@@ -351,6 +379,7 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 	const PhaseParams &pu = a.pu;
 	const double J0 = P.J0, hdt = P.dt * .5;
 	const double zs = pe.zs, zi = pe.zi, fr = pe.friction, alpha = P.passive_alpha;
+	const double rfr = 1.0 / fr;
 	const int tb = table_base(lx), tby = table_base(ly);
 
 	for(int q = threadIdx.x; q < n; q += blockDim.x) {
@@ -374,8 +403,8 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 				const double fix = -(0.5 * (a.sq00[kb.r] - a.sq00[kb.l]) + 0.5 * (a.sq01[kb.u] - a.sq01[kb.d])) - fsx;
 				const double fiy = -(0.5 * (a.sq01[kb.r] - a.sq01[kb.l]) - 0.5 * (a.sq00[kb.u] - a.sq00[kb.d])) - fsy;
 				if(MODEL == M_NEMATIC) {
-					vx = (mu * dx + fsx * zs + fix * zi) / fr;
-					vy = (mu * dy + fsy * zs + fiy * zi) / fr;
+					vx = div_rn(mu * dx + fsx * zs + fix * zi, fr, rfr);
+					vy = div_rn(mu * dy + fsy * zs + fiy * zi, fr, rfr);
 				}
 				else {
 					// Passive stress of WetModel.cpp:634-635 from neighbours' mu, f_d and gradients.
@@ -409,8 +438,8 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 						a.fyg[start + q] = fy;
 					}
 					else {
-						vx = fx / fr;
-						vy = fy / fr;
+						vx = div_rn(fx, fr, rfr);
+						vy = div_rn(fy, fr, rfr);
 					}
 				}
 			}
@@ -435,8 +464,8 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 					a.fyg[start + q] = fy;
 				}
 				else {
-					vx = fx / fr;
-					vy = fy / fr;
+					vx = div_rn(fx, fr, rfr);
+					vy = div_rn(fy, fr, rfr);
 				}
 			}
 			if(EVAL == EV_STORE && dry) {

@@ -76,13 +76,14 @@ __device__ bool grid_reduce(const CGArgs &a, int nv, const double *v, double *ou
 	}
 	else if(threadIdx.x == 0) {
 		long long spins = 0;
-		while(atomicAdd(&a.bar[1], 0u) == s_gen) {
+		const volatile unsigned *gen = a.bar + 1;
+		while(*gen == s_gen) {
 			if(++spins > BARRIER_SPIN_LIMIT) {
 				atomicOr(&a.st->err, ERR_BARRIER);
 				s_fail = 1;
 				break;
 			}
-			__nanosleep(64);
+			__nanosleep(32);
 		}
 		__threadfence();
 	}
@@ -186,22 +187,53 @@ __device__ bool true_residual(const CGArgs &a, CGShared &sh, bool x_zero, bool t
 }
 
 // Jacobi-preconditioned CG iterations from the state in sh (act, rz, thr) and
-// the residual in (rx, ry): Eigen's loop.  T is the storage type of r, p and
-// the box sums, U that of the solution accumulator; dot products are FP64.
-template<typename T, typename U>
-__device__ bool cg_iterate(const CGArgs &a, CGShared &sh, T *rx, T *ry, T *px, T *py, T *Pbx, T *Pby, U *ux, U *uy,
-                           long long max_it) {
+// the residual in (rx, ry): Eigen's loop.  T is the storage type of r, p, Ap
+// and the box sums, U that of the solution accumulator; dot products are
+// FP64.  Updates use fused multiply-adds (the solve is not bitwise Eigen's in
+// any case: its reductions run in a different order).
+template<typename T>
+__device__ __forceinline__ T fmaT(T a, T b, T c);
+template<>
+__device__ __forceinline__ double fmaT<double>(double a, double b, double c) { return __fma_rn(a, b, c); }
+template<>
+__device__ __forceinline__ float fmaT<float>(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+template<typename T>
+__device__ __forceinline__ T box_n4T(const T *P, int k, int L) {
+	const int x = k % L, y = k / L;
+	const int kr = (x == L - 1) ? k - (L - 1) : k + 1;
+	const int kl = (x == 0) ? k + (L - 1) : k - 1;
+	const int ku = (y == L - 1) ? k - (L - 1) * L : k + L;
+	const int kd = (y == 0) ? k + (L - 1) * L : k - L;
+	return P[kd] + P[kl] + P[kr] + P[ku];
+}
+
+// Jacobi-preconditioned CG iterations from the state in sh (act, rz, thr) and
+// the residual in (rx, ry): Eigen's loop.  Vectors, box sums and the
+// element-wise arithmetic are in T (FP64 for the plain solve, FP32 for the
+// inner solves of the mixed path); every thread's partial dot product is
+// summed into FP64 for the block and grid reductions, and the scalars alpha,
+// beta are FP64.  Updates use fused multiply-adds (the solve is not bitwise
+// Eigen's in any case: its reductions run in a different order).
+template<typename T>
+__device__ bool cg_iterate(const CGArgs &a, CGShared &sh, T *rx, T *ry, T *px, T *py, T *apx, T *apy, T *Pbx, T *Pby,
+                           T *ux, T *uy, long long max_it) {
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
 	const long long S = a.st->S;
-	const double neta = -a.eta * 1.0;
+	const T neta = (T) (-a.eta * 1.0);
 	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
 	const long long gstride = (long long) gridDim.x * blockDim.x;
+	__shared__ T dT[CG_MAX_D + 1], iTT[CG_MAX_D + 1];
+	for(int d = threadIdx.x; d <= CG_MAX_D; d += blockDim.x) {
+		dT[d] = (T) sh.T[d];
+		iTT[d] = (T) sh.iT[d];
+	}
 	if(threadIdx.x == 0) sh.first = 1;
 	__syncthreads();
 	while(sh.act[0] || sh.act[1]) {
 		const int ax = sh.act[0], ay = sh.act[1], first = sh.first;
-		const double bx = sh.beta[0], by = sh.beta[1];
+		const T bx = (T) sh.beta[0], by = (T) sh.beta[1];
 		// Phase A: p = z + beta p (p = z on the first sweep), box sums P = S p
 		for(long long k = gtid; k < L2; k += gstride) {
 			const int n = a.cnt[k];
@@ -210,42 +242,47 @@ __device__ bool cg_iterate(const CGArgs &a, CGShared &sh, T *rx, T *ry, T *px, T
 				if(ay) Pby[k] = (T) 0;
 				continue;
 			}
-			const double id = sh.iT[box_deg(a.cnt, k, L)];
-			double sx = 0.0, sy = 0.0;
+			const T id = iTT[box_deg(a.cnt, k, L)];
+			T sx = (T) 0, sy = (T) 0;
 			for(int i = 0; i < n; i++) {
 				const int j = a.cover[(size_t) i * L2 + k];
 				if(ax) {
-					const double z = id * (double) rx[j];
-					const T p = (T) (first ? z : z + bx * (double) px[j]);
+					const T z = id * rx[j];
+					const T p = first ? z : fmaT<T>(bx, px[j], z);
 					px[j] = p;
-					sx += (double) p;
+					sx += p;
 				}
 				if(ay) {
-					const double z = id * (double) ry[j];
-					const T p = (T) (first ? z : z + by * (double) py[j]);
+					const T z = id * ry[j];
+					const T p = first ? z : fmaT<T>(by, py[j], z);
 					py[j] = p;
-					sy += (double) p;
+					sy += p;
 				}
 			}
-			if(ax) Pbx[k] = (T) sx;
-			if(ay) Pby[k] = (T) sy;
+			if(ax) Pbx[k] = sx;
+			if(ay) Pby[k] = sy;
 		}
 		if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
-		// Phase B: p.Ap
+		// Phase B: Ap (stored) and p.Ap
 		{
-			double v[2] = {0, 0};
+			T w[2] = {(T) 0, (T) 0};
 			for(long long j = gtid; j < S; j += gstride) {
 				const int k = a.mapg[j];
-				const double d = sh.T[box_deg(a.cnt, k, L)];
+				const T d = dT[box_deg(a.cnt, k, L)];
 				if(ax) {
-					const double p = (double) px[j];
-					v[0] += p * (d * p + neta * (double) box_n4(Pbx, k, L));
+					const T p = px[j];
+					const T ap = fmaT<T>(d, p, neta * box_n4T<T>(Pbx, k, L));
+					apx[j] = ap;
+					w[0] = fmaT<T>(p, ap, w[0]);
 				}
 				if(ay) {
-					const double p = (double) py[j];
-					v[1] += p * (d * p + neta * (double) box_n4(Pby, k, L));
+					const T p = py[j];
+					const T ap = fmaT<T>(d, p, neta * box_n4T<T>(Pby, k, L));
+					apy[j] = ap;
+					w[1] = fmaT<T>(p, ap, w[1]);
 				}
 			}
+			double v[2] = {(double) w[0], (double) w[1]};
 			block_sum<2>(v, sh.red);
 			if(!grid_reduce(a, 2, v, sh.tot, sh.red)) return false;
 		}
@@ -256,33 +293,27 @@ __device__ bool cg_iterate(const CGArgs &a, CGShared &sh, T *rx, T *ry, T *px, T
 		__syncthreads();
 		// Phase C: u += alpha p; r -= alpha Ap; |r|^2 and r.z
 		{
-			const double alx = sh.alpha[0], aly = sh.alpha[1];
-			double v[4] = {0, 0, 0, 0};
+			const T alx = (T) sh.alpha[0], aly = (T) sh.alpha[1];
+			T w[4] = {(T) 0, (T) 0, (T) 0, (T) 0};
 			for(long long j = gtid; j < S; j += gstride) {
 				const int k = a.mapg[j];
-				const int D = box_deg(a.cnt, k, L);
-				const double d = sh.T[D], id = sh.iT[D];
+				const T id = iTT[box_deg(a.cnt, k, L)];
 				if(ax) {
-					const double p = (double) px[j];
-					const double ap = d * p + neta * (double) box_n4(Pbx, k, L);
-					ux[j] = (U) ((double) ux[j] + alx * p);
-					const T r = (T) ((double) rx[j] - alx * ap);
+					ux[j] = fmaT<T>(alx, px[j], ux[j]);
+					const T r = fmaT<T>(-alx, apx[j], rx[j]);
 					rx[j] = r;
-					const double rd = (double) r;
-					v[0] += rd * rd;
-					v[2] += rd * (id * rd);
+					w[0] = fmaT<T>(r, r, w[0]);
+					w[2] = fmaT<T>(r, id * r, w[2]);
 				}
 				if(ay) {
-					const double p = (double) py[j];
-					const double ap = d * p + neta * (double) box_n4(Pby, k, L);
-					uy[j] = (U) ((double) uy[j] + aly * p);
-					const T r = (T) ((double) ry[j] - aly * ap);
+					uy[j] = fmaT<T>(aly, py[j], uy[j]);
+					const T r = fmaT<T>(-aly, apy[j], ry[j]);
 					ry[j] = r;
-					const double rd = (double) r;
-					v[1] += rd * rd;
-					v[3] += rd * (id * rd);
+					w[1] = fmaT<T>(r, r, w[1]);
+					w[3] = fmaT<T>(r, id * r, w[3]);
 				}
 			}
+			double v[4] = {(double) w[0], (double) w[1], (double) w[2], (double) w[3]};
 			block_sum<4>(v, sh.red);
 			if(!grid_reduce(a, 4, v, sh.tot, sh.red)) return false;
 		}
@@ -354,7 +385,7 @@ __global__ void __launch_bounds__(CG_THREADS) cg_kernel(const CGArgs a) {
 	const long long max_it = 2 * S;
 	int refinements = 0;
 	if(!mixed) {
-		if(!cg_iterate<double, double>(a, sh, a.rx, a.ry, a.px, a.py, a.Px, a.Py, a.vx, a.vy, max_it)) return;
+		if(!cg_iterate<double>(a, sh, a.rx, a.ry, a.px, a.py, a.apx, a.apy, a.Px, a.Py, a.vx, a.vy, max_it)) return;
 	}
 	else {
 		// Iterative refinement: FP32 Jacobi-PCG for the correction A e = r,
@@ -375,7 +406,7 @@ __global__ void __launch_bounds__(CG_THREADS) cg_kernel(const CGArgs a) {
 				}
 			}
 			__syncthreads();
-			if(!cg_iterate<float, float>(a, sh, a.rxf, a.ryf, a.pxf, a.pyf, a.Pxf, a.Pyf, a.exf, a.eyf, max_it)) return;
+			if(!cg_iterate<float>(a, sh, a.rxf, a.ryf, a.pxf, a.pyf, a.apxf, a.apyf, a.Pxf, a.Pyf, a.exf, a.eyf, max_it)) return;
 			for(long long j = gtid; j < S; j += gstride) {
 				a.vx[j] += (double) a.exf[j];
 				a.vy[j] += (double) a.eyf[j];
@@ -409,7 +440,7 @@ __global__ void __launch_bounds__(CG_THREADS) cg_kernel(const CGArgs a) {
 				}
 			}
 			__syncthreads();
-			if(!cg_iterate<double, double>(a, sh, a.rx, a.ry, a.px, a.py, a.Px, a.Py, a.vx, a.vy, max_it)) return;
+			if(!cg_iterate<double>(a, sh, a.rx, a.ry, a.px, a.py, a.apx, a.apy, a.Px, a.Py, a.vx, a.vy, max_it)) return;
 		}
 	}
 	if(blockIdx.x == 0 && threadIdx.x == 0) {

@@ -64,10 +64,11 @@ struct rc_engine {
 	double *tab_cos = nullptr, *tab_sin = nullptr;
 	DevStatus *st = nullptr;
 	DevStatus *st_host = nullptr;
-	double *rx = nullptr, *ry = nullptr, *px = nullptr, *py = nullptr, *Px = nullptr, *Py = nullptr;
+	double *rx = nullptr, *ry = nullptr, *px = nullptr, *py = nullptr, *apx = nullptr, *apy = nullptr, *Px = nullptr, *Py = nullptr;
 	double *partials = nullptr, *scalars = nullptr;
 	unsigned *bar = nullptr;
-	float *rxf = nullptr, *ryf = nullptr, *pxf = nullptr, *pyf = nullptr, *Pxf = nullptr, *Pyf = nullptr;
+	float *rxf = nullptr, *ryf = nullptr, *pxf = nullptr, *pyf = nullptr, *apxf = nullptr, *apyf = nullptr;
+	float *Pxf = nullptr, *Pyf = nullptr;
 	float *exf = nullptr, *eyf = nullptr;
 	double *scratch_phi = nullptr, *scratch_rep = nullptr;
 	std::vector<void *> allocs;
@@ -248,6 +249,10 @@ static void solve(rc_engine *e, int phase) {
 	g.ry = e->ry;
 	g.px = e->px;
 	g.py = e->py;
+	g.apx = e->apx;
+	g.apy = e->apy;
+	g.apxf = e->apxf;
+	g.apyf = e->apyf;
 	g.Px = e->Px;
 	g.Py = e->Py;
 	g.partials = e->partials;
@@ -650,12 +655,14 @@ int rc_create(const rc_params *params, const rc_box *box, int n_cells, const rc_
 	if(wet) {
 		if((rc = dalloc(e, &e->fx, cap)) || (rc = dalloc(e, &e->fy, cap)) || (rc = dalloc(e, &e->cover, L2 * STORE_MAX)) ||
 		   (rc = dalloc(e, &e->rx, cap)) || (rc = dalloc(e, &e->ry, cap)) || (rc = dalloc(e, &e->px, cap)) ||
-		   (rc = dalloc(e, &e->py, cap)) || (rc = dalloc(e, &e->Px, L2)) || (rc = dalloc(e, &e->Py, L2)) ||
+		   (rc = dalloc(e, &e->py, cap)) || (rc = dalloc(e, &e->apx, cap)) || (rc = dalloc(e, &e->apy, cap)) ||
+		   (rc = dalloc(e, &e->Px, L2)) || (rc = dalloc(e, &e->Py, L2)) ||
 		   (rc = dalloc(e, &e->partials, 8 * 4096)) || (rc = dalloc(e, &e->scalars, 64)) || (rc = dalloc(e, &e->bar, 2)))
 			return bail(rc);
 		if(params->precision == RC_PRECISION_MIXED) {
 			if((rc = dalloc(e, &e->rxf, cap)) || (rc = dalloc(e, &e->ryf, cap)) || (rc = dalloc(e, &e->pxf, cap)) ||
 			   (rc = dalloc(e, &e->pyf, cap)) || (rc = dalloc(e, &e->exf, cap)) || (rc = dalloc(e, &e->eyf, cap)) ||
+			   (rc = dalloc(e, &e->apxf, cap)) || (rc = dalloc(e, &e->apyf, cap)) ||
 			   (rc = dalloc(e, &e->Pxf, L2)) || (rc = dalloc(e, &e->Pyf, L2)))
 				return bail(rc);
 		}

@@ -53,7 +53,7 @@ struct CGArgs {
 	const int *cnt, *cover;
 	const double *fx, *fy;   // right-hand sides
 	double *vx, *vy;         // solution; warm start
-	double *rx, *ry, *px, *py;
+	double *rx, *ry, *px, *py, *apx, *apy;
 	double *Px, *Py;         // box-grid sums of p
 	double *partials;        // per-block partial sums
 	double *scalars;         // solver scalars (see rc_cg.cu)
@@ -64,7 +64,7 @@ struct CGArgs {
 	double xi, eta, tol;
 	int mixed;               // FP32 inner iterations inside FP64 refinement
 	double inner_tol;        // mixed: relative residual reduction per refinement sweep
-	float *rxf, *ryf, *pxf, *pyf, *Pxf, *Pyf;
+	float *rxf, *ryf, *pxf, *pyf, *apxf, *apyf, *Pxf, *Pyf;
 	float *exf, *eyf;        // mixed: correction of one refinement sweep
 };
 

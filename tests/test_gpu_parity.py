@@ -161,3 +161,22 @@ def test_mixed_precision_solve(model):
     e.set_phase(1)
     st = e.step(2)
     assert st.refinements >= 4 and 0 < st.cg_max_rel_residual < 1e-8
+
+
+@pytest.mark.parametrize("model", ["wetpolarmodel", "activenematic", "simplefield", "wetmodel"])
+def test_first_evaluation_bitwise(model):
+    """One force evaluation from identical inputs is bit-identical to the CPU
+    restatement (itself bit-identical to the reference's exact build): box
+    sums in the reference's order, IEEE FP64 in its order of operations, and
+    correctly rounded divisions.  lambda = 2.5 and friction = 1.7 make the
+    divisions inexact."""
+    m = g.make_monolayer(96, 36, seed=14, types=[i % 2 for i in range(36)])
+    params = dict(g.DRY_POLAR, interaction_type=model, **{"lambda": 2.5}, friction=1.7, omega=0.004,
+                  zetaQ_self=0.1, zetaQ_inter=0.05, J_Q=0.2)
+    keys, m2 = case_from_monolayer(m, params, seed=15)
+    p, cells = build_inputs(keys, m2)
+    a = engine.Engine(p, m2.L, cells).state()
+    p, cells = build_inputs(keys, m2)
+    b = orc.OracleSim(p, m2.L, cells).state()
+    for k in ("mu", "vx", "vy", "box_index", "area", "sum_f"):
+        assert np.array_equal(a[k], b[k]), (k, rel_err(a[k], b[k]))
