@@ -122,6 +122,68 @@ struct CGShared {
 	int act[2], it[2], first, zero[2];
 };
 
+// Cover lists in CSR form for this solve: cov_off[k] = sum of n over box
+// sites before k, cov_idx[cov_off[k] + i] = cover[i][k] (unknowns covering k,
+// in cell order).  Block b scans the contiguous box range it owns; the block
+// totals meet through one grid barrier.
+__device__ bool build_csr(const CGArgs &a, CGShared &sh) {
+	const long long L2 = (long long) a.L * a.L;
+	const long long chunk = (L2 + gridDim.x - 1) / gridDim.x;
+	const long long lo = blockIdx.x * chunk, hi = min(L2, lo + chunk);
+	__shared__ int s_scan[CG_THREADS];
+	__shared__ long long s_base;
+	// per-thread contiguous sub-range of the block's range
+	const long long per = (chunk + blockDim.x - 1) / blockDim.x;
+	const long long tlo = min(hi, lo + threadIdx.x * per), thi = min(hi, tlo + per);
+	int tsum = 0;
+	for(long long k = tlo; k < thi; k++) tsum += a.cnt[k];
+	s_scan[threadIdx.x] = tsum;
+	__syncthreads();
+	for(int o = 1; o < (int) blockDim.x; o <<= 1) {
+		const int add = (threadIdx.x >= (unsigned) o) ? s_scan[threadIdx.x - o] : 0;
+		__syncthreads();
+		s_scan[threadIdx.x] += add;
+		__syncthreads();
+	}
+	const int block_total = s_scan[blockDim.x - 1];
+	double v[1] = {(double) block_total};
+	if(threadIdx.x == 0) a.partials[(size_t) 7 * gridDim.x + blockIdx.x] = v[0];
+	if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
+	{
+		double acc[1] = {0.0};
+		for(unsigned b = threadIdx.x; b < blockIdx.x; b += blockDim.x) acc[0] += ldcg(&a.partials[(size_t) 7 * gridDim.x + b]);
+		block_sum<1>(acc, sh.red);
+		if(threadIdx.x == 0) s_base = (long long) acc[0];
+		__syncthreads();
+	}
+	long long off = s_base + s_scan[threadIdx.x] - tsum;
+	for(long long k = tlo; k < thi; k++) {
+		const int n = a.cnt[k];
+		a.cov_off[k] = (int) off;
+		for(int i = 0; i < n; i++) a.cov_idx[off + i] = a.cover[(size_t) i * L2 + k];
+		off += n;
+	}
+	if(blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) a.cov_off[L2] = (int) off;
+	return grid_reduce(a, 0, nullptr, sh.tot, sh.red);
+}
+
+// Warp-segmented sum of v over consecutive lanes with equal key (keys sorted
+// within the warp); returns the segment's partial sum in its last lane of
+// this warp (others: unused), and whether this lane is that tail.
+template<typename T>
+__device__ __forceinline__ T seg_sum(T v, int key, bool &tail) {
+	const int lane = threadIdx.x & 31;
+#pragma unroll
+	for(int d = 1; d < 32; d <<= 1) {
+		const T u = __shfl_up_sync(0xffffffffu, v, d);
+		const int kd = __shfl_up_sync(0xffffffffu, key, d);
+		if(lane >= d && kd == key) v += u;
+	}
+	const int kn = __shfl_down_sync(0xffffffffu, key, 1);
+	tail = (lane == 31) || (kn != key);
+	return v;
+}
+
 // r = b - A x for both components (x = 0 when `x_zero`), written in FP64 and,
 // for the mixed path, also rounded to FP32.  Reduces |b|^2, |r|^2 and r.M^-1 r
 // (the latter on the stored precision of r) into sh.tot[0..5].
@@ -133,16 +195,28 @@ __device__ bool true_residual(const CGArgs &a, CGShared &sh, bool x_zero, bool t
 	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
 	const long long gstride = (long long) gridDim.x * blockDim.x;
 	if(!x_zero) {
+		// box sums of x over the CSR cover lists: clear, then add
 		for(long long k = gtid; k < L2; k += gstride) {
-			const int n = a.cnt[k];
-			double sx = 0.0, sy = 0.0;
-			for(int i = 0; i < n; i++) {
-				const int j = a.cover[(size_t) i * L2 + k];
-				sx += a.vx[j];
-				sy += a.vy[j];
+			a.Px[k] = 0.0;
+			a.Py[k] = 0.0;
+		}
+		if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
+		const long long E = __ldcg(&a.cov_off[L2]);
+		const long long gwarp = gtid >> 5, nwarps = gstride >> 5;
+		const int lane = threadIdx.x & 31;
+		for(long long base = gwarp * 32; base < E; base += nwarps * 32) {
+			const long long t = base + lane;
+			const bool valid = t < E;
+			const int j = valid ? a.cov_idx[t] : 0;
+			const int key = valid ? a.mapg[j] : -1;
+			bool tail;
+			const double sx = seg_sum<double>(valid ? a.vx[j] : 0.0, key, tail);
+			bool tail2;
+			const double sy = seg_sum<double>(valid ? a.vy[j] : 0.0, key, tail2);
+			if(valid && tail) {
+				atomicAdd(&a.Px[key], sx);
+				atomicAdd(&a.Py[key], sy);
 			}
-			a.Px[k] = sx;
-			a.Py[k] = sy;
 		}
 		if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
 	}
@@ -230,37 +304,47 @@ __device__ bool cg_iterate(const CGArgs &a, CGShared &sh, T *rx, T *ry, T *px, T
 		iTT[d] = (T) sh.iT[d];
 	}
 	if(threadIdx.x == 0) sh.first = 1;
-	__syncthreads();
+	for(long long k = gtid; k < L2; k += gstride) {
+		Pbx[k] = (T) 0;
+		Pby[k] = (T) 0;
+	}
+	if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
+	const long long E = __ldcg(&a.cov_off[L2]);
 	while(sh.act[0] || sh.act[1]) {
 		const int ax = sh.act[0], ay = sh.act[1], first = sh.first;
 		const T bx = (T) sh.beta[0], by = (T) sh.beta[1];
-		// Phase A: p = z + beta p (p = z on the first sweep), box sums P = S p
-		for(long long k = gtid; k < L2; k += gstride) {
-			const int n = a.cnt[k];
-			if(n == 0) {
-				if(ax) Pbx[k] = (T) 0;
-				if(ay) Pby[k] = (T) 0;
-				continue;
-			}
-			const T id = iTT[box_deg(a.cnt, k, L)];
-			T sx = (T) 0, sy = (T) 0;
-			for(int i = 0; i < n; i++) {
-				const int j = a.cover[(size_t) i * L2 + k];
-				if(ax) {
+		// Phase A: p = z + beta p (p = z on the first sweep), box sums P = S p,
+		// one thread per cover entry; P is zero on entry (cleared in phase C)
+		{
+			const long long gwarp = gtid >> 5, nwarps = gstride >> 5;
+			const int lane = threadIdx.x & 31;
+			for(long long base = gwarp * 32; base < E; base += nwarps * 32) {
+				const long long t = base + lane;
+				const bool valid = t < E;
+				const int j = valid ? a.cov_idx[t] : 0;
+				const int key = valid ? a.mapg[j] : -1;
+				const T id = valid ? iTT[box_deg(a.cnt, key, L)] : (T) 0;
+				T vx = (T) 0, vy = (T) 0;
+				if(valid && ax) {
 					const T z = id * rx[j];
 					const T p = first ? z : fmaT<T>(bx, px[j], z);
 					px[j] = p;
-					sx += p;
+					vx = p;
 				}
-				if(ay) {
+				if(valid && ay) {
 					const T z = id * ry[j];
 					const T p = first ? z : fmaT<T>(by, py[j], z);
 					py[j] = p;
-					sy += p;
+					vy = p;
+				}
+				bool tail = false, tail2 = false;
+				if(ax) vx = seg_sum<T>(vx, key, tail);
+				if(ay) vy = seg_sum<T>(vy, key, tail2);
+				if(valid) {
+					if(ax && tail) atomicAdd(&Pbx[key], vx);
+					if(ay && tail2) atomicAdd(&Pby[key], vy);
 				}
 			}
-			if(ax) Pbx[k] = sx;
-			if(ay) Pby[k] = sy;
 		}
 		if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
 		// Phase B: Ap (stored) and p.Ap
@@ -314,6 +398,11 @@ __device__ bool cg_iterate(const CGArgs &a, CGShared &sh, T *rx, T *ry, T *px, T
 				}
 			}
 			double v[4] = {(double) w[0], (double) w[1], (double) w[2], (double) w[3]};
+			// clear the box sums for the next sweep's phase A
+			for(long long k = gtid; k < L2; k += gstride) {
+				Pbx[k] = (T) 0;
+				Pby[k] = (T) 0;
+			}
 			block_sum<4>(v, sh.red);
 			if(!grid_reduce(a, 4, v, sh.tot, sh.red)) return false;
 		}
@@ -359,6 +448,7 @@ __global__ void __launch_bounds__(CG_THREADS) cg_kernel(const CGArgs a) {
 		}
 	}
 	const bool mixed = a.mixed != 0;
+	if(!build_csr(a, sh)) return;
 	if(!true_residual(a, sh, cold != 0, mixed)) return;
 	if(threadIdx.x == 0) {
 		for(int c = 0; c < 2; c++) {

@@ -59,7 +59,7 @@ struct rc_engine {
 	double *vx = nullptr, *vy = nullptr, *fx = nullptr, *fy = nullptr, *rep = nullptr;
 	int *mapg = nullptr;
 	double *phi2 = nullptr, *sq00 = nullptr, *sq01 = nullptr;
-	int *cnt = nullptr, *cover = nullptr;
+	int *cnt = nullptr, *cover = nullptr, *cov_off = nullptr, *cov_idx = nullptr;
 	int *bin_count = nullptr, *bin_cells = nullptr;
 	double *tab_cos = nullptr, *tab_sin = nullptr;
 	DevStatus *st = nullptr;
@@ -241,6 +241,8 @@ static void solve(rc_engine *e, int phase) {
 	g.mapg = e->mapg;
 	g.cnt = e->cnt;
 	g.cover = e->cover;
+	g.cov_off = e->cov_off;
+	g.cov_idx = e->cov_idx;
 	g.fx = e->fx;
 	g.fy = e->fy;
 	g.vx = e->vx;
@@ -654,6 +656,7 @@ int rc_create(const rc_params *params, const rc_box *box, int n_cells, const rc_
 		return bail(rc);
 	if(wet) {
 		if((rc = dalloc(e, &e->fx, cap)) || (rc = dalloc(e, &e->fy, cap)) || (rc = dalloc(e, &e->cover, L2 * STORE_MAX)) ||
+		   (rc = dalloc(e, &e->cov_off, L2 + 1)) || (rc = dalloc(e, &e->cov_idx, cap)) ||
 		   (rc = dalloc(e, &e->rx, cap)) || (rc = dalloc(e, &e->ry, cap)) || (rc = dalloc(e, &e->px, cap)) ||
 		   (rc = dalloc(e, &e->py, cap)) || (rc = dalloc(e, &e->apx, cap)) || (rc = dalloc(e, &e->apy, cap)) ||
 		   (rc = dalloc(e, &e->Px, L2)) || (rc = dalloc(e, &e->Py, L2)) ||

@@ -51,6 +51,7 @@ struct CGArgs {
 	const CellDev *cells;
 	const int *mapg;
 	const int *cnt, *cover;
+	int *cov_off, *cov_idx;  // CSR cover lists built by the solve
 	const double *fx, *fy;   // right-hand sides
 	double *vx, *vy;         // solution; warm start
 	double *rx, *ry, *px, *py, *apx, *apy;
