@@ -19,7 +19,9 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "librheocell_gb300.so")
 CLI = os.path.join(BUILD, "rheocell")
+GEN = os.path.join(BUILD, "confgenerator")
 HOST_SRC = os.path.join(HERE, "host", "rheocell.cpp")
+GEN_SRC = os.path.join(HERE, "host", "confgenerator.cpp")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
                      "-Xptxas", "-O3"]
@@ -44,10 +46,10 @@ def _deps():
 
 
 def up_to_date() -> bool:
-    if not os.path.exists(LIB) or not os.path.exists(CLI):
+    if not all(os.path.exists(f) for f in (LIB, CLI, GEN)):
         return False
-    t = min(os.path.getmtime(LIB), os.path.getmtime(CLI))
-    return all(os.path.getmtime(d) <= t for d in _deps() + [HOST_SRC])
+    t = min(os.path.getmtime(LIB), os.path.getmtime(CLI), os.path.getmtime(GEN))
+    return all(os.path.getmtime(d) <= t for d in _deps() + [HOST_SRC, GEN_SRC])
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
@@ -82,6 +84,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError("host driver build failed:\n%s%s" % (r.stdout, r.stderr))
     os.replace(CLI + ".tmp", CLI)
+    cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-ffp-contract=off", GEN_SRC, "-o", GEN + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("confgenerator build failed:\n%s%s" % (r.stdout, r.stderr))
+    os.replace(GEN + ".tmp", GEN)
     return LIB
 
 

@@ -234,7 +234,7 @@ template<int MODEL, int EVAL, int UPD>
 __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 	extern __shared__ double smem[];
 	__shared__ CellDev c;
-	__shared__ double red[12 * (CELL_THREADS / 32)];
+	__shared__ double red[12 * (CELL_THREADS / 32 + 1)];
 	__shared__ int ired[2 * (CELL_THREADS / 32)];
 
 	const int ci = blockIdx.x;

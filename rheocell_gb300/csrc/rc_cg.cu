@@ -116,7 +116,7 @@ __device__ __forceinline__ double box_n4(const T *P, int k, int L) {
 
 struct CGShared {
 	double T[CG_MAX_D + 1], iT[CG_MAX_D + 1];
-	double red[8 * (CG_THREADS / 32)];
+	double red[8 * (CG_THREADS / 32 + 1)];
 	double tot[8];
 	double rz[2], thr[2], bn2[2], rn2[2], alpha[2], beta[2];
 	int act[2], it[2], first, zero[2];

@@ -107,7 +107,9 @@ __device__ inline int box_site(const CellDev &c, int sx, int sy, int L) {
 __host__ __device__ inline int table_base(int l) { return (l * (l - 1)) / 2; }
 
 // Deterministic block-wide sum of NV doubles per thread (fixed shuffle tree).
-// `scratch` holds NV * (blockDim/32) doubles.  Result valid in every thread.
+// `scratch` holds NV * (blockDim/32 + 1) doubles.  Result valid in every thread.
+// Only warp 0 combines the per-warp partials: on GB300 every FP64 warp
+// instruction is expensive, so no thread repeats that work.
 template<int NV>
 __device__ inline void block_sum(double (&v)[NV], double *scratch) {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -122,12 +124,18 @@ __device__ inline void block_sum(double (&v)[NV], double *scratch) {
 		for(int i = 0; i < NV; i++) scratch[i * nw + warp] = v[i];
 	}
 	__syncthreads();
+	if(warp == 0) {
 #pragma unroll
-	for(int i = 0; i < NV; i++) {
-		double s = 0.0;
-		for(int w = 0; w < nw; w++) s += scratch[i * nw + w];
-		v[i] = s;
+		for(int i = 0; i < NV; i++) {
+			double s = lane < nw ? scratch[i * nw + lane] : 0.0;
+#pragma unroll
+			for(int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+			if(lane == 0) scratch[NV * nw + i] = s;
+		}
 	}
+	__syncthreads();
+#pragma unroll
+	for(int i = 0; i < NV; i++) v[i] = scratch[NV * nw + i];
 	__syncthreads();
 }
 

@@ -125,6 +125,28 @@ def record_cli():
     np.savez_compressed(os.path.join(HERE, "cli_polar.npz"), **out)
 
 
+def record_confgenerator():
+    """The reference's confGenerator on three placement modes: byte-exact
+    goldens for rheocell_gb300/_build/confgenerator."""
+    out = {}
+    for mode, inter in (("random", "wetmodel"), ("lattice", "wetpolarmodel"), ("cluster", "wetpolarmodel")):
+        d = tempfile.mkdtemp(prefix="rc_golden_")
+        try:
+            with open(os.path.join(d, "topo.top"), "w") as f:
+                f.write("6 1\n0 1 0 1 0 1\n")
+            inp = ("interaction_type = %s\nR = 8\nseed = 77\ntopology = topo.top\nconf_file = ref.dat\n"
+                   "trajectory_file = t.dat\ninitial_configuration_type = %s\nn_rows = 2\nn_columns = 3\n" % (inter, mode))
+            with open(os.path.join(d, "input"), "w") as f:
+                f.write(inp)
+            subprocess.run([os.path.join(refdump.REF_DIR, "confGenerator_exact"), "input", "80"], cwd=d,
+                           capture_output=True, check=True)
+            out[mode + "_input"] = np.array(inp)
+            out[mode + "_conf"] = np.array(open(os.path.join(d, "ref.dat")).read())
+        finally:
+            shutil.rmtree(d, ignore_errors=True)
+    np.savez_compressed(os.path.join(HERE, "confgenerator.npz"), **out)
+
+
 def main():
     if not refdump.have_reference("exact"):
         subprocess.check_call(["make", "-C", os.path.join(ROOT, "oracle"), "-j8"])
@@ -135,6 +157,7 @@ def main():
                                                                 sorted(set(zip(recs[-1]["lx"], recs[-1]["ly"]))), sz / 1024))
     print("overlap", record_overlap())
     record_cli()
+    record_confgenerator()
     print("cli_polar %.0f KB" % (os.path.getsize(os.path.join(HERE, "cli_polar.npz")) / 1024))
 
 
