@@ -10,7 +10,7 @@ A "step" is one FD_CPUBackend::sim_step (Heun predictor + corrector, two
 force evaluations, four viscous solves).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--workload wet256|dry140] [--precision double|mixed]
+                  [--workload wet256|dry140|ensemble64] [--precision double|mixed]
 
 Prints one JSON line (rank 0).  `value` is site-updates/s over all ranks with
 the state resident on the device, timed with CUDA events per step on the
@@ -46,15 +46,37 @@ def workload(name):
     if name == "dry140":
         return dict(name="dry polar MPF 140x140, 100 cells, R=8, 41x41 patches, wetpolarmodel friction_cell=0",
                     L=140, n=100, params=g.DRY_POLAR, seed=1)
+    if name == "ensemble64":
+        return dict(name="ensemble of 64 dry polar monolayers, box side uniform in 96-256 (numpy seed 64), "
+                         "N = round(0.75 L^2 / (pi 8^2)) cells each, R=8, 41x41 patches, seeds 1000-1063, FP64",
+                    members=ensemble_members(), params=g.DRY_POLAR, seed=1000)
     raise SystemExit("unknown workload %s" % name)
 
 
+def ensemble_members(count=64, seed=64, R=8.0):
+    """(L, N, seed) of each ensemble member: L uniform in [96, 256], N at 75%
+    area fraction of radius-R discs."""
+    import math
+    import numpy as np
+    sides = np.random.default_rng(seed).integers(96, 257, size=count)
+    return [(int(L), int(round(0.75 * L * L / (math.pi * R * R))), 1000 + i) for i, L in enumerate(sides)]
+
+
 def make_case(w):
+    """[(keys, monolayer)] of the workload's members (one for a single box)."""
     from rheocell_gb300 import generator as g
-    from tests.common import build_inputs, case_from_monolayer
+    from tests.common import case_from_monolayer
+    if "members" in w:
+        out = []
+        for L, n, seed in w["members"]:
+            m = g.make_monolayer(L, n, seed=seed)
+            keys = {k: str(v) for k, v in w["params"].items()}
+            keys.update(seed=str(seed), box="square")
+            out.append((keys, m))
+        return out
     m = g.make_monolayer(w["L"], w["n"], seed=w["seed"])
     keys, m2 = case_from_monolayer(m, w["params"], seed=w["seed"])
-    return keys, m2
+    return [(keys, m2)]
 
 
 def measured_peaks():
@@ -136,17 +158,23 @@ def run_gb300(args, rank, world):
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     w = workload(args.workload)
-    keys, m = make_case(w)
+    members = make_case(w)
     prec = abi.RC_PRECISION_MIXED if args.precision == "mixed" else abi.RC_PRECISION_DOUBLE
-    p, cells = build_inputs(keys, m, precision=prec)
+    built = [build_inputs(keys, m, precision=prec) for keys, m in members]
     stream = torch.cuda.Stream(dev)  # a real stream: the engine's graphs cannot capture on the legacy one
     torch.cuda.set_stream(stream)
-    eng = engine.Engine(p, m.L, cells, device=dev)
+    if len(members) == 1:
+        p, cells = built[0]
+        eng = engine.Engine(p, members[0][1].L, cells, device=dev)
+    else:
+        eng = engine.Engine.batch(built[0][0], [(m.L, cells, p.rng_state) for (_, m), (p, cells)
+                                                in zip(members, built)], device=dev)
     eng.set_stream(stream.cuda_stream)
     eng.set_phase(1)
     lib = eng._lib
     S = eng.site_count()
-    L2 = m.L * m.L
+    L2 = sum(m.L * m.L for _, m in members)
+    n_cells = sum(m.n for _, m in members)
     # warm-up
     eng.step(max(args.warmup, 3) if args.warmup >= 0 else 3)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -246,7 +274,8 @@ def run_gb300(args, rank, world):
         "vs_baseline": None,
         "dtype": "f64" if args.precision == "double" else "f64 fields, f32 solve inner iterations",
         "data": "synthetic (seeded jittered lattice, tanh interfaces)",
-        "config": {"workload": w["name"], "L": m.L, "cells": m.n, "sites": S, "precision": args.precision,
+        "config": {"workload": w["name"], "L": [m.L for _, m in members] if len(members) > 1 else members[0][1].L,
+                   "monolayers": len(members), "cells": n_cells, "sites": S, "precision": args.precision,
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "flushed (256 MiB write) before every timed step"},
         "cg": {"solves": st.cg_solves, "iterations": st.cg_iterations, "max_iterations": st.cg_max_iterations,
@@ -267,33 +296,83 @@ def run_gb300(args, rank, world):
     if S_after != S:
         out["config"]["sites_after"] = S_after
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(args, w, keys, m)
+        out["cpu_baseline"] = cpu_baseline(args, w, members)
     return out
 
 
-def cpu_baseline(args, w, keys, m, budget_s=25.0, max_steps=None):
+def cpu_baseline(args, w, members, budget_s=25.0, max_steps=None):
     """The CPU restatement (oracle/, serial FP64, the reference's algorithm)
-    on the same workload, timed on this host for a bounded number of steps."""
+    on the same workload, timed on this host for a bounded sample: main-loop
+    steps of the single box, or for an ensemble one step of each member in
+    turn (creation untimed) until the budget is spent."""
     from oracle import oracle as orc
     from tests.common import build_inputs
     orc.build()
-    p, cells = build_inputs(keys, m)
-    sim = orc.OracleSim(p, m.L, cells)
-    sim.set_phase(1)
+    sites = 0
+    el = 0.0
     steps = 0
-    t0 = time.perf_counter()
-    while True:
-        sim.step(1)
-        steps += 1
-        el = time.perf_counter() - t0
-        if el >= budget_s or (max_steps and steps >= max_steps):
-            break
-        if el / steps * (steps + 1) > budget_s * 1.5:
-            break
-    S = sim.site_count() if hasattr(sim, "site_count") else m.sites
-    sim.close()
-    return {"value": m.sites * steps / el, "unit": "site-updates/s", "cores": 1, "kind": "port",
-            "sample": "%d main-loop step(s) of the same workload, %.1f s wall" % (steps, el)}
+    if len(members) == 1:
+        keys, m = members[0]
+        p, cells = build_inputs(keys, m)
+        sim = orc.OracleSim(p, m.L, cells)
+        sim.set_phase(1)
+        t0 = time.perf_counter()
+        while True:
+            sim.step(1)
+            steps += 1
+            el = time.perf_counter() - t0
+            if el >= budget_s or (max_steps and steps >= max_steps):
+                break
+            if el / steps * (steps + 1) > budget_s * 1.5:
+                break
+        sites = m.sites * steps
+        sim.close()
+        sample = "%d main-loop step(s) of the same workload, %.1f s wall" % (steps, el)
+    else:
+        # independent members spread over the host cores (spawned workers),
+        # each timing its own main-loop steps; aggregate = sum over workers of
+        # work / step time (all workers run concurrently)
+        import multiprocessing as mp
+        cores = max(1, min(os.cpu_count() or 1, len(members)))
+        per_member = budget_s * cores / len(members)
+        groups = [[] for _ in range(cores)]
+        for i, (keys, m) in enumerate(members):
+            groups[i % cores].append((keys, m, per_member))
+        with mp.get_context("spawn").Pool(cores) as pool:
+            res = pool.map(_ensemble_worker, groups)
+        value = sum(w / t for w, t, _ in res if t > 0)
+        steps = sum(n for _, _, n in res)
+        el = max(t for _, t, _ in res)
+        sample = ("%d main-loop steps over the %d members (>= 1 each, about %.1f s per member), %d worker "
+                  "processes, %.1f s of stepping per worker" % (steps, len(members), per_member, cores, el))
+        return {"value": value, "unit": "site-updates/s", "cores": cores, "kind": "port", "sample": sample}
+    return {"value": sites / el, "unit": "site-updates/s", "cores": 1, "kind": "port", "sample": sample}
+
+
+def _ensemble_worker(group):
+    """Step each (keys, monolayer, seconds) of a group with the oracle;
+    returns (site-updates, stepping seconds, steps)."""
+    sys.path.insert(0, ROOT)
+    from oracle import oracle as orc
+    from tests.common import build_inputs
+    work, el, n = 0.0, 0.0, 0
+    for keys, m, budget in group:
+        p, cells = build_inputs(keys, m)
+        sim = orc.OracleSim(p, m.L, cells)
+        sim.set_phase(1)
+        t0 = time.perf_counter()
+        k = 0
+        while True:
+            sim.step(1)
+            k += 1
+            t = time.perf_counter() - t0
+            if t >= budget or t / k * (k + 1) > budget * 1.5:
+                break
+        sim.close()
+        el += t
+        work += m.sites * k
+        n += k
+    return work, el, n
 
 
 def run_reference(args, rank, world):
@@ -305,11 +384,10 @@ def run_reference(args, rank, world):
     if rank != 0:
         return None
     w = workload(args.workload)
-    keys, m = make_case(w)
-    from oracle import refdump
+    members = make_case(w)
     kind = "port"
     budget = 90.0
-    base = cpu_baseline(args, w, keys, m, budget_s=budget, max_steps=max(1, args.steps))
+    base = cpu_baseline(args, w, members, budget_s=budget, max_steps=max(1, args.steps))
     line = {
         "impl": "reference",
         "metric": METRIC,
@@ -323,7 +401,9 @@ def run_reference(args, rank, world):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded jittered lattice, tanh interfaces)",
-        "config": {"workload": w["name"], "L": m.L, "cells": m.n, "sites": m.sites, "precision": "double"},
+        "config": {"workload": w["name"], "L": [m.L for _, m in members] if len(members) > 1 else members[0][1].L,
+                   "monolayers": len(members), "cells": sum(m.n for _, m in members),
+                   "sites": sum(m.sites for _, m in members), "precision": "double"},
         "cpu_baseline": dict(base, kind=kind),
         "e2e": {"value": base["value"], "unit": "site-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -336,7 +416,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="wet256", choices=["wet256", "dry140"])
+    ap.add_argument("--workload", default="wet256", choices=["wet256", "dry140", "ensemble64"])
     ap.add_argument("--precision", default="double", choices=["double", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

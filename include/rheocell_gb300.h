@@ -157,6 +157,21 @@ int rc_create(const rc_params *params, const rc_box *box, int n_cells,
               const rc_cell_host *cells, int device, rc_engine **out);
 
 /*
+ * Create an engine that advances n_layers independent monolayers together
+ * (an ensemble: every launch covers all of them).  Layer l has box boxes[l]
+ * and the next n_cells_per_layer[l] entries of `cells` (layer-major);
+ * rng_states[l] is its drand48 state (NULL: params->rng_state for all).  All
+ * layers share `params`.  Batches are provided for dry evaluations
+ * (friction_cell = 0 in both phases); downloads and uploads address the cells
+ * in the same layer-major order.  A monolayer simulation is a batch of one.
+ */
+int rc_batch_create(const rc_params *params, int n_layers, const rc_box *boxes, const int *n_cells_per_layer,
+                    const rc_cell_host *cells, const unsigned long long *rng_states, int device, rc_engine **out);
+
+/* Number of monolayers the engine advances. */
+int rc_layer_count(const rc_engine *e);
+
+/*
  * Advance n_steps time steps (FD_CPUBackend::sim_step,
  * src/Backends/FD_CPUBackend.cpp:134-160, called n_steps times).  stats may
  * be NULL.  Returns after the work is complete on the device.

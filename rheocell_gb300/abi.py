@@ -121,6 +121,11 @@ def declare(lib: C.CDLL, prefix: str) -> C.CDLL:
         lib.rc_download_phi.restype = C.c_int
         lib.rc_upload_phi.argtypes = [vp, DP, C.c_longlong]
         lib.rc_upload_phi.restype = C.c_int
+        lib.rc_batch_create.argtypes = [C.POINTER(RcParams), C.c_int, C.POINTER(RcBox), C.POINTER(C.c_int),
+                                        C.POINTER(RcCellHost), C.POINTER(C.c_ulonglong), C.c_int, C.POINTER(vp)]
+        lib.rc_batch_create.restype = C.c_int
+        lib.rc_layer_count.argtypes = [vp]
+        lib.rc_layer_count.restype = C.c_int
         lib.rc_set_timing.argtypes = [vp, C.c_int]
         lib.rc_set_timing.restype = C.c_int
         lib.rc_timers.argtypes = [vp, DP, C.POINTER(C.c_longlong), C.c_int]
@@ -132,7 +137,7 @@ def declare(lib: C.CDLL, prefix: str) -> C.CDLL:
 
 
 # Every symbol the header declares (checked by the CPU test suite).
-EXPORTED = ["rc_abi_version", "rc_create", "rc_step", "rc_step_async", "rc_wait", "rc_set_phase",
+EXPORTED = ["rc_abi_version", "rc_create", "rc_batch_create", "rc_layer_count", "rc_step", "rc_step_async", "rc_wait", "rc_set_phase",
             "rc_get_sizes", "rc_download", "rc_upload", "rc_download_phi", "rc_upload_phi", "rc_set_stream",
             "rc_set_timing", "rc_timers", "rc_site_count", "rc_last_error", "rc_destroy"]
 

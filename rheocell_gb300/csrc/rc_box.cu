@@ -26,9 +26,18 @@ __global__ void __launch_bounds__(BIN_X *BIN_Y) box_gather_kernel(const BoxArgs 
 	__shared__ int s_cx[BIN_CAP], s_cy[BIN_CAP], s_lx[BIN_CAP], s_ly[BIN_CAP], s_ox[BIN_CAP], s_oy[BIN_CAP],
 	    s_start[BIN_CAP];
 	__shared__ double s_q00[BIN_CAP], s_q01[BIN_CAP];
+	// layer of this bin: the last layer whose bin_off <= blockIdx.x
+	int lo = 0, hi = a.n_layers - 1;
+	while(lo < hi) {
+		const int mid = (lo + hi + 1) / 2;
+		if(a.layers[mid].bin_off <= (int) blockIdx.x) lo = mid;
+		else hi = mid - 1;
+	}
+	const LayerDev lay = a.layers[lo];
 	const int b = blockIdx.x;
-	const int bxi = b % a.nbx, byi = b / a.nbx;
-	const int L = a.L;
+	const int lb = b - lay.bin_off;
+	const int bxi = lb % lay.nbx, byi = lb / lay.nbx;
+	const int L = lay.L;
 	int count = a.bin_count[b];
 	if(count > BIN_CAP) count = BIN_CAP;  // overflow already flagged by the appender
 	const int t = threadIdx.x;
@@ -58,7 +67,8 @@ __global__ void __launch_bounds__(BIN_X *BIN_Y) box_gather_kernel(const BoxArgs 
 	const int x = bxi * BIN_X + (t % BIN_X);
 	const int y = byi * BIN_Y + (t / BIN_X);
 	if(x >= L || y >= L) return;
-	const int k = x + y * L;
+	const int kl = x + y * L;                      // site in the layer's box
+	const long long k = lay.box_off + kl;          // index into the batch's box arrays
 	const size_t L2 = (size_t) L * (size_t) L;
 	double p2 = 0.0, q0 = 0.0, q1 = 0.0;
 	int n = 0;
@@ -115,7 +125,7 @@ __global__ void bookkeeping_kernel(DevStatus *st, int restart_every, int solve_f
 }
 
 void launch_box_gather(const BoxArgs &a, cudaStream_t s) {
-	box_gather_kernel<<<a.nbx * a.nby, BIN_X * BIN_Y, 0, s>>>(a);
+	box_gather_kernel<<<a.total_bins, BIN_X * BIN_Y, 0, s>>>(a);
 	if(a.bookkeeping) bookkeeping_kernel<<<1, 1, 0, s>>>(a.st, a.restart_every, a.solve_follows);
 }
 

@@ -79,8 +79,11 @@ __device__ inline BoxNb box_nb(int k, int L) {
 }
 
 // Appends cell ci to the bins its patch rectangle overlaps (periodic).
-__device__ void append_bins(const CellDev &c, int ci, int L, int *bin_count, int *bin_cells, int nbx, int nby,
+__device__ void append_bins(const CellDev &c, int ci, const LayerDev &ly, int *bin_count_all, int *bin_cells_all,
                             DevStatus *st) {
+	const int L = ly.L, nbx = ly.nbx;
+	int *bin_count = bin_count_all + ly.bin_off;
+	int *bin_cells = bin_cells_all + (size_t) ly.bin_off * BIN_CAP;
 	// patch sides are <= MAX_TABLE_SIDE (128): at most 5 x-bins and 17 y-bins
 	int bxs[8], bys[24];
 	int nbxs = 0, nbys = 0;
@@ -123,8 +126,8 @@ __device__ void append_bins(const CellDev &c, int ci, int L, int *bin_count, int
 
 // set_positions (Fields/MultiPhaseField.cpp:223-310).  The resize branch only
 // records the new geometry; the field copy runs in the repack kernels.
-__device__ void set_positions_dev(CellDev &c, const DevParams &P, DevStatus *st, int ci) {
-	const int L = P.L, border = P.border;
+__device__ void set_positions_dev(CellDev &c, const DevParams &P, int L, DevStatus *st, int ci) {
+	const int border = P.border;
 	if(c.xl >= border && c.yb >= border) {
 		const int site = box_el(c.corner, (int) c.comx, (int) c.comy, L);
 		c.comy = (int) (site / L) + (c.comy - (int) c.comy);
@@ -244,7 +247,11 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 		for(int i = threadIdx.x; i < (int) (sizeof(CellDev) / 4); i += blockDim.x) dst[i] = src[i];
 	}
 	__syncthreads();
-	const int n = c.n, lx = c.lx, ly = c.ly, L = a.P.L, start = c.start;
+	const LayerDev lay = a.layers[c.layer];
+	const int n = c.n, lx = c.lx, ly = c.ly, L = lay.L, start = c.start;
+	const double *phi2 = a.phi2 + lay.box_off;
+	const double *sq00 = a.sq00 + lay.box_off;
+	const double *sq01 = a.sq01 + lay.box_off;
 	if(n > a.smem_n) {
 		if(threadIdx.x == 0) {
 			atomicOr(&a.st->err, ERR_CAPACITY);
@@ -303,11 +310,11 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 			const double pr = sphi[nb.r], pl = sphi[nb.l], pu_ = sphi[nb.u], pd = sphi[nb.d];
 			const double dx = .5 * (pr - pl), dy = .5 * (pu_ - pd);
 			const int k = box_site(c, x, y, L);
-			const double p2 = a.phi2[k];
+			const double p2 = phi2[k];
 			double ls = 0.0;
 			if(omega != 0.0 && MODEL != M_SIMPLE) {
 				const BoxNb kb = box_nb(k, L);
-				ls = a.phi2[kb.r] + a.phi2[kb.u] + a.phi2[kb.l] + a.phi2[kb.d] - 4. * p2;
+				ls = phi2[kb.r] + phi2[kb.u] + phi2[kb.l] + phi2[kb.d] - 4. * p2;
 			}
 			double mu = 0.0;
 			if(MODEL == M_SIMPLE) {
@@ -400,8 +407,8 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 				const BoxNb kb = box_nb(k, L);
 				const double fsx = -(c.q00 * dx + c.q01 * dy);
 				const double fsy = -(c.q01 * dx - c.q00 * dy);
-				const double fix = -(0.5 * (a.sq00[kb.r] - a.sq00[kb.l]) + 0.5 * (a.sq01[kb.u] - a.sq01[kb.d])) - fsx;
-				const double fiy = -(0.5 * (a.sq01[kb.r] - a.sq01[kb.l]) - 0.5 * (a.sq00[kb.u] - a.sq00[kb.d])) - fsy;
+				const double fix = -(0.5 * (sq00[kb.r] - sq00[kb.l]) + 0.5 * (sq01[kb.u] - sq01[kb.d])) - fsx;
+				const double fiy = -(0.5 * (sq01[kb.r] - sq01[kb.l]) - 0.5 * (sq00[kb.u] - sq00[kb.d])) - fsy;
 				if(MODEL == M_NEMATIC) {
 					vx = div_rn(mu * dx + fsx * zs + fix * zi, fr, rfr);
 					vy = div_rn(mu * dy + fsy * zs + fiy * zi, fr, rfr);
@@ -624,10 +631,10 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 				atomicOr(&a.st->err, ERR_NONFINITE);
 				a.st->err_where = ci;
 			}
-			if(UPD == UP_CORR) set_positions_dev(c, P, a.st, ci);
+			if(UPD == UP_CORR) set_positions_dev(c, P, L, a.st, ci);
 			directed_forces_dev(c, P, pu, UPD == UP_PRED, a.st, ci);
 			if(UPD == UP_CORR) {
-				append_bins(c, ci, L, a.bin_count, a.bin_cells, a.nbx, a.nby, a.st);
+				append_bins(c, ci, lay, a.bin_count, a.bin_cells, a.st);
 				atomicMax(&a.st->max_n, c.n);
 			}
 		}
@@ -703,7 +710,10 @@ void launch_cell_kernel(int model, int eval, int upd, const CellArgs &a, cudaStr
 __constant__ unsigned long long c_jumpA[2 * CELL_THREADS + 1];
 __constant__ unsigned long long c_jumpC[2 * CELL_THREADS + 1];
 
-__global__ void __launch_bounds__(CELL_THREADS) rng_kernel(CellDev *cells, int N, DevStatus *st) {
+__global__ void __launch_bounds__(CELL_THREADS) rng_kernel(CellDev *cells_all, LayerDev *layers, DevStatus *st) {
+	LayerDev *lay = &layers[blockIdx.x];
+	CellDev *cells = cells_all + lay->cell_lo;
+	const int N = lay->cell_hi - lay->cell_lo;
 	__shared__ int s_scan[CELL_THREADS];
 	__shared__ unsigned long long s_state;
 	__shared__ int s_produced, s_has, s_last;
@@ -711,9 +721,9 @@ __global__ void __launch_bounds__(CELL_THREADS) rng_kernel(CellDev *cells, int N
 	const unsigned long long M = (1ULL << 48) - 1;
 	const int t = threadIdx.x;
 	if(t == 0) {
-		s_state = st->rng_state;
-		s_has = st->rng_has;
-		s_cached = st->rng_cached;
+		s_state = lay->rng_state;
+		s_has = lay->rng_has;
+		s_cached = lay->rng_cached;
 		s_produced = 0;
 		if(s_has && N > 0) {
 			cells[0].gauss = s_cached;
@@ -775,14 +785,14 @@ __global__ void __launch_bounds__(CELL_THREADS) rng_kernel(CellDev *cells, int N
 	}
 	if(t == 0) {
 		if(s_produced < N) atomicOr(&st->err, ERR_NONFINITE);
-		st->rng_state = s_state;
-		st->rng_has = s_has;
-		st->rng_cached = s_cached;
+		lay->rng_state = s_state;
+		lay->rng_has = s_has;
+		lay->rng_cached = s_cached;
 	}
 }
 
-void launch_rng(CellDev *cells, int N, DevStatus *st, cudaStream_t s) {
-	rng_kernel<<<1, CELL_THREADS, 0, s>>>(cells, N, st);
+void launch_rng(CellDev *cells, LayerDev *layers, int n_layers, DevStatus *st, cudaStream_t s) {
+	if(n_layers > 0) rng_kernel<<<n_layers, CELL_THREADS, 0, s>>>(cells, layers, st);
 }
 
 // One-time, per-device set-up that must not happen inside stream capture:
@@ -807,19 +817,19 @@ cudaError_t configure_kernels() {
 }
 
 // ----------------------------------------------------------------- bins ---
-__global__ void bins_kernel(const CellDev *cells, int N, int L, int *bin_count, int *bin_cells, int nbx, int nby,
+__global__ void bins_kernel(const CellDev *cells, const LayerDev *layers, int N, int *bin_count, int *bin_cells,
                             DevStatus *st) {
 	const int ci = blockIdx.x * blockDim.x + threadIdx.x;
 	if(ci >= N) return;
 	CellDev c = cells[ci];
-	append_bins(c, ci, L, bin_count, bin_cells, nbx, nby, st);
+	append_bins(c, ci, layers[c.layer], bin_count, bin_cells, st);
 	atomicMax(&st->max_n, c.n);
 }
 
-void launch_bins(CellDev *cells, int N, int L, int *bin_count, int *bin_cells, int nbx, int nby, DevStatus *st,
-                 cudaStream_t s) {
-	cudaMemsetAsync(bin_count, 0, sizeof(int) * (size_t) nbx * nby, s);
-	if(N > 0) bins_kernel<<<(N + 127) / 128, 128, 0, s>>>(cells, N, L, bin_count, bin_cells, nbx, nby, st);
+void launch_bins(CellDev *cells, const LayerDev *layers, int N, int *bin_count, int *bin_cells, int total_bins,
+                 DevStatus *st, cudaStream_t s) {
+	cudaMemsetAsync(bin_count, 0, sizeof(int) * (size_t) total_bins, s);
+	if(N > 0) bins_kernel<<<(N + 127) / 128, 128, 0, s>>>(cells, layers, N, bin_count, bin_cells, st);
 }
 
 // --------------------------------------------------------------- repack ---
@@ -845,8 +855,8 @@ __global__ void repack_scan_kernel(CellDev *cells, int N, DevStatus *st, int *ne
 	}
 }
 
-__global__ void repack_copy_kernel(CellDev *cells, int N, DevStatus *st, const int *new_start, const double *phi,
-                                   double *out_phi, const double *rep, double *out_rep, int rep_on, int L,
+__global__ void repack_copy_kernel(CellDev *cells, const LayerDev *layers, int N, DevStatus *st, const int *new_start,
+                                   const double *phi, double *out_phi, const double *rep, double *out_rep, int rep_on,
                                    long long cap) {
 	if(st->resized == 0 || (st->err & ERR_CAPACITY)) return;
 	const int ci = blockIdx.x;
@@ -860,6 +870,7 @@ __global__ void repack_copy_kernel(CellDev *cells, int N, DevStatus *st, const i
 		return;
 	}
 	const int nlx = c.lx, nly = c.ly, nn = c.n, olx = c.old_lx, oly = c.old_ly;
+	const int L = layers[c.layer].L;
 	for(int q = threadIdx.x; q < nn; q += blockDim.x) {
 		out_phi[ns + q] = 0.0;
 		if(rep_on) out_rep[ns + q] = (q < olx * oly) ? rep[c.start + q] : 0.0;
@@ -933,8 +944,8 @@ void launch_repack(CellArgs a, double *scratch_phi, double *scratch_rep, long lo
 	// new_start lives behind the scratch buffers' tail (allocated by the engine)
 	int *new_start = reinterpret_cast<int *>(scratch_phi + cap);
 	repack_scan_kernel<<<1, 32, 0, s>>>(a.cells, a.N, a.st, new_start, cap);
-	repack_copy_kernel<<<a.N, CELL_THREADS, 0, s>>>(a.cells, a.N, a.st, new_start, a.phi_out, scratch_phi, a.rep,
-	                                                 scratch_rep, a.rep_on, a.P.L, cap);
+	repack_copy_kernel<<<a.N, CELL_THREADS, 0, s>>>(a.cells, a.layers, a.N, a.st, new_start, a.phi_out, scratch_phi,
+	                                                 a.rep, scratch_rep, a.rep_on, cap);
 	repack_finish_kernel<<<304, 256, 0, s>>>(a.cells, a.N, a.st, new_start, a.phi_out, scratch_phi, a.rep, scratch_rep,
 	                                         a.rep_on);
 	repack_done_kernel<<<(a.N + 255) / 256, 256, 0, s>>>(a.cells, a.N, a.st, new_start);

@@ -61,12 +61,35 @@ __device__ bool grid_reduce(const CGArgs &a, int nv, const double *v, double *ou
 	}
 	__syncthreads();
 	if(s_last) {
-		for(int i = 0; i < nv; i++) {
-			double acc[1] = {0.0};
-			for(unsigned b = threadIdx.x; b < nb; b += blockDim.x) acc[0] += ldcg(&a.partials[(size_t) i * nb + b]);
-			block_sum<1>(acc, red);
-			if(threadIdx.x == 0) a.scalars[SC_RED + i] = acc[0];
+		// all values in one block-wide reduction (fixed order: threads stride
+		// the block partials, then the fixed shuffle tree)
+		double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+		for(int i = 0; i < 8; i++)
+			if(i < nv)
+				for(unsigned b = threadIdx.x; b < nb; b += blockDim.x) acc[i] += ldcg(&a.partials[(size_t) i * nb + b]);
+		if(nv > 0) {
+			if(nv <= 2) {
+				double t[2] = {acc[0], acc[1]};
+				block_sum<2>(t, red);
+				acc[0] = t[0];
+				acc[1] = t[1];
+			}
+			else if(nv <= 4) {
+				double t[4] = {acc[0], acc[1], acc[2], acc[3]};
+				block_sum<4>(t, red);
+#pragma unroll
+				for(int i = 0; i < 4; i++) acc[i] = t[i];
+			}
+			else
+				block_sum<8>(acc, red);
+			if(threadIdx.x == 0) {
+#pragma unroll
+				for(int i = 0; i < 8; i++)
+					if(i < nv) a.scalars[SC_RED + i] = acc[i];
+			}
 		}
+		__syncthreads();
 		if(threadIdx.x == 0) {
 			__threadfence();
 			atomicExch(&a.bar[0], 0u);
@@ -116,7 +139,7 @@ __device__ __forceinline__ double box_n4(const T *P, int k, int L) {
 
 struct CGShared {
 	double T[CG_MAX_D + 1], iT[CG_MAX_D + 1];
-	double red[8 * (CG_THREADS / 32 + 1)];
+	double red[8 * (CG_THREADS / 32 + 1)];  // block_sum<8> scratch
 	double tot[8];
 	double rz[2], thr[2], bn2[2], rn2[2], alpha[2], beta[2];
 	int act[2], it[2], first, zero[2];
@@ -265,6 +288,43 @@ __device__ bool true_residual(const CGArgs &a, CGShared &sh, bool x_zero, bool t
 // and the box sums, U that of the solution accumulator; dot products are
 // FP64.  Updates use fused multiply-adds (the solve is not bitwise Eigen's in
 // any case: its reductions run in a different order).
+// Shuffle tree within each warp in the vectors' own precision (lane 0 ends
+// with the warp's sum).
+template<typename T, int NV>
+__device__ __forceinline__ void warp_tree(T (&w)[NV]) {
+#pragma unroll
+	for(int i = 0; i < NV; i++) {
+#pragma unroll
+		for(int o = 16; o > 0; o >>= 1) w[i] += __shfl_down_sync(0xffffffffu, w[i], o);
+	}
+}
+
+// Block sum of values already reduced within each warp (valid in lane 0),
+// FP64 across warps; result in every thread.
+template<int NV>
+__device__ inline void block_sum_warps(double (&v)[NV], double *scratch) {
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+	__syncthreads();
+	if(lane == 0) {
+#pragma unroll
+		for(int i = 0; i < NV; i++) scratch[i * nw + warp] = v[i];
+	}
+	__syncthreads();
+	if(warp == 0) {
+#pragma unroll
+		for(int i = 0; i < NV; i++) {
+			double t = lane < nw ? scratch[i * nw + lane] : 0.0;
+#pragma unroll
+			for(int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+			if(lane == 0) scratch[NV * nw + i] = t;
+		}
+	}
+	__syncthreads();
+#pragma unroll
+	for(int i = 0; i < NV; i++) v[i] = scratch[NV * nw + i];
+	__syncthreads();
+}
+
 template<typename T>
 __device__ __forceinline__ T fmaT(T a, T b, T c);
 template<>
@@ -366,8 +426,9 @@ __device__ bool cg_iterate(const CGArgs &a, CGShared &sh, T *rx, T *ry, T *px, T
 					w[1] = fmaT<T>(p, ap, w[1]);
 				}
 			}
+			warp_tree<T, 2>(w);
 			double v[2] = {(double) w[0], (double) w[1]};
-			block_sum<2>(v, sh.red);
+			block_sum_warps<2>(v, sh.red);
 			if(!grid_reduce(a, 2, v, sh.tot, sh.red)) return false;
 		}
 		if(threadIdx.x == 0) {

@@ -52,6 +52,7 @@ struct CellDev {
 	int corner, type, start, n;
 	int xl, yb, resized, old_lx;
 	int old_ly, old_offx, old_offy, old_corner;
+	int layer, pad_i;
 	double comx, comy, com_oldx, com_oldy;
 	double unrapx, unrapy, q00, q01;
 	double thq, thq_old, nqx, nqy;
@@ -59,6 +60,17 @@ struct CellDev {
 	double sumf, sumf_old, perim, s00;
 	double s01, trx, try_, tfx;
 	double tfy, gauss, pad0, pad1;
+};
+
+// One monolayer of a batch: its own periodic box, box arrays at box_off,
+// bins at bin_off, cells [cell_lo, cell_hi), and its own drand48 stream.
+struct LayerDev {
+	int L, nbx, nby, bin_off;
+	long long box_off;
+	int cell_lo, cell_hi;
+	unsigned long long rng_state;
+	int rng_has, pad;
+	double rng_cached;
 };
 
 // Device status word block (one per engine).

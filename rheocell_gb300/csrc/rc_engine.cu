@@ -52,7 +52,11 @@ struct rc_engine {
 	int max_n_host = 0;
 	int rep_on = 0;
 	int cg_blocks = 0;
-	int nbx = 0, nby = 0;
+	int nbx = 0, nby = 0;        // bins of layer 0 (single-monolayer solver paths)
+	int n_layers = 1, total_bins = 0;
+	long long total_box = 0;
+	std::vector<LayerDev> layers_h;
+	LayerDev *layers = nullptr;
 
 	CellDev *cells = nullptr;
 	double *phiA = nullptr, *phiB = nullptr, *dphi_old = nullptr, *mu = nullptr, *dxg = nullptr, *dyg = nullptr;
@@ -200,6 +204,7 @@ static CellArgs cell_args(rc_engine *e) {
 	a.bin_cells = e->bin_cells;
 	a.nbx = e->nbx;
 	a.nby = e->nby;
+	a.layers = e->layers;
 	a.st = e->st;
 	a.P = e->P;
 	a.rep_on = e->rep_on;
@@ -221,6 +226,9 @@ static void gather(rc_engine *e, const double *phi, int phase) {
 	b.bin_cells = e->bin_cells;
 	b.nbx = e->nbx;
 	b.nby = e->nby;
+	b.layers = e->layers;
+	b.n_layers = e->n_layers;
+	b.total_bins = e->total_bins;
 	b.want_q = (e->P.model == M_NEMATIC || e->P.model == M_WET);
 	b.want_cover = wet_phase(e, phase);
 	b.check_overlap = (e->P.model == M_POLAR || e->P.model == M_WET);
@@ -310,7 +318,7 @@ static void one_step(rc_engine *e) {
 	cudaStream_t s = e->stream;
 	if(e->P.model == M_POLAR) {
 		StageMark sm(e, RC_TIMER_RNG);
-		launch_rng(e->cells, e->N, e->st, s);
+		launch_rng(e->cells, e->layers, e->n_layers, e->st, s);
 		e->launches += 1;
 	}
 	CellArgs a = cell_args(e);
@@ -330,7 +338,7 @@ static void one_step(rc_engine *e) {
 	}
 	e->launches += 1;
 	gather(e, e->phiB, cur);
-	cudaMemsetAsync(e->bin_count, 0, sizeof(int) * (size_t) e->nbx * e->nby, s);
+	cudaMemsetAsync(e->bin_count, 0, sizeof(int) * (size_t) e->total_bins, s);
 	CellArgs c = cell_args(e);
 	c.phi_old = e->phiA;
 	c.phi_out = e->phiA;
@@ -493,8 +501,9 @@ static int check_status(rc_engine *e, rc_step_stats *stats) {
 	return RC_OK;
 }
 
-static void host_cell(const rc_cell_host &h, CellDev &c, int start) {
+static void host_cell(const rc_cell_host &h, CellDev &c, int start, int layer = 0) {
 	memset(&c, 0, sizeof(c));
+	c.layer = layer;
 	c.lx = h.lsub_x;
 	c.ly = h.lsub_y;
 	c.offx = h.offset_x;
@@ -552,32 +561,69 @@ int rc_abi_version(void) { return RC_ABI_VERSION; }
 
 int rc_create(const rc_params *params, const rc_box *box, int n_cells, const rc_cell_host *cells, int device,
               rc_engine **out) {
+	if(!params) return set_err(nullptr, RC_ERR_INVALID, "invalid arguments");
+	const unsigned long long rs = params->rng_state;
+	return rc_batch_create(params, 1, box, &n_cells, cells, &rs, device, out);
+}
+
+int rc_batch_create(const rc_params *params, int n_layers, const rc_box *boxes, const int *n_cells_per_layer,
+                    const rc_cell_host *cells, const unsigned long long *rng_states, int device, rc_engine **out) {
 	if(!out) return set_err(nullptr, RC_ERR_INVALID, "out is NULL");
 	*out = nullptr;
-	if(!params || !box || (n_cells > 0 && !cells) || n_cells < 0)
+	if(!params || !boxes || !n_cells_per_layer || n_layers < 1)
 		return set_err(nullptr, RC_ERR_INVALID, "invalid arguments");
-	if(box->Lx != box->Ly || box->Lx < 3 || box->Lx > 46340)
-		return set_err(nullptr, RC_ERR_INVALID, "The box in the configuration file is not a square (%dx%d)", box->Lx, box->Ly);
 	if(params->model < RC_SIMPLEFIELD || params->model > RC_WETMODEL)
 		return set_err(nullptr, RC_ERR_INVALID, "unknown interaction model %d", params->model);
 	if(params->anchoring) return set_err(nullptr, RC_ERR_UNSUPPORTED, "anchoring is not provided");
 	if(params->precision != RC_PRECISION_DOUBLE && params->precision != RC_PRECISION_MIXED)
 		return set_err(nullptr, RC_ERR_INVALID, "unknown precision %d", params->precision);
-	const int L = box->Lx;
+	const bool any_wet = (params->model == RC_WETMODEL || params->model == RC_WETPOLARMODEL) &&
+	                     (params->friction_cell[0] != 0.0 || params->friction_cell[1] != 0.0);
+	if(n_layers > 1 && any_wet)
+		return set_err(nullptr, RC_ERR_UNSUPPORTED, "batches of monolayers are provided for dry evaluations only");
+	std::vector<LayerDev> layers((size_t) n_layers);
+	int n_cells = 0, total_bins = 0;
+	long long total_box = 0;
+	for(int l = 0; l < n_layers; l++) {
+		const rc_box &bx = boxes[l];
+		if(bx.Lx != bx.Ly || bx.Lx < 3 || bx.Lx > 46340)
+			return set_err(nullptr, RC_ERR_INVALID, "The box in the configuration file is not a square (%dx%d)", bx.Lx, bx.Ly);
+		if(n_cells_per_layer[l] < 0) return set_err(nullptr, RC_ERR_INVALID, "negative cell count");
+		LayerDev &ly = layers[(size_t) l];
+		memset(&ly, 0, sizeof(ly));
+		ly.L = bx.Lx;
+		ly.nbx = (bx.Lx + BIN_X - 1) / BIN_X;
+		ly.nby = (bx.Lx + BIN_Y - 1) / BIN_Y;
+		ly.bin_off = total_bins;
+		ly.box_off = total_box;
+		ly.cell_lo = n_cells;
+		ly.cell_hi = n_cells + n_cells_per_layer[l];
+		ly.rng_state = (rng_states ? rng_states[l] : params->rng_state) & ((1ULL << 48) - 1);
+		ly.rng_has = (n_layers == 1) ? params->rng_has_cached : 0;
+		ly.rng_cached = (n_layers == 1) ? params->rng_cached : 0.0;
+		total_bins += ly.nbx * ly.nby;
+		total_box += (long long) bx.Lx * bx.Lx;
+		n_cells += n_cells_per_layer[l];
+	}
+	if(n_cells > 0 && !cells) return set_err(nullptr, RC_ERR_INVALID, "cells is NULL");
 	long long S = 0;
 	int max_n = 0;
-	for(int i = 0; i < n_cells; i++) {
-		const rc_cell_host &h = cells[i];
-		if(h.lsub_x <= 0 || h.lsub_y <= 0 || h.lsub_x > L || h.lsub_y > L || h.lsub_x > MAX_TABLE_SIDE ||
-		   h.lsub_y > MAX_TABLE_SIDE)
-			return set_err(nullptr, RC_ERR_INVALID, "cell %d: patch %dx%d does not fit the box/tables", i, h.lsub_x, h.lsub_y);
-		if(h.offset_x < 0 || h.offset_x >= h.lsub_x || h.offset_y < 0 || h.offset_y >= h.lsub_y)
-			return set_err(nullptr, RC_ERR_INVALID, "cell %d: offset out of range", i);
-		if(h.corner < 0 || h.corner >= L * L) return set_err(nullptr, RC_ERR_INVALID, "cell %d: corner out of box", i);
-		if(!h.phi) return set_err(nullptr, RC_ERR_INVALID, "cell %d: phi is NULL", i);
-		S += (long long) h.lsub_x * h.lsub_y;
-		max_n = std::max(max_n, h.lsub_x * h.lsub_y);
+	for(int l = 0; l < n_layers; l++) {
+		const int L = layers[(size_t) l].L;
+		for(int i = layers[(size_t) l].cell_lo; i < layers[(size_t) l].cell_hi; i++) {
+			const rc_cell_host &h = cells[i];
+			if(h.lsub_x <= 0 || h.lsub_y <= 0 || h.lsub_x > L || h.lsub_y > L || h.lsub_x > MAX_TABLE_SIDE ||
+			   h.lsub_y > MAX_TABLE_SIDE)
+				return set_err(nullptr, RC_ERR_INVALID, "cell %d: patch %dx%d does not fit the box/tables", i, h.lsub_x, h.lsub_y);
+			if(h.offset_x < 0 || h.offset_x >= h.lsub_x || h.offset_y < 0 || h.offset_y >= h.lsub_y)
+				return set_err(nullptr, RC_ERR_INVALID, "cell %d: offset out of range", i);
+			if(h.corner < 0 || h.corner >= L * L) return set_err(nullptr, RC_ERR_INVALID, "cell %d: corner out of box", i);
+			if(!h.phi) return set_err(nullptr, RC_ERR_INVALID, "cell %d: phi is NULL", i);
+			S += (long long) h.lsub_x * h.lsub_y;
+			max_n = std::max(max_n, h.lsub_x * h.lsub_y);
+		}
 	}
+	const int L = layers[0].L;
 	if(S >= (1LL << 31) - (1LL << 24)) return set_err(nullptr, RC_ERR_CAPACITY, "too many sites (%lld)", S);
 
 	rc_engine *e = new rc_engine();
@@ -586,6 +632,10 @@ int rc_create(const rc_params *params, const rc_box *box, int n_cells, const rc_
 	e->L = L;
 	e->N = n_cells;
 	e->S = S;
+	e->n_layers = n_layers;
+	e->layers_h = layers;
+	e->total_bins = total_bins;
+	e->total_box = total_box;
 	e->S_cap = std::min((1LL << 31) - 1, S + std::max(S / 4, 65536LL));
 	e->max_n_host = max_n;
 	int rc;
@@ -635,9 +685,9 @@ int rc_create(const rc_params *params, const rc_box *box, int n_cells, const rc_
 		e->ph[k].beta = params->beta[k];
 	}
 	e->rep_on = (P.model == M_POLAR) && (params->J_Q[0] != 0.0 || params->J_Q[1] != 0.0);
-	e->nbx = (L + BIN_X - 1) / BIN_X;
-	e->nby = (L + BIN_Y - 1) / BIN_Y;
-	const size_t L2 = (size_t) L * L;
+	e->nbx = layers[0].nbx;
+	e->nby = layers[0].nby;
+	const size_t L2 = (size_t) total_box;  // box arrays of all layers (one layer for the wet paths)
 	const size_t cap = (size_t) e->S_cap;
 	const bool wet = (P.model == M_POLAR || P.model == M_WET);
 	if((rc = dalloc(e, &e->cells, (size_t) std::max(n_cells, 1))) ||
@@ -646,8 +696,9 @@ int rc_create(const rc_params *params, const rc_box *box, int n_cells, const rc_
 	   (rc = dalloc(e, &e->vx, cap)) || (rc = dalloc(e, &e->vy, cap)) || (rc = dalloc(e, &e->mapg, cap)) ||
 	   (rc = dalloc(e, &e->phi2, L2)) || (rc = dalloc(e, &e->sq00, L2)) || (rc = dalloc(e, &e->sq01, L2)) ||
 	   (rc = dalloc(e, &e->cnt, L2)) ||
-	   (rc = dalloc(e, &e->bin_count, (size_t) e->nbx * e->nby)) ||
-	   (rc = dalloc(e, &e->bin_cells, (size_t) e->nbx * e->nby * BIN_CAP)) ||
+	   (rc = dalloc(e, &e->bin_count, (size_t) total_bins)) ||
+	   (rc = dalloc(e, &e->bin_cells, (size_t) total_bins * BIN_CAP)) ||
+	   (rc = dalloc(e, &e->layers, (size_t) n_layers)) ||
 	   (rc = dalloc(e, &e->tab_cos, (size_t) table_base(MAX_TABLE_SIDE + 1))) ||
 	   (rc = dalloc(e, &e->tab_sin, (size_t) table_base(MAX_TABLE_SIDE + 1))) ||
 	   (rc = dalloc(e, &e->st, 1)) ||
@@ -693,11 +744,14 @@ int rc_create(const rc_params *params, const rc_box *box, int n_cells, const rc_
 		std::vector<double> phi((size_t) S);
 		long long start = 0;
 		for(int i = 0; i < n_cells; i++) {
-			host_cell(cells[i], hc[i], (int) start);
+			int layer = 0;
+			while(layer + 1 < n_layers && i >= layers[(size_t) layer].cell_hi) layer++;
+			host_cell(cells[i], hc[i], (int) start, layer);
 			memcpy(&phi[(size_t) start], cells[i].phi, sizeof(double) * (size_t) hc[i].n);
 			start += hc[i].n;
 		}
 		CUDA_TRY(e, cudaMemcpy(e->cells, hc.data(), sizeof(CellDev) * (size_t) std::max(n_cells, 1), cudaMemcpyHostToDevice));
+		CUDA_TRY(e, cudaMemcpy(e->layers, layers.data(), sizeof(LayerDev) * (size_t) n_layers, cudaMemcpyHostToDevice));
 		if(S) CUDA_TRY(e, cudaMemcpy(e->phiA, phi.data(), sizeof(double) * (size_t) S, cudaMemcpyHostToDevice));
 		DevStatus h;
 		memset(&h, 0, sizeof(h));
@@ -705,15 +759,12 @@ int rc_create(const rc_params *params, const rc_box *box, int n_cells, const rc_
 		h.S_rows = 0;
 		h.restart = 0;
 		h.max_n = max_n;
-		h.rng_state = params->rng_state & ((1ULL << 48) - 1);
-		h.rng_has = params->rng_has_cached;
-		h.rng_cached = params->rng_cached;
 		CUDA_TRY(e, cudaMemcpy(e->st, &h, sizeof(h), cudaMemcpyHostToDevice));
 	}
 	if((rc = choose_smem(e))) return bail(rc);
 	if(n_cells > 0) {
 		init_sums_kernel<<<(n_cells + 63) / 64, 64, 0, e->stream>>>(e->cells, e->phiA, n_cells);
-		launch_bins(e->cells, n_cells, L, e->bin_count, e->bin_cells, e->nbx, e->nby, e->st, e->stream);
+		launch_bins(e->cells, e->layers, n_cells, e->bin_count, e->bin_cells, total_bins, e->st, e->stream);
 		// FD_CPUBackend::init: first force evaluation with the phase-0 parameters
 		evaluate_end(e, e->phiA, 0);
 	}
@@ -879,7 +930,7 @@ int rc_upload(rc_engine *e, const rc_cell_host *cells, unsigned mask) {
 		if(mask & RC_FIELD_SCALARS) {
 			if(h.lsub_x != c.lx || h.lsub_y != c.ly) return set_err(e, RC_ERR_INVALID, "cell %d: patch size cannot change on upload", i);
 			CellDev n;
-			host_cell(h, n, c.start);
+			host_cell(h, n, c.start, c.layer);
 			n.area = h.area;
 			n.sumf = h.sum_f;
 			n.perim = h.perimeter;
@@ -898,7 +949,7 @@ int rc_upload(rc_engine *e, const rc_cell_host *cells, unsigned mask) {
 	}
 	if(mask & RC_FIELD_SCALARS) {
 		CUDA_TRY(e, cudaMemcpyAsync(e->cells, hc.data(), sizeof(CellDev) * (size_t) std::max(e->N, 1), cudaMemcpyHostToDevice, e->stream));
-		launch_bins(e->cells, e->N, e->L, e->bin_count, e->bin_cells, e->nbx, e->nby, e->st, e->stream);
+		launch_bins(e->cells, e->layers, e->N, e->bin_count, e->bin_cells, e->total_bins, e->st, e->stream);
 	}
 	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
 	return RC_OK;
@@ -933,6 +984,8 @@ int rc_set_stream(rc_engine *e, void *cuda_stream) {
 }
 
 long long rc_site_count(const rc_engine *e) { return e ? e->S : 0; }
+
+int rc_layer_count(const rc_engine *e) { return e ? e->n_layers : 0; }
 
 const char *rc_last_error(const rc_engine *e) { return e ? e->err.c_str() : g_create_error.c_str(); }
 

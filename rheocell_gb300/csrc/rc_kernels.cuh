@@ -11,6 +11,7 @@ enum UpdMode { UP_NONE = 0, UP_PRED = 1, UP_CORR = 2 };
 
 struct CellArgs {
 	CellDev *cells;
+	const LayerDev *layers;
 	int N;
 	int smem_n;            // per-site capacity of the dynamic shared memory
 	const double *phi_eval;  // phi at which forces are evaluated; PRED update also reads phi^n here
@@ -34,6 +35,8 @@ struct CellArgs {
 
 struct BoxArgs {
 	const CellDev *cells;
+	const LayerDev *layers;
+	int n_layers, total_bins;
 	const double *phi;
 	double *phi2, *sq00, *sq01;
 	int *cnt, *cover;      // cover[slot * L*L + k]
@@ -73,9 +76,9 @@ cudaError_t configure_kernels();
 void launch_cell_kernel(int model, int eval, int upd, const CellArgs &a, cudaStream_t s);
 size_t cell_smem_bytes(int model, int smem_n);
 int cell_smem_arrays(int model);
-void launch_rng(CellDev *cells, int N, DevStatus *st, cudaStream_t s);
-void launch_bins(CellDev *cells, int N, int L, int *bin_count, int *bin_cells, int nbx, int nby, DevStatus *st,
-                 cudaStream_t s);
+void launch_rng(CellDev *cells, LayerDev *layers, int n_layers, DevStatus *st, cudaStream_t s);
+void launch_bins(CellDev *cells, const LayerDev *layers, int N, int *bin_count, int *bin_cells, int total_bins,
+                 DevStatus *st, cudaStream_t s);
 void launch_repack(CellArgs a, double *scratch_phi, double *scratch_rep, long long cap, cudaStream_t s);
 void launch_box_gather(const BoxArgs &a, cudaStream_t s);
 int cg_grid_blocks(int device);

@@ -43,6 +43,7 @@ class EngineError(RuntimeError):
 SCALARS = ["lsub_x", "lsub_y", "offset_x", "offset_y", "corner", "type", "com_x", "com_y",
            "unrap_x", "unrap_y", "q00", "q01", "theta_q", "nemq_x", "nemq_y", "area", "sum_f",
            "perimeter", "s00", "s01", "force_rep_x", "force_rep_y"]
+SITE_FIELDS = ("phi", "vx", "vy", "mu", "dx", "dy", "box_index")
 
 
 class Engine:
@@ -61,7 +62,59 @@ class Engine:
             raise EngineError(rc, msg)
         self.n = cells.n
         self.L = L
+        self.layer_sizes = [cells.n]
         self.stats = abi.RcStepStats()
+
+    @classmethod
+    def batch(cls, params: abi.RcParams, layers, device: int = 0) -> "Engine":
+        """An ensemble of independent monolayers advanced together
+        (rc_batch_create).  `layers` is a list of (L, HostCells, rng_state);
+        cells of all layers are addressed layer-major afterwards."""
+        self = cls.__new__(cls)
+        self._lib = lib()
+        self.h = C.c_void_p()
+        nl = len(layers)
+        boxes = (abi.RcBox * nl)(*[abi.RcBox(L, L) for L, _, _ in layers])
+        counts = (C.c_int * nl)(*[hc.n for _, hc, _ in layers])
+        total = sum(hc.n for _, hc, _ in layers)
+        arr = (abi.RcCellHost * max(total, 1))()
+        j = 0
+        for _, hc, _ in layers:
+            for i in range(hc.n):
+                arr[j] = hc.arr[i]
+                j += 1
+        states = (C.c_ulonglong * nl)(*[int(s) for _, _, s in layers])
+        self._keep = [hc for _, hc, _ in layers]
+        rc = self._lib.rc_batch_create(C.byref(params), nl, boxes, counts, arr, states, device, C.byref(self.h))
+        if rc != 0:
+            msg = self._lib.rc_last_error(self.h).decode()
+            if self.h:
+                self._lib.rc_destroy(self.h)
+            self.h = None
+            raise EngineError(rc, msg)
+        self.n = total
+        self.L = [L for L, _, _ in layers]
+        self.layer_sizes = [hc.n for _, hc, _ in layers]
+        self.stats = abi.RcStepStats()
+        return self
+
+    def layer_count(self) -> int:
+        return int(self._lib.rc_layer_count(self.h))
+
+    def split(self, state: Dict[str, np.ndarray]) -> List[Dict[str, np.ndarray]]:
+        """Split a state() of a batch into one dict per layer."""
+        lx, ly = np.asarray(state["lsub_x"]), np.asarray(state["lsub_y"])
+        sizes = lx * ly
+        out, c0, s0 = [], 0, 0
+        for n in self.layer_sizes:
+            ns = int(sizes[c0:c0 + n].sum())
+            d = {}
+            for k, v in state.items():
+                d[k] = v[s0:s0 + ns] if k in SITE_FIELDS else v[c0:c0 + n]
+            out.append(d)
+            c0 += n
+            s0 += ns
+        return out
 
     def _check(self, rc: int, what: str):
         if rc != 0:
