@@ -247,6 +247,27 @@ int rc_timers(rc_engine *e, double *ms, long long *launches, int reset);
 /* Issue the engine's work on this cudaStream_t (NULL: the engine's own). */
 int rc_set_stream(rc_engine *e, void *cuda_stream);
 
+/*
+ * No counterpart in the reference.  Re-run the viscous solve of the last
+ * force evaluation (both components, from a cold start, plain FP64 CG at the
+ * engine's tolerance) into vx and vy, device arrays of n = rc_site_count(e)
+ * doubles in the order of rc_download_phi, without allocating any memory:
+ * the solver's work arrays live in one fixed device area of about 2.2 MB per
+ * device, so the state must have at most RC_NOALLOC_MAX_UNKNOWNS unknowns
+ * and a box of at most RC_NOALLOC_MAX_BOX_SITES sites (RC_ERR_CAPACITY
+ * otherwise, nothing launched).  For hosts that may not allocate device
+ * memory inside their time loop.  The first call on a device looks the area
+ * up (cudaGetSymbolAddress); make that call before any stream capture.  The
+ * area is shared: calls on one device must not overlap in time (from any
+ * engine or stream), or they race.  Runs on the engine's stream and returns
+ * when the solve is done; `iterations` (may be NULL) receives the CG
+ * iterations of both components.  RC_ERR_UNSUPPORTED if the last evaluation
+ * had no viscous solve.
+ */
+#define RC_NOALLOC_MAX_UNKNOWNS 32768
+#define RC_NOALLOC_MAX_BOX_SITES 16384
+int rc_viscous_resolve_noalloc(rc_engine *e, double *vx, double *vy, long long n, int *iterations);
+
 /* Sites (sum of LsubX*LsubY) in the current configuration. */
 long long rc_site_count(const rc_engine *e);
 

@@ -17,6 +17,8 @@ RC_ERR_NONFINITE = -5
 RC_ERR_CG = -6
 RC_ERR_CAPACITY = -7
 RC_ERR_UNSUPPORTED = -8
+RC_NOALLOC_MAX_UNKNOWNS = 32768
+RC_NOALLOC_MAX_BOX_SITES = 16384
 
 RC_SIMPLEFIELD = 0
 RC_ACTIVENEMATIC = 1
@@ -126,6 +128,8 @@ def declare(lib: C.CDLL, prefix: str) -> C.CDLL:
         lib.rc_batch_create.restype = C.c_int
         lib.rc_layer_count.argtypes = [vp]
         lib.rc_layer_count.restype = C.c_int
+        lib.rc_viscous_resolve_noalloc.argtypes = [vp, vp, vp, C.c_longlong, C.POINTER(C.c_int)]
+        lib.rc_viscous_resolve_noalloc.restype = C.c_int
         lib.rc_set_timing.argtypes = [vp, C.c_int]
         lib.rc_set_timing.restype = C.c_int
         lib.rc_timers.argtypes = [vp, DP, C.POINTER(C.c_longlong), C.c_int]
@@ -137,7 +141,7 @@ def declare(lib: C.CDLL, prefix: str) -> C.CDLL:
 
 
 # Every symbol the header declares (checked by the CPU test suite).
-EXPORTED = ["rc_abi_version", "rc_create", "rc_batch_create", "rc_layer_count", "rc_step", "rc_step_async", "rc_wait", "rc_set_phase",
+EXPORTED = ["rc_abi_version", "rc_create", "rc_batch_create", "rc_layer_count", "rc_viscous_resolve_noalloc", "rc_step", "rc_step_async", "rc_wait", "rc_set_phase",
             "rc_get_sizes", "rc_download", "rc_upload", "rc_download_phi", "rc_upload_phi", "rc_set_stream",
             "rc_set_timing", "rc_timers", "rc_site_count", "rc_last_error", "rc_destroy"]
 

@@ -29,6 +29,7 @@
 #include <cstdio>
 #include <cstddef>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -988,6 +989,143 @@ long long rc_site_count(const rc_engine *e) { return e ? e->S : 0; }
 int rc_layer_count(const rc_engine *e) { return e ? e->n_layers : 0; }
 
 const char *rc_last_error(const rc_engine *e) { return e ? e->err.c_str() : g_create_error.c_str(); }
+
+}  // extern "C"
+
+namespace {
+
+constexpr long long NA_MAX_UNKNOWNS = RC_NOALLOC_MAX_UNKNOWNS;
+constexpr long long NA_MAX_BOX_SITES = RC_NOALLOC_MAX_BOX_SITES;
+constexpr long long NA_MAX_BLOCKS = 4096;
+
+constexpr size_t na_round(size_t b) { return (b + 255) / 256 * 256; }
+constexpr size_t NA_OFF_ST = 0;
+constexpr size_t NA_OFF_BAR = NA_OFF_ST + na_round(sizeof(rc::DevStatus));
+constexpr size_t NA_OFF_SCALARS = NA_OFF_BAR + na_round(2 * sizeof(unsigned));
+constexpr size_t NA_OFF_PARTIALS = NA_OFF_SCALARS + na_round(64 * sizeof(double));
+constexpr size_t NA_OFF_VEC = NA_OFF_PARTIALS + na_round(8 * NA_MAX_BLOCKS * sizeof(double));
+constexpr size_t NA_VEC = na_round(NA_MAX_UNKNOWNS * sizeof(double));
+constexpr size_t NA_OFF_BOX = NA_OFF_VEC + 6 * NA_VEC;
+constexpr size_t NA_BOX = na_round(NA_MAX_BOX_SITES * sizeof(double));
+constexpr size_t NA_OFF_COV_OFF = NA_OFF_BOX + 2 * NA_BOX;
+constexpr size_t NA_OFF_COV_IDX = NA_OFF_COV_OFF + na_round((NA_MAX_BOX_SITES + 1) * sizeof(int));
+constexpr size_t NA_BYTES = NA_OFF_COV_IDX + na_round(NA_MAX_UNKNOWNS * sizeof(int));
+
+// The fixed solver area (about 2.2 MB): status, barrier words, reduction
+// slots, six work vectors, two box-grid sums and the CSR cover lists, laid
+// out at the offsets above.  One area per device, shared by every caller.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
+
+// Device address of the area, looked up once per device.
+std::mutex g_noalloc_mu;
+std::vector<unsigned char *> g_noalloc_ptr;
+
+// Resets what the solve needs zero at its start: the status record (then S
+// and the cold-start flag) and the barrier's arrival count.  The barrier's
+// generation word may hold any value; the work arrays are initialised by the
+// solve itself.
+__global__ void noalloc_header_kernel(rc::DevStatus *st, unsigned *bar, long long S) {
+	if(threadIdx.x == 0 && blockIdx.x == 0) {
+		memset(st, 0, sizeof(*st));
+		st->S = S;
+		st->cg_cold = 1;
+		bar[0] = 0u;
+	}
+}
+
+}  // namespace
+
+extern "C" {
+
+/*
+ * rc_viscous_resolve_noalloc: the viscous solve of the last force evaluation,
+ * run again from a cold start into caller-owned device arrays, with every
+ * solver work array taken from a fixed, statically sized device area instead
+ * of engine or runtime allocations.  It exists for hosts that must not
+ * allocate device memory while they run: a driver that has already handed
+ * the HBM to its own pool for an ensemble of engines, or one that cannot take
+ * the device-wide synchronisation cudaMalloc/cudaFree imply in the middle of
+ * its time loop.  The reference has no counterpart (Eigen allocates its CG
+ * work vectors on every solve, WetModel.cpp:279-376).
+ */
+int rc_viscous_resolve_noalloc(rc_engine *e, double *vx, double *vy, long long n, int *iterations) {
+	if(!e) return RC_ERR_INVALID;
+	if(!vx || !vy) return set_err(e, RC_ERR_INVALID, "rc_viscous_resolve_noalloc: NULL output array");
+	if(n != e->S)
+		return set_err(e, RC_ERR_INVALID, "rc_viscous_resolve_noalloc: n = %lld but the state has %lld unknowns", n, e->S);
+	if(e->pending || !wet_phase(e, e->eval_phase))
+		return set_err(e, RC_ERR_UNSUPPORTED, "rc_viscous_resolve_noalloc: the last evaluation had no viscous solve");
+	if(e->S > NA_MAX_UNKNOWNS)
+		return set_err(e, RC_ERR_CAPACITY,
+		               "rc_viscous_resolve_noalloc: %lld unknowns per component, the fixed area holds at most %lld",
+		               e->S, NA_MAX_UNKNOWNS);
+	if((long long) e->L * e->L > NA_MAX_BOX_SITES)
+		return set_err(e, RC_ERR_CAPACITY,
+		               "rc_viscous_resolve_noalloc: box of %d x %d sites, the fixed area holds at most %lld sites", e->L,
+		               e->L, NA_MAX_BOX_SITES);
+	if(e->cg_blocks > NA_MAX_BLOCKS)
+		return set_err(e, RC_ERR_CAPACITY, "rc_viscous_resolve_noalloc: %d solver blocks, at most %lld", e->cg_blocks,
+		               NA_MAX_BLOCKS);
+	CUDA_TRY(e, cudaSetDevice(e->device));
+	unsigned char *base = nullptr;
+	{
+		std::lock_guard<std::mutex> lock(g_noalloc_mu);
+		if(g_noalloc_ptr.size() <= (size_t) e->device) g_noalloc_ptr.resize((size_t) e->device + 1, nullptr);
+		if(!g_noalloc_ptr[(size_t) e->device]) {
+			void *q = nullptr;
+			const cudaError_t c = cudaGetSymbolAddress(&q, g_noalloc_scratch);
+			if(c != cudaSuccess)
+				return set_err(e, RC_ERR_CUDA, "rc_viscous_resolve_noalloc: cudaGetSymbolAddress failed: %s",
+				               cudaGetErrorString(c));
+			g_noalloc_ptr[(size_t) e->device] = (unsigned char *) q;
+		}
+		base = g_noalloc_ptr[(size_t) e->device];
+	}
+	rc::DevStatus *st = (rc::DevStatus *) (base + NA_OFF_ST);
+	unsigned *bar = (unsigned *) (base + NA_OFF_BAR);
+	double *vec = (double *) (base + NA_OFF_VEC);
+	const size_t vs = NA_VEC / sizeof(double), bs = NA_BOX / sizeof(double);
+	noalloc_header_kernel<<<1, 32, 0, e->stream>>>(st, bar, e->S);
+	CUDA_TRY(e, cudaGetLastError());
+	CGArgs g;
+	memset(&g, 0, sizeof(g));
+	g.cells = e->cells;
+	g.mapg = e->mapg;
+	g.cnt = e->cnt;
+	g.cover = e->cover;
+	g.cov_off = (int *) (base + NA_OFF_COV_OFF);
+	g.cov_idx = (int *) (base + NA_OFF_COV_IDX);
+	g.fx = e->fx;
+	g.fy = e->fy;
+	g.vx = vx;
+	g.vy = vy;
+	g.rx = vec;
+	g.ry = vec + vs;
+	g.px = vec + 2 * vs;
+	g.py = vec + 3 * vs;
+	g.apx = vec + 4 * vs;
+	g.apy = vec + 5 * vs;
+	g.Px = (double *) (base + NA_OFF_BOX);
+	g.Py = g.Px + bs;
+	g.partials = (double *) (base + NA_OFF_PARTIALS);
+	g.scalars = (double *) (base + NA_OFF_SCALARS);
+	g.bar = bar;
+	g.st = st;
+	g.L = e->L;
+	g.restart_every = 0;
+	g.xi = e->ph[e->eval_phase].friction;
+	g.eta = e->ph[e->eval_phase].friction_cell;
+	g.tol = e->hp.cg_tolerance > 0 ? e->hp.cg_tolerance : 2.220446049250313e-16;
+	g.mixed = 0;
+	CUDA_TRY(e, launch_cg(g, e->cg_blocks, e->stream));
+	rc::DevStatus h;
+	CUDA_TRY(e, cudaMemcpyAsync(&h, st, sizeof(h), cudaMemcpyDeviceToHost, e->stream));
+	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+	if(h.err & ERR_BARRIER) return set_err(e, RC_ERR_CG, "rc_viscous_resolve_noalloc: grid barrier timed out");
+	if(h.err) return set_err(e, RC_ERR_INVALID, "rc_viscous_resolve_noalloc: device error 0x%x", h.err);
+	if(iterations) *iterations = h.cg_iters;
+	return RC_OK;
+}
 
 void rc_destroy(rc_engine *e) {
 	if(!e) return;
