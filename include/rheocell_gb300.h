@@ -268,6 +268,79 @@ int rc_set_stream(rc_engine *e, void *cuda_stream);
 #define RC_NOALLOC_MAX_BOX_SITES 16384
 int rc_viscous_resolve_noalloc(rc_engine *e, double *vx, double *vy, long long n, int *iterations);
 
+/*
+ * The learned preconditioner's network (no counterpart in the reference).
+ * RC_UNET_PARAMS parameters: 11 layers of 3x3 convolutions on the periodic
+ * box grid, each 9*ci*co weights w[tap][ci][co] then co biases; the layer
+ * list is in rheocell_gb300/csrc/rc_unet.cuh.
+ *
+ * rc_unet_loss_grad: one FP32 forward, loss and backward pass on the device
+ * for host data: input [batch][L][L][2], target [batch][L][L]; loss = mean
+ * over samples of |f - target|^2 / |target|^2; grad (RC_UNET_PARAMS values)
+ * and output ([batch][L][L]) may be NULL.  L must be a multiple of 4.
+ */
+#define RC_UNET_PARAMS 25937
+int rc_unet_loss_grad(int L, int batch, const double *params, const double *input, const double *target,
+                      double *loss, double *grad, double *output, int device);
+
+/*
+ * Learned preconditioner for the wet models' viscous solve (no counterpart
+ * in the reference, whose solve is Eigen's Jacobi-preconditioned CG,
+ * WetModel.cpp:361-376).
+ *
+ * The patch-stacked system reduces exactly to a box-grid one: with
+ * T(k) = xi + eta D(k), R[k] = sum_{j at k} r_j / T(k), W[k] = n(k) / T(k),
+ * the box sums V = S v solve V - eta W (N4 V) = R, and v_j = (r_j + eta
+ * (N4 V)[k_j]) / T(k_j).  The network maps (R/s, W) to V/s (s = |r| /
+ * sqrt(S)); inside flexible CG (FCG(1)) it serves as the preconditioner of
+ * the FP32 inner iterations of the mixed-precision solve, whose FP64
+ * iterative refinement keeps the RC_PRECISION_MIXED guarantees (true FP64
+ * residual below cg_tolerance; a sweep that fails to halve the residual
+ * hands over to plain FP64 CG).
+ *
+ * rc_learned_harvest: collect training samples from the following plain
+ * FP64 solves (RC_PRECISION_DOUBLE and RC_SOLVER_PLAIN): at sweeps 0,
+ * every, 2*every, ... (at most per_solve points per solve) each velocity
+ * component gives the pair (box residual, box error), until `capacity`
+ * samples are stored.  capacity = 0 stops harvesting and frees the store.
+ * rc_learned_harvested: samples stored so far (synchronises).
+ * rc_learned_train: Adam on the stored samples (device forward and backward
+ * kernels); the trained parameters become the engine's.
+ * rc_set_solver: RC_SOLVER_PLAIN (default) or RC_SOLVER_LEARNED (needs
+ * parameters, from training or rc_learned_set_params, and a box side that
+ * is a multiple of 4).
+ */
+#define RC_SOLVER_PLAIN 0
+#define RC_SOLVER_LEARNED 1
+
+typedef struct rc_train_options {
+	int epochs;                 /* passes over the training samples (<= 0: 8)         */
+	int batch;                  /* samples per Adam step (<= 0: 8)                     */
+	double learning_rate;       /* Adam step size (<= 0: 1e-3)                         */
+	double validation;          /* fraction held out for validation (< 0: 0.1)         */
+	unsigned long long seed;    /* initialisation and shuffling                        */
+	int init;                   /* 1: fresh initialisation; 0: continue from the current parameters */
+	int max_samples;            /* use at most this many samples (<= 0: all)           */
+} rc_train_options;
+
+typedef struct rc_train_report {
+	int samples;                /* valid harvested samples used                        */
+	int train_samples, validation_samples;
+	int epochs, steps;
+	double loss_first_epoch;    /* mean training loss over the first epoch             */
+	double loss_last_epoch;     /* ... over the last epoch                             */
+	double validation_loss_init;/* validation loss before training                     */
+	double validation_loss;     /* ... after                                           */
+	double ms;                  /* wall time of the training                           */
+} rc_train_report;
+
+int rc_learned_harvest(rc_engine *e, int capacity, int every, int per_solve);
+int rc_learned_harvested(rc_engine *e);
+int rc_learned_train(rc_engine *e, const rc_train_options *options, rc_train_report *report);
+int rc_learned_get_params(rc_engine *e, double *params);
+int rc_learned_set_params(rc_engine *e, const double *params);
+int rc_set_solver(rc_engine *e, int solver);
+
 /* Sites (sum of LsubX*LsubY) in the current configuration. */
 long long rc_site_count(const rc_engine *e);
 

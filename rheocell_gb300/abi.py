@@ -19,6 +19,9 @@ RC_ERR_CAPACITY = -7
 RC_ERR_UNSUPPORTED = -8
 RC_NOALLOC_MAX_UNKNOWNS = 32768
 RC_NOALLOC_MAX_BOX_SITES = 16384
+RC_UNET_PARAMS = 25937
+RC_SOLVER_PLAIN = 0
+RC_SOLVER_LEARNED = 1
 
 RC_SIMPLEFIELD = 0
 RC_ACTIVENEMATIC = 1
@@ -86,6 +89,21 @@ class RcStepStats(C.Structure):
     ]
 
 
+class RcTrainOptions(C.Structure):
+    _fields_ = [
+        ("epochs", C.c_int), ("batch", C.c_int), ("learning_rate", C.c_double), ("validation", C.c_double),
+        ("seed", C.c_ulonglong), ("init", C.c_int), ("max_samples", C.c_int),
+    ]
+
+
+class RcTrainReport(C.Structure):
+    _fields_ = [
+        ("samples", C.c_int), ("train_samples", C.c_int), ("validation_samples", C.c_int), ("epochs", C.c_int),
+        ("steps", C.c_int), ("loss_first_epoch", C.c_double), ("loss_last_epoch", C.c_double),
+        ("validation_loss_init", C.c_double), ("validation_loss", C.c_double), ("ms", C.c_double),
+    ]
+
+
 def declare(lib: C.CDLL, prefix: str) -> C.CDLL:
     """Declare the argument/return types of the rc_*-style API under ``prefix``
     ("rc" for the engine, "orc" for the oracle)."""
@@ -128,6 +146,20 @@ def declare(lib: C.CDLL, prefix: str) -> C.CDLL:
         lib.rc_batch_create.restype = C.c_int
         lib.rc_layer_count.argtypes = [vp]
         lib.rc_layer_count.restype = C.c_int
+        lib.rc_learned_harvest.argtypes = [vp, C.c_int, C.c_int, C.c_int]
+        lib.rc_learned_harvest.restype = C.c_int
+        lib.rc_learned_harvested.argtypes = [vp]
+        lib.rc_learned_harvested.restype = C.c_int
+        lib.rc_learned_train.argtypes = [vp, C.POINTER(RcTrainOptions), C.POINTER(RcTrainReport)]
+        lib.rc_learned_train.restype = C.c_int
+        lib.rc_learned_get_params.argtypes = [vp, DP]
+        lib.rc_learned_get_params.restype = C.c_int
+        lib.rc_learned_set_params.argtypes = [vp, DP]
+        lib.rc_learned_set_params.restype = C.c_int
+        lib.rc_set_solver.argtypes = [vp, C.c_int]
+        lib.rc_set_solver.restype = C.c_int
+        lib.rc_unet_loss_grad.argtypes = [C.c_int, C.c_int, DP, DP, DP, DP, DP, DP, C.c_int]
+        lib.rc_unet_loss_grad.restype = C.c_int
         lib.rc_viscous_resolve_noalloc.argtypes = [vp, vp, vp, C.c_longlong, C.POINTER(C.c_int)]
         lib.rc_viscous_resolve_noalloc.restype = C.c_int
         lib.rc_set_timing.argtypes = [vp, C.c_int]
@@ -141,7 +173,9 @@ def declare(lib: C.CDLL, prefix: str) -> C.CDLL:
 
 
 # Every symbol the header declares (checked by the CPU test suite).
-EXPORTED = ["rc_abi_version", "rc_create", "rc_batch_create", "rc_layer_count", "rc_viscous_resolve_noalloc", "rc_step", "rc_step_async", "rc_wait", "rc_set_phase",
+EXPORTED = ["rc_abi_version", "rc_create", "rc_batch_create", "rc_layer_count", "rc_viscous_resolve_noalloc", "rc_unet_loss_grad",
+            "rc_learned_harvest", "rc_learned_harvested", "rc_learned_train", "rc_learned_get_params",
+            "rc_learned_set_params", "rc_set_solver", "rc_step", "rc_step_async", "rc_wait", "rc_set_phase",
             "rc_get_sizes", "rc_download", "rc_upload", "rc_download_phi", "rc_upload_phi", "rc_set_stream",
             "rc_set_timing", "rc_timers", "rc_site_count", "rc_last_error", "rc_destroy"]
 

@@ -142,7 +142,9 @@ struct CGShared {
 	double red[8 * (CG_THREADS / 32 + 1)];  // block_sum<8> scratch
 	double tot[8];
 	double rz[2], thr[2], bn2[2], rn2[2], alpha[2], beta[2];
+	double pap[2], scale[2];  // learned path: p.Ap of the sweep, residual scale
 	int act[2], it[2], first, zero[2];
+	int hbase, hm;            // harvesting: first slot of this solve, points taken
 };
 
 // Cover lists in CSR form for this solve: cov_off[k] = sum of n over box
@@ -325,6 +327,9 @@ __device__ inline void block_sum_warps(double (&v)[NV], double *scratch) {
 	__syncthreads();
 }
 
+__device__ bool harvest_point(const CGArgs &a, CGShared &sh, const double *ux, const double *uy, const double *rx,
+                              const double *ry, int m);
+
 template<typename T>
 __device__ __forceinline__ T fmaT(T a, T b, T c);
 template<>
@@ -370,7 +375,17 @@ __device__ bool cg_iterate(const CGArgs &a, CGShared &sh, T *rx, T *ry, T *px, T
 	}
 	if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
 	const long long E = __ldcg(&a.cov_off[L2]);
+	long long sweep = 0;
 	while(sh.act[0] || sh.act[1]) {
+		if constexpr(sizeof(T) == sizeof(double)) {
+			if(a.harv_in && !a.mixed && sh.hm < a.harv_per_solve && sweep % a.harv_every == 0 &&
+			   sh.hbase + 2LL * (sh.hm + 1) <= a.harv_cap) {
+				if(!harvest_point(a, sh, ux, uy, rx, ry, sh.hm)) return false;
+				if(threadIdx.x == 0) sh.hm++;
+				__syncthreads();
+			}
+		}
+		sweep++;
 		const int ax = sh.act[0], ay = sh.act[1], first = sh.first;
 		const T bx = (T) sh.beta[0], by = (T) sh.beta[1];
 		// Phase A: p = z + beta p (p = z on the first sweep), box sums P = S p,
@@ -488,8 +503,351 @@ __device__ bool cg_iterate(const CGArgs &a, CGShared &sh, T *rx, T *ry, T *px, T
 	return true;
 }
 
+// ---------------------------------------------------------------------------
+// Training samples for the learned preconditioner, taken from the FP64 solve.
+//
+// Eliminating the patch unknowns at one box site k (they share T = xi + eta
+// D(k)) turns A v = r into a box-grid system: with R[k] = sum_{j at k} r_j / T
+// and V = S v (box sums), V - eta W (N4 V) = R where W[k] = n(k) / T(k), and
+// then v_j = (r_j + eta (N4 V)[k_j]) / T_j exactly.  The network learns
+// R -> V.  At iteration k of the plain solve, with x_k the iterate and r_k
+// its residual, the error e_k = x* - x_k solves A e_k = r_k, so the pair is
+// (R_k, V = S x* - S x_k).  Inputs and targets are divided by the residual
+// scale s = sqrt(|r_k|^2 / S), the same normalisation the solve applies.
+
+__device__ __forceinline__ float box_w(const CGArgs &a, const CGShared &sh, int k, int L) {
+	const int n = a.cnt[k];
+	return n ? (float) ((double) n * sh.iT[box_deg(a.cnt, k, L)]) : 0.f;
+}
+
+// Record harvest point m: box sums of x (into the target slot) and of r/T
+// (into the input slot) for both components; slots hbase + 2m + c.
+__device__ bool harvest_point(const CGArgs &a, CGShared &sh, const double *ux, const double *uy, const double *rx,
+                              const double *ry, int m) {
+	const int L = a.L;
+	const long long L2 = (long long) L * L;
+	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+	const long long gstride = (long long) gridDim.x * blockDim.x;
+	const long long q0 = sh.hbase + 2LL * m;
+	for(long long k = gtid; k < L2; k += gstride) {
+		const float w = box_w(a, sh, (int) k, L);
+		for(int c = 0; c < 2; c++) {
+			a.harv_in[((q0 + c) * L2 + k) * 2] = 0.f;
+			a.harv_in[((q0 + c) * L2 + k) * 2 + 1] = w;
+			a.harv_tgt[(q0 + c) * L2 + k] = 0.f;
+		}
+	}
+	if(blockIdx.x == 0 && threadIdx.x < 2) {
+		const int c = threadIdx.x;
+		a.harv_s[q0 + c] = sh.act[c] ? (float) sqrt(sh.rn2[c] / (double) a.st->S) : 0.f;
+	}
+	if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
+	const long long E = __ldcg(&a.cov_off[L2]);
+	const long long gwarp = gtid >> 5, nwarps = gstride >> 5;
+	const int lane = threadIdx.x & 31;
+	for(long long base = gwarp * 32; base < E; base += nwarps * 32) {
+		const long long t = base + lane;
+		const bool valid = t < E;
+		const int j = valid ? a.cov_idx[t] : 0;
+		const int key = valid ? a.mapg[j] : -1;
+		const double id = valid ? sh.iT[box_deg(a.cnt, key, L)] : 0.0;
+		bool t0, t1, t2, t3;
+		const double sx = seg_sum<double>(valid ? ux[j] : 0.0, key, t0);
+		const double sy = seg_sum<double>(valid ? uy[j] : 0.0, key, t1);
+		const double rxs = seg_sum<double>(valid ? rx[j] * id : 0.0, key, t2);
+		const double rys = seg_sum<double>(valid ? ry[j] * id : 0.0, key, t3);
+		if(valid && t0) {
+			atomicAdd(&a.harv_tgt[q0 * L2 + key], (float) sx);
+			atomicAdd(&a.harv_tgt[(q0 + 1) * L2 + key], (float) sy);
+			atomicAdd(&a.harv_in[(q0 * L2 + key) * 2], (float) rxs);
+			atomicAdd(&a.harv_in[((q0 + 1) * L2 + key) * 2], (float) rys);
+		}
+	}
+	return grid_reduce(a, 0, nullptr, sh.tot, sh.red);
+}
+
+// After the solve: targets (S x* - S x_k) / s and inputs R / s for the
+// points taken, then publish the new sample count.
+__device__ bool harvest_finish(const CGArgs &a, CGShared &sh, const double *ux, const double *uy) {
+	const int L = a.L;
+	const long long L2 = (long long) L * L;
+	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+	const long long gstride = (long long) gridDim.x * blockDim.x;
+	for(long long k = gtid; k < L2; k += gstride) {
+		a.Px[k] = 0.0;
+		a.Py[k] = 0.0;
+	}
+	if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
+	const long long E = __ldcg(&a.cov_off[L2]);
+	const long long gwarp = gtid >> 5, nwarps = gstride >> 5;
+	const int lane = threadIdx.x & 31;
+	for(long long base = gwarp * 32; base < E; base += nwarps * 32) {
+		const long long t = base + lane;
+		const bool valid = t < E;
+		const int j = valid ? a.cov_idx[t] : 0;
+		const int key = valid ? a.mapg[j] : -1;
+		bool t0, t1;
+		const double sx = seg_sum<double>(valid ? ux[j] : 0.0, key, t0);
+		const double sy = seg_sum<double>(valid ? uy[j] : 0.0, key, t1);
+		if(valid && t0) {
+			atomicAdd(&a.Px[key], sx);
+			atomicAdd(&a.Py[key], sy);
+		}
+	}
+	if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
+	const long long n = 2LL * sh.hm;
+	for(long long e = gtid; e < n * L2; e += gstride) {
+		const long long q = sh.hbase + e / L2, k = e % L2;
+		const float sc = __ldcg(&a.harv_s[q]);
+		if(sc > 0.f) {
+			const double xs = ((e / L2) & 1) ? a.Py[k] : a.Px[k];
+			a.harv_tgt[q * L2 + k] = (float) ((xs - (double) a.harv_tgt[q * L2 + k]) / (double) sc);
+			a.harv_in[(q * L2 + k) * 2] = a.harv_in[(q * L2 + k) * 2] / sc;
+		}
+	}
+	if(blockIdx.x == 0 && threadIdx.x == 0) *a.harv_count = sh.hbase + 2 * sh.hm;
+	return true;
+}
+
+// ---------------------------------------------------------------------------
+// Learned preconditioner: z = M r for both components.
+//   D: R[c][k] = sum_{j at k} r_j / (T_j s_c) into the network's input
+//      (the R channel was cleared in an earlier phase; W is in place);
+//   the network (11 convolution layers, a grid barrier after each);
+//   E: z_j = (r_j + eta s_c (N4 V_c)[k_j]) / T_j, with r.z and z.Ap reduced
+//      into sh.tot[0..3].
+// Runs in FP32 with FP64 reductions.
+__device__ bool precond_apply(const CGArgs &a, CGShared &sh, float *wsm, const float *iTT) {
+	const int L = a.L;
+	const long long L2 = (long long) L * L;
+	const long long S = a.st->S;
+	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+	const long long gstride = (long long) gridDim.x * blockDim.x;
+	const float inv0 = sh.scale[0] > 0.0 ? (float) (1.0 / sh.scale[0]) : 0.f;
+	const float inv1 = sh.scale[1] > 0.0 ? (float) (1.0 / sh.scale[1]) : 0.f;
+	float *x0 = a.unet.x0;
+	{
+		const long long E = __ldcg(&a.cov_off[L2]);
+		const long long gwarp = gtid >> 5, nwarps = gstride >> 5;
+		const int lane = threadIdx.x & 31;
+		for(long long base = gwarp * 32; base < E; base += nwarps * 32) {
+			const long long t = base + lane;
+			const bool valid = t < E;
+			const int j = valid ? a.cov_idx[t] : 0;
+			const int key = valid ? a.mapg[j] : -1;
+			const float id = valid ? iTT[box_deg(a.cnt, key, L)] : 0.f;
+			bool t0, t1;
+			const float sx = seg_sum<float>(valid ? a.rxf[j] * id * inv0 : 0.f, key, t0);
+			const float sy = seg_sum<float>(valid ? a.ryf[j] * id * inv1 : 0.f, key, t1);
+			if(valid && t0) {
+				atomicAdd(&x0[(size_t) key * 2], sx);
+				atomicAdd(&x0[((size_t) L2 + key) * 2], sy);
+			}
+		}
+	}
+	if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
+	for(int l = 0; l < UNET_LAYERS; l++) {
+		const UNetLayerDesc d = unet_layer(l);
+		const int nw = 9 * d.ci * d.co + d.co;
+		const float *src = a.unet_params + unet_weight_offset(l);
+		for(int k = threadIdx.x; k < nw; k += blockDim.x) wsm[k] = src[k];
+		__syncthreads();
+		conv_layer_range(l, unet_src(l, a.unet), wsm, wsm + 9 * d.ci * d.co, unet_dst(l, a.unet), 2, L >> d.level, gtid,
+		                 gstride);
+		if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
+	}
+	const float es0 = (float) (a.eta * sh.scale[0]), es1 = (float) (a.eta * sh.scale[1]);
+	const float *V = a.unet.out;
+	float w[4] = {0.f, 0.f, 0.f, 0.f};
+	for(long long j = gtid; j < S; j += gstride) {
+		const int k = a.mapg[j];
+		const float id = iTT[box_deg(a.cnt, k, L)];
+		const float rxv = a.rxf[j], ryv = a.ryf[j];
+		const float zx = id * __fmaf_rn(es0, box_n4T<float>(V, k, L), rxv);
+		const float zy = id * __fmaf_rn(es1, box_n4T<float>(V + L2, k, L), ryv);
+		a.zxf[j] = zx;
+		a.zyf[j] = zy;
+		w[0] = __fmaf_rn(rxv, zx, w[0]);
+		w[1] = __fmaf_rn(ryv, zy, w[1]);
+		w[2] = __fmaf_rn(zx, a.apxf[j], w[2]);
+		w[3] = __fmaf_rn(zy, a.apyf[j], w[3]);
+	}
+	warp_tree<float, 4>(w);
+	double v[4] = {(double) w[0], (double) w[1], (double) w[2], (double) w[3]};
+	block_sum_warps<4>(v, sh.red);
+	return grid_reduce(a, 4, v, sh.tot, sh.red);
+}
+
+// Flexible CG (Notay's FCG(1): beta = -z'.Ap / p.Ap) on the FP32 correction
+// system A e = r of one refinement sweep, preconditioned by the network.
+// Same conventions as cg_iterate<float>: r in rxf/ryf, e in exf/eyf, stop at
+// |r|^2 < thr per component.
+__device__ bool fcg_iterate(const CGArgs &a, CGShared &sh, float *wsm, long long max_it) {
+	const int L = a.L;
+	const long long L2 = (long long) L * L;
+	const long long S = a.st->S;
+	const float neta = (float) (-a.eta * 1.0);
+	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+	const long long gstride = (long long) gridDim.x * blockDim.x;
+	__shared__ float dT[CG_MAX_D + 1], iTT[CG_MAX_D + 1];
+	for(int d = threadIdx.x; d <= CG_MAX_D; d += blockDim.x) {
+		dT[d] = (float) sh.T[d];
+		iTT[d] = (float) sh.iT[d];
+	}
+	float *px = a.pxf, *py = a.pyf, *apx = a.apxf, *apy = a.apyf, *Pbx = a.Pxf, *Pby = a.Pyf;
+	// box sums cleared for phase A, network input: R cleared, W in place
+	for(long long k = gtid; k < L2; k += gstride) {
+		Pbx[k] = 0.f;
+		Pby[k] = 0.f;
+		const float wv = box_w(a, sh, (int) k, L);
+		a.unet.x0[k * 2] = 0.f;
+		a.unet.x0[k * 2 + 1] = wv;
+		a.unet.x0[(L2 + k) * 2] = 0.f;
+		a.unet.x0[(L2 + k) * 2 + 1] = wv;
+	}
+	for(long long j = gtid; j < S; j += gstride) {
+		apx[j] = 0.f;
+		apy[j] = 0.f;
+	}
+	if(threadIdx.x == 0) {
+		for(int c = 0; c < 2; c++) sh.scale[c] = sqrt(sh.rn2[c] / (double) S);
+		sh.first = 1;
+	}
+	if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
+	if(!precond_apply(a, sh, wsm, iTT)) return false;
+	if(threadIdx.x == 0) {
+		sh.rz[0] = sh.tot[0];
+		sh.rz[1] = sh.tot[1];
+	}
+	__syncthreads();
+	const long long E = __ldcg(&a.cov_off[L2]);
+	while(sh.act[0] || sh.act[1]) {
+		const int ax = sh.act[0], ay = sh.act[1], first = sh.first;
+		const float bx = (float) sh.beta[0], by = (float) sh.beta[1];
+		// Phase A: p = z + beta p, box sums P = S p
+		{
+			const long long gwarp = gtid >> 5, nwarps = gstride >> 5;
+			const int lane = threadIdx.x & 31;
+			for(long long base = gwarp * 32; base < E; base += nwarps * 32) {
+				const long long t = base + lane;
+				const bool valid = t < E;
+				const int j = valid ? a.cov_idx[t] : 0;
+				const int key = valid ? a.mapg[j] : -1;
+				float vx = 0.f, vy = 0.f;
+				if(valid && ax) {
+					const float z = a.zxf[j];
+					const float p = first ? z : __fmaf_rn(bx, px[j], z);
+					px[j] = p;
+					vx = p;
+				}
+				if(valid && ay) {
+					const float z = a.zyf[j];
+					const float p = first ? z : __fmaf_rn(by, py[j], z);
+					py[j] = p;
+					vy = p;
+				}
+				bool tail = false, tail2 = false;
+				if(ax) vx = seg_sum<float>(vx, key, tail);
+				if(ay) vy = seg_sum<float>(vy, key, tail2);
+				if(valid) {
+					if(ax && tail) atomicAdd(&Pbx[key], vx);
+					if(ay && tail2) atomicAdd(&Pby[key], vy);
+				}
+			}
+		}
+		if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
+		// Phase B: Ap (stored) and p.Ap; the network's R channel is cleared
+		{
+			float w[2] = {0.f, 0.f};
+			for(long long j = gtid; j < S; j += gstride) {
+				const int k = a.mapg[j];
+				const float d = dT[box_deg(a.cnt, k, L)];
+				if(ax) {
+					const float p = px[j];
+					const float ap = __fmaf_rn(d, p, neta * box_n4T<float>(Pbx, k, L));
+					apx[j] = ap;
+					w[0] = __fmaf_rn(p, ap, w[0]);
+				}
+				if(ay) {
+					const float p = py[j];
+					const float ap = __fmaf_rn(d, p, neta * box_n4T<float>(Pby, k, L));
+					apy[j] = ap;
+					w[1] = __fmaf_rn(p, ap, w[1]);
+				}
+			}
+			for(long long k = gtid; k < L2; k += gstride) {
+				a.unet.x0[k * 2] = 0.f;
+				a.unet.x0[(L2 + k) * 2] = 0.f;
+			}
+			warp_tree<float, 2>(w);
+			double v[2] = {(double) w[0], (double) w[1]};
+			block_sum_warps<2>(v, sh.red);
+			if(!grid_reduce(a, 2, v, sh.tot, sh.red)) return false;
+		}
+		if(threadIdx.x == 0) {
+			for(int c = 0; c < 2; c++) {
+				if(!sh.act[c]) continue;
+				sh.pap[c] = sh.tot[c];
+				sh.alpha[c] = sh.rz[c] / sh.tot[c];
+			}
+		}
+		__syncthreads();
+		// Phase C: e += alpha p, r -= alpha Ap, |r|^2; box sums cleared
+		{
+			const float alx = (float) sh.alpha[0], aly = (float) sh.alpha[1];
+			float w[2] = {0.f, 0.f};
+			for(long long j = gtid; j < S; j += gstride) {
+				if(ax) {
+					a.exf[j] = __fmaf_rn(alx, px[j], a.exf[j]);
+					const float r = __fmaf_rn(-alx, apx[j], a.rxf[j]);
+					a.rxf[j] = r;
+					w[0] = __fmaf_rn(r, r, w[0]);
+				}
+				if(ay) {
+					a.eyf[j] = __fmaf_rn(aly, py[j], a.eyf[j]);
+					const float r = __fmaf_rn(-aly, apy[j], a.ryf[j]);
+					a.ryf[j] = r;
+					w[1] = __fmaf_rn(r, r, w[1]);
+				}
+			}
+			for(long long k = gtid; k < L2; k += gstride) {
+				Pbx[k] = 0.f;
+				Pby[k] = 0.f;
+			}
+			warp_tree<float, 2>(w);
+			double v[2] = {(double) w[0], (double) w[1]};
+			block_sum_warps<2>(v, sh.red);
+			if(!grid_reduce(a, 2, v, sh.tot, sh.red)) return false;
+		}
+		if(threadIdx.x == 0) {
+			for(int c = 0; c < 2; c++) {
+				if(!sh.act[c]) continue;
+				sh.rn2[c] = sh.tot[c];
+				sh.it[c]++;
+				if(sh.rn2[c] < sh.thr[c] || sh.it[c] >= max_it || !isfinite(sh.rn2[c])) sh.act[c] = 0;
+				sh.scale[c] = sqrt(sh.rn2[c] / (double) S);
+			}
+		}
+		__syncthreads();
+		if(!sh.act[0] && !sh.act[1]) break;
+		if(!precond_apply(a, sh, wsm, iTT)) return false;
+		if(threadIdx.x == 0) {
+			for(int c = 0; c < 2; c++) {
+				if(!sh.act[c]) continue;
+				sh.rz[c] = sh.tot[c];
+				sh.beta[c] = -sh.tot[2 + c] / sh.pap[c];
+			}
+			sh.first = 0;
+		}
+		__syncthreads();
+	}
+	return true;
+}
+
+template<bool LEARNED>
 __global__ void __launch_bounds__(CG_THREADS) cg_kernel(const CGArgs a) {
 	__shared__ CGShared sh;
+	extern __shared__ float wsm[];
 	const long long S = a.st->S;
 	const int cold = a.st->cg_cold;
 	const double eta = a.eta;
@@ -500,6 +858,8 @@ __global__ void __launch_bounds__(CG_THREADS) cg_kernel(const CGArgs a) {
 		for(int d = 1; d <= CG_MAX_D; d++) sh.T[d] = sh.T[d - 1] + eta * 1.0;
 		for(int d = 0; d <= CG_MAX_D; d++) sh.iT[d] = sh.T[d] != 0.0 ? 1.0 / sh.T[d] : 1.0;
 		sh.beta[0] = sh.beta[1] = 0.0;
+		sh.hm = 0;
+		sh.hbase = a.harv_count ? __ldcg(a.harv_count) : 0;
 	}
 	__syncthreads();
 	if(cold) {
@@ -537,6 +897,7 @@ __global__ void __launch_bounds__(CG_THREADS) cg_kernel(const CGArgs a) {
 	int refinements = 0;
 	if(!mixed) {
 		if(!cg_iterate<double>(a, sh, a.rx, a.ry, a.px, a.py, a.apx, a.apy, a.Px, a.Py, a.vx, a.vy, max_it)) return;
+		if(a.harv_in && sh.hm > 0 && !harvest_finish(a, sh, a.vx, a.vy)) return;
 	}
 	else {
 		// Iterative refinement: FP32 Jacobi-PCG for the correction A e = r,
@@ -557,7 +918,13 @@ __global__ void __launch_bounds__(CG_THREADS) cg_kernel(const CGArgs a) {
 				}
 			}
 			__syncthreads();
-			if(!cg_iterate<float>(a, sh, a.rxf, a.ryf, a.pxf, a.pyf, a.apxf, a.apyf, a.Pxf, a.Pyf, a.exf, a.eyf, max_it)) return;
+			if constexpr(LEARNED) {
+				if(!fcg_iterate(a, sh, wsm, max_it < 1000 ? max_it : 1000)) return;
+			}
+			else {
+				if(!cg_iterate<float>(a, sh, a.rxf, a.ryf, a.pxf, a.pyf, a.apxf, a.apyf, a.Pxf, a.Pyf, a.exf, a.eyf, max_it))
+					return;
+			}
 			for(long long j = gtid; j < S; j += gstride) {
 				a.vx[j] += (double) a.exf[j];
 				a.vy[j] += (double) a.eyf[j];
@@ -572,7 +939,7 @@ __global__ void __launch_bounds__(CG_THREADS) cg_kernel(const CGArgs a) {
 					sh.beta[c] = 0.0;
 					if(sh.zero[c]) continue;
 					sh.act[c] = (sh.rn2[c] < s_goal[c]) ? 0 : 1;
-					if(sh.act[c] && sh.rn2[c] > 0.25 * s_prev[c]) s_fallback = 1;
+					if(sh.act[c] && !(sh.rn2[c] <= 0.25 * s_prev[c])) s_fallback = 1;
 				}
 			}
 			__syncthreads();
@@ -609,10 +976,13 @@ __global__ void __launch_bounds__(CG_THREADS) cg_kernel(const CGArgs a) {
 	}
 }
 
-int cg_grid_blocks(int device) {
+constexpr size_t LEARNED_SMEM = sizeof(float) * UNET_MAX_LAYER_PARAMS;
+
+int cg_grid_blocks(int device, bool learned) {
 	int sms = 0, per_sm = 0;
 	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cg_kernel, CG_THREADS, 0);
+	if(learned) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cg_kernel<true>, CG_THREADS, LEARNED_SMEM);
+	else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cg_kernel<false>, CG_THREADS, 0);
 	if(per_sm < 1) per_sm = 1;
 	if(per_sm > 2) per_sm = 2;
 	return sms * per_sm;
@@ -624,14 +994,16 @@ cudaError_t launch_cg(const CGArgs &a, int blocks, cudaStream_t s) {
 	cudaLaunchConfig_t cfg = {};
 	cfg.gridDim = dim3(blocks);
 	cfg.blockDim = dim3(CG_THREADS);
-	cfg.dynamicSmemBytes = 0;
+	const bool learned = a.unet_params != nullptr && a.mixed;
+	cfg.dynamicSmemBytes = learned ? LEARNED_SMEM : 0;
 	cfg.stream = s;
 	cudaLaunchAttribute attr[1];
 	attr[0].id = cudaLaunchAttributeCooperative;
 	attr[0].val.cooperative = 1;
 	cfg.attrs = attr;
 	cfg.numAttrs = 1;
-	return cudaLaunchKernelEx(&cfg, cg_kernel, a);
+	if(learned) return cudaLaunchKernelEx(&cfg, cg_kernel<true>, a);
+	return cudaLaunchKernelEx(&cfg, cg_kernel<false>, a);
 }
 
 }  // namespace rc

@@ -19,11 +19,13 @@
 //     [rng] -> cell(predictor) -> gather(phi*) -> cell(forces, rhs) -> CG ->
 //     cell(corrector) -> [repack] -> gather(phi^{n+1}) -> cell(forces, rhs) -> CG
 #include "rc_kernels.cuh"
+#include "rc_unet_train.cuh"
 #include "../../include/rheocell_gb300.h"
 
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -101,6 +103,16 @@ struct rc_engine {
 	};
 	std::vector<StepGraph> graphs;
 	bool use_graphs = true;
+	// learned preconditioner
+	int solver = RC_SOLVER_PLAIN;
+	float *unet_params = nullptr;  // FP32 network parameters (null: none yet)
+	UNetActs unet{};               // activations for the two velocity components
+	float *zxf = nullptr, *zyf = nullptr;
+	int cg_blocks_learned = 0;
+	// harvested training samples
+	float *harv_in = nullptr, *harv_tgt = nullptr, *harv_s = nullptr;
+	int *harv_count = nullptr;
+	int harv_cap = 0, harv_every = 4, harv_per_solve = 4;
 };
 
 static cudaEvent_t get_event(rc_engine *e) {
@@ -285,8 +297,26 @@ static void solve(rc_engine *e, int phase) {
 	g.Pyf = e->Pyf;
 	g.exf = e->exf;
 	g.eyf = e->eyf;
+	int blocks = e->cg_blocks;
+	if(e->solver == RC_SOLVER_LEARNED) {
+		g.mixed = 1;
+		g.unet_params = e->unet_params;
+		g.unet = e->unet;
+		g.zxf = e->zxf;
+		g.zyf = e->zyf;
+		blocks = e->cg_blocks_learned;
+	}
+	else if(e->harv_cap > 0 && !g.mixed) {
+		g.harv_in = e->harv_in;
+		g.harv_tgt = e->harv_tgt;
+		g.harv_s = e->harv_s;
+		g.harv_count = e->harv_count;
+		g.harv_cap = e->harv_cap;
+		g.harv_every = e->harv_every;
+		g.harv_per_solve = e->harv_per_solve;
+	}
 	StageMark sm(e, RC_TIMER_SOLVE);
-	const cudaError_t c = launch_cg(g, e->cg_blocks, e->stream);
+	const cudaError_t c = launch_cg(g, blocks, e->stream);
 	e->launches += 1;
 	if(c != cudaSuccess && e->launch_error.empty()) e->launch_error = cudaGetErrorString(c);
 }
@@ -721,7 +751,7 @@ int rc_batch_create(const rc_params *params, int n_layers, const rc_box *boxes, 
 			   (rc = dalloc(e, &e->Pxf, L2)) || (rc = dalloc(e, &e->Pyf, L2)))
 				return bail(rc);
 		}
-		e->cg_blocks = cg_grid_blocks(device);
+		e->cg_blocks = cg_grid_blocks(device, false);
 	}
 	if(cudaMallocHost(&e->st_host, sizeof(DevStatus)) != cudaSuccess) return bail(set_err(e, RC_ERR_OOM, "pinned alloc failed"));
 
@@ -981,6 +1011,259 @@ int rc_set_stream(rc_engine *e, void *cuda_stream) {
 	if(!e) return RC_ERR_INVALID;
 	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
 	e->stream = cuda_stream ? (cudaStream_t) cuda_stream : e->own_stream;
+	return RC_OK;
+}
+
+// --- learned preconditioner -----------------------------------------------------
+
+static void dfree(rc_engine *e, void *p) {
+	if(!p) return;
+	cudaFree(p);
+	e->allocs.erase(std::remove(e->allocs.begin(), e->allocs.end(), p), e->allocs.end());
+}
+
+static void drop_graphs(rc_engine *e) {
+	for(auto &g : e->graphs) cudaGraphExecDestroy(g.exec);
+	e->graphs.clear();
+}
+
+static bool is_wet_engine(const rc_engine *e) { return e->fx != nullptr; }
+
+int rc_learned_harvest(rc_engine *e, int capacity, int every, int per_solve) {
+	if(!e) return RC_ERR_INVALID;
+	if(!is_wet_engine(e)) return set_err(e, RC_ERR_UNSUPPORTED, "rc_learned_harvest: the engine has no viscous solve");
+	if(capacity < 0 || (capacity > 0 && (every < 1 || per_solve < 1)))
+		return set_err(e, RC_ERR_INVALID, "rc_learned_harvest: capacity %d, every %d, per_solve %d", capacity, every, per_solve);
+	CUDA_TRY(e, cudaSetDevice(e->device));
+	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+	dfree(e, e->harv_in);
+	dfree(e, e->harv_tgt);
+	dfree(e, e->harv_s);
+	dfree(e, e->harv_count);
+	e->harv_in = e->harv_tgt = e->harv_s = nullptr;
+	e->harv_count = nullptr;
+	e->harv_cap = 0;
+	drop_graphs(e);
+	if(capacity == 0) return RC_OK;
+	const size_t L2 = (size_t) e->L * e->L;
+	int rc;
+	if((rc = dalloc(e, &e->harv_in, (size_t) capacity * L2 * 2)) || (rc = dalloc(e, &e->harv_tgt, (size_t) capacity * L2)) ||
+	   (rc = dalloc(e, &e->harv_s, (size_t) capacity)) || (rc = dalloc(e, &e->harv_count, 1)))
+		return rc;
+	e->harv_cap = capacity;
+	e->harv_every = every;
+	e->harv_per_solve = per_solve;
+	return RC_OK;
+}
+
+int rc_learned_harvested(rc_engine *e) {
+	if(!e || !e->harv_count) return 0;
+	int n = 0;
+	cudaSetDevice(e->device);
+	cudaStreamSynchronize(e->stream);
+	if(cudaMemcpy(&n, e->harv_count, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return 0;
+	return n;
+}
+
+static unsigned long long splitmix(unsigned long long &x) {
+	unsigned long long z = (x += 0x9E3779B97F4A7C15ULL);
+	z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+	z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+	return z ^ (z >> 31);
+}
+
+static void shuffle(std::vector<int> &v, unsigned long long &st) {
+	for(size_t i = v.size(); i > 1; i--) {
+		const size_t j = (size_t) (splitmix(st) % i);
+		std::swap(v[i - 1], v[j]);
+	}
+}
+
+// He initialisation: normal(0, sqrt(2 / (9 c_in))) weights (Box-Muller on
+// splitmix64 uniforms), zero biases.
+static void init_params(std::vector<float> &p, unsigned long long seed) {
+	unsigned long long st = seed ^ 0x5DEECE66DULL;
+	p.assign(UNET_PARAMS, 0.f);
+	for(int l = 0; l < UNET_LAYERS; l++) {
+		const UNetLayerDesc d = unet_layer(l);
+		const double sd = sqrt(2.0 / (9.0 * d.ci));
+		const int n = 9 * d.ci * d.co;
+		for(int k = 0; k < n; k++) {
+			const double u1 = ((splitmix(st) >> 11) + 0.5) / 9007199254740992.0;
+			const double u2 = ((splitmix(st) >> 11) + 0.5) / 9007199254740992.0;
+			p[(size_t) unet_weight_offset(l) + k] = (float) (sd * sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2));
+		}
+	}
+}
+
+// mean loss of the network in T over samples idx (device copy in didx)
+static double eval_loss(UNetTrainer &T, rc_engine *e, const std::vector<int> &idx, int *didx, double *dacc, int cap) {
+	if(idx.empty()) return 0.0;
+	cudaMemsetAsync(dacc, 0, sizeof(double), e->stream);
+	cudaMemcpyAsync(didx, idx.data(), sizeof(int) * idx.size(), cudaMemcpyHostToDevice, e->stream);
+	for(size_t b0 = 0; b0 < idx.size(); b0 += (size_t) cap) {
+		const int n = (int) std::min((size_t) cap, idx.size() - b0);
+		T.batch = n;
+		unet_gather(T, e->harv_in, e->harv_tgt, didx + b0, n, e->stream);
+		unet_forward(T, T.params, e->stream);
+		unet_loss(T, e->stream);
+		unet_accumulate_loss(T, dacc, e->stream);
+	}
+	T.batch = cap;
+	double h = 0.0;
+	cudaMemcpyAsync(&h, dacc, sizeof(double), cudaMemcpyDeviceToHost, e->stream);
+	cudaStreamSynchronize(e->stream);
+	return h / (double) idx.size();
+}
+
+int rc_learned_train(rc_engine *e, const rc_train_options *o, rc_train_report *rep) {
+	if(!e || !o) return RC_ERR_INVALID;
+	if(!e->harv_count) return set_err(e, RC_ERR_INVALID, "rc_learned_train: no harvested samples (call rc_learned_harvest first)");
+	if(e->L % 4 != 0 || e->L < 8) return set_err(e, RC_ERR_UNSUPPORTED, "rc_learned_train: box side %d is not a multiple of 4", e->L);
+	const int epochs = o->epochs > 0 ? o->epochs : 8;
+	const int batch = o->batch > 0 ? o->batch : 8;
+	const float lr = (float) (o->learning_rate > 0 ? o->learning_rate : 1e-3);
+	const double vfrac = o->validation >= 0 ? o->validation : 0.1;
+	CUDA_TRY(e, cudaSetDevice(e->device));
+	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+	const auto t0 = std::chrono::steady_clock::now();
+	int count = 0;
+	CUDA_TRY(e, cudaMemcpy(&count, e->harv_count, sizeof(int), cudaMemcpyDeviceToHost));
+	std::vector<float> sc((size_t) std::max(count, 1));
+	if(count) CUDA_TRY(e, cudaMemcpy(sc.data(), e->harv_s, sizeof(float) * (size_t) count, cudaMemcpyDeviceToHost));
+	std::vector<int> valid;
+	for(int q = 0; q < count; q++)
+		if(sc[(size_t) q] > 0.f) valid.push_back(q);
+	unsigned long long st = o->seed;
+	shuffle(valid, st);
+	if(o->max_samples > 0 && (int) valid.size() > o->max_samples) valid.resize((size_t) o->max_samples);
+	if(valid.size() < 2) return set_err(e, RC_ERR_INVALID, "rc_learned_train: %zu usable samples", valid.size());
+	int nval = (int) llround(vfrac * (double) valid.size());
+	if(vfrac > 0 && nval < 1) nval = 1;
+	if(nval >= (int) valid.size()) nval = (int) valid.size() - 1;
+	std::vector<int> val(valid.begin(), valid.begin() + nval), train(valid.begin() + nval, valid.end());
+	UNetTrainer T;
+	const int rc0 = unet_trainer_init(T, e->L, batch);
+	if(rc0) {
+		unet_trainer_free(T);
+		return set_err(e, rc0 == -2 ? RC_ERR_INVALID : RC_ERR_OOM, "rc_learned_train: trainer allocation failed");
+	}
+	int *didx = nullptr;
+	double *dacc = nullptr;
+	if(cudaMalloc(&didx, sizeof(int) * valid.size()) != cudaSuccess || cudaMalloc(&dacc, sizeof(double)) != cudaSuccess) {
+		cudaFree(didx);
+		unet_trainer_free(T);
+		return set_err(e, RC_ERR_OOM, "rc_learned_train: allocation failed");
+	}
+	if(o->init || !e->unet_params) {
+		std::vector<float> p;
+		init_params(p, o->seed);
+		cudaMemcpy(T.params, p.data(), sizeof(float) * UNET_PARAMS, cudaMemcpyHostToDevice);
+	}
+	else
+		cudaMemcpy(T.params, e->unet_params, sizeof(float) * UNET_PARAMS, cudaMemcpyDeviceToDevice);
+	rc_train_report r;
+	memset(&r, 0, sizeof(r));
+	r.samples = (int) valid.size();
+	r.train_samples = (int) train.size();
+	r.validation_samples = (int) val.size();
+	r.validation_loss_init = eval_loss(T, e, val, didx, dacc, batch);
+	for(int ep = 0; ep < epochs; ep++) {
+		shuffle(train, st);
+		cudaMemsetAsync(dacc, 0, sizeof(double), e->stream);
+		cudaMemcpyAsync(didx, train.data(), sizeof(int) * train.size(), cudaMemcpyHostToDevice, e->stream);
+		for(size_t b0 = 0; b0 < train.size(); b0 += (size_t) batch) {
+			const int n = (int) std::min((size_t) batch, train.size() - b0);
+			T.batch = n;
+			unet_gather(T, e->harv_in, e->harv_tgt, didx + b0, n, e->stream);
+			unet_forward(T, T.params, e->stream);
+			unet_loss(T, e->stream);
+			unet_accumulate_loss(T, dacc, e->stream);
+			unet_backward(T, T.params, e->stream);
+			unet_adam(T, lr, e->stream);
+			r.steps++;
+		}
+		T.batch = batch;
+		double h = 0.0;
+		cudaMemcpyAsync(&h, dacc, sizeof(double), cudaMemcpyDeviceToHost, e->stream);
+		cudaStreamSynchronize(e->stream);
+		const double mean = h / (double) train.size();
+		if(ep == 0) r.loss_first_epoch = mean;
+		r.loss_last_epoch = mean;
+		r.epochs = ep + 1;
+	}
+	r.validation_loss = eval_loss(T, e, val, didx, dacc, batch);
+	int rc = RC_OK;
+	if(!e->unet_params) rc = dalloc(e, &e->unet_params, UNET_PARAMS);
+	if(rc == RC_OK) cudaMemcpyAsync(e->unet_params, T.params, sizeof(float) * UNET_PARAMS, cudaMemcpyDeviceToDevice, e->stream);
+	const cudaError_t ce = cudaStreamSynchronize(e->stream);
+	cudaFree(didx);
+	cudaFree(dacc);
+	unet_trainer_free(T);
+	if(rc) return rc;
+	if(ce != cudaSuccess) return set_err(e, RC_ERR_CUDA, "rc_learned_train: %s", cudaGetErrorString(ce));
+	r.ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+	if(rep) *rep = r;
+	return RC_OK;
+}
+
+int rc_learned_get_params(rc_engine *e, double *params) {
+	if(!e || !params) return RC_ERR_INVALID;
+	if(!e->unet_params) return set_err(e, RC_ERR_INVALID, "rc_learned_get_params: the engine has no network parameters");
+	CUDA_TRY(e, cudaSetDevice(e->device));
+	std::vector<float> h(UNET_PARAMS);
+	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+	CUDA_TRY(e, cudaMemcpy(h.data(), e->unet_params, sizeof(float) * UNET_PARAMS, cudaMemcpyDeviceToHost));
+	for(int k = 0; k < UNET_PARAMS; k++) params[k] = h[(size_t) k];
+	return RC_OK;
+}
+
+int rc_learned_set_params(rc_engine *e, const double *params) {
+	if(!e || !params) return RC_ERR_INVALID;
+	CUDA_TRY(e, cudaSetDevice(e->device));
+	int rc;
+	if(!e->unet_params && (rc = dalloc(e, &e->unet_params, UNET_PARAMS))) return rc;
+	std::vector<float> h(UNET_PARAMS);
+	for(int k = 0; k < UNET_PARAMS; k++) h[(size_t) k] = (float) params[k];
+	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+	CUDA_TRY(e, cudaMemcpy(e->unet_params, h.data(), sizeof(float) * UNET_PARAMS, cudaMemcpyHostToDevice));
+	return RC_OK;
+}
+
+int rc_set_solver(rc_engine *e, int solver) {
+	if(!e) return RC_ERR_INVALID;
+	if(solver != RC_SOLVER_PLAIN && solver != RC_SOLVER_LEARNED)
+		return set_err(e, RC_ERR_INVALID, "rc_set_solver: unknown solver %d", solver);
+	CUDA_TRY(e, cudaSetDevice(e->device));
+	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+	if(solver == RC_SOLVER_LEARNED) {
+		if(!is_wet_engine(e)) return set_err(e, RC_ERR_UNSUPPORTED, "rc_set_solver: the engine has no viscous solve");
+		if(e->L % 4 != 0 || e->L < 8)
+			return set_err(e, RC_ERR_UNSUPPORTED, "rc_set_solver: box side %d is not a multiple of 4", e->L);
+		if(!e->unet_params) return set_err(e, RC_ERR_INVALID, "rc_set_solver: no network parameters (train or set them first)");
+		const size_t cap = (size_t) e->S_cap, L2 = (size_t) e->L * e->L;
+		int rc;
+		if(!e->rxf) {
+			if((rc = dalloc(e, &e->rxf, cap)) || (rc = dalloc(e, &e->ryf, cap)) || (rc = dalloc(e, &e->pxf, cap)) ||
+			   (rc = dalloc(e, &e->pyf, cap)) || (rc = dalloc(e, &e->exf, cap)) || (rc = dalloc(e, &e->eyf, cap)) ||
+			   (rc = dalloc(e, &e->apxf, cap)) || (rc = dalloc(e, &e->apyf, cap)) || (rc = dalloc(e, &e->Pxf, L2)) ||
+			   (rc = dalloc(e, &e->Pyf, L2)))
+				return rc;
+		}
+		if(!e->zxf) {
+			const size_t p0 = 2 * L2, p1 = p0 / 4, p2 = p0 / 16;
+			UNetActs &A = e->unet;
+			if((rc = dalloc(e, &e->zxf, cap)) || (rc = dalloc(e, &e->zyf, cap)) || (rc = dalloc(e, &A.x0, p0 * 2)) ||
+			   (rc = dalloc(e, &A.e0a, p0 * 16)) || (rc = dalloc(e, &A.s0, p0 * 16)) || (rc = dalloc(e, &A.d0a, p0 * 16)) ||
+			   (rc = dalloc(e, &A.t0, p0 * 16)) || (rc = dalloc(e, &A.out, p0)) || (rc = dalloc(e, &A.e1a, p1 * 16)) ||
+			   (rc = dalloc(e, &A.s1, p1 * 16)) || (rc = dalloc(e, &A.d1a, p1 * 16)) || (rc = dalloc(e, &A.t1, p1 * 16)) ||
+			   (rc = dalloc(e, &A.b0, p2 * 16)) || (rc = dalloc(e, &A.t2, p2 * 16)))
+				return rc;
+		}
+		if(!e->cg_blocks_learned) e->cg_blocks_learned = cg_grid_blocks(e->device, true);
+	}
+	if(solver != e->solver) drop_graphs(e);
+	e->solver = solver;
 	return RC_OK;
 }
 

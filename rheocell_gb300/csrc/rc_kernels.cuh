@@ -3,6 +3,7 @@
 #pragma once
 
 #include "rc_common.cuh"
+#include "rc_unet.cuh"
 
 namespace rc {
 
@@ -70,6 +71,17 @@ struct CGArgs {
 	double inner_tol;        // mixed: relative residual reduction per refinement sweep
 	float *rxf, *ryf, *pxf, *pyf, *apxf, *apyf, *Pxf, *Pyf;
 	float *exf, *eyf;        // mixed: correction of one refinement sweep
+	// learned preconditioner for the inner iterations of the mixed path
+	// (flexible CG); null: Jacobi
+	const float *unet_params;
+	UNetActs unet;           // activations for the two components (batch 2)
+	float *zxf, *zyf;        // z = M r
+	// training samples harvested from the plain FP64 solve; null: none.
+	// Sample q: harv_in[q][L2][2] = (R/s, W), harv_tgt[q][L2] = (X* - X)/s,
+	// harv_s[q] = s (0 marks an unused slot); *harv_count samples stored.
+	float *harv_in, *harv_tgt, *harv_s;
+	int *harv_count;
+	int harv_cap, harv_every, harv_per_solve;
 };
 
 cudaError_t configure_kernels();
@@ -81,7 +93,7 @@ void launch_bins(CellDev *cells, const LayerDev *layers, int N, int *bin_count, 
                  DevStatus *st, cudaStream_t s);
 void launch_repack(CellArgs a, double *scratch_phi, double *scratch_rep, long long cap, cudaStream_t s);
 void launch_box_gather(const BoxArgs &a, cudaStream_t s);
-int cg_grid_blocks(int device);
+int cg_grid_blocks(int device, bool learned);
 cudaError_t launch_cg(const CGArgs &a, int blocks, cudaStream_t s);
 
 }  // namespace rc

@@ -157,6 +157,36 @@ class Engine:
     def upload(self, hc: HostCells, mask: int) -> None:
         self._check(self._lib.rc_upload(self.h, hc.arr, mask), "rc_upload")
 
+    # --- learned preconditioner of the viscous solve ---------------------------
+
+    def harvest(self, capacity: int, every: int = 4, per_solve: int = 4) -> None:
+        """Collect training samples from the following plain FP64 solves."""
+        self._check(self._lib.rc_learned_harvest(self.h, capacity, every, per_solve), "rc_learned_harvest")
+
+    def harvested(self) -> int:
+        return int(self._lib.rc_learned_harvested(self.h))
+
+    def train(self, epochs: int = 8, batch: int = 8, learning_rate: float = 1e-3, validation: float = 0.1,
+              seed: int = 0, init: bool = True, max_samples: int = 0) -> Dict[str, float]:
+        """Train the network on the harvested samples (device kernels)."""
+        o = abi.RcTrainOptions(epochs, batch, learning_rate, validation, seed, int(init), max_samples)
+        r = abi.RcTrainReport()
+        self._check(self._lib.rc_learned_train(self.h, C.byref(o), C.byref(r)), "rc_learned_train")
+        return {name: getattr(r, name) for name, _ in abi.RcTrainReport._fields_}
+
+    def set_solver(self, solver: int) -> None:
+        self._check(self._lib.rc_set_solver(self.h, solver), "rc_set_solver")
+
+    def get_params(self) -> np.ndarray:
+        p = np.zeros(abi.RC_UNET_PARAMS)
+        self._check(self._lib.rc_learned_get_params(self.h, p.ctypes.data_as(abi.DP)), "rc_learned_get_params")
+        return p
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        assert p.size == abi.RC_UNET_PARAMS
+        self._check(self._lib.rc_learned_set_params(self.h, p.ctypes.data_as(abi.DP)), "rc_learned_set_params")
+
     def close(self):
         if self.h:
             self._lib.rc_destroy(self.h)

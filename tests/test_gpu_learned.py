@@ -1,0 +1,89 @@
+"""Learned preconditioner of the viscous solve: samples harvested from the
+plain FP64 solve, device training, and the flexible-CG solve that uses the
+network.  Its velocities must stay within 1e-7 (relative) of the FP64 oracle,
+the solve must stop at the FP64 tolerance, and the trained network must cut
+the inner iterations of the mixed solve compared with the same solve
+without it."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+from rheocell_gb300 import abi, engine, generator as g
+from tests.common import build_inputs, case_from_monolayer, rel_err
+
+pytestmark = pytest.mark.gpu
+
+WARM = 20  # plain FP64 steps that harvest the training samples
+
+
+def _case(L=64, n=16, seed=31):
+    m = g.make_monolayer(L, n, seed=seed)
+    return case_from_monolayer(m, dict(g.WET_NEMATIC, zetaQ_inter=0.02), seed=seed + 1)
+
+
+@pytest.fixture(scope="module")
+def trained():
+    keys, m = _case()
+    p, cells = build_inputs(keys, m)
+    e = engine.Engine(p, m.L, cells)
+    e.set_phase(1)
+    e.harvest(capacity=2000, every=3, per_solve=6)
+    e.step(WARM)
+    n = e.harvested()
+    rep = e.train(epochs=40, batch=8, learning_rate=2e-3, seed=1)
+    return keys, m, e, n, rep
+
+
+def test_training_reduces_validation_loss(trained):
+    _, _, _, n, rep = trained
+    print("harvested", n, "report", rep)
+    assert n >= 200
+    assert rep["samples"] > 100 and rep["steps"] > 0
+    assert rep["validation_loss"] < 0.3 * rep["validation_loss_init"], rep
+    assert rep["loss_last_epoch"] < rep["loss_first_epoch"], rep
+
+
+def test_learned_solve_matches_fp64_oracle(trained):
+    keys, m, e, _, _ = trained
+    steps = 4
+    e.set_solver(abi.RC_SOLVER_LEARNED)
+    st = e.step(steps)
+    print("learned solve:", st.cg_iterations, st.refinements, st.cg_max_rel_residual)
+    assert st.cg_max_rel_residual < 1e-8
+    got = e.state()
+    # the oracle from the same initial state, plain FP64 CG throughout
+    p, cells = build_inputs(keys, m)
+    o = orc.OracleSim(p, m.L, cells)
+    o.set_phase(1)
+    o.step(WARM + steps)
+    want = o.state()
+    for k in ("vx", "vy", "phi", "area", "com_x"):
+        assert rel_err(got[k], want[k]) < 1e-7, k
+    e.set_solver(abi.RC_SOLVER_PLAIN)
+
+
+def test_network_cuts_inner_iterations(trained):
+    """Same state, same mixed-precision refinement: inner iterations with the
+    network (flexible CG) against the Jacobi inner iterations without it."""
+    keys, m, e, _, _ = trained
+    params = e.get_params()
+
+    def run(solver):
+        p, cells = build_inputs(keys, m, precision=abi.RC_PRECISION_MIXED)
+        f = engine.Engine(p, m.L, cells)
+        f.set_phase(1)
+        f.step(WARM)
+        f.set_params(params)
+        f.set_solver(solver)
+        s = f.step(4)
+        out = (s.cg_iterations, s.cg_max_rel_residual)
+        f.close()
+        return out
+
+    it_plain, res_plain = run(abi.RC_SOLVER_PLAIN)
+    it_learned, res_learned = run(abi.RC_SOLVER_LEARNED)
+    print("inner iterations: plain", it_plain, res_plain, "learned", it_learned, res_learned)
+    assert res_plain < 1e-8 and res_learned < 1e-8
+    assert it_learned < 0.5 * it_plain, (it_learned, it_plain)
