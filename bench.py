@@ -150,6 +150,65 @@ def fused_bytes_per_site(model):
     return 72.0
 
 
+def solve_stage(eng, lib, steps, flush):
+    """(solve ms per step, CG iterations per solve) over `steps` steps, from
+    the stage timers (CUDA events around each solve launch)."""
+    import torch
+    from rheocell_gb300 import abi
+    lib.rc_set_timing(eng.h, 1)
+    lib.rc_timers(eng.h, None, None, 1)
+    st = abi.RcStepStats()
+    lib.rc_wait(eng.h, C.byref(st))
+    for _ in range(steps):
+        flush.zero_()
+        lib.rc_step_async(eng.h, 1)
+    torch.cuda.synchronize()
+    lib.rc_wait(eng.h, C.byref(st))
+    tms = (C.c_double * 6)()
+    tn = (C.c_longlong * 6)()
+    lib.rc_timers(eng.h, tms, tn, 1)
+    lib.rc_set_timing(eng.h, 0)
+    return tms[3] / steps, st.cg_iterations / max(st.cg_solves, 1), st.cg_max_rel_residual
+
+
+def prepare_learned(args, eng, lib):
+    """Harvest samples from the plain FP64 solve, train the network on the
+    device, then time the solve stage with the plain FP64 CG and with the
+    learned flexible CG on the same state; leaves the learned solver on."""
+    import torch
+    from rheocell_gb300 import abi
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    eng.harvest(capacity=args.harvest_capacity, every=3, per_solve=6)
+    t0 = time.perf_counter()
+    eng.step(args.harvest_steps)
+    harvest_s = time.perf_counter() - t0
+    n = eng.harvested()
+    eng.harvest(args.harvest_capacity, 3, 0)  # stop collecting, keep the samples
+    rep = eng.train(epochs=args.train_epochs, batch=8, learning_rate=2e-3, seed=1)
+    k = max(2, min(args.steps, 10))
+    plain_ms, plain_it, plain_res = solve_stage(eng, lib, k, flush)
+    eng.set_solver(abi.RC_SOLVER_LEARNED)
+    solve_stage(eng, lib, 1, flush)
+    learned_ms, learned_it, learned_res = solve_stage(eng, lib, k, flush)
+    # per-phase breakdown of the learned solve (device clock, one block)
+    phases = None
+    if args.solver_phases:
+        lib.rc_solver_profile(eng.h, 1, None, 0)
+        for _ in range(k):
+            lib.rc_step_async(eng.h, 1)
+        torch.cuda.synchronize()
+        ms = (C.c_double * 15)()
+        lib.rc_solver_profile(eng.h, 0, ms, 15)
+        phases = {nm: round(ms[i] / k, 4) for i, nm in enumerate(abi.SOLVER_PHASES)}
+    return {"harvest_steps": args.harvest_steps, "harvest_s": harvest_s, "samples": n,
+            "training": {kk: (round(v, 6) if isinstance(v, float) else v) for kk, v in rep.items()},
+            "solve_ms_per_step": {"plain_fp64_cg": plain_ms, "learned_fcg": learned_ms,
+                                  "speedup": plain_ms / learned_ms if learned_ms > 0 else None},
+            "iterations_per_solve": {"plain_fp64_cg": plain_it, "learned_fcg_inner": learned_it},
+            "max_rel_residual": {"plain_fp64_cg": plain_res, "learned_fcg": learned_res},
+            "steps_each": k, "phases_ms_per_step": phases}
+
+
 def run_gb300(args, rank, world):
     import torch
     from rheocell_gb300 import abi, engine
@@ -175,6 +234,9 @@ def run_gb300(args, rank, world):
     S = eng.site_count()
     L2 = sum(m.L * m.L for _, m in members)
     n_cells = sum(m.n for _, m in members)
+    learned = None
+    if args.solver == "learned":
+        learned = prepare_learned(args, eng, lib)
     # warm-up
     eng.step(max(args.warmup, 3) if args.warmup >= 0 else 3)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -295,6 +357,10 @@ def run_gb300(args, rank, world):
     }
     if S_after != S:
         out["config"]["sites_after"] = S_after
+    if learned is not None:
+        out["learned_pcg"] = learned
+        out["config"]["solver"] = "learned flexible CG (FP32 inner, FP64 refinement)"
+        out["dtype"] = "f64 fields, f32 solve inner iterations, learned preconditioner"
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, w, members)
     return out
@@ -419,6 +485,11 @@ def main():
     ap.add_argument("--workload", default="wet256", choices=["wet256", "dry140", "ensemble64"])
     ap.add_argument("--precision", default="double", choices=["double", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--solver", default="plain", choices=["plain", "learned"])
+    ap.add_argument("--harvest-steps", type=int, default=30)
+    ap.add_argument("--harvest-capacity", type=int, default=1200)
+    ap.add_argument("--train-epochs", type=int, default=10)
+    ap.add_argument("--solver-phases", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

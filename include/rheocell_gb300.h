@@ -280,6 +280,10 @@ int rc_viscous_resolve_noalloc(rc_engine *e, double *vx, double *vy, long long n
  * and output ([batch][L][L]) may be NULL.  L must be a multiple of 4.
  */
 #define RC_UNET_PARAMS 25937
+/* rc_unet_forward_tc: the network's forward pass as the solve runs it
+ * (BF16 activations, tensor-core layers, FP32 first and last layers);
+ * input [batch][L][L][2], output [batch][L][L]. */
+int rc_unet_forward_tc(int L, int batch, const double *params, const double *input, double *output, int device);
 int rc_unet_loss_grad(int L, int batch, const double *params, const double *input, const double *target,
                       double *loss, double *grad, double *output, int device);
 
@@ -302,7 +306,8 @@ int rc_unet_loss_grad(int L, int batch, const double *params, const double *inpu
  * FP64 solves (RC_PRECISION_DOUBLE and RC_SOLVER_PLAIN): at sweeps 0,
  * every, 2*every, ... (at most per_solve points per solve) each velocity
  * component gives the pair (box residual, box error), until `capacity`
- * samples are stored.  capacity = 0 stops harvesting and frees the store.
+ * samples are stored.  capacity = 0 stops harvesting and frees the store;
+ * per_solve = 0 (capacity > 0) stops collecting and keeps the samples.
  * rc_learned_harvested: samples stored so far (synchronises).
  * rc_learned_train: Adam on the stored samples (device forward and backward
  * kernels); the trained parameters become the engine's.
@@ -311,7 +316,8 @@ int rc_unet_loss_grad(int L, int batch, const double *params, const double *inpu
  * is a multiple of 4).
  */
 #define RC_SOLVER_PLAIN 0
-#define RC_SOLVER_LEARNED 1
+#define RC_SOLVER_LEARNED 1        /* network on the tensor cores (BF16 activations) */
+#define RC_SOLVER_LEARNED_FP32 2   /* the same network in FP32 on the CUDA cores     */
 
 typedef struct rc_train_options {
 	int epochs;                 /* passes over the training samples (<= 0: 8)         */
@@ -340,6 +346,18 @@ int rc_learned_train(rc_engine *e, const rc_train_options *options, rc_train_rep
 int rc_learned_get_params(rc_engine *e, double *params);
 int rc_learned_set_params(rc_engine *e, const double *params);
 int rc_set_solver(rc_engine *e, int solver);
+
+/*
+ * Diagnostic timers of the learned solve, read on the device clock by one
+ * block at the end of each phase (each phase's time includes the grid
+ * barrier that ends it).  enable = 1 zeroes and starts them, 0 stops them;
+ * ms (may be NULL) receives the totals so far, up to n of: network input
+ * gather, first layer, tensor-core layers at levels 0, 1, 2, last layer,
+ * preconditioned residual, flexible-CG phases A, B, C, everything else,
+ * then (within the tensor-core layers) weight staging, operand staging,
+ * MMA issue and completion, epilogue.
+ */
+int rc_solver_profile(rc_engine *e, int enable, double *ms, int n);
 
 /* Sites (sum of LsubX*LsubY) in the current configuration. */
 long long rc_site_count(const rc_engine *e);

@@ -22,6 +22,10 @@ RC_NOALLOC_MAX_BOX_SITES = 16384
 RC_UNET_PARAMS = 25937
 RC_SOLVER_PLAIN = 0
 RC_SOLVER_LEARNED = 1
+RC_SOLVER_LEARNED_FP32 = 2
+SOLVER_PHASES = ["input_gather", "first_layer", "tc_level0", "tc_level1", "tc_level2", "last_layer",
+                 "precond_residual", "fcg_A", "fcg_B", "fcg_C", "other",
+                 "tc_weights", "tc_staging", "tc_mma", "tc_epilogue"]
 
 RC_SIMPLEFIELD = 0
 RC_ACTIVENEMATIC = 1
@@ -156,8 +160,12 @@ def declare(lib: C.CDLL, prefix: str) -> C.CDLL:
         lib.rc_learned_get_params.restype = C.c_int
         lib.rc_learned_set_params.argtypes = [vp, DP]
         lib.rc_learned_set_params.restype = C.c_int
+        lib.rc_solver_profile.argtypes = [vp, C.c_int, DP, C.c_int]
+        lib.rc_solver_profile.restype = C.c_int
         lib.rc_set_solver.argtypes = [vp, C.c_int]
         lib.rc_set_solver.restype = C.c_int
+        lib.rc_unet_forward_tc.argtypes = [C.c_int, C.c_int, DP, DP, DP, C.c_int]
+        lib.rc_unet_forward_tc.restype = C.c_int
         lib.rc_unet_loss_grad.argtypes = [C.c_int, C.c_int, DP, DP, DP, DP, DP, DP, C.c_int]
         lib.rc_unet_loss_grad.restype = C.c_int
         lib.rc_viscous_resolve_noalloc.argtypes = [vp, vp, vp, C.c_longlong, C.POINTER(C.c_int)]
@@ -173,9 +181,9 @@ def declare(lib: C.CDLL, prefix: str) -> C.CDLL:
 
 
 # Every symbol the header declares (checked by the CPU test suite).
-EXPORTED = ["rc_abi_version", "rc_create", "rc_batch_create", "rc_layer_count", "rc_viscous_resolve_noalloc", "rc_unet_loss_grad",
+EXPORTED = ["rc_abi_version", "rc_create", "rc_batch_create", "rc_layer_count", "rc_viscous_resolve_noalloc", "rc_unet_loss_grad", "rc_unet_forward_tc",
             "rc_learned_harvest", "rc_learned_harvested", "rc_learned_train", "rc_learned_get_params",
-            "rc_learned_set_params", "rc_set_solver", "rc_step", "rc_step_async", "rc_wait", "rc_set_phase",
+            "rc_learned_set_params", "rc_set_solver", "rc_solver_profile", "rc_step", "rc_step_async", "rc_wait", "rc_set_phase",
             "rc_get_sizes", "rc_download", "rc_upload", "rc_download_phi", "rc_upload_phi", "rc_set_stream",
             "rc_set_timing", "rc_timers", "rc_site_count", "rc_last_error", "rc_destroy"]
 

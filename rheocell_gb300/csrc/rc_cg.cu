@@ -25,8 +25,8 @@
 // The solve is one persistent cooperative kernel: every phase is a grid-stride
 // loop, and phases are separated by a grid barrier.  Barrier waits are bounded;
 // on timeout the kernel records ERR_BARRIER and returns.  Dot products are
-// summed in a fixed order (per-block tree, then the last block to arrive sums
-// the block partials in block order), so results are bit-reproducible.
+// summed in a fixed order (per-block tree, then every block sums the block
+// partials in block order), so results are bit-reproducible.
 #include "rc_kernels.cuh"
 
 #include <float.h>
@@ -42,80 +42,83 @@ enum { SC_RED = 0 };
 
 __device__ __forceinline__ double ldcg(const double *p) { return __ldcg(p); }
 
-// Grid-wide barrier with an optional fixed-order reduction of nv doubles.
-// v[i] must hold this block's partial sums (valid in thread 0).  On return,
-// out[i] (shared) holds the grid totals in every thread.  Returns false if
-// the barrier timed out anywhere.
-__device__ bool grid_reduce(const CGArgs &a, int nv, const double *v, double *out, double *red) {
-	__shared__ int s_last;
-	__shared__ unsigned s_gen;
-	__shared__ int s_fail;
+struct CGShared {
+	double T[CG_MAX_D + 1], iT[CG_MAX_D + 1];
+	double red[8 * (CG_THREADS / 32 + 1)];  // block_sum<8> scratch
+	double tot[8];
+	double rz[2], thr[2], bn2[2], rn2[2], alpha[2], beta[2];
+	double pap[2], scale[2];  // learned path: p.Ap of the sweep, residual scale
+	float Tf[CG_MAX_D + 1], iTf[CG_MAX_D + 1];  // FP32 copies of T, 1/T (learned path)
+	int act[2], it[2], first, zero[2];
+	int hbase, hm;            // harvesting: first slot of this solve, points taken
+	unsigned long long tmark; // diagnostic phase timers: last mark (block 0, thread 0)
+	unsigned epoch;           // grid barriers passed (the same count in every block)
+	int fail;                 // a barrier wait ran out (sticky)
+};
+
+// Grid-wide barrier with an optional fixed-order reduction of nv <= 8
+// doubles.  v[i] holds this block's partial sums (valid in thread 0); on
+// return sh.tot[i] holds the grid totals.  Every block arrives once on a
+// monotonic counter (a.bar[0], zero at launch) and waits for it to reach
+// (barriers passed + 1) * blocks; then every block sums the partials itself,
+// in block order, so all blocks obtain the same, reproducible totals.  The
+// partials alternate between two buffers by barrier parity, so a block that
+// runs ahead never overwrites sums another block is still reading.  Returns
+// false if the wait ran out (then ERR_BARRIER is set).
+__device__ __forceinline__ bool grid_reduce(const CGArgs &a, CGShared &sh, int nv, const double *v) {
 	const unsigned nb = gridDim.x;
+	__syncthreads();  // the whole block's writes of this phase precede the arrival
 	if(threadIdx.x == 0) {
-		for(int i = 0; i < nv; i++) a.partials[(size_t) i * nb + blockIdx.x] = v[i];
-		s_gen = atomicAdd(&a.bar[1], 0u);
+		const unsigned e = sh.epoch;
+		double *part = a.partials + (size_t) (e & 1u) * 8 * nb;
+		for(int i = 0; i < nv; i++) part[(size_t) i * nb + blockIdx.x] = v[i];
+		const unsigned target = (e + 1u) * nb;
 		__threadfence();
-		const unsigned prev = atomicAdd(&a.bar[0], 1u);
-		s_last = (prev == nb - 1);
-		s_fail = 0;
+		atomicAdd(&a.bar[0], 1u);
+		long long spins = 0;
+		unsigned c;
+		while(true) {
+			asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(c) : "l"(a.bar) : "memory");
+			if((int) (c - target) >= 0) break;
+			if(++spins > BARRIER_SPIN_LIMIT) {
+				atomicOr(&a.st->err, ERR_BARRIER);
+				sh.fail = 1;
+				break;
+			}
+			__nanosleep(20);
+		}
+		sh.epoch = e + 1u;
 	}
 	__syncthreads();
-	if(s_last) {
-		// all values in one block-wide reduction (fixed order: threads stride
-		// the block partials, then the fixed shuffle tree)
+	if(nv > 0) {
+		const double *part = a.partials + (size_t) ((sh.epoch - 1u) & 1u) * 8 * nb;
 		double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 #pragma unroll
 		for(int i = 0; i < 8; i++)
 			if(i < nv)
-				for(unsigned b = threadIdx.x; b < nb; b += blockDim.x) acc[i] += ldcg(&a.partials[(size_t) i * nb + b]);
-		if(nv > 0) {
-			if(nv <= 2) {
-				double t[2] = {acc[0], acc[1]};
-				block_sum<2>(t, red);
-				acc[0] = t[0];
-				acc[1] = t[1];
-			}
-			else if(nv <= 4) {
-				double t[4] = {acc[0], acc[1], acc[2], acc[3]};
-				block_sum<4>(t, red);
+				for(unsigned b = threadIdx.x; b < nb; b += blockDim.x) acc[i] += ldcg(&part[(size_t) i * nb + b]);
+		if(nv <= 2) {
+			double t[2] = {acc[0], acc[1]};
+			block_sum<2>(t, sh.red);
+			acc[0] = t[0];
+			acc[1] = t[1];
+		}
+		else if(nv <= 4) {
+			double t[4] = {acc[0], acc[1], acc[2], acc[3]};
+			block_sum<4>(t, sh.red);
 #pragma unroll
-				for(int i = 0; i < 4; i++) acc[i] = t[i];
-			}
-			else
-				block_sum<8>(acc, red);
-			if(threadIdx.x == 0) {
+			for(int i = 0; i < 4; i++) acc[i] = t[i];
+		}
+		else
+			block_sum<8>(acc, sh.red);
+		if(threadIdx.x == 0) {
 #pragma unroll
-				for(int i = 0; i < 8; i++)
-					if(i < nv) a.scalars[SC_RED + i] = acc[i];
-			}
+			for(int i = 0; i < 8; i++)
+				if(i < nv) sh.tot[i] = acc[i];
 		}
 		__syncthreads();
-		if(threadIdx.x == 0) {
-			__threadfence();
-			atomicExch(&a.bar[0], 0u);
-			__threadfence();
-			atomicAdd(&a.bar[1], 1u);
-		}
 	}
-	else if(threadIdx.x == 0) {
-		long long spins = 0;
-		const volatile unsigned *gen = a.bar + 1;
-		while(*gen == s_gen) {
-			if(++spins > BARRIER_SPIN_LIMIT) {
-				atomicOr(&a.st->err, ERR_BARRIER);
-				s_fail = 1;
-				break;
-			}
-			__nanosleep(32);
-		}
-		__threadfence();
-	}
-	__syncthreads();
-	if(threadIdx.x == 0 && (atomicAdd(&a.st->err, 0) & ERR_BARRIER)) s_fail = 1;
-	__syncthreads();
-	for(int i = threadIdx.x; i < nv; i += blockDim.x) out[i] = ldcg(&a.scalars[SC_RED + i]);
-	__syncthreads();
-	return !s_fail;
+	return !sh.fail;
 }
 
 __device__ __forceinline__ int box_deg(const int *cnt, int k, int L) {
@@ -137,21 +140,32 @@ __device__ __forceinline__ double box_n4(const T *P, int k, int L) {
 	return (double) P[kd] + (double) P[kl] + (double) P[kr] + (double) P[ku];
 }
 
-struct CGShared {
-	double T[CG_MAX_D + 1], iT[CG_MAX_D + 1];
-	double red[8 * (CG_THREADS / 32 + 1)];  // block_sum<8> scratch
-	double tot[8];
-	double rz[2], thr[2], bn2[2], rn2[2], alpha[2], beta[2];
-	double pap[2], scale[2];  // learned path: p.Ap of the sweep, residual scale
-	int act[2], it[2], first, zero[2];
-	int hbase, hm;            // harvesting: first slot of this solve, points taken
-};
+
+__device__ __forceinline__ unsigned long long gtimer() {
+	unsigned long long t;
+	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+	return t;
+}
+
+// Diagnostic phase timers: block 0's thread 0 charges the time since the
+// previous mark (including its wait at the barrier that ended the phase) to
+// phase k.  Phases: 0 network input gather, 1 first layer, 2-4 tensor-core
+// layers of levels 0-2, 5 last layer, 6 preconditioned residual, 7-9 FCG
+// phases A-C, 10 everything else.
+enum { PH_GATHER, PH_E0A, PH_TC0, PH_TC1, PH_TC2, PH_OUT, PH_Z, PH_A, PH_B, PH_C, PH_OTHER, PH_COUNT };
+__device__ __forceinline__ void pmark(const CGArgs &a, CGShared &sh, int k) {
+	if(a.phase_ns && blockIdx.x == 0 && threadIdx.x == 0) {
+		const unsigned long long t = gtimer();
+		a.phase_ns[k] += t - sh.tmark;
+		sh.tmark = t;
+	}
+}
 
 // Cover lists in CSR form for this solve: cov_off[k] = sum of n over box
 // sites before k, cov_idx[cov_off[k] + i] = cover[i][k] (unknowns covering k,
 // in cell order).  Block b scans the contiguous box range it owns; the block
 // totals meet through one grid barrier.
-__device__ bool build_csr(const CGArgs &a, CGShared &sh) {
+__device__ __forceinline__ bool build_csr(const CGArgs &a, CGShared &sh) {
 	const long long L2 = (long long) a.L * a.L;
 	const long long chunk = (L2 + gridDim.x - 1) / gridDim.x;
 	const long long lo = blockIdx.x * chunk, hi = min(L2, lo + chunk);
@@ -173,7 +187,7 @@ __device__ bool build_csr(const CGArgs &a, CGShared &sh) {
 	const int block_total = s_scan[blockDim.x - 1];
 	double v[1] = {(double) block_total};
 	if(threadIdx.x == 0) a.partials[(size_t) 7 * gridDim.x + blockIdx.x] = v[0];
-	if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
+	if(!grid_reduce(a, sh, 0, nullptr)) return false;
 	{
 		double acc[1] = {0.0};
 		for(unsigned b = threadIdx.x; b < blockIdx.x; b += blockDim.x) acc[0] += ldcg(&a.partials[(size_t) 7 * gridDim.x + b]);
@@ -189,7 +203,7 @@ __device__ bool build_csr(const CGArgs &a, CGShared &sh) {
 		off += n;
 	}
 	if(blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) a.cov_off[L2] = (int) off;
-	return grid_reduce(a, 0, nullptr, sh.tot, sh.red);
+	return grid_reduce(a, sh, 0, nullptr);
 }
 
 // Warp-segmented sum of v over consecutive lanes with equal key (keys sorted
@@ -212,7 +226,7 @@ __device__ __forceinline__ T seg_sum(T v, int key, bool &tail) {
 // r = b - A x for both components (x = 0 when `x_zero`), written in FP64 and,
 // for the mixed path, also rounded to FP32.  Reduces |b|^2, |r|^2 and r.M^-1 r
 // (the latter on the stored precision of r) into sh.tot[0..5].
-__device__ bool true_residual(const CGArgs &a, CGShared &sh, bool x_zero, bool to_float) {
+__device__ __forceinline__ bool true_residual(const CGArgs &a, CGShared &sh, bool x_zero, bool to_float) {
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
 	const long long S = a.st->S;
@@ -225,7 +239,7 @@ __device__ bool true_residual(const CGArgs &a, CGShared &sh, bool x_zero, bool t
 			a.Px[k] = 0.0;
 			a.Py[k] = 0.0;
 		}
-		if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
+		if(!grid_reduce(a, sh, 0, nullptr)) return false;
 		const long long E = __ldcg(&a.cov_off[L2]);
 		const long long gwarp = gtid >> 5, nwarps = gstride >> 5;
 		const int lane = threadIdx.x & 31;
@@ -243,7 +257,7 @@ __device__ bool true_residual(const CGArgs &a, CGShared &sh, bool x_zero, bool t
 				atomicAdd(&a.Py[key], sy);
 			}
 		}
-		if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
+		if(!grid_reduce(a, sh, 0, nullptr)) return false;
 	}
 	double v[6] = {0, 0, 0, 0, 0, 0};
 	for(long long j = gtid; j < S; j += gstride) {
@@ -282,7 +296,7 @@ __device__ bool true_residual(const CGArgs &a, CGShared &sh, bool x_zero, bool t
 		}
 	}
 	block_sum<6>(v, sh.red);
-	return grid_reduce(a, 6, v, sh.tot, sh.red);
+	return grid_reduce(a, sh, 6, v);
 }
 
 // Jacobi-preconditioned CG iterations from the state in sh (act, rz, thr) and
@@ -327,7 +341,7 @@ __device__ inline void block_sum_warps(double (&v)[NV], double *scratch) {
 	__syncthreads();
 }
 
-__device__ bool harvest_point(const CGArgs &a, CGShared &sh, const double *ux, const double *uy, const double *rx,
+__device__ __forceinline__ bool harvest_point(const CGArgs &a, CGShared &sh, const double *ux, const double *uy, const double *rx,
                               const double *ry, int m);
 
 template<typename T>
@@ -347,141 +361,195 @@ __device__ __forceinline__ T box_n4T(const T *P, int k, int L) {
 	return P[kd] + P[kl] + P[kr] + P[ku];
 }
 
+// Vectors of one CG run: residual, direction, A p, box sums of p, solution.
+template<typename T>
+struct CGVecs {
+	T *rx, *ry, *px, *py, *apx, *apy, *Pbx, *Pby, *ux, *uy;
+};
+
+// T and 1/T tables in the precision of the iteration
+template<typename T>
+__device__ __forceinline__ const T *tab_T(const CGShared &sh);
+template<typename T>
+__device__ __forceinline__ const T *tab_iT(const CGShared &sh);
+template<>
+__device__ __forceinline__ const double *tab_T<double>(const CGShared &sh) { return sh.T; }
+template<>
+__device__ __forceinline__ const double *tab_iT<double>(const CGShared &sh) { return sh.iT; }
+template<>
+__device__ __forceinline__ const float *tab_T<float>(const CGShared &sh) { return sh.Tf; }
+template<>
+__device__ __forceinline__ const float *tab_iT<float>(const CGShared &sh) { return sh.iTf; }
+
+// Phase A: p = z + beta p (p = z on the first sweep, z = r / diag), box sums
+// P = S p, one thread per cover entry; P is zero on entry (cleared in phase C).
+template<typename T>
+__device__ __forceinline__ bool cg_phase_a(const CGArgs &a, CGShared &sh, const CGVecs<T> &V) {
+	const int L = a.L;
+	const long long L2 = (long long) L * L;
+	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+	const long long gstride = (long long) gridDim.x * blockDim.x;
+	const int ax = sh.act[0], ay = sh.act[1], first = sh.first;
+	const T bx = (T) sh.beta[0], by = (T) sh.beta[1];
+	const T *iTT = tab_iT<T>(sh);
+	const T *rx = V.rx, *ry = V.ry;
+	T *px = V.px, *py = V.py, *Pbx = V.Pbx, *Pby = V.Pby;
+	const int *cov_idx = a.cov_idx, *mapg = a.mapg, *cnt = a.cnt;
+	const long long E = __ldcg(&a.cov_off[L2]);
+	const long long gwarp = gtid >> 5, nwarps = gstride >> 5;
+	const int lane = threadIdx.x & 31;
+	for(long long base = gwarp * 32; base < E; base += nwarps * 32) {
+		const long long t = base + lane;
+		const bool valid = t < E;
+		const int j = valid ? cov_idx[t] : 0;
+		const int key = valid ? mapg[j] : -1;
+		const T id = valid ? iTT[box_deg(cnt, key, L)] : (T) 0;
+		T vx = (T) 0, vy = (T) 0;
+		if(valid && ax) {
+			const T z = id * rx[j];
+			const T p = first ? z : fmaT<T>(bx, px[j], z);
+			px[j] = p;
+			vx = p;
+		}
+		if(valid && ay) {
+			const T z = id * ry[j];
+			const T p = first ? z : fmaT<T>(by, py[j], z);
+			py[j] = p;
+			vy = p;
+		}
+		bool tail = false, tail2 = false;
+		if(ax) vx = seg_sum<T>(vx, key, tail);
+		if(ay) vy = seg_sum<T>(vy, key, tail2);
+		if(valid) {
+			if(ax && tail) atomicAdd(&Pbx[key], vx);
+			if(ay && tail2) atomicAdd(&Pby[key], vy);
+		}
+	}
+	return grid_reduce(a, sh, 0, nullptr);
+}
+
+// Phase B: Ap (stored) and p.Ap into sh.tot[0..1].
+template<typename T>
+__device__ __forceinline__ bool cg_phase_b(const CGArgs &a, CGShared &sh, const CGVecs<T> &V) {
+	const int L = a.L;
+	const long long S = a.st->S;
+	const T neta = (T) (-a.eta * 1.0);
+	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+	const long long gstride = (long long) gridDim.x * blockDim.x;
+	const int ax = sh.act[0], ay = sh.act[1];
+	const T *dT = tab_T<T>(sh);
+	const T *px = V.px, *py = V.py, *Pbx = V.Pbx, *Pby = V.Pby;
+	T *apx = V.apx, *apy = V.apy;
+	const int *mapg = a.mapg, *cnt = a.cnt;
+	T w[2] = {(T) 0, (T) 0};
+	for(long long j = gtid; j < S; j += gstride) {
+		const int k = mapg[j];
+		const T d = dT[box_deg(cnt, k, L)];
+		if(ax) {
+			const T p = px[j];
+			const T ap = fmaT<T>(d, p, neta * box_n4T<T>(Pbx, k, L));
+			apx[j] = ap;
+			w[0] = fmaT<T>(p, ap, w[0]);
+		}
+		if(ay) {
+			const T p = py[j];
+			const T ap = fmaT<T>(d, p, neta * box_n4T<T>(Pby, k, L));
+			apy[j] = ap;
+			w[1] = fmaT<T>(p, ap, w[1]);
+		}
+	}
+	warp_tree<T, 2>(w);
+	double v[2] = {(double) w[0], (double) w[1]};
+	block_sum_warps<2>(v, sh.red);
+	return grid_reduce(a, sh, 2, v);
+}
+
+// Phase C: u += alpha p; r -= alpha Ap; |r|^2 and r.z into sh.tot[0..3];
+// the box sums are cleared for the next phase A.
+template<typename T>
+__device__ __forceinline__ bool cg_phase_c(const CGArgs &a, CGShared &sh, const CGVecs<T> &V) {
+	const int L = a.L;
+	const long long L2 = (long long) L * L;
+	const long long S = a.st->S;
+	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+	const long long gstride = (long long) gridDim.x * blockDim.x;
+	const int ax = sh.act[0], ay = sh.act[1];
+	const T alx = (T) sh.alpha[0], aly = (T) sh.alpha[1];
+	const T *iTT = tab_iT<T>(sh);
+	const T *px = V.px, *py = V.py, *apx = V.apx, *apy = V.apy;
+	T *rx = V.rx, *ry = V.ry, *ux = V.ux, *uy = V.uy, *Pbx = V.Pbx, *Pby = V.Pby;
+	const int *mapg = a.mapg, *cnt = a.cnt;
+	T w[4] = {(T) 0, (T) 0, (T) 0, (T) 0};
+	for(long long j = gtid; j < S; j += gstride) {
+		const int k = mapg[j];
+		const T id = iTT[box_deg(cnt, k, L)];
+		if(ax) {
+			ux[j] = fmaT<T>(alx, px[j], ux[j]);
+			const T r = fmaT<T>(-alx, apx[j], rx[j]);
+			rx[j] = r;
+			w[0] = fmaT<T>(r, r, w[0]);
+			w[2] = fmaT<T>(r, id * r, w[2]);
+		}
+		if(ay) {
+			uy[j] = fmaT<T>(aly, py[j], uy[j]);
+			const T r = fmaT<T>(-aly, apy[j], ry[j]);
+			ry[j] = r;
+			w[1] = fmaT<T>(r, r, w[1]);
+			w[3] = fmaT<T>(r, id * r, w[3]);
+		}
+	}
+	double v[4] = {(double) w[0], (double) w[1], (double) w[2], (double) w[3]};
+	for(long long k = gtid; k < L2; k += gstride) {
+		Pbx[k] = (T) 0;
+		Pby[k] = (T) 0;
+	}
+	block_sum<4>(v, sh.red);
+	return grid_reduce(a, sh, 4, v);
+}
+
 // Jacobi-preconditioned CG iterations from the state in sh (act, rz, thr) and
-// the residual in (rx, ry): Eigen's loop.  Vectors, box sums and the
+// the residual in V.rx, V.ry: Eigen's loop.  Vectors, box sums and the
 // element-wise arithmetic are in T (FP64 for the plain solve, FP32 for the
 // inner solves of the mixed path); every thread's partial dot product is
 // summed into FP64 for the block and grid reductions, and the scalars alpha,
 // beta are FP64.  Updates use fused multiply-adds (the solve is not bitwise
 // Eigen's in any case: its reductions run in a different order).
 template<typename T>
-__device__ bool cg_iterate(const CGArgs &a, CGShared &sh, T *rx, T *ry, T *px, T *py, T *apx, T *apy, T *Pbx, T *Pby,
-                           T *ux, T *uy, long long max_it) {
+__device__ __forceinline__ bool cg_iterate(const CGArgs &a, CGShared &sh, const CGVecs<T> &V, long long max_it) {
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
-	const long long S = a.st->S;
-	const T neta = (T) (-a.eta * 1.0);
 	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
 	const long long gstride = (long long) gridDim.x * blockDim.x;
-	__shared__ T dT[CG_MAX_D + 1], iTT[CG_MAX_D + 1];
 	for(int d = threadIdx.x; d <= CG_MAX_D; d += blockDim.x) {
-		dT[d] = (T) sh.T[d];
-		iTT[d] = (T) sh.iT[d];
+		sh.Tf[d] = (float) sh.T[d];
+		sh.iTf[d] = (float) sh.iT[d];
 	}
 	if(threadIdx.x == 0) sh.first = 1;
 	for(long long k = gtid; k < L2; k += gstride) {
-		Pbx[k] = (T) 0;
-		Pby[k] = (T) 0;
+		V.Pbx[k] = (T) 0;
+		V.Pby[k] = (T) 0;
 	}
-	if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
-	const long long E = __ldcg(&a.cov_off[L2]);
+	if(!grid_reduce(a, sh, 0, nullptr)) return false;
 	long long sweep = 0;
 	while(sh.act[0] || sh.act[1]) {
 		if constexpr(sizeof(T) == sizeof(double)) {
 			if(a.harv_in && !a.mixed && sh.hm < a.harv_per_solve && sweep % a.harv_every == 0 &&
 			   sh.hbase + 2LL * (sh.hm + 1) <= a.harv_cap) {
-				if(!harvest_point(a, sh, ux, uy, rx, ry, sh.hm)) return false;
+				if(!harvest_point(a, sh, V.ux, V.uy, V.rx, V.ry, sh.hm)) return false;
 				if(threadIdx.x == 0) sh.hm++;
 				__syncthreads();
 			}
 		}
 		sweep++;
-		const int ax = sh.act[0], ay = sh.act[1], first = sh.first;
-		const T bx = (T) sh.beta[0], by = (T) sh.beta[1];
-		// Phase A: p = z + beta p (p = z on the first sweep), box sums P = S p,
-		// one thread per cover entry; P is zero on entry (cleared in phase C)
-		{
-			const long long gwarp = gtid >> 5, nwarps = gstride >> 5;
-			const int lane = threadIdx.x & 31;
-			for(long long base = gwarp * 32; base < E; base += nwarps * 32) {
-				const long long t = base + lane;
-				const bool valid = t < E;
-				const int j = valid ? a.cov_idx[t] : 0;
-				const int key = valid ? a.mapg[j] : -1;
-				const T id = valid ? iTT[box_deg(a.cnt, key, L)] : (T) 0;
-				T vx = (T) 0, vy = (T) 0;
-				if(valid && ax) {
-					const T z = id * rx[j];
-					const T p = first ? z : fmaT<T>(bx, px[j], z);
-					px[j] = p;
-					vx = p;
-				}
-				if(valid && ay) {
-					const T z = id * ry[j];
-					const T p = first ? z : fmaT<T>(by, py[j], z);
-					py[j] = p;
-					vy = p;
-				}
-				bool tail = false, tail2 = false;
-				if(ax) vx = seg_sum<T>(vx, key, tail);
-				if(ay) vy = seg_sum<T>(vy, key, tail2);
-				if(valid) {
-					if(ax && tail) atomicAdd(&Pbx[key], vx);
-					if(ay && tail2) atomicAdd(&Pby[key], vy);
-				}
-			}
-		}
-		if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
-		// Phase B: Ap (stored) and p.Ap
-		{
-			T w[2] = {(T) 0, (T) 0};
-			for(long long j = gtid; j < S; j += gstride) {
-				const int k = a.mapg[j];
-				const T d = dT[box_deg(a.cnt, k, L)];
-				if(ax) {
-					const T p = px[j];
-					const T ap = fmaT<T>(d, p, neta * box_n4T<T>(Pbx, k, L));
-					apx[j] = ap;
-					w[0] = fmaT<T>(p, ap, w[0]);
-				}
-				if(ay) {
-					const T p = py[j];
-					const T ap = fmaT<T>(d, p, neta * box_n4T<T>(Pby, k, L));
-					apy[j] = ap;
-					w[1] = fmaT<T>(p, ap, w[1]);
-				}
-			}
-			warp_tree<T, 2>(w);
-			double v[2] = {(double) w[0], (double) w[1]};
-			block_sum_warps<2>(v, sh.red);
-			if(!grid_reduce(a, 2, v, sh.tot, sh.red)) return false;
-		}
+		const int ax = sh.act[0], ay = sh.act[1];
+		if(!cg_phase_a<T>(a, sh, V)) return false;
+		if(!cg_phase_b<T>(a, sh, V)) return false;
 		if(threadIdx.x == 0) {
 			if(ax) sh.alpha[0] = sh.rz[0] / sh.tot[0];
 			if(ay) sh.alpha[1] = sh.rz[1] / sh.tot[1];
 		}
 		__syncthreads();
-		// Phase C: u += alpha p; r -= alpha Ap; |r|^2 and r.z
-		{
-			const T alx = (T) sh.alpha[0], aly = (T) sh.alpha[1];
-			T w[4] = {(T) 0, (T) 0, (T) 0, (T) 0};
-			for(long long j = gtid; j < S; j += gstride) {
-				const int k = a.mapg[j];
-				const T id = iTT[box_deg(a.cnt, k, L)];
-				if(ax) {
-					ux[j] = fmaT<T>(alx, px[j], ux[j]);
-					const T r = fmaT<T>(-alx, apx[j], rx[j]);
-					rx[j] = r;
-					w[0] = fmaT<T>(r, r, w[0]);
-					w[2] = fmaT<T>(r, id * r, w[2]);
-				}
-				if(ay) {
-					uy[j] = fmaT<T>(aly, py[j], uy[j]);
-					const T r = fmaT<T>(-aly, apy[j], ry[j]);
-					ry[j] = r;
-					w[1] = fmaT<T>(r, r, w[1]);
-					w[3] = fmaT<T>(r, id * r, w[3]);
-				}
-			}
-			double v[4] = {(double) w[0], (double) w[1], (double) w[2], (double) w[3]};
-			// clear the box sums for the next sweep's phase A
-			for(long long k = gtid; k < L2; k += gstride) {
-				Pbx[k] = (T) 0;
-				Pby[k] = (T) 0;
-			}
-			block_sum<4>(v, sh.red);
-			if(!grid_reduce(a, 4, v, sh.tot, sh.red)) return false;
-		}
+		if(!cg_phase_c<T>(a, sh, V)) return false;
 		if(threadIdx.x == 0) {
 			for(int c = 0; c < 2; c++) {
 				if(!sh.act[c]) continue;
@@ -522,7 +590,7 @@ __device__ __forceinline__ float box_w(const CGArgs &a, const CGShared &sh, int 
 
 // Record harvest point m: box sums of x (into the target slot) and of r/T
 // (into the input slot) for both components; slots hbase + 2m + c.
-__device__ bool harvest_point(const CGArgs &a, CGShared &sh, const double *ux, const double *uy, const double *rx,
+__device__ __forceinline__ bool harvest_point(const CGArgs &a, CGShared &sh, const double *ux, const double *uy, const double *rx,
                               const double *ry, int m) {
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
@@ -541,7 +609,7 @@ __device__ bool harvest_point(const CGArgs &a, CGShared &sh, const double *ux, c
 		const int c = threadIdx.x;
 		a.harv_s[q0 + c] = sh.act[c] ? (float) sqrt(sh.rn2[c] / (double) a.st->S) : 0.f;
 	}
-	if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
+	if(!grid_reduce(a, sh, 0, nullptr)) return false;
 	const long long E = __ldcg(&a.cov_off[L2]);
 	const long long gwarp = gtid >> 5, nwarps = gstride >> 5;
 	const int lane = threadIdx.x & 31;
@@ -563,12 +631,12 @@ __device__ bool harvest_point(const CGArgs &a, CGShared &sh, const double *ux, c
 			atomicAdd(&a.harv_in[((q0 + 1) * L2 + key) * 2], (float) rys);
 		}
 	}
-	return grid_reduce(a, 0, nullptr, sh.tot, sh.red);
+	return grid_reduce(a, sh, 0, nullptr);
 }
 
 // After the solve: targets (S x* - S x_k) / s and inputs R / s for the
 // points taken, then publish the new sample count.
-__device__ bool harvest_finish(const CGArgs &a, CGShared &sh, const double *ux, const double *uy) {
+__device__ __forceinline__ bool harvest_finish(const CGArgs &a, CGShared &sh, const double *ux, const double *uy) {
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
 	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
@@ -577,7 +645,7 @@ __device__ bool harvest_finish(const CGArgs &a, CGShared &sh, const double *ux, 
 		a.Px[k] = 0.0;
 		a.Py[k] = 0.0;
 	}
-	if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
+	if(!grid_reduce(a, sh, 0, nullptr)) return false;
 	const long long E = __ldcg(&a.cov_off[L2]);
 	const long long gwarp = gtid >> 5, nwarps = gstride >> 5;
 	const int lane = threadIdx.x & 31;
@@ -594,7 +662,7 @@ __device__ bool harvest_finish(const CGArgs &a, CGShared &sh, const double *ux, 
 			atomicAdd(&a.Py[key], sy);
 		}
 	}
-	if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
+	if(!grid_reduce(a, sh, 0, nullptr)) return false;
 	const long long n = 2LL * sh.hm;
 	for(long long e = gtid; e < n * L2; e += gstride) {
 		const long long q = sh.hbase + e / L2, k = e % L2;
@@ -617,7 +685,15 @@ __device__ bool harvest_finish(const CGArgs &a, CGShared &sh, const double *ux, 
 //   E: z_j = (r_j + eta s_c (N4 V_c)[k_j]) / T_j, with r.z and z.Ap reduced
 //      into sh.tot[0..3].
 // Runs in FP32 with FP64 reductions.
-__device__ bool precond_apply(const CGArgs &a, CGShared &sh, float *wsm, const float *iTT) {
+struct TcState {
+	unsigned char *dsm;  // dynamic shared memory (tensor-core staging, FP32 weights)
+	uint32_t tmem;       // allocated TMEM columns
+	uint32_t phase;      // mbarrier parity
+};
+
+__device__ __noinline__ bool precond_apply(const CGArgs &a, CGShared &sh, TcState &tc, const float *iTT) {
+	float *wsm = reinterpret_cast<float *>(tc.dsm);
+	pmark(a, sh, PH_OTHER);
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
 	const long long S = a.st->S;
@@ -645,16 +721,48 @@ __device__ bool precond_apply(const CGArgs &a, CGShared &sh, float *wsm, const f
 			}
 		}
 	}
-	if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
-	for(int l = 0; l < UNET_LAYERS; l++) {
-		const UNetLayerDesc d = unet_layer(l);
-		const int nw = 9 * d.ci * d.co + d.co;
-		const float *src = a.unet_params + unet_weight_offset(l);
-		for(int k = threadIdx.x; k < nw; k += blockDim.x) wsm[k] = src[k];
-		__syncthreads();
-		conv_layer_range(l, unet_src(l, a.unet), wsm, wsm + 9 * d.ci * d.co, unet_dst(l, a.unet), 2, L >> d.level, gtid,
-		                 gstride);
-		if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
+	if(!grid_reduce(a, sh, 0, nullptr)) return false;
+	pmark(a, sh, PH_GATHER);
+	if(a.unet_tc) {
+		// first layer (FP32, CUDA cores) -> BF16; nine tensor-core layers; last layer -> FP32
+		{
+			const int nw = 9 * 2 * 16 + 16;
+			for(int k = threadIdx.x; k < nw; k += blockDim.x) wsm[k] = a.unet_params[unet_weight_offset(L_E0A) + k];
+			__syncthreads();
+			e0a_range(a.unet.x0, wsm, a.unet_bf.e0a, 2, L, gtid, gstride);
+			if(!grid_reduce(a, sh, 0, nullptr)) return false;
+			pmark(a, sh, PH_E0A);
+		}
+		for(int l = L_E0B; l <= L_D0B; l++) {
+			if(!tc_conv_layer(l, unet_tc_src(l, a.unet_bf), a.unet_wpack + unet_pack_offset(l),
+			                  a.unet_params + unet_bias_offset(l), unet_tc_dst(l, a.unet_bf), 2, L >> unet_layer(l).level,
+			                  tc.dsm, tc.tmem, tc.phase, &a.st->err, ERR_MMA, a.phase_ns ? a.phase_ns + PH_COUNT : nullptr))
+				return false;
+			if(!grid_reduce(a, sh, 0, nullptr)) return false;
+			pmark(a, sh, PH_TC0 + unet_layer(l).level);
+		}
+		{
+			__syncthreads();
+			const int nw = 9 * 16 + 1;
+			for(int k = threadIdx.x; k < nw; k += blockDim.x) wsm[k] = a.unet_params[unet_weight_offset(L_OUT) + k];
+			__syncthreads();
+			out_range(a.unet_bf.t0, wsm, a.unet.out, 2, L, gtid, gstride);
+			if(!grid_reduce(a, sh, 0, nullptr)) return false;
+			pmark(a, sh, PH_OUT);
+		}
+	}
+	else {
+		for(int l = 0; l < UNET_LAYERS; l++) {
+			const UNetLayerDesc d = unet_layer(l);
+			const int nw = 9 * d.ci * d.co + d.co;
+			const float *src = a.unet_params + unet_weight_offset(l);
+			__syncthreads();
+			for(int k = threadIdx.x; k < nw; k += blockDim.x) wsm[k] = src[k];
+			__syncthreads();
+			conv_layer_range(l, unet_src(l, a.unet), wsm, wsm + 9 * d.ci * d.co, unet_dst(l, a.unet), 2, L >> d.level,
+			                 gtid, gstride);
+			if(!grid_reduce(a, sh, 0, nullptr)) return false;
+		}
 	}
 	const float es0 = (float) (a.eta * sh.scale[0]), es1 = (float) (a.eta * sh.scale[1]);
 	const float *V = a.unet.out;
@@ -675,30 +783,154 @@ __device__ bool precond_apply(const CGArgs &a, CGShared &sh, float *wsm, const f
 	warp_tree<float, 4>(w);
 	double v[4] = {(double) w[0], (double) w[1], (double) w[2], (double) w[3]};
 	block_sum_warps<4>(v, sh.red);
-	return grid_reduce(a, 4, v, sh.tot, sh.red);
+	const bool ok = grid_reduce(a, sh, 4, v);
+	pmark(a, sh, PH_Z);
+	return ok;
 }
 
 // Flexible CG (Notay's FCG(1): beta = -z'.Ap / p.Ap) on the FP32 correction
 // system A e = r of one refinement sweep, preconditioned by the network.
 // Same conventions as cg_iterate<float>: r in rxf/ryf, e in exf/eyf, stop at
 // |r|^2 < thr per component.
-__device__ bool fcg_iterate(const CGArgs &a, CGShared &sh, float *wsm, long long max_it) {
+// Flexible CG phases of the learned path (each its own function, so that
+// each gets the register file to itself).
+// Phase A: p = z + beta p (p = z on the first sweep), box sums P = S p.
+__device__ __noinline__ bool fcg_phase_a(const CGArgs &a, CGShared &sh) {
+	const int L = a.L;
+	const long long L2 = (long long) L * L;
+	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+	const long long gstride = (long long) gridDim.x * blockDim.x;
+	const int ax = sh.act[0], ay = sh.act[1], first = sh.first;
+	const float bx = (float) sh.beta[0], by = (float) sh.beta[1];
+	float *px = a.pxf, *py = a.pyf, *Pbx = a.Pxf, *Pby = a.Pyf;
+	const float *zx = a.zxf, *zy = a.zyf;
+	const int *cov_idx = a.cov_idx, *mapg = a.mapg;
+	const long long E = __ldcg(&a.cov_off[L2]);
+	const long long gwarp = gtid >> 5, nwarps = gstride >> 5;
+	const int lane = threadIdx.x & 31;
+	for(long long base = gwarp * 32; base < E; base += nwarps * 32) {
+		const long long t = base + lane;
+		const bool valid = t < E;
+		const int j = valid ? cov_idx[t] : 0;
+		const int key = valid ? mapg[j] : -1;
+		float vx = 0.f, vy = 0.f;
+		if(valid && ax) {
+			const float z = zx[j];
+			const float p = first ? z : __fmaf_rn(bx, px[j], z);
+			px[j] = p;
+			vx = p;
+		}
+		if(valid && ay) {
+			const float z = zy[j];
+			const float p = first ? z : __fmaf_rn(by, py[j], z);
+			py[j] = p;
+			vy = p;
+		}
+		bool tail = false, tail2 = false;
+		if(ax) vx = seg_sum<float>(vx, key, tail);
+		if(ay) vy = seg_sum<float>(vy, key, tail2);
+		if(valid) {
+			if(ax && tail) atomicAdd(&Pbx[key], vx);
+			if(ay && tail2) atomicAdd(&Pby[key], vy);
+		}
+	}
+	return grid_reduce(a, sh, 0, nullptr);
+}
+
+// Phase B: Ap (stored) and p.Ap into sh.tot[0..1]; the network's R channel is cleared.
+__device__ __noinline__ bool fcg_phase_b(const CGArgs &a, CGShared &sh) {
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
 	const long long S = a.st->S;
 	const float neta = (float) (-a.eta * 1.0);
 	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
 	const long long gstride = (long long) gridDim.x * blockDim.x;
-	__shared__ float dT[CG_MAX_D + 1], iTT[CG_MAX_D + 1];
-	for(int d = threadIdx.x; d <= CG_MAX_D; d += blockDim.x) {
-		dT[d] = (float) sh.T[d];
-		iTT[d] = (float) sh.iT[d];
+	const int ax = sh.act[0], ay = sh.act[1];
+	const float *px = a.pxf, *py = a.pyf, *Pbx = a.Pxf, *Pby = a.Pyf;
+	float *apx = a.apxf, *apy = a.apyf;
+	const int *mapg = a.mapg, *cnt = a.cnt;
+	float w[2] = {0.f, 0.f};
+	for(long long j = gtid; j < S; j += gstride) {
+		const int k = mapg[j];
+		const float d = sh.Tf[box_deg(cnt, k, L)];
+		if(ax) {
+			const float p = px[j];
+			const float ap = __fmaf_rn(d, p, neta * box_n4T<float>(Pbx, k, L));
+			apx[j] = ap;
+			w[0] = __fmaf_rn(p, ap, w[0]);
+		}
+		if(ay) {
+			const float p = py[j];
+			const float ap = __fmaf_rn(d, p, neta * box_n4T<float>(Pby, k, L));
+			apy[j] = ap;
+			w[1] = __fmaf_rn(p, ap, w[1]);
+		}
 	}
-	float *px = a.pxf, *py = a.pyf, *apx = a.apxf, *apy = a.apyf, *Pbx = a.Pxf, *Pby = a.Pyf;
-	// box sums cleared for phase A, network input: R cleared, W in place
+	float *x0 = a.unet.x0;
+	for(long long k = gtid; k < L2; k += gstride) {
+		x0[k * 2] = 0.f;
+		x0[(L2 + k) * 2] = 0.f;
+	}
+	warp_tree<float, 2>(w);
+	double v[2] = {(double) w[0], (double) w[1]};
+	block_sum_warps<2>(v, sh.red);
+	return grid_reduce(a, sh, 2, v);
+}
+
+// Phase C: e += alpha p, r -= alpha Ap, |r|^2 into sh.tot[0..1]; box sums cleared.
+__device__ __noinline__ bool fcg_phase_c(const CGArgs &a, CGShared &sh) {
+	const int L = a.L;
+	const long long L2 = (long long) L * L;
+	const long long S = a.st->S;
+	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+	const long long gstride = (long long) gridDim.x * blockDim.x;
+	const int ax = sh.act[0], ay = sh.act[1];
+	const float alx = (float) sh.alpha[0], aly = (float) sh.alpha[1];
+	const float *px = a.pxf, *py = a.pyf, *apx = a.apxf, *apy = a.apyf;
+	float *ex = a.exf, *ey = a.eyf, *rx = a.rxf, *ry = a.ryf, *Pbx = a.Pxf, *Pby = a.Pyf;
+	float w[2] = {0.f, 0.f};
+	for(long long j = gtid; j < S; j += gstride) {
+		if(ax) {
+			ex[j] = __fmaf_rn(alx, px[j], ex[j]);
+			const float r = __fmaf_rn(-alx, apx[j], rx[j]);
+			rx[j] = r;
+			w[0] = __fmaf_rn(r, r, w[0]);
+		}
+		if(ay) {
+			ey[j] = __fmaf_rn(aly, py[j], ey[j]);
+			const float r = __fmaf_rn(-aly, apy[j], ry[j]);
+			ry[j] = r;
+			w[1] = __fmaf_rn(r, r, w[1]);
+		}
+	}
 	for(long long k = gtid; k < L2; k += gstride) {
 		Pbx[k] = 0.f;
 		Pby[k] = 0.f;
+	}
+	warp_tree<float, 2>(w);
+	double v[2] = {(double) w[0], (double) w[1]};
+	block_sum_warps<2>(v, sh.red);
+	return grid_reduce(a, sh, 2, v);
+}
+
+// Flexible CG (Notay's FCG(1): beta = -z'.Ap / p.Ap) on the FP32 correction
+// system A e = r of one refinement sweep, preconditioned by the network.
+// Same conventions as cg_iterate<float>: r in rxf/ryf, e in exf/eyf, stop at
+// |r|^2 < thr per component.
+__device__ __noinline__ bool fcg_iterate(const CGArgs &a, CGShared &sh, TcState &tc, long long max_it) {
+	const int L = a.L;
+	const long long L2 = (long long) L * L;
+	const long long S = a.st->S;
+	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+	const long long gstride = (long long) gridDim.x * blockDim.x;
+	for(int d = threadIdx.x; d <= CG_MAX_D; d += blockDim.x) {
+		sh.Tf[d] = (float) sh.T[d];
+		sh.iTf[d] = (float) sh.iT[d];
+	}
+	// box sums cleared for phase A, network input: R cleared, W in place
+	for(long long k = gtid; k < L2; k += gstride) {
+		a.Pxf[k] = 0.f;
+		a.Pyf[k] = 0.f;
 		const float wv = box_w(a, sh, (int) k, L);
 		a.unet.x0[k * 2] = 0.f;
 		a.unet.x0[k * 2 + 1] = wv;
@@ -706,84 +938,25 @@ __device__ bool fcg_iterate(const CGArgs &a, CGShared &sh, float *wsm, long long
 		a.unet.x0[(L2 + k) * 2 + 1] = wv;
 	}
 	for(long long j = gtid; j < S; j += gstride) {
-		apx[j] = 0.f;
-		apy[j] = 0.f;
+		a.apxf[j] = 0.f;
+		a.apyf[j] = 0.f;
 	}
 	if(threadIdx.x == 0) {
 		for(int c = 0; c < 2; c++) sh.scale[c] = sqrt(sh.rn2[c] / (double) S);
 		sh.first = 1;
 	}
-	if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
-	if(!precond_apply(a, sh, wsm, iTT)) return false;
+	if(!grid_reduce(a, sh, 0, nullptr)) return false;
+	if(!precond_apply(a, sh, tc, sh.iTf)) return false;
 	if(threadIdx.x == 0) {
 		sh.rz[0] = sh.tot[0];
 		sh.rz[1] = sh.tot[1];
 	}
 	__syncthreads();
-	const long long E = __ldcg(&a.cov_off[L2]);
 	while(sh.act[0] || sh.act[1]) {
-		const int ax = sh.act[0], ay = sh.act[1], first = sh.first;
-		const float bx = (float) sh.beta[0], by = (float) sh.beta[1];
-		// Phase A: p = z + beta p, box sums P = S p
-		{
-			const long long gwarp = gtid >> 5, nwarps = gstride >> 5;
-			const int lane = threadIdx.x & 31;
-			for(long long base = gwarp * 32; base < E; base += nwarps * 32) {
-				const long long t = base + lane;
-				const bool valid = t < E;
-				const int j = valid ? a.cov_idx[t] : 0;
-				const int key = valid ? a.mapg[j] : -1;
-				float vx = 0.f, vy = 0.f;
-				if(valid && ax) {
-					const float z = a.zxf[j];
-					const float p = first ? z : __fmaf_rn(bx, px[j], z);
-					px[j] = p;
-					vx = p;
-				}
-				if(valid && ay) {
-					const float z = a.zyf[j];
-					const float p = first ? z : __fmaf_rn(by, py[j], z);
-					py[j] = p;
-					vy = p;
-				}
-				bool tail = false, tail2 = false;
-				if(ax) vx = seg_sum<float>(vx, key, tail);
-				if(ay) vy = seg_sum<float>(vy, key, tail2);
-				if(valid) {
-					if(ax && tail) atomicAdd(&Pbx[key], vx);
-					if(ay && tail2) atomicAdd(&Pby[key], vy);
-				}
-			}
-		}
-		if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return false;
-		// Phase B: Ap (stored) and p.Ap; the network's R channel is cleared
-		{
-			float w[2] = {0.f, 0.f};
-			for(long long j = gtid; j < S; j += gstride) {
-				const int k = a.mapg[j];
-				const float d = dT[box_deg(a.cnt, k, L)];
-				if(ax) {
-					const float p = px[j];
-					const float ap = __fmaf_rn(d, p, neta * box_n4T<float>(Pbx, k, L));
-					apx[j] = ap;
-					w[0] = __fmaf_rn(p, ap, w[0]);
-				}
-				if(ay) {
-					const float p = py[j];
-					const float ap = __fmaf_rn(d, p, neta * box_n4T<float>(Pby, k, L));
-					apy[j] = ap;
-					w[1] = __fmaf_rn(p, ap, w[1]);
-				}
-			}
-			for(long long k = gtid; k < L2; k += gstride) {
-				a.unet.x0[k * 2] = 0.f;
-				a.unet.x0[(L2 + k) * 2] = 0.f;
-			}
-			warp_tree<float, 2>(w);
-			double v[2] = {(double) w[0], (double) w[1]};
-			block_sum_warps<2>(v, sh.red);
-			if(!grid_reduce(a, 2, v, sh.tot, sh.red)) return false;
-		}
+		if(!fcg_phase_a(a, sh)) return false;
+		pmark(a, sh, PH_A);
+		if(!fcg_phase_b(a, sh)) return false;
+		pmark(a, sh, PH_B);
 		if(threadIdx.x == 0) {
 			for(int c = 0; c < 2; c++) {
 				if(!sh.act[c]) continue;
@@ -792,33 +965,8 @@ __device__ bool fcg_iterate(const CGArgs &a, CGShared &sh, float *wsm, long long
 			}
 		}
 		__syncthreads();
-		// Phase C: e += alpha p, r -= alpha Ap, |r|^2; box sums cleared
-		{
-			const float alx = (float) sh.alpha[0], aly = (float) sh.alpha[1];
-			float w[2] = {0.f, 0.f};
-			for(long long j = gtid; j < S; j += gstride) {
-				if(ax) {
-					a.exf[j] = __fmaf_rn(alx, px[j], a.exf[j]);
-					const float r = __fmaf_rn(-alx, apx[j], a.rxf[j]);
-					a.rxf[j] = r;
-					w[0] = __fmaf_rn(r, r, w[0]);
-				}
-				if(ay) {
-					a.eyf[j] = __fmaf_rn(aly, py[j], a.eyf[j]);
-					const float r = __fmaf_rn(-aly, apy[j], a.ryf[j]);
-					a.ryf[j] = r;
-					w[1] = __fmaf_rn(r, r, w[1]);
-				}
-			}
-			for(long long k = gtid; k < L2; k += gstride) {
-				Pbx[k] = 0.f;
-				Pby[k] = 0.f;
-			}
-			warp_tree<float, 2>(w);
-			double v[2] = {(double) w[0], (double) w[1]};
-			block_sum_warps<2>(v, sh.red);
-			if(!grid_reduce(a, 2, v, sh.tot, sh.red)) return false;
-		}
+		if(!fcg_phase_c(a, sh)) return false;
+		pmark(a, sh, PH_C);
 		if(threadIdx.x == 0) {
 			for(int c = 0; c < 2; c++) {
 				if(!sh.act[c]) continue;
@@ -830,7 +978,7 @@ __device__ bool fcg_iterate(const CGArgs &a, CGShared &sh, float *wsm, long long
 		}
 		__syncthreads();
 		if(!sh.act[0] && !sh.act[1]) break;
-		if(!precond_apply(a, sh, wsm, iTT)) return false;
+		if(!precond_apply(a, sh, tc, sh.iTf)) return false;
 		if(threadIdx.x == 0) {
 			for(int c = 0; c < 2; c++) {
 				if(!sh.act[c]) continue;
@@ -845,9 +993,7 @@ __device__ bool fcg_iterate(const CGArgs &a, CGShared &sh, float *wsm, long long
 }
 
 template<bool LEARNED>
-__global__ void __launch_bounds__(CG_THREADS) cg_kernel(const CGArgs a) {
-	__shared__ CGShared sh;
-	extern __shared__ float wsm[];
+__device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcState &tc) {
 	const long long S = a.st->S;
 	const int cold = a.st->cg_cold;
 	const double eta = a.eta;
@@ -896,7 +1042,7 @@ __global__ void __launch_bounds__(CG_THREADS) cg_kernel(const CGArgs a) {
 	const long long max_it = 2 * S;
 	int refinements = 0;
 	if(!mixed) {
-		if(!cg_iterate<double>(a, sh, a.rx, a.ry, a.px, a.py, a.apx, a.apy, a.Px, a.Py, a.vx, a.vy, max_it)) return;
+		if(!cg_iterate<double>(a, sh, CGVecs<double>{a.rx, a.ry, a.px, a.py, a.apx, a.apy, a.Px, a.Py, a.vx, a.vy}, max_it)) return;
 		if(a.harv_in && sh.hm > 0 && !harvest_finish(a, sh, a.vx, a.vy)) return;
 	}
 	else {
@@ -919,10 +1065,10 @@ __global__ void __launch_bounds__(CG_THREADS) cg_kernel(const CGArgs a) {
 			}
 			__syncthreads();
 			if constexpr(LEARNED) {
-				if(!fcg_iterate(a, sh, wsm, max_it < 1000 ? max_it : 1000)) return;
+				if(!fcg_iterate(a, sh, tc, max_it < 1000 ? max_it : 1000)) return;
 			}
 			else {
-				if(!cg_iterate<float>(a, sh, a.rxf, a.ryf, a.pxf, a.pyf, a.apxf, a.apyf, a.Pxf, a.Pyf, a.exf, a.eyf, max_it))
+				if(!cg_iterate<float>(a, sh, CGVecs<float>{a.rxf, a.ryf, a.pxf, a.pyf, a.apxf, a.apyf, a.Pxf, a.Pyf, a.exf, a.eyf}, max_it))
 					return;
 			}
 			for(long long j = gtid; j < S; j += gstride) {
@@ -930,7 +1076,7 @@ __global__ void __launch_bounds__(CG_THREADS) cg_kernel(const CGArgs a) {
 				a.vy[j] += (double) a.eyf[j];
 			}
 			refinements++;
-			if(!grid_reduce(a, 0, nullptr, sh.tot, sh.red)) return;
+			if(!grid_reduce(a, sh, 0, nullptr)) return;
 			if(!true_residual(a, sh, false, true)) return;
 			if(threadIdx.x == 0) {
 				for(int c = 0; c < 2; c++) {
@@ -958,7 +1104,7 @@ __global__ void __launch_bounds__(CG_THREADS) cg_kernel(const CGArgs a) {
 				}
 			}
 			__syncthreads();
-			if(!cg_iterate<double>(a, sh, a.rx, a.ry, a.px, a.py, a.apx, a.apy, a.Px, a.Py, a.vx, a.vy, max_it)) return;
+			if(!cg_iterate<double>(a, sh, CGVecs<double>{a.rx, a.ry, a.px, a.py, a.apx, a.apy, a.Px, a.Py, a.vx, a.vy}, max_it)) return;
 		}
 	}
 	if(blockIdx.x == 0 && threadIdx.x == 0) {
@@ -976,16 +1122,55 @@ __global__ void __launch_bounds__(CG_THREADS) cg_kernel(const CGArgs a) {
 	}
 }
 
-constexpr size_t LEARNED_SMEM = sizeof(float) * UNET_MAX_LAYER_PARAMS;
+constexpr size_t LEARNED_SMEM = TC_SMEM > sizeof(float) * UNET_MAX_LAYER_PARAMS ? TC_SMEM : sizeof(float) * UNET_MAX_LAYER_PARAMS;
+
+// The plain solve keeps two CTAs per SM (64 registers); the learned one
+// needs the whole register file of one CTA.
+template<bool LEARNED>
+__global__ void __launch_bounds__(CG_THREADS, LEARNED ? 1 : 2) cg_kernel(const __grid_constant__ CGArgs a) {
+	__shared__ CGShared sh;
+	extern __shared__ __align__(1024) unsigned char dsm[];
+	TcState tc{dsm, 0u, 0u};
+	if(threadIdx.x == 0) {
+		sh.epoch = 0u;
+		sh.fail = 0;
+	}
+	__syncthreads();
+	if(a.phase_ns && blockIdx.x == 0 && threadIdx.x == 0) sh.tmark = gtimer();
+	if constexpr(LEARNED) {
+		if(a.unet_tc) {
+			uint32_t *hold = reinterpret_cast<uint32_t *>(dsm + TC_HOLD_OFF);
+			if(threadIdx.x < 32) tc_alloc(hold, TC_COLS);
+			if(threadIdx.x == 0) mbar_init(reinterpret_cast<uint64_t *>(dsm + TC_MBAR_OFF), 1);
+			tc_fence_before();
+			__syncthreads();
+			tc_fence_after();
+			tc.tmem = *hold;
+		}
+	}
+	cg_body<LEARNED>(a, sh, tc);
+	pmark(a, sh, PH_OTHER);
+	if constexpr(LEARNED) {
+		if(a.unet_tc) {
+			tc_fence_before();
+			__syncthreads();
+			if(threadIdx.x < 32) tc_dealloc(tc.tmem, TC_COLS);
+		}
+	}
+}
 
 int cg_grid_blocks(int device, bool learned) {
 	int sms = 0, per_sm = 0;
 	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-	if(learned) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cg_kernel<true>, CG_THREADS, LEARNED_SMEM);
+	if(learned) {
+		cudaFuncSetAttribute(cg_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) LEARNED_SMEM);
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cg_kernel<true>, CG_THREADS, LEARNED_SMEM);
+	}
 	else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cg_kernel<false>, CG_THREADS, 0);
 	if(per_sm < 1) per_sm = 1;
 	if(per_sm > 2) per_sm = 2;
-	return sms * per_sm;
+	const int blocks = sms * per_sm;
+	return blocks < 2048 ? blocks : 2048;  // partial sums: 2 x 8 x blocks doubles
 }
 
 cudaError_t launch_cg(const CGArgs &a, int blocks, cudaStream_t s) {

@@ -35,6 +35,7 @@ enum ErrBits {
 	ERR_BIN = 8,        // bin list overflow
 	ERR_BARRIER = 16,   // a grid barrier timed out
 	ERR_TYPE = 32,      // activenematic type other than 0/1
+	ERR_MMA = 64,       // a tensor-core completion wait timed out
 };
 
 // Phase-dependent parameters (see rc_params in the C header).

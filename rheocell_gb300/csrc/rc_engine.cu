@@ -108,11 +108,16 @@ struct rc_engine {
 	float *unet_params = nullptr;  // FP32 network parameters (null: none yet)
 	UNetActs unet{};               // activations for the two velocity components
 	float *zxf = nullptr, *zyf = nullptr;
+	bf16 *unet_pack = nullptr;     // BF16 weights of the tensor-core layers
+	UNetActsBF unet_bf{};          // BF16 activations of the tensor-core path
 	int cg_blocks_learned = 0;
 	// harvested training samples
 	float *harv_in = nullptr, *harv_tgt = nullptr, *harv_s = nullptr;
 	int *harv_count = nullptr;
 	int harv_cap = 0, harv_every = 4, harv_per_solve = 4;
+	bool harv_collect = false;
+	unsigned long long *phase_ns = nullptr;  // diagnostic solve phase timers (null: off)
+	bool phase_on = false;
 };
 
 static cudaEvent_t get_event(rc_engine *e) {
@@ -298,15 +303,19 @@ static void solve(rc_engine *e, int phase) {
 	g.exf = e->exf;
 	g.eyf = e->eyf;
 	int blocks = e->cg_blocks;
-	if(e->solver == RC_SOLVER_LEARNED) {
+	if(e->solver == RC_SOLVER_LEARNED || e->solver == RC_SOLVER_LEARNED_FP32) {
 		g.mixed = 1;
 		g.unet_params = e->unet_params;
 		g.unet = e->unet;
+		g.unet_tc = e->solver == RC_SOLVER_LEARNED;
+		g.phase_ns = e->phase_on ? e->phase_ns : nullptr;
+		g.unet_bf = e->unet_bf;
+		g.unet_wpack = e->unet_pack;
 		g.zxf = e->zxf;
 		g.zyf = e->zyf;
 		blocks = e->cg_blocks_learned;
 	}
-	else if(e->harv_cap > 0 && !g.mixed) {
+	else if(e->harv_cap > 0 && e->harv_collect && !g.mixed) {
 		g.harv_in = e->harv_in;
 		g.harv_tgt = e->harv_tgt;
 		g.harv_s = e->harv_s;
@@ -316,6 +325,7 @@ static void solve(rc_engine *e, int phase) {
 		g.harv_per_solve = e->harv_per_solve;
 	}
 	StageMark sm(e, RC_TIMER_SOLVE);
+	cudaMemsetAsync(e->bar, 0, sizeof(unsigned) * 4, e->stream);  // the barrier counter starts at zero
 	const cudaError_t c = launch_cg(g, blocks, e->stream);
 	e->launches += 1;
 	if(c != cudaSuccess && e->launch_error.empty()) e->launch_error = cudaGetErrorString(c);
@@ -406,6 +416,11 @@ static void one_step(rc_engine *e) {
 	}
 	e->launches += 5;
 	evaluate_end(e, e->phiA, cur);
+}
+
+static void drop_graphs(rc_engine *e) {
+	for(auto &g : e->graphs) cudaGraphExecDestroy(g.exec);
+	e->graphs.clear();
 }
 
 // One step, replayed from a captured CUDA graph when possible.  A graph is
@@ -527,6 +542,7 @@ static int check_status(rc_engine *e, rc_step_stats *stats) {
 		if(h.err & ERR_NONFINITE) return set_err(e, RC_ERR_NONFINITE, "non-finite state in cell %d", h.err_where);
 		if(h.err & ERR_BARRIER) return set_err(e, RC_ERR_CG, "viscous solve: grid barrier timed out");
 		if(h.err & ERR_TYPE) return set_err(e, RC_ERR_INVALID, "Too many field types (cell %d)", h.err_where);
+		if(h.err & ERR_MMA) return set_err(e, RC_ERR_CG, "viscous solve: tensor-core completion wait timed out");
 		return set_err(e, RC_ERR_INVALID, "device error 0x%x", h.err);
 	}
 	return RC_OK;
@@ -742,7 +758,7 @@ int rc_batch_create(const rc_params *params, int n_layers, const rc_box *boxes, 
 		   (rc = dalloc(e, &e->rx, cap)) || (rc = dalloc(e, &e->ry, cap)) || (rc = dalloc(e, &e->px, cap)) ||
 		   (rc = dalloc(e, &e->py, cap)) || (rc = dalloc(e, &e->apx, cap)) || (rc = dalloc(e, &e->apy, cap)) ||
 		   (rc = dalloc(e, &e->Px, L2)) || (rc = dalloc(e, &e->Py, L2)) ||
-		   (rc = dalloc(e, &e->partials, 8 * 4096)) || (rc = dalloc(e, &e->scalars, 64)) || (rc = dalloc(e, &e->bar, 2)))
+		   (rc = dalloc(e, &e->partials, 8 * 4096)) || (rc = dalloc(e, &e->scalars, 64)) || (rc = dalloc(e, &e->bar, 4)))
 			return bail(rc);
 		if(params->precision == RC_PRECISION_MIXED) {
 			if((rc = dalloc(e, &e->rxf, cap)) || (rc = dalloc(e, &e->ryf, cap)) || (rc = dalloc(e, &e->pxf, cap)) ||
@@ -1022,16 +1038,20 @@ static void dfree(rc_engine *e, void *p) {
 	e->allocs.erase(std::remove(e->allocs.begin(), e->allocs.end(), p), e->allocs.end());
 }
 
-static void drop_graphs(rc_engine *e) {
-	for(auto &g : e->graphs) cudaGraphExecDestroy(g.exec);
-	e->graphs.clear();
-}
 
 static bool is_wet_engine(const rc_engine *e) { return e->fx != nullptr; }
 
 int rc_learned_harvest(rc_engine *e, int capacity, int every, int per_solve) {
 	if(!e) return RC_ERR_INVALID;
 	if(!is_wet_engine(e)) return set_err(e, RC_ERR_UNSUPPORTED, "rc_learned_harvest: the engine has no viscous solve");
+	if(per_solve == 0 && capacity > 0) {
+		// stop collecting, keep the stored samples
+		CUDA_TRY(e, cudaSetDevice(e->device));
+		CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+		if(e->harv_collect) drop_graphs(e);
+		e->harv_collect = false;
+		return RC_OK;
+	}
 	if(capacity < 0 || (capacity > 0 && (every < 1 || per_solve < 1)))
 		return set_err(e, RC_ERR_INVALID, "rc_learned_harvest: capacity %d, every %d, per_solve %d", capacity, every, per_solve);
 	CUDA_TRY(e, cudaSetDevice(e->device));
@@ -1043,6 +1063,7 @@ int rc_learned_harvest(rc_engine *e, int capacity, int every, int per_solve) {
 	e->harv_in = e->harv_tgt = e->harv_s = nullptr;
 	e->harv_count = nullptr;
 	e->harv_cap = 0;
+	e->harv_collect = false;
 	drop_graphs(e);
 	if(capacity == 0) return RC_OK;
 	const size_t L2 = (size_t) e->L * e->L;
@@ -1053,6 +1074,7 @@ int rc_learned_harvest(rc_engine *e, int capacity, int every, int per_solve) {
 	e->harv_cap = capacity;
 	e->harv_every = every;
 	e->harv_per_solve = per_solve;
+	e->harv_collect = true;
 	return RC_OK;
 }
 
@@ -1196,6 +1218,7 @@ int rc_learned_train(rc_engine *e, const rc_train_options *o, rc_train_report *r
 	int rc = RC_OK;
 	if(!e->unet_params) rc = dalloc(e, &e->unet_params, UNET_PARAMS);
 	if(rc == RC_OK) cudaMemcpyAsync(e->unet_params, T.params, sizeof(float) * UNET_PARAMS, cudaMemcpyDeviceToDevice, e->stream);
+	if(rc == RC_OK && e->unet_pack) unet_pack_bf16(e->unet_params, e->unet_pack, e->stream);
 	const cudaError_t ce = cudaStreamSynchronize(e->stream);
 	cudaFree(didx);
 	cudaFree(dacc);
@@ -1227,16 +1250,20 @@ int rc_learned_set_params(rc_engine *e, const double *params) {
 	for(int k = 0; k < UNET_PARAMS; k++) h[(size_t) k] = (float) params[k];
 	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
 	CUDA_TRY(e, cudaMemcpy(e->unet_params, h.data(), sizeof(float) * UNET_PARAMS, cudaMemcpyHostToDevice));
+	if(e->unet_pack) {
+		unet_pack_bf16(e->unet_params, e->unet_pack, e->stream);
+		CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+	}
 	return RC_OK;
 }
 
 int rc_set_solver(rc_engine *e, int solver) {
 	if(!e) return RC_ERR_INVALID;
-	if(solver != RC_SOLVER_PLAIN && solver != RC_SOLVER_LEARNED)
+	if(solver != RC_SOLVER_PLAIN && solver != RC_SOLVER_LEARNED && solver != RC_SOLVER_LEARNED_FP32)
 		return set_err(e, RC_ERR_INVALID, "rc_set_solver: unknown solver %d", solver);
 	CUDA_TRY(e, cudaSetDevice(e->device));
 	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
-	if(solver == RC_SOLVER_LEARNED) {
+	if(solver != RC_SOLVER_PLAIN) {
 		if(!is_wet_engine(e)) return set_err(e, RC_ERR_UNSUPPORTED, "rc_set_solver: the engine has no viscous solve");
 		if(e->L % 4 != 0 || e->L < 8)
 			return set_err(e, RC_ERR_UNSUPPORTED, "rc_set_solver: box side %d is not a multiple of 4", e->L);
@@ -1260,10 +1287,38 @@ int rc_set_solver(rc_engine *e, int solver) {
 			   (rc = dalloc(e, &A.b0, p2 * 16)) || (rc = dalloc(e, &A.t2, p2 * 16)))
 				return rc;
 		}
+		if(solver == RC_SOLVER_LEARNED && !e->unet_pack) {
+			const size_t p0 = 2 * L2, p1 = p0 / 4, p2 = p0 / 16;
+			UNetActsBF &B = e->unet_bf;
+			if((rc = dalloc(e, &e->unet_pack, UNET_PACKED)) || (rc = dalloc(e, &B.e0a, p0 * 16)) ||
+			   (rc = dalloc(e, &B.s0, p0 * 16)) || (rc = dalloc(e, &B.d0a, p0 * 16)) || (rc = dalloc(e, &B.t0, p0 * 16)) ||
+			   (rc = dalloc(e, &B.e1a, p1 * 16)) || (rc = dalloc(e, &B.s1, p1 * 16)) || (rc = dalloc(e, &B.d1a, p1 * 16)) ||
+			   (rc = dalloc(e, &B.t1, p1 * 16)) || (rc = dalloc(e, &B.b0, p2 * 16)) || (rc = dalloc(e, &B.t2, p2 * 16)))
+				return rc;
+			unet_pack_bf16(e->unet_params, e->unet_pack, e->stream);
+			CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+		}
 		if(!e->cg_blocks_learned) e->cg_blocks_learned = cg_grid_blocks(e->device, true);
 	}
 	if(solver != e->solver) drop_graphs(e);
 	e->solver = solver;
+	return RC_OK;
+}
+
+int rc_solver_profile(rc_engine *e, int enable, double *ms, int n) {
+	if(!e) return RC_ERR_INVALID;
+	CUDA_TRY(e, cudaSetDevice(e->device));
+	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+	int rc;
+	if(!e->phase_ns && (rc = dalloc(e, &e->phase_ns, 32))) return rc;
+	if(ms && n > 0) {
+		unsigned long long h[32];
+		CUDA_TRY(e, cudaMemcpy(h, e->phase_ns, sizeof(h), cudaMemcpyDeviceToHost));
+		for(int k = 0; k < n && k < 32; k++) ms[k] = (double) h[k] * 1e-6;
+	}
+	if((enable != 0) != e->phase_on) drop_graphs(e);
+	if(enable) CUDA_TRY(e, cudaMemset(e->phase_ns, 0, sizeof(unsigned long long) * 32));
+	e->phase_on = enable != 0;
 	return RC_OK;
 }
 
@@ -1304,15 +1359,15 @@ std::mutex g_noalloc_mu;
 std::vector<unsigned char *> g_noalloc_ptr;
 
 // Resets what the solve needs zero at its start: the status record (then S
-// and the cold-start flag) and the barrier's arrival count.  The barrier's
-// generation word may hold any value; the work arrays are initialised by the
-// solve itself.
+// and the cold-start flag) and the grid barrier's arrival counter.  The work
+// arrays are initialised by the solve itself.
 __global__ void noalloc_header_kernel(rc::DevStatus *st, unsigned *bar, long long S) {
 	if(threadIdx.x == 0 && blockIdx.x == 0) {
 		memset(st, 0, sizeof(*st));
 		st->S = S;
 		st->cg_cold = 1;
 		bar[0] = 0u;
+		bar[1] = 0u;
 	}
 }
 
@@ -1346,9 +1401,9 @@ int rc_viscous_resolve_noalloc(rc_engine *e, double *vx, double *vy, long long n
 		return set_err(e, RC_ERR_CAPACITY,
 		               "rc_viscous_resolve_noalloc: box of %d x %d sites, the fixed area holds at most %lld sites", e->L,
 		               e->L, NA_MAX_BOX_SITES);
-	if(e->cg_blocks > NA_MAX_BLOCKS)
+	if(e->cg_blocks > NA_MAX_BLOCKS / 2)
 		return set_err(e, RC_ERR_CAPACITY, "rc_viscous_resolve_noalloc: %d solver blocks, at most %lld", e->cg_blocks,
-		               NA_MAX_BLOCKS);
+		               NA_MAX_BLOCKS / 2);
 	CUDA_TRY(e, cudaSetDevice(e->device));
 	unsigned char *base = nullptr;
 	{

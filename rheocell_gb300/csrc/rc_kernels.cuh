@@ -4,6 +4,7 @@
 
 #include "rc_common.cuh"
 #include "rc_unet.cuh"
+#include "rc_unet_tc.cuh"
 
 namespace rc {
 
@@ -75,10 +76,14 @@ struct CGArgs {
 	// (flexible CG); null: Jacobi
 	const float *unet_params;
 	UNetActs unet;           // activations for the two components (batch 2)
+	int unet_tc;             // 1: BF16 tensor-core layers (unet_bf, unet_wpack)
+	UNetActsBF unet_bf;
+	const bf16 *unet_wpack;
 	float *zxf, *zyf;        // z = M r
 	// training samples harvested from the plain FP64 solve; null: none.
 	// Sample q: harv_in[q][L2][2] = (R/s, W), harv_tgt[q][L2] = (X* - X)/s,
 	// harv_s[q] = s (0 marks an unused slot); *harv_count samples stored.
+	unsigned long long *phase_ns;  // diagnostic per-phase times of the learned solve (null: off)
 	float *harv_in, *harv_tgt, *harv_s;
 	int *harv_count;
 	int harv_cap, harv_every, harv_per_solve;

@@ -4,6 +4,8 @@
 // so a training run is reproducible bit for bit.
 #include "rc_unet.cuh"
 #include "rc_unet_train.cuh"
+#include "rc_unet_tc.cuh"
+#include "../../include/rheocell_gb300.h"
 
 #include <cuda_runtime.h>
 
@@ -407,9 +409,147 @@ double unet_read_loss(UNetTrainer &T, cudaStream_t s) {
 
 }  // namespace rc
 
-// --- C ABI: one forward/loss/backward pass on host data ----------------------
+// --- tensor-core inference ----------------------------------------------------
 
-#include "../../include/rheocell_gb300.h"
+namespace rc {
+
+namespace {
+
+__global__ void pack_bf16_kernel(const float *params, bf16 *packed) {
+	for(int l = 0; l < UNET_LAYERS; l++) {
+		const UNetLayerDesc d = unet_layer(l);
+		if(d.co != 16 || d.ci < 16) continue;
+		const int KC = d.ci / 8, n = 9 * d.ci * 16;
+		const float *w = params + unet_weight_offset(l);
+		bf16 *o = packed + unet_pack_offset(l);
+		for(int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+			const int e = idx & 7, co = (idx >> 3) & 15;
+			const int tk = idx >> 7, kc = tk % KC, t = tk / KC;
+			o[idx] = __float2bfloat16_rn(w[(t * d.ci + kc * 8 + e) * 16 + co]);
+		}
+	}
+}
+
+__global__ void __launch_bounds__(512) tc_layer_kernel(int l, TcSrc src, const bf16 *packed, const float *params,
+                                                        bf16 *dst, int batch, int L, int *err) {
+	extern __shared__ __align__(1024) unsigned char tsm[];
+	uint32_t *hold = reinterpret_cast<uint32_t *>(tsm + TC_HOLD_OFF);
+	uint64_t *mbar = reinterpret_cast<uint64_t *>(tsm + TC_MBAR_OFF);
+	if(threadIdx.x < 32) tc_alloc(hold, TC_COLS);
+	if(threadIdx.x == 0) mbar_init(mbar, 1);
+	tc_fence_before();
+	__syncthreads();
+	tc_fence_after();
+	const uint32_t tmem = *hold;
+	uint32_t phase = 0;
+	tc_conv_layer(l, src, packed + unet_pack_offset(l), params + unet_bias_offset(l), dst, batch, L, tsm, tmem, phase, err,
+	              1, nullptr);
+	tc_fence_before();
+	__syncthreads();
+	if(threadIdx.x < 32) tc_dealloc(tmem, TC_COLS);
+}
+
+__global__ void e0a_kernel(const float *x0, const float *params, bf16 *dst, int batch, int L) {
+	__shared__ float w[9 * 2 * 16 + 16];
+	for(int k = threadIdx.x; k < 9 * 2 * 16 + 16; k += blockDim.x) w[k] = params[unet_weight_offset(L_E0A) + k];
+	__syncthreads();
+	e0a_range(x0, w, dst, batch, L, blockIdx.x * (long long) blockDim.x + threadIdx.x, (long long) gridDim.x * blockDim.x);
+}
+
+__global__ void out_kernel(const bf16 *t0, const float *params, float *dst, int batch, int L) {
+	__shared__ float w[9 * 16 + 1];
+	for(int k = threadIdx.x; k < 9 * 16 + 1; k += blockDim.x) w[k] = params[unet_weight_offset(L_OUT) + k];
+	__syncthreads();
+	out_range(t0, w, dst, batch, L, blockIdx.x * (long long) blockDim.x + threadIdx.x, (long long) gridDim.x * blockDim.x);
+}
+
+}  // namespace
+
+void unet_pack_bf16(const float *params, bf16 *packed, cudaStream_t s) { pack_bf16_kernel<<<64, 256, 0, s>>>(params, packed); }
+
+cudaError_t unet_tc_configure() {
+	return cudaFuncSetAttribute(tc_layer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) TC_SMEM);
+}
+
+// Forward pass with the tensor-core layers (separate launches): x0 (FP32) ->
+// out (FP32) through the BF16 activations A.
+void unet_tc_forward(const float *params, const bf16 *packed, const float *x0, const UNetActsBF &A, float *out, int batch,
+                     int L, int sms, int *err, cudaStream_t s) {
+	const long long p0 = (long long) batch * L * L;
+	e0a_kernel<<<grid_for(p0, 256), 256, 0, s>>>(x0, params, A.e0a, batch, L);
+	for(int l = L_E0B; l <= L_D0B; l++) {
+		const int Ll = L >> unet_layer(l).level;
+		const long long tiles = ((long long) batch * Ll * Ll + 127) / 128;
+		long long g = (tiles + TC_RT - 1) / TC_RT;
+		if(g > sms) g = sms;
+		tc_layer_kernel<<<(int) g, 512, TC_SMEM, s>>>(l, unet_tc_src(l, A), packed, params, unet_tc_dst(l, A), batch, Ll,
+		                                              err);
+	}
+	out_kernel<<<grid_for(p0, 256), 256, 0, s>>>(A.t0, params, out, batch, L);
+}
+
+}  // namespace rc
+
+extern "C" int rc_unet_forward_tc(int L, int batch, const double *params, const double *input, double *output,
+                                  int device) {
+	using namespace rc;
+	if(!params || !input || !output || batch < 1 || L < 8 || L % 4 != 0) return RC_ERR_INVALID;
+	if(cudaSetDevice(device) != cudaSuccess) return RC_ERR_CUDA;
+	if(unet_tc_configure() != cudaSuccess) return RC_ERR_CUDA;
+	int sms = 0;
+	cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+	const size_t p0 = (size_t) batch * L * L, p1 = p0 / 4, p2 = p0 / 16;
+	std::vector<void *> al;
+	auto get = [&](size_t bytes) -> void * {
+		void *q = nullptr;
+		if(cudaMalloc(&q, bytes ? bytes : 16) != cudaSuccess) return nullptr;
+		cudaMemset(q, 0, bytes ? bytes : 16);
+		al.push_back(q);
+		return q;
+	};
+	float *dp = (float *) get(sizeof(float) * UNET_PARAMS);
+	bf16 *pk = (bf16 *) get(sizeof(bf16) * UNET_PACKED);
+	float *x0 = (float *) get(sizeof(float) * p0 * 2);
+	float *out = (float *) get(sizeof(float) * p0);
+	int *err = (int *) get(sizeof(int));
+	UNetActsBF A;
+	A.e0a = (bf16 *) get(2 * p0 * 16);
+	A.s0 = (bf16 *) get(2 * p0 * 16);
+	A.d0a = (bf16 *) get(2 * p0 * 16);
+	A.t0 = (bf16 *) get(2 * p0 * 16);
+	A.e1a = (bf16 *) get(2 * p1 * 16);
+	A.s1 = (bf16 *) get(2 * p1 * 16);
+	A.d1a = (bf16 *) get(2 * p1 * 16);
+	A.t1 = (bf16 *) get(2 * p1 * 16);
+	A.b0 = (bf16 *) get(2 * p2 * 16);
+	A.t2 = (bf16 *) get(2 * p2 * 16);
+	bool okalloc = true;
+	for(void *q : al) okalloc = okalloc && q;
+	int rc = RC_OK;
+	if(!okalloc || al.size() != 15) rc = RC_ERR_OOM;
+	else {
+		std::vector<float> hp(UNET_PARAMS), hx(p0 * 2), hy(p0);
+		for(int k = 0; k < UNET_PARAMS; k++) hp[(size_t) k] = (float) params[k];
+		for(size_t k = 0; k < 2 * p0; k++) hx[k] = (float) input[k];
+		cudaMemcpy(dp, hp.data(), sizeof(float) * UNET_PARAMS, cudaMemcpyHostToDevice);
+		cudaMemcpy(x0, hx.data(), sizeof(float) * 2 * p0, cudaMemcpyHostToDevice);
+		unet_pack_bf16(dp, pk, nullptr);
+		unet_tc_forward(dp, pk, x0, A, out, batch, L, sms, err, nullptr);
+		const cudaError_t ce = cudaDeviceSynchronize();
+		int herr = 0;
+		cudaMemcpy(&herr, err, sizeof(int), cudaMemcpyDeviceToHost);
+		cudaMemcpy(hy.data(), out, sizeof(float) * p0, cudaMemcpyDeviceToHost);
+		if(ce != cudaSuccess) rc = RC_ERR_CUDA;
+		else if(herr) rc = RC_ERR_CG;
+		else
+			for(size_t k = 0; k < p0; k++) output[k] = hy[k];
+	}
+	for(void *q : al)
+		if(q) cudaFree(q);
+	return rc;
+}
+
+// --- C ABI: one forward/loss/backward pass on host data ----------------------
 
 extern "C" int rc_unet_loss_grad(int L, int batch, const double *params, const double *input, const double *target,
                                  double *loss, double *grad, double *output, int device) {

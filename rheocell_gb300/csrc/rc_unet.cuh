@@ -159,7 +159,7 @@ __device__ __forceinline__ void conv_pixel(const ConvSrc &s, const float *w, con
 	float acc[CO];
 #pragma unroll
 	for(int o = 0; o < CO; o++) acc[o] = bias[o];
-#pragma unroll 1
+#pragma unroll(CI <= 2 ? 9 : 1)
 	for(int t = 0; t < 9; t++) {
 		const int ii = wrap(i + t / 3 - 1, L), jj = wrap(j + t % 3 - 1, L);
 		float x[CI];

@@ -2,6 +2,7 @@
 #pragma once
 
 #include "rc_unet.cuh"
+#include "rc_unet_tc.cuh"
 
 #include <cuda_runtime.h>
 
@@ -36,5 +37,8 @@ double unet_read_loss(UNetTrainer &T, cudaStream_t s);
 void unet_gather(UNetTrainer &T, const float *hin, const float *htgt, const int *idx, int n, cudaStream_t s);
 // acc[0] += sum over the last loss evaluation's samples of |f - y|^2 / |y|^2
 void unet_accumulate_loss(UNetTrainer &T, double *acc, cudaStream_t s);
+// BF16 copy of the tensor-core layers' weights in the B-operand order
+void unet_pack_bf16(const float *params, bf16 *packed, cudaStream_t s);
+cudaError_t unet_tc_configure();
 
 }  // namespace rc

@@ -64,7 +64,8 @@ def test_learned_solve_matches_fp64_oracle(trained):
     e.set_solver(abi.RC_SOLVER_PLAIN)
 
 
-def test_network_cuts_inner_iterations(trained):
+@pytest.mark.parametrize("solver", [abi.RC_SOLVER_LEARNED, abi.RC_SOLVER_LEARNED_FP32])
+def test_network_cuts_inner_iterations(trained, solver):
     """Same state, same mixed-precision refinement: inner iterations with the
     network (flexible CG) against the Jacobi inner iterations without it."""
     keys, m, e, _, _ = trained
@@ -83,7 +84,7 @@ def test_network_cuts_inner_iterations(trained):
         return out
 
     it_plain, res_plain = run(abi.RC_SOLVER_PLAIN)
-    it_learned, res_learned = run(abi.RC_SOLVER_LEARNED)
+    it_learned, res_learned = run(solver)
     print("inner iterations: plain", it_plain, res_plain, "learned", it_learned, res_learned)
     assert res_plain < 1e-8 and res_learned < 1e-8
     assert it_learned < 0.5 * it_plain, (it_learned, it_plain)

@@ -41,3 +41,22 @@ def test_forward_loss_and_gradients_match_oracle(L, batch):
     for name, ci, co, w, b in U.param_layout():
         gw, gw_ref = grad[w:b + co], g_ref[w:b + co]
         assert np.max(np.abs(gw - gw_ref)) <= 1e-3 * np.max(np.abs(gw_ref)), name
+
+
+@pytest.mark.parametrize("L,batch", [(16, 2), (64, 2), (256, 2)])
+def test_tensor_core_forward_matches_oracle(L, batch):
+    """The solve's forward pass (BF16 activations, tcgen05 layers) against the
+    FP64 oracle, within BF16 rounding over eleven layers."""
+    lib = engine.lib()
+    rng = np.random.default_rng(100 + L)
+    p = U.init_params(L + 1)
+    for name, ci, co, w, b in U.param_layout():
+        p[b:b + co] = rng.normal(0.0, 0.05, size=co)
+    x = np.ascontiguousarray(rng.normal(size=(batch, L, L, 2)))
+    x[..., 1] = np.abs(x[..., 1]) * 0.25
+    out = np.zeros((batch, L, L))
+    rc = lib.rc_unet_forward_tc(L, batch, _dp(p), _dp(x), _dp(out), 0)
+    assert rc == 0
+    y = U.forward(p, x)[..., 0]
+    err = np.max(np.abs(out - y)) / np.max(np.abs(y))
+    assert err < 3e-2, err
