@@ -184,7 +184,8 @@ def prepare_learned(args, eng, lib):
     harvest_s = time.perf_counter() - t0
     n = eng.harvested()
     eng.harvest(args.harvest_capacity, 3, 0)  # stop collecting, keep the samples
-    rep = eng.train(epochs=args.train_epochs, batch=8, learning_rate=2e-3, seed=1)
+    rep = eng.train(epochs=args.train_epochs, batch=8, learning_rate=args.train_lr, seed=1,
+                    learning_rate_final=args.train_lr * args.train_lr_final)
     k = max(2, min(args.steps, 10))
     plain_ms, plain_it, plain_res = solve_stage(eng, lib, k, flush)
     eng.set_solver(abi.RC_SOLVER_LEARNED)
@@ -486,10 +487,12 @@ def main():
     ap.add_argument("--precision", default="double", choices=["double", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--solver", default="plain", choices=["plain", "learned"])
-    ap.add_argument("--harvest-steps", type=int, default=30)
-    ap.add_argument("--harvest-capacity", type=int, default=1200)
+    ap.add_argument("--harvest-steps", type=int, default=40)
+    ap.add_argument("--harvest-capacity", type=int, default=2000)
     ap.add_argument("--train-epochs", type=int, default=10)
     ap.add_argument("--solver-phases", action="store_true")
+    ap.add_argument("--train-lr", type=float, default=2e-3)
+    ap.add_argument("--train-lr-final", type=float, default=0.05, help="final step size as a fraction of --train-lr")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

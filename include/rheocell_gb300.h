@@ -327,6 +327,7 @@ typedef struct rc_train_options {
 	unsigned long long seed;    /* initialisation and shuffling                        */
 	int init;                   /* 1: fresh initialisation; 0: continue from the current parameters */
 	int max_samples;            /* use at most this many samples (<= 0: all)           */
+	double learning_rate_final; /* cosine decay of the step size to this value over the run (<= 0: constant) */
 } rc_train_options;
 
 typedef struct rc_train_report {

@@ -96,7 +96,7 @@ class RcStepStats(C.Structure):
 class RcTrainOptions(C.Structure):
     _fields_ = [
         ("epochs", C.c_int), ("batch", C.c_int), ("learning_rate", C.c_double), ("validation", C.c_double),
-        ("seed", C.c_ulonglong), ("init", C.c_int), ("max_samples", C.c_int),
+        ("seed", C.c_ulonglong), ("init", C.c_int), ("max_samples", C.c_int), ("learning_rate_final", C.c_double),
     ]
 
 

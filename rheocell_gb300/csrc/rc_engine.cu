@@ -1190,6 +1190,8 @@ int rc_learned_train(rc_engine *e, const rc_train_options *o, rc_train_report *r
 	r.train_samples = (int) train.size();
 	r.validation_samples = (int) val.size();
 	r.validation_loss_init = eval_loss(T, e, val, didx, dacc, batch);
+	const long long total_steps = (long long) epochs * (long long) ((train.size() + batch - 1) / batch);
+	const double lr_final = o->learning_rate_final > 0 ? o->learning_rate_final : (double) lr;
 	for(int ep = 0; ep < epochs; ep++) {
 		shuffle(train, st);
 		cudaMemsetAsync(dacc, 0, sizeof(double), e->stream);
@@ -1202,7 +1204,10 @@ int rc_learned_train(rc_engine *e, const rc_train_options *o, rc_train_report *r
 			unet_loss(T, e->stream);
 			unet_accumulate_loss(T, dacc, e->stream);
 			unet_backward(T, T.params, e->stream);
-			unet_adam(T, lr, e->stream);
+			// cosine decay from lr to lr_final over the run
+			const double frac = total_steps > 1 ? (double) r.steps / (double) (total_steps - 1) : 0.0;
+			const double lr_k = lr_final + 0.5 * ((double) lr - lr_final) * (1.0 + cos(3.141592653589793 * frac));
+			unet_adam(T, (float) lr_k, e->stream);
 			r.steps++;
 		}
 		T.batch = batch;

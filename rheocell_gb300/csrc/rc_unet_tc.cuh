@@ -70,13 +70,18 @@ __host__ __device__ constexpr int unet_pack_offset(int l) {
 }
 constexpr int UNET_PACKED = unet_pack_offset(UNET_LAYERS);
 
-constexpr int TC_RT = 2;    // tiles (of 128 pixels) per round
-constexpr int TC_COLS = 32; // TMEM columns: TC_RT accumulators of 16
-constexpr size_t TC_A_BYTES = (size_t) TC_RT * 9 * 4 * 128 * 16;
+constexpr int TC_RT = 2;       // tiles (of 128 pixels) per round, gathered operands
+constexpr int TC_RT_ROWS = 4;  // tiles per round, row-halo operands
+constexpr int TC_COLS = 64;    // TMEM columns: up to TC_RT_ROWS accumulators of 16
+constexpr int TC_HALO = 130;   // staged positions per row: 128 pixels and a periodic neighbour on each side
+constexpr size_t TC_A_GATHER = (size_t) TC_RT * 9 * 4 * 128 * 16;
+constexpr size_t TC_A_ROWS = (size_t) TC_RT_ROWS * 4 * 3 * TC_HALO * 16;
+constexpr size_t TC_A_BYTES = TC_A_GATHER > TC_A_ROWS ? TC_A_GATHER : TC_A_ROWS;
 constexpr size_t TC_B_OFF = TC_A_BYTES;
 constexpr size_t TC_B_BYTES = 9 * 4 * 16 * 16;
 constexpr size_t TC_BIAS_OFF = TC_B_OFF + TC_B_BYTES;
-constexpr size_t TC_MBAR_OFF = TC_BIAS_OFF + 64;
+constexpr size_t TC_TILE_OFF = TC_BIAS_OFF + 64;        // per-tile (n, y, x0), row mode
+constexpr size_t TC_MBAR_OFF = TC_TILE_OFF + 16 * TC_RT_ROWS;
 constexpr size_t TC_HOLD_OFF = TC_MBAR_OFF + 8;
 constexpr size_t TC_SMEM = TC_HOLD_OFF + 8;
 constexpr uint32_t TC_IDESC = tc_idesc_bf16(128, 16);
@@ -123,9 +128,60 @@ __device__ __forceinline__ uint4 tc_load_chunk(const TcSrc &s, int ci, int n, in
 	return *reinterpret_cast<const uint4 *>(s.b + ((size_t) (n * L + i) * L + j) * 16 + (kc - 2) * 8);
 }
 
+// Row-mode operand staging of nt tiles (KC = input channels / 8): chunk
+// c = r * RB + (kc * 3 + row) * TC_HALO + pos holds channels 8 kc .. of input
+// pixel (n, y + row - 1, x0 + pos - 1) of tile r (coordinates in tile[r]).
+template<int KC>
+__device__ __forceinline__ void tc_stage_rows(const TcSrc &src, const int4 *tile, int nt, int L, uint4 *As) {
+	constexpr int RB = KC * 3 * TC_HALO;
+	const int nchunk = nt * RB;
+	if(src.mode != IN_POOL) {
+		for(int c = threadIdx.x; c < nchunk; c += blockDim.x) {
+			const int r = c / RB, rem = c - r * RB;
+			const int kc = rem / (3 * TC_HALO), rem2 = rem - kc * (3 * TC_HALO);
+			const int row = rem2 / TC_HALO, pos = rem2 - row * TC_HALO;
+			const int4 tl = tile[r];
+			const int ii = wrap(tl.y + row - 1, L), jj = wrap(tl.z + pos - 1, L);
+			const bf16 *g;
+			if(src.mode == IN_DIRECT) g = src.a + ((size_t) (tl.x * L + ii) * L + jj) * (KC * 8) + kc * 8;
+			else if(kc < 2) g = src.a + ((size_t) (tl.x * (L / 2) + ii / 2) * (L / 2) + jj / 2) * 16 + kc * 8;
+			else g = src.b + ((size_t) (tl.x * L + ii) * L + jj) * 16 + (kc - 2) * 8;
+			cp_async16(As + c, g, 16u);
+		}
+		cp_async_wait_all();
+	}
+	else {
+		for(int c0 = threadIdx.x; c0 < nchunk; c0 += 3 * blockDim.x) {
+			uint4 v[3];
+#pragma unroll
+			for(int u = 0; u < 3; u++) {
+				const int c = c0 + u * blockDim.x;
+				v[u] = make_uint4(0u, 0u, 0u, 0u);
+				if(c < nchunk) {
+					const int r = c / RB, rem = c - r * RB;
+					const int kc = rem / (3 * TC_HALO), rem2 = rem - kc * (3 * TC_HALO);
+					const int row = rem2 / TC_HALO, pos = rem2 - row * TC_HALO;
+					const int4 tl = tile[r];
+					v[u] = tc_load_chunk(src, KC * 8, tl.x, wrap(tl.y + row - 1, L), wrap(tl.z + pos - 1, L), L, kc);
+				}
+			}
+#pragma unroll
+			for(int u = 0; u < 3; u++) {
+				const int c = c0 + u * blockDim.x;
+				if(c < nchunk) As[c] = v[u];
+			}
+		}
+	}
+}
+
 // One tensor-core layer (ci = 16 or 32 -> 16 channels, ReLU) over all
-// 128-pixel tiles of `batch` samples at side L, the CTA's tiles TC_RT at a
-// time.  sm: TC_SMEM bytes of shared memory (mbarrier at TC_MBAR_OFF
+// 128-pixel tiles of `batch` samples at side L.  Tile t is pixels
+// [128 t, 128 t + 128) in (sample, row, column) order.  When L is a multiple
+// of 128 a tile is a row segment: its three input rows, each with the
+// periodic neighbour on either side (130 positions), are staged once, and the
+// nine taps are nine shifted descriptors into them (TC_RT_ROWS tiles per
+// round).  Otherwise each tap's operand is gathered pixel by pixel (TC_RT
+// tiles per round).  sm: TC_SMEM bytes of shared memory (mbarrier at TC_MBAR_OFF
 // initialised with count 1), tmem: TC_COLS allocated columns, phase: the
 // mbarrier's current parity (advanced here).  Returns false (and sets
 // *err |= err_bit) if an MMA completion wait ran out; the caller then stops.
@@ -159,8 +215,23 @@ static __device__ __noinline__ bool tc_conv_layer(int l, const TcSrc &src, const
 	const uint32_t a_base = smem_u32(As), b_base = smem_u32(Bs);
 	const long long LL = (long long) L * L;
 	mark(0);
-	for(long long t0 = (long long) blockIdx.x * TC_RT; t0 < ntiles; t0 += (long long) gridDim.x * TC_RT) {
-		const int nt = (int) (ntiles - t0 < TC_RT ? ntiles - t0 : TC_RT);
+	const bool rowmode = (L % 128) == 0;
+	const int RT = rowmode ? TC_RT_ROWS : TC_RT;
+	const int RB = KC * 3 * TC_HALO;  // row mode: 16-byte chunks per tile
+	for(long long t0 = (long long) blockIdx.x * RT; t0 < ntiles; t0 += (long long) gridDim.x * RT) {
+		const int nt = (int) (ntiles - t0 < RT ? ntiles - t0 : RT);
+		if(rowmode) {
+			int4 *tile = reinterpret_cast<int4 *>(sm + TC_TILE_OFF);
+			if(threadIdx.x < (unsigned) nt) {
+				const int P0 = (int) ((t0 + threadIdx.x) * 128);
+				const int n = P0 / (int) LL, rr = P0 - n * (int) LL;
+				tile[threadIdx.x] = make_int4(n, rr / L, rr - (rr / L) * L, 0);
+			}
+			__syncthreads();
+			if(KC == 4) tc_stage_rows<4>(src, tile, nt, L, As);
+			else tc_stage_rows<2>(src, tile, nt, L, As);
+		}
+		else
 		// staging: thread -> (tile r, pixel p, half of the (tap, kc) chunks);
 		// requires 512 threads.  Copies go straight to shared memory
 		// (cp.async, all in flight); pooled inputs are averaged in registers.
@@ -172,8 +243,8 @@ static __device__ __noinline__ bool tc_conv_layer(int l, const TcSrc &src, const
 				const bool valid = P < npix;
 				int n = 0, y = 0, x = 0;
 				if(valid) {
-					n = (int) (P / LL);
-					const int rr = (int) (P - (long long) n * LL);
+					n = (int) P / (int) LL;
+					const int rr = (int) P - n * (int) LL;
 					y = rr / L;
 					x = rr - y * L;
 				}
@@ -219,13 +290,24 @@ static __device__ __noinline__ bool tc_conv_layer(int l, const TcSrc &src, const
 		mark(1);
 		if(threadIdx.x == 0) {
 			tc_fence_after();
-			for(int r = 0; r < nt; r++)
-				for(int t = 0; t < 9; t++)
-					for(int ks = 0; ks < KC / 2; ks++) {
-						const uint64_t ad = tc_sdesc(a_base + (uint32_t) ((((r * 9 + t) * KC + 2 * ks) * 128) * 16), 128 * 16, 128);
-						const uint64_t bd = tc_sdesc(b_base + (uint32_t) (((t * KC + 2 * ks) * 16) * 16), 16 * 16, 128);
-						tc_mma(tmem + (uint32_t) (r * 16), ad, bd, TC_IDESC, (t | ks) != 0);
+			// descriptors as base + offset: the start-address field counts 16-byte
+			// units and shared addresses stay below 256 KB, so offsets (in
+			// 16-byte chunks) add without carrying out of the field
+			const uint64_t ad0 = rowmode ? tc_sdesc(a_base, 3 * TC_HALO * 16, 128) : tc_sdesc(a_base, 128 * 16, 128);
+			const uint64_t bd0 = tc_sdesc(b_base, 16 * 16, 128);
+			const int nks = KC / 2;
+			// taps outer, tiles inner: consecutive MMAs go to different accumulators
+#pragma unroll
+			for(int t = 0; t < 9; t++) {
+				for(int ks = 0; ks < nks; ks++) {
+					const uint32_t boff = (uint32_t) ((t * KC + 2 * ks) * 16);
+					for(int r = 0; r < nt; r++) {
+						const uint32_t aoff = rowmode ? (uint32_t) (r * RB + ((2 * ks) * 3 + t / 3) * TC_HALO + t % 3)
+						                              : (uint32_t) (((r * 9 + t) * KC + 2 * ks) * 128);
+						tc_mma(tmem + (uint32_t) (r * 16), ad0 + aoff, bd0 + boff, TC_IDESC, (t | ks) != 0);
 					}
+				}
+			}
 			tc_commit(mbar);
 		}
 		bool ok = mbar_wait(mbar, phase, TC_WAIT_LIMIT);

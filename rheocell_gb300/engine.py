@@ -167,9 +167,11 @@ class Engine:
         return int(self._lib.rc_learned_harvested(self.h))
 
     def train(self, epochs: int = 8, batch: int = 8, learning_rate: float = 1e-3, validation: float = 0.1,
-              seed: int = 0, init: bool = True, max_samples: int = 0) -> Dict[str, float]:
+              seed: int = 0, init: bool = True, max_samples: int = 0,
+              learning_rate_final: float = 0.0) -> Dict[str, float]:
         """Train the network on the harvested samples (device kernels)."""
-        o = abi.RcTrainOptions(epochs, batch, learning_rate, validation, seed, int(init), max_samples)
+        o = abi.RcTrainOptions(epochs, batch, learning_rate, validation, seed, int(init), max_samples,
+                               learning_rate_final)
         r = abi.RcTrainReport()
         self._check(self._lib.rc_learned_train(self.h, C.byref(o), C.byref(r)), "rc_learned_train")
         return {name: getattr(r, name) for name, _ in abi.RcTrainReport._fields_}
