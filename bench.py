@@ -219,7 +219,8 @@ def run_gb300(args, rank, world):
     torch.cuda.set_device(dev)
     w = workload(args.workload)
     members = make_case(w)
-    prec = abi.RC_PRECISION_MIXED if args.precision == "mixed" else abi.RC_PRECISION_DOUBLE
+    prec = {"double": abi.RC_PRECISION_DOUBLE, "mixed": abi.RC_PRECISION_MIXED,
+            "float": abi.RC_PRECISION_FLOAT}[args.precision]
     built = [build_inputs(keys, m, precision=prec) for keys, m in members]
     stream = torch.cuda.Stream(dev)  # a real stream: the engine's graphs cannot capture on the legacy one
     torch.cuda.set_stream(stream)
@@ -335,7 +336,8 @@ def run_gb300(args, rank, world):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64" if args.precision == "double" else "f64 fields, f32 solve inner iterations",
+        "dtype": {"double": "f64", "mixed": "f64 fields, f32 solve inner iterations",
+                  "float": "f32 site arithmetic, f64 field storage and cell-area integrals"}[args.precision],
         "data": "synthetic (seeded jittered lattice, tanh interfaces)",
         "config": {"workload": w["name"], "L": [m.L for _, m in members] if len(members) > 1 else members[0][1].L,
                    "monolayers": len(members), "cells": n_cells, "sites": S, "precision": args.precision,
@@ -484,7 +486,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="wet256", choices=["wet256", "dry140", "ensemble64"])
-    ap.add_argument("--precision", default="double", choices=["double", "mixed"])
+    ap.add_argument("--precision", default="double", choices=["double", "mixed", "float"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--solver", default="plain", choices=["plain", "learned"])
     ap.add_argument("--harvest-steps", type=int, default=40)

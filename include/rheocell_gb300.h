@@ -55,8 +55,10 @@ typedef enum rc_model {
 /* backend_precision values (src/Backends/BackendFactory.cpp:14-16,38-63). */
 typedef enum rc_precision {
 	RC_PRECISION_DOUBLE = 0, /* FP64 everywhere; the parity path                    */
-	RC_PRECISION_MIXED = 1   /* FP64 fields; FP32 viscous-solve inner iterations,
+	RC_PRECISION_MIXED = 1,  /* FP64 fields; FP32 viscous-solve inner iterations,
 	                            FP64 dots and FP64 true-residual refinement        */
+	RC_PRECISION_FLOAT = 2   /* dry polar model: FP32 site arithmetic, FP64 field
+	                            storage and FP64 cell-area integrals               */
 } rc_precision;
 
 /*

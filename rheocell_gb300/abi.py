@@ -37,6 +37,7 @@ MODEL_NAMES = {"simplefield": RC_SIMPLEFIELD, "activenematic": RC_ACTIVENEMATIC,
 
 RC_PRECISION_DOUBLE = 0
 RC_PRECISION_MIXED = 1
+RC_PRECISION_FLOAT = 2
 
 RC_FIELD_SCALARS = 0x01
 RC_FIELD_PHI = 0x02

@@ -230,6 +230,59 @@ __device__ void directed_forces_dev(CellDev &c, const DevParams &P, const PhaseP
 	}
 }
 
+// Per-cell epilogue of an evaluation / update (one thread): cell outputs,
+// area, centre of mass, set_positions, the per-cell scalar dynamics and the
+// bins of the next gather.  Shared by the FP64 and FP32 cell kernels.
+template<int MODEL, int EVAL, int UPD>
+__device__ __forceinline__ void cell_finish(CellDev &c, const double (&acc)[12], const int (&imin)[2], double perim,
+                                            const CellArgs &a, const LayerDev &lay, int ci) {
+	const DevParams &P = a.P;
+	const PhaseParams &pu = a.pu;
+	const int lx = c.lx, ly = c.ly, L = lay.L;
+	(void) lx;
+	(void) ly;
+	if(EVAL != EV_NONE) {
+		// per-cell outputs of the evaluation (perimeter, force totals)
+		c.perim = (MODEL == M_POLAR) ? perim : 0.0;
+		if(MODEL == M_POLAR) {
+			c.trx = acc[8];
+			c.try_ = acc[9];
+			c.tfx = acc[10];
+			c.tfy = acc[11];
+		}
+		else {
+			c.trx = c.try_ = c.tfx = c.tfy = 0.0;
+		}
+	}
+	if(UPD != UP_NONE) {
+		if(UPD == UP_PRED) {
+			c.com_oldx = c.comx;
+			c.com_oldy = c.comy;
+			c.area_old = c.area;
+			c.sumf_old = c.sumf;
+		}
+		c.area = acc[0];
+		c.sumf = acc[1];
+		c.s00 = acc[6];
+		c.s01 = acc[7];
+		c.perim = 0.0;
+		c.xl = (UPD == UP_CORR) ? imin[0] : lx;
+		c.yb = (UPD == UP_CORR) ? imin[1] : ly;
+		c.comx = c.lx * (atan2(-acc[3] / c.sumf, -acc[2] / c.sumf) + RC_PI_F) / (2 * RC_PI_F);
+		c.comy = c.ly * (atan2(-acc[5] / c.sumf, -acc[4] / c.sumf) + RC_PI_F) / (2 * RC_PI_F);
+		if(!isfinite(c.area) || !isfinite(c.sumf) || !isfinite(c.comx) || !isfinite(c.comy)) {
+			atomicOr(&a.st->err, ERR_NONFINITE);
+			a.st->err_where = ci;
+		}
+		if(UPD == UP_CORR) set_positions_dev(c, P, L, a.st, ci);
+		directed_forces_dev(c, P, pu, UPD == UP_PRED, a.st, ci);
+		if(UPD == UP_CORR) {
+			append_bins(c, ci, lay, a.bin_count, a.bin_cells, a.st);
+			atomicMax(&a.st->max_n, c.n);
+		}
+	}
+}
+
 // Forces of one site from the shared-memory patch (stage 2 of the evaluation)
 // and the update of that site.  Kept as one templated kernel so that the fused
 // (dry) and split (wet) variants share every line of arithmetic.
@@ -597,53 +650,374 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 		}
 	}
 
-	if(threadIdx.x == 0) {
-		if(EVAL != EV_NONE) {
-			// per-cell outputs of the evaluation (perimeter, force totals)
-			c.perim = (MODEL == M_POLAR) ? perim : 0.0;
-			if(MODEL == M_POLAR) {
-				c.trx = acc[8];
-				c.try_ = acc[9];
-				c.tfx = acc[10];
-				c.tfy = acc[11];
-			}
-			else {
-				c.trx = c.try_ = c.tfx = c.tfy = 0.0;
-			}
+	if(a.split) {
+		if(threadIdx.x == 0) {
+			CellSum &o = a.csum[ci];
+#pragma unroll
+			for(int i = 0; i < 12; i++) o.acc[i] = acc[i];
+			o.imin[0] = imin[0];
+			o.imin[1] = imin[1];
+			o.perim = perim;
 		}
-		if(UPD != UP_NONE) {
-			if(UPD == UP_PRED) {
-				c.com_oldx = c.comx;
-				c.com_oldy = c.comy;
-				c.area_old = c.area;
-				c.sumf_old = c.sumf;
-			}
-			c.area = acc[0];
-			c.sumf = acc[1];
-			c.s00 = acc[6];
-			c.s01 = acc[7];
-			c.perim = 0.0;
-			c.xl = (UPD == UP_CORR) ? imin[0] : lx;
-			c.yb = (UPD == UP_CORR) ? imin[1] : ly;
-			c.comx = c.lx * (atan2(-acc[3] / c.sumf, -acc[2] / c.sumf) + RC_PI_F) / (2 * RC_PI_F);
-			c.comy = c.ly * (atan2(-acc[5] / c.sumf, -acc[4] / c.sumf) + RC_PI_F) / (2 * RC_PI_F);
-			if(!isfinite(c.area) || !isfinite(c.sumf) || !isfinite(c.comx) || !isfinite(c.comy)) {
-				atomicOr(&a.st->err, ERR_NONFINITE);
-				a.st->err_where = ci;
-			}
-			if(UPD == UP_CORR) set_positions_dev(c, P, L, a.st, ci);
-			directed_forces_dev(c, P, pu, UPD == UP_PRED, a.st, ci);
-			if(UPD == UP_CORR) {
-				append_bins(c, ci, lay, a.bin_count, a.bin_cells, a.st);
-				atomicMax(&a.st->max_n, c.n);
-			}
-		}
+		return;
 	}
+	if(threadIdx.x == 0) cell_finish<MODEL, EVAL, UPD>(c, acc, imin, perim, a, lay, ci);
 	__syncthreads();
 	{
 		const int *src = reinterpret_cast<const int *>(&c);
 		int *dst = reinterpret_cast<int *>(&a.cells[ci]);
 		for(int i = threadIdx.x; i < (int) (sizeof(CellDev) / 4); i += blockDim.x) dst[i] = src[i];
+	}
+}
+
+// ---------------------------------------------------------------- FP32 ---
+// double <-> float conversions on the integer pipes (on GB300 the conversion
+// instructions issue on the narrow FP64 pipe).  Round to nearest even;
+// magnitudes below the FP32 normal range become zero and the fields' values
+// never reach the FP32 overflow range.
+__device__ __forceinline__ float d2f_int(double v) {
+	const unsigned hi = (unsigned) __double2hiint(v), lo = (unsigned) __double2loint(v);
+	const unsigned sign = hi & 0x80000000u;
+	const int e = (int) ((hi >> 20) & 0x7FFu) - 896;  // FP32 biased exponent
+	if(e <= 0) return __uint_as_float(sign);
+	unsigned m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+	const unsigned r = lo & 0x1FFFFFFFu;
+	unsigned bits = sign | ((unsigned) e << 23);
+	bits += m;
+	if(r > 0x10000000u || (r == 0x10000000u && (m & 1u))) bits += 1u;  // carries into the exponent
+	return __uint_as_float(bits);
+}
+
+__device__ __forceinline__ double f2d_int(float v) {
+	const unsigned b = __float_as_uint(v);
+	const unsigned sign = b & 0x80000000u, e = (b >> 23) & 0xFFu, m = b & 0x7FFFFFu;
+	if(e == 0u) return __hiloint2double((int) sign, 0);
+	return __hiloint2double((int) (sign | ((e + 896u) << 20) | (m >> 3)), (int) (m << 29));
+}
+
+// Double-float accumulation of x*x: (s, c) holds the running sum with its
+// error term (exact product by FMA, Knuth's TwoSum), close to FP64 accuracy
+// with FP32 arithmetic only.
+__device__ __forceinline__ void acc_square(float x, float &s, float &c) {
+	const float p = x * x;
+	const float ep = __fmaf_rn(x, x, -p);
+	const float t = s + p;
+	const float bp = t - s;
+	const float err = (s - (t - bp)) + (p - bp);
+	s = t;
+	c += err + ep;
+}
+
+// The dry polar model (wetpolarmodel with friction_cell = 0, the
+// ensemble's model) with FP32 site arithmetic: the patch, chemical
+// potential, forces and the update in FP32 (shared memory in FP32, fields
+// stored in FP64); the area integral sum(phi^2) that drives the area
+// constraint accumulates in double-float (near FP64), the other per-cell
+// sums from FP32 per-thread partials in FP64.  Same stages, expressions and per-cell
+// epilogue as cell_kernel<M_POLAR, ...>; not bitwise the reference.
+template<int EVAL, int UPD>
+__global__ void __launch_bounds__(CELL_THREADS) cell_kernel_f32(const CellArgs a) {
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	__shared__ CellDev c;
+	__shared__ double red[12 * (CELL_THREADS / 32 + 1)];
+	__shared__ int ired[2 * (CELL_THREADS / 32)];
+	const int ci = blockIdx.x;
+	{
+		const int *src = reinterpret_cast<const int *>(&a.cells[ci]);
+		int *dst = reinterpret_cast<int *>(&c);
+		for(int i = threadIdx.x; i < (int) (sizeof(CellDev) / 4); i += blockDim.x) dst[i] = src[i];
+	}
+	__syncthreads();
+	const LayerDev lay = a.layers[c.layer];
+	const int n = c.n, lx = c.lx, ly = c.ly, L = lay.L, start = c.start;
+	const double *phi2 = a.phi2 + lay.box_off;
+	if(n > a.smem_n) {
+		if(threadIdx.x == 0) {
+			atomicOr(&a.st->err, ERR_CAPACITY);
+			a.st->err_where = ci;
+		}
+		return;
+	}
+	float *sphi = reinterpret_cast<float *>(smem_raw);
+	float *smu = sphi + a.smem_n;
+	float *saux = smu + a.smem_n;
+	const DevParams &P = a.P;
+	const PhaseParams &pe = a.pe;
+	const float gamma = (float) P.gamma, lambda = (float) P.lambda, omega = (float) P.omega;
+	const float rlambda = (float) (1.0 / P.lambda), two_lambda = 2.f * lambda;
+	const float A_c = (float) (-4 * (P.mu / P.a0) * (1 - c.area / P.a0));
+	const float Rep_c = (float) (4 * (P.kappa / P.lambda));
+	double perim = 0.0;
+	if(EVAL != EV_NONE) {
+		for(int q = threadIdx.x; q < n; q += blockDim.x) sphi[q] = d2f_int(a.phi_eval[start + q]);
+		__syncthreads();
+		if(pe.beta != 0.0) {
+			float pp = 0.f;
+			for(int q = threadIdx.x; q < n; q += blockDim.x) {
+				const int y = q / lx, x = q - y * lx;
+				const Nb nb = patch_nb(q, x, y, lx, ly);
+				const float dx = .5f * (sphi[nb.r] - sphi[nb.l]);
+				const float dy = .5f * (sphi[nb.u] - sphi[nb.d]);
+				pp += dx * dx + dy * dy;
+			}
+#pragma unroll
+			for(int o = 16; o > 0; o >>= 1) pp += __shfl_down_sync(0xffffffffu, pp, o);
+			__shared__ float s_pp[CELL_THREADS / 32];
+			if((threadIdx.x & 31) == 0) s_pp[threadIdx.x >> 5] = pp;
+			__syncthreads();
+			double t = 0.0;
+			for(int w = 0; w < (int) (blockDim.x >> 5); w++) t += (double) s_pp[w];
+			perim = t;
+		}
+		const float beta_t = (float) (4 * (pe.beta / 12.) * (1 - perim / 12.));
+		for(int q = threadIdx.x; q < n; q += blockDim.x) {
+			const int y = q / lx, x = q - y * lx;
+			const Nb nb = patch_nb(q, x, y, lx, ly);
+			const float phi = sphi[q];
+			const float pr = sphi[nb.r], pl = sphi[nb.l], pu_ = sphi[nb.u], pd = sphi[nb.d];
+			const int k = box_site(c, x, y, L);
+			const float p2 = d2f_int(phi2[k]);
+			const float lap = pu_ + pd + pr + pl - 4.f * phi;
+			const float CH = gamma * (8.f * phi * (1.f - phi) * (1.f - 2.f * phi) * rlambda - two_lambda * lap);
+			const float Rep = Rep_c * phi * (p2 - phi * phi);
+			float V = CH + A_c * phi + Rep;
+			if(omega != 0.f) {
+				const BoxNb kb = box_nb(k, L);
+				const float ls = (float) (phi2[kb.r] + phi2[kb.u] + phi2[kb.l] + phi2[kb.d] - 4. * phi2[k]);
+				const float dx = .5f * (pr - pl), dy = .5f * (pu_ - pd);
+				const float lsq = 2.f * phi * lap + 2.f * (dx * dx + dy * dy);
+				const float sup = (ls - lsq) * rsqrtf(1.f + (ls - lsq) * (ls - lsq));
+				V = V + (-4.f * lambda * omega * sup * phi);
+			}
+			if(pe.beta != 0.0) V = V + beta_t * lap;
+			if(a.rep_on) {
+				const float r = d2f_int(a.rep[start + q]) + Rep;
+				if(a.accumulate_rep) a.rep[start + q] = f2d_int(r);
+				saux[q] = r;
+			}
+			smu[q] = V;
+		}
+		__syncthreads();
+	}
+	double acc[12];
+#pragma unroll
+	for(int i = 0; i < 12; i++) acc[i] = 0.0;
+	float af[12];
+#pragma unroll
+	for(int i = 0; i < 12; i++) af[i] = 0.f;
+	int imin[2] = {lx, ly};
+	float area_s = 0.f, area_c = 0.f;
+	const PhaseParams &pu = a.pu;
+	const float J0 = (float) P.J0, hdt = (float) (P.dt * .5);
+	const float zs = (float) pe.zs, alpha = (float) P.passive_alpha, lam = lambda;
+	const float rfr = (float) (1.0 / pe.friction);
+	const int tb = table_base(lx), tby = table_base(ly);
+	const float q00 = (float) c.q00, q01 = (float) c.q01;
+	for(int q = threadIdx.x; q < n; q += blockDim.x) {
+		const int y = q / lx, x = q - y * lx;
+		float mu, vx, vy, dx, dy, phi_e = 0.f;
+		if(EVAL != EV_NONE) {
+			const Nb nb = patch_nb(q, x, y, lx, ly);
+			phi_e = sphi[q];
+			dx = .5f * (sphi[nb.r] - sphi[nb.l]);
+			dy = .5f * (sphi[nb.u] - sphi[nb.d]);
+			mu = smu[q];
+			const float fpx = -.5f * (smu[nb.r] - smu[nb.l]);
+			const float fpy = -.5f * (smu[nb.u] - smu[nb.d]);
+			if(a.rep_on) {
+				af[8] += -.5f * (saux[nb.r] - saux[nb.l]) * phi_e;
+				af[9] += -.5f * (saux[nb.u] - saux[nb.d]) * phi_e;
+			}
+			const float sx = -dx * q00, sy = -dy * q01;
+			const float fsx = sx < 0.f ? 0.f : lam * sx * q00;
+			const float fsy = sy < 0.f ? 0.f : lam * sy * q01;
+			const float fx = fpx * alpha + fsx * zs;
+			const float fy = fpy * alpha + fsy * zs;
+			af[10] += fx * phi_e;
+			af[11] += fy * phi_e;
+			vx = fx * rfr;
+			vy = fy * rfr;
+		}
+		else {
+			mu = d2f_int(a.mu[start + q]);
+			vx = d2f_int(a.vxg[start + q]);
+			vy = d2f_int(a.vyg[start + q]);
+			dx = d2f_int(a.dxg[start + q]);
+			dy = d2f_int(a.dyg[start + q]);
+		}
+		const float dphi = -J0 * mu - vx * dx - vy * dy;
+		float phi_new;
+		if(UPD == UP_PRED) {
+			const float phi_old = (EVAL != EV_NONE) ? phi_e : d2f_int(a.phi_eval[start + q]);
+			a.dphi_old[start + q] = f2d_int(dphi);
+			phi_new = phi_old + hdt * (dphi + dphi);
+		}
+		else {
+			phi_new = d2f_int(a.phi_old[start + q]) + hdt * (dphi + d2f_int(a.dphi_old[start + q]));
+		}
+		a.phi_out[start + q] = f2d_int(phi_new);
+		acc_square(phi_new, area_s, area_c);
+		af[1] += phi_new;
+		int lxx = x + c.offx;
+		if(lxx >= lx) lxx -= lx;
+		int lyy = y + c.offy;
+		if(lyy >= ly) lyy -= ly;
+		af[2] += phi_new * a.tab_cosf[tb + lxx];
+		af[3] += phi_new * a.tab_sinf[tb + lxx];
+		af[4] += phi_new * a.tab_cosf[tby + lyy];
+		af[5] += phi_new * a.tab_sinf[tby + lyy];
+		if(UPD == UP_CORR && phi_new < 0.09f && phi_new > 0.01f) {
+			imin[0] = min(imin[0], lxx);
+			imin[1] = min(imin[1], lyy);
+		}
+		af[6] += -.5f * (dx * dx - dy * dy);
+		af[7] += -dx * dy;
+	}
+	if(a.split) {
+		// per-warp partials for the epilogue kernel: FP32 warp trees, the area
+		// as a double-float pair, converted once per warp
+		const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+		for(int o = 16; o > 0; o >>= 1) {
+			const float s2 = __shfl_down_sync(0xffffffffu, area_s, o);
+			const float c2 = __shfl_down_sync(0xffffffffu, area_c, o);
+			const float t = area_s + s2, bp = t - area_s;
+			area_c += ((area_s - (t - bp)) + (s2 - bp)) + c2;
+			area_s = t;
+#pragma unroll
+			for(int i = 1; i < 12; i++) af[i] += __shfl_down_sync(0xffffffffu, af[i], o);
+		}
+		if(UPD == UP_CORR) block_min<2>(imin, ired);
+		CellSum &o = a.csum[ci];
+		if(lane == 0) {
+			o.area[warp] = (double) area_s + (double) area_c;
+#pragma unroll
+			for(int i = 1; i < 12; i++) o.part[warp][i] = af[i];
+		}
+		if(threadIdx.x == 0) {
+			o.imin[0] = imin[0];
+			o.imin[1] = imin[1];
+			o.perim = perim;
+		}
+		return;
+	}
+	acc[0] = (double) area_s + (double) area_c;
+	// per-cell sums: warp trees in FP32 (the area term in FP64), then the
+	// warps' partial sums in FP64 by one warp; the totals are needed by thread 0 only
+	{
+		const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+		for(int o = 16; o > 0; o >>= 1) {
+			acc[0] += __shfl_down_sync(0xffffffffu, acc[0], o);
+#pragma unroll
+			for(int i = 1; i < 12; i++) af[i] += __shfl_down_sync(0xffffffffu, af[i], o);
+		}
+		if(lane == 0) {
+			red[warp] = acc[0];
+#pragma unroll
+			for(int i = 1; i < 12; i++) red[i * nw + warp] = (double) af[i];
+		}
+		__syncthreads();
+		if(warp == 0) {
+#pragma unroll
+			for(int i = 0; i < 12; i++) {
+				double t = lane < nw ? red[i * nw + lane] : 0.0;
+#pragma unroll
+				for(int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+				acc[i] = t;
+			}
+		}
+	}
+	if(UPD == UP_CORR) block_min<2>(imin, ired);
+	if(threadIdx.x == 0) cell_finish<M_POLAR, EVAL, UPD>(c, acc, imin, perim, a, lay, ci);
+	__syncthreads();
+	{
+		const int *src = reinterpret_cast<const int *>(&c);
+		int *dst = reinterpret_cast<int *>(&a.cells[ci]);
+		for(int i = threadIdx.x; i < (int) (sizeof(CellDev) / 4); i += blockDim.x) dst[i] = src[i];
+	}
+}
+
+bool launch_cell_kernel_f32(int eval, int upd, const CellArgs &a, cudaStream_t s) {
+	if(a.N <= 0) return true;
+	const size_t smem = sizeof(float) * 3 * (size_t) a.smem_n;
+	if(eval == EV_LOCAL && upd == UP_PRED) cell_kernel_f32<EV_LOCAL, UP_PRED><<<a.N, CELL_THREADS, smem, s>>>(a);
+	else if(eval == EV_LOCAL && upd == UP_CORR) cell_kernel_f32<EV_LOCAL, UP_CORR><<<a.N, CELL_THREADS, smem, s>>>(a);
+	else if(eval == EV_NONE && upd == UP_PRED) cell_kernel_f32<EV_NONE, UP_PRED><<<a.N, CELL_THREADS, smem, s>>>(a);
+	else return false;
+	return true;
+}
+
+static cudaError_t configure_f32() {
+	cudaError_t e = cudaSuccess, c;
+	if((c = cudaFuncSetAttribute(cell_kernel_f32<EV_LOCAL, UP_PRED>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)) !=
+	   cudaSuccess)
+		e = c;
+	if((c = cudaFuncSetAttribute(cell_kernel_f32<EV_LOCAL, UP_CORR>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)) !=
+	   cudaSuccess)
+		e = c;
+	if((c = cudaFuncSetAttribute(cell_kernel_f32<EV_NONE, UP_PRED>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)) !=
+	   cudaSuccess)
+		e = c;
+	return e;
+}
+
+// Split mode: the per-cell epilogue with one thread per cell, so that 32
+// cells share every FP64 instruction of the centre-of-mass, re-centering and
+// per-cell dynamics code (the same cell_finish the fused kernels run).
+template<int MODEL, int EVAL, int UPD, bool F32>
+__global__ void __launch_bounds__(128) cell_finish_kernel(const CellArgs a) {
+	const int ci = blockIdx.x * blockDim.x + threadIdx.x;
+	if(ci >= a.N) return;
+	CellDev c = a.cells[ci];
+	const CellSum &sm = a.csum[ci];
+	double acc[12];
+	if(F32) {
+		double t = 0.0;
+		for(int w = 0; w < CELL_THREADS / 32; w++) t += sm.area[w];
+		acc[0] = t;
+#pragma unroll
+		for(int i = 1; i < 12; i++) {
+			double u = 0.0;
+			for(int w = 0; w < CELL_THREADS / 32; w++) u += (double) sm.part[w][i];
+			acc[i] = u;
+		}
+	}
+	else {
+#pragma unroll
+		for(int i = 0; i < 12; i++) acc[i] = sm.acc[i];
+	}
+	const int imin[2] = {sm.imin[0], sm.imin[1]};
+	const LayerDev lay = a.layers[c.layer];
+	cell_finish<MODEL, EVAL, UPD>(c, acc, imin, sm.perim, a, lay, ci);
+	a.cells[ci] = c;
+}
+
+template<int MODEL, bool F32>
+static void launch_finish_m(int eval, int upd, const CellArgs &a, cudaStream_t s) {
+	const int g = (a.N + 127) / 128;
+	if(eval == EV_STORE && upd == UP_NONE) cell_finish_kernel<MODEL, EV_STORE, UP_NONE, F32><<<g, 128, 0, s>>>(a);
+	else if(eval == EV_WET_RHS && upd == UP_NONE) cell_finish_kernel<MODEL, EV_WET_RHS, UP_NONE, F32><<<g, 128, 0, s>>>(a);
+	else if(eval == EV_LOCAL && upd == UP_PRED) cell_finish_kernel<MODEL, EV_LOCAL, UP_PRED, F32><<<g, 128, 0, s>>>(a);
+	else if(eval == EV_LOCAL && upd == UP_CORR) cell_finish_kernel<MODEL, EV_LOCAL, UP_CORR, F32><<<g, 128, 0, s>>>(a);
+	else if(eval == EV_NONE && upd == UP_PRED) cell_finish_kernel<MODEL, EV_NONE, UP_PRED, F32><<<g, 128, 0, s>>>(a);
+	else if(eval == EV_NONE && upd == UP_CORR) cell_finish_kernel<MODEL, EV_NONE, UP_CORR, F32><<<g, 128, 0, s>>>(a);
+}
+
+void launch_cell_finish(int model, int eval, int upd, bool f32, const CellArgs &a, cudaStream_t s) {
+	if(a.N <= 0) return;
+	if(f32) {
+		const int g = (a.N + 127) / 128;
+		if(eval == EV_LOCAL && upd == UP_PRED) cell_finish_kernel<M_POLAR, EV_LOCAL, UP_PRED, true><<<g, 128, 0, s>>>(a);
+		else if(eval == EV_LOCAL && upd == UP_CORR) cell_finish_kernel<M_POLAR, EV_LOCAL, UP_CORR, true><<<g, 128, 0, s>>>(a);
+		else cell_finish_kernel<M_POLAR, EV_NONE, UP_PRED, true><<<g, 128, 0, s>>>(a);
+		return;
+	}
+	switch(model) {
+		case M_SIMPLE: launch_finish_m<M_SIMPLE, false>(eval, upd, a, s); break;
+		case M_NEMATIC: launch_finish_m<M_NEMATIC, false>(eval, upd, a, s); break;
+		case M_POLAR: launch_finish_m<M_POLAR, false>(eval, upd, a, s); break;
+		default: launch_finish_m<M_WET, false>(eval, upd, a, s); break;
 	}
 }
 
@@ -803,6 +1177,7 @@ cudaError_t configure_kernels() {
 	if((c = configure_m<M_NEMATIC>()) != cudaSuccess) e = c;
 	if((c = configure_m<M_POLAR>()) != cudaSuccess) e = c;
 	if((c = configure_m<M_WET>()) != cudaSuccess) e = c;
+	if((c = configure_f32()) != cudaSuccess) e = c;
 	unsigned long long A[2 * CELL_THREADS + 1], Cc[2 * CELL_THREADS + 1];
 	const unsigned long long a = 0x5DEECE66DULL, cc = 0xBULL, M = (1ULL << 48) - 1;
 	A[0] = 1;

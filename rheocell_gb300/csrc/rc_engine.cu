@@ -39,6 +39,10 @@ using namespace rc;
 
 #define RC_PI_F 3.141592653589793238462643f
 
+// From this many cells on, the per-cell epilogue runs as its own kernel with
+// one thread per cell (its FP64 code then shares instructions across cells).
+constexpr int SPLIT_FINISH_CELLS = 256;
+
 struct rc_engine {
 	int device = 0;
 	cudaStream_t stream = nullptr;
@@ -69,6 +73,8 @@ struct rc_engine {
 	int *cnt = nullptr, *cover = nullptr, *cov_off = nullptr, *cov_idx = nullptr;
 	int *bin_count = nullptr, *bin_cells = nullptr;
 	double *tab_cos = nullptr, *tab_sin = nullptr;
+	float *tab_cosf = nullptr, *tab_sinf = nullptr;
+	CellSum *csum = nullptr;  // split mode (many cells): per-cell sums for the epilogue kernel
 	DevStatus *st = nullptr;
 	DevStatus *st_host = nullptr;
 	double *rx = nullptr, *ry = nullptr, *px = nullptr, *py = nullptr, *apx = nullptr, *apy = nullptr, *Px = nullptr, *Py = nullptr;
@@ -218,6 +224,8 @@ static CellArgs cell_args(rc_engine *e) {
 	a.sq01 = e->sq01;
 	a.tab_cos = e->tab_cos;
 	a.tab_sin = e->tab_sin;
+	a.tab_cosf = e->tab_cosf;
+	a.tab_sinf = e->tab_sinf;
 	a.bin_count = e->bin_count;
 	a.bin_cells = e->bin_cells;
 	a.nbx = e->nbx;
@@ -228,6 +236,21 @@ static CellArgs cell_args(rc_engine *e) {
 	a.rep_on = e->rep_on;
 	a.accumulate_rep = 1;
 	return a;
+}
+
+// Cell kernel launch: the FP32 variant where the engine runs
+// RC_PRECISION_FLOAT and one exists for (eval, upd), else FP64; in split
+// mode (many cells) followed by the per-cell epilogue kernel.  Returns the
+// number of kernels launched.
+static int cell_launch(rc_engine *e, int eval, int upd, const CellArgs &a0, cudaStream_t s) {
+	CellArgs a = a0;
+	a.split = e->csum != nullptr;
+	a.csum = e->csum;
+	const bool f32 = e->hp.precision == RC_PRECISION_FLOAT && launch_cell_kernel_f32(eval, upd, a, s);
+	if(!f32) launch_cell_kernel(e->P.model, eval, upd, a, s);
+	if(!a.split) return 1;
+	launch_cell_finish(e->P.model, eval, upd, f32, a, s);
+	return 2;
 }
 
 static void gather(rc_engine *e, const double *phi, int phase) {
@@ -342,7 +365,7 @@ static void evaluate_end(rc_engine *e, const double *phi, int phase) {
 		a.pu = e->ph[phase];
 		{
 			StageMark sm(e, RC_TIMER_FORCES);
-			launch_cell_kernel(e->P.model, EV_WET_RHS, UP_NONE, a, e->stream);
+			e->launches += cell_launch(e, EV_WET_RHS, UP_NONE, a, e->stream) - 1;
 		}
 		e->launches += 1;
 		solve(e, phase);
@@ -370,11 +393,11 @@ static void one_step(rc_engine *e) {
 		StageMark sm(e, RC_TIMER_UPDATE);
 		if(e->pending) {
 			a.pe = e->ph[e->eval_phase];
-			launch_cell_kernel(e->P.model, EV_LOCAL, UP_PRED, a, s);
+			e->launches += cell_launch(e, EV_LOCAL, UP_PRED, a, s) - 1;
 		}
 		else {
 			a.pe = e->ph[cur];
-			launch_cell_kernel(e->P.model, EV_NONE, UP_PRED, a, s);
+			e->launches += cell_launch(e, EV_NONE, UP_PRED, a, s) - 1;
 		}
 	}
 	e->launches += 1;
@@ -388,7 +411,7 @@ static void one_step(rc_engine *e) {
 	if(!wet_phase(e, cur)) {
 		c.phi_eval = e->phiB;
 		StageMark sm(e, RC_TIMER_UPDATE);
-		launch_cell_kernel(e->P.model, EV_LOCAL, UP_CORR, c, s);
+		e->launches += cell_launch(e, EV_LOCAL, UP_CORR, c, s) - 1;
 		e->launches += 1;
 	}
 	else {
@@ -398,13 +421,13 @@ static void one_step(rc_engine *e) {
 		f.pu = e->ph[cur];
 		{
 			StageMark sm(e, RC_TIMER_FORCES);
-			launch_cell_kernel(e->P.model, EV_WET_RHS, UP_NONE, f, s);
+			e->launches += cell_launch(e, EV_WET_RHS, UP_NONE, f, s) - 1;
 		}
 		solve(e, cur);
 		c.phi_eval = e->phiB;
 		{
 			StageMark sm(e, RC_TIMER_UPDATE);
-			launch_cell_kernel(e->P.model, EV_NONE, UP_CORR, c, s);
+			e->launches += cell_launch(e, EV_NONE, UP_CORR, c, s) - 1;
 		}
 		e->launches += 2;
 	}
@@ -493,7 +516,7 @@ static void materialise(rc_engine *e, int accumulate) {
 	a.pe = e->ph[e->eval_phase];
 	a.pu = e->ph[e->eval_phase];
 	a.accumulate_rep = accumulate;
-	launch_cell_kernel(e->P.model, EV_STORE, UP_NONE, a, e->stream);
+	e->launches += cell_launch(e, EV_STORE, UP_NONE, a, e->stream) - 1;
 	e->launches += 1;
 	if(accumulate) e->pending = false;
 }
@@ -622,10 +645,13 @@ int rc_batch_create(const rc_params *params, int n_layers, const rc_box *boxes, 
 	if(params->model < RC_SIMPLEFIELD || params->model > RC_WETMODEL)
 		return set_err(nullptr, RC_ERR_INVALID, "unknown interaction model %d", params->model);
 	if(params->anchoring) return set_err(nullptr, RC_ERR_UNSUPPORTED, "anchoring is not provided");
-	if(params->precision != RC_PRECISION_DOUBLE && params->precision != RC_PRECISION_MIXED)
+	if(params->precision != RC_PRECISION_DOUBLE && params->precision != RC_PRECISION_MIXED &&
+	   params->precision != RC_PRECISION_FLOAT)
 		return set_err(nullptr, RC_ERR_INVALID, "unknown precision %d", params->precision);
 	const bool any_wet = (params->model == RC_WETMODEL || params->model == RC_WETPOLARMODEL) &&
 	                     (params->friction_cell[0] != 0.0 || params->friction_cell[1] != 0.0);
+	if(params->precision == RC_PRECISION_FLOAT && (params->model != RC_WETPOLARMODEL || any_wet))
+		return set_err(nullptr, RC_ERR_UNSUPPORTED, "FP32 fields are provided for the dry polar model only");
 	if(n_layers > 1 && any_wet)
 		return set_err(nullptr, RC_ERR_UNSUPPORTED, "batches of monolayers are provided for dry evaluations only");
 	std::vector<LayerDev> layers((size_t) n_layers);
@@ -748,6 +774,9 @@ int rc_batch_create(const rc_params *params, int n_layers, const rc_box *boxes, 
 	   (rc = dalloc(e, &e->layers, (size_t) n_layers)) ||
 	   (rc = dalloc(e, &e->tab_cos, (size_t) table_base(MAX_TABLE_SIDE + 1))) ||
 	   (rc = dalloc(e, &e->tab_sin, (size_t) table_base(MAX_TABLE_SIDE + 1))) ||
+	   (rc = dalloc(e, &e->tab_cosf, (size_t) table_base(MAX_TABLE_SIDE + 1))) ||
+	   (n_cells >= SPLIT_FINISH_CELLS && (rc = dalloc(e, &e->csum, (size_t) n_cells))) ||
+	   (rc = dalloc(e, &e->tab_sinf, (size_t) table_base(MAX_TABLE_SIDE + 1))) ||
 	   (rc = dalloc(e, &e->st, 1)) ||
 	   (rc = dalloc(e, &e->scratch_phi, cap + (size_t) n_cells / 2 + 8)) ||
 	   (rc = dalloc(e, &e->rep, e->rep_on ? cap : 1)) || (rc = dalloc(e, &e->scratch_rep, e->rep_on ? cap : 1)))
@@ -784,6 +813,9 @@ int rc_batch_create(const rc_params *params, int n_layers, const rc_box *boxes, 
 			}
 		CUDA_TRY(e, cudaMemcpy(e->tab_cos, tc.data(), sizeof(double) * tc.size(), cudaMemcpyHostToDevice));
 		CUDA_TRY(e, cudaMemcpy(e->tab_sin, ts.data(), sizeof(double) * ts.size(), cudaMemcpyHostToDevice));
+		std::vector<float> tcf(tc.begin(), tc.end()), tsf(ts.begin(), ts.end());
+		CUDA_TRY(e, cudaMemcpy(e->tab_cosf, tcf.data(), sizeof(float) * tcf.size(), cudaMemcpyHostToDevice));
+		CUDA_TRY(e, cudaMemcpy(e->tab_sinf, tsf.data(), sizeof(float) * tsf.size(), cudaMemcpyHostToDevice));
 	}
 	// cells and fields
 	{

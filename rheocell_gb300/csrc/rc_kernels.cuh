@@ -11,6 +11,18 @@ namespace rc {
 enum EvalMode { EV_NONE = 0, EV_STORE = 1, EV_WET_RHS = 2, EV_LOCAL = 3 };
 enum UpdMode { UP_NONE = 0, UP_PRED = 1, UP_CORR = 2 };
 
+// Per-cell sums handed from a cell kernel to the per-cell epilogue kernel
+// (split mode): the FP64 kernels' block totals, or the FP32 kernel's
+// per-warp partials (combined in FP64 by the epilogue kernel).
+struct CellSum {
+	double acc[12];
+	double area[CELL_THREADS / 32];
+	float part[CELL_THREADS / 32][12];
+	int imin[2];
+	int pad[2];
+	double perim;
+};
+
 struct CellArgs {
 	CellDev *cells;
 	const LayerDev *layers;
@@ -25,6 +37,9 @@ struct CellArgs {
 	double *rep;
 	const double *phi2, *sq00, *sq01;
 	const double *tab_cos, *tab_sin;
+	const float *tab_cosf, *tab_sinf;  // the same tables rounded to FP32 (FP32 kernels)
+	CellSum *csum;                     // split mode: sums for the epilogue kernel
+	int split;                         // 1: the per-cell epilogue runs in cell_finish_kernel
 	int *bin_count, *bin_cells;
 	int nbx, nby;
 	DevStatus *st;
@@ -91,6 +106,10 @@ struct CGArgs {
 
 cudaError_t configure_kernels();
 void launch_cell_kernel(int model, int eval, int upd, const CellArgs &a, cudaStream_t s);
+// FP32 site arithmetic for the dry polar model; false if (eval, upd) has no FP32 variant
+bool launch_cell_kernel_f32(int eval, int upd, const CellArgs &a, cudaStream_t s);
+// split mode: the per-cell epilogue, one thread per cell (f32: after the FP32 kernel)
+void launch_cell_finish(int model, int eval, int upd, bool f32, const CellArgs &a, cudaStream_t s);
 size_t cell_smem_bytes(int model, int smem_n);
 int cell_smem_arrays(int model);
 void launch_rng(CellDev *cells, LayerDev *layers, int n_layers, DevStatus *st, cudaStream_t s);

@@ -114,6 +114,7 @@ public:
 		std::string prec = inp.str("backend_precision", "double");
 		if(prec == "double") params_.precision = RC_PRECISION_DOUBLE;
 		else if(prec == "mixed") params_.precision = RC_PRECISION_MIXED;
+		else if(prec == "float") params_.precision = RC_PRECISION_FLOAT;
 		else throw RCexception("Backend precision '" + prec + "' is not allowed");
 		if(inp.str("box", "square") != "square") throw RCexception("only the periodic square box is provided");
 		if(inp.integer("external_forces", 0) != 0) throw RCexception("external forces are not provided");

@@ -85,6 +85,15 @@ def test_dry_polar_140_100cells_100_steps():
     _check(a, b, [1, 10, 100], absolute=("s00", "s01"))
 
 
+def test_many_cells_split_epilogue_vs_oracle():
+    """400 cells: the per-cell epilogue runs as its own kernel (one thread per
+    cell); results must still follow the reference's arithmetic."""
+    m = g.make_monolayer(256, 400, seed=12)
+    keys, m2 = case_from_monolayer(m, dict(g.DRY_POLAR, zetaQ_inter=0.1, J_Q=0.2, omega=0.004), seed=13)
+    a, b = _pair(keys, m2, [1, 3])
+    _check(a, b, [1, 3], absolute=("s00", "s01"))
+
+
 @pytest.mark.parametrize("model", ["activenematic", "simplefield"])
 def test_dry_models_vs_oracle(model):
     m = g.make_monolayer(96, 36, seed=2, types=[i % 2 for i in range(36)])
