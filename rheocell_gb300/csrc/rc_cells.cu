@@ -324,21 +324,31 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 	const bool dry = (MODEL == M_NEMATIC) || (MODEL == M_SIMPLE) || pe.friction_cell == 0;
 
 	// Per-cell constant factors of the reference's left-to-right products
-	// (hoisting a leading sub-product leaves every rounding unchanged).
-	const double rlambda = 1.0 / lambda;
+	// (hoisting a leading sub-product leaves every rounding unchanged), formed
+	// once by thread 0: FP64 divisions are expensive on GB300.
+	__shared__ double kd[8];
+	if(threadIdx.x == 0) {
+		kd[0] = 1.0 / lambda;
+		if(MODEL == M_SIMPLE || MODEL == M_NEMATIC) {
+			kd[1] = -4 * mu_c / a0 * (1 - c.area / a0);
+			kd[2] = 4 * kappa / lambda;
+			kd[3] = 0.0;
+			kd[4] = 0.0;
+		}
+		else {
+			kd[1] = -4 * (mu_c / a0) * (1 - c.area / a0);
+			kd[2] = 4 * (kappa / lambda);
+			kd[3] = -mu_c / a0;
+			kd[4] = (gamma / lambda) * 4;
+		}
+		kd[5] = kappa / lambda;
+		kd[6] = 1.0 / pe.friction;
+	}
+	__syncthreads();
+	const double rlambda = kd[0];
 	const double two_lambda = 2 * lambda;
-	double A_c, Rep_c, Ad_c = 0.0, CHd_c = 0.0, gl_c = gamma * lambda;
-	if(MODEL == M_SIMPLE || MODEL == M_NEMATIC) {
-		A_c = -4 * mu_c / a0 * (1 - c.area / a0);
-		Rep_c = 4 * kappa / lambda;
-	}
-	else {
-		A_c = -4 * (mu_c / a0) * (1 - c.area / a0);
-		Rep_c = 4 * (kappa / lambda);
-		Ad_c = -mu_c / a0;
-		CHd_c = (gamma / lambda) * 4;
-	}
-	const double kl_c = kappa / lambda;
+	const double A_c = kd[1], Rep_c = kd[2], Ad_c = kd[3], CHd_c = kd[4], gl_c = gamma * lambda;
+	const double kl_c = kd[5];
 	double perim = 0.0;
 	if(EVAL != EV_NONE) {
 		for(int q = threadIdx.x; q < n; q += blockDim.x) sphi[q] = a.phi_eval[start + q];
@@ -439,7 +449,7 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 	const PhaseParams &pu = a.pu;
 	const double J0 = P.J0, hdt = P.dt * .5;
 	const double zs = pe.zs, zi = pe.zi, fr = pe.friction, alpha = P.passive_alpha;
-	const double rfr = 1.0 / fr;
+	const double rfr = kd[6];
 	const int tb = table_base(lx), tby = table_base(ly);
 
 	for(int q = threadIdx.x; q < n; q += blockDim.x) {
@@ -715,6 +725,28 @@ __device__ __forceinline__ void acc_square(float x, float &s, float &c) {
 // constraint accumulates in double-float (near FP64), the other per-cell
 // sums from FP32 per-thread partials in FP64.  Same stages, expressions and per-cell
 // epilogue as cell_kernel<M_POLAR, ...>; not bitwise the reference.
+// Patch coordinates of q = threadIdx.x, threadIdx.x + blockDim.x, ... without
+// a per-site division: the stride's row and column steps are fixed per cell.
+struct PatchWalk {
+	int q, x, y, sx, sy, lx;
+	__device__ __forceinline__ PatchWalk(int lx_) : lx(lx_) {
+		q = threadIdx.x;
+		y = q / lx;
+		x = q - y * lx;
+		sy = (int) blockDim.x / lx;
+		sx = (int) blockDim.x - sy * lx;
+	}
+	__device__ __forceinline__ void next() {
+		q += blockDim.x;
+		x += sx;
+		y += sy;
+		if(x >= lx) {
+			x -= lx;
+			y += 1;
+		}
+	}
+};
+
 template<int EVAL, int UPD>
 __global__ void __launch_bounds__(CELL_THREADS) cell_kernel_f32(const CellArgs a) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -731,6 +763,19 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel_f32(const CellArgs a
 	const LayerDev lay = a.layers[c.layer];
 	const int n = c.n, lx = c.lx, ly = c.ly, L = lay.L, start = c.start;
 	const double *phi2 = a.phi2 + lay.box_off;
+	const int cx0 = c.corner % L, cy0 = c.corner / L;
+	// box site of patch site (x, y): GetSubIndex without divisions
+	auto site_of = [&](int x, int y) {
+		int px = x + c.offx;
+		if(px >= lx) px -= lx;
+		int py = y + c.offy;
+		if(py >= ly) py -= ly;
+		int bx = cx0 + px;
+		if(bx >= L) bx -= L;
+		int by = cy0 + py;
+		if(by >= L) by -= L;
+		return bx + by * L;
+	};
 	if(n > a.smem_n) {
 		if(threadIdx.x == 0) {
 			atomicOr(&a.st->err, ERR_CAPACITY);
@@ -743,18 +788,43 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel_f32(const CellArgs a
 	float *saux = smu + a.smem_n;
 	const DevParams &P = a.P;
 	const PhaseParams &pe = a.pe;
-	const float gamma = (float) P.gamma, lambda = (float) P.lambda, omega = (float) P.omega;
-	const float rlambda = (float) (1.0 / P.lambda), two_lambda = 2.f * lambda;
-	const float A_c = (float) (-4 * (P.mu / P.a0) * (1 - c.area / P.a0));
-	const float Rep_c = (float) (4 * (P.kappa / P.lambda));
+	// Per-cell constants, formed once by thread 0: on GB300 an FP64 warp
+	// instruction (a division is ~10 of them) costs tens of issue cycles, too
+	// many to repeat in every thread.
+	enum { K_GAMMA, K_LAMBDA, K_OMEGA, K_RLAMBDA, K_AC, K_REPC, K_J0, K_HDT, K_ZS, K_ALPHA, K_RFR, K_Q00, K_Q01, K_BETA,
+	       K_HAS_BETA, K_HAS_OMEGA, K_N };
+	__shared__ float kc[K_N];
+	__shared__ double s_perim;
+	if(threadIdx.x == 0) {
+		kc[K_GAMMA] = (float) P.gamma;
+		kc[K_LAMBDA] = (float) P.lambda;
+		kc[K_OMEGA] = (float) P.omega;
+		kc[K_RLAMBDA] = (float) (1.0 / P.lambda);
+		kc[K_AC] = (float) (-4 * (P.mu / P.a0) * (1 - c.area / P.a0));
+		kc[K_REPC] = (float) (4 * (P.kappa / P.lambda));
+		kc[K_J0] = (float) P.J0;
+		kc[K_HDT] = (float) (P.dt * .5);
+		kc[K_ZS] = (float) pe.zs;
+		kc[K_ALPHA] = (float) P.passive_alpha;
+		kc[K_RFR] = (float) (1.0 / pe.friction);
+		kc[K_Q00] = (float) c.q00;
+		kc[K_Q01] = (float) c.q01;
+		kc[K_HAS_BETA] = pe.beta != 0.0 ? 1.f : 0.f;
+		kc[K_HAS_OMEGA] = P.omega != 0.0 ? 1.f : 0.f;
+	}
+	__syncthreads();
+	const float gamma = kc[K_GAMMA], lambda = kc[K_LAMBDA], omega = kc[K_OMEGA];
+	const float rlambda = kc[K_RLAMBDA], two_lambda = 2.f * lambda;
+	const float A_c = kc[K_AC], Rep_c = kc[K_REPC];
 	double perim = 0.0;
+	const bool has_beta = kc[K_HAS_BETA] != 0.f, has_omega = kc[K_HAS_OMEGA] != 0.f;
 	if(EVAL != EV_NONE) {
 		for(int q = threadIdx.x; q < n; q += blockDim.x) sphi[q] = d2f_int(a.phi_eval[start + q]);
 		__syncthreads();
-		if(pe.beta != 0.0) {
+		if(has_beta) {
 			float pp = 0.f;
-			for(int q = threadIdx.x; q < n; q += blockDim.x) {
-				const int y = q / lx, x = q - y * lx;
+			for(PatchWalk w(lx); w.q < n; w.next()) {
+				const int q = w.q, x = w.x, y = w.y;
 				const Nb nb = patch_nb(q, x, y, lx, ly);
 				const float dx = .5f * (sphi[nb.r] - sphi[nb.l]);
 				const float dy = .5f * (sphi[nb.u] - sphi[nb.d]);
@@ -765,23 +835,28 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel_f32(const CellArgs a
 			__shared__ float s_pp[CELL_THREADS / 32];
 			if((threadIdx.x & 31) == 0) s_pp[threadIdx.x >> 5] = pp;
 			__syncthreads();
-			double t = 0.0;
-			for(int w = 0; w < (int) (blockDim.x >> 5); w++) t += (double) s_pp[w];
-			perim = t;
+			if(threadIdx.x == 0) {
+				double t = 0.0;
+				for(int w = 0; w < (int) (blockDim.x >> 5); w++) t += (double) s_pp[w];
+				s_perim = t;
+				kc[K_BETA] = (float) (4 * (pe.beta / 12.) * (1 - t / 12.));
+			}
+			__syncthreads();
+			perim = s_perim;
 		}
-		const float beta_t = (float) (4 * (pe.beta / 12.) * (1 - perim / 12.));
-		for(int q = threadIdx.x; q < n; q += blockDim.x) {
-			const int y = q / lx, x = q - y * lx;
+		const float beta_t = has_beta ? kc[K_BETA] : 0.f;
+		for(PatchWalk w(lx); w.q < n; w.next()) {
+			const int q = w.q, x = w.x, y = w.y;
 			const Nb nb = patch_nb(q, x, y, lx, ly);
 			const float phi = sphi[q];
 			const float pr = sphi[nb.r], pl = sphi[nb.l], pu_ = sphi[nb.u], pd = sphi[nb.d];
-			const int k = box_site(c, x, y, L);
+			const int k = site_of(x, y);
 			const float p2 = d2f_int(phi2[k]);
 			const float lap = pu_ + pd + pr + pl - 4.f * phi;
 			const float CH = gamma * (8.f * phi * (1.f - phi) * (1.f - 2.f * phi) * rlambda - two_lambda * lap);
 			const float Rep = Rep_c * phi * (p2 - phi * phi);
 			float V = CH + A_c * phi + Rep;
-			if(omega != 0.f) {
+			if(has_omega) {
 				const BoxNb kb = box_nb(k, L);
 				const float ls = (float) (phi2[kb.r] + phi2[kb.u] + phi2[kb.l] + phi2[kb.d] - 4. * phi2[k]);
 				const float dx = .5f * (pr - pl), dy = .5f * (pu_ - pd);
@@ -789,7 +864,13 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel_f32(const CellArgs a
 				const float sup = (ls - lsq) * rsqrtf(1.f + (ls - lsq) * (ls - lsq));
 				V = V + (-4.f * lambda * omega * sup * phi);
 			}
-			if(pe.beta != 0.0) V = V + beta_t * lap;
+			if(has_beta) V = V + beta_t * lap;
+			if(EVAL == EV_STORE) {
+				a.mu[start + q] = f2d_int(V);
+				a.dxg[start + q] = f2d_int(.5f * (pr - pl));
+				a.dyg[start + q] = f2d_int(.5f * (pu_ - pd));
+				a.mapg[start + q] = k;
+			}
 			if(a.rep_on) {
 				const float r = d2f_int(a.rep[start + q]) + Rep;
 				if(a.accumulate_rep) a.rep[start + q] = f2d_int(r);
@@ -808,13 +889,13 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel_f32(const CellArgs a
 	int imin[2] = {lx, ly};
 	float area_s = 0.f, area_c = 0.f;
 	const PhaseParams &pu = a.pu;
-	const float J0 = (float) P.J0, hdt = (float) (P.dt * .5);
-	const float zs = (float) pe.zs, alpha = (float) P.passive_alpha, lam = lambda;
-	const float rfr = (float) (1.0 / pe.friction);
+	const float J0 = kc[K_J0], hdt = kc[K_HDT];
+	const float zs = kc[K_ZS], alpha = kc[K_ALPHA], lam = lambda;
+	const float rfr = kc[K_RFR];
 	const int tb = table_base(lx), tby = table_base(ly);
-	const float q00 = (float) c.q00, q01 = (float) c.q01;
-	for(int q = threadIdx.x; q < n; q += blockDim.x) {
-		const int y = q / lx, x = q - y * lx;
+	const float q00 = kc[K_Q00], q01 = kc[K_Q01];
+	for(PatchWalk w(lx); w.q < n; w.next()) {
+		const int q = w.q, x = w.x, y = w.y;
 		float mu, vx, vy, dx, dy, phi_e = 0.f;
 		if(EVAL != EV_NONE) {
 			const Nb nb = patch_nb(q, x, y, lx, ly);
@@ -837,6 +918,10 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel_f32(const CellArgs a
 			af[11] += fy * phi_e;
 			vx = fx * rfr;
 			vy = fy * rfr;
+			if(EVAL == EV_STORE) {
+				a.vxg[start + q] = f2d_int(vx);
+				a.vyg[start + q] = f2d_int(vy);
+			}
 		}
 		else {
 			mu = d2f_int(a.mu[start + q]);
@@ -845,6 +930,7 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel_f32(const CellArgs a
 			dx = d2f_int(a.dxg[start + q]);
 			dy = d2f_int(a.dyg[start + q]);
 		}
+		if(UPD == UP_NONE) continue;
 		const float dphi = -J0 * mu - vx * dx - vy * dy;
 		float phi_new;
 		if(UPD == UP_PRED) {
@@ -944,6 +1030,7 @@ bool launch_cell_kernel_f32(int eval, int upd, const CellArgs &a, cudaStream_t s
 	if(eval == EV_LOCAL && upd == UP_PRED) cell_kernel_f32<EV_LOCAL, UP_PRED><<<a.N, CELL_THREADS, smem, s>>>(a);
 	else if(eval == EV_LOCAL && upd == UP_CORR) cell_kernel_f32<EV_LOCAL, UP_CORR><<<a.N, CELL_THREADS, smem, s>>>(a);
 	else if(eval == EV_NONE && upd == UP_PRED) cell_kernel_f32<EV_NONE, UP_PRED><<<a.N, CELL_THREADS, smem, s>>>(a);
+	else if(eval == EV_STORE && upd == UP_NONE) cell_kernel_f32<EV_STORE, UP_NONE><<<a.N, CELL_THREADS, smem, s>>>(a);
 	else return false;
 	return true;
 }
@@ -957,6 +1044,9 @@ static cudaError_t configure_f32() {
 	   cudaSuccess)
 		e = c;
 	if((c = cudaFuncSetAttribute(cell_kernel_f32<EV_NONE, UP_PRED>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)) !=
+	   cudaSuccess)
+		e = c;
+	if((c = cudaFuncSetAttribute(cell_kernel_f32<EV_STORE, UP_NONE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)) !=
 	   cudaSuccess)
 		e = c;
 	return e;
@@ -1010,6 +1100,7 @@ void launch_cell_finish(int model, int eval, int upd, bool f32, const CellArgs &
 		const int g = (a.N + 127) / 128;
 		if(eval == EV_LOCAL && upd == UP_PRED) cell_finish_kernel<M_POLAR, EV_LOCAL, UP_PRED, true><<<g, 128, 0, s>>>(a);
 		else if(eval == EV_LOCAL && upd == UP_CORR) cell_finish_kernel<M_POLAR, EV_LOCAL, UP_CORR, true><<<g, 128, 0, s>>>(a);
+		else if(eval == EV_STORE && upd == UP_NONE) cell_finish_kernel<M_POLAR, EV_STORE, UP_NONE, true><<<g, 128, 0, s>>>(a);
 		else cell_finish_kernel<M_POLAR, EV_NONE, UP_PRED, true><<<g, 128, 0, s>>>(a);
 		return;
 	}
