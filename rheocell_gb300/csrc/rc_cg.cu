@@ -91,30 +91,21 @@ __device__ __forceinline__ bool grid_reduce(const CGArgs &a, CGShared &sh, int n
 	}
 	__syncthreads();
 	if(nv > 0) {
-		const double *part = a.partials + (size_t) ((sh.epoch - 1u) & 1u) * 8 * nb;
-		double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+		// one warp: lane l sums partials l, l + 32, ... in order, then a fixed
+		// shuffle tree (FP64 warp instructions are expensive on GB300: no
+		// other warp repeats this work)
+		if(threadIdx.x < 32) {
+			const double *part = a.partials + (size_t) ((sh.epoch - 1u) & 1u) * 8 * nb;
+			const int lane = threadIdx.x;
 #pragma unroll
-		for(int i = 0; i < 8; i++)
-			if(i < nv)
-				for(unsigned b = threadIdx.x; b < nb; b += blockDim.x) acc[i] += ldcg(&part[(size_t) i * nb + b]);
-		if(nv <= 2) {
-			double t[2] = {acc[0], acc[1]};
-			block_sum<2>(t, sh.red);
-			acc[0] = t[0];
-			acc[1] = t[1];
-		}
-		else if(nv <= 4) {
-			double t[4] = {acc[0], acc[1], acc[2], acc[3]};
-			block_sum<4>(t, sh.red);
+			for(int i = 0; i < 8; i++) {
+				if(i >= nv) break;
+				double t = 0.0;
+				for(unsigned b = lane; b < nb; b += 32) t += ldcg(&part[(size_t) i * nb + b]);
 #pragma unroll
-			for(int i = 0; i < 4; i++) acc[i] = t[i];
-		}
-		else
-			block_sum<8>(acc, sh.red);
-		if(threadIdx.x == 0) {
-#pragma unroll
-			for(int i = 0; i < 8; i++)
-				if(i < nv) sh.tot[i] = acc[i];
+				for(int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+				if(lane == 0) sh.tot[i] = t;
+			}
 		}
 		__syncthreads();
 	}
@@ -383,8 +374,91 @@ __device__ __forceinline__ const float *tab_iT<float>(const CGShared &sh) { retu
 
 // Phase A: p = z + beta p (p = z on the first sweep, z = r / diag), box sums
 // P = S p, one thread per cover entry; P is zero on entry (cleared in phase C).
+// FP64 phase A by box site: thread k walks its cover list in order, updates
+// p there and stores P[k] (every site written, so P needs no clearing).  All
+// unknowns at k share D(k): one table lookup per site, one FP64 add per entry.
+__device__ __forceinline__ bool cg_phase_a_sites(const CGArgs &a, CGShared &sh, const CGVecs<double> &V) {
+	const int L = a.L;
+	const long long L2 = (long long) L * L;
+	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+	const long long gstride = (long long) gridDim.x * blockDim.x;
+	const int ax = sh.act[0], ay = sh.act[1], first = sh.first;
+	const double bx = sh.beta[0], by = sh.beta[1];
+	const double *rx = V.rx, *ry = V.ry;
+	double *px = V.px, *py = V.py, *Pbx = V.Pbx, *Pby = V.Pby;
+	const int *cov_idx = a.cov_idx, *cov_off = a.cov_off, *cnt = a.cnt;
+	for(long long k = gtid; k < L2; k += gstride) {
+		const int e0 = cov_off[k], e1 = cov_off[k + 1];
+		double sx = 0.0, sy = 0.0;
+		if(e1 > e0) {
+			const double id = sh.iT[box_deg(cnt, (int) k, L)];
+			for(int e = e0; e < e1; e++) {
+				const int j = cov_idx[e];
+				if(ax) {
+					const double z = id * rx[j];
+					const double p = first ? z : __fma_rn(bx, px[j], z);
+					px[j] = p;
+					sx += p;
+				}
+				if(ay) {
+					const double z = id * ry[j];
+					const double p = first ? z : __fma_rn(by, py[j], z);
+					py[j] = p;
+					sy += p;
+				}
+			}
+		}
+		if(ax) Pbx[k] = sx;
+		if(ay) Pby[k] = sy;
+	}
+	return grid_reduce(a, sh, 0, nullptr);
+}
+
+// FP64 phase B by box site: the four-neighbour sum of P and the diagonal once
+// per site, then Ap and p.Ap for its unknowns.
+__device__ __forceinline__ bool cg_phase_b_sites(const CGArgs &a, CGShared &sh, const CGVecs<double> &V) {
+	const int L = a.L;
+	const long long L2 = (long long) L * L;
+	const double neta = -a.eta * 1.0;
+	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+	const long long gstride = (long long) gridDim.x * blockDim.x;
+	const int ax = sh.act[0], ay = sh.act[1];
+	const double *px = V.px, *py = V.py, *Pbx = V.Pbx, *Pby = V.Pby;
+	double *apx = V.apx, *apy = V.apy;
+	const int *cov_idx = a.cov_idx, *cov_off = a.cov_off, *cnt = a.cnt;
+	double w0 = 0.0, w1 = 0.0;
+	for(long long k = gtid; k < L2; k += gstride) {
+		const int e0 = cov_off[k], e1 = cov_off[k + 1];
+		if(e1 == e0) continue;
+		const double d = sh.T[box_deg(cnt, (int) k, L)];
+		const double qx = ax ? neta * box_n4T<double>(Pbx, (int) k, L) : 0.0;
+		const double qy = ay ? neta * box_n4T<double>(Pby, (int) k, L) : 0.0;
+		for(int e = e0; e < e1; e++) {
+			const int j = cov_idx[e];
+			if(ax) {
+				const double p = px[j];
+				const double ap = __fma_rn(d, p, qx);
+				apx[j] = ap;
+				w0 = __fma_rn(p, ap, w0);
+			}
+			if(ay) {
+				const double p = py[j];
+				const double ap = __fma_rn(d, p, qy);
+				apy[j] = ap;
+				w1 = __fma_rn(p, ap, w1);
+			}
+		}
+	}
+	double w[2] = {w0, w1};
+	warp_tree<double, 2>(w);
+	double v[2] = {w[0], w[1]};
+	block_sum_warps<2>(v, sh.red);
+	return grid_reduce(a, sh, 2, v);
+}
+
 template<typename T>
 __device__ __forceinline__ bool cg_phase_a(const CGArgs &a, CGShared &sh, const CGVecs<T> &V) {
+	if constexpr(sizeof(T) == sizeof(double)) return cg_phase_a_sites(a, sh, V);
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
 	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
@@ -431,6 +505,7 @@ __device__ __forceinline__ bool cg_phase_a(const CGArgs &a, CGShared &sh, const 
 // Phase B: Ap (stored) and p.Ap into sh.tot[0..1].
 template<typename T>
 __device__ __forceinline__ bool cg_phase_b(const CGArgs &a, CGShared &sh, const CGVecs<T> &V) {
+	if constexpr(sizeof(T) == sizeof(double)) return cg_phase_b_sites(a, sh, V);
 	const int L = a.L;
 	const long long S = a.st->S;
 	const T neta = (T) (-a.eta * 1.0);
@@ -499,9 +574,12 @@ __device__ __forceinline__ bool cg_phase_c(const CGArgs &a, CGShared &sh, const 
 		}
 	}
 	double v[4] = {(double) w[0], (double) w[1], (double) w[2], (double) w[3]};
-	for(long long k = gtid; k < L2; k += gstride) {
-		Pbx[k] = (T) 0;
-		Pby[k] = (T) 0;
+	if constexpr(sizeof(T) != sizeof(double)) {
+		// the FP32 phase A accumulates into P with atomics: clear it
+		for(long long k = gtid; k < L2; k += gstride) {
+			Pbx[k] = (T) 0;
+			Pby[k] = (T) 0;
+		}
 	}
 	block_sum<4>(v, sh.red);
 	return grid_reduce(a, sh, 4, v);
