@@ -362,6 +362,32 @@ int rc_set_solver(rc_engine *e, int solver);
  */
 int rc_solver_profile(rc_engine *e, int enable, double *ms, int n);
 
+/*
+ * Diagnostic observables computed on the device from the current state.
+ *
+ * rc_observe_field: the box fields of the reference's field observables --
+ * RC_OBS_VELOCITY (VelocityField::calc_field, src/Observables/
+ * VelocityField.cpp:69-78: sum of v * phi), RC_OBS_SHAPE (ShapeField.cpp:
+ * 69-78: S00 * phi, S01 * phi) and RC_OBS_NEMATIC (NematicField.cpp:69-78:
+ * Q00 * phi, Q01 * phi) -- summed over the cells of monolayer `layer` (of
+ * type only_type; -1: all) in index order, into fx, fy (L*L each, row-major
+ * box sites).  With size_grid > 0 also the coarse-grained fields
+ * (VelocityField.cpp:105-121) into coarse_x, coarse_y (may be NULL).
+ *
+ * rc_observe_cells: per cell (6 doubles each, cell order): unwrapped centre
+ * of mass x, y; area; elongation |S|; aspect ratio sqrt(s1/s2) - 1;
+ * orientation atan2(S01, S00)/2 -- from the current gradients, as
+ * scripts/calcAvgShape.py:274-336 forms them; and per monolayer (4 doubles
+ * each): mean area, area variance, mean elongation, mean aspect ratio.
+ * Either pointer may be NULL.
+ */
+#define RC_OBS_VELOCITY 0
+#define RC_OBS_SHAPE 1
+#define RC_OBS_NEMATIC 2
+int rc_observe_field(rc_engine *e, int kind, int layer, int only_type, int size_grid, double *fx, double *fy,
+                     double *coarse_x, double *coarse_y);
+int rc_observe_cells(rc_engine *e, double *cell_obs, double *layer_obs);
+
 /* Sites (sum of LsubX*LsubY) in the current configuration. */
 long long rc_site_count(const rc_engine *e);
 

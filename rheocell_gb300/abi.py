@@ -23,6 +23,9 @@ RC_UNET_PARAMS = 25937
 RC_SOLVER_PLAIN = 0
 RC_SOLVER_LEARNED = 1
 RC_SOLVER_LEARNED_FP32 = 2
+RC_OBS_VELOCITY = 0
+RC_OBS_SHAPE = 1
+RC_OBS_NEMATIC = 2
 SOLVER_PHASES = ["input_gather", "first_layer", "tc_level0", "tc_level1", "tc_level2", "last_layer",
                  "precond_residual", "fcg_A", "fcg_B", "fcg_C", "other",
                  "tc_weights", "tc_staging", "tc_mma", "tc_epilogue"]
@@ -161,6 +164,10 @@ def declare(lib: C.CDLL, prefix: str) -> C.CDLL:
         lib.rc_learned_get_params.restype = C.c_int
         lib.rc_learned_set_params.argtypes = [vp, DP]
         lib.rc_learned_set_params.restype = C.c_int
+        lib.rc_observe_field.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, DP, DP, DP, DP]
+        lib.rc_observe_field.restype = C.c_int
+        lib.rc_observe_cells.argtypes = [vp, DP, DP]
+        lib.rc_observe_cells.restype = C.c_int
         lib.rc_solver_profile.argtypes = [vp, C.c_int, DP, C.c_int]
         lib.rc_solver_profile.restype = C.c_int
         lib.rc_set_solver.argtypes = [vp, C.c_int]
@@ -184,7 +191,8 @@ def declare(lib: C.CDLL, prefix: str) -> C.CDLL:
 # Every symbol the header declares (checked by the CPU test suite).
 EXPORTED = ["rc_abi_version", "rc_create", "rc_batch_create", "rc_layer_count", "rc_viscous_resolve_noalloc", "rc_unet_loss_grad", "rc_unet_forward_tc",
             "rc_learned_harvest", "rc_learned_harvested", "rc_learned_train", "rc_learned_get_params",
-            "rc_learned_set_params", "rc_set_solver", "rc_solver_profile", "rc_step", "rc_step_async", "rc_wait", "rc_set_phase",
+            "rc_learned_set_params", "rc_set_solver", "rc_solver_profile",
+            "rc_observe_field", "rc_observe_cells", "rc_step", "rc_step_async", "rc_wait", "rc_set_phase",
             "rc_get_sizes", "rc_download", "rc_upload", "rc_download_phi", "rc_upload_phi", "rc_set_stream",
             "rc_set_timing", "rc_timers", "rc_site_count", "rc_last_error", "rc_destroy"]
 

@@ -124,6 +124,8 @@ struct rc_engine {
 	bool harv_collect = false;
 	unsigned long long *phase_ns = nullptr;  // diagnostic solve phase timers (null: off)
 	bool phase_on = false;
+	double *obs_buf = nullptr;               // diagnostic observables scratch
+	size_t obs_cap = 0;
 };
 
 static cudaEvent_t get_event(rc_engine *e) {
@@ -1356,6 +1358,62 @@ int rc_solver_profile(rc_engine *e, int enable, double *ms, int n) {
 	if((enable != 0) != e->phase_on) drop_graphs(e);
 	if(enable) CUDA_TRY(e, cudaMemset(e->phase_ns, 0, sizeof(unsigned long long) * 32));
 	e->phase_on = enable != 0;
+	return RC_OK;
+}
+
+// --- diagnostic observables ---------------------------------------------------
+
+static int obs_scratch(rc_engine *e, size_t n) {
+	if(e->obs_cap >= n) return RC_OK;
+	dfree(e, e->obs_buf);
+	e->obs_buf = nullptr;
+	e->obs_cap = 0;
+	int rc;
+	if((rc = dalloc(e, &e->obs_buf, n))) return rc;
+	e->obs_cap = n;
+	return RC_OK;
+}
+
+int rc_observe_field(rc_engine *e, int kind, int layer, int only_type, int size_grid, double *fx, double *fy,
+                     double *coarse_x, double *coarse_y) {
+	if(!e || !fx || !fy) return RC_ERR_INVALID;
+	if(kind < RC_OBS_VELOCITY || kind > RC_OBS_NEMATIC) return set_err(e, RC_ERR_INVALID, "rc_observe_field: kind %d", kind);
+	if(layer < 0 || layer >= e->n_layers) return set_err(e, RC_ERR_INVALID, "rc_observe_field: layer %d", layer);
+	CUDA_TRY(e, cudaSetDevice(e->device));
+	const LayerDev &lay = e->layers_h[(size_t) layer];
+	const size_t L2 = (size_t) lay.L * lay.L;
+	int rc;
+	if((rc = obs_scratch(e, 4 * L2))) return rc;
+	materialise(e, 0);  // current velocities (dry models)
+	double *f0 = e->obs_buf, *f1 = f0 + L2, *c0 = f1 + L2, *c1 = c0 + L2;
+	launch_obs_field(e->cells, e->layers, lay, e->bin_count, e->bin_cells, e->phiA, e->vx, e->vy, kind, layer, only_type,
+	                 f0, f1, e->stream);
+	if(size_grid > 0) {
+		launch_obs_coarse(f0, c0, lay.L, size_grid, e->stream);
+		launch_obs_coarse(f1, c1, lay.L, size_grid, e->stream);
+	}
+	CUDA_TRY(e, cudaGetLastError());
+	CUDA_TRY(e, cudaMemcpyAsync(fx, f0, sizeof(double) * L2, cudaMemcpyDeviceToHost, e->stream));
+	CUDA_TRY(e, cudaMemcpyAsync(fy, f1, sizeof(double) * L2, cudaMemcpyDeviceToHost, e->stream));
+	if(size_grid > 0 && coarse_x) CUDA_TRY(e, cudaMemcpyAsync(coarse_x, c0, sizeof(double) * L2, cudaMemcpyDeviceToHost, e->stream));
+	if(size_grid > 0 && coarse_y) CUDA_TRY(e, cudaMemcpyAsync(coarse_y, c1, sizeof(double) * L2, cudaMemcpyDeviceToHost, e->stream));
+	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+	return RC_OK;
+}
+
+int rc_observe_cells(rc_engine *e, double *cell_obs, double *layer_obs) {
+	if(!e) return RC_ERR_INVALID;
+	CUDA_TRY(e, cudaSetDevice(e->device));
+	const size_t nc = (size_t) std::max(e->N, 1), nl = (size_t) e->n_layers;
+	int rc;
+	if((rc = obs_scratch(e, 6 * nc + 4 * nl))) return rc;
+	materialise(e, 0);  // current gradients (dry models)
+	double *co = e->obs_buf, *lo = co + 6 * nc;
+	launch_obs_cells(e->cells, e->layers, e->N, e->n_layers, e->dxg, e->dyg, co, lo, e->stream);
+	CUDA_TRY(e, cudaGetLastError());
+	if(cell_obs && e->N) CUDA_TRY(e, cudaMemcpyAsync(cell_obs, co, sizeof(double) * 6 * (size_t) e->N, cudaMemcpyDeviceToHost, e->stream));
+	if(layer_obs) CUDA_TRY(e, cudaMemcpyAsync(layer_obs, lo, sizeof(double) * 4 * nl, cudaMemcpyDeviceToHost, e->stream));
+	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
 	return RC_OK;
 }
 

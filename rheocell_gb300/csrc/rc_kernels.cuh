@@ -118,6 +118,13 @@ void launch_bins(CellDev *cells, const LayerDev *layers, int N, int *bin_count, 
 void launch_repack(CellArgs a, double *scratch_phi, double *scratch_rep, long long cap, cudaStream_t s);
 void launch_box_gather(const BoxArgs &a, cudaStream_t s);
 int cg_grid_blocks(int device, bool learned);
+// diagnostic observables (rc_obs.cu)
+void launch_obs_field(const CellDev *cells, const LayerDev *layers, const LayerDev &lay_h, const int *bin_count,
+                      const int *bin_cells, const double *phi, const double *vx, const double *vy, int kind, int layer,
+                      int only_type, double *fx, double *fy, cudaStream_t s);
+void launch_obs_coarse(const double *f, double *out, int L, int sg, cudaStream_t s);
+void launch_obs_cells(const CellDev *cells, const LayerDev *layers, int N, int n_layers, const double *dxg,
+                      const double *dyg, double *cell_obs, double *layer_obs, cudaStream_t s);
 cudaError_t launch_cg(const CGArgs &a, int blocks, cudaStream_t s);
 
 }  // namespace rc
