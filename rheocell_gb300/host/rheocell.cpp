@@ -17,11 +17,28 @@
 //                       and Configuration::headers/field (Observables/Configuration.cpp:36-56)
 //   output ............ trajectory (appended), last_conf (overwritten),
 //                       equilibrated_conf (ObservableOutput.cpp:86-190,
-//                       SimBackend.cpp:398-410)
+//                       SimBackend.cpp:398-410); the I/O-rate limit max_io
+//                       (SimBackend.cpp:157-166, 366-376)
+//
+// Output runs on a writer thread: at a print point the state is downloaded
+// into a host snapshot, the snapshot is queued, and stepping continues while
+// the thread formats and writes it (at most two snapshots in flight).
+//
+// Extra keys (not read by the reference): backend_precision = float (dry
+// polar model), CUDA_device, and the learned preconditioner of the wet
+// models' viscous solve -- cg_solver = learned with learned_harvest_steps
+// (plain-CG steps that collect training samples, default 40),
+// learned_train_epochs (default 20), learned_params_file (parameters to load
+// instead of training, or to save after training).
 #include "../../include/rheocell_gb300.h"
 
+#include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <csignal>
+#include <deque>
+#include <mutex>
+#include <thread>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -32,6 +49,7 @@
 #include <stdexcept>
 #include <string>
 #include <vector>
+#include <atomic>
 
 namespace {
 
@@ -182,6 +200,60 @@ public:
 		if(inp.integer("confs_to_skip", 0) != 0) throw RCexception("confs_to_skip is not provided");
 		restart_step_counter_ = inp.boolean("restart_step_counter", false);
 		device_ = (int) inp.integer("CUDA_device", 0);
+		const std::string solver = inp.str("cg_solver", "plain");
+		if(solver != "plain" && solver != "learned") throw RCexception("cg_solver '" + solver + "' is not provided");
+		learned_ = solver == "learned";
+		if(learned_ && !wet) throw RCexception("cg_solver = learned needs a wet model (friction_cell != 0)");
+		harvest_steps_ = inp.integer("learned_harvest_steps", 40);
+		train_epochs_ = (int) inp.integer("learned_train_epochs", 20);
+		params_file_ = inp.str("learned_params_file", "");
+	}
+
+	bool learned() const { return learned_; }
+	long long harvest_steps() const { return harvest_steps_; }
+
+	// Learned solver: parameters from learned_params_file when it exists,
+	// otherwise harvesting during the first learned_harvest_steps steps.
+	// Returns true when harvesting was started.
+	bool start_learned() {
+		if(!params_file_.empty()) {
+			std::ifstream f(params_file_);
+			if(f.good()) {
+				std::vector<double> p(RC_UNET_PARAMS);
+				for(auto &v : p)
+					if(!(f >> v)) throw RCexception("learned_params_file " + params_file_ + ": too few values");
+				check(rc_learned_set_params(engine_, p.data()));
+				check(rc_set_solver(engine_, RC_SOLVER_LEARNED));
+				fprintf(stderr, "INFO: learned preconditioner parameters read from %s\n", params_file_.c_str());
+				return false;
+			}
+		}
+		check(rc_learned_harvest(engine_, 4000, 3, 6));
+		return true;
+	}
+
+	void finish_learned() {
+		rc_train_options o = {};
+		o.epochs = train_epochs_;
+		o.batch = 8;
+		o.learning_rate = 2e-3;
+		o.learning_rate_final = 1e-4;
+		o.validation = 0.1;
+		o.seed = 1;
+		o.init = 1;
+		rc_train_report r = {};
+		check(rc_learned_train(engine_, &o, &r));
+		check(rc_learned_harvest(engine_, 0, 0, 0));
+		check(rc_set_solver(engine_, RC_SOLVER_LEARNED));
+		fprintf(stderr, "INFO: learned preconditioner trained on %d samples in %.1f s, validation loss %.4g -> %.4g\n",
+		        r.samples, r.ms * 1e-3, r.validation_loss_init, r.validation_loss);
+		if(!params_file_.empty()) {
+			std::vector<double> p(RC_UNET_PARAMS);
+			check(rc_learned_get_params(engine_, p.data()));
+			std::ofstream f(params_file_);
+			f.precision(17);
+			for(double v : p) f << v << "\n";
+		}
 	}
 
 	// SimBackend::init + FD_CPUBackend::init
@@ -232,22 +304,45 @@ public:
 		}
 	}
 
-	std::string configuration(long long step) const {
+	// host snapshot of the configuration (Configuration::headers/field)
+	struct Snapshot {
+		long long step;
+		int L;
+		std::vector<rc_cell_host> h;
+		std::vector<std::vector<double>> phi;
+		std::vector<std::vector<int>> map;
+	};
+
+	Snapshot snapshot(long long step) const {
+		Snapshot sn;
+		sn.step = step;
+		sn.L = L_;
+		for(const auto &f : fields_) {
+			sn.h.push_back(f.h);
+			sn.phi.push_back(f.phi);
+			sn.map.push_back(f.map);
+		}
+		return sn;
+	}
+
+	static std::string format(const Snapshot &sn) {
 		std::stringstream conf;
 		conf.precision(15);
-		conf << "t = " << step << std::endl;
-		conf << "b = " << L_ << " " << L_ << std::endl;
-		for(size_t i = 0; i < fields_.size(); i++) {
-			const rc_cell_host &h = fields_[i].h;
+		conf << "t = " << sn.step << std::endl;
+		conf << "b = " << sn.L << " " << sn.L << std::endl;
+		for(size_t i = 0; i < sn.h.size(); i++) {
+			const rc_cell_host &h = sn.h[i];
 			if(i > 0) conf << std::endl;
 			conf << h.lsub_x << " " << h.lsub_y << " " << h.com_x << " " << h.com_y << " " << h.offset_x << " "
 			     << h.offset_y << " " << h.corner << " " << h.unrap_x << " " << h.unrap_y << " " << h.q00 << " "
 			     << h.q01 << " ";
-			for(size_t q = 0; q < fields_[i].phi.size(); q++) conf << fields_[i].map[q] << " " << fields_[i].phi[q] << " ";
+			for(size_t q = 0; q < sn.phi[i].size(); q++) conf << sn.map[i][q] << " " << sn.phi[i][q] << " ";
 		}
 		conf << std::endl;
 		return conf.str();
 	}
+
+	std::string configuration(long long step) const { return format(snapshot(step)); }
 
 	long long start_step() const { return restart_step_counter_ ? 0 : conf_step_; }
 	const rc_step_stats &stats() const { return stats_; }
@@ -347,6 +442,10 @@ private:
 	long long conf_step_ = 0;
 	bool restart_step_counter_ = false;
 	int device_ = 0;
+	bool learned_ = false;
+	long long harvest_steps_ = 40;
+	int train_epochs_ = 20;
+	std::string params_file_;
 };
 
 void write_file(const std::string &path, const std::string &text, bool append) {
@@ -354,6 +453,77 @@ void write_file(const std::string &path, const std::string &text, bool append) {
 	if(!f.good()) throw RCexception("Stream " + path + " not writable");
 	f << text;
 }
+
+// Formats and writes configuration snapshots in order on its own thread
+// (trajectory appended, last_conf overwritten); at most two snapshots wait.
+class ConfWriter {
+public:
+	ConfWriter(std::string traj, std::string last) : traj_(std::move(traj)), last_(std::move(last)) {
+		th_ = std::thread([this] { run(); });
+	}
+	~ConfWriter() { close(); }
+
+	void push(FD_CUDABackend::Snapshot &&sn) {
+		std::unique_lock<std::mutex> lk(mu_);
+		cv_.wait(lk, [this] { return q_.size() < 2 || !err_.empty(); });
+		if(!err_.empty()) throw RCexception(err_);
+		q_.push_back(std::move(sn));
+		cv_.notify_all();
+	}
+
+	// waits for the queue to drain; rethrows a writer error
+	void close() {
+		{
+			std::unique_lock<std::mutex> lk(mu_);
+			done_ = true;
+			cv_.notify_all();
+		}
+		if(th_.joinable()) th_.join();
+		if(!err_.empty()) {
+			std::string e = err_;
+			err_.clear();
+			throw RCexception(e);
+		}
+	}
+
+	long long bytes() const { return bytes_.load(); }
+
+private:
+	void run() {
+		while(true) {
+			FD_CUDABackend::Snapshot sn;
+			{
+				std::unique_lock<std::mutex> lk(mu_);
+				cv_.wait(lk, [this] { return !q_.empty() || done_; });
+				if(q_.empty()) return;
+				sn = std::move(q_.front());
+				q_.pop_front();
+				cv_.notify_all();
+			}
+			try {
+				const std::string c = FD_CUDABackend::format(sn);
+				write_file(traj_, c, true);
+				write_file(last_, c, false);
+				bytes_ += (long long) c.size();
+			}
+			catch(std::exception &e) {
+				std::unique_lock<std::mutex> lk(mu_);
+				err_ = e.what();
+				cv_.notify_all();
+				return;
+			}
+		}
+	}
+
+	std::string traj_, last_;
+	std::thread th_;
+	std::mutex mu_;
+	std::condition_variable cv_;
+	std::deque<FD_CUDABackend::Snapshot> q_;
+	bool done_ = false;
+	std::string err_;
+	std::atomic<long long> bytes_{0};
+};
 
 }  // namespace
 
@@ -378,6 +548,11 @@ int main(int argc, char *argv[]) {
 		const std::string traj = input.str("trajectory_file", "", true);
 		const std::string last_conf = input.str("lastconf_file", "last_conf.dat");
 		const std::string eq_conf = input.str("equilibratedconf_file", "equilibrated_conf.dat");
+		double max_io = 1.0;  // MB/s, the reference's default
+		if(input.has("max_io")) {
+			max_io = input.num("max_io");
+			if(max_io < 0) throw RCexception("Cannot run with a negative I/O limit. Set the max_io key to something > 0");
+		}
 
 		// SimManager::init
 		srand48(seed);
@@ -396,30 +571,45 @@ int main(int argc, char *argv[]) {
 		backend.apply_simulation_data_changes();
 		write_file(eq_conf, backend.configuration(cur), false);
 		backend.apply_simulation_changes_after_equilibration();
+		long long learn_at = -1;  // main-loop step at which the network is trained
+		if(backend.learned() && backend.start_learned()) learn_at = backend.harvest_steps();
+		const auto t_start = std::chrono::steady_clock::now();
+		ConfWriter writer(traj, last_conf);
+		auto print = [&]() {
+			backend.apply_simulation_data_changes();
+			writer.push(backend.snapshot(cur));
+			// SimBackend::print_observables: data-rate limit after 30 s
+			const double t = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+			if(t > 30) {
+				const double MBps = ((double) writer.bytes() / (1024. * 1024.)) / t;
+				if(MBps > max_io) {
+					char msg[512];
+					snprintf(msg, sizeof(msg),
+					         "Aborting because the program is generating too much data (%g MB/s).\n\t\t\tThe current "
+					         "limit is set to %g MB/s;\n\t\t\tyou can change it by setting max_io=<float> in the input "
+					         "file.",
+					         MBps, max_io);
+					throw RCexception(msg);
+				}
+			}
+		};
 		long long run = 0;
 		while(run < steps && !g_stop) {
 			if(cur == next_print) {
-				if(run > 0) {
-					backend.apply_simulation_data_changes();
-					const std::string c = backend.configuration(cur);
-					write_file(traj, c, true);
-					write_file(last_conf, c, false);
-				}
+				if(run > 0) print();
 				next_print += interval;
 			}
-			// advance to the next print point in one call
+			// advance to the next print point (or the training point) in one call
 			long long chunk = std::min(steps - run, next_print - cur);
+			if(learn_at > run) chunk = std::min(chunk, learn_at - run);
 			if(chunk < 1) chunk = 1;
 			backend.sim_steps((int) chunk);
 			cur += chunk;
 			run += chunk;
+			if(run == learn_at) backend.finish_learned();
 		}
-		if(cur == next_print && run > 0) {
-			backend.apply_simulation_data_changes();
-			const std::string c = backend.configuration(cur);
-			write_file(traj, c, true);
-			write_file(last_conf, c, false);
-		}
+		if(cur == next_print && run > 0) print();
+		writer.close();
 		backend.apply_simulation_data_changes();
 		write_file(last_conf, backend.configuration(cur), false);
 		fprintf(stderr, "INFO: END OF THE SIMULATION, everything went OK! (%lld steps)\n", run);

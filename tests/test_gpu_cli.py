@@ -70,3 +70,25 @@ def test_cli_reports_reference_errors(tmp_path):
     build.build()
     res = subprocess.run([build.CLI, "input"], cwd=str(tmp_path), capture_output=True, text=True, timeout=120)
     assert res.returncode != 0 and "not provided" in res.stderr
+
+
+def test_cli_learned_solver_trains_then_reuses_parameters(tmp_path):
+    """cg_solver = learned: harvest during the first steps, train, switch,
+    save the parameters; a second run loads them instead of training."""
+    from rheocell_gb300 import generator as g
+    m = g.make_monolayer(64, 16, seed=31)
+    params = dict(g.WET_NEMATIC, zetaQ_inter=0.02)
+    g.write_case(str(tmp_path), m, params, steps=30, seed=32,
+                 extra=dict(cg_solver="learned", learned_harvest_steps=10, learned_train_epochs=5,
+                            learned_params_file="unet.txt", max_io=1e9, print_conf_interval=10))
+    build.build()
+    res = subprocess.run([build.CLI, "input"], cwd=str(tmp_path), capture_output=True, text=True, timeout=600)
+    assert res.returncode == 0, res.stderr[-2000:]
+    assert "trained on" in res.stderr
+    vals = (tmp_path / "unet.txt").read_text().split()
+    assert len(vals) == 25937
+    confs = parse_confs((tmp_path / "trajectory.dat").read_text())
+    assert [c[0] for c in confs] == [10, 20, 30]
+    res2 = subprocess.run([build.CLI, "input"], cwd=str(tmp_path), capture_output=True, text=True, timeout=600)
+    assert res2.returncode == 0, res2.stderr[-2000:]
+    assert "read from unet.txt" in res2.stderr
