@@ -10,7 +10,7 @@ A "step" is one FD_CPUBackend::sim_step (Heun predictor + corrector, two
 force evaluations, four viscous solves).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--workload wet256|dry140|ensemble64] [--precision double|mixed]
+                  [--workload wet256|wet512|wet1024|dry140|ensemble64] [--precision double|mixed]
 
 Prints one JSON line (rank 0).  `value` is site-updates/s over all ranks with
 the state resident on the device, timed with CUDA events per step on the
@@ -43,6 +43,13 @@ def workload(name):
     if name == "wet256":
         return dict(name="wet MPF 256x256, 400 cells, R=8, 41x41 patches, wetmodel xi=eta=1, CG rtol 1e-8",
                     L=256, n=400, params=g.WET_NEMATIC, seed=1)
+    if name == "wet512":
+        return dict(name="wet MPF 512x512, 1600 cells, R=8, 41x41 patches, wetmodel nematic zeta=0.05, xi=eta=1, "
+                         "CG rtol 1e-8", L=512, n=1600, params=g.WET_NEMATIC, seed=1)
+    if name == "wet1024":
+        return dict(name="wet MPF 1024x1024, 6400 cells, R=8, 41x41 patches, wetmodel nematic zeta=0.05, xi=eta=1, "
+                         "CG rtol 1e-8 (polar+nematic activity has no single reference model)",
+                    L=1024, n=6400, params=g.WET_NEMATIC, seed=1)
     if name == "dry140":
         return dict(name="dry polar MPF 140x140, 100 cells, R=8, 41x41 patches, wetpolarmodel friction_cell=0",
                     L=140, n=100, params=g.DRY_POLAR, seed=1)
@@ -185,7 +192,7 @@ def prepare_learned(args, eng, lib):
     n = eng.harvested()
     eng.harvest(args.harvest_capacity, 3, 0)  # stop collecting, keep the samples
     rep = eng.train(epochs=args.train_epochs, batch=8, learning_rate=args.train_lr, seed=1,
-                    learning_rate_final=args.train_lr * args.train_lr_final)
+                    learning_rate_final=args.train_lr * args.train_lr_final, max_samples=args.train_max_samples)
     k = max(2, min(args.steps, 10))
     plain_ms, plain_it, plain_res = solve_stage(eng, lib, k, flush)
     eng.set_solver(abi.RC_SOLVER_LEARNED)
@@ -318,7 +325,10 @@ def run_gb300(args, rank, world):
         unit_desc = "per-cell update kernel: 36 B/site per launch"
     achieved = bytes_launch / dom_avg_s / 1e9
     traffic = None
-    prof = os.path.join(ROOT, "profiles", "traffic_%s.json" % args.workload)
+    # DRAM bytes per launch of the dominant kernel from an ncu capture of the
+    # same workload, precision and solver (profiles/), when one was taken
+    prof = os.path.join(ROOT, "profiles", "traffic_%s_%s%s.json" % (args.workload, args.precision,
+                                                                 "_learned" if args.solver == "learned" else ""))
     if os.path.exists(prof):
         try:
             traffic = json.load(open(prof)).get(names[dom])
@@ -485,7 +495,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="wet256", choices=["wet256", "dry140", "ensemble64"])
+    ap.add_argument("--workload", default="wet256", choices=["wet256", "wet512", "wet1024", "dry140", "ensemble64"])
     ap.add_argument("--precision", default="double", choices=["double", "mixed", "float"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--solver", default="plain", choices=["plain", "learned"])
@@ -493,6 +503,7 @@ def main():
     ap.add_argument("--harvest-capacity", type=int, default=2000)
     ap.add_argument("--train-epochs", type=int, default=10)
     ap.add_argument("--solver-phases", action="store_true")
+    ap.add_argument("--train-max-samples", type=int, default=0, help="train on at most this many samples (0: all)")
     ap.add_argument("--train-lr", type=float, default=2e-3)
     ap.add_argument("--train-lr-final", type=float, default=0.05, help="final step size as a fraction of --train-lr")
     args = ap.parse_args()
