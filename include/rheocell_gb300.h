@@ -91,6 +91,9 @@ typedef struct rc_params {
 	unsigned long long rng_state;
 	int rng_has_cached;
 	double rng_cached;
+	/* 1: conserved dynamics of sim_type = FD_CH (src/Backends/FD_CHBackend.cpp:44-118),
+	 * d(phi)/dt = J0 lap(mu) - v.grad(phi); 0: FD_CPU, d(phi)/dt = -J0 mu - v.grad(phi) */
+	int conserved;
 } rc_params;
 
 typedef struct rc_box {

@@ -40,8 +40,7 @@ _lib = None
 def lib() -> C.CDLL:
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB):
-            build()
+        build()
         _lib = abi.declare(C.CDLL(LIB), "orc")
     return _lib
 

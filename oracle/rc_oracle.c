@@ -684,7 +684,19 @@ static int first_step(orc_sim *s, int store) {
 		c->sumf = 0;
 		c->com[0] = c->com[1] = 0.;
 		for(int q = 0; q < c->n; q++) {
-			const double dphi = -J0 * c->mu[q] - vel_x(s, c, ci, q) * c->dx[q] - vel_y(s, c, ci, q) * c->dy[q];
+			double dphi;
+			if(s->P.conserved) {
+				/* FD_CHBackend::first_step (FD_CHBackend.cpp:63-68).  For the simple and
+				 * nematic models the freeEnergy of the sites already updated in this loop
+				 * has been reset to the external term (0) by updateFieldProperties
+				 * (BaseInteraction.cpp:62-69), as mu[] is below; the wet models'
+				 * updateFieldProperties (WetModel.cpp:167, WetPolarModel.cpp:130) keeps it. */
+				const int nr = patch_nb(c, q, 5), nu = patch_nb(c, q, 7), nl = patch_nb(c, q, 3), nd = patch_nb(c, q, 1);
+				const double lmu = c->mu[nr] + c->mu[nu] + c->mu[nl] + c->mu[nd] - 4. * c->mu[q];
+				dphi = J0 * lmu - vel_x(s, c, ci, q) * c->dx[q] - vel_y(s, c, ci, q) * c->dy[q];
+			}
+			else
+				dphi = -J0 * c->mu[q] - vel_x(s, c, ci, q) * c->dx[q] - vel_y(s, c, ci, q) * c->dy[q];
 			if(store) {
 				c->phi_old[q] = c->phi[q];
 				c->dphi_old[q] = dphi;

@@ -64,6 +64,7 @@ class RcParams(C.Structure):
         ("friction", D2), ("friction_cell", D2), ("zetaQ_self", D2), ("zetaQ_inter", D2),
         ("J_Q", D2), ("beta", D2),
         ("rng_state", C.c_ulonglong), ("rng_has_cached", C.c_int), ("rng_cached", C.c_double),
+        ("conserved", C.c_int),
     ]
 
 

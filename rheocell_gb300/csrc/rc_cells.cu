@@ -551,7 +551,25 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 			dy = a.dyg[start + q];
 		}
 		if(UPD != UP_NONE) {
-			const double dphi = -J0 * mu - vx * dx - vy * dy;
+			double dphi;
+			if(P.conserved) {
+				// FD_CHBackend::first_step (FD_CHBackend.cpp:63-68): J0 lap(mu) - v.grad(phi).
+				// For the simple and nematic models the reference resets
+				// freeEnergy[q'] to the external term (0) as each site q' is updated
+				// (BaseInteraction::updateFieldProperties, BaseInteraction.cpp:62-69),
+				// so neighbours earlier in storage order enter the Laplacian as 0; the
+				// polar and wet models' updateFieldProperties (WetPolarModel.cpp:130,
+				// WetModel.cpp:167) keep it.
+				const Nb nb = patch_nb(q, x, y, lx, ly);
+				auto fe = [&](int s_) {
+					if((MODEL == M_SIMPLE || MODEL == M_NEMATIC) && s_ < q) return 0.0;
+					return (EVAL != EV_NONE) ? smu[s_] : a.mu[start + s_];
+				};
+				const double lmu = fe(nb.r) + fe(nb.u) + fe(nb.l) + fe(nb.d) - 4. * mu;
+				dphi = J0 * lmu - vx * dx - vy * dy;
+			}
+			else
+				dphi = -J0 * mu - vx * dx - vy * dy;
 			double phi_new;
 			if(UPD == UP_PRED) {
 				const double phi_old = (EVAL != EV_NONE) ? phi_e : a.phi_eval[start + q];
@@ -890,6 +908,7 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel_f32(const CellArgs a
 	float area_s = 0.f, area_c = 0.f;
 	const PhaseParams &pu = a.pu;
 	const float J0 = kc[K_J0], hdt = kc[K_HDT];
+	const bool conserved = P.conserved != 0;
 	const float zs = kc[K_ZS], alpha = kc[K_ALPHA], lam = lambda;
 	const float rfr = kc[K_RFR];
 	const int tb = table_base(lx), tby = table_base(ly);
@@ -931,7 +950,19 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel_f32(const CellArgs a
 			dy = d2f_int(a.dyg[start + q]);
 		}
 		if(UPD == UP_NONE) continue;
-		const float dphi = -J0 * mu - vx * dx - vy * dy;
+		float dphi;
+		if(conserved) {
+			// FD_CH (FD_CHBackend.cpp:63-68); the polar model keeps every
+			// neighbour's freeEnergy through the loop (WetPolarModel.cpp:130)
+			const Nb nb = patch_nb(q, x, y, lx, ly);
+			auto fe = [&](int s_) {
+				return (EVAL != EV_NONE) ? smu[s_] : d2f_int(a.mu[start + s_]);
+			};
+			const float lmu = fe(nb.r) + fe(nb.u) + fe(nb.l) + fe(nb.d) - 4.f * mu;
+			dphi = J0 * lmu - vx * dx - vy * dy;
+		}
+		else
+			dphi = -J0 * mu - vx * dx - vy * dy;
 		float phi_new;
 		if(UPD == UP_PRED) {
 			const float phi_old = (EVAL != EV_NONE) ? phi_e : d2f_int(a.phi_eval[start + q]);

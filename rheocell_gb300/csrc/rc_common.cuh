@@ -44,7 +44,7 @@ struct PhaseParams {
 };
 
 struct DevParams {
-	int model, L, border, pad;
+	int model, L, border, conserved;  // conserved: FD_CH dynamics
 	double dt, J0, gamma, lambda, omega, mu, kappa, passive_alpha, a0, cg_tol;
 };
 

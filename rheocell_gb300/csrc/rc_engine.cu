@@ -740,6 +740,7 @@ int rc_batch_create(const rc_params *params, int n_layers, const rc_box *boxes, 
 	P.border = params->border > 0 ? params->border : 4;
 	P.dt = params->dt;
 	P.J0 = params->J0;
+	P.conserved = params->conserved != 0;
 	P.gamma = params->gamma;
 	P.lambda = params->lambda;
 	P.omega = params->omega;

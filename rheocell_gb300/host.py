@@ -108,6 +108,10 @@ def make_params(keys: Dict[str, object], precision: int = abi.RC_PRECISION_DOUBL
     p.border = 4
     p.dt = float(keys["dt"])
     p.J0 = _num(keys, "J0", 1.0)
+    sim_type = str(keys.get("sim_type", "FD_CPU")).strip()
+    if sim_type not in ("FD_CPU", "FD_CH"):
+        raise ValueError("sim_type '%s' is not provided by the GB300 engine" % sim_type)
+    p.conserved = 1 if sim_type == "FD_CH" else 0
     d = dict(_DEFAULTS[name])
     for k in _READS[name]:
         if k in keys:

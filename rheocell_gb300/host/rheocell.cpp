@@ -128,7 +128,9 @@ public:
 		if(backend != "CUDA" && backend != "CPU")
 			throw RCexception("Backend '" + backend + "' not supported");
 		std::string sim_type = inp.str("sim_type", "FD_CPU");
-		if(sim_type != "FD_CPU") throw RCexception("sim_type '" + sim_type + "' is not provided by the GB300 engine");
+		if(sim_type != "FD_CPU" && sim_type != "FD_CH")
+			throw RCexception("sim_type '" + sim_type + "' is not provided by the GB300 engine");
+		params_.conserved = sim_type == "FD_CH" ? 1 : 0;
 		std::string prec = inp.str("backend_precision", "double");
 		if(prec == "double") params_.precision = RC_PRECISION_DOUBLE;
 		else if(prec == "mixed") params_.precision = RC_PRECISION_MIXED;

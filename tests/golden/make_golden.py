@@ -51,6 +51,11 @@ CASES = {
     "wet_equil": (dict(L=36, n=4, seed=9, **SMALL), WET_S, [0, 2], 17, 3),
     "polar41": (dict(L=64, n=4, seed=10), g.DRY_POLAR, [0, 1, 3], 18, 0),
     "resize": (dict(L=64, n=4, seed=11, R=5, lam=1.5, patch=27, aspect=2.2), DRY_POLAR_S, [0, 1, 2], 19, 0),
+    # conserved dynamics (sim_type = FD_CH); the fourth-order update wants a smaller dt
+    "ch_polar": (dict(L=48, n=9, seed=21, **SMALL), dict(DRY_POLAR_S, sim_type="FD_CH", dt=0.01), [0, 1, 5], 31, 0),
+    "ch_nematic": (dict(L=48, n=9, seed=22, types=[0, 1, 1, 0, 1, 1, 0, 1, 1], **SMALL),
+                   dict(NEMATIC_S, sim_type="FD_CH", dt=0.01), [0, 1, 5], 32, 0),
+    "ch_wet": (dict(L=36, n=4, seed=23, **SMALL), dict(WET_S, sim_type="FD_CH", dt=0.01), [0, 1, 3], 33, 0),
 }
 
 
@@ -150,11 +155,16 @@ def record_confgenerator():
 def main():
     if not refdump.have_reference("exact"):
         subprocess.check_call(["make", "-C", os.path.join(ROOT, "oracle"), "-j8"])
+    only = sys.argv[1:]  # optional: record only these cases
     for name in CASES:
+        if only and name not in only:
+            continue
         recs = record(name)
         sz = os.path.getsize(os.path.join(HERE, name + ".npz"))
         print("%-12s steps %s  cells %d  sizes %s  %.0f KB" % (name, [r["step"] for r in recs], recs[0]["N"],
                                                                 sorted(set(zip(recs[-1]["lx"], recs[-1]["ly"]))), sz / 1024))
+    if only:
+        return
     print("overlap", record_overlap())
     record_cli()
     record_confgenerator()
