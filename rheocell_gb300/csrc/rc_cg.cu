@@ -140,10 +140,11 @@ __device__ __forceinline__ unsigned long long gtimer() {
 
 // Diagnostic phase timers: block 0's thread 0 charges the time since the
 // previous mark (including its wait at the barrier that ended the phase) to
-// phase k.  Phases: 0 network input gather, 1 first layer, 2-4 tensor-core
-// layers of levels 0-2, 5 last layer, 6 preconditioned residual, 7-9 FCG
-// phases A-C, 10 everything else.
-enum { PH_GATHER, PH_E0A, PH_TC0, PH_TC1, PH_TC2, PH_OUT, PH_Z, PH_A, PH_B, PH_C, PH_OTHER, PH_COUNT };
+// phase k.  Phases: 0 set-up of a flexible CG run, 1 first layer, 2-4
+// tensor-core layers of levels 0-2, 5 last layer (all network layers when the
+// network runs in FP32), 6 flexible CG phase E, 7 phase AB, 8 (unused),
+// 9 phase C, 10 everything else.
+enum { PH_INIT, PH_E0A, PH_TC0, PH_TC1, PH_TC2, PH_OUT, PH_Z, PH_AB, PH_UNUSED, PH_C, PH_OTHER, PH_COUNT };
 __device__ __forceinline__ void pmark(const CGArgs &a, CGShared &sh, int k) {
 	if(a.phase_ns && blockIdx.x == 0 && threadIdx.x == 0) {
 		const unsigned long long t = gtimer();
@@ -214,76 +215,102 @@ __device__ __forceinline__ T seg_sum(T v, int key, bool &tail) {
 	return v;
 }
 
-// r = b - A x for both components (x = 0 when `x_zero`), written in FP64 and,
-// for the mixed path, also rounded to FP32.  Reduces |b|^2, |r|^2 and r.M^-1 r
-// (the latter on the stored precision of r) into sh.tot[0..5].
-__device__ __forceinline__ bool true_residual(const CGArgs &a, CGShared &sh, bool x_zero, bool to_float) {
+// W(k) = n(k) / T(k), the network's second input channel.
+__device__ __forceinline__ float box_w(const CGArgs &a, const CGShared &sh, int k, int L) {
+	const int n = a.cnt[k];
+	return n ? (float) ((double) n * sh.iT[box_deg(a.cnt, k, L)]) : 0.f;
+}
+
+// FP32 copies of the residual made by true_residual.
+enum { RES_FP64 = 0, RES_FLOAT_UNKNOWN = 1, RES_FLOAT_COVER = 2 };
+
+// r = b - A x for both components (x = 0 when `x_zero`), written in FP64,
+// by box site: thread k forms the box sums of x at k (first pass), then the
+// four-neighbour sum and the diagonal once for the unknowns covering k.
+// fmode RES_FLOAT_UNKNOWN also rounds r to FP32 by unknown (rxf[j]) and
+// clears the correction exf[j] (Jacobi inner iterations);
+// RES_FLOAT_COVER stores them in cover order (rxf[e], exf[e] for
+// cov_idx[e] = j; the flexible CG's layout) and writes the network input of
+// its first application: x0 = (sum over the unknowns at k of r / T, W(k))
+// per component, unscaled.  Reduces |b|^2, |r|^2 and r.M^-1 r (the latter
+// on the stored precision of r) into sh.tot[0..5], each thread's partial
+// sums in box-site order, so the totals are reproducible.
+template<int fmode>
+__device__ __forceinline__ bool true_residual(const CGArgs &a, CGShared &sh, bool x_zero) {
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
-	const long long S = a.st->S;
 	const double neta = -a.eta * 1.0;
 	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
 	const long long gstride = (long long) gridDim.x * blockDim.x;
+	const int *cov_idx = a.cov_idx, *cov_off = a.cov_off;
 	if(!x_zero) {
-		// box sums of x over the CSR cover lists: clear, then add
 		for(long long k = gtid; k < L2; k += gstride) {
-			a.Px[k] = 0.0;
-			a.Py[k] = 0.0;
-		}
-		if(!grid_reduce(a, sh, 0, nullptr)) return false;
-		const long long E = __ldcg(&a.cov_off[L2]);
-		const long long gwarp = gtid >> 5, nwarps = gstride >> 5;
-		const int lane = threadIdx.x & 31;
-		for(long long base = gwarp * 32; base < E; base += nwarps * 32) {
-			const long long t = base + lane;
-			const bool valid = t < E;
-			const int j = valid ? a.cov_idx[t] : 0;
-			const int key = valid ? a.mapg[j] : -1;
-			bool tail;
-			const double sx = seg_sum<double>(valid ? a.vx[j] : 0.0, key, tail);
-			bool tail2;
-			const double sy = seg_sum<double>(valid ? a.vy[j] : 0.0, key, tail2);
-			if(valid && tail) {
-				atomicAdd(&a.Px[key], sx);
-				atomicAdd(&a.Py[key], sy);
+			const int e0 = cov_off[k], e1 = cov_off[k + 1];
+			double sx = 0.0, sy = 0.0;
+#pragma unroll 1
+			for(int e = e0; e < e1; e++) {
+				const int j = cov_idx[e];
+				sx += a.vx[j];
+				sy += a.vy[j];
 			}
+			a.Px[k] = sx;
+			a.Py[k] = sy;
 		}
 		if(!grid_reduce(a, sh, 0, nullptr)) return false;
 	}
 	double v[6] = {0, 0, 0, 0, 0, 0};
-	for(long long j = gtid; j < S; j += gstride) {
-		const int k = a.mapg[j];
-		const int D = box_deg(a.cnt, k, L);
-		const double bx = a.fx[j], by = a.fy[j];
-		double rx, ry;
-		if(x_zero) {
-			rx = bx - 0.0;
-			ry = by - 0.0;
+	for(long long k = gtid; k < L2; k += gstride) {
+		const int e0 = cov_off[k], e1 = cov_off[k + 1];
+		float Rx = 0.f, Ry = 0.f;
+		if(e1 > e0) {
+			const int D = box_deg(a.cnt, (int) k, L);
+			const double T = sh.T[D], iT = sh.iT[D];
+			const float iTf = (float) iT;
+			const double qx = x_zero ? 0.0 : neta * box_n4(a.Px, (int) k, L);
+			const double qy = x_zero ? 0.0 : neta * box_n4(a.Py, (int) k, L);
+#pragma unroll 1
+			for(int e = e0; e < e1; e++) {
+				const int j = cov_idx[e];
+				const double bx = a.fx[j], by = a.fy[j];
+				double rx, ry;
+				if(x_zero) {
+					rx = bx - 0.0;
+					ry = by - 0.0;
+				}
+				else {
+					rx = bx - (T * a.vx[j] + qx);
+					ry = by - (T * a.vy[j] + qy);
+				}
+				a.rx[j] = rx;
+				a.ry[j] = ry;
+				v[0] += bx * bx;
+				v[1] += by * by;
+				v[2] += rx * rx;
+				v[3] += ry * ry;
+				if(fmode != RES_FP64) {
+					const float fx = (float) rx, fy = (float) ry;
+					const int o = fmode == RES_FLOAT_COVER ? e : j;
+					a.rxf[o] = fx;
+					a.ryf[o] = fy;
+					a.exf[o] = 0.0f;
+					a.eyf[o] = 0.0f;
+					v[4] += (double) fx * (iT * (double) fx);
+					v[5] += (double) fy * (iT * (double) fy);
+					Rx += fx * iTf;
+					Ry += fy * iTf;
+				}
+				else {
+					v[4] += rx * (iT * rx);
+					v[5] += ry * (iT * ry);
+				}
+			}
 		}
-		else {
-			const double ax = sh.T[D] * a.vx[j] + neta * box_n4(a.Px, k, L);
-			const double ay = sh.T[D] * a.vy[j] + neta * box_n4(a.Py, k, L);
-			rx = bx - ax;
-			ry = by - ay;
-		}
-		a.rx[j] = rx;
-		a.ry[j] = ry;
-		v[0] += bx * bx;
-		v[1] += by * by;
-		v[2] += rx * rx;
-		v[3] += ry * ry;
-		if(to_float) {
-			const float fx = (float) rx, fy = (float) ry;
-			a.rxf[j] = fx;
-			a.ryf[j] = fy;
-			a.exf[j] = 0.0f;
-			a.eyf[j] = 0.0f;
-			v[4] += (double) fx * (sh.iT[D] * (double) fx);
-			v[5] += (double) fy * (sh.iT[D] * (double) fy);
-		}
-		else {
-			v[4] += rx * (sh.iT[D] * rx);
-			v[5] += ry * (sh.iT[D] * ry);
+		if(fmode == RES_FLOAT_COVER) {
+			const float wv = box_w(a, sh, (int) k, L);
+			a.unet.x0[k * 2] = Rx;
+			a.unet.x0[k * 2 + 1] = wv;
+			a.unet.x0[(L2 + k) * 2] = Ry;
+			a.unet.x0[(L2 + k) * 2 + 1] = wv;
 		}
 	}
 	block_sum<6>(v, sh.red);
@@ -661,11 +688,6 @@ __device__ __forceinline__ bool cg_iterate(const CGArgs &a, CGShared &sh, const 
 // (R_k, V = S x* - S x_k).  Inputs and targets are divided by the residual
 // scale s = sqrt(|r_k|^2 / S), the same normalisation the solve applies.
 
-__device__ __forceinline__ float box_w(const CGArgs &a, const CGShared &sh, int k, int L) {
-	const int n = a.cnt[k];
-	return n ? (float) ((double) n * sh.iT[box_deg(a.cnt, k, L)]) : 0.f;
-}
-
 // Record harvest point m: box sums of x (into the target slot) and of r/T
 // (into the input slot) for both components; slots hbase + 2m + c.
 __device__ __forceinline__ bool harvest_point(const CGArgs &a, CGShared &sh, const double *ux, const double *uy, const double *rx,
@@ -756,61 +778,95 @@ __device__ __forceinline__ bool harvest_finish(const CGArgs &a, CGShared &sh, co
 }
 
 // ---------------------------------------------------------------------------
-// Learned preconditioner: z = M r for both components.
-//   D: R[c][k] = sum_{j at k} r_j / (T_j s_c) into the network's input
-//      (the R channel was cleared in an earlier phase; W is in place);
-//   the network (11 convolution layers, a grid barrier after each);
-//   E: z_j = (r_j + eta s_c (N4 V_c)[k_j]) / T_j, with r.z and z.Ap reduced
-//      into sh.tot[0..3].
-// Runs in FP32 with FP64 reductions.
+// Learned preconditioner inside flexible CG.
+//
+// The FP32 vectors of the flexible CG (r, z, p, Ap, e) are stored in cover
+// order: entry e is the unknown cov_idx[e], and the entries of box site k are
+// [cov_off[k], cov_off[k+1]).  Every phase is a loop over box sites in which
+// a thread walks its site's contiguous entries: no index indirection, box
+// sums stored without atomics, all sums in a fixed order.
+//
+// One iteration (both components at once, each with its own scalars):
+//   network  V = N(R / s, W)                (input R written by phase C)
+//   phase E  z = (r + eta s N4V) / T, Z = S z, r.z and z.Ap_old
+//   phase AB p = z + beta p with beta = -z.Ap_old / p.Ap_old (Notay's
+//            FCG(1)); P' = S p; Ap = T p - eta N4(P'), the neighbours' P'
+//            taken as Z + beta P (linearity, so no barrier); p.Ap
+//   phase C  e += alpha p, r -= alpha Ap, |r|^2, R = sum r / T
+// with alpha = r.z / p.Ap.  P alternates between two box buffers.
 struct TcState {
 	unsigned char *dsm;  // dynamic shared memory (tensor-core staging, FP32 weights)
 	uint32_t tmem;       // allocated TMEM columns
 	uint32_t phase;      // mbarrier parity
 };
 
-__device__ __noinline__ bool precond_apply(const CGArgs &a, CGShared &sh, TcState &tc, const float *iTT) {
+// First layer (2 -> 16, ReLU) at one pixel of sample n, FP32: channel 0 of
+// the input (R) is multiplied by sc (1/s of the component) as it is read.
+// w: [9][2][16] then 16 biases.
+__device__ __forceinline__ void e0a_pixel(const float *x0, const float *w, int n, int i, int j, int L, float sc, float *y) {
+#pragma unroll
+	for(int o = 0; o < 16; o++) y[o] = w[9 * 2 * 16 + o];
+#pragma unroll
+	for(int t = 0; t < 9; t++) {
+		const int ii = wrap(i + t / 3 - 1, L), jj = wrap(j + t % 3 - 1, L);
+		const float2 in = *reinterpret_cast<const float2 *>(x0 + ((size_t) (n * L + ii) * L + jj) * 2);
+		const float r = in.x * sc, wv = in.y;
+		const float *wt = w + t * 32;
+#pragma unroll
+		for(int o = 0; o < 16; o++) y[o] = fmaf(r, wt[o], y[o]);
+#pragma unroll
+		for(int o = 0; o < 16; o++) y[o] = fmaf(wv, wt[16 + o], y[o]);
+	}
+#pragma unroll
+	for(int o = 0; o < 16; o++) y[o] = fmaxf(y[o], 0.f);
+}
+
+// The network on both components: V (a.unet.out, FP32) from x0.
+__device__ __noinline__ bool precond_network(const CGArgs &a, CGShared &sh, TcState &tc) {
 	float *wsm = reinterpret_cast<float *>(tc.dsm);
 	pmark(a, sh, PH_OTHER);
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
-	const long long S = a.st->S;
 	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
 	const long long gstride = (long long) gridDim.x * blockDim.x;
-	const float inv0 = sh.scale[0] > 0.0 ? (float) (1.0 / sh.scale[0]) : 0.f;
-	const float inv1 = sh.scale[1] > 0.0 ? (float) (1.0 / sh.scale[1]) : 0.f;
-	float *x0 = a.unet.x0;
+	const float sc[2] = {sh.scale[0] > 0.0 ? (float) (1.0 / sh.scale[0]) : 0.f,
+	                     sh.scale[1] > 0.0 ? (float) (1.0 / sh.scale[1]) : 0.f};
 	{
-		const long long E = __ldcg(&a.cov_off[L2]);
-		const long long gwarp = gtid >> 5, nwarps = gstride >> 5;
-		const int lane = threadIdx.x & 31;
-		for(long long base = gwarp * 32; base < E; base += nwarps * 32) {
-			const long long t = base + lane;
-			const bool valid = t < E;
-			const int j = valid ? a.cov_idx[t] : 0;
-			const int key = valid ? a.mapg[j] : -1;
-			const float id = valid ? iTT[box_deg(a.cnt, key, L)] : 0.f;
-			bool t0, t1;
-			const float sx = seg_sum<float>(valid ? a.rxf[j] * id * inv0 : 0.f, key, t0);
-			const float sy = seg_sum<float>(valid ? a.ryf[j] * id * inv1 : 0.f, key, t1);
-			if(valid && t0) {
-				atomicAdd(&x0[(size_t) key * 2], sx);
-				atomicAdd(&x0[((size_t) L2 + key) * 2], sy);
+		const int nw = 9 * 2 * 16 + 16;
+		__syncthreads();
+		for(int k = threadIdx.x; k < nw; k += blockDim.x) wsm[k] = a.unet_params[unet_weight_offset(L_E0A) + k];
+		__syncthreads();
+		for(long long p = gtid; p < 2 * L2; p += gstride) {
+			const int n = p >= L2;
+			const int r = (int) (p - n * L2);
+			const int i = r / L, j = r - (r / L) * L;
+			float y[16];
+			e0a_pixel(a.unet.x0, wsm, n, i, j, L, sc[n], y);
+			if(a.unet_tc) {
+				uint4 o0, o1;
+				o0.x = f2bf(y[0], y[1]);
+				o0.y = f2bf(y[2], y[3]);
+				o0.z = f2bf(y[4], y[5]);
+				o0.w = f2bf(y[6], y[7]);
+				o1.x = f2bf(y[8], y[9]);
+				o1.y = f2bf(y[10], y[11]);
+				o1.z = f2bf(y[12], y[13]);
+				o1.w = f2bf(y[14], y[15]);
+				uint4 *o = reinterpret_cast<uint4 *>(a.unet_bf.e0a + p * 16);
+				o[0] = o0;
+				o[1] = o1;
+			}
+			else {
+				float4 *o = reinterpret_cast<float4 *>(a.unet.e0a + p * 16);
+#pragma unroll
+				for(int q = 0; q < 4; q++) o[q] = make_float4(y[4 * q], y[4 * q + 1], y[4 * q + 2], y[4 * q + 3]);
 			}
 		}
+		if(!grid_reduce(a, sh, 0, nullptr)) return false;
+		pmark(a, sh, PH_E0A);
 	}
-	if(!grid_reduce(a, sh, 0, nullptr)) return false;
-	pmark(a, sh, PH_GATHER);
 	if(a.unet_tc) {
-		// first layer (FP32, CUDA cores) -> BF16; nine tensor-core layers; last layer -> FP32
-		{
-			const int nw = 9 * 2 * 16 + 16;
-			for(int k = threadIdx.x; k < nw; k += blockDim.x) wsm[k] = a.unet_params[unet_weight_offset(L_E0A) + k];
-			__syncthreads();
-			e0a_range(a.unet.x0, wsm, a.unet_bf.e0a, 2, L, gtid, gstride);
-			if(!grid_reduce(a, sh, 0, nullptr)) return false;
-			pmark(a, sh, PH_E0A);
-		}
+		// nine tensor-core layers; last layer (FP32, CUDA cores) -> V
 		for(int l = L_E0B; l <= L_D0B; l++) {
 			if(!tc_conv_layer(l, unet_tc_src(l, a.unet_bf), a.unet_wpack + unet_pack_offset(l),
 			                  a.unet_params + unet_bias_offset(l), unet_tc_dst(l, a.unet_bf), 2, L >> unet_layer(l).level,
@@ -819,18 +875,16 @@ __device__ __noinline__ bool precond_apply(const CGArgs &a, CGShared &sh, TcStat
 			if(!grid_reduce(a, sh, 0, nullptr)) return false;
 			pmark(a, sh, PH_TC0 + unet_layer(l).level);
 		}
-		{
-			__syncthreads();
-			const int nw = 9 * 16 + 1;
-			for(int k = threadIdx.x; k < nw; k += blockDim.x) wsm[k] = a.unet_params[unet_weight_offset(L_OUT) + k];
-			__syncthreads();
-			out_range(a.unet_bf.t0, wsm, a.unet.out, 2, L, gtid, gstride);
-			if(!grid_reduce(a, sh, 0, nullptr)) return false;
-			pmark(a, sh, PH_OUT);
-		}
+		__syncthreads();
+		const int nw = 9 * 16 + 1;
+		for(int k = threadIdx.x; k < nw; k += blockDim.x) wsm[k] = a.unet_params[unet_weight_offset(L_OUT) + k];
+		__syncthreads();
+		out_range(a.unet_bf.t0, wsm, a.unet.out, 2, L, gtid, gstride);
+		if(!grid_reduce(a, sh, 0, nullptr)) return false;
+		pmark(a, sh, PH_OUT);
 	}
 	else {
-		for(int l = 0; l < UNET_LAYERS; l++) {
+		for(int l = L_E0B; l < UNET_LAYERS; l++) {
 			const UNetLayerDesc d = unet_layer(l);
 			const int nw = 9 * d.ci * d.co + d.co;
 			const float *src = a.unet_params + unet_weight_offset(l);
@@ -841,113 +895,113 @@ __device__ __noinline__ bool precond_apply(const CGArgs &a, CGShared &sh, TcStat
 			                 gtid, gstride);
 			if(!grid_reduce(a, sh, 0, nullptr)) return false;
 		}
+		pmark(a, sh, PH_OUT);
 	}
+	return true;
+}
+
+// Phase E: z = (r + eta s N4V) / T, Z = S z; r.z, and z.Ap of the previous
+// direction (not on the first sweep) into sh.tot[0..3].
+__device__ __noinline__ bool fcg_phase_e(const CGArgs &a, CGShared &sh, bool first) {
+	const int L = a.L;
+	const long long L2 = (long long) L * L;
+	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+	const long long gstride = (long long) gridDim.x * blockDim.x;
+	const int ax = sh.act[0], ay = sh.act[1];
 	const float es0 = (float) (a.eta * sh.scale[0]), es1 = (float) (a.eta * sh.scale[1]);
 	const float *V = a.unet.out;
+	const float *rx = a.rxf, *ry = a.ryf, *apx = a.apxf, *apy = a.apyf;
+	float *zx = a.zxf, *zy = a.zyf;
+	const int *cov_off = a.cov_off;
 	float w[4] = {0.f, 0.f, 0.f, 0.f};
-	for(long long j = gtid; j < S; j += gstride) {
-		const int k = a.mapg[j];
-		const float id = iTT[box_deg(a.cnt, k, L)];
-		const float rxv = a.rxf[j], ryv = a.ryf[j];
-		const float zx = id * __fmaf_rn(es0, box_n4T<float>(V, k, L), rxv);
-		const float zy = id * __fmaf_rn(es1, box_n4T<float>(V + L2, k, L), ryv);
-		a.zxf[j] = zx;
-		a.zyf[j] = zy;
-		w[0] = __fmaf_rn(rxv, zx, w[0]);
-		w[1] = __fmaf_rn(ryv, zy, w[1]);
-		w[2] = __fmaf_rn(zx, a.apxf[j], w[2]);
-		w[3] = __fmaf_rn(zy, a.apyf[j], w[3]);
+	for(long long k = gtid; k < L2; k += gstride) {
+		const int e0 = cov_off[k], e1 = cov_off[k + 1];
+		float Zx = 0.f, Zy = 0.f;
+		if(e1 > e0) {
+			const float id = sh.iTf[box_deg(a.cnt, (int) k, L)];
+			if(ax) {
+				const float nv = es0 * box_n4T<float>(V, (int) k, L);
+				for(int e = e0; e < e1; e++) {
+					const float r = rx[e];
+					const float z = id * (r + nv);
+					zx[e] = z;
+					Zx += z;
+					w[0] = __fmaf_rn(r, z, w[0]);
+					if(!first) w[2] = __fmaf_rn(z, apx[e], w[2]);
+				}
+			}
+			if(ay) {
+				const float nv = es1 * box_n4T<float>(V + L2, (int) k, L);
+				for(int e = e0; e < e1; e++) {
+					const float r = ry[e];
+					const float z = id * (r + nv);
+					zy[e] = z;
+					Zy += z;
+					w[1] = __fmaf_rn(r, z, w[1]);
+					if(!first) w[3] = __fmaf_rn(z, apy[e], w[3]);
+				}
+			}
+		}
+		if(ax) a.Zxf[k] = Zx;
+		if(ay) a.Zyf[k] = Zy;
 	}
 	warp_tree<float, 4>(w);
 	double v[4] = {(double) w[0], (double) w[1], (double) w[2], (double) w[3]};
 	block_sum_warps<4>(v, sh.red);
-	const bool ok = grid_reduce(a, sh, 4, v);
-	pmark(a, sh, PH_Z);
-	return ok;
+	return grid_reduce(a, sh, 4, v);
 }
 
-// Flexible CG (Notay's FCG(1): beta = -z'.Ap / p.Ap) on the FP32 correction
-// system A e = r of one refinement sweep, preconditioned by the network.
-// Same conventions as cg_iterate<float>: r in rxf/ryf, e in exf/eyf, stop at
-// |r|^2 < thr per component.
-// Flexible CG phases of the learned path (each its own function, so that
-// each gets the register file to itself).
-// Phase A: p = z + beta p (p = z on the first sweep), box sums P = S p.
-__device__ __noinline__ bool fcg_phase_a(const CGArgs &a, CGShared &sh) {
+// Phase AB: p = z + beta p, box sums into Pn, Ap = T p - eta N4(Pn) with the
+// neighbours' Pn = Z + beta Po; p.Ap into sh.tot[0..1].
+__device__ __noinline__ bool fcg_phase_ab(const CGArgs &a, CGShared &sh, bool first, const float *Pox, const float *Poy,
+                                          float *Pnx, float *Pny) {
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
-	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-	const long long gstride = (long long) gridDim.x * blockDim.x;
-	const int ax = sh.act[0], ay = sh.act[1], first = sh.first;
-	const float bx = (float) sh.beta[0], by = (float) sh.beta[1];
-	float *px = a.pxf, *py = a.pyf, *Pbx = a.Pxf, *Pby = a.Pyf;
-	const float *zx = a.zxf, *zy = a.zyf;
-	const int *cov_idx = a.cov_idx, *mapg = a.mapg;
-	const long long E = __ldcg(&a.cov_off[L2]);
-	const long long gwarp = gtid >> 5, nwarps = gstride >> 5;
-	const int lane = threadIdx.x & 31;
-	for(long long base = gwarp * 32; base < E; base += nwarps * 32) {
-		const long long t = base + lane;
-		const bool valid = t < E;
-		const int j = valid ? cov_idx[t] : 0;
-		const int key = valid ? mapg[j] : -1;
-		float vx = 0.f, vy = 0.f;
-		if(valid && ax) {
-			const float z = zx[j];
-			const float p = first ? z : __fmaf_rn(bx, px[j], z);
-			px[j] = p;
-			vx = p;
-		}
-		if(valid && ay) {
-			const float z = zy[j];
-			const float p = first ? z : __fmaf_rn(by, py[j], z);
-			py[j] = p;
-			vy = p;
-		}
-		bool tail = false, tail2 = false;
-		if(ax) vx = seg_sum<float>(vx, key, tail);
-		if(ay) vy = seg_sum<float>(vy, key, tail2);
-		if(valid) {
-			if(ax && tail) atomicAdd(&Pbx[key], vx);
-			if(ay && tail2) atomicAdd(&Pby[key], vy);
-		}
-	}
-	return grid_reduce(a, sh, 0, nullptr);
-}
-
-// Phase B: Ap (stored) and p.Ap into sh.tot[0..1]; the network's R channel is cleared.
-__device__ __noinline__ bool fcg_phase_b(const CGArgs &a, CGShared &sh) {
-	const int L = a.L;
-	const long long L2 = (long long) L * L;
-	const long long S = a.st->S;
-	const float neta = (float) (-a.eta * 1.0);
 	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
 	const long long gstride = (long long) gridDim.x * blockDim.x;
 	const int ax = sh.act[0], ay = sh.act[1];
-	const float *px = a.pxf, *py = a.pyf, *Pbx = a.Pxf, *Pby = a.Pyf;
-	float *apx = a.apxf, *apy = a.apyf;
-	const int *mapg = a.mapg, *cnt = a.cnt;
+	const float bx = (float) sh.beta[0], by = (float) sh.beta[1];
+	const float neta = (float) (-a.eta * 1.0);
+	const float *zx = a.zxf, *zy = a.zyf, *Zx = a.Zxf, *Zy = a.Zyf;
+	float *px = a.pxf, *py = a.pyf, *apx = a.apxf, *apy = a.apyf;
+	const int *cov_off = a.cov_off;
 	float w[2] = {0.f, 0.f};
-	for(long long j = gtid; j < S; j += gstride) {
-		const int k = mapg[j];
-		const float d = sh.Tf[box_deg(cnt, k, L)];
-		if(ax) {
-			const float p = px[j];
-			const float ap = __fmaf_rn(d, p, neta * box_n4T<float>(Pbx, k, L));
-			apx[j] = ap;
-			w[0] = __fmaf_rn(p, ap, w[0]);
-		}
-		if(ay) {
-			const float p = py[j];
-			const float ap = __fmaf_rn(d, p, neta * box_n4T<float>(Pby, k, L));
-			apy[j] = ap;
-			w[1] = __fmaf_rn(p, ap, w[1]);
-		}
-	}
-	float *x0 = a.unet.x0;
 	for(long long k = gtid; k < L2; k += gstride) {
-		x0[k * 2] = 0.f;
-		x0[(L2 + k) * 2] = 0.f;
+		const int e0 = cov_off[k], e1 = cov_off[k + 1];
+		float sx = 0.f, sy = 0.f;
+		if(e1 > e0) {
+			const float d = sh.Tf[box_deg(a.cnt, (int) k, L)];
+			if(ax) {
+				const float n4 = first ? box_n4T<float>(Zx, (int) k, L)
+				                       : __fmaf_rn(bx, box_n4T<float>(Pox, (int) k, L), box_n4T<float>(Zx, (int) k, L));
+				const float q = neta * n4;
+				for(int e = e0; e < e1; e++) {
+					const float z = zx[e];
+					const float p = first ? z : __fmaf_rn(bx, px[e], z);
+					px[e] = p;
+					sx += p;
+					const float ap = __fmaf_rn(d, p, q);
+					apx[e] = ap;
+					w[0] = __fmaf_rn(p, ap, w[0]);
+				}
+			}
+			if(ay) {
+				const float n4 = first ? box_n4T<float>(Zy, (int) k, L)
+				                       : __fmaf_rn(by, box_n4T<float>(Poy, (int) k, L), box_n4T<float>(Zy, (int) k, L));
+				const float q = neta * n4;
+				for(int e = e0; e < e1; e++) {
+					const float z = zy[e];
+					const float p = first ? z : __fmaf_rn(by, py[e], z);
+					py[e] = p;
+					sy += p;
+					const float ap = __fmaf_rn(d, p, q);
+					apy[e] = ap;
+					w[1] = __fmaf_rn(p, ap, w[1]);
+				}
+			}
+		}
+		if(ax) Pnx[k] = sx;
+		if(ay) Pny[k] = sy;
 	}
 	warp_tree<float, 2>(w);
 	double v[2] = {(double) w[0], (double) w[1]};
@@ -955,35 +1009,45 @@ __device__ __noinline__ bool fcg_phase_b(const CGArgs &a, CGShared &sh) {
 	return grid_reduce(a, sh, 2, v);
 }
 
-// Phase C: e += alpha p, r -= alpha Ap, |r|^2 into sh.tot[0..1]; box sums cleared.
+// Phase C: e += alpha p, r -= alpha Ap, |r|^2 into sh.tot[0..1]; the next
+// network input R = sum over the site's unknowns of r / T (unscaled).
 __device__ __noinline__ bool fcg_phase_c(const CGArgs &a, CGShared &sh) {
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
-	const long long S = a.st->S;
 	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
 	const long long gstride = (long long) gridDim.x * blockDim.x;
 	const int ax = sh.act[0], ay = sh.act[1];
 	const float alx = (float) sh.alpha[0], aly = (float) sh.alpha[1];
 	const float *px = a.pxf, *py = a.pyf, *apx = a.apxf, *apy = a.apyf;
-	float *ex = a.exf, *ey = a.eyf, *rx = a.rxf, *ry = a.ryf, *Pbx = a.Pxf, *Pby = a.Pyf;
+	float *ex = a.exf, *ey = a.eyf, *rx = a.rxf, *ry = a.ryf, *x0 = a.unet.x0;
+	const int *cov_off = a.cov_off;
 	float w[2] = {0.f, 0.f};
-	for(long long j = gtid; j < S; j += gstride) {
+	for(long long k = gtid; k < L2; k += gstride) {
+		const int e0 = cov_off[k], e1 = cov_off[k + 1];
+		if(e1 == e0) continue;
+		const float id = sh.iTf[box_deg(a.cnt, (int) k, L)];
 		if(ax) {
-			ex[j] = __fmaf_rn(alx, px[j], ex[j]);
-			const float r = __fmaf_rn(-alx, apx[j], rx[j]);
-			rx[j] = r;
-			w[0] = __fmaf_rn(r, r, w[0]);
+			float R = 0.f;
+			for(int e = e0; e < e1; e++) {
+				ex[e] = __fmaf_rn(alx, px[e], ex[e]);
+				const float r = __fmaf_rn(-alx, apx[e], rx[e]);
+				rx[e] = r;
+				w[0] = __fmaf_rn(r, r, w[0]);
+				R += r * id;
+			}
+			x0[k * 2] = R;
 		}
 		if(ay) {
-			ey[j] = __fmaf_rn(aly, py[j], ey[j]);
-			const float r = __fmaf_rn(-aly, apy[j], ry[j]);
-			ry[j] = r;
-			w[1] = __fmaf_rn(r, r, w[1]);
+			float R = 0.f;
+			for(int e = e0; e < e1; e++) {
+				ey[e] = __fmaf_rn(aly, py[e], ey[e]);
+				const float r = __fmaf_rn(-aly, apy[e], ry[e]);
+				ry[e] = r;
+				w[1] = __fmaf_rn(r, r, w[1]);
+				R += r * id;
+			}
+			x0[(L2 + k) * 2] = R;
 		}
-	}
-	for(long long k = gtid; k < L2; k += gstride) {
-		Pbx[k] = 0.f;
-		Pby[k] = 0.f;
 	}
 	warp_tree<float, 2>(w);
 	double v[2] = {(double) w[0], (double) w[1]};
@@ -991,50 +1055,39 @@ __device__ __noinline__ bool fcg_phase_c(const CGArgs &a, CGShared &sh) {
 	return grid_reduce(a, sh, 2, v);
 }
 
-// Flexible CG (Notay's FCG(1): beta = -z'.Ap / p.Ap) on the FP32 correction
-// system A e = r of one refinement sweep, preconditioned by the network.
-// Same conventions as cg_iterate<float>: r in rxf/ryf, e in exf/eyf, stop at
-// |r|^2 < thr per component.
+// Flexible CG on the FP32 correction system A e = r of one refinement sweep,
+// preconditioned by the network; r and e in cover order (rxf, exf ...) and
+// the network input x0 as true_residual(RES_FLOAT_COVER) leaves them.  Stops
+// a component at |r|^2 < thr.
 __device__ __noinline__ bool fcg_iterate(const CGArgs &a, CGShared &sh, TcState &tc, long long max_it) {
-	const int L = a.L;
-	const long long L2 = (long long) L * L;
 	const long long S = a.st->S;
-	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-	const long long gstride = (long long) gridDim.x * blockDim.x;
 	for(int d = threadIdx.x; d <= CG_MAX_D; d += blockDim.x) {
 		sh.Tf[d] = (float) sh.T[d];
 		sh.iTf[d] = (float) sh.iT[d];
 	}
-	// box sums cleared for phase A, network input: R cleared, W in place
-	for(long long k = gtid; k < L2; k += gstride) {
-		a.Pxf[k] = 0.f;
-		a.Pyf[k] = 0.f;
-		const float wv = box_w(a, sh, (int) k, L);
-		a.unet.x0[k * 2] = 0.f;
-		a.unet.x0[k * 2 + 1] = wv;
-		a.unet.x0[(L2 + k) * 2] = 0.f;
-		a.unet.x0[(L2 + k) * 2 + 1] = wv;
-	}
-	for(long long j = gtid; j < S; j += gstride) {
-		a.apxf[j] = 0.f;
-		a.apyf[j] = 0.f;
-	}
 	if(threadIdx.x == 0) {
 		for(int c = 0; c < 2; c++) sh.scale[c] = sqrt(sh.rn2[c] / (double) S);
-		sh.first = 1;
-	}
-	if(!grid_reduce(a, sh, 0, nullptr)) return false;
-	if(!precond_apply(a, sh, tc, sh.iTf)) return false;
-	if(threadIdx.x == 0) {
-		sh.rz[0] = sh.tot[0];
-		sh.rz[1] = sh.tot[1];
 	}
 	__syncthreads();
+	pmark(a, sh, PH_INIT);
+	bool first = true;
+	int par = 0;
 	while(sh.act[0] || sh.act[1]) {
-		if(!fcg_phase_a(a, sh)) return false;
-		pmark(a, sh, PH_A);
-		if(!fcg_phase_b(a, sh)) return false;
-		pmark(a, sh, PH_B);
+		if(!precond_network(a, sh, tc)) return false;
+		if(!fcg_phase_e(a, sh, first)) return false;
+		pmark(a, sh, PH_Z);
+		if(threadIdx.x == 0) {
+			for(int c = 0; c < 2; c++) {
+				if(!sh.act[c]) continue;
+				sh.rz[c] = sh.tot[c];
+				sh.beta[c] = first ? 0.0 : -sh.tot[2 + c] / sh.pap[c];
+			}
+		}
+		__syncthreads();
+		float *Pox = par ? a.Pxf2 : a.Pxf, *Poy = par ? a.Pyf2 : a.Pyf;
+		float *Pnx = par ? a.Pxf : a.Pxf2, *Pny = par ? a.Pyf : a.Pyf2;
+		if(!fcg_phase_ab(a, sh, first, Pox, Poy, Pnx, Pny)) return false;
+		pmark(a, sh, PH_AB);
 		if(threadIdx.x == 0) {
 			for(int c = 0; c < 2; c++) {
 				if(!sh.act[c]) continue;
@@ -1055,17 +1108,8 @@ __device__ __noinline__ bool fcg_iterate(const CGArgs &a, CGShared &sh, TcState 
 			}
 		}
 		__syncthreads();
-		if(!sh.act[0] && !sh.act[1]) break;
-		if(!precond_apply(a, sh, tc, sh.iTf)) return false;
-		if(threadIdx.x == 0) {
-			for(int c = 0; c < 2; c++) {
-				if(!sh.act[c]) continue;
-				sh.rz[c] = sh.tot[c];
-				sh.beta[c] = -sh.tot[2 + c] / sh.pap[c];
-			}
-			sh.first = 0;
-		}
-		__syncthreads();
+		first = false;
+		par ^= 1;
 	}
 	return true;
 }
@@ -1094,7 +1138,8 @@ __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcState &
 	}
 	const bool mixed = a.mixed != 0;
 	if(!build_csr(a, sh)) return;
-	if(!true_residual(a, sh, cold != 0, mixed)) return;
+	constexpr int fmode = LEARNED ? RES_FLOAT_COVER : RES_FLOAT_UNKNOWN;
+	if(!(mixed ? true_residual<fmode>(a, sh, cold != 0) : true_residual<RES_FP64>(a, sh, cold != 0))) return;
 	if(threadIdx.x == 0) {
 		for(int c = 0; c < 2; c++) {
 			sh.bn2[c] = sh.tot[c];
@@ -1149,13 +1194,23 @@ __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcState &
 				if(!cg_iterate<float>(a, sh, CGVecs<float>{a.rxf, a.ryf, a.pxf, a.pyf, a.apxf, a.apyf, a.Pxf, a.Pyf, a.exf, a.eyf}, max_it))
 					return;
 			}
-			for(long long j = gtid; j < S; j += gstride) {
-				a.vx[j] += (double) a.exf[j];
-				a.vy[j] += (double) a.eyf[j];
+			if constexpr(LEARNED) {
+				// the correction is in cover order
+				for(long long e = gtid; e < S; e += gstride) {
+					const int j = a.cov_idx[e];
+					a.vx[j] += (double) a.exf[e];
+					a.vy[j] += (double) a.eyf[e];
+				}
+			}
+			else {
+				for(long long j = gtid; j < S; j += gstride) {
+					a.vx[j] += (double) a.exf[j];
+					a.vy[j] += (double) a.eyf[j];
+				}
 			}
 			refinements++;
 			if(!grid_reduce(a, sh, 0, nullptr)) return;
-			if(!true_residual(a, sh, false, true)) return;
+			if(!true_residual<fmode>(a, sh, false)) return;
 			if(threadIdx.x == 0) {
 				for(int c = 0; c < 2; c++) {
 					sh.rn2[c] = sh.tot[2 + c];
@@ -1171,7 +1226,7 @@ __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcState &
 		}
 		if(s_fallback || sh.act[0] || sh.act[1]) {
 			// plain FP64 CG from the current x (the residual is in rx, ry)
-			if(!true_residual(a, sh, false, false)) return;
+			if(!true_residual<RES_FP64>(a, sh, false)) return;
 			if(threadIdx.x == 0) {
 				for(int c = 0; c < 2; c++) {
 					sh.rn2[c] = sh.tot[2 + c];

@@ -113,7 +113,7 @@ struct rc_engine {
 	int solver = RC_SOLVER_PLAIN;
 	float *unet_params = nullptr;  // FP32 network parameters (null: none yet)
 	UNetActs unet{};               // activations for the two velocity components
-	float *zxf = nullptr, *zyf = nullptr;
+	float *zxf = nullptr, *zyf = nullptr, *Zxf = nullptr, *Zyf = nullptr, *Pxf2 = nullptr, *Pyf2 = nullptr;
 	bf16 *unet_pack = nullptr;     // BF16 weights of the tensor-core layers
 	UNetActsBF unet_bf{};          // BF16 activations of the tensor-core path
 	int cg_blocks_learned = 0;
@@ -338,6 +338,10 @@ static void solve(rc_engine *e, int phase) {
 		g.unet_wpack = e->unet_pack;
 		g.zxf = e->zxf;
 		g.zyf = e->zyf;
+		g.Zxf = e->Zxf;
+		g.Zyf = e->Zyf;
+		g.Pxf2 = e->Pxf2;
+		g.Pyf2 = e->Pyf2;
 		blocks = e->cg_blocks_learned;
 	}
 	else if(e->harv_cap > 0 && e->harv_collect && !g.mixed) {
@@ -1320,7 +1324,9 @@ int rc_set_solver(rc_engine *e, int solver) {
 		if(!e->zxf) {
 			const size_t p0 = 2 * L2, p1 = p0 / 4, p2 = p0 / 16;
 			UNetActs &A = e->unet;
-			if((rc = dalloc(e, &e->zxf, cap)) || (rc = dalloc(e, &e->zyf, cap)) || (rc = dalloc(e, &A.x0, p0 * 2)) ||
+			if((rc = dalloc(e, &e->zxf, cap)) || (rc = dalloc(e, &e->zyf, cap)) || (rc = dalloc(e, &e->Zxf, L2)) ||
+			   (rc = dalloc(e, &e->Zyf, L2)) || (rc = dalloc(e, &e->Pxf2, L2)) || (rc = dalloc(e, &e->Pyf2, L2)) ||
+			   (rc = dalloc(e, &A.x0, p0 * 2)) ||
 			   (rc = dalloc(e, &A.e0a, p0 * 16)) || (rc = dalloc(e, &A.s0, p0 * 16)) || (rc = dalloc(e, &A.d0a, p0 * 16)) ||
 			   (rc = dalloc(e, &A.t0, p0 * 16)) || (rc = dalloc(e, &A.out, p0)) || (rc = dalloc(e, &A.e1a, p1 * 16)) ||
 			   (rc = dalloc(e, &A.s1, p1 * 16)) || (rc = dalloc(e, &A.d1a, p1 * 16)) || (rc = dalloc(e, &A.t1, p1 * 16)) ||

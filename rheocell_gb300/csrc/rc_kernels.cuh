@@ -95,6 +95,8 @@ struct CGArgs {
 	UNetActsBF unet_bf;
 	const bf16 *unet_wpack;
 	float *zxf, *zyf;        // z = M r
+	float *Zxf, *Zyf;        // box sums of z
+	float *Pxf2, *Pyf2;      // second buffer of the direction's box sums
 	// training samples harvested from the plain FP64 solve; null: none.
 	// Sample q: harv_in[q][L2][2] = (R/s, W), harv_tgt[q][L2] = (X* - X)/s,
 	// harv_s[q] = s (0 marks an unused slot); *harv_count samples stored.
