@@ -794,11 +794,6 @@ __device__ __forceinline__ bool harvest_finish(const CGArgs &a, CGShared &sh, co
 //            taken as Z + beta P (linearity, so no barrier); p.Ap
 //   phase C  e += alpha p, r -= alpha Ap, |r|^2, R = sum r / T
 // with alpha = r.z / p.Ap.  P alternates between two box buffers.
-struct TcState {
-	unsigned char *dsm;  // dynamic shared memory (tensor-core staging, FP32 weights)
-	uint32_t tmem;       // allocated TMEM columns
-	uint32_t phase;      // mbarrier parity
-};
 
 // First layer (2 -> 16, ReLU) at one pixel of sample n, FP32: channel 0 of
 // the input (R) is multiplied by sc (1/s of the component) as it is read.
@@ -822,8 +817,8 @@ __device__ __forceinline__ void e0a_pixel(const float *x0, const float *w, int n
 }
 
 // The network on both components: V (a.unet.out, FP32) from x0.
-__device__ __noinline__ bool precond_network(const CGArgs &a, CGShared &sh, TcState &tc) {
-	float *wsm = reinterpret_cast<float *>(tc.dsm);
+__device__ __noinline__ bool precond_network(const CGArgs &a, CGShared &sh, TcCtx &tc) {
+	float *wsm = reinterpret_cast<float *>(tc.sm);
 	pmark(a, sh, PH_OTHER);
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
@@ -869,8 +864,8 @@ __device__ __noinline__ bool precond_network(const CGArgs &a, CGShared &sh, TcSt
 		// nine tensor-core layers; last layer (FP32, CUDA cores) -> V
 		for(int l = L_E0B; l <= L_D0B; l++) {
 			if(!tc_conv_layer(l, unet_tc_src(l, a.unet_bf), a.unet_wpack + unet_pack_offset(l),
-			                  a.unet_params + unet_bias_offset(l), unet_tc_dst(l, a.unet_bf), 2, L >> unet_layer(l).level,
-			                  tc.dsm, tc.tmem, tc.phase, &a.st->err, ERR_MMA, a.phase_ns ? a.phase_ns + PH_COUNT : nullptr))
+			                  a.unet_params + unet_weight_offset(l), a.unet_params + unet_bias_offset(l),
+			                  unet_tc_dst(l, a.unet_bf), 2, L >> unet_layer(l).level, tc))
 				return false;
 			if(!grid_reduce(a, sh, 0, nullptr)) return false;
 			pmark(a, sh, PH_TC0 + unet_layer(l).level);
@@ -900,50 +895,137 @@ __device__ __noinline__ bool precond_network(const CGArgs &a, CGShared &sh, TcSt
 	return true;
 }
 
+// Warp-cooperative walk over the entries of 32 consecutive box sites: lane l
+// owns site k0 + l (entries [e0, e1) of it); the warp then streams the
+// entries [E0, E1) of its 32 sites in coalesced chunks of 32.  For an entry,
+// `s` is the lane owning its site (found by a five-step search over the
+// lanes' e0), `same[i]` whether the entry 2^i lanes below belongs to the same
+// site and `tail` whether it is the last entry of its site in this chunk;
+// per-site sums are formed by a segmented scan in the chunk and added by the
+// tail lane to the owner's slot of a per-warp accumulator, chunk after chunk,
+// so all sums have a fixed order.
+constexpr int FCG_BATCH = 4;  // chunks whose loads are in flight together
+
+struct SegLane {
+	int s;
+	bool valid, tail;
+	bool same[5];
+};
+
+__device__ __forceinline__ SegLane seg_lane(int e, int E1, int e0) {
+	SegLane g;
+	const int lane = threadIdx.x & 31;
+	g.valid = e < E1;
+	int s = 0;
+#pragma unroll
+	for(int step = 16; step > 0; step >>= 1) {
+		const int v = __shfl_sync(0xffffffffu, e0, s + step);
+		if(v <= e) s += step;
+	}
+	g.s = g.valid ? s : 32;
+#pragma unroll
+	for(int i = 0; i < 5; i++) {
+		const int ks = __shfl_up_sync(0xffffffffu, g.s, 1 << i);
+		g.same[i] = lane >= (1 << i) && ks == g.s;
+	}
+	const int kn = __shfl_down_sync(0xffffffffu, g.s, 1);
+	g.tail = g.valid && (lane == 31 || kn != g.s);
+	return g;
+}
+
+__device__ __forceinline__ float seg_scan(float v, const SegLane &g) {
+#pragma unroll
+	for(int i = 0; i < 5; i++) {
+		const float u = __shfl_up_sync(0xffffffffu, v, 1 << i);
+		if(g.same[i]) v += u;
+	}
+	return v;
+}
+
 // Phase E: z = (r + eta s N4V) / T, Z = S z; r.z, and z.Ap of the previous
-// direction (not on the first sweep) into sh.tot[0..3].
-__device__ __noinline__ bool fcg_phase_e(const CGArgs &a, CGShared &sh, bool first) {
+// direction (not on the first sweep) into sh.tot[0..3].  wacc: 2 x blockDim
+// floats of shared memory.
+__device__ __noinline__ bool fcg_phase_e(const CGArgs &a, CGShared &sh, bool first, float *wacc) {
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
-	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-	const long long gstride = (long long) gridDim.x * blockDim.x;
+	const int lane = threadIdx.x & 31;
+	const long long gwarp = (blockIdx.x * (long long) blockDim.x + threadIdx.x) >> 5;
+	const long long nwarps = ((long long) gridDim.x * blockDim.x) >> 5;
 	const int ax = sh.act[0], ay = sh.act[1];
 	const float es0 = (float) (a.eta * sh.scale[0]), es1 = (float) (a.eta * sh.scale[1]);
 	const float *V = a.unet.out;
 	const float *rx = a.rxf, *ry = a.ryf, *apx = a.apxf, *apy = a.apyf;
 	float *zx = a.zxf, *zy = a.zyf;
 	const int *cov_off = a.cov_off;
+	const int Etot = __ldcg(&cov_off[L2]);
+	float *accx = wacc, *accy = wacc + blockDim.x;
 	float w[4] = {0.f, 0.f, 0.f, 0.f};
-	for(long long k = gtid; k < L2; k += gstride) {
-		const int e0 = cov_off[k], e1 = cov_off[k + 1];
-		float Zx = 0.f, Zy = 0.f;
+	for(long long g = gwarp; g * 32 < L2; g += nwarps) {
+		const long long k = g * 32 + lane;
+		const bool kv = k < L2;
+		const int e0 = kv ? cov_off[k] : Etot, e1 = kv ? cov_off[k + 1] : Etot;
+		float id = 0.f, nvx = 0.f, nvy = 0.f;
 		if(e1 > e0) {
-			const float id = sh.iTf[box_deg(a.cnt, (int) k, L)];
-			if(ax) {
-				const float nv = es0 * box_n4T<float>(V, (int) k, L);
-				for(int e = e0; e < e1; e++) {
-					const float r = rx[e];
-					const float z = id * (r + nv);
-					zx[e] = z;
-					Zx += z;
-					w[0] = __fmaf_rn(r, z, w[0]);
-					if(!first) w[2] = __fmaf_rn(z, apx[e], w[2]);
-				}
+			id = sh.iTf[box_deg(a.cnt, (int) k, L)];
+			if(ax) nvx = es0 * box_n4T<float>(V, (int) k, L);
+			if(ay) nvy = es1 * box_n4T<float>(V + L2, (int) k, L);
+		}
+		accx[threadIdx.x] = 0.f;
+		accy[threadIdx.x] = 0.f;
+		__syncwarp();
+		const int E0 = __shfl_sync(0xffffffffu, e0, 0), E1 = __shfl_sync(0xffffffffu, e1, 31);
+		// chunks in batches of FCG_BATCH: all loads of a batch are issued first
+		for(int c0 = E0; c0 < E1; c0 += 32 * FCG_BATCH) {
+			float r0[FCG_BATCH], q0[FCG_BATCH], r1[FCG_BATCH], q1[FCG_BATCH];
+#pragma unroll
+			for(int u = 0; u < FCG_BATCH; u++) {
+				const int e = c0 + 32 * u + lane;
+				const bool v = e < E1;
+				r0[u] = (v && ax) ? rx[e] : 0.f;
+				q0[u] = (v && ax && !first) ? apx[e] : 0.f;
+				r1[u] = (v && ay) ? ry[e] : 0.f;
+				q1[u] = (v && ay && !first) ? apy[e] : 0.f;
 			}
-			if(ay) {
-				const float nv = es1 * box_n4T<float>(V + L2, (int) k, L);
-				for(int e = e0; e < e1; e++) {
-					const float r = ry[e];
-					const float z = id * (r + nv);
-					zy[e] = z;
-					Zy += z;
-					w[1] = __fmaf_rn(r, z, w[1]);
-					if(!first) w[3] = __fmaf_rn(z, apy[e], w[3]);
+#pragma unroll
+			for(int u = 0; u < FCG_BATCH; u++) {
+				if(c0 + 32 * u >= E1) break;
+				const int e = c0 + 32 * u + lane;
+				const SegLane sg = seg_lane(e, E1, e0);
+				const int src = sg.s & 31;
+				const float ids = __shfl_sync(0xffffffffu, id, src);
+				const int slot = (threadIdx.x & ~31) + src;
+				if(ax) {
+					const float nv = __shfl_sync(0xffffffffu, nvx, src);
+					float z = 0.f;
+					if(sg.valid) {
+						z = ids * (r0[u] + nv);
+						zx[e] = z;
+						w[0] = __fmaf_rn(r0[u], z, w[0]);
+						w[2] = __fmaf_rn(z, q0[u], w[2]);
+					}
+					const float t = seg_scan(z, sg);
+					if(sg.tail) accx[slot] += t;
 				}
+				if(ay) {
+					const float nv = __shfl_sync(0xffffffffu, nvy, src);
+					float z = 0.f;
+					if(sg.valid) {
+						z = ids * (r1[u] + nv);
+						zy[e] = z;
+						w[1] = __fmaf_rn(r1[u], z, w[1]);
+						w[3] = __fmaf_rn(z, q1[u], w[3]);
+					}
+					const float t = seg_scan(z, sg);
+					if(sg.tail) accy[slot] += t;
+				}
+				__syncwarp();
 			}
 		}
-		if(ax) a.Zxf[k] = Zx;
-		if(ay) a.Zyf[k] = Zy;
+		if(kv) {
+			if(ax) a.Zxf[k] = accx[threadIdx.x];
+			if(ay) a.Zyf[k] = accy[threadIdx.x];
+		}
+		__syncwarp();
 	}
 	warp_tree<float, 4>(w);
 	double v[4] = {(double) w[0], (double) w[1], (double) w[2], (double) w[3]};
@@ -954,54 +1036,90 @@ __device__ __noinline__ bool fcg_phase_e(const CGArgs &a, CGShared &sh, bool fir
 // Phase AB: p = z + beta p, box sums into Pn, Ap = T p - eta N4(Pn) with the
 // neighbours' Pn = Z + beta Po; p.Ap into sh.tot[0..1].
 __device__ __noinline__ bool fcg_phase_ab(const CGArgs &a, CGShared &sh, bool first, const float *Pox, const float *Poy,
-                                          float *Pnx, float *Pny) {
+                                          float *Pnx, float *Pny, float *wacc) {
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
-	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-	const long long gstride = (long long) gridDim.x * blockDim.x;
+	const int lane = threadIdx.x & 31;
+	const long long gwarp = (blockIdx.x * (long long) blockDim.x + threadIdx.x) >> 5;
+	const long long nwarps = ((long long) gridDim.x * blockDim.x) >> 5;
 	const int ax = sh.act[0], ay = sh.act[1];
 	const float bx = (float) sh.beta[0], by = (float) sh.beta[1];
 	const float neta = (float) (-a.eta * 1.0);
 	const float *zx = a.zxf, *zy = a.zyf, *Zx = a.Zxf, *Zy = a.Zyf;
 	float *px = a.pxf, *py = a.pyf, *apx = a.apxf, *apy = a.apyf;
 	const int *cov_off = a.cov_off;
+	const int Etot = __ldcg(&cov_off[L2]);
+	float *accx = wacc, *accy = wacc + blockDim.x;
 	float w[2] = {0.f, 0.f};
-	for(long long k = gtid; k < L2; k += gstride) {
-		const int e0 = cov_off[k], e1 = cov_off[k + 1];
-		float sx = 0.f, sy = 0.f;
+	for(long long g = gwarp; g * 32 < L2; g += nwarps) {
+		const long long k = g * 32 + lane;
+		const bool kv = k < L2;
+		const int e0 = kv ? cov_off[k] : Etot, e1 = kv ? cov_off[k + 1] : Etot;
+		float d = 0.f, qx = 0.f, qy = 0.f;
 		if(e1 > e0) {
-			const float d = sh.Tf[box_deg(a.cnt, (int) k, L)];
-			if(ax) {
-				const float n4 = first ? box_n4T<float>(Zx, (int) k, L)
-				                       : __fmaf_rn(bx, box_n4T<float>(Pox, (int) k, L), box_n4T<float>(Zx, (int) k, L));
-				const float q = neta * n4;
-				for(int e = e0; e < e1; e++) {
-					const float z = zx[e];
-					const float p = first ? z : __fmaf_rn(bx, px[e], z);
-					px[e] = p;
-					sx += p;
-					const float ap = __fmaf_rn(d, p, q);
-					apx[e] = ap;
-					w[0] = __fmaf_rn(p, ap, w[0]);
-				}
+			d = sh.Tf[box_deg(a.cnt, (int) k, L)];
+			if(ax) qx = neta * (first ? box_n4T<float>(Zx, (int) k, L)
+			                          : __fmaf_rn(bx, box_n4T<float>(Pox, (int) k, L), box_n4T<float>(Zx, (int) k, L)));
+			if(ay) qy = neta * (first ? box_n4T<float>(Zy, (int) k, L)
+			                          : __fmaf_rn(by, box_n4T<float>(Poy, (int) k, L), box_n4T<float>(Zy, (int) k, L)));
+		}
+		accx[threadIdx.x] = 0.f;
+		accy[threadIdx.x] = 0.f;
+		__syncwarp();
+		const int E0 = __shfl_sync(0xffffffffu, e0, 0), E1 = __shfl_sync(0xffffffffu, e1, 31);
+		for(int c0 = E0; c0 < E1; c0 += 32 * FCG_BATCH) {
+			float z0[FCG_BATCH], p0[FCG_BATCH], z1[FCG_BATCH], p1[FCG_BATCH];
+#pragma unroll
+			for(int u = 0; u < FCG_BATCH; u++) {
+				const int e = c0 + 32 * u + lane;
+				const bool v = e < E1;
+				z0[u] = (v && ax) ? zx[e] : 0.f;
+				p0[u] = (v && ax && !first) ? px[e] : 0.f;
+				z1[u] = (v && ay) ? zy[e] : 0.f;
+				p1[u] = (v && ay && !first) ? py[e] : 0.f;
 			}
-			if(ay) {
-				const float n4 = first ? box_n4T<float>(Zy, (int) k, L)
-				                       : __fmaf_rn(by, box_n4T<float>(Poy, (int) k, L), box_n4T<float>(Zy, (int) k, L));
-				const float q = neta * n4;
-				for(int e = e0; e < e1; e++) {
-					const float z = zy[e];
-					const float p = first ? z : __fmaf_rn(by, py[e], z);
-					py[e] = p;
-					sy += p;
-					const float ap = __fmaf_rn(d, p, q);
-					apy[e] = ap;
-					w[1] = __fmaf_rn(p, ap, w[1]);
+#pragma unroll
+			for(int u = 0; u < FCG_BATCH; u++) {
+				if(c0 + 32 * u >= E1) break;
+				const int e = c0 + 32 * u + lane;
+				const SegLane sg = seg_lane(e, E1, e0);
+				const int src = sg.s & 31;
+				const float ds = __shfl_sync(0xffffffffu, d, src);
+				const int slot = (threadIdx.x & ~31) + src;
+				if(ax) {
+					const float q = __shfl_sync(0xffffffffu, qx, src);
+					float p = 0.f;
+					if(sg.valid) {
+						p = first ? z0[u] : __fmaf_rn(bx, p0[u], z0[u]);
+						px[e] = p;
+						const float ap = __fmaf_rn(ds, p, q);
+						apx[e] = ap;
+						w[0] = __fmaf_rn(p, ap, w[0]);
+					}
+					const float t = seg_scan(p, sg);
+					if(sg.tail) accx[slot] += t;
 				}
+				if(ay) {
+					const float q = __shfl_sync(0xffffffffu, qy, src);
+					float p = 0.f;
+					if(sg.valid) {
+						p = first ? z1[u] : __fmaf_rn(by, p1[u], z1[u]);
+						py[e] = p;
+						const float ap = __fmaf_rn(ds, p, q);
+						apy[e] = ap;
+						w[1] = __fmaf_rn(p, ap, w[1]);
+					}
+					const float t = seg_scan(p, sg);
+					if(sg.tail) accy[slot] += t;
+				}
+				__syncwarp();
 			}
 		}
-		if(ax) Pnx[k] = sx;
-		if(ay) Pny[k] = sy;
+		if(kv) {
+			if(ax) Pnx[k] = accx[threadIdx.x];
+			if(ay) Pny[k] = accy[threadIdx.x];
+		}
+		__syncwarp();
 	}
 	warp_tree<float, 2>(w);
 	double v[2] = {(double) w[0], (double) w[1]};
@@ -1011,43 +1129,85 @@ __device__ __noinline__ bool fcg_phase_ab(const CGArgs &a, CGShared &sh, bool fi
 
 // Phase C: e += alpha p, r -= alpha Ap, |r|^2 into sh.tot[0..1]; the next
 // network input R = sum over the site's unknowns of r / T (unscaled).
-__device__ __noinline__ bool fcg_phase_c(const CGArgs &a, CGShared &sh) {
+__device__ __noinline__ bool fcg_phase_c(const CGArgs &a, CGShared &sh, float *wacc) {
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
-	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-	const long long gstride = (long long) gridDim.x * blockDim.x;
+	const int lane = threadIdx.x & 31;
+	const long long gwarp = (blockIdx.x * (long long) blockDim.x + threadIdx.x) >> 5;
+	const long long nwarps = ((long long) gridDim.x * blockDim.x) >> 5;
 	const int ax = sh.act[0], ay = sh.act[1];
 	const float alx = (float) sh.alpha[0], aly = (float) sh.alpha[1];
 	const float *px = a.pxf, *py = a.pyf, *apx = a.apxf, *apy = a.apyf;
 	float *ex = a.exf, *ey = a.eyf, *rx = a.rxf, *ry = a.ryf, *x0 = a.unet.x0;
 	const int *cov_off = a.cov_off;
+	const int Etot = __ldcg(&cov_off[L2]);
+	float *accx = wacc, *accy = wacc + blockDim.x;
 	float w[2] = {0.f, 0.f};
-	for(long long k = gtid; k < L2; k += gstride) {
-		const int e0 = cov_off[k], e1 = cov_off[k + 1];
-		if(e1 == e0) continue;
-		const float id = sh.iTf[box_deg(a.cnt, (int) k, L)];
-		if(ax) {
-			float R = 0.f;
-			for(int e = e0; e < e1; e++) {
-				ex[e] = __fmaf_rn(alx, px[e], ex[e]);
-				const float r = __fmaf_rn(-alx, apx[e], rx[e]);
-				rx[e] = r;
-				w[0] = __fmaf_rn(r, r, w[0]);
-				R += r * id;
+	for(long long g = gwarp; g * 32 < L2; g += nwarps) {
+		const long long k = g * 32 + lane;
+		const bool kv = k < L2;
+		const int e0 = kv ? cov_off[k] : Etot, e1 = kv ? cov_off[k + 1] : Etot;
+		const float id = (e1 > e0) ? sh.iTf[box_deg(a.cnt, (int) k, L)] : 0.f;
+		accx[threadIdx.x] = 0.f;
+		accy[threadIdx.x] = 0.f;
+		__syncwarp();
+		const int E0 = __shfl_sync(0xffffffffu, e0, 0), E1 = __shfl_sync(0xffffffffu, e1, 31);
+		for(int c0 = E0; c0 < E1; c0 += 32 * FCG_BATCH) {
+			float e0v[FCG_BATCH], p0[FCG_BATCH], r0[FCG_BATCH], q0[FCG_BATCH];
+			float e1v[FCG_BATCH], p1[FCG_BATCH], r1[FCG_BATCH], q1[FCG_BATCH];
+#pragma unroll
+			for(int u = 0; u < FCG_BATCH; u++) {
+				const int e = c0 + 32 * u + lane;
+				const bool v = e < E1;
+				e0v[u] = (v && ax) ? ex[e] : 0.f;
+				p0[u] = (v && ax) ? px[e] : 0.f;
+				r0[u] = (v && ax) ? rx[e] : 0.f;
+				q0[u] = (v && ax) ? apx[e] : 0.f;
+				e1v[u] = (v && ay) ? ey[e] : 0.f;
+				p1[u] = (v && ay) ? py[e] : 0.f;
+				r1[u] = (v && ay) ? ry[e] : 0.f;
+				q1[u] = (v && ay) ? apy[e] : 0.f;
 			}
-			x0[k * 2] = R;
-		}
-		if(ay) {
-			float R = 0.f;
-			for(int e = e0; e < e1; e++) {
-				ey[e] = __fmaf_rn(aly, py[e], ey[e]);
-				const float r = __fmaf_rn(-aly, apy[e], ry[e]);
-				ry[e] = r;
-				w[1] = __fmaf_rn(r, r, w[1]);
-				R += r * id;
+#pragma unroll
+			for(int u = 0; u < FCG_BATCH; u++) {
+				if(c0 + 32 * u >= E1) break;
+				const int e = c0 + 32 * u + lane;
+				const SegLane sg = seg_lane(e, E1, e0);
+				const int src = sg.s & 31;
+				const float ids = __shfl_sync(0xffffffffu, id, src);
+				const int slot = (threadIdx.x & ~31) + src;
+				if(ax) {
+					float rv = 0.f;
+					if(sg.valid) {
+						ex[e] = __fmaf_rn(alx, p0[u], e0v[u]);
+						const float r = __fmaf_rn(-alx, q0[u], r0[u]);
+						rx[e] = r;
+						w[0] = __fmaf_rn(r, r, w[0]);
+						rv = r * ids;
+					}
+					const float t = seg_scan(rv, sg);
+					if(sg.tail) accx[slot] += t;
+				}
+				if(ay) {
+					float rv = 0.f;
+					if(sg.valid) {
+						ey[e] = __fmaf_rn(aly, p1[u], e1v[u]);
+						const float r = __fmaf_rn(-aly, q1[u], r1[u]);
+						ry[e] = r;
+						w[1] = __fmaf_rn(r, r, w[1]);
+						rv = r * ids;
+					}
+					const float t = seg_scan(rv, sg);
+					if(sg.tail) accy[slot] += t;
+				}
+				__syncwarp();
 			}
-			x0[(L2 + k) * 2] = R;
 		}
+		if(kv) {
+			if(ax) x0[k * 2] = accx[threadIdx.x];
+			if(ay) x0[(L2 + k) * 2] = accy[threadIdx.x];
+		}
+		__syncwarp();
 	}
 	warp_tree<float, 2>(w);
 	double v[2] = {(double) w[0], (double) w[1]};
@@ -1059,7 +1219,7 @@ __device__ __noinline__ bool fcg_phase_c(const CGArgs &a, CGShared &sh) {
 // preconditioned by the network; r and e in cover order (rxf, exf ...) and
 // the network input x0 as true_residual(RES_FLOAT_COVER) leaves them.  Stops
 // a component at |r|^2 < thr.
-__device__ __noinline__ bool fcg_iterate(const CGArgs &a, CGShared &sh, TcState &tc, long long max_it) {
+__device__ __noinline__ bool fcg_iterate(const CGArgs &a, CGShared &sh, TcCtx &tc, long long max_it) {
 	const long long S = a.st->S;
 	for(int d = threadIdx.x; d <= CG_MAX_D; d += blockDim.x) {
 		sh.Tf[d] = (float) sh.T[d];
@@ -1074,7 +1234,7 @@ __device__ __noinline__ bool fcg_iterate(const CGArgs &a, CGShared &sh, TcState 
 	int par = 0;
 	while(sh.act[0] || sh.act[1]) {
 		if(!precond_network(a, sh, tc)) return false;
-		if(!fcg_phase_e(a, sh, first)) return false;
+		if(!fcg_phase_e(a, sh, first, reinterpret_cast<float *>(tc.sm))) return false;
 		pmark(a, sh, PH_Z);
 		if(threadIdx.x == 0) {
 			for(int c = 0; c < 2; c++) {
@@ -1086,7 +1246,7 @@ __device__ __noinline__ bool fcg_iterate(const CGArgs &a, CGShared &sh, TcState 
 		__syncthreads();
 		float *Pox = par ? a.Pxf2 : a.Pxf, *Poy = par ? a.Pyf2 : a.Pyf;
 		float *Pnx = par ? a.Pxf : a.Pxf2, *Pny = par ? a.Pyf : a.Pyf2;
-		if(!fcg_phase_ab(a, sh, first, Pox, Poy, Pnx, Pny)) return false;
+		if(!fcg_phase_ab(a, sh, first, Pox, Poy, Pnx, Pny, reinterpret_cast<float *>(tc.sm))) return false;
 		pmark(a, sh, PH_AB);
 		if(threadIdx.x == 0) {
 			for(int c = 0; c < 2; c++) {
@@ -1096,7 +1256,7 @@ __device__ __noinline__ bool fcg_iterate(const CGArgs &a, CGShared &sh, TcState 
 			}
 		}
 		__syncthreads();
-		if(!fcg_phase_c(a, sh)) return false;
+		if(!fcg_phase_c(a, sh, reinterpret_cast<float *>(tc.sm))) return false;
 		pmark(a, sh, PH_C);
 		if(threadIdx.x == 0) {
 			for(int c = 0; c < 2; c++) {
@@ -1115,7 +1275,7 @@ __device__ __noinline__ bool fcg_iterate(const CGArgs &a, CGShared &sh, TcState 
 }
 
 template<bool LEARNED>
-__device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcState &tc) {
+__device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcCtx &tc) {
 	const long long S = a.st->S;
 	const int cold = a.st->cg_cold;
 	const double eta = a.eta;
@@ -1263,7 +1423,7 @@ template<bool LEARNED>
 __global__ void __launch_bounds__(CG_THREADS, LEARNED ? 1 : 2) cg_kernel(const __grid_constant__ CGArgs a) {
 	__shared__ CGShared sh;
 	extern __shared__ __align__(1024) unsigned char dsm[];
-	TcState tc{dsm, 0u, 0u};
+	TcCtx tc{dsm, 0u, {0u, 0u}, &a.st->err, ERR_MMA, a.phase_ns ? a.phase_ns + PH_COUNT : nullptr};
 	if(threadIdx.x == 0) {
 		sh.epoch = 0u;
 		sh.fail = 0;
@@ -1274,7 +1434,10 @@ __global__ void __launch_bounds__(CG_THREADS, LEARNED ? 1 : 2) cg_kernel(const _
 		if(a.unet_tc) {
 			uint32_t *hold = reinterpret_cast<uint32_t *>(dsm + TC_HOLD_OFF);
 			if(threadIdx.x < 32) tc_alloc(hold, TC_COLS);
-			if(threadIdx.x == 0) mbar_init(reinterpret_cast<uint64_t *>(dsm + TC_MBAR_OFF), 1);
+			if(threadIdx.x == 0) {
+				mbar_init(reinterpret_cast<uint64_t *>(dsm + TC_MBAR_OFF), 1);
+				mbar_init(reinterpret_cast<uint64_t *>(dsm + TC_MBAR_OFF) + 1, 1);
+			}
 			tc_fence_before();
 			__syncthreads();
 			tc_fence_after();
@@ -1302,6 +1465,9 @@ int cg_grid_blocks(int device, bool learned) {
 	else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cg_kernel<false>, CG_THREADS, 0);
 	if(per_sm < 1) per_sm = 1;
 	if(per_sm > 2) per_sm = 2;
+	// the learned solve holds all of an SM's TMEM columns: one CTA per SM, or
+	// a second CTA would wait in its allocation for one that waits for it
+	if(learned) per_sm = 1;
 	const int blocks = sms * per_sm;
 	return blocks < 2048 ? blocks : 2048;  // partial sums: 2 x 8 x blocks doubles
 }

@@ -430,23 +430,26 @@ __global__ void pack_bf16_kernel(const float *params, bf16 *packed) {
 	}
 }
 
-__global__ void __launch_bounds__(512) tc_layer_kernel(int l, TcSrc src, const bf16 *packed, const float *params,
-                                                        bf16 *dst, int batch, int L, int *err) {
+// One CTA per SM (the TMEM allocation is the whole of an SM's 512 columns).
+__global__ void __launch_bounds__(512, 1) tc_layer_kernel(int l, TcSrc src, const bf16 *packed, const float *params,
+                                                           bf16 *dst, int batch, int L, int *err) {
 	extern __shared__ __align__(1024) unsigned char tsm[];
 	uint32_t *hold = reinterpret_cast<uint32_t *>(tsm + TC_HOLD_OFF);
 	uint64_t *mbar = reinterpret_cast<uint64_t *>(tsm + TC_MBAR_OFF);
 	if(threadIdx.x < 32) tc_alloc(hold, TC_COLS);
-	if(threadIdx.x == 0) mbar_init(mbar, 1);
+	if(threadIdx.x == 0) {
+		mbar_init(mbar, 1);
+		mbar_init(mbar + 1, 1);
+	}
 	tc_fence_before();
 	__syncthreads();
 	tc_fence_after();
-	const uint32_t tmem = *hold;
-	uint32_t phase = 0;
-	tc_conv_layer(l, src, packed + unet_pack_offset(l), params + unet_bias_offset(l), dst, batch, L, tsm, tmem, phase, err,
-	              1, nullptr);
+	TcCtx c{tsm, *hold, {0u, 0u}, err, 1, nullptr};
+	tc_conv_layer(l, src, packed + unet_pack_offset(l), params + unet_weight_offset(l), params + unet_bias_offset(l), dst,
+	              batch, L, c);
 	tc_fence_before();
 	__syncthreads();
-	if(threadIdx.x < 32) tc_dealloc(tmem, TC_COLS);
+	if(threadIdx.x < 32) tc_dealloc(c.tmem, TC_COLS);
 }
 
 __global__ void e0a_kernel(const float *x0, const float *params, bf16 *dst, int batch, int L) {
@@ -480,7 +483,7 @@ void unet_tc_forward(const float *params, const bf16 *packed, const float *x0, c
 	for(int l = L_E0B; l <= L_D0B; l++) {
 		const int Ll = L >> unet_layer(l).level;
 		const long long tiles = ((long long) batch * Ll * Ll + 127) / 128;
-		long long g = (tiles + TC_RT - 1) / TC_RT;
+		long long g = tiles;
 		if(g > sms) g = sms;
 		tc_layer_kernel<<<(int) g, 512, TC_SMEM, s>>>(l, unet_tc_src(l, A), packed, params, unet_tc_dst(l, A), batch, Ll,
 		                                              err);

@@ -70,22 +70,59 @@ __host__ __device__ constexpr int unet_pack_offset(int l) {
 }
 constexpr int UNET_PACKED = unet_pack_offset(UNET_LAYERS);
 
-constexpr int TC_RT = 2;       // tiles (of 128 pixels) per round, gathered operands
-constexpr int TC_RT_ROWS = 4;  // tiles per round, row-halo operands
-constexpr int TC_COLS = 64;    // TMEM columns: up to TC_RT_ROWS accumulators of 16
-constexpr int TC_HALO = 130;   // staged positions per row: 128 pixels and a periodic neighbour on each side
+// Shared memory and TMEM of the tensor-core layers.
+//
+// Strip mode (level side a multiple of 128): a CTA streams the rows of a
+// column strip of T tiles of 128 pixels.  Each staged input row rho (its
+// W = 128 T pixels plus the periodic neighbour on either side, channel
+// chunks of 8 in planes [kc][position]) is consumed by 3 x KS MMAs per tile,
+// one per horizontal tap dx (the A descriptor shifted by dx) and channel
+// pair: A = 128 pixels x 16 channels, B = the three vertical taps' weights
+// stacked along N (N = 48: dy = +1, 0, -1), D = the accumulators of output
+// rows rho - 1, rho, rho + 1, which sit in consecutive 16-column slots of a
+// ring of R = 32 / T slots per tile in TMEM.  An output row is complete once
+// input row + 1 has been multiplied; the epilogue reads it, writes BF16
+// (bias, ReLU) and zeroes the slot for reuse.  Rows are pipelined: the MMAs
+// of input row i run while output row i - 3 is written out and input row
+// i + 1 is staged.  An MMA is costed by the tensor core at about the same
+// time whatever N is (16 to 256), so stacking the vertical taps along N cuts
+// the instruction count threefold against one MMA per tap.
+//
+// Gather mode (other sides, small levels only): each tap's operand is
+// gathered pixel by pixel for one tile of 128 pixels (K-major A), nine taps
+// times KC/2 MMAs of N = 16 into one accumulator.
+constexpr int TC_RT = 1;        // gather mode: tiles per round
+constexpr int TC_STRIP_T = 4;   // strip mode: at most 4 tiles (512 pixels) per strip
+constexpr int TC_COLS = 512;    // TMEM columns: T x R slots of 16
+constexpr int TC_HW_MAX = TC_STRIP_T * 128 + 2;
 constexpr size_t TC_A_GATHER = (size_t) TC_RT * 9 * 4 * 128 * 16;
-constexpr size_t TC_A_ROWS = (size_t) TC_RT_ROWS * 4 * 3 * TC_HALO * 16;
-constexpr size_t TC_A_BYTES = TC_A_GATHER > TC_A_ROWS ? TC_A_GATHER : TC_A_ROWS;
+constexpr size_t TC_A_STRIP = (size_t) 2 * 4 * TC_HW_MAX * 16;  // two input-row buffers, up to 4 channel chunks
+constexpr size_t TC_A_BYTES = TC_A_GATHER > TC_A_STRIP ? TC_A_GATHER : TC_A_STRIP;
 constexpr size_t TC_B_OFF = TC_A_BYTES;
-constexpr size_t TC_B_BYTES = 9 * 4 * 16 * 16;
+constexpr size_t TC_B_BYTES = 9 * 4 * 16 * 16;  // either layout: 9 taps x 32 channels x 16 outputs, BF16
 constexpr size_t TC_BIAS_OFF = TC_B_OFF + TC_B_BYTES;
-constexpr size_t TC_TILE_OFF = TC_BIAS_OFF + 64;        // per-tile (n, y, x0), row mode
-constexpr size_t TC_MBAR_OFF = TC_TILE_OFF + 16 * TC_RT_ROWS;
-constexpr size_t TC_HOLD_OFF = TC_MBAR_OFF + 8;
-constexpr size_t TC_SMEM = TC_HOLD_OFF + 8;
+constexpr size_t TC_MBAR_OFF = TC_BIAS_OFF + 64;  // two mbarriers
+constexpr size_t TC_HOLD_OFF = TC_MBAR_OFF + 16;
+constexpr size_t TC_SMEM = TC_HOLD_OFF + 16;
 constexpr uint32_t TC_IDESC = tc_idesc_bf16(128, 16);
+constexpr uint32_t TC_IDESC32 = tc_idesc_bf16(128, 32);
+constexpr uint32_t TC_IDESC48 = tc_idesc_bf16(128, 48);
 constexpr long long TC_WAIT_LIMIT = 2000000;  // mbarrier polls (each a bounded hardware wait)
+
+// Per-CTA state of the tensor-core layers: shared memory (TC_SMEM bytes,
+// the two mbarriers at TC_MBAR_OFF initialised with count 1), the TMEM
+// allocation (TC_COLS columns) and the parities the mbarriers wait for next.
+// err/err_bit: where a wait that ran out is recorded.  tns (diagnostics, may
+// be null): block 0 adds the time of weight staging, operand staging, MMA
+// completion waits and the epilogue to tns[0..3].
+struct TcCtx {
+	unsigned char *sm;
+	uint32_t tmem;
+	uint32_t phase[2];
+	int *err;
+	int err_bit;
+	unsigned long long *tns;
+};
 
 __device__ __forceinline__ float2 bf2f(uint32_t u) {
 	__nv_bfloat162 h = *reinterpret_cast<__nv_bfloat162 *>(&u);
@@ -128,223 +165,300 @@ __device__ __forceinline__ uint4 tc_load_chunk(const TcSrc &s, int ci, int n, in
 	return *reinterpret_cast<const uint4 *>(s.b + ((size_t) (n * L + i) * L + j) * 16 + (kc - 2) * 8);
 }
 
-// Row-mode operand staging of nt tiles (KC = input channels / 8): chunk
-// c = r * RB + (kc * 3 + row) * TC_HALO + pos holds channels 8 kc .. of input
-// pixel (n, y + row - 1, x0 + pos - 1) of tile r (coordinates in tile[r]).
-template<int KC>
-__device__ __forceinline__ void tc_stage_rows(const TcSrc &src, const int4 *tile, int nt, int L, uint4 *As) {
-	constexpr int RB = KC * 3 * TC_HALO;
-	const int nchunk = nt * RB;
+// Source of input chunk kc of pixel (n, i, j) for a plain copy (direct and
+// up-sampled/concatenated inputs).
+__device__ __forceinline__ const bf16 *tc_chunk_ptr(const TcSrc &s, int ci, int n, int i, int j, int L, int kc) {
+	if(s.mode == IN_DIRECT) return s.a + ((size_t) (n * L + i) * L + j) * ci + kc * 8;
+	if(kc < 2) return s.a + ((size_t) (n * (L / 2) + i / 2) * (L / 2) + j / 2) * 16 + kc * 8;
+	return s.b + ((size_t) (n * L + i) * L + j) * 16 + (kc - 2) * 8;
+}
+
+// Stage input row `row` of sample n, pixels x0 - 1 .. x0 + W (periodic), into
+// buf[kc * HW + position] (HW = W + 2).  Consecutive threads take
+// consecutive 16-byte chunks of global memory (kc fastest).  Plain inputs go
+// by cp.async (the caller waits); pooled inputs are averaged in registers.
+__device__ __forceinline__ void tc_stage_strip_row(const TcSrc &src, int KC, int n, int row, int x0, int HW, int L, uint4 *buf) {
+	const int nchunk = KC * HW;
 	if(src.mode != IN_POOL) {
 		for(int c = threadIdx.x; c < nchunk; c += blockDim.x) {
-			const int r = c / RB, rem = c - r * RB;
-			const int kc = rem / (3 * TC_HALO), rem2 = rem - kc * (3 * TC_HALO);
-			const int row = rem2 / TC_HALO, pos = rem2 - row * TC_HALO;
-			const int4 tl = tile[r];
-			const int ii = wrap(tl.y + row - 1, L), jj = wrap(tl.z + pos - 1, L);
-			const bf16 *g;
-			if(src.mode == IN_DIRECT) g = src.a + ((size_t) (tl.x * L + ii) * L + jj) * (KC * 8) + kc * 8;
-			else if(kc < 2) g = src.a + ((size_t) (tl.x * (L / 2) + ii / 2) * (L / 2) + jj / 2) * 16 + kc * 8;
-			else g = src.b + ((size_t) (tl.x * L + ii) * L + jj) * 16 + (kc - 2) * 8;
-			cp_async16(As + c, g, 16u);
+			const int pos = c / KC, kc = c - pos * KC;
+			const int x = wrap(x0 - 1 + pos, L);
+			cp_async16(buf + kc * HW + pos, tc_chunk_ptr(src, KC * 8, n, row, x, L, kc), 16u);
 		}
-		cp_async_wait_all();
 	}
 	else {
-		for(int c0 = threadIdx.x; c0 < nchunk; c0 += 3 * blockDim.x) {
-			uint4 v[3];
-#pragma unroll
-			for(int u = 0; u < 3; u++) {
-				const int c = c0 + u * blockDim.x;
-				v[u] = make_uint4(0u, 0u, 0u, 0u);
-				if(c < nchunk) {
-					const int r = c / RB, rem = c - r * RB;
-					const int kc = rem / (3 * TC_HALO), rem2 = rem - kc * (3 * TC_HALO);
-					const int row = rem2 / TC_HALO, pos = rem2 - row * TC_HALO;
-					const int4 tl = tile[r];
-					v[u] = tc_load_chunk(src, KC * 8, tl.x, wrap(tl.y + row - 1, L), wrap(tl.z + pos - 1, L), L, kc);
-				}
-			}
-#pragma unroll
-			for(int u = 0; u < 3; u++) {
-				const int c = c0 + u * blockDim.x;
-				if(c < nchunk) As[c] = v[u];
-			}
+		for(int c = threadIdx.x; c < nchunk; c += blockDim.x) {
+			const int pos = c / KC, kc = c - pos * KC;
+			buf[kc * HW + pos] = tc_load_chunk(src, KC * 8, n, row, wrap(x0 - 1 + pos, L), L, kc);
 		}
 	}
 }
 
-// One tensor-core layer (ci = 16 or 32 -> 16 channels, ReLU) over all
-// 128-pixel tiles of `batch` samples at side L.  Tile t is pixels
-// [128 t, 128 t + 128) in (sample, row, column) order.  When L is a multiple
-// of 128 a tile is a row segment: its three input rows, each with the
-// periodic neighbour on either side (130 positions), are staged once, and the
-// nine taps are nine shifted descriptors into them (TC_RT_ROWS tiles per
-// round).  Otherwise each tap's operand is gathered pixel by pixel (TC_RT
-// tiles per round).  sm: TC_SMEM bytes of shared memory (mbarrier at TC_MBAR_OFF
-// initialised with count 1), tmem: TC_COLS allocated columns, phase: the
-// mbarrier's current parity (advanced here).  Returns false (and sets
-// *err |= err_bit) if an MMA completion wait ran out; the caller then stops.
-// tns (diagnostics, may be null): block 0 adds the time of weight staging,
-// operand staging, MMA issue and completion, and the epilogue to tns[0..3].
-static __device__ __noinline__ bool tc_conv_layer(int l, const TcSrc &src, const bf16 *wpack, const float *bias, bf16 *dst,
-                                                  int batch, int L, unsigned char *sm, uint32_t tmem, uint32_t &phase, int *err,
-                                                  int err_bit, unsigned long long *tns) {
-	const bool timed = tns && blockIdx.x == 0 && threadIdx.x == 0;
-	unsigned long long tm = 0;
-	if(timed) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(tm));
-	auto mark = [&](int k) {
-		if(timed) {
-			unsigned long long t;
-			asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-			tns[k] += t - tm;
-			tm = t;
+// 16 consecutive TMEM columns of this thread's lane set to zero.
+__device__ __forceinline__ void tc_st16_zero(uint32_t taddr) {
+	const uint32_t z = 0u;
+	asm volatile(
+	    "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1};" ::"r"(
+	        taddr),
+	    "r"(z)
+	    : "memory");
+}
+__device__ __forceinline__ void tc_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+// Bias, ReLU and BF16 conversion of one pixel's 16 accumulators; 32-byte store.
+__device__ __forceinline__ void tc_store_pixel(const float (&v)[16], const float *bs, bf16 *dst, long long P) {
+	uint4 o0, o1;
+	o0.x = f2bf(fmaxf(v[0] + bs[0], 0.f), fmaxf(v[1] + bs[1], 0.f));
+	o0.y = f2bf(fmaxf(v[2] + bs[2], 0.f), fmaxf(v[3] + bs[3], 0.f));
+	o0.z = f2bf(fmaxf(v[4] + bs[4], 0.f), fmaxf(v[5] + bs[5], 0.f));
+	o0.w = f2bf(fmaxf(v[6] + bs[6], 0.f), fmaxf(v[7] + bs[7], 0.f));
+	o1.x = f2bf(fmaxf(v[8] + bs[8], 0.f), fmaxf(v[9] + bs[9], 0.f));
+	o1.y = f2bf(fmaxf(v[10] + bs[10], 0.f), fmaxf(v[11] + bs[11], 0.f));
+	o1.z = f2bf(fmaxf(v[12] + bs[12], 0.f), fmaxf(v[13] + bs[13], 0.f));
+	o1.w = f2bf(fmaxf(v[14] + bs[14], 0.f), fmaxf(v[15] + bs[15], 0.f));
+	uint4 *o = reinterpret_cast<uint4 *>(dst + P * 16);
+	o[0] = o0;
+	o[1] = o1;
+}
+
+struct TcTimer {
+	bool on;
+	unsigned long long t;
+	unsigned long long *tns;
+	__device__ __forceinline__ TcTimer(unsigned long long *p) : on(p && blockIdx.x == 0 && threadIdx.x == 0), t(0), tns(p) {
+		if(on) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+	}
+	__device__ __forceinline__ void mark(int k) {
+		if(on) {
+			unsigned long long u;
+			asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(u));
+			tns[k] += u - t;
+			t = u;
 		}
-	};
+	}
+};
+
+// Strip mode (L a multiple of 128); requires 512 threads.  wl: the layer's
+// FP32 weights [tap = (dy + 1) * 3 + dx + 1][ci][16]; bias: 16 FP32.
+static __device__ __noinline__ bool tc_conv_strip(int l, const TcSrc &src, const float *wl, const float *bias, bf16 *dst,
+                                                  int batch, int L, TcCtx &c) {
+	TcTimer tm(c.tns);
+	const UNetLayerDesc d = unet_layer(l);
+	const int KC = d.ci / 8, KS = KC / 2;
+	const int ntile = L / 128;
+	int T = TC_STRIP_T;
+	while(ntile % T) T >>= 1;
+	const int R = TC_COLS / 16 / T;  // accumulator slots per tile
+	const int W = T * 128, HW = W + 2;
+	const int NS = ntile / T;
+	const long long U = (long long) batch * NS * L;  // (sample, strip, row) units
+	uint4 *Abuf = reinterpret_cast<uint4 *>(c.sm);
+	bf16 *Bh = reinterpret_cast<bf16 *>(c.sm + TC_B_OFF);
+	float *bs = reinterpret_cast<float *>(c.sm + TC_BIAS_OFF);
+	uint64_t *mbar = reinterpret_cast<uint64_t *>(c.sm + TC_MBAR_OFF);
+	__syncthreads();  // the previous user of the shared buffers is done
+	// B of (dx, channel pair ks): rows n = 16 j + co hold the weights of
+	// dy = 1 - j; K-major core matrices, LBO 768 B (K halves), SBO 128 B
+	const int nB = 3 * KS * 2 * 48 * 8;
+	for(int idx = threadIdx.x; idx < nB; idx += blockDim.x) {
+		const int e = idx & 7, rest = idx >> 3;
+		const int n = rest % 48, hq = rest / 48;
+		const int h = hq & 1, q = hq >> 1;
+		const int ks = q % KS, dxi = q / KS;
+		const int j = n >> 4, co = n & 15;
+		const int t = (2 - j) * 3 + dxi;
+		Bh[idx] = __float2bfloat16_rn(wl[(t * d.ci + 16 * ks + 8 * h + e) * 16 + co]);
+	}
+	if(threadIdx.x < 16) bs[threadIdx.x] = bias[threadIdx.x];
+	fence_async_smem();
+	__syncthreads();
+	tm.mark(0);
+	const uint32_t a_base = smem_u32(Abuf), b_base = smem_u32(Bh);
+	const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const long long per = (U + gridDim.x - 1) / gridDim.x;
+	const long long u0 = blockIdx.x * per, u1 = u0 + per < U ? u0 + per : U;
+	for(long long u = u0; u < u1;) {
+		const long long col = u / L;
+		const int y0 = (int) (u - col * L);
+		const int y1 = (int) ((u1 - col * L) < L ? (u1 - col * L) : L);  // exclusive
+		const int n = (int) (col / NS), x0 = (int) (col - (long long) n * NS) * W;
+		const int nin = y1 - y0 + 2;  // input rows y0 - 1 .. y1
+		// all slots of this CTA's tiles zero; first input row staged
+		for(int pr = w; pr < T * 4; pr += 16) {
+			const int r = pr >> 2, q = pr & 3;
+			for(int sl = 0; sl < R; sl++) tc_st16_zero(c.tmem + ((uint32_t) (32 * q) << 16) + (uint32_t) ((r * R + sl) * 16));
+		}
+		tc_wait_st();
+		tc_stage_strip_row(src, KC, n, wrap(y0 - 1, L), x0, HW, L, Abuf);
+		cp_async_wait_all();
+		fence_async_smem();
+		tc_fence_before();
+		__syncthreads();
+		tc_fence_after();
+		tm.mark(1);
+		for(int i = 0; i <= nin; i++) {
+			// MMAs of input row y0 - 1 + i (buffer i & 1) into the slots of
+			// output rows y0 - 2 + i .. y0 + i
+			if(i < nin && threadIdx.x == 0) {
+				const uint32_t abuf = a_base + (uint32_t) ((i & 1) * KC * HW * 16);
+				const int s0 = i % R;
+				for(int r = 0; r < T; r++) {
+					const uint32_t dcol = c.tmem + (uint32_t) (r * R * 16);
+					for(int dxi = 0; dxi < 3; dxi++) {
+						for(int ks = 0; ks < KS; ks++) {
+							const uint64_t ad = tc_sdesc(abuf + (uint32_t) (((2 * ks) * HW + r * 128 + dxi) * 16), (uint32_t) (HW * 16), 128);
+							const uint32_t bq = b_base + (uint32_t) ((dxi * KS + ks) * 1536);
+							if(s0 + 2 < R) tc_mma(dcol + (uint32_t) (s0 * 16), ad, tc_sdesc(bq, 768, 128), TC_IDESC48, 1u);
+							else if(s0 == R - 2) {
+								tc_mma(dcol + (uint32_t) (s0 * 16), ad, tc_sdesc(bq, 768, 128), TC_IDESC32, 1u);
+								tc_mma(dcol, ad, tc_sdesc(bq + 512, 768, 128), TC_IDESC, 1u);
+							}
+							else {
+								tc_mma(dcol + (uint32_t) (s0 * 16), ad, tc_sdesc(bq, 768, 128), TC_IDESC, 1u);
+								tc_mma(dcol, ad, tc_sdesc(bq + 256, 768, 128), TC_IDESC32, 1u);
+							}
+						}
+					}
+				}
+				tc_commit(&mbar[i & 1]);
+			}
+			bool fail = false;
+			if(i >= 1) {
+				// MMAs of input row i - 1 done: its buffer is free and output
+				// row y0 - 3 + i is complete
+				const int b = (i - 1) & 1;
+				fail = !mbar_wait(&mbar[b], c.phase[b], TC_WAIT_LIMIT);
+				c.phase[b] ^= 1u;
+				tc_fence_after();
+			}
+			tm.mark(2);
+			if(!fail && i + 1 < nin)
+				tc_stage_strip_row(src, KC, n, wrap(y0 + i, L), x0, HW, L, Abuf + ((i + 1) & 1) * KC * HW);
+			if(!fail && i >= 1) {
+				const int y = y0 - 3 + i, sl = (i - 1) % R;
+				for(int pr = w; pr < T * 4; pr += 16) {
+					const int r = pr >> 2, q = pr & 3;
+					const uint32_t ta = c.tmem + ((uint32_t) (32 * q) << 16) + (uint32_t) ((r * R + sl) * 16);
+					if(y >= y0) {
+						float v[16];
+						tc_ld16(ta, v);
+						tc_store_pixel(v, bs, dst, ((long long) n * L + y) * L + x0 + r * 128 + 32 * q + lane);
+					}
+					tc_st16_zero(ta);
+				}
+				tc_wait_st();
+			}
+			tm.mark(3);
+			cp_async_wait_all();
+			fence_async_smem();
+			tc_fence_before();
+			if(__syncthreads_or(fail)) {
+				// let the MMAs in flight finish before giving up
+				if(threadIdx.x == 0) atomicOr(c.err, c.err_bit);
+				mbar_wait(&mbar[i & 1], c.phase[i & 1], TC_WAIT_LIMIT);
+				return false;
+			}
+			tc_fence_after();
+			tm.mark(1);
+		}
+		u += y1 - y0;
+	}
+	return true;
+}
+
+// Gather mode: one tile of 128 pixels per round, operands gathered pixel by
+// pixel; wpack: the layer's packed BF16 weights [tap][kc][co][8].
+static __device__ __noinline__ bool tc_conv_gather(int l, const TcSrc &src, const bf16 *wpack, const float *bias, bf16 *dst,
+                                                   int batch, int L, TcCtx &c) {
+	TcTimer tm(c.tns);
 	const UNetLayerDesc d = unet_layer(l);
 	const int KC = d.ci / 8;
 	const long long npix = (long long) batch * L * L;
 	const long long ntiles = (npix + 127) / 128;
-	uint4 *As = reinterpret_cast<uint4 *>(sm);
-	uint4 *Bs = reinterpret_cast<uint4 *>(sm + TC_B_OFF);
-	float *bs = reinterpret_cast<float *>(sm + TC_BIAS_OFF);
-	uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + TC_MBAR_OFF);
-	__syncthreads();  // the previous user of the shared buffers is done
-	for(int c = threadIdx.x; c < 9 * KC * 16; c += blockDim.x) Bs[c] = reinterpret_cast<const uint4 *>(wpack)[c];
+	uint4 *As = reinterpret_cast<uint4 *>(c.sm);
+	uint4 *Bs = reinterpret_cast<uint4 *>(c.sm + TC_B_OFF);
+	float *bs = reinterpret_cast<float *>(c.sm + TC_BIAS_OFF);
+	uint64_t *mbar = reinterpret_cast<uint64_t *>(c.sm + TC_MBAR_OFF);
+	__syncthreads();
+	for(int k = threadIdx.x; k < 9 * KC * 16; k += blockDim.x) Bs[k] = reinterpret_cast<const uint4 *>(wpack)[k];
 	if(threadIdx.x < 16) bs[threadIdx.x] = bias[threadIdx.x];
 	const uint32_t a_base = smem_u32(As), b_base = smem_u32(Bs);
 	const long long LL = (long long) L * L;
-	mark(0);
-	const bool rowmode = (L % 128) == 0;
-	const int RT = rowmode ? TC_RT_ROWS : TC_RT;
-	const int RB = KC * 3 * TC_HALO;  // row mode: 16-byte chunks per tile
-	for(long long t0 = (long long) blockIdx.x * RT; t0 < ntiles; t0 += (long long) gridDim.x * RT) {
-		const int nt = (int) (ntiles - t0 < RT ? ntiles - t0 : RT);
-		if(rowmode) {
-			int4 *tile = reinterpret_cast<int4 *>(sm + TC_TILE_OFF);
-			if(threadIdx.x < (unsigned) nt) {
-				const int P0 = (int) ((t0 + threadIdx.x) * 128);
-				const int n = P0 / (int) LL, rr = P0 - n * (int) LL;
-				tile[threadIdx.x] = make_int4(n, rr / L, rr - (rr / L) * L, 0);
-			}
-			__syncthreads();
-			if(KC == 4) tc_stage_rows<4>(src, tile, nt, L, As);
-			else tc_stage_rows<2>(src, tile, nt, L, As);
-		}
-		else
-		// staging: thread -> (tile r, pixel p, half of the (tap, kc) chunks);
-		// requires 512 threads.  Copies go straight to shared memory
-		// (cp.async, all in flight); pooled inputs are averaged in registers.
+	tm.mark(0);
+	const int lgk = KC == 4 ? 2 : 1;
+	for(long long t0 = blockIdx.x; t0 < ntiles; t0 += gridDim.x) {
+		// thread -> (pixel p, half of the (tap, kc) chunks)
 		{
-			const int pix = threadIdx.x & 255, half = threadIdx.x >> 8;
-			const int r = pix >> 7, p = pix & 127;
-			if(r < nt) {
-				const long long P = (t0 + r) * 128 + p;
-				const bool valid = P < npix;
-				int n = 0, y = 0, x = 0;
-				if(valid) {
-					n = (int) P / (int) LL;
-					const int rr = (int) P - n * (int) LL;
-					y = rr / L;
-					x = rr - y * L;
-				}
-				const int ys[3] = {wrap(y - 1, L), y, wrap(y + 1, L)};
-				const int xs[3] = {wrap(x - 1, L), x, wrap(x + 1, L)};
-				uint4 *dst_base = As + (size_t) r * 9 * KC * 128 + p;
-				const int lgk = KC == 4 ? 2 : 1;
-				if(src.mode != IN_POOL) {
-					for(int q = half; q < 9 * KC; q += 2) {
-						const int t = q >> lgk, kc = q & (KC - 1);
-						const int ii = ys[t / 3], jj = xs[t % 3];
-						const bf16 *g;
-						if(src.mode == IN_DIRECT) g = src.a + ((size_t) (n * L + ii) * L + jj) * d.ci + kc * 8;
-						else if(kc < 2) g = src.a + ((size_t) (n * (L / 2) + ii / 2) * (L / 2) + jj / 2) * 16 + kc * 8;
-						else g = src.b + ((size_t) (n * L + ii) * L + jj) * 16 + (kc - 2) * 8;
-						cp_async16(dst_base + (size_t) q * 128, valid ? (const void *) g : (const void *) src.a, valid ? 16u : 0u);
-					}
-					cp_async_wait_all();
-				}
-				else {
-					for(int q0 = half; q0 < 9 * KC; q0 += 6) {
-						uint4 v[3];
-#pragma unroll
-						for(int u = 0; u < 3; u++) {
-							const int q = q0 + 2 * u;
-							v[u] = make_uint4(0u, 0u, 0u, 0u);
-							if(q < 9 * KC && valid) {
-								const int t = q >> lgk, kc = q & (KC - 1);
-								v[u] = tc_load_chunk(src, d.ci, n, ys[t / 3], xs[t % 3], L, kc);
-							}
-						}
-#pragma unroll
-						for(int u = 0; u < 3; u++) {
-							const int q = q0 + 2 * u;
-							if(q < 9 * KC) dst_base[(size_t) q * 128] = v[u];
-						}
-					}
-				}
+			const int p = threadIdx.x & 127, part = threadIdx.x >> 7;
+			const long long P = t0 * 128 + p;
+			const bool valid = P < npix;
+			int n = 0, y = 0, x = 0;
+			if(valid) {
+				n = (int) (P / LL);
+				const int rr = (int) (P - n * LL);
+				y = rr / L;
+				x = rr - y * L;
 			}
+			const int ys[3] = {wrap(y - 1, L), y, wrap(y + 1, L)};
+			const int xs[3] = {wrap(x - 1, L), x, wrap(x + 1, L)};
+			uint4 *dst_base = As + p;
+			for(int q = part; q < 9 * KC; q += 4) {
+				const int t = q >> lgk, kc = q & (KC - 1);
+				if(src.mode != IN_POOL) {
+					const bf16 *g = valid ? tc_chunk_ptr(src, d.ci, n, ys[t / 3], xs[t % 3], L, kc) : src.a;
+					cp_async16(dst_base + (size_t) q * 128, g, valid ? 16u : 0u);
+				}
+				else dst_base[(size_t) q * 128] = valid ? tc_load_chunk(src, d.ci, n, ys[t / 3], xs[t % 3], L, kc) : make_uint4(0u, 0u, 0u, 0u);
+			}
+			cp_async_wait_all();
 		}
 		fence_async_smem();
 		__syncthreads();
-		mark(1);
+		tm.mark(1);
 		if(threadIdx.x == 0) {
 			tc_fence_after();
-			// descriptors as base + offset: the start-address field counts 16-byte
-			// units and shared addresses stay below 256 KB, so offsets (in
-			// 16-byte chunks) add without carrying out of the field
-			const uint64_t ad0 = rowmode ? tc_sdesc(a_base, 3 * TC_HALO * 16, 128) : tc_sdesc(a_base, 128 * 16, 128);
+			const uint64_t ad0 = tc_sdesc(a_base, 128 * 16, 128);
 			const uint64_t bd0 = tc_sdesc(b_base, 16 * 16, 128);
 			const int nks = KC / 2;
-			// taps outer, tiles inner: consecutive MMAs go to different accumulators
 #pragma unroll
 			for(int t = 0; t < 9; t++) {
 				for(int ks = 0; ks < nks; ks++) {
 					const uint32_t boff = (uint32_t) ((t * KC + 2 * ks) * 16);
-					for(int r = 0; r < nt; r++) {
-						const uint32_t aoff = rowmode ? (uint32_t) (r * RB + ((2 * ks) * 3 + t / 3) * TC_HALO + t % 3)
-						                              : (uint32_t) (((r * 9 + t) * KC + 2 * ks) * 128);
-						tc_mma(tmem + (uint32_t) (r * 16), ad0 + aoff, bd0 + boff, TC_IDESC, (t | ks) != 0);
-					}
+					const uint32_t aoff = (uint32_t) ((t * KC + 2 * ks) * 128);
+					tc_mma(c.tmem, ad0 + aoff, bd0 + boff, TC_IDESC, (t | ks) != 0);
 				}
 			}
-			tc_commit(mbar);
+			tc_commit(&mbar[0]);
 		}
-		bool ok = mbar_wait(mbar, phase, TC_WAIT_LIMIT);
-		if(!ok) {
-			if(threadIdx.x == 0) atomicOr(err, err_bit);
-			ok = mbar_wait(mbar, phase, TC_WAIT_LIMIT);  // let the MMAs in flight finish before returning
+		const bool ok = mbar_wait(&mbar[0], c.phase[0], TC_WAIT_LIMIT);
+		c.phase[0] ^= 1u;
+		tc_fence_after();
+		if(__syncthreads_or(!ok)) {
+			if(threadIdx.x == 0) atomicOr(c.err, c.err_bit);
 			return false;
 		}
-		phase ^= 1u;
-		tc_fence_after();
-		mark(2);
+		tm.mark(2);
 		const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-		if(w < 4 * nt) {
-			const int r = w >> 2, q = w & 3;
+		if(w < 4) {
 			float v[16];
-			tc_ld16(tmem + ((uint32_t) (32 * q) << 16) + (uint32_t) (r * 16), v);
-			const long long P = (t0 + r) * 128 + 32 * q + lane;
-			if(P < npix) {
-				uint4 o0, o1;
-				o0.x = f2bf(fmaxf(v[0] + bs[0], 0.f), fmaxf(v[1] + bs[1], 0.f));
-				o0.y = f2bf(fmaxf(v[2] + bs[2], 0.f), fmaxf(v[3] + bs[3], 0.f));
-				o0.z = f2bf(fmaxf(v[4] + bs[4], 0.f), fmaxf(v[5] + bs[5], 0.f));
-				o0.w = f2bf(fmaxf(v[6] + bs[6], 0.f), fmaxf(v[7] + bs[7], 0.f));
-				o1.x = f2bf(fmaxf(v[8] + bs[8], 0.f), fmaxf(v[9] + bs[9], 0.f));
-				o1.y = f2bf(fmaxf(v[10] + bs[10], 0.f), fmaxf(v[11] + bs[11], 0.f));
-				o1.z = f2bf(fmaxf(v[12] + bs[12], 0.f), fmaxf(v[13] + bs[13], 0.f));
-				o1.w = f2bf(fmaxf(v[14] + bs[14], 0.f), fmaxf(v[15] + bs[15], 0.f));
-				uint4 *o = reinterpret_cast<uint4 *>(dst + P * 16);
-				o[0] = o0;
-				o[1] = o1;
-			}
+			tc_ld16(c.tmem + ((uint32_t) (32 * w) << 16), v);
+			const long long P = t0 * 128 + 32 * w + lane;
+			if(P < npix) tc_store_pixel(v, bs, dst, P);
 		}
 		tc_fence_before();
 		__syncthreads();
-		mark(3);
+		tm.mark(3);
 	}
 	return true;
+}
+
+// One tensor-core layer (ci = 16 or 32 -> 16 channels, ReLU) over `batch`
+// samples at side L.  Returns false (and sets *c.err |= c.err_bit) if an MMA
+// completion wait ran out; the caller then stops.
+__device__ __forceinline__ bool tc_conv_layer(int l, const TcSrc &src, const bf16 *wpack, const float *wl, const float *bias,
+                                              bf16 *dst, int batch, int L, TcCtx &c) {
+	if(L % 128 == 0) return tc_conv_strip(l, src, wl, bias, dst, batch, L, c);
+	return tc_conv_gather(l, src, wpack, bias, dst, batch, L, c);
 }
 
 // First layer (2 -> 16, ReLU) on the CUDA cores: FP32 input [R/s, W], BF16 output.

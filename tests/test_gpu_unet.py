@@ -43,10 +43,13 @@ def test_forward_loss_and_gradients_match_oracle(L, batch):
         assert np.max(np.abs(gw - gw_ref)) <= 1e-3 * np.max(np.abs(gw_ref)), name
 
 
-@pytest.mark.parametrize("L,batch", [(16, 2), (64, 2), (256, 2)])
+@pytest.mark.parametrize("L,batch", [(16, 2), (64, 2), (128, 1), (256, 2), (384, 1), (512, 2), (1024, 1)])
 def test_tensor_core_forward_matches_oracle(L, batch):
     """The solve's forward pass (BF16 activations, tcgen05 layers) against the
-    FP64 oracle, within BF16 rounding over eleven layers."""
+    FP64 oracle, within BF16 rounding over eleven layers.  Sides that are
+    multiples of 128 take the strip path (one to four tiles per strip, one or
+    more strips per row); the others, and the coarse levels below 128, the
+    gathered path."""
     lib = engine.lib()
     rng = np.random.default_rng(100 + L)
     p = U.init_params(L + 1)
