@@ -185,14 +185,21 @@ def prepare_learned(args, eng, lib):
     import torch
     from rheocell_gb300 import abi
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    eng.harvest(capacity=args.harvest_capacity, every=3, per_solve=6)
+    # samples come from this monolayer's own plain solve, or from a smaller
+    # monolayer of the same physics (--train-workload): the network is
+    # convolutional, so parameters trained there apply at any box side
+    src = eng if not args.train_workload else make_engine(args.train_workload, abi.RC_PRECISION_DOUBLE, eng.device)
+    src.harvest(capacity=args.harvest_capacity, every=3, per_solve=6)
     t0 = time.perf_counter()
-    eng.step(args.harvest_steps)
+    src.step(args.harvest_steps)
     harvest_s = time.perf_counter() - t0
-    n = eng.harvested()
-    eng.harvest(args.harvest_capacity, 3, 0)  # stop collecting, keep the samples
-    rep = eng.train(epochs=args.train_epochs, batch=8, learning_rate=args.train_lr, seed=1,
+    n = src.harvested()
+    src.harvest(args.harvest_capacity, 3, 0)  # stop collecting, keep the samples
+    rep = src.train(epochs=args.train_epochs, batch=8, learning_rate=args.train_lr, seed=1,
                     learning_rate_final=args.train_lr * args.train_lr_final, max_samples=args.train_max_samples)
+    if src is not eng:
+        eng.set_params(src.get_params())
+        src.close()
     k = max(2, min(args.steps, 10))
     plain_ms, plain_it, plain_res = solve_stage(eng, lib, k, flush)
     eng.set_solver(abi.RC_SOLVER_LEARNED)
@@ -209,12 +216,24 @@ def prepare_learned(args, eng, lib):
         lib.rc_solver_profile(eng.h, 0, ms, 15)
         phases = {nm: round(ms[i] / k, 4) for i, nm in enumerate(abi.SOLVER_PHASES)}
     return {"harvest_steps": args.harvest_steps, "harvest_s": harvest_s, "samples": n,
+            "trained_on": args.train_workload or args.workload,
             "training": {kk: (round(v, 6) if isinstance(v, float) else v) for kk, v in rep.items()},
             "solve_ms_per_step": {"plain_fp64_cg": plain_ms, "learned_fcg": learned_ms,
                                   "speedup": plain_ms / learned_ms if learned_ms > 0 else None},
             "iterations_per_solve": {"plain_fp64_cg": plain_it, "learned_fcg_inner": learned_it},
             "max_rel_residual": {"plain_fp64_cg": plain_res, "learned_fcg": learned_res},
             "steps_each": k, "phases_ms_per_step": phases}
+
+
+def make_engine(name, prec, dev):
+    """A single-monolayer engine of workload `name` on device `dev`, in phase 1."""
+    from rheocell_gb300 import engine
+    from tests.common import build_inputs
+    (keys, m), = make_case(workload(name))
+    p, cells = build_inputs(keys, m, precision=prec)
+    e = engine.Engine(p, m.L, cells, device=dev)
+    e.set_phase(1)
+    return e
 
 
 def run_gb300(args, rank, world):
@@ -503,6 +522,8 @@ def main():
     ap.add_argument("--harvest-capacity", type=int, default=2000)
     ap.add_argument("--train-epochs", type=int, default=10)
     ap.add_argument("--solver-phases", action="store_true")
+    ap.add_argument("--train-workload", default=None, choices=["wet256", "wet512", "wet1024"],
+                    help="harvest and train on this monolayer instead of the timed one")
     ap.add_argument("--train-max-samples", type=int, default=0, help="train on at most this many samples (0: all)")
     ap.add_argument("--train-lr", type=float, default=2e-3)
     ap.add_argument("--train-lr-final", type=float, default=0.05, help="final step size as a fraction of --train-lr")

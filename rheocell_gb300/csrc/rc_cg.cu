@@ -795,27 +795,6 @@ __device__ __forceinline__ bool harvest_finish(const CGArgs &a, CGShared &sh, co
 //   phase C  e += alpha p, r -= alpha Ap, |r|^2, R = sum r / T
 // with alpha = r.z / p.Ap.  P alternates between two box buffers.
 
-// First layer (2 -> 16, ReLU) at one pixel of sample n, FP32: channel 0 of
-// the input (R) is multiplied by sc (1/s of the component) as it is read.
-// w: [9][2][16] then 16 biases.
-__device__ __forceinline__ void e0a_pixel(const float *x0, const float *w, int n, int i, int j, int L, float sc, float *y) {
-#pragma unroll
-	for(int o = 0; o < 16; o++) y[o] = w[9 * 2 * 16 + o];
-#pragma unroll
-	for(int t = 0; t < 9; t++) {
-		const int ii = wrap(i + t / 3 - 1, L), jj = wrap(j + t % 3 - 1, L);
-		const float2 in = *reinterpret_cast<const float2 *>(x0 + ((size_t) (n * L + ii) * L + jj) * 2);
-		const float r = in.x * sc, wv = in.y;
-		const float *wt = w + t * 32;
-#pragma unroll
-		for(int o = 0; o < 16; o++) y[o] = fmaf(r, wt[o], y[o]);
-#pragma unroll
-		for(int o = 0; o < 16; o++) y[o] = fmaf(wv, wt[16 + o], y[o]);
-	}
-#pragma unroll
-	for(int o = 0; o < 16; o++) y[o] = fmaxf(y[o], 0.f);
-}
-
 // The network on both components: V (a.unet.out, FP32) from x0.
 __device__ __noinline__ bool precond_network(const CGArgs &a, CGShared &sh, TcCtx &tc) {
 	float *wsm = reinterpret_cast<float *>(tc.sm);
@@ -826,7 +805,10 @@ __device__ __noinline__ bool precond_network(const CGArgs &a, CGShared &sh, TcCt
 	const long long gstride = (long long) gridDim.x * blockDim.x;
 	const float sc[2] = {sh.scale[0] > 0.0 ? (float) (1.0 / sh.scale[0]) : 0.f,
 	                     sh.scale[1] > 0.0 ? (float) (1.0 / sh.scale[1]) : 0.f};
-	{
+	// the tensor-core path evaluates the first layer while staging the
+	// second's rows when the box side allows strips
+	const bool fused_first = a.unet_tc && L % 128 == 0;
+	if(!fused_first) {
 		const int nw = 9 * 2 * 16 + 16;
 		__syncthreads();
 		for(int k = threadIdx.x; k < nw; k += blockDim.x) wsm[k] = a.unet_params[unet_weight_offset(L_E0A) + k];
@@ -863,7 +845,15 @@ __device__ __noinline__ bool precond_network(const CGArgs &a, CGShared &sh, TcCt
 	if(a.unet_tc) {
 		// nine tensor-core layers; last layer (FP32, CUDA cores) -> V
 		for(int l = L_E0B; l <= L_D0B; l++) {
-			if(!tc_conv_layer(l, unet_tc_src(l, a.unet_bf), a.unet_wpack + unet_pack_offset(l),
+			TcSrc src = unet_tc_src(l, a.unet_bf);
+			if(l == L_E0B && fused_first) {
+				src.mode = IN_FIRST;
+				src.x = a.unet.x0;
+				src.w0 = a.unet_params + unet_weight_offset(L_E0A);
+				src.sc[0] = sc[0];
+				src.sc[1] = sc[1];
+			}
+			if(!tc_conv_layer(l, src, a.unet_wpack + unet_pack_offset(l),
 			                  a.unet_params + unet_weight_offset(l), a.unet_params + unet_bias_offset(l),
 			                  unet_tc_dst(l, a.unet_bf), 2, L >> unet_layer(l).level, tc))
 				return false;

@@ -479,14 +479,22 @@ cudaError_t unet_tc_configure() {
 void unet_tc_forward(const float *params, const bf16 *packed, const float *x0, const UNetActsBF &A, float *out, int batch,
                      int L, int sms, int *err, cudaStream_t s) {
 	const long long p0 = (long long) batch * L * L;
-	e0a_kernel<<<grid_for(p0, 256), 256, 0, s>>>(x0, params, A.e0a, batch, L);
+	// as in the solve: the first layer is evaluated while the second stages
+	// its rows when L allows strips
+	const bool fused_first = L % 128 == 0;
+	if(!fused_first) e0a_kernel<<<grid_for(p0, 256), 256, 0, s>>>(x0, params, A.e0a, batch, L);
 	for(int l = L_E0B; l <= L_D0B; l++) {
 		const int Ll = L >> unet_layer(l).level;
 		const long long tiles = ((long long) batch * Ll * Ll + 127) / 128;
 		long long g = tiles;
 		if(g > sms) g = sms;
-		tc_layer_kernel<<<(int) g, 512, TC_SMEM, s>>>(l, unet_tc_src(l, A), packed, params, unet_tc_dst(l, A), batch, Ll,
-		                                              err);
+		TcSrc src = unet_tc_src(l, A);
+		if(l == L_E0B && fused_first) {
+			src.mode = IN_FIRST;
+			src.x = x0;
+			src.w0 = params + unet_weight_offset(L_E0A);
+		}
+		tc_layer_kernel<<<(int) g, 512, TC_SMEM, s>>>(l, src, packed, params, unet_tc_dst(l, A), batch, Ll, err);
 	}
 	out_kernel<<<grid_for(p0, 256), 256, 0, s>>>(A.t0, params, out, batch, L);
 }

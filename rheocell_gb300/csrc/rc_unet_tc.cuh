@@ -22,11 +22,41 @@ struct UNetActsBF {
 	bf16 *b0, *t2;              // level 2
 };
 
+// Input of a tensor-core layer: BF16 activations (IN_DIRECT, IN_POOL,
+// IN_UPCAT as for the FP32 layers), or IN_FIRST: the first layer (2 -> 16,
+// ReLU) evaluated while staging, from the FP32 network input x (channel 0
+// multiplied by sc[sample]) with the FP32 weights w0 ([9][2][16] + 16 biases).
+enum { IN_FIRST = 3 };
 struct TcSrc {
 	int mode;
 	const bf16 *a;
 	const bf16 *b;
+	const float *x = nullptr;
+	const float *w0 = nullptr;
+	float sc[2] = {1.f, 1.f};
 };
+
+// First layer (2 -> 16, ReLU) at one pixel of sample n, FP32: channel 0 of
+// the input (R) is multiplied by sc (1/s of the component) as it is read.
+// w: [9][2][16] then 16 biases.
+__device__ __forceinline__ void e0a_pixel(const float *x0, const float *w, int n, int i, int j, int L, float sc, float *y) {
+#pragma unroll
+	for(int o = 0; o < 16; o++) y[o] = w[9 * 2 * 16 + o];
+#pragma unroll
+	for(int t = 0; t < 9; t++) {
+		const int ii = wrap(i + t / 3 - 1, L), jj = wrap(j + t % 3 - 1, L);
+		const float2 in = *reinterpret_cast<const float2 *>(x0 + ((size_t) (n * L + ii) * L + jj) * 2);
+		const float r = in.x * sc, wv = in.y;
+		const float *wt = w + t * 32;
+#pragma unroll
+		for(int o = 0; o < 16; o++) y[o] = fmaf(r, wt[o], y[o]);
+#pragma unroll
+		for(int o = 0; o < 16; o++) y[o] = fmaf(wv, wt[16 + o], y[o]);
+	}
+#pragma unroll
+	for(int o = 0; o < 16; o++) y[o] = fmaxf(y[o], 0.f);
+}
+
 
 __host__ __device__ inline TcSrc unet_tc_src(int l, const UNetActsBF &A) {
 	switch(l) {
@@ -80,7 +110,10 @@ constexpr int UNET_PACKED = unet_pack_offset(UNET_LAYERS);
 // pair: A = 128 pixels x 16 channels, B = the three vertical taps' weights
 // stacked along N (N = 48: dy = +1, 0, -1), D = the accumulators of output
 // rows rho - 1, rho, rho + 1, which sit in consecutive 16-column slots of a
-// ring of R = 32 / T slots per tile in TMEM.  An output row is complete once
+// ring of R = 32 / T - 2 slots per tile in TMEM; the ring is followed by two
+// overflow slots, so the three slots of an MMA are always contiguous (what
+// lands in slot R or R + 1 belongs to logical slot 0 or 1 and is added by
+// the epilogue).  An output row is complete once
 // input row + 1 has been multiplied; the epilogue reads it, writes BF16
 // (bias, ReLU) and zeroes the slot for reuse.  Rows are pipelined: the MMAs
 // of input row i run while output row i - 3 is written out and input row
@@ -96,12 +129,13 @@ constexpr int TC_STRIP_T = 4;   // strip mode: at most 4 tiles (512 pixels) per 
 constexpr int TC_COLS = 512;    // TMEM columns: T x R slots of 16
 constexpr int TC_HW_MAX = TC_STRIP_T * 128 + 2;
 constexpr size_t TC_A_GATHER = (size_t) TC_RT * 9 * 4 * 128 * 16;
-constexpr size_t TC_A_STRIP = (size_t) 2 * 4 * TC_HW_MAX * 16;  // two input-row buffers, up to 4 channel chunks
+constexpr size_t TC_A_STRIP = (size_t) 3 * 4 * TC_HW_MAX * 16;  // three input-row buffers, up to 4 channel chunks
 constexpr size_t TC_A_BYTES = TC_A_GATHER > TC_A_STRIP ? TC_A_GATHER : TC_A_STRIP;
 constexpr size_t TC_B_OFF = TC_A_BYTES;
 constexpr size_t TC_B_BYTES = 9 * 4 * 16 * 16;  // either layout: 9 taps x 32 channels x 16 outputs, BF16
 constexpr size_t TC_BIAS_OFF = TC_B_OFF + TC_B_BYTES;
-constexpr size_t TC_MBAR_OFF = TC_BIAS_OFF + 64;  // two mbarriers
+constexpr size_t TC_W0_OFF = TC_BIAS_OFF + 64;  // first layer's FP32 weights (IN_FIRST)
+constexpr size_t TC_MBAR_OFF = TC_W0_OFF + sizeof(float) * (9 * 2 * 16 + 16);  // two mbarriers
 constexpr size_t TC_HOLD_OFF = TC_MBAR_OFF + 16;
 constexpr size_t TC_SMEM = TC_HOLD_OFF + 16;
 constexpr uint32_t TC_IDESC = tc_idesc_bf16(128, 16);
@@ -113,8 +147,10 @@ constexpr long long TC_WAIT_LIMIT = 2000000;  // mbarrier polls (each a bounded 
 // the two mbarriers at TC_MBAR_OFF initialised with count 1), the TMEM
 // allocation (TC_COLS columns) and the parities the mbarriers wait for next.
 // err/err_bit: where a wait that ran out is recorded.  tns (diagnostics, may
-// be null): block 0 adds the time of weight staging, operand staging, MMA
-// completion waits and the epilogue to tns[0..3].
+// be null): block 0 adds the time of weight and operand staging (tns[0]),
+// waits for staged rows and the block barrier (tns[1]), waits for MMA
+// completion (tns[2]) and the epilogue (tns[3]); in strip mode as seen by the
+// first staging/epilogue thread.
 struct TcCtx {
 	unsigned char *sm;
 	uint32_t tmem;
@@ -176,18 +212,29 @@ __device__ __forceinline__ const bf16 *tc_chunk_ptr(const TcSrc &s, int ci, int 
 // Stage input row `row` of sample n, pixels x0 - 1 .. x0 + W (periodic), into
 // buf[kc * HW + position] (HW = W + 2).  Consecutive threads take
 // consecutive 16-byte chunks of global memory (kc fastest).  Plain inputs go
-// by cp.async (the caller waits); pooled inputs are averaged in registers.
-__device__ __forceinline__ void tc_stage_strip_row(const TcSrc &src, int KC, int n, int row, int x0, int HW, int L, uint4 *buf) {
+// by cp.async (the caller waits); pooled inputs are averaged in registers;
+// IN_FIRST rows are computed from the network input (w0s: the first layer's
+// weights in shared memory).
+__device__ __forceinline__ void tc_stage_strip_row(const TcSrc &src, int KC, int n, int row, int x0, int HW, int L, uint4 *buf,
+                                                   const float *w0s, int t0, int nthr) {
 	const int nchunk = KC * HW;
-	if(src.mode != IN_POOL) {
-		for(int c = threadIdx.x; c < nchunk; c += blockDim.x) {
+	if(src.mode == IN_FIRST) {
+		for(int pos = t0; pos < HW; pos += nthr) {
+			float y[16];
+			e0a_pixel(src.x, w0s, n, row, wrap(x0 - 1 + pos, L), L, src.sc[n], y);
+			buf[pos] = make_uint4(f2bf(y[0], y[1]), f2bf(y[2], y[3]), f2bf(y[4], y[5]), f2bf(y[6], y[7]));
+			buf[HW + pos] = make_uint4(f2bf(y[8], y[9]), f2bf(y[10], y[11]), f2bf(y[12], y[13]), f2bf(y[14], y[15]));
+		}
+	}
+	else if(src.mode != IN_POOL) {
+		for(int c = t0; c < nchunk; c += nthr) {
 			const int pos = c / KC, kc = c - pos * KC;
 			const int x = wrap(x0 - 1 + pos, L);
 			cp_async16(buf + kc * HW + pos, tc_chunk_ptr(src, KC * 8, n, row, x, L, kc), 16u);
 		}
 	}
 	else {
-		for(int c = threadIdx.x; c < nchunk; c += blockDim.x) {
+		for(int c = t0; c < nchunk; c += nthr) {
 			const int pos = c / KC, kc = c - pos * KC;
 			buf[kc * HW + pos] = tc_load_chunk(src, KC * 8, n, row, wrap(x0 - 1 + pos, L), L, kc);
 		}
@@ -225,7 +272,8 @@ struct TcTimer {
 	bool on;
 	unsigned long long t;
 	unsigned long long *tns;
-	__device__ __forceinline__ TcTimer(unsigned long long *p) : on(p && blockIdx.x == 0 && threadIdx.x == 0), t(0), tns(p) {
+	__device__ __forceinline__ TcTimer(unsigned long long *p, unsigned who = 0)
+	    : on(p && blockIdx.x == 0 && threadIdx.x == who), t(0), tns(p) {
 		if(on) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
 	}
 	__device__ __forceinline__ void mark(int k) {
@@ -238,17 +286,24 @@ struct TcTimer {
 	}
 };
 
-// Strip mode (L a multiple of 128); requires 512 threads.  wl: the layer's
+// Warp that writes out tile r's lane quarter q (TMEM lanes 32 q .. 32 q + 31
+// are readable by warps w with w % 4 == q): warp q + 4 r, except that warp
+// 0 only issues MMAs, so quarter 0 of tiles 0 .. 3 goes to warps 4, 8, 12, 4.
+__device__ __forceinline__ int tc_epi_warp(int r, int q) { return q ? q + 4 * r : 4 + 4 * (r % 3); }
+
+// Strip mode (L a multiple of 128); requires 512 threads: warp 0 issues the
+// MMAs, warps 1 - 15 stage rows (two rows ahead, three buffers) and write
+// out finished rows.  wl: the layer's
 // FP32 weights [tap = (dy + 1) * 3 + dx + 1][ci][16]; bias: 16 FP32.
 static __device__ __noinline__ bool tc_conv_strip(int l, const TcSrc &src, const float *wl, const float *bias, bf16 *dst,
                                                   int batch, int L, TcCtx &c) {
-	TcTimer tm(c.tns);
+	TcTimer tm(c.tns, 32);  // block 0's first staging/epilogue thread
 	const UNetLayerDesc d = unet_layer(l);
 	const int KC = d.ci / 8, KS = KC / 2;
 	const int ntile = L / 128;
 	int T = TC_STRIP_T;
 	while(ntile % T) T >>= 1;
-	const int R = TC_COLS / 16 / T;  // accumulator slots per tile
+	const int R = TC_COLS / 16 / T - 2;  // output-row slots per tile, plus two overflow slots
 	const int W = T * 128, HW = W + 2;
 	const int NS = ntile / T;
 	const long long U = (long long) batch * NS * L;  // (sample, strip, row) units
@@ -270,6 +325,9 @@ static __device__ __noinline__ bool tc_conv_strip(int l, const TcSrc &src, const
 		Bh[idx] = __float2bfloat16_rn(wl[(t * d.ci + 16 * ks + 8 * h + e) * 16 + co]);
 	}
 	if(threadIdx.x < 16) bs[threadIdx.x] = bias[threadIdx.x];
+	float *w0s = reinterpret_cast<float *>(c.sm + TC_W0_OFF);
+	if(src.mode == IN_FIRST)
+		for(int k = threadIdx.x; k < 9 * 2 * 16 + 16; k += blockDim.x) w0s[k] = src.w0[k];
 	fence_async_smem();
 	__syncthreads();
 	tm.mark(0);
@@ -283,79 +341,101 @@ static __device__ __noinline__ bool tc_conv_strip(int l, const TcSrc &src, const
 		const int y1 = (int) ((u1 - col * L) < L ? (u1 - col * L) : L);  // exclusive
 		const int n = (int) (col / NS), x0 = (int) (col - (long long) n * NS) * W;
 		const int nin = y1 - y0 + 2;  // input rows y0 - 1 .. y1
-		// all slots of this CTA's tiles zero; first input row staged
-		for(int pr = w; pr < T * 4; pr += 16) {
+		// all slots of this CTA's tiles zero; input rows 0 and 1 staged
+		for(int pr = 0; pr < T * 4; pr++) {
 			const int r = pr >> 2, q = pr & 3;
-			for(int sl = 0; sl < R; sl++) tc_st16_zero(c.tmem + ((uint32_t) (32 * q) << 16) + (uint32_t) ((r * R + sl) * 16));
+			if(w != tc_epi_warp(r, q)) continue;
+			for(int sl = 0; sl < R + 2; sl++)
+				tc_st16_zero(c.tmem + ((uint32_t) (32 * q) << 16) + (uint32_t) ((r * (R + 2) + sl) * 16));
 		}
 		tc_wait_st();
-		tc_stage_strip_row(src, KC, n, wrap(y0 - 1, L), x0, HW, L, Abuf);
-		cp_async_wait_all();
+		if(w > 0) {
+			tc_stage_strip_row(src, KC, n, wrap(y0 - 1, L), x0, HW, L, Abuf, w0s, threadIdx.x - 32, blockDim.x - 32);
+			cp_async_commit();
+			if(nin > 1) tc_stage_strip_row(src, KC, n, wrap(y0, L), x0, HW, L, Abuf + KC * HW, w0s, threadIdx.x - 32, blockDim.x - 32);
+			cp_async_commit();
+			cp_async_wait_1();
+		}
 		fence_async_smem();
 		tc_fence_before();
 		__syncthreads();
 		tc_fence_after();
 		tm.mark(1);
 		for(int i = 0; i <= nin; i++) {
-			// MMAs of input row y0 - 1 + i (buffer i & 1) into the slots of
-			// output rows y0 - 2 + i .. y0 + i
-			if(i < nin && threadIdx.x == 0) {
-				const uint32_t abuf = a_base + (uint32_t) ((i & 1) * KC * HW * 16);
-				const int s0 = i % R;
-				for(int r = 0; r < T; r++) {
-					const uint32_t dcol = c.tmem + (uint32_t) (r * R * 16);
-					for(int dxi = 0; dxi < 3; dxi++) {
-						for(int ks = 0; ks < KS; ks++) {
-							const uint64_t ad = tc_sdesc(abuf + (uint32_t) (((2 * ks) * HW + r * 128 + dxi) * 16), (uint32_t) (HW * 16), 128);
-							const uint32_t bq = b_base + (uint32_t) ((dxi * KS + ks) * 1536);
-							if(s0 + 2 < R) tc_mma(dcol + (uint32_t) (s0 * 16), ad, tc_sdesc(bq, 768, 128), TC_IDESC48, 1u);
-							else if(s0 == R - 2) {
-								tc_mma(dcol + (uint32_t) (s0 * 16), ad, tc_sdesc(bq, 768, 128), TC_IDESC32, 1u);
-								tc_mma(dcol, ad, tc_sdesc(bq + 512, 768, 128), TC_IDESC, 1u);
-							}
-							else {
-								tc_mma(dcol + (uint32_t) (s0 * 16), ad, tc_sdesc(bq, 768, 128), TC_IDESC, 1u);
-								tc_mma(dcol, ad, tc_sdesc(bq + 256, 768, 128), TC_IDESC32, 1u);
+			bool fail = false;
+			if(w == 0) {
+				// the MMA warp: MMAs of input row y0 - 1 + i (buffer i % 3) into
+				// the slots of output rows y0 - 2 + i .. y0 + i: physical slots
+				// s0 .. s0 + 2, where physical slot R or R + 1 stands for
+				// logical slot 0 or 1
+				if(i < nin && lane == 0) {
+					const uint32_t abuf = a_base + (uint32_t) ((i % 3) * KC * HW * 16);
+					const int s0 = i % R;
+					for(int r = 0; r < T; r++) {
+						const uint32_t dcol = c.tmem + (uint32_t) ((r * (R + 2) + s0) * 16);
+						for(int dxi = 0; dxi < 3; dxi++) {
+							for(int ks = 0; ks < KS; ks++) {
+								const uint64_t ad =
+								    tc_sdesc(abuf + (uint32_t) (((2 * ks) * HW + r * 128 + dxi) * 16), (uint32_t) (HW * 16), 128);
+								const uint32_t bq = b_base + (uint32_t) ((dxi * KS + ks) * 1536);
+								tc_mma(dcol, ad, tc_sdesc(bq, 768, 128), TC_IDESC48, 1u);
 							}
 						}
 					}
+					tc_commit(&mbar[i & 1]);
 				}
-				tc_commit(&mbar[i & 1]);
+				__syncwarp();
+				if(i >= 1) c.phase[(i - 1) & 1] ^= 1u;
 			}
-			bool fail = false;
-			if(i >= 1) {
-				// MMAs of input row i - 1 done: its buffer is free and output
-				// row y0 - 3 + i is complete
-				const int b = (i - 1) & 1;
-				fail = !mbar_wait(&mbar[b], c.phase[b], TC_WAIT_LIMIT);
-				c.phase[b] ^= 1u;
-				tc_fence_after();
-			}
-			tm.mark(2);
-			if(!fail && i + 1 < nin)
-				tc_stage_strip_row(src, KC, n, wrap(y0 + i, L), x0, HW, L, Abuf + ((i + 1) & 1) * KC * HW);
-			if(!fail && i >= 1) {
-				const int y = y0 - 3 + i, sl = (i - 1) % R;
-				for(int pr = w; pr < T * 4; pr += 16) {
-					const int r = pr >> 2, q = pr & 3;
-					const uint32_t ta = c.tmem + ((uint32_t) (32 * q) << 16) + (uint32_t) ((r * R + sl) * 16);
-					if(y >= y0) {
-						float v[16];
-						tc_ld16(ta, v);
-						tc_store_pixel(v, bs, dst, ((long long) n * L + y) * L + x0 + r * 128 + 32 * q + lane);
+			else {
+				if(i >= 1) {
+					// MMAs of input row i - 1 done: its buffer is free and
+					// output row y0 - 3 + i is complete
+					const int b = (i - 1) & 1;
+					fail = !mbar_wait(&mbar[b], c.phase[b], TC_WAIT_LIMIT);
+					c.phase[b] ^= 1u;
+					tc_fence_after();
+				}
+				tm.mark(2);
+				// input row i + 2 into buffer (i + 2) % 3 (that of row i - 1)
+				if(!fail && i + 2 < nin)
+					tc_stage_strip_row(src, KC, n, wrap(y0 + 1 + i, L), x0, HW, L, Abuf + ((i + 2) % 3) * KC * HW, w0s,
+					                   threadIdx.x - 32, blockDim.x - 32);
+				cp_async_commit();
+				tm.mark(0);
+				if(!fail && i >= 1) {
+					const int y = y0 - 3 + i, sl = (i - 1) % R;
+					for(int pr = 0; pr < T * 4; pr++) {
+						const int r = pr >> 2, q = pr & 3;
+						if(w != tc_epi_warp(r, q)) continue;
+						const uint32_t ta = c.tmem + ((uint32_t) (32 * q) << 16) + (uint32_t) ((r * (R + 2) + sl) * 16);
+						if(y >= y0) {
+							float v[16];
+							tc_ld16(ta, v);
+							if(sl < 2) {
+								float o[16];
+								tc_ld16(ta + (uint32_t) (R * 16), o);
+#pragma unroll
+								for(int k = 0; k < 16; k++) v[k] += o[k];
+							}
+							tc_store_pixel(v, bs, dst, ((long long) n * L + y) * L + x0 + r * 128 + 32 * q + lane);
+						}
+						tc_st16_zero(ta);
+						if(sl < 2) tc_st16_zero(ta + (uint32_t) (R * 16));
 					}
-					tc_st16_zero(ta);
+					tc_wait_st();
 				}
-				tc_wait_st();
+				tm.mark(3);
+				// input row i + 1 landed (the group of the previous iteration)
+				cp_async_wait_1();
 			}
-			tm.mark(3);
-			cp_async_wait_all();
 			fence_async_smem();
 			tc_fence_before();
 			if(__syncthreads_or(fail)) {
 				// let the MMAs in flight finish before giving up
 				if(threadIdx.x == 0) atomicOr(c.err, c.err_bit);
 				mbar_wait(&mbar[i & 1], c.phase[i & 1], TC_WAIT_LIMIT);
+				cp_async_wait_all();
 				return false;
 			}
 			tc_fence_after();
@@ -367,7 +447,8 @@ static __device__ __noinline__ bool tc_conv_strip(int l, const TcSrc &src, const
 }
 
 // Gather mode: one tile of 128 pixels per round, operands gathered pixel by
-// pixel; wpack: the layer's packed BF16 weights [tap][kc][co][8].
+// pixel; wpack: the layer's packed BF16 weights [tap][kc][co][8].  Inputs
+// IN_DIRECT, IN_POOL and IN_UPCAT (not IN_FIRST).
 static __device__ __noinline__ bool tc_conv_gather(int l, const TcSrc &src, const bf16 *wpack, const float *bias, bf16 *dst,
                                                    int batch, int L, TcCtx &c) {
 	TcTimer tm(c.tns);

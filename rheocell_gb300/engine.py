@@ -62,6 +62,7 @@ class Engine:
             raise EngineError(rc, msg)
         self.n = cells.n
         self.L = L
+        self.device = device
         self.layer_sizes = [cells.n]
         self.stats = abi.RcStepStats()
 
@@ -93,6 +94,7 @@ class Engine:
             self.h = None
             raise EngineError(rc, msg)
         self.n = total
+        self.device = device
         self.L = [L for L, _, _ in layers]
         self.layer_sizes = [hc.n for _, hc, _ in layers]
         self.stats = abi.RcStepStats()
