@@ -27,7 +27,7 @@ RC_OBS_VELOCITY = 0
 RC_OBS_SHAPE = 1
 RC_OBS_NEMATIC = 2
 SOLVER_PHASES = ["fcg_setup", "first_layer", "tc_level0", "tc_level1", "tc_level2", "last_layer",
-                 "fcg_z", "fcg_direction", "unused", "fcg_update", "other",
+                 "fcg_z", "fcg_direction", "solve_start", "fcg_update", "other",
                  "tc_weights", "tc_staging", "tc_mma", "tc_epilogue"]
 
 RC_SIMPLEFIELD = 0

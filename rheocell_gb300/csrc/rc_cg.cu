@@ -140,11 +140,12 @@ __device__ __forceinline__ unsigned long long gtimer() {
 
 // Diagnostic phase timers: block 0's thread 0 charges the time since the
 // previous mark (including its wait at the barrier that ended the phase) to
-// phase k.  Phases: 0 set-up of a flexible CG run, 1 first layer, 2-4
-// tensor-core layers of levels 0-2, 5 last layer (all network layers when the
-// network runs in FP32), 6 flexible CG phase E, 7 phase AB, 8 (unused),
-// 9 phase C, 10 everything else.
-enum { PH_INIT, PH_E0A, PH_TC0, PH_TC1, PH_TC2, PH_OUT, PH_Z, PH_AB, PH_UNUSED, PH_C, PH_OTHER, PH_COUNT };
+// phase k.  Phases: 0 refinement update and true residual before a flexible
+// CG run, 1 first layer, 2-4 tensor-core layers of levels 0-2, 5 last layer
+// (all network layers when the network runs in FP32), 6 flexible CG phase E,
+// 7 phase AB, 8 start of a solve (cover lists, first true residual), 9 phase
+// C, 10 everything else.
+enum { PH_INIT, PH_E0A, PH_TC0, PH_TC1, PH_TC2, PH_OUT, PH_Z, PH_AB, PH_START, PH_C, PH_OTHER, PH_COUNT };
 __device__ __forceinline__ void pmark(const CGArgs &a, CGShared &sh, int k) {
 	if(a.phase_ns && blockIdx.x == 0 && threadIdx.x == 0) {
 		const unsigned long long t = gtimer();
@@ -281,8 +282,12 @@ __device__ __forceinline__ bool true_residual(const CGArgs &a, CGShared &sh, boo
 					rx = bx - (T * a.vx[j] + qx);
 					ry = by - (T * a.vy[j] + qy);
 				}
-				a.rx[j] = rx;
-				a.ry[j] = ry;
+				if(fmode != RES_FLOAT_COVER) {
+					// the learned path never reads the FP64 residual (its FP64
+					// fallback recomputes it)
+					a.rx[j] = rx;
+					a.ry[j] = ry;
+				}
 				v[0] += bx * bx;
 				v[1] += by * by;
 				v[2] += rx * rx;
@@ -1290,6 +1295,7 @@ __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcCtx &tc
 	if(!build_csr(a, sh)) return;
 	constexpr int fmode = LEARNED ? RES_FLOAT_COVER : RES_FLOAT_UNKNOWN;
 	if(!(mixed ? true_residual<fmode>(a, sh, cold != 0) : true_residual<RES_FP64>(a, sh, cold != 0))) return;
+	pmark(a, sh, PH_START);
 	if(threadIdx.x == 0) {
 		for(int c = 0; c < 2; c++) {
 			sh.bn2[c] = sh.tot[c];
