@@ -265,6 +265,10 @@ def run_gb300(args, rank, world):
     learned = None
     if args.solver == "learned":
         learned = prepare_learned(args, eng, lib)
+    # tile shape of the FP32 cell kernel, timed on this workload (setup, untimed)
+    tuned = None
+    if args.precision == "float" and not args.no_autotune:
+        tuned = eng.autotune(steps_per_candidate=4)
     # warm-up
     eng.step(max(args.warmup, 3) if args.warmup >= 0 else 3)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -389,6 +393,10 @@ def run_gb300(args, rank, world):
     }
     if S_after != S:
         out["config"]["sites_after"] = S_after
+    if tuned is not None:
+        out["config"]["cell_tile_threads"] = tuned["chosen"]
+        out["autotune"] = {"candidates_ms_per_step": {str(t): round(ms, 4) for t, ms in tuned["candidates"]},
+                           "chosen": tuned["chosen"]}
     if learned is not None:
         out["learned_pcg"] = learned
         out["config"]["solver"] = "learned flexible CG (FP32 inner, FP64 refinement)"
@@ -522,6 +530,7 @@ def main():
     ap.add_argument("--harvest-capacity", type=int, default=2000)
     ap.add_argument("--train-epochs", type=int, default=10)
     ap.add_argument("--solver-phases", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default cell tile (FP32 only)")
     ap.add_argument("--train-workload", default=None, choices=["wet256", "wet512", "wet1024"],
                     help="harvest and train on this monolayer instead of the timed one")
     ap.add_argument("--train-max-samples", type=int, default=0, help="train on at most this many samples (0: all)")

@@ -285,6 +285,28 @@ int rc_viscous_resolve_noalloc(rc_engine *e, double *vx, double *vy, long long n
  * and output ([batch][L][L]) may be NULL.  L must be a multiple of 4.
  */
 #define RC_UNET_PARAMS 25937
+/*
+ * Tile-shape autotuning of the FP32 cell kernel (precision RC_PRECISION_FLOAT;
+ * no counterpart in the reference, whose update is one serial loop,
+ * FD_CPUBackend.cpp:44-120).  Each cell patch is swept by one CTA in tiles of
+ * `threads` patch sites; rc_autotune times every candidate tile (128, 256,
+ * 512 sites) over `steps_per_candidate` steps of this engine's own workload
+ * (one untimed step first) and keeps the fastest.  The simulation advances by
+ * 3 x (steps_per_candidate + 1) steps.  The FP32 results of different tiles
+ * differ by rounding only (their per-warp partial sums are grouped
+ * differently).  FP64 engines keep one tile (their summation order is part of
+ * their parity with the reference): candidates = 0.
+ * rc_set_cell_threads sets the tile directly (128, 256 or 512).
+ */
+typedef struct rc_autotune_report {
+    int candidates;          /* tiles tried */
+    int threads[4];          /* patch sites per tile of each candidate */
+    double ms_per_step[4];   /* measured step time of each (CUDA events) */
+    int chosen;              /* tile in use afterwards */
+} rc_autotune_report;
+int rc_autotune(rc_engine *e, int steps_per_candidate, rc_autotune_report *report);
+int rc_set_cell_threads(rc_engine *e, int threads);
+
 /* rc_unet_forward_tc: the network's forward pass as the solve runs it
  * (BF16 activations, tensor-core layers, FP32 first and last layers);
  * input [batch][L][L][2], output [batch][L][L]. */

@@ -98,6 +98,10 @@ class RcStepStats(C.Structure):
     ]
 
 
+class RcAutotuneReport(C.Structure):
+    _fields_ = [("candidates", C.c_int), ("threads", C.c_int * 4), ("ms_per_step", C.c_double * 4), ("chosen", C.c_int)]
+
+
 class RcTrainOptions(C.Structure):
     _fields_ = [
         ("epochs", C.c_int), ("batch", C.c_int), ("learning_rate", C.c_double), ("validation", C.c_double),
@@ -179,6 +183,10 @@ def declare(lib: C.CDLL, prefix: str) -> C.CDLL:
         lib.rc_unet_loss_grad.restype = C.c_int
         lib.rc_viscous_resolve_noalloc.argtypes = [vp, vp, vp, C.c_longlong, C.POINTER(C.c_int)]
         lib.rc_viscous_resolve_noalloc.restype = C.c_int
+        lib.rc_autotune.argtypes = [vp, C.c_int, C.POINTER(RcAutotuneReport)]
+        lib.rc_autotune.restype = C.c_int
+        lib.rc_set_cell_threads.argtypes = [vp, C.c_int]
+        lib.rc_set_cell_threads.restype = C.c_int
         lib.rc_set_timing.argtypes = [vp, C.c_int]
         lib.rc_set_timing.restype = C.c_int
         lib.rc_timers.argtypes = [vp, DP, C.POINTER(C.c_longlong), C.c_int]
@@ -193,7 +201,7 @@ def declare(lib: C.CDLL, prefix: str) -> C.CDLL:
 EXPORTED = ["rc_abi_version", "rc_create", "rc_batch_create", "rc_layer_count", "rc_viscous_resolve_noalloc", "rc_unet_loss_grad", "rc_unet_forward_tc",
             "rc_learned_harvest", "rc_learned_harvested", "rc_learned_train", "rc_learned_get_params",
             "rc_learned_set_params", "rc_set_solver", "rc_solver_profile",
-            "rc_observe_field", "rc_observe_cells", "rc_step", "rc_step_async", "rc_wait", "rc_set_phase",
+            "rc_observe_field", "rc_observe_cells", "rc_autotune", "rc_set_cell_threads", "rc_step", "rc_step_async", "rc_wait", "rc_set_phase",
             "rc_get_sizes", "rc_download", "rc_upload", "rc_download_phi", "rc_upload_phi", "rc_set_stream",
             "rc_set_timing", "rc_timers", "rc_site_count", "rc_last_error", "rc_destroy"]
 

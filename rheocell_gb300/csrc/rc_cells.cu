@@ -765,12 +765,12 @@ struct PatchWalk {
 	}
 };
 
-template<int EVAL, int UPD>
-__global__ void __launch_bounds__(CELL_THREADS) cell_kernel_f32(const CellArgs a) {
+template<int EVAL, int UPD, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) cell_kernel_f32(const CellArgs a) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	__shared__ CellDev c;
-	__shared__ double red[12 * (CELL_THREADS / 32 + 1)];
-	__shared__ int ired[2 * (CELL_THREADS / 32)];
+	__shared__ double red[12 * (BLOCK / 32 + 1)];
+	__shared__ int ired[2 * (BLOCK / 32)];
 	const int ci = blockIdx.x;
 	{
 		const int *src = reinterpret_cast<const int *>(&a.cells[ci]);
@@ -850,7 +850,7 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel_f32(const CellArgs a
 			}
 #pragma unroll
 			for(int o = 16; o > 0; o >>= 1) pp += __shfl_down_sync(0xffffffffu, pp, o);
-			__shared__ float s_pp[CELL_THREADS / 32];
+			__shared__ float s_pp[BLOCK / 32];
 			if((threadIdx.x & 31) == 0) s_pp[threadIdx.x >> 5] = pp;
 			__syncthreads();
 			if(threadIdx.x == 0) {
@@ -1014,6 +1014,7 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel_f32(const CellArgs a
 		if(threadIdx.x == 0) {
 			o.imin[0] = imin[0];
 			o.imin[1] = imin[1];
+			o.nw = BLOCK / 32;
 			o.perim = perim;
 		}
 		return;
@@ -1055,31 +1056,48 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel_f32(const CellArgs a
 	}
 }
 
-bool launch_cell_kernel_f32(int eval, int upd, const CellArgs &a, cudaStream_t s) {
-	if(a.N <= 0) return true;
+template<int BLOCK>
+static bool launch_f32_block(int eval, int upd, const CellArgs &a, cudaStream_t s) {
 	const size_t smem = sizeof(float) * 3 * (size_t) a.smem_n;
-	if(eval == EV_LOCAL && upd == UP_PRED) cell_kernel_f32<EV_LOCAL, UP_PRED><<<a.N, CELL_THREADS, smem, s>>>(a);
-	else if(eval == EV_LOCAL && upd == UP_CORR) cell_kernel_f32<EV_LOCAL, UP_CORR><<<a.N, CELL_THREADS, smem, s>>>(a);
-	else if(eval == EV_NONE && upd == UP_PRED) cell_kernel_f32<EV_NONE, UP_PRED><<<a.N, CELL_THREADS, smem, s>>>(a);
-	else if(eval == EV_STORE && upd == UP_NONE) cell_kernel_f32<EV_STORE, UP_NONE><<<a.N, CELL_THREADS, smem, s>>>(a);
+	if(eval == EV_LOCAL && upd == UP_PRED) cell_kernel_f32<EV_LOCAL, UP_PRED, BLOCK><<<a.N, BLOCK, smem, s>>>(a);
+	else if(eval == EV_LOCAL && upd == UP_CORR) cell_kernel_f32<EV_LOCAL, UP_CORR, BLOCK><<<a.N, BLOCK, smem, s>>>(a);
+	else if(eval == EV_NONE && upd == UP_PRED) cell_kernel_f32<EV_NONE, UP_PRED, BLOCK><<<a.N, BLOCK, smem, s>>>(a);
+	else if(eval == EV_STORE && upd == UP_NONE) cell_kernel_f32<EV_STORE, UP_NONE, BLOCK><<<a.N, BLOCK, smem, s>>>(a);
 	else return false;
 	return true;
 }
 
+bool launch_cell_kernel_f32(int eval, int upd, const CellArgs &a, cudaStream_t s, int block) {
+	if(a.N <= 0) return true;
+	if(block == 128) return launch_f32_block<128>(eval, upd, a, s);
+	if(block == 512) return launch_f32_block<512>(eval, upd, a, s);
+	return launch_f32_block<256>(eval, upd, a, s);
+}
+
+template<int BLOCK>
+static cudaError_t configure_f32_block() {
+	cudaError_t e = cudaSuccess, c;
+	const int mx = 200 * 1024;
+	if((c = cudaFuncSetAttribute(cell_kernel_f32<EV_LOCAL, UP_PRED, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx)) !=
+	   cudaSuccess)
+		e = c;
+	if((c = cudaFuncSetAttribute(cell_kernel_f32<EV_LOCAL, UP_CORR, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx)) !=
+	   cudaSuccess)
+		e = c;
+	if((c = cudaFuncSetAttribute(cell_kernel_f32<EV_NONE, UP_PRED, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx)) !=
+	   cudaSuccess)
+		e = c;
+	if((c = cudaFuncSetAttribute(cell_kernel_f32<EV_STORE, UP_NONE, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx)) !=
+	   cudaSuccess)
+		e = c;
+	return e;
+}
+
 static cudaError_t configure_f32() {
 	cudaError_t e = cudaSuccess, c;
-	if((c = cudaFuncSetAttribute(cell_kernel_f32<EV_LOCAL, UP_PRED>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)) !=
-	   cudaSuccess)
-		e = c;
-	if((c = cudaFuncSetAttribute(cell_kernel_f32<EV_LOCAL, UP_CORR>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)) !=
-	   cudaSuccess)
-		e = c;
-	if((c = cudaFuncSetAttribute(cell_kernel_f32<EV_NONE, UP_PRED>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)) !=
-	   cudaSuccess)
-		e = c;
-	if((c = cudaFuncSetAttribute(cell_kernel_f32<EV_STORE, UP_NONE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)) !=
-	   cudaSuccess)
-		e = c;
+	if((c = configure_f32_block<128>()) != cudaSuccess) e = c;
+	if((c = configure_f32_block<256>()) != cudaSuccess) e = c;
+	if((c = configure_f32_block<512>()) != cudaSuccess) e = c;
 	return e;
 }
 
@@ -1094,13 +1112,14 @@ __global__ void __launch_bounds__(128) cell_finish_kernel(const CellArgs a) {
 	const CellSum &sm = a.csum[ci];
 	double acc[12];
 	if(F32) {
+		const int nw = sm.nw;
 		double t = 0.0;
-		for(int w = 0; w < CELL_THREADS / 32; w++) t += sm.area[w];
+		for(int w = 0; w < nw; w++) t += sm.area[w];
 		acc[0] = t;
 #pragma unroll
 		for(int i = 1; i < 12; i++) {
 			double u = 0.0;
-			for(int w = 0; w < CELL_THREADS / 32; w++) u += (double) sm.part[w][i];
+			for(int w = 0; w < nw; w++) u += (double) sm.part[w][i];
 			acc[i] = u;
 		}
 	}

@@ -23,6 +23,9 @@ constexpr int MAX_PATCH_SITES = 16384;
 constexpr int BIN_X = 32, BIN_Y = 8; // box bins for the cover search (one CTA each)
 constexpr int BIN_CAP = 128;         // cells listed per bin
 constexpr int CELL_THREADS = 256;
+// FP32 cell kernel: threads per cell patch, chosen among these by rc_autotune
+constexpr int CELL_MAX_THREADS = 512;
+constexpr int CELL_F32_BLOCKS[3] = {128, 256, 512};
 constexpr int OVERFLOW_SLOTS = 64;   // cells per launch whose patch exceeds shared memory
 
 enum Model { M_SIMPLE = 0, M_NEMATIC = 1, M_POLAR = 2, M_WET = 3 };

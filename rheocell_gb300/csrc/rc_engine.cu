@@ -88,6 +88,7 @@ struct rc_engine {
 	std::string err;
 	std::string launch_error;  // first failed cooperative launch
 	long long launches = 0;    // engine kernels enqueued since the last status read
+	int f32_block = CELL_THREADS;  // FP32 cell kernel: patch sites per tile (rc_autotune)
 	long long async_steps = 0;
 	// stage timers
 	bool timing = false;
@@ -248,7 +249,7 @@ static int cell_launch(rc_engine *e, int eval, int upd, const CellArgs &a0, cuda
 	CellArgs a = a0;
 	a.split = e->csum != nullptr;
 	a.csum = e->csum;
-	const bool f32 = e->hp.precision == RC_PRECISION_FLOAT && launch_cell_kernel_f32(eval, upd, a, s);
+	const bool f32 = e->hp.precision == RC_PRECISION_FLOAT && launch_cell_kernel_f32(eval, upd, a, s, e->f32_block);
 	if(!f32) launch_cell_kernel(e->P.model, eval, upd, a, s);
 	if(!a.split) return 1;
 	launch_cell_finish(e->P.model, eval, upd, f32, a, s);
@@ -899,6 +900,58 @@ int rc_wait(rc_engine *e, rc_step_stats *stats) {
 	if(stats) stats->steps_done = e->async_steps;
 	e->async_steps = 0;
 	return rc;
+}
+
+int rc_set_cell_threads(rc_engine *e, int threads) {
+	if(!e) return RC_ERR_INVALID;
+	bool ok = false;
+	for(int b : CELL_F32_BLOCKS) ok = ok || b == threads;
+	if(!ok) return set_err(e, RC_ERR_INVALID, "rc_set_cell_threads: %d is not one of 128, 256, 512", threads);
+	CUDA_TRY(e, cudaSetDevice(e->device));
+	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+	if(threads != e->f32_block) {
+		e->f32_block = threads;
+		drop_graphs(e);
+	}
+	return RC_OK;
+}
+
+int rc_autotune(rc_engine *e, int steps_per_candidate, rc_autotune_report *report) {
+	if(!e || steps_per_candidate < 1) return RC_ERR_INVALID;
+	rc_autotune_report r;
+	memset(&r, 0, sizeof(r));
+	r.chosen = e->hp.precision == RC_PRECISION_FLOAT ? e->f32_block : CELL_THREADS;
+	if(e->hp.precision != RC_PRECISION_FLOAT) {
+		if(report) *report = r;
+		return RC_OK;
+	}
+	CUDA_TRY(e, cudaSetDevice(e->device));
+	cudaEvent_t t0, t1;
+	CUDA_TRY(e, cudaEventCreate(&t0));
+	CUDA_TRY(e, cudaEventCreate(&t1));
+	int rc = RC_OK, best = -1;
+	for(int b : CELL_F32_BLOCKS) {
+		if((rc = rc_set_cell_threads(e, b))) break;
+		if((rc = rc_step(e, 1, nullptr))) break;  // captures this tile's step graph
+		cudaEventRecord(t0, e->stream);
+		if((rc = rc_step_async(e, steps_per_candidate))) break;
+		cudaEventRecord(t1, e->stream);
+		cudaEventSynchronize(t1);
+		if((rc = rc_wait(e, nullptr))) break;
+		float ms = 0.f;
+		cudaEventElapsedTime(&ms, t0, t1);
+		r.threads[r.candidates] = b;
+		r.ms_per_step[r.candidates] = (double) ms / steps_per_candidate;
+		if(best < 0 || r.ms_per_step[r.candidates] < r.ms_per_step[best]) best = r.candidates;
+		r.candidates++;
+	}
+	cudaEventDestroy(t0);
+	cudaEventDestroy(t1);
+	if(rc) return rc;
+	if((rc = rc_set_cell_threads(e, r.threads[best]))) return rc;
+	r.chosen = e->f32_block;
+	if(report) *report = r;
+	return RC_OK;
 }
 
 int rc_download_phi(rc_engine *e, double *phi, long long n) {

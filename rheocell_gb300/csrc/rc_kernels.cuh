@@ -16,10 +16,11 @@ enum UpdMode { UP_NONE = 0, UP_PRED = 1, UP_CORR = 2 };
 // per-warp partials (combined in FP64 by the epilogue kernel).
 struct CellSum {
 	double acc[12];
-	double area[CELL_THREADS / 32];
-	float part[CELL_THREADS / 32][12];
+	double area[CELL_MAX_THREADS / 32];
+	float part[CELL_MAX_THREADS / 32][12];
 	int imin[2];
-	int pad[2];
+	int nw;  // FP32 kernel: warps that wrote area/part
+	int pad;
 	double perim;
 };
 
@@ -109,7 +110,8 @@ struct CGArgs {
 cudaError_t configure_kernels();
 void launch_cell_kernel(int model, int eval, int upd, const CellArgs &a, cudaStream_t s);
 // FP32 site arithmetic for the dry polar model; false if (eval, upd) has no FP32 variant
-bool launch_cell_kernel_f32(int eval, int upd, const CellArgs &a, cudaStream_t s);
+// block: threads per cell (CELL_F32_BLOCKS); false if (eval, upd, block) has no kernel
+bool launch_cell_kernel_f32(int eval, int upd, const CellArgs &a, cudaStream_t s, int block);
 // split mode: the per-cell epilogue, one thread per cell (f32: after the FP32 kernel)
 void launch_cell_finish(int model, int eval, int upd, bool f32, const CellArgs &a, cudaStream_t s);
 size_t cell_smem_bytes(int model, int smem_n);

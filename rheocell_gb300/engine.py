@@ -191,6 +191,18 @@ class Engine:
         assert p.size == abi.RC_UNET_PARAMS
         self._check(self._lib.rc_learned_set_params(self.h, p.ctypes.data_as(abi.DP)), "rc_learned_set_params")
 
+    # --- tile-shape autotuning of the FP32 cell kernel ----------------------------
+
+    def autotune(self, steps_per_candidate: int = 4) -> Dict[str, object]:
+        """Time every cell tile on this workload and keep the fastest
+        (advances the simulation by 3 x (steps_per_candidate + 1) steps)."""
+        r = abi.RcAutotuneReport()
+        self._check(self._lib.rc_autotune(self.h, steps_per_candidate, C.byref(r)), "rc_autotune")
+        return {"candidates": [(r.threads[i], r.ms_per_step[i]) for i in range(r.candidates)], "chosen": r.chosen}
+
+    def set_cell_threads(self, threads: int) -> None:
+        self._check(self._lib.rc_set_cell_threads(self.h, threads), "rc_set_cell_threads")
+
     def close(self):
         if self.h:
             self._lib.rc_destroy(self.h)
