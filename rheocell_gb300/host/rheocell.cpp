@@ -136,6 +136,9 @@ public:
 		else if(prec == "mixed") params_.precision = RC_PRECISION_MIXED;
 		else if(prec == "float") params_.precision = RC_PRECISION_FLOAT;
 		else throw RCexception("Backend precision '" + prec + "' is not allowed");
+		cell_tile_ = inp.integer("cell_tile", 0);
+		if(cell_tile_ != 0 && cell_tile_ != 128 && cell_tile_ != 256 && cell_tile_ != 512)
+			throw RCexception("cell_tile must be 128, 256 or 512");
 		if(inp.str("box", "square") != "square") throw RCexception("only the periodic square box is provided");
 		if(inp.integer("external_forces", 0) != 0) throw RCexception("external forces are not provided");
 		if(inp.has("wall_slip") && inp.num("wall_slip") <= 0) throw RCexception("wall stencils are not provided");
@@ -277,6 +280,7 @@ public:
 		for(auto &f : fields_) hc.push_back(f.h);
 		int rc = rc_create(&params_, &box, (int) hc.size(), hc.data(), device_, &engine_);
 		if(rc) throw RCexception(std::string("GB300 engine: ") + rc_last_error(engine_));
+		if(cell_tile_) check(rc_set_cell_threads(engine_, cell_tile_));
 	}
 
 	void sim_step() { check(rc_step(engine_, 1, &stats_)); }
@@ -444,6 +448,7 @@ private:
 	long long conf_step_ = 0;
 	bool restart_step_counter_ = false;
 	int device_ = 0;
+	int cell_tile_ = 0;  // FP32 cell kernel tile (patch sites per CTA); 0: the engine's default
 	bool learned_ = false;
 	long long harvest_steps_ = 40;
 	int train_epochs_ = 20;

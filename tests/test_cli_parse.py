@@ -11,3 +11,21 @@ def test_golden_cli_files_parse():
     last = parse_confs(str(gd["last_conf_dat"]))
     assert last[0][0] == 20 and len(last[0][2]) == 9
     compare(str(gd["last_conf_dat"]), str(gd["last_conf_dat"]))
+
+
+def test_cli_rejects_invalid_keys_before_touching_the_gpu(tmp_path):
+    """Input validation of the stand-alone driver runs before the engine is
+    created, so it is checked here without a GPU."""
+    import os
+    import subprocess
+    from rheocell_gb300 import build
+    exe = os.path.join(os.path.dirname(build.LIB), "rheocell")
+    if not os.path.exists(exe):
+        build.build()
+    base = str(golden("cli_polar")["input"])
+    for extra, msg in [("cell_tile = 200", "cell_tile must be 128, 256 or 512"),
+                       ("sim_type = FD_GPU", "sim_type 'FD_GPU' is not provided"),
+                       ("backend_precision = half", "Backend precision 'half' is not allowed")]:
+        (tmp_path / "input").write_text(base + "\n" + extra + "\n")
+        res = subprocess.run([exe, "input"], cwd=tmp_path, capture_output=True, text=True, timeout=60)
+        assert res.returncode != 0 and msg in (res.stdout + res.stderr), (extra, res.stdout, res.stderr)
