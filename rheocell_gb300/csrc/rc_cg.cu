@@ -1430,10 +1430,8 @@ __global__ void __launch_bounds__(CG_THREADS, LEARNED ? 1 : 2) cg_kernel(const _
 		if(a.unet_tc) {
 			uint32_t *hold = reinterpret_cast<uint32_t *>(dsm + TC_HOLD_OFF);
 			if(threadIdx.x < 32) tc_alloc(hold, TC_COLS);
-			if(threadIdx.x == 0) {
-				mbar_init(reinterpret_cast<uint64_t *>(dsm + TC_MBAR_OFF), 1);
-				mbar_init(reinterpret_cast<uint64_t *>(dsm + TC_MBAR_OFF) + 1, 1);
-			}
+			if(threadIdx.x == 0)
+				for(int k = 0; k < TC_NMBAR; k++) mbar_init(reinterpret_cast<uint64_t *>(dsm + TC_MBAR_OFF) + k, 1);
 			tc_fence_before();
 			__syncthreads();
 			tc_fence_after();

@@ -437,10 +437,8 @@ __global__ void __launch_bounds__(512, 1) tc_layer_kernel(int l, TcSrc src, cons
 	uint32_t *hold = reinterpret_cast<uint32_t *>(tsm + TC_HOLD_OFF);
 	uint64_t *mbar = reinterpret_cast<uint64_t *>(tsm + TC_MBAR_OFF);
 	if(threadIdx.x < 32) tc_alloc(hold, TC_COLS);
-	if(threadIdx.x == 0) {
-		mbar_init(mbar, 1);
-		mbar_init(mbar + 1, 1);
-	}
+	if(threadIdx.x == 0)
+		for(int k = 0; k < TC_NMBAR; k++) mbar_init(mbar + k, 1);
 	tc_fence_before();
 	__syncthreads();
 	tc_fence_after();

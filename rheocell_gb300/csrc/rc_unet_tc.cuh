@@ -135,8 +135,10 @@ constexpr size_t TC_B_OFF = TC_A_BYTES;
 constexpr size_t TC_B_BYTES = 9 * 4 * 16 * 16;  // either layout: 9 taps x 32 channels x 16 outputs, BF16
 constexpr size_t TC_BIAS_OFF = TC_B_OFF + TC_B_BYTES;
 constexpr size_t TC_W0_OFF = TC_BIAS_OFF + 64;  // first layer's FP32 weights (IN_FIRST)
-constexpr size_t TC_MBAR_OFF = TC_W0_OFF + sizeof(float) * (9 * 2 * 16 + 16);  // two mbarriers
-constexpr size_t TC_HOLD_OFF = TC_MBAR_OFF + 16;
+constexpr int TC_NMBAR = 6;  // [0] gather mode, [1] spare, [2..5] strip mode's MMA completions
+constexpr size_t TC_MBAR_OFF = TC_W0_OFF + sizeof(float) * (9 * 2 * 16 + 16);
+constexpr size_t TC_CTRL_OFF = TC_MBAR_OFF + 8 * TC_NMBAR;  // strip mode: rows staged, rows written, abort, MMAs issued
+constexpr size_t TC_HOLD_OFF = TC_CTRL_OFF + 16;
 constexpr size_t TC_SMEM = TC_HOLD_OFF + 16;
 constexpr uint32_t TC_IDESC = tc_idesc_bf16(128, 16);
 constexpr uint32_t TC_IDESC32 = tc_idesc_bf16(128, 32);
@@ -144,7 +146,7 @@ constexpr uint32_t TC_IDESC48 = tc_idesc_bf16(128, 48);
 constexpr long long TC_WAIT_LIMIT = 2000000;  // mbarrier polls (each a bounded hardware wait)
 
 // Per-CTA state of the tensor-core layers: shared memory (TC_SMEM bytes,
-// the two mbarriers at TC_MBAR_OFF initialised with count 1), the TMEM
+// the TC_NMBAR mbarriers at TC_MBAR_OFF initialised with count 1), the TMEM
 // allocation (TC_COLS columns) and the parities the mbarriers wait for next.
 // err/err_bit: where a wait that ran out is recorded.  tns (diagnostics, may
 // be null): block 0 adds the time of weight and operand staging (tns[0]),
@@ -158,7 +160,38 @@ struct TcCtx {
 	int *err;
 	int err_bit;
 	unsigned long long *tns;
+	unsigned long long mma_rows = 0;  // strip mode: input rows multiplied so far (indexes the MMA mbarriers)
 };
+
+// Shared-memory flags between the roles of the strip pipeline.
+__device__ __forceinline__ int ld_acquire_s32(const int *p) {
+	int v;
+	asm volatile("ld.acquire.cta.shared::cta.b32 %0, [%1];" : "=r"(v) : "r"(smem_u32(p)) : "memory");
+	return v;
+}
+__device__ __forceinline__ void st_release_s32(int *p, int v) {
+	asm volatile("st.release.cta.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(p)), "r"(v) : "memory");
+}
+// Barrier among `n` threads (a multiple of 32) under id (1 - 15).
+__device__ __forceinline__ void bar_named(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+// The same, returning whether any participant passed v = true.
+__device__ __forceinline__ bool bar_named_or(int id, int n, bool v) {
+	uint32_t r;
+	asm volatile(
+	    "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.or.pred q, %2, %3, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
+	    : "=r"(r)
+	    : "r"((uint32_t) v), "r"(id), "r"(n)
+	    : "memory");
+	return r != 0;
+}
+// Bounded wait for an mbarrier phase that also gives up once *abort is set.
+__device__ __forceinline__ bool mbar_wait_abort(uint64_t *mbar, uint32_t parity, const volatile int *abort, long long limit) {
+	for(long long i = 0; i < limit; i++) {
+		if(mbar_try_wait(mbar, parity)) return true;
+		if((i & 31) == 31 && *abort) return false;
+	}
+	return false;
+}
 
 __device__ __forceinline__ float2 bf2f(uint32_t u) {
 	__nv_bfloat162 h = *reinterpret_cast<__nv_bfloat162 *>(&u);
@@ -291,13 +324,17 @@ struct TcTimer {
 // 0 only issues MMAs, so quarter 0 of tiles 0 .. 3 goes to warps 4, 8, 12, 4.
 __device__ __forceinline__ int tc_epi_warp(int r, int q) { return q ? q + 4 * r : 4 + 4 * (r % 3); }
 
-// Strip mode (L a multiple of 128); requires 512 threads: warp 0 issues the
-// MMAs, warps 1 - 15 stage rows (two rows ahead, three buffers) and write
-// out finished rows.  wl: the layer's
+// Strip mode (L a multiple of 128); requires 512 threads in three roles that
+// run decoupled: warp 0 issues the MMAs, warps 1 - 7 stage input rows into a
+// ring of three buffers, warps 8 - 15 write finished output rows out of TMEM.
+// Rows pass between the roles through release/acquire counters in shared
+// memory (rows staged, rows written out) and the MMA completion mbarriers;
+// every wait is bounded and gives up when any role has set the abort flag,
+// and the roles' own barriers are reached by all of their threads or none.  wl: the layer's
 // FP32 weights [tap = (dy + 1) * 3 + dx + 1][ci][16]; bias: 16 FP32.
 static __device__ __noinline__ bool tc_conv_strip(int l, const TcSrc &src, const float *wl, const float *bias, bf16 *dst,
                                                   int batch, int L, TcCtx &c) {
-	TcTimer tm(c.tns, 32);  // block 0's first staging/epilogue thread
+	TcTimer tm(c.tns, 256);  // block 0's first write-out thread
 	const UNetLayerDesc d = unet_layer(l);
 	const int KC = d.ci / 8, KS = KC / 2;
 	const int ntile = L / 128;
@@ -328,11 +365,15 @@ static __device__ __noinline__ bool tc_conv_strip(int l, const TcSrc &src, const
 	float *w0s = reinterpret_cast<float *>(c.sm + TC_W0_OFF);
 	if(src.mode == IN_FIRST)
 		for(int k = threadIdx.x; k < 9 * 2 * 16 + 16; k += blockDim.x) w0s[k] = src.w0[k];
+	if(threadIdx.x == 0) reinterpret_cast<int *>(c.sm + TC_CTRL_OFF)[2] = 0;
 	fence_async_smem();
 	__syncthreads();
 	tm.mark(0);
 	const uint32_t a_base = smem_u32(Abuf), b_base = smem_u32(Bh);
 	const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	int *ctrl = reinterpret_cast<int *>(c.sm + TC_CTRL_OFF);  // [0] rows staged, [1] rows written, [2] abort, [3] MMAs issued
+	const volatile int *abort = ctrl + 2;
+	uint64_t *acc = mbar + 2;  // MMA completion of input row g on acc[g & 3], phase (g >> 2) & 1
 	const long long per = (U + gridDim.x - 1) / gridDim.x;
 	const long long u0 = blockIdx.x * per, u1 = u0 + per < U ? u0 + per : U;
 	for(long long u = u0; u < u1;) {
@@ -340,35 +381,43 @@ static __device__ __noinline__ bool tc_conv_strip(int l, const TcSrc &src, const
 		const int y0 = (int) (u - col * L);
 		const int y1 = (int) ((u1 - col * L) < L ? (u1 - col * L) : L);  // exclusive
 		const int n = (int) (col / NS), x0 = (int) (col - (long long) n * NS) * W;
-		const int nin = y1 - y0 + 2;  // input rows y0 - 1 .. y1
-		// all slots of this CTA's tiles zero; input rows 0 and 1 staged
-		for(int pr = 0; pr < T * 4; pr++) {
-			const int r = pr >> 2, q = pr & 3;
-			if(w != tc_epi_warp(r, q)) continue;
-			for(int sl = 0; sl < R + 2; sl++)
-				tc_st16_zero(c.tmem + ((uint32_t) (32 * q) << 16) + (uint32_t) ((r * (R + 2) + sl) * 16));
-		}
+		const int nin = y1 - y0 + 2;  // input rows y0 - 1 .. y1; output rows y0 - 2 .. y1 - 1
+		// all slots zero (by the warps that will write them out), counters reset
+		if(w >= 8)
+			for(int r = (w - 8) >> 2; r < T; r += 2)
+				for(int sl = 0; sl < R + 2; sl++)
+					tc_st16_zero(c.tmem + ((uint32_t) (32 * (w & 3)) << 16) + (uint32_t) ((r * (R + 2) + sl) * 16));
 		tc_wait_st();
-		if(w > 0) {
-			tc_stage_strip_row(src, KC, n, wrap(y0 - 1, L), x0, HW, L, Abuf, w0s, threadIdx.x - 32, blockDim.x - 32);
-			cp_async_commit();
-			if(nin > 1) tc_stage_strip_row(src, KC, n, wrap(y0, L), x0, HW, L, Abuf + KC * HW, w0s, threadIdx.x - 32, blockDim.x - 32);
-			cp_async_commit();
-			cp_async_wait_1();
+		if(threadIdx.x == 0) {
+			ctrl[0] = 0;
+			ctrl[1] = 0;
+			ctrl[3] = 0;
 		}
-		fence_async_smem();
 		tc_fence_before();
 		__syncthreads();
 		tc_fence_after();
 		tm.mark(1);
-		for(int i = 0; i <= nin; i++) {
-			bool fail = false;
-			if(w == 0) {
-				// the MMA warp: MMAs of input row y0 - 1 + i (buffer i % 3) into
-				// the slots of output rows y0 - 2 + i .. y0 + i: physical slots
-				// s0 .. s0 + 2, where physical slot R or R + 1 stands for
-				// logical slot 0 or 1
-				if(i < nin && lane == 0) {
+		const unsigned long long G = c.mma_rows;
+		if(w == 0) {
+			// MMA warp: input row i (buffer i % 3) once it is staged and output
+			// row i - 4 has been written out (its slot is reused and the MMA
+			// mbarriers stay at most one phase ahead of their waiters)
+			if(lane == 0) {
+				for(int i = 0; i < nin; i++) {
+					bool ok = false;
+					for(long long t = 0; t < TC_WAIT_LIMIT; t++) {
+						if(ld_acquire_s32(&ctrl[0]) >= i + 1 && ld_acquire_s32(&ctrl[1]) >= i - 3) {
+							ok = true;
+							break;
+						}
+						if(*abort) break;
+					}
+					if(!ok) {
+						ctrl[2] = 1;
+						break;
+					}
+					tc_fence_after();
+					fence_async_smem();
 					const uint32_t abuf = a_base + (uint32_t) ((i % 3) * KC * HW * 16);
 					const int s0 = i % R;
 					for(int r = 0; r < T; r++) {
@@ -382,65 +431,82 @@ static __device__ __noinline__ bool tc_conv_strip(int l, const TcSrc &src, const
 							}
 						}
 					}
-					tc_commit(&mbar[i & 1]);
+					tc_commit(&acc[(G + i) & 3]);
+					ctrl[3] = i + 1;
 				}
-				__syncwarp();
-				if(i >= 1) c.phase[(i - 1) & 1] ^= 1u;
 			}
-			else {
-				if(i >= 1) {
-					// MMAs of input row i - 1 done: its buffer is free and
-					// output row y0 - 3 + i is complete
-					const int b = (i - 1) & 1;
-					fail = !mbar_wait(&mbar[b], c.phase[b], TC_WAIT_LIMIT);
-					c.phase[b] ^= 1u;
-					tc_fence_after();
-				}
-				tm.mark(2);
-				// input row i + 2 into buffer (i + 2) % 3 (that of row i - 1)
-				if(!fail && i + 2 < nin)
-					tc_stage_strip_row(src, KC, n, wrap(y0 + 1 + i, L), x0, HW, L, Abuf + ((i + 2) % 3) * KC * HW, w0s,
-					                   threadIdx.x - 32, blockDim.x - 32);
-				cp_async_commit();
-				tm.mark(0);
-				if(!fail && i >= 1) {
-					const int y = y0 - 3 + i, sl = (i - 1) % R;
-					for(int pr = 0; pr < T * 4; pr++) {
-						const int r = pr >> 2, q = pr & 3;
-						if(w != tc_epi_warp(r, q)) continue;
-						const uint32_t ta = c.tmem + ((uint32_t) (32 * q) << 16) + (uint32_t) ((r * (R + 2) + sl) * 16);
-						if(y >= y0) {
-							float v[16];
-							tc_ld16(ta, v);
-							if(sl < 2) {
-								float o[16];
-								tc_ld16(ta + (uint32_t) (R * 16), o);
-#pragma unroll
-								for(int k = 0; k < 16; k++) v[k] += o[k];
-							}
-							tc_store_pixel(v, bs, dst, ((long long) n * L + y) * L + x0 + r * 128 + 32 * q + lane);
-						}
-						tc_st16_zero(ta);
-						if(sl < 2) tc_st16_zero(ta + (uint32_t) (R * 16));
-					}
-					tc_wait_st();
-				}
-				tm.mark(3);
-				// input row i + 1 landed (the group of the previous iteration)
-				cp_async_wait_1();
-			}
-			fence_async_smem();
-			tc_fence_before();
-			if(__syncthreads_or(fail)) {
-				// let the MMAs in flight finish before giving up
-				if(threadIdx.x == 0) atomicOr(c.err, c.err_bit);
-				mbar_wait(&mbar[i & 1], c.phase[i & 1], TC_WAIT_LIMIT);
-				cp_async_wait_all();
-				return false;
-			}
-			tc_fence_after();
-			tm.mark(1);
+			__syncwarp();
 		}
+		else if(w < 8) {
+			// staging warps: row r into buffer r % 3 once the MMAs of row r - 3
+			// (the buffer's previous row) are done
+			const int pt = threadIdx.x - 32, np = 224;
+			for(int r = 0; r < nin; r++) {
+				bool ok = true;
+				if(r >= 3 && pt == 0) {
+					const unsigned long long g = G + r - 3;
+					ok = mbar_wait_abort(&acc[g & 3], (uint32_t) ((g >> 2) & 1), abort, TC_WAIT_LIMIT);
+					if(!ok) ctrl[2] = 1;
+				}
+				if(bar_named_or(1, np, !ok || *abort != 0)) break;
+				tc_stage_strip_row(src, KC, n, wrap(y0 - 1 + r, L), x0, HW, L, Abuf + (r % 3) * KC * HW, w0s, pt, np);
+				cp_async_wait_all();
+				fence_async_smem();
+				bar_named(1, np);
+				if(pt == 0) st_release_s32(&ctrl[0], r + 1);
+			}
+		}
+		else {
+			// write-out warps: output row y0 - 2 + m once the MMAs of input row
+			// m are done (bias, ReLU, BF16; rows above the band only cleared)
+			const int et = threadIdx.x - 256;
+			for(int m = 0; m < nin; m++) {
+				const unsigned long long g = G + m;
+				const bool ok = mbar_wait_abort(&acc[g & 3], (uint32_t) ((g >> 2) & 1), abort, TC_WAIT_LIMIT);
+				if(!ok) ctrl[2] = 1;
+				if(bar_named_or(2, 256, !ok || *abort != 0)) break;
+				tc_fence_after();
+				tm.mark(2);
+				const int y = y0 - 2 + m, sl = m % R;
+				for(int r = (w - 8) >> 2; r < T; r += 2) {
+					const uint32_t ta = c.tmem + ((uint32_t) (32 * (w & 3)) << 16) + (uint32_t) ((r * (R + 2) + sl) * 16);
+					if(y >= y0) {
+						float v[16];
+						tc_ld16(ta, v);
+						if(sl < 2) {
+							float o[16];
+							tc_ld16(ta + (uint32_t) (R * 16), o);
+#pragma unroll
+							for(int k = 0; k < 16; k++) v[k] += o[k];
+						}
+						tc_store_pixel(v, bs, dst, ((long long) n * L + y) * L + x0 + r * 128 + 32 * (w & 3) + lane);
+					}
+					tc_st16_zero(ta);
+					if(sl < 2) tc_st16_zero(ta + (uint32_t) (R * 16));
+				}
+				tc_wait_st();
+				tc_fence_before();
+				bar_named(2, 256);
+				if(et == 0) st_release_s32(&ctrl[1], m + 1);
+				tm.mark(3);
+			}
+		}
+		__syncthreads();
+		if(ctrl[2]) {
+			// let the MMAs in flight finish before giving up
+			if(threadIdx.x == 0) {
+				atomicOr(c.err, c.err_bit);
+				const int issued = ctrl[3];
+				if(issued > 0) {
+					const unsigned long long g = G + issued - 1;
+					mbar_wait(&acc[g & 3], (uint32_t) ((g >> 2) & 1), TC_WAIT_LIMIT);
+				}
+			}
+			cp_async_wait_all();
+			__syncthreads();
+			return false;
+		}
+		c.mma_rows += nin;
 		u += y1 - y0;
 	}
 	return true;
