@@ -236,8 +236,12 @@ enum { RES_FP64 = 0, RES_FLOAT_UNKNOWN = 1, RES_FLOAT_COVER = 2 };
 // per component, unscaled.  Reduces |b|^2, |r|^2 and r.M^-1 r (the latter
 // on the stored precision of r) into sh.tot[0..5], each thread's partial
 // sums in box-site order, so the totals are reproducible.
+// want_b: also |b|^2 (needed once per solve); want_rz: also r.M^-1 r (not
+// needed by the flexible CG, which forms its own).  Unrequested sums are 0.
+// GB300 issues FP64 at a small fraction of the FP32 rate, so the residual
+// does no FP64 work it does not need.
 template<int fmode>
-__device__ __forceinline__ bool true_residual(const CGArgs &a, CGShared &sh, bool x_zero) {
+__device__ __forceinline__ bool true_residual(const CGArgs &a, CGShared &sh, bool x_zero, bool want_b = true, bool want_rz = true) {
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
 	const double neta = -a.eta * 1.0;
@@ -279,8 +283,8 @@ __device__ __forceinline__ bool true_residual(const CGArgs &a, CGShared &sh, boo
 					ry = by - 0.0;
 				}
 				else {
-					rx = bx - (T * a.vx[j] + qx);
-					ry = by - (T * a.vy[j] + qy);
+					rx = bx - __fma_rn(T, a.vx[j], qx);
+					ry = by - __fma_rn(T, a.vy[j], qy);
 				}
 				if(fmode != RES_FLOAT_COVER) {
 					// the learned path never reads the FP64 residual (its FP64
@@ -288,10 +292,12 @@ __device__ __forceinline__ bool true_residual(const CGArgs &a, CGShared &sh, boo
 					a.rx[j] = rx;
 					a.ry[j] = ry;
 				}
-				v[0] += bx * bx;
-				v[1] += by * by;
-				v[2] += rx * rx;
-				v[3] += ry * ry;
+				if(want_b) {
+					v[0] = __fma_rn(bx, bx, v[0]);
+					v[1] = __fma_rn(by, by, v[1]);
+				}
+				v[2] = __fma_rn(rx, rx, v[2]);
+				v[3] = __fma_rn(ry, ry, v[3]);
 				if(fmode != RES_FP64) {
 					const float fx = (float) rx, fy = (float) ry;
 					const int o = fmode == RES_FLOAT_COVER ? e : j;
@@ -299,12 +305,14 @@ __device__ __forceinline__ bool true_residual(const CGArgs &a, CGShared &sh, boo
 					a.ryf[o] = fy;
 					a.exf[o] = 0.0f;
 					a.eyf[o] = 0.0f;
-					v[4] += (double) fx * (iT * (double) fx);
-					v[5] += (double) fy * (iT * (double) fy);
+					if(want_rz) {
+						v[4] += (double) fx * (iT * (double) fx);
+						v[5] += (double) fy * (iT * (double) fy);
+					}
 					Rx += fx * iTf;
 					Ry += fy * iTf;
 				}
-				else {
+				else if(want_rz) {
 					v[4] += rx * (iT * rx);
 					v[5] += ry * (iT * ry);
 				}
@@ -1294,7 +1302,7 @@ __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcCtx &tc
 	const bool mixed = a.mixed != 0;
 	if(!build_csr(a, sh)) return;
 	constexpr int fmode = LEARNED ? RES_FLOAT_COVER : RES_FLOAT_UNKNOWN;
-	if(!(mixed ? true_residual<fmode>(a, sh, cold != 0) : true_residual<RES_FP64>(a, sh, cold != 0))) return;
+	if(!(mixed ? true_residual<fmode>(a, sh, cold != 0, true, !LEARNED) : true_residual<RES_FP64>(a, sh, cold != 0))) return;
 	pmark(a, sh, PH_START);
 	if(threadIdx.x == 0) {
 		for(int c = 0; c < 2; c++) {
@@ -1366,7 +1374,7 @@ __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcCtx &tc
 			}
 			refinements++;
 			if(!grid_reduce(a, sh, 0, nullptr)) return;
-			if(!true_residual<fmode>(a, sh, false)) return;
+			if(!true_residual<fmode>(a, sh, false, false, !LEARNED)) return;
 			if(threadIdx.x == 0) {
 				for(int c = 0; c < 2; c++) {
 					sh.rn2[c] = sh.tot[2 + c];
@@ -1382,7 +1390,7 @@ __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcCtx &tc
 		}
 		if(s_fallback || sh.act[0] || sh.act[1]) {
 			// plain FP64 CG from the current x (the residual is in rx, ry)
-			if(!true_residual<RES_FP64>(a, sh, false)) return;
+			if(!true_residual<RES_FP64>(a, sh, false, false, true)) return;
 			if(threadIdx.x == 0) {
 				for(int c = 0; c < 2; c++) {
 					sh.rn2[c] = sh.tot[2 + c];
