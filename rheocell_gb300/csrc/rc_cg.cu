@@ -240,8 +240,12 @@ enum { RES_FP64 = 0, RES_FLOAT_UNKNOWN = 1, RES_FLOAT_COVER = 2 };
 // needed by the flexible CG, which forms its own).  Unrequested sums are 0.
 // GB300 issues FP64 at a small fraction of the FP32 rate, so the residual
 // does no FP64 work it does not need.
+// add_e: first x += e, the FP32 correction of the last refinement sweep
+// (exf/eyf, in cover order for RES_FLOAT_COVER, by unknown otherwise), fused
+// into the pass that forms the box sums of x.
 template<int fmode>
-__device__ __forceinline__ bool true_residual(const CGArgs &a, CGShared &sh, bool x_zero, bool want_b = true, bool want_rz = true) {
+__device__ __forceinline__ bool true_residual(const CGArgs &a, CGShared &sh, bool x_zero, bool want_b = true, bool want_rz = true,
+                                              bool add_e = false) {
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
 	const double neta = -a.eta * 1.0;
@@ -255,8 +259,16 @@ __device__ __forceinline__ bool true_residual(const CGArgs &a, CGShared &sh, boo
 #pragma unroll 1
 			for(int e = e0; e < e1; e++) {
 				const int j = cov_idx[e];
-				sx += a.vx[j];
-				sy += a.vy[j];
+				double ux = a.vx[j], uy = a.vy[j];
+				if(add_e) {
+					const int o = fmode == RES_FLOAT_COVER ? e : j;
+					ux += (double) a.exf[o];
+					uy += (double) a.eyf[o];
+					a.vx[j] = ux;
+					a.vy[j] = uy;
+				}
+				sx += ux;
+				sy += uy;
 			}
 			a.Px[k] = sx;
 			a.Py[k] = sy;
@@ -1358,23 +1370,9 @@ __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcCtx &tc
 				if(!cg_iterate<float>(a, sh, CGVecs<float>{a.rxf, a.ryf, a.pxf, a.pyf, a.apxf, a.apyf, a.Pxf, a.Pyf, a.exf, a.eyf}, max_it))
 					return;
 			}
-			if constexpr(LEARNED) {
-				// the correction is in cover order
-				for(long long e = gtid; e < S; e += gstride) {
-					const int j = a.cov_idx[e];
-					a.vx[j] += (double) a.exf[e];
-					a.vy[j] += (double) a.eyf[e];
-				}
-			}
-			else {
-				for(long long j = gtid; j < S; j += gstride) {
-					a.vx[j] += (double) a.exf[j];
-					a.vy[j] += (double) a.eyf[j];
-				}
-			}
 			refinements++;
-			if(!grid_reduce(a, sh, 0, nullptr)) return;
-			if(!true_residual<fmode>(a, sh, false, false, !LEARNED)) return;
+			// x += e and r = b - A x
+			if(!true_residual<fmode>(a, sh, false, false, !LEARNED, true)) return;
 			if(threadIdx.x == 0) {
 				for(int c = 0; c < 2; c++) {
 					sh.rn2[c] = sh.tot[2 + c];
