@@ -20,6 +20,10 @@
 
 namespace rc {
 
+// F32: for the FP32 engines (dry polar, phi^2 only): conversions on the
+// integer pipes and FP32 sums in the same cell order, stored exactly as
+// doubles; the FP32 cell kernel reads them back in FP32.
+template<bool F32>
 __global__ void __launch_bounds__(BIN_X *BIN_Y) box_gather_kernel(const BoxArgs a) {
 	__shared__ int s_ids[BIN_CAP];
 	__shared__ int s_sorted[BIN_CAP];
@@ -70,6 +74,30 @@ __global__ void __launch_bounds__(BIN_X *BIN_Y) box_gather_kernel(const BoxArgs 
 	const int kl = x + y * L;                      // site in the layer's box
 	const long long k = lay.box_off + kl;          // index into the batch's box arrays
 	const size_t L2 = (size_t) L * (size_t) L;
+	if constexpr(F32) {
+		float p2f = 0.f;
+		int n = 0;
+		for(int i = 0; i < count; i++) {
+			int rx = x - s_cx[i];
+			if(rx < 0) rx += L;
+			int ry = y - s_cy[i];
+			if(ry < 0) ry += L;
+			if(rx >= s_lx[i] || ry >= s_ly[i]) continue;
+			int sx = rx - s_ox[i];
+			if(sx < 0) sx += s_lx[i];
+			int sy = ry - s_oy[i];
+			if(sy < 0) sy += s_ly[i];
+			const float phi = d2f_int(a.phi[s_start[i] + sy * s_lx[i] + sx]);
+			p2f = __fmaf_rn(phi, phi, p2f);
+			n++;
+		}
+		a.phi2[k] = f2d_int(p2f);
+		if(a.check_overlap && n > STORE_MAX) {
+			atomicOr(&a.st->err, ERR_OVERLAP);
+			a.st->err_where = k;
+		}
+		return;
+	}
 	double p2 = 0.0, q0 = 0.0, q1 = 0.0;
 	int n = 0;
 	for(int i = 0; i < count; i++) {
@@ -125,7 +153,8 @@ __global__ void bookkeeping_kernel(DevStatus *st, int restart_every, int solve_f
 }
 
 void launch_box_gather(const BoxArgs &a, cudaStream_t s) {
-	box_gather_kernel<<<a.total_bins, BIN_X * BIN_Y, 0, s>>>(a);
+	if(a.f32) box_gather_kernel<true><<<a.total_bins, BIN_X * BIN_Y, 0, s>>>(a);
+	else box_gather_kernel<false><<<a.total_bins, BIN_X * BIN_Y, 0, s>>>(a);
 	if(a.bookkeeping) bookkeeping_kernel<<<1, 1, 0, s>>>(a.st, a.restart_every, a.solve_follows);
 }
 

@@ -699,30 +699,6 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 }
 
 // ---------------------------------------------------------------- FP32 ---
-// double <-> float conversions on the integer pipes (on GB300 the conversion
-// instructions issue on the narrow FP64 pipe).  Round to nearest even;
-// magnitudes below the FP32 normal range become zero and the fields' values
-// never reach the FP32 overflow range.
-__device__ __forceinline__ float d2f_int(double v) {
-	const unsigned hi = (unsigned) __double2hiint(v), lo = (unsigned) __double2loint(v);
-	const unsigned sign = hi & 0x80000000u;
-	const int e = (int) ((hi >> 20) & 0x7FFu) - 896;  // FP32 biased exponent
-	if(e <= 0) return __uint_as_float(sign);
-	unsigned m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
-	const unsigned r = lo & 0x1FFFFFFFu;
-	unsigned bits = sign | ((unsigned) e << 23);
-	bits += m;
-	if(r > 0x10000000u || (r == 0x10000000u && (m & 1u))) bits += 1u;  // carries into the exponent
-	return __uint_as_float(bits);
-}
-
-__device__ __forceinline__ double f2d_int(float v) {
-	const unsigned b = __float_as_uint(v);
-	const unsigned sign = b & 0x80000000u, e = (b >> 23) & 0xFFu, m = b & 0x7FFFFFu;
-	if(e == 0u) return __hiloint2double((int) sign, 0);
-	return __hiloint2double((int) (sign | ((e + 896u) << 20) | (m >> 3)), (int) (m << 29));
-}
-
 // Double-float accumulation of x*x: (s, c) holds the running sum with its
 // error term (exact product by FMA, Knuth's TwoSum), close to FP64 accuracy
 // with FP32 arithmetic only.

@@ -276,6 +276,7 @@ static void gather(rc_engine *e, const double *phi, int phase) {
 	b.want_q = (e->P.model == M_NEMATIC || e->P.model == M_WET);
 	b.want_cover = wet_phase(e, phase);
 	b.check_overlap = (e->P.model == M_POLAR || e->P.model == M_WET);
+	b.f32 = e->hp.precision == RC_PRECISION_FLOAT && !b.want_q && !b.want_cover;
 	b.bookkeeping = (e->P.model == M_POLAR || e->P.model == M_WET);
 	b.restart_every = e->hp.cg_restart_every;
 	b.solve_follows = wet_phase(e, phase);

@@ -61,6 +61,7 @@ struct BoxArgs {
 	const int *bin_count, *bin_cells;
 	int nbx, nby;
 	int want_q, want_cover, check_overlap;
+	int f32;               // FP32 engines: phi^2 summed in FP32 (the cell kernel reads it in FP32)
 	int bookkeeping;       // wet models: size_rows / restart bookkeeping of this evaluation
 	int restart_every;
 	int solve_follows;     // a viscous solve follows this evaluation
