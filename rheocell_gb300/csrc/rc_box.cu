@@ -20,6 +20,7 @@
 
 namespace rc {
 
+
 // F32: for the FP32 engines (dry polar, phi^2 only): conversions on the
 // integer pipes and FP32 sums in the same cell order, stored exactly as
 // doubles; the FP32 cell kernel reads them back in FP32.
@@ -30,14 +31,7 @@ __global__ void __launch_bounds__(BIN_X *BIN_Y) box_gather_kernel(const BoxArgs 
 	__shared__ int s_cx[BIN_CAP], s_cy[BIN_CAP], s_lx[BIN_CAP], s_ly[BIN_CAP], s_ox[BIN_CAP], s_oy[BIN_CAP],
 	    s_start[BIN_CAP];
 	__shared__ double s_q00[BIN_CAP], s_q01[BIN_CAP];
-	// layer of this bin: the last layer whose bin_off <= blockIdx.x
-	int lo = 0, hi = a.n_layers - 1;
-	while(lo < hi) {
-		const int mid = (lo + hi + 1) / 2;
-		if(a.layers[mid].bin_off <= (int) blockIdx.x) lo = mid;
-		else hi = mid - 1;
-	}
-	const LayerDev lay = a.layers[lo];
+	const LayerDev lay = a.layers[a.bin_layer[blockIdx.x]];
 	const int b = blockIdx.x;
 	const int lb = b - lay.bin_off;
 	const int bxi = lb % lay.nbx, byi = lb / lay.nbx;
@@ -74,20 +68,25 @@ __global__ void __launch_bounds__(BIN_X *BIN_Y) box_gather_kernel(const BoxArgs 
 	const int kl = x + y * L;                      // site in the layer's box
 	const long long k = lay.box_off + kl;          // index into the batch's box arrays
 	const size_t L2 = (size_t) L * (size_t) L;
+	auto site_in = [&](int i) {
+		int rx = x - s_cx[i];
+		if(rx < 0) rx += L;
+		int ry = y - s_cy[i];
+		if(ry < 0) ry += L;
+		if(rx >= s_lx[i] || ry >= s_ly[i]) return -1;
+		int sx = rx - s_ox[i];
+		if(sx < 0) sx += s_lx[i];
+		int sy = ry - s_oy[i];
+		if(sy < 0) sy += s_ly[i];
+		return s_start[i] + sy * s_lx[i] + sx;
+	};
 	if constexpr(F32) {
 		float p2f = 0.f;
 		int n = 0;
 		for(int i = 0; i < count; i++) {
-			int rx = x - s_cx[i];
-			if(rx < 0) rx += L;
-			int ry = y - s_cy[i];
-			if(ry < 0) ry += L;
-			if(rx >= s_lx[i] || ry >= s_ly[i]) continue;
-			int sx = rx - s_ox[i];
-			if(sx < 0) sx += s_lx[i];
-			int sy = ry - s_oy[i];
-			if(sy < 0) sy += s_ly[i];
-			const float phi = d2f_int(a.phi[s_start[i] + sy * s_lx[i] + sx]);
+			const int j = site_in(i);
+			if(j < 0) continue;
+			const float phi = d2f_int(a.phi[j]);
 			p2f = __fmaf_rn(phi, phi, p2f);
 			n++;
 		}
@@ -101,16 +100,8 @@ __global__ void __launch_bounds__(BIN_X *BIN_Y) box_gather_kernel(const BoxArgs 
 	double p2 = 0.0, q0 = 0.0, q1 = 0.0;
 	int n = 0;
 	for(int i = 0; i < count; i++) {
-		int rx = x - s_cx[i];
-		if(rx < 0) rx += L;
-		int ry = y - s_cy[i];
-		if(ry < 0) ry += L;
-		if(rx >= s_lx[i] || ry >= s_ly[i]) continue;
-		int sx = rx - s_ox[i];
-		if(sx < 0) sx += s_lx[i];
-		int sy = ry - s_oy[i];
-		if(sy < 0) sy += s_ly[i];
-		const int j = s_start[i] + sy * s_lx[i] + sx;
+		const int j = site_in(i);
+		if(j < 0) continue;
 		const double phi = a.phi[j];
 		p2 += phi * phi;
 		if(a.want_q) {

@@ -61,6 +61,7 @@ struct rc_engine {
 	int cg_blocks = 0;
 	int nbx = 0, nby = 0;        // bins of layer 0 (single-monolayer solver paths)
 	int n_layers = 1, total_bins = 0;
+	int *bin_layer = nullptr;  // layer of each bin
 	long long total_box = 0;
 	std::vector<LayerDev> layers_h;
 	LayerDev *layers = nullptr;
@@ -273,6 +274,7 @@ static void gather(rc_engine *e, const double *phi, int phase) {
 	b.layers = e->layers;
 	b.n_layers = e->n_layers;
 	b.total_bins = e->total_bins;
+	b.bin_layer = e->bin_layer;
 	b.want_q = (e->P.model == M_NEMATIC || e->P.model == M_WET);
 	b.want_cover = wet_phase(e, phase);
 	b.check_overlap = (e->P.model == M_POLAR || e->P.model == M_WET);
@@ -778,7 +780,7 @@ int rc_batch_create(const rc_params *params, int n_layers, const rc_box *boxes, 
 	   (rc = dalloc(e, &e->vx, cap)) || (rc = dalloc(e, &e->vy, cap)) || (rc = dalloc(e, &e->mapg, cap)) ||
 	   (rc = dalloc(e, &e->phi2, L2)) || (rc = dalloc(e, &e->sq00, L2)) || (rc = dalloc(e, &e->sq01, L2)) ||
 	   (rc = dalloc(e, &e->cnt, L2)) ||
-	   (rc = dalloc(e, &e->bin_count, (size_t) total_bins)) ||
+	   (rc = dalloc(e, &e->bin_count, (size_t) total_bins)) || (rc = dalloc(e, &e->bin_layer, (size_t) total_bins)) ||
 	   (rc = dalloc(e, &e->bin_cells, (size_t) total_bins * BIN_CAP)) ||
 	   (rc = dalloc(e, &e->layers, (size_t) n_layers)) ||
 	   (rc = dalloc(e, &e->tab_cos, (size_t) table_base(MAX_TABLE_SIDE + 1))) ||
@@ -840,6 +842,13 @@ int rc_batch_create(const rc_params *params, int n_layers, const rc_box *boxes, 
 		}
 		CUDA_TRY(e, cudaMemcpy(e->cells, hc.data(), sizeof(CellDev) * (size_t) std::max(n_cells, 1), cudaMemcpyHostToDevice));
 		CUDA_TRY(e, cudaMemcpy(e->layers, layers.data(), sizeof(LayerDev) * (size_t) n_layers, cudaMemcpyHostToDevice));
+		{
+			// bin -> layer, so that a bin's CTA finds its layer with one load
+			std::vector<int> bl((size_t) total_bins);
+			for(int l = 0; l < n_layers; l++)
+				for(int b = 0; b < layers[(size_t) l].nbx * layers[(size_t) l].nby; b++) bl[(size_t) (layers[(size_t) l].bin_off + b)] = l;
+			CUDA_TRY(e, cudaMemcpy(e->bin_layer, bl.data(), sizeof(int) * (size_t) total_bins, cudaMemcpyHostToDevice));
+		}
 		if(S) CUDA_TRY(e, cudaMemcpy(e->phiA, phi.data(), sizeof(double) * (size_t) S, cudaMemcpyHostToDevice));
 		DevStatus h;
 		memset(&h, 0, sizeof(h));

@@ -59,6 +59,7 @@ struct BoxArgs {
 	double *phi2, *sq00, *sq01;
 	int *cnt, *cover;      // cover[slot * L*L + k]
 	const int *bin_count, *bin_cells;
+	const int *bin_layer;  // layer of each bin
 	int nbx, nby;
 	int want_q, want_cover, check_overlap;
 	int f32;               // FP32 engines: phi^2 summed in FP32 (the cell kernel reads it in FP32)
