@@ -88,3 +88,33 @@ def test_network_cuts_inner_iterations(trained, solver):
     print("inner iterations: plain", it_plain, res_plain, "learned", it_learned, res_learned)
     assert res_plain < 1e-8 and res_learned < 1e-8
     assert it_learned < 0.5 * it_plain, (it_learned, it_plain)
+
+
+def test_learned_solve_with_strip_layers_matches_fp64_oracle(trained):
+    """A 128^2 monolayer with the network trained on the 64^2 one: its finest
+    level runs the strip tensor-core layers (first layer fused into the
+    second's staging, decoupled row pipeline), the coarser levels the gathered
+    ones; velocities within 1e-7 of the FP64 oracle, FP64 stopping rule met."""
+    _, _, e64, _, _ = trained
+    params = e64.get_params()
+    m = g.make_monolayer(128, 64, seed=41)
+    keys, m2 = case_from_monolayer(m, dict(g.WET_NEMATIC, zetaQ_inter=0.02), seed=42)
+    warm, steps = 6, 3
+    p, cells = build_inputs(keys, m2)
+    e = engine.Engine(p, m2.L, cells)
+    e.set_phase(1)
+    e.step(warm)
+    e.set_params(params)
+    e.set_solver(abi.RC_SOLVER_LEARNED)
+    st = e.step(steps)
+    print("learned solve at 128:", st.cg_iterations, st.refinements, st.cg_max_rel_residual)
+    assert st.cg_max_rel_residual < 1e-8
+    got = e.state()
+    p, cells = build_inputs(keys, m2)
+    o = orc.OracleSim(p, m2.L, cells)
+    o.set_phase(1)
+    o.step(warm + steps)
+    want = o.state()
+    for k in ("vx", "vy", "phi", "area", "com_x"):
+        assert rel_err(got[k], want[k]) < 1e-7, k
+    e.close()
