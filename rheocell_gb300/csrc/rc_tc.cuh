@@ -91,10 +91,6 @@ __device__ __forceinline__ void cp_async_wait_all() {
 	asm volatile("cp.async.commit_group;" ::: "memory");
 	asm volatile("cp.async.wait_group 0;" ::: "memory");
 }
-// Close the current group of copies (possibly empty).
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-// Wait until at most one group (the most recent) is still in flight.
-__device__ __forceinline__ void cp_async_wait_1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
 // Generic-proxy shared-memory writes made visible to the tensor cores.
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }

@@ -124,11 +124,10 @@ constexpr int UNET_PACKED = unet_pack_offset(UNET_LAYERS);
 // Gather mode (other sides, small levels only): each tap's operand is
 // gathered pixel by pixel for one tile of 128 pixels (K-major A), nine taps
 // times KC/2 MMAs of N = 16 into one accumulator.
-constexpr int TC_RT = 1;        // gather mode: tiles per round
 constexpr int TC_STRIP_T = 4;   // strip mode: at most 4 tiles (512 pixels) per strip
 constexpr int TC_COLS = 512;    // TMEM columns: T x R slots of 16
 constexpr int TC_HW_MAX = TC_STRIP_T * 128 + 2;
-constexpr size_t TC_A_GATHER = (size_t) TC_RT * 9 * 4 * 128 * 16;
+constexpr size_t TC_A_GATHER = (size_t) 9 * 4 * 128 * 16;  // gather mode: one tile's operands
 constexpr size_t TC_A_STRIP = (size_t) 3 * 4 * TC_HW_MAX * 16;  // three input-row buffers, up to 4 channel chunks
 constexpr size_t TC_A_BYTES = TC_A_GATHER > TC_A_STRIP ? TC_A_GATHER : TC_A_STRIP;
 constexpr size_t TC_B_OFF = TC_A_BYTES;
@@ -141,7 +140,6 @@ constexpr size_t TC_CTRL_OFF = TC_MBAR_OFF + 8 * TC_NMBAR;  // strip mode: rows 
 constexpr size_t TC_HOLD_OFF = TC_CTRL_OFF + 16;
 constexpr size_t TC_SMEM = TC_HOLD_OFF + 16;
 constexpr uint32_t TC_IDESC = tc_idesc_bf16(128, 16);
-constexpr uint32_t TC_IDESC32 = tc_idesc_bf16(128, 32);
 constexpr uint32_t TC_IDESC48 = tc_idesc_bf16(128, 48);
 constexpr long long TC_WAIT_LIMIT = 2000000;  // mbarrier polls (each a bounded hardware wait)
 
@@ -149,10 +147,10 @@ constexpr long long TC_WAIT_LIMIT = 2000000;  // mbarrier polls (each a bounded 
 // the TC_NMBAR mbarriers at TC_MBAR_OFF initialised with count 1), the TMEM
 // allocation (TC_COLS columns) and the parities the mbarriers wait for next.
 // err/err_bit: where a wait that ran out is recorded.  tns (diagnostics, may
-// be null): block 0 adds the time of weight and operand staging (tns[0]),
-// waits for staged rows and the block barrier (tns[1]), waits for MMA
-// completion (tns[2]) and the epilogue (tns[3]); in strip mode as seen by the
-// first staging/epilogue thread.
+// be null): block 0 adds times to tns[0..3] -- in gather mode weight
+// staging, operand staging, MMA completion waits and the epilogue; in strip
+// mode, as seen by the first write-out thread, weight staging, band set-up,
+// waits for MMA completion and the write-out work.
 struct TcCtx {
 	unsigned char *sm;
 	uint32_t tmem;
@@ -319,10 +317,6 @@ struct TcTimer {
 	}
 };
 
-// Warp that writes out tile r's lane quarter q (TMEM lanes 32 q .. 32 q + 31
-// are readable by warps w with w % 4 == q): warp q + 4 r, except that warp
-// 0 only issues MMAs, so quarter 0 of tiles 0 .. 3 goes to warps 4, 8, 12, 4.
-__device__ __forceinline__ int tc_epi_warp(int r, int q) { return q ? q + 4 * r : 4 + 4 * (r % 3); }
 
 // Strip mode (L a multiple of 128); requires 512 threads in three roles that
 // run decoupled: warp 0 issues the MMAs, warps 1 - 7 stage input rows into a
