@@ -807,7 +807,7 @@ int rc_batch_create(const rc_params *params, int n_layers, const rc_box *boxes, 
 			   (rc = dalloc(e, &e->Pxf, L2)) || (rc = dalloc(e, &e->Pyf, L2)))
 				return bail(rc);
 		}
-		e->cg_blocks = cg_grid_blocks(device, false);
+		e->cg_blocks = cg_grid_blocks(device, false, (long long) L * L);
 	}
 	if(cudaMallocHost(&e->st_host, sizeof(DevStatus)) != cudaSuccess) return bail(set_err(e, RC_ERR_OOM, "pinned alloc failed"));
 
@@ -1407,7 +1407,7 @@ int rc_set_solver(rc_engine *e, int solver) {
 			unet_pack_bf16(e->unet_params, e->unet_pack, e->stream);
 			CUDA_TRY(e, cudaStreamSynchronize(e->stream));
 		}
-		if(!e->cg_blocks_learned) e->cg_blocks_learned = cg_grid_blocks(e->device, true);
+		if(!e->cg_blocks_learned) e->cg_blocks_learned = cg_grid_blocks(e->device, true, (long long) e->L * e->L);
 	}
 	if(solver != e->solver) drop_graphs(e);
 	e->solver = solver;

@@ -123,7 +123,7 @@ void launch_bins(CellDev *cells, const LayerDev *layers, int N, int *bin_count, 
                  DevStatus *st, cudaStream_t s);
 void launch_repack(CellArgs a, double *scratch_phi, double *scratch_rep, long long cap, cudaStream_t s);
 void launch_box_gather(const BoxArgs &a, cudaStream_t s);
-int cg_grid_blocks(int device, bool learned);
+int cg_grid_blocks(int device, bool learned, long long box_sites);
 // diagnostic observables (rc_obs.cu)
 void launch_obs_field(const CellDev *cells, const LayerDev *layers, const LayerDev &lay_h, const int *bin_count,
                       const int *bin_cells, const double *phi, const double *vx, const double *vy, int kind, int layer,
