@@ -429,6 +429,10 @@ __device__ __forceinline__ const float *tab_iT<float>(const CGShared &sh) { retu
 // FP64 phase A by box site: thread k walks its cover list in order, updates
 // p there and stores P[k] (every site written, so P needs no clearing).  All
 // unknowns at k share D(k): one table lookup per site, one FP64 add per entry.
+// NB: unknowns of a site whose loads are issued together (their indices
+// first, then their values), summed in the same order; 1 in the two-CTA
+// build, more where one CTA per SM leaves the registers for it.
+template<int NB>
 __device__ __forceinline__ bool cg_phase_a_sites(const CGArgs &a, CGShared &sh, const CGVecs<double> &V) {
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
@@ -444,19 +448,36 @@ __device__ __forceinline__ bool cg_phase_a_sites(const CGArgs &a, CGShared &sh, 
 		double sx = 0.0, sy = 0.0;
 		if(e1 > e0) {
 			const double id = sh.iT[box_deg(cnt, (int) k, L)];
-			for(int e = e0; e < e1; e++) {
-				const int j = cov_idx[e];
-				if(ax) {
-					const double z = id * rx[j];
-					const double p = first ? z : __fma_rn(bx, px[j], z);
-					px[j] = p;
-					sx += p;
+			for(int e = e0; e < e1; e += NB) {
+				int js[NB];
+				double rxv[NB], ryv[NB], pxv[NB], pyv[NB];
+#pragma unroll
+				for(int u = 0; u < NB; u++) js[u] = e + u < e1 ? cov_idx[e + u] : -1;
+#pragma unroll
+				for(int u = 0; u < NB; u++) {
+					const int j = js[u];
+					const bool v = j >= 0;
+					rxv[u] = (v && ax) ? rx[j] : 0.0;
+					pxv[u] = (v && ax && !first) ? px[j] : 0.0;
+					ryv[u] = (v && ay) ? ry[j] : 0.0;
+					pyv[u] = (v && ay && !first) ? py[j] : 0.0;
 				}
-				if(ay) {
-					const double z = id * ry[j];
-					const double p = first ? z : __fma_rn(by, py[j], z);
-					py[j] = p;
-					sy += p;
+#pragma unroll
+				for(int u = 0; u < NB; u++) {
+					const int j = js[u];
+					if(j < 0) break;
+					if(ax) {
+						const double z = id * rxv[u];
+						const double p = first ? z : __fma_rn(bx, pxv[u], z);
+						px[j] = p;
+						sx += p;
+					}
+					if(ay) {
+						const double z = id * ryv[u];
+						const double p = first ? z : __fma_rn(by, pyv[u], z);
+						py[j] = p;
+						sy += p;
+					}
 				}
 			}
 		}
@@ -468,6 +489,7 @@ __device__ __forceinline__ bool cg_phase_a_sites(const CGArgs &a, CGShared &sh, 
 
 // FP64 phase B by box site: the four-neighbour sum of P and the diagonal once
 // per site, then Ap and p.Ap for its unknowns.
+template<int NB>
 __device__ __forceinline__ bool cg_phase_b_sites(const CGArgs &a, CGShared &sh, const CGVecs<double> &V) {
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
@@ -485,19 +507,33 @@ __device__ __forceinline__ bool cg_phase_b_sites(const CGArgs &a, CGShared &sh, 
 		const double d = sh.T[box_deg(cnt, (int) k, L)];
 		const double qx = ax ? neta * box_n4T<double>(Pbx, (int) k, L) : 0.0;
 		const double qy = ay ? neta * box_n4T<double>(Pby, (int) k, L) : 0.0;
-		for(int e = e0; e < e1; e++) {
-			const int j = cov_idx[e];
-			if(ax) {
-				const double p = px[j];
-				const double ap = __fma_rn(d, p, qx);
-				apx[j] = ap;
-				w0 = __fma_rn(p, ap, w0);
+		for(int e = e0; e < e1; e += NB) {
+			int js[NB];
+			double pxv[NB], pyv[NB];
+#pragma unroll
+			for(int u = 0; u < NB; u++) js[u] = e + u < e1 ? cov_idx[e + u] : -1;
+#pragma unroll
+			for(int u = 0; u < NB; u++) {
+				const int j = js[u];
+				pxv[u] = (j >= 0 && ax) ? px[j] : 0.0;
+				pyv[u] = (j >= 0 && ay) ? py[j] : 0.0;
 			}
-			if(ay) {
-				const double p = py[j];
-				const double ap = __fma_rn(d, p, qy);
-				apy[j] = ap;
-				w1 = __fma_rn(p, ap, w1);
+#pragma unroll
+			for(int u = 0; u < NB; u++) {
+				const int j = js[u];
+				if(j < 0) break;
+				if(ax) {
+					const double p = pxv[u];
+					const double ap = __fma_rn(d, p, qx);
+					apx[j] = ap;
+					w0 = __fma_rn(p, ap, w0);
+				}
+				if(ay) {
+					const double p = pyv[u];
+					const double ap = __fma_rn(d, p, qy);
+					apy[j] = ap;
+					w1 = __fma_rn(p, ap, w1);
+				}
 			}
 		}
 	}
@@ -508,9 +544,9 @@ __device__ __forceinline__ bool cg_phase_b_sites(const CGArgs &a, CGShared &sh, 
 	return grid_reduce(a, sh, 2, v);
 }
 
-template<typename T>
+template<typename T, int NB>
 __device__ __forceinline__ bool cg_phase_a(const CGArgs &a, CGShared &sh, const CGVecs<T> &V) {
-	if constexpr(sizeof(T) == sizeof(double)) return cg_phase_a_sites(a, sh, V);
+	if constexpr(sizeof(T) == sizeof(double)) return cg_phase_a_sites<NB>(a, sh, V);
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
 	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
@@ -555,9 +591,9 @@ __device__ __forceinline__ bool cg_phase_a(const CGArgs &a, CGShared &sh, const 
 }
 
 // Phase B: Ap (stored) and p.Ap into sh.tot[0..1].
-template<typename T>
+template<typename T, int NB>
 __device__ __forceinline__ bool cg_phase_b(const CGArgs &a, CGShared &sh, const CGVecs<T> &V) {
-	if constexpr(sizeof(T) == sizeof(double)) return cg_phase_b_sites(a, sh, V);
+	if constexpr(sizeof(T) == sizeof(double)) return cg_phase_b_sites<NB>(a, sh, V);
 	const int L = a.L;
 	const long long S = a.st->S;
 	const T neta = (T) (-a.eta * 1.0);
@@ -644,7 +680,7 @@ __device__ __forceinline__ bool cg_phase_c(const CGArgs &a, CGShared &sh, const 
 // summed into FP64 for the block and grid reductions, and the scalars alpha,
 // beta are FP64.  Updates use fused multiply-adds (the solve is not bitwise
 // Eigen's in any case: its reductions run in a different order).
-template<typename T>
+template<typename T, int NB = 1>
 __device__ __forceinline__ bool cg_iterate(const CGArgs &a, CGShared &sh, const CGVecs<T> &V, long long max_it) {
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
@@ -672,8 +708,8 @@ __device__ __forceinline__ bool cg_iterate(const CGArgs &a, CGShared &sh, const 
 		}
 		sweep++;
 		const int ax = sh.act[0], ay = sh.act[1];
-		if(!cg_phase_a<T>(a, sh, V)) return false;
-		if(!cg_phase_b<T>(a, sh, V)) return false;
+		if(!cg_phase_a<T, NB>(a, sh, V)) return false;
+		if(!cg_phase_b<T, NB>(a, sh, V)) return false;
 		if(threadIdx.x == 0) {
 			if(ax) sh.alpha[0] = sh.rz[0] / sh.tot[0];
 			if(ay) sh.alpha[1] = sh.rz[1] / sh.tot[1];
@@ -1289,7 +1325,7 @@ __device__ __noinline__ bool fcg_iterate(const CGArgs &a, CGShared &sh, TcCtx &t
 	return true;
 }
 
-template<bool LEARNED>
+template<bool LEARNED, int NB>
 __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcCtx &tc) {
 	const long long S = a.st->S;
 	const int cold = a.st->cg_cold;
@@ -1341,7 +1377,7 @@ __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcCtx &tc
 	const long long max_it = 2 * S;
 	int refinements = 0;
 	if(!mixed) {
-		if(!cg_iterate<double>(a, sh, CGVecs<double>{a.rx, a.ry, a.px, a.py, a.apx, a.apy, a.Px, a.Py, a.vx, a.vy}, max_it)) return;
+		if(!cg_iterate<double, NB>(a, sh, CGVecs<double>{a.rx, a.ry, a.px, a.py, a.apx, a.apy, a.Px, a.Py, a.vx, a.vy}, max_it)) return;
 		if(a.harv_in && sh.hm > 0 && !harvest_finish(a, sh, a.vx, a.vy)) return;
 	}
 	else {
@@ -1421,8 +1457,11 @@ constexpr size_t LEARNED_SMEM = TC_SMEM > sizeof(float) * UNET_MAX_LAYER_PARAMS 
 
 // The plain solve keeps two CTAs per SM (64 registers); the learned one
 // needs the whole register file of one CTA.
-template<bool LEARNED>
-__global__ void __launch_bounds__(CG_THREADS, LEARNED ? 1 : 2) cg_kernel(const __grid_constant__ CGArgs a) {
+// MINB: CTAs per SM the kernel is built for.  The plain solve has a two-CTA
+// build (64 registers) and, for the small boxes that run one CTA per SM, a
+// one-CTA build whose spare registers hold batched loads (NB 4).
+template<bool LEARNED, int MINB = (LEARNED ? 1 : 2)>
+__global__ void __launch_bounds__(CG_THREADS, MINB) cg_kernel(const __grid_constant__ CGArgs a) {
 	__shared__ CGShared sh;
 	extern __shared__ __align__(1024) unsigned char dsm[];
 	TcCtx tc{dsm, 0u, {0u, 0u}, &a.st->err, ERR_MMA, a.phase_ns ? a.phase_ns + PH_COUNT : nullptr};
@@ -1444,7 +1483,7 @@ __global__ void __launch_bounds__(CG_THREADS, LEARNED ? 1 : 2) cg_kernel(const _
 			tc.tmem = *hold;
 		}
 	}
-	cg_body<LEARNED>(a, sh, tc);
+	cg_body<LEARNED, (!LEARNED && MINB == 1) ? 4 : 1>(a, sh, tc);
 	pmark(a, sh, PH_OTHER);
 	if constexpr(LEARNED) {
 		if(a.unet_tc) {
@@ -1493,7 +1532,14 @@ cudaError_t launch_cg(const CGArgs &a, int blocks, cudaStream_t s) {
 	cfg.attrs = attr;
 	cfg.numAttrs = 1;
 	if(learned) return cudaLaunchKernelEx(&cfg, cg_kernel<true>, a);
-	return cudaLaunchKernelEx(&cfg, cg_kernel<false>, a);
+	static int sms = 0;
+	if(!sms) {
+		int dev = 0;
+		cudaGetDevice(&dev);
+		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+	}
+	if(blocks <= sms) return cudaLaunchKernelEx(&cfg, cg_kernel<false, 1>, a);
+	return cudaLaunchKernelEx(&cfg, cg_kernel<false, 2>, a);
 }
 
 }  // namespace rc
