@@ -1458,8 +1458,9 @@ constexpr size_t LEARNED_SMEM = TC_SMEM > sizeof(float) * UNET_MAX_LAYER_PARAMS 
 // The plain solve keeps two CTAs per SM (64 registers); the learned one
 // needs the whole register file of one CTA.
 // MINB: CTAs per SM the kernel is built for.  The plain solve has a two-CTA
-// build (64 registers) and, for the small boxes that run one CTA per SM, a
-// one-CTA build whose spare registers hold batched loads (NB 4).
+// build (64 registers; box-site phases batch the loads of two unknowns) and,
+// for the small boxes that run one CTA per SM, a one-CTA build whose spare
+// registers hold the loads of four.
 template<bool LEARNED, int MINB = (LEARNED ? 1 : 2)>
 __global__ void __launch_bounds__(CG_THREADS, MINB) cg_kernel(const __grid_constant__ CGArgs a) {
 	__shared__ CGShared sh;
@@ -1483,7 +1484,7 @@ __global__ void __launch_bounds__(CG_THREADS, MINB) cg_kernel(const __grid_const
 			tc.tmem = *hold;
 		}
 	}
-	cg_body<LEARNED, (!LEARNED && MINB == 1) ? 4 : 1>(a, sh, tc);
+	cg_body<LEARNED, LEARNED ? 1 : (MINB == 1 ? 4 : 2)>(a, sh, tc);
 	pmark(a, sh, PH_OTHER);
 	if constexpr(LEARNED) {
 		if(a.unet_tc) {
