@@ -330,7 +330,7 @@ __device__ __forceinline__ bool true_residual(const CGArgs &a, CGShared &sh, boo
 				}
 			}
 		}
-		if(fmode == RES_FLOAT_COVER) {
+		if(fmode == RES_FLOAT_COVER && a.unet_params) {
 			const float wv = box_w(a, sh, (int) k, L);
 			a.unet.x0[k * 2] = Rx;
 			a.unet.x0[k * 2 + 1] = wv;
@@ -1004,6 +1004,7 @@ __device__ __noinline__ bool fcg_phase_e(const CGArgs &a, CGShared &sh, bool fir
 	const long long nwarps = ((long long) gridDim.x * blockDim.x) >> 5;
 	const int ax = sh.act[0], ay = sh.act[1];
 	const float es0 = (float) (a.eta * sh.scale[0]), es1 = (float) (a.eta * sh.scale[1]);
+	const bool net = a.unet_params != nullptr;  // without a network: z = r / T (Jacobi)
 	const float *V = a.unet.out;
 	const float *rx = a.rxf, *ry = a.ryf, *apx = a.apxf, *apy = a.apyf;
 	float *zx = a.zxf, *zy = a.zyf;
@@ -1018,8 +1019,8 @@ __device__ __noinline__ bool fcg_phase_e(const CGArgs &a, CGShared &sh, bool fir
 		float id = 0.f, nvx = 0.f, nvy = 0.f;
 		if(e1 > e0) {
 			id = sh.iTf[box_deg(a.cnt, (int) k, L)];
-			if(ax) nvx = es0 * box_n4T<float>(V, (int) k, L);
-			if(ay) nvy = es1 * box_n4T<float>(V + L2, (int) k, L);
+			if(net && ax) nvx = es0 * box_n4T<float>(V, (int) k, L);
+			if(net && ay) nvy = es1 * box_n4T<float>(V + L2, (int) k, L);
 		}
 		accx[threadIdx.x] = 0.f;
 		accy[threadIdx.x] = 0.f;
@@ -1190,6 +1191,7 @@ __device__ __noinline__ bool fcg_phase_c(const CGArgs &a, CGShared &sh, float *w
 	const float alx = (float) sh.alpha[0], aly = (float) sh.alpha[1];
 	const float *px = a.pxf, *py = a.pyf, *apx = a.apxf, *apy = a.apyf;
 	float *ex = a.exf, *ey = a.eyf, *rx = a.rxf, *ry = a.ryf, *x0 = a.unet.x0;
+	const bool net = a.unet_params != nullptr;
 	const int *cov_off = a.cov_off;
 	const int Etot = __ldcg(&cov_off[L2]);
 	float *accx = wacc, *accy = wacc + blockDim.x;
@@ -1236,8 +1238,10 @@ __device__ __noinline__ bool fcg_phase_c(const CGArgs &a, CGShared &sh, float *w
 						w[0] = __fmaf_rn(r, r, w[0]);
 						rv = r * ids;
 					}
-					const float t = seg_scan(rv, sg);
-					if(sg.tail) accx[slot] += t;
+					if(net) {
+						const float t = seg_scan(rv, sg);
+						if(sg.tail) accx[slot] += t;
+					}
 				}
 				if(ay) {
 					float rv = 0.f;
@@ -1248,13 +1252,15 @@ __device__ __noinline__ bool fcg_phase_c(const CGArgs &a, CGShared &sh, float *w
 						w[1] = __fmaf_rn(r, r, w[1]);
 						rv = r * ids;
 					}
-					const float t = seg_scan(rv, sg);
-					if(sg.tail) accy[slot] += t;
+					if(net) {
+						const float t = seg_scan(rv, sg);
+						if(sg.tail) accy[slot] += t;
+					}
 				}
 				__syncwarp();
 			}
 		}
-		if(kv) {
+		if(kv && net) {
 			if(ax) x0[k * 2] = accx[threadIdx.x];
 			if(ay) x0[(L2 + k) * 2] = accy[threadIdx.x];
 		}
@@ -1284,7 +1290,7 @@ __device__ __noinline__ bool fcg_iterate(const CGArgs &a, CGShared &sh, TcCtx &t
 	bool first = true;
 	int par = 0;
 	while(sh.act[0] || sh.act[1]) {
-		if(!precond_network(a, sh, tc)) return false;
+		if(a.unet_params && !precond_network(a, sh, tc)) return false;
 		if(!fcg_phase_e(a, sh, first, reinterpret_cast<float *>(tc.sm))) return false;
 		pmark(a, sh, PH_Z);
 		if(threadIdx.x == 0) {
@@ -1524,7 +1530,7 @@ cudaError_t launch_cg(const CGArgs &a, int blocks, cudaStream_t s) {
 	cudaLaunchConfig_t cfg = {};
 	cfg.gridDim = dim3(blocks);
 	cfg.blockDim = dim3(CG_THREADS);
-	const bool learned = a.unet_params != nullptr && a.mixed;
+	const bool learned = a.fcg != 0;
 	cfg.dynamicSmemBytes = learned ? LEARNED_SMEM : 0;
 	cfg.stream = s;
 	cudaLaunchAttribute attr[1];

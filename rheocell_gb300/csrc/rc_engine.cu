@@ -332,8 +332,20 @@ static void solve(rc_engine *e, int phase) {
 	g.exf = e->exf;
 	g.eyf = e->eyf;
 	int blocks = e->cg_blocks;
+	if(g.mixed && e->solver == RC_SOLVER_PLAIN) {
+		// mixed precision: Jacobi-preconditioned flexible CG in cover order
+		g.fcg = 1;
+		g.zxf = e->zxf;
+		g.zyf = e->zyf;
+		g.Zxf = e->Zxf;
+		g.Zyf = e->Zyf;
+		g.Pxf2 = e->Pxf2;
+		g.Pyf2 = e->Pyf2;
+		blocks = e->cg_blocks_learned;
+	}
 	if(e->solver == RC_SOLVER_LEARNED || e->solver == RC_SOLVER_LEARNED_FP32) {
 		g.mixed = 1;
+		g.fcg = 1;
 		g.unet_params = e->unet_params;
 		g.unet = e->unet;
 		g.unet_tc = e->solver == RC_SOLVER_LEARNED;
@@ -801,11 +813,15 @@ int rc_batch_create(const rc_params *params, int n_layers, const rc_box *boxes, 
 		   (rc = dalloc(e, &e->partials, 8 * 4096)) || (rc = dalloc(e, &e->scalars, 64)) || (rc = dalloc(e, &e->bar, 4)))
 			return bail(rc);
 		if(params->precision == RC_PRECISION_MIXED) {
+			// FP32 inner iterations: the flexible CG in cover order, Jacobi-preconditioned
 			if((rc = dalloc(e, &e->rxf, cap)) || (rc = dalloc(e, &e->ryf, cap)) || (rc = dalloc(e, &e->pxf, cap)) ||
 			   (rc = dalloc(e, &e->pyf, cap)) || (rc = dalloc(e, &e->exf, cap)) || (rc = dalloc(e, &e->eyf, cap)) ||
 			   (rc = dalloc(e, &e->apxf, cap)) || (rc = dalloc(e, &e->apyf, cap)) ||
-			   (rc = dalloc(e, &e->Pxf, L2)) || (rc = dalloc(e, &e->Pyf, L2)))
+			   (rc = dalloc(e, &e->Pxf, L2)) || (rc = dalloc(e, &e->Pyf, L2)) || (rc = dalloc(e, &e->zxf, cap)) ||
+			   (rc = dalloc(e, &e->zyf, cap)) || (rc = dalloc(e, &e->Zxf, L2)) || (rc = dalloc(e, &e->Zyf, L2)) ||
+			   (rc = dalloc(e, &e->Pxf2, L2)) || (rc = dalloc(e, &e->Pyf2, L2)))
 				return bail(rc);
+			e->cg_blocks_learned = cg_grid_blocks(device, true, (long long) L * L);
 		}
 		e->cg_blocks = cg_grid_blocks(device, false, (long long) L * L);
 	}
@@ -1385,11 +1401,14 @@ int rc_set_solver(rc_engine *e, int solver) {
 				return rc;
 		}
 		if(!e->zxf) {
+			if((rc = dalloc(e, &e->zxf, cap)) || (rc = dalloc(e, &e->zyf, cap)) || (rc = dalloc(e, &e->Zxf, L2)) ||
+			   (rc = dalloc(e, &e->Zyf, L2)) || (rc = dalloc(e, &e->Pxf2, L2)) || (rc = dalloc(e, &e->Pyf2, L2)))
+				return rc;
+		}
+		if(!e->unet.x0) {
 			const size_t p0 = 2 * L2, p1 = p0 / 4, p2 = p0 / 16;
 			UNetActs &A = e->unet;
-			if((rc = dalloc(e, &e->zxf, cap)) || (rc = dalloc(e, &e->zyf, cap)) || (rc = dalloc(e, &e->Zxf, L2)) ||
-			   (rc = dalloc(e, &e->Zyf, L2)) || (rc = dalloc(e, &e->Pxf2, L2)) || (rc = dalloc(e, &e->Pyf2, L2)) ||
-			   (rc = dalloc(e, &A.x0, p0 * 2)) ||
+			if((rc = dalloc(e, &A.x0, p0 * 2)) ||
 			   (rc = dalloc(e, &A.e0a, p0 * 16)) || (rc = dalloc(e, &A.s0, p0 * 16)) || (rc = dalloc(e, &A.d0a, p0 * 16)) ||
 			   (rc = dalloc(e, &A.t0, p0 * 16)) || (rc = dalloc(e, &A.out, p0)) || (rc = dalloc(e, &A.e1a, p1 * 16)) ||
 			   (rc = dalloc(e, &A.s1, p1 * 16)) || (rc = dalloc(e, &A.d1a, p1 * 16)) || (rc = dalloc(e, &A.t1, p1 * 16)) ||

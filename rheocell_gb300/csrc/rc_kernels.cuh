@@ -87,6 +87,7 @@ struct CGArgs {
 	int restart_every;
 	double xi, eta, tol;
 	int mixed;               // FP32 inner iterations inside FP64 refinement
+	int fcg;                 // the inner iterations are the flexible CG in cover order (network or Jacobi)
 	double inner_tol;        // mixed: relative residual reduction per refinement sweep
 	float *rxf, *ryf, *pxf, *pyf, *apxf, *apyf, *Pxf, *Pyf;
 	float *exf, *eyf;        // mixed: correction of one refinement sweep
