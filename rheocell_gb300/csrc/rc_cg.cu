@@ -223,15 +223,14 @@ __device__ __forceinline__ float box_w(const CGArgs &a, const CGShared &sh, int 
 }
 
 // FP32 copies of the residual made by true_residual.
-enum { RES_FP64 = 0, RES_FLOAT_UNKNOWN = 1, RES_FLOAT_COVER = 2 };
+enum { RES_FP64 = 0, RES_FLOAT_COVER = 1 };
 
 // r = b - A x for both components (x = 0 when `x_zero`), written in FP64,
 // by box site: thread k forms the box sums of x at k (first pass), then the
 // four-neighbour sum and the diagonal once for the unknowns covering k.
-// fmode RES_FLOAT_UNKNOWN also rounds r to FP32 by unknown (rxf[j]) and
-// clears the correction exf[j] (Jacobi inner iterations);
-// RES_FLOAT_COVER stores them in cover order (rxf[e], exf[e] for
-// cov_idx[e] = j; the flexible CG's layout) and writes the network input of
+// fmode RES_FLOAT_COVER also rounds r to FP32 and clears the correction,
+// both in cover order (rxf[e], exf[e] for cov_idx[e] = j; the flexible CG's
+// layout), and writes the network input of
 // its first application: x0 = (sum over the unknowns at k of r / T, W(k))
 // per component, unscaled.  Reduces |b|^2, |r|^2 and r.M^-1 r (the latter
 // on the stored precision of r) into sh.tot[0..5], each thread's partial
@@ -241,8 +240,8 @@ enum { RES_FP64 = 0, RES_FLOAT_UNKNOWN = 1, RES_FLOAT_COVER = 2 };
 // GB300 issues FP64 at a small fraction of the FP32 rate, so the residual
 // does no FP64 work it does not need.
 // add_e: first x += e, the FP32 correction of the last refinement sweep
-// (exf/eyf, in cover order for RES_FLOAT_COVER, by unknown otherwise), fused
-// into the pass that forms the box sums of x.
+// (exf/eyf, in cover order; RES_FLOAT_COVER only), fused into the pass that
+// forms the box sums of x.
 template<int fmode>
 __device__ __forceinline__ bool true_residual(const CGArgs &a, CGShared &sh, bool x_zero, bool want_b = true, bool want_rz = true,
                                               bool add_e = false) {
@@ -260,10 +259,9 @@ __device__ __forceinline__ bool true_residual(const CGArgs &a, CGShared &sh, boo
 			for(int e = e0; e < e1; e++) {
 				const int j = cov_idx[e];
 				double ux = a.vx[j], uy = a.vy[j];
-				if(add_e) {
-					const int o = fmode == RES_FLOAT_COVER ? e : j;
-					ux += (double) a.exf[o];
-					uy += (double) a.eyf[o];
+				if(fmode == RES_FLOAT_COVER && add_e) {
+					ux += (double) a.exf[e];
+					uy += (double) a.eyf[e];
 					a.vx[j] = ux;
 					a.vy[j] = uy;
 				}
@@ -312,11 +310,10 @@ __device__ __forceinline__ bool true_residual(const CGArgs &a, CGShared &sh, boo
 				v[3] = __fma_rn(ry, ry, v[3]);
 				if(fmode != RES_FP64) {
 					const float fx = (float) rx, fy = (float) ry;
-					const int o = fmode == RES_FLOAT_COVER ? e : j;
-					a.rxf[o] = fx;
-					a.ryf[o] = fy;
-					a.exf[o] = 0.0f;
-					a.eyf[o] = 0.0f;
+					a.rxf[e] = fx;
+					a.ryf[e] = fy;
+					a.exf[e] = 0.0f;
+					a.eyf[e] = 0.0f;
 					if(want_rz) {
 						v[4] += (double) fx * (iT * (double) fx);
 						v[5] += (double) fy * (iT * (double) fy);
@@ -342,11 +339,6 @@ __device__ __forceinline__ bool true_residual(const CGArgs &a, CGShared &sh, boo
 	return grid_reduce(a, sh, 6, v);
 }
 
-// Jacobi-preconditioned CG iterations from the state in sh (act, rz, thr) and
-// the residual in (rx, ry): Eigen's loop.  T is the storage type of r, p, Ap
-// and the box sums, U that of the solution accumulator; dot products are
-// FP64.  Updates use fused multiply-adds (the solve is not bitwise Eigen's in
-// any case: its reductions run in a different order).
 // Shuffle tree within each warp in the vectors' own precision (lane 0 ends
 // with the warp's sum).
 template<typename T, int NV>
@@ -391,8 +383,6 @@ template<typename T>
 __device__ __forceinline__ T fmaT(T a, T b, T c);
 template<>
 __device__ __forceinline__ double fmaT<double>(double a, double b, double c) { return __fma_rn(a, b, c); }
-template<>
-__device__ __forceinline__ float fmaT<float>(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 
 template<typename T>
 __device__ __forceinline__ T box_n4T(const T *P, int k, int L) {
@@ -419,10 +409,6 @@ template<>
 __device__ __forceinline__ const double *tab_T<double>(const CGShared &sh) { return sh.T; }
 template<>
 __device__ __forceinline__ const double *tab_iT<double>(const CGShared &sh) { return sh.iT; }
-template<>
-__device__ __forceinline__ const float *tab_T<float>(const CGShared &sh) { return sh.Tf; }
-template<>
-__device__ __forceinline__ const float *tab_iT<float>(const CGShared &sh) { return sh.iTf; }
 
 // Phase A: p = z + beta p (p = z on the first sweep, z = r / diag), box sums
 // P = S p, one thread per cover entry; P is zero on entry (cleared in phase C).
@@ -544,89 +530,6 @@ __device__ __forceinline__ bool cg_phase_b_sites(const CGArgs &a, CGShared &sh, 
 	return grid_reduce(a, sh, 2, v);
 }
 
-template<typename T, int NB>
-__device__ __forceinline__ bool cg_phase_a(const CGArgs &a, CGShared &sh, const CGVecs<T> &V) {
-	if constexpr(sizeof(T) == sizeof(double)) return cg_phase_a_sites<NB>(a, sh, V);
-	const int L = a.L;
-	const long long L2 = (long long) L * L;
-	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-	const long long gstride = (long long) gridDim.x * blockDim.x;
-	const int ax = sh.act[0], ay = sh.act[1], first = sh.first;
-	const T bx = (T) sh.beta[0], by = (T) sh.beta[1];
-	const T *iTT = tab_iT<T>(sh);
-	const T *rx = V.rx, *ry = V.ry;
-	T *px = V.px, *py = V.py, *Pbx = V.Pbx, *Pby = V.Pby;
-	const int *cov_idx = a.cov_idx, *mapg = a.mapg, *cnt = a.cnt;
-	const long long E = __ldcg(&a.cov_off[L2]);
-	const long long gwarp = gtid >> 5, nwarps = gstride >> 5;
-	const int lane = threadIdx.x & 31;
-	for(long long base = gwarp * 32; base < E; base += nwarps * 32) {
-		const long long t = base + lane;
-		const bool valid = t < E;
-		const int j = valid ? cov_idx[t] : 0;
-		const int key = valid ? mapg[j] : -1;
-		const T id = valid ? iTT[box_deg(cnt, key, L)] : (T) 0;
-		T vx = (T) 0, vy = (T) 0;
-		if(valid && ax) {
-			const T z = id * rx[j];
-			const T p = first ? z : fmaT<T>(bx, px[j], z);
-			px[j] = p;
-			vx = p;
-		}
-		if(valid && ay) {
-			const T z = id * ry[j];
-			const T p = first ? z : fmaT<T>(by, py[j], z);
-			py[j] = p;
-			vy = p;
-		}
-		bool tail = false, tail2 = false;
-		if(ax) vx = seg_sum<T>(vx, key, tail);
-		if(ay) vy = seg_sum<T>(vy, key, tail2);
-		if(valid) {
-			if(ax && tail) atomicAdd(&Pbx[key], vx);
-			if(ay && tail2) atomicAdd(&Pby[key], vy);
-		}
-	}
-	return grid_reduce(a, sh, 0, nullptr);
-}
-
-// Phase B: Ap (stored) and p.Ap into sh.tot[0..1].
-template<typename T, int NB>
-__device__ __forceinline__ bool cg_phase_b(const CGArgs &a, CGShared &sh, const CGVecs<T> &V) {
-	if constexpr(sizeof(T) == sizeof(double)) return cg_phase_b_sites<NB>(a, sh, V);
-	const int L = a.L;
-	const long long S = a.st->S;
-	const T neta = (T) (-a.eta * 1.0);
-	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-	const long long gstride = (long long) gridDim.x * blockDim.x;
-	const int ax = sh.act[0], ay = sh.act[1];
-	const T *dT = tab_T<T>(sh);
-	const T *px = V.px, *py = V.py, *Pbx = V.Pbx, *Pby = V.Pby;
-	T *apx = V.apx, *apy = V.apy;
-	const int *mapg = a.mapg, *cnt = a.cnt;
-	T w[2] = {(T) 0, (T) 0};
-	for(long long j = gtid; j < S; j += gstride) {
-		const int k = mapg[j];
-		const T d = dT[box_deg(cnt, k, L)];
-		if(ax) {
-			const T p = px[j];
-			const T ap = fmaT<T>(d, p, neta * box_n4T<T>(Pbx, k, L));
-			apx[j] = ap;
-			w[0] = fmaT<T>(p, ap, w[0]);
-		}
-		if(ay) {
-			const T p = py[j];
-			const T ap = fmaT<T>(d, p, neta * box_n4T<T>(Pby, k, L));
-			apy[j] = ap;
-			w[1] = fmaT<T>(p, ap, w[1]);
-		}
-	}
-	warp_tree<T, 2>(w);
-	double v[2] = {(double) w[0], (double) w[1]};
-	block_sum_warps<2>(v, sh.red);
-	return grid_reduce(a, sh, 2, v);
-}
-
 // Phase C: u += alpha p; r -= alpha Ap; |r|^2 and r.z into sh.tot[0..3];
 // the box sums are cleared for the next phase A.
 template<typename T>
@@ -640,7 +543,7 @@ __device__ __forceinline__ bool cg_phase_c(const CGArgs &a, CGShared &sh, const 
 	const T alx = (T) sh.alpha[0], aly = (T) sh.alpha[1];
 	const T *iTT = tab_iT<T>(sh);
 	const T *px = V.px, *py = V.py, *apx = V.apx, *apy = V.apy;
-	T *rx = V.rx, *ry = V.ry, *ux = V.ux, *uy = V.uy, *Pbx = V.Pbx, *Pby = V.Pby;
+	T *rx = V.rx, *ry = V.ry, *ux = V.ux, *uy = V.uy;
 	const int *mapg = a.mapg, *cnt = a.cnt;
 	T w[4] = {(T) 0, (T) 0, (T) 0, (T) 0};
 	for(long long j = gtid; j < S; j += gstride) {
@@ -662,23 +565,14 @@ __device__ __forceinline__ bool cg_phase_c(const CGArgs &a, CGShared &sh, const 
 		}
 	}
 	double v[4] = {(double) w[0], (double) w[1], (double) w[2], (double) w[3]};
-	if constexpr(sizeof(T) != sizeof(double)) {
-		// the FP32 phase A accumulates into P with atomics: clear it
-		for(long long k = gtid; k < L2; k += gstride) {
-			Pbx[k] = (T) 0;
-			Pby[k] = (T) 0;
-		}
-	}
 	block_sum<4>(v, sh.red);
 	return grid_reduce(a, sh, 4, v);
 }
 
 // Jacobi-preconditioned CG iterations from the state in sh (act, rz, thr) and
-// the residual in V.rx, V.ry: Eigen's loop.  Vectors, box sums and the
-// element-wise arithmetic are in T (FP64 for the plain solve, FP32 for the
-// inner solves of the mixed path); every thread's partial dot product is
-// summed into FP64 for the block and grid reductions, and the scalars alpha,
-// beta are FP64.  Updates use fused multiply-adds (the solve is not bitwise
+// the residual in V.rx, V.ry: Eigen's loop, in FP64 (the plain solve and
+// the FP64 fallback of the mixed-precision refinement); every thread's
+// partial dot product is summed for the block and grid reductions.  Updates use fused multiply-adds (the solve is not bitwise
 // Eigen's in any case: its reductions run in a different order).
 template<typename T, int NB = 1>
 __device__ __forceinline__ bool cg_iterate(const CGArgs &a, CGShared &sh, const CGVecs<T> &V, long long max_it) {
@@ -686,10 +580,6 @@ __device__ __forceinline__ bool cg_iterate(const CGArgs &a, CGShared &sh, const 
 	const long long L2 = (long long) L * L;
 	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
 	const long long gstride = (long long) gridDim.x * blockDim.x;
-	for(int d = threadIdx.x; d <= CG_MAX_D; d += blockDim.x) {
-		sh.Tf[d] = (float) sh.T[d];
-		sh.iTf[d] = (float) sh.iT[d];
-	}
 	if(threadIdx.x == 0) sh.first = 1;
 	for(long long k = gtid; k < L2; k += gstride) {
 		V.Pbx[k] = (T) 0;
@@ -708,8 +598,8 @@ __device__ __forceinline__ bool cg_iterate(const CGArgs &a, CGShared &sh, const 
 		}
 		sweep++;
 		const int ax = sh.act[0], ay = sh.act[1];
-		if(!cg_phase_a<T, NB>(a, sh, V)) return false;
-		if(!cg_phase_b<T, NB>(a, sh, V)) return false;
+		if(!cg_phase_a_sites<NB>(a, sh, V)) return false;
+		if(!cg_phase_b_sites<NB>(a, sh, V)) return false;
 		if(threadIdx.x == 0) {
 			if(ax) sh.alpha[0] = sh.rz[0] / sh.tot[0];
 			if(ay) sh.alpha[1] = sh.rz[1] / sh.tot[1];
@@ -1353,10 +1243,15 @@ __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcCtx &tc
 			a.vy[j] = 0.0;
 		}
 	}
-	const bool mixed = a.mixed != 0;
 	if(!build_csr(a, sh)) return;
-	constexpr int fmode = LEARNED ? RES_FLOAT_COVER : RES_FLOAT_UNKNOWN;
-	if(!(mixed ? true_residual<fmode>(a, sh, cold != 0, true, !LEARNED) : true_residual<RES_FP64>(a, sh, cold != 0))) return;
+	// the flexible-CG kernel runs every mixed-precision solve (with or
+	// without a network); the plain kernel only FP64 ones
+	if constexpr(LEARNED) {
+		if(!true_residual<RES_FLOAT_COVER>(a, sh, cold != 0, true, false)) return;
+	}
+	else {
+		if(!true_residual<RES_FP64>(a, sh, cold != 0)) return;
+	}
 	pmark(a, sh, PH_START);
 	if(threadIdx.x == 0) {
 		for(int c = 0; c < 2; c++) {
@@ -1382,14 +1277,15 @@ __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcCtx &tc
 	}
 	const long long max_it = 2 * S;
 	int refinements = 0;
-	if(!mixed) {
+	if constexpr(!LEARNED) {
 		if(!cg_iterate<double, NB>(a, sh, CGVecs<double>{a.rx, a.ry, a.px, a.py, a.apx, a.apy, a.Px, a.Py, a.vx, a.vy}, max_it)) return;
 		if(a.harv_in && sh.hm > 0 && !harvest_finish(a, sh, a.vx, a.vy)) return;
 	}
 	else {
-		// Iterative refinement: FP32 Jacobi-PCG for the correction A e = r,
-		// stopped at inner_tol * |r|, then x += e and r = b - A x in FP64.
-		// A sweep that fails to reduce |r| by 2x hands over to FP64 CG.
+		// Iterative refinement: FP32 flexible CG (network or Jacobi
+		// preconditioner) for the correction A e = r, stopped at
+		// inner_tol * |r|, then x += e and r = b - A x in FP64.  A sweep that
+		// fails to reduce |r| by 2x hands over to FP64 CG.
 		__shared__ double s_goal[2], s_prev[2];
 		__shared__ int s_fallback;
 		if(threadIdx.x == 0) {
@@ -1405,16 +1301,10 @@ __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcCtx &tc
 				}
 			}
 			__syncthreads();
-			if constexpr(LEARNED) {
-				if(!fcg_iterate(a, sh, tc, max_it < 1000 ? max_it : 1000)) return;
-			}
-			else {
-				if(!cg_iterate<float>(a, sh, CGVecs<float>{a.rxf, a.ryf, a.pxf, a.pyf, a.apxf, a.apyf, a.Pxf, a.Pyf, a.exf, a.eyf}, max_it))
-					return;
-			}
+			if(!fcg_iterate(a, sh, tc, max_it < 1000 ? max_it : 1000)) return;
 			refinements++;
 			// x += e and r = b - A x
-			if(!true_residual<fmode>(a, sh, false, false, !LEARNED, true)) return;
+			if(!true_residual<RES_FLOAT_COVER>(a, sh, false, false, false, true)) return;
 			if(threadIdx.x == 0) {
 				for(int c = 0; c < 2; c++) {
 					sh.rn2[c] = sh.tot[2 + c];
