@@ -379,10 +379,6 @@ __device__ inline void block_sum_warps(double (&v)[NV], double *scratch) {
 __device__ __forceinline__ bool harvest_point(const CGArgs &a, CGShared &sh, const double *ux, const double *uy, const double *rx,
                               const double *ry, int m);
 
-template<typename T>
-__device__ __forceinline__ T fmaT(T a, T b, T c);
-template<>
-__device__ __forceinline__ double fmaT<double>(double a, double b, double c) { return __fma_rn(a, b, c); }
 
 template<typename T>
 __device__ __forceinline__ T box_n4T(const T *P, int k, int L) {
@@ -394,32 +390,30 @@ __device__ __forceinline__ T box_n4T(const T *P, int k, int L) {
 	return P[kd] + P[kl] + P[kr] + P[ku];
 }
 
-// Vectors of one CG run: residual, direction, A p, box sums of p, solution.
-template<typename T>
+// Vectors of one FP64 CG run: residual r, scaled direction q = T p, A p, box
+// sums P of p, solution x.
 struct CGVecs {
-	T *rx, *ry, *px, *py, *apx, *apy, *Pbx, *Pby, *ux, *uy;
+	double *rx, *ry, *qx, *qy, *apx, *apy, *Pbx, *Pby, *ux, *uy;
 };
 
-// T and 1/T tables in the precision of the iteration
-template<typename T>
-__device__ __forceinline__ const T *tab_T(const CGShared &sh);
-template<typename T>
-__device__ __forceinline__ const T *tab_iT(const CGShared &sh);
-template<>
-__device__ __forceinline__ const double *tab_T<double>(const CGShared &sh) { return sh.T; }
-template<>
-__device__ __forceinline__ const double *tab_iT<double>(const CGShared &sh) { return sh.iT; }
+// The Jacobi preconditioner is constant on a box site (every unknown at k has
+// the diagonal T(k)), so the plain solve carries q = T p in place of Eigen's
+// direction p.  Eigen's p = z + beta p with z = r / T becomes q = r + beta q,
+// and every other 1/T factor is taken once per site instead of once per
+// unknown: P(k) = (1/T) sum q, Ap = q - eta N4(P), p.Ap = sum_k (1/T) sum q Ap,
+// x += (alpha / T) q, r.z = sum_k (1/T) sum r^2.  GB300 issues FP64 at a small
+// fraction of its FP32 rate and the solve is bound by that issue: this cuts
+// the FP64 operations per unknown and iteration from ten to seven.  The
+// iterates are Eigen's up to rounding (the solve is not bitwise Eigen's in any
+// case: its reductions run in a different order).
 
-// Phase A: p = z + beta p (p = z on the first sweep, z = r / diag), box sums
-// P = S p, one thread per cover entry; P is zero on entry (cleared in phase C).
-// FP64 phase A by box site: thread k walks its cover list in order, updates
-// p there and stores P[k] (every site written, so P needs no clearing).  All
-// unknowns at k share D(k): one table lookup per site, one FP64 add per entry.
+// Phase A by box site: thread k walks its cover list in order, updates q
+// there and stores P(k) (every site written, so P needs no clearing).
 // NB: unknowns of a site whose loads are issued together (their indices
-// first, then their values), summed in the same order; 1 in the two-CTA
-// build, more where one CTA per SM leaves the registers for it.
+// first, then their values), summed in the same order; 2 in the two-CTA
+// build, 4 where one CTA per SM leaves the registers for it.
 template<int NB>
-__device__ __forceinline__ bool cg_phase_a_sites(const CGArgs &a, CGShared &sh, const CGVecs<double> &V) {
+__device__ __forceinline__ bool cg_phase_a_sites(const CGArgs &a, CGShared &sh, const CGVecs &V) {
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
 	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
@@ -427,16 +421,15 @@ __device__ __forceinline__ bool cg_phase_a_sites(const CGArgs &a, CGShared &sh, 
 	const int ax = sh.act[0], ay = sh.act[1], first = sh.first;
 	const double bx = sh.beta[0], by = sh.beta[1];
 	const double *rx = V.rx, *ry = V.ry;
-	double *px = V.px, *py = V.py, *Pbx = V.Pbx, *Pby = V.Pby;
+	double *qx = V.qx, *qy = V.qy, *Pbx = V.Pbx, *Pby = V.Pby;
 	const int *cov_idx = a.cov_idx, *cov_off = a.cov_off, *cnt = a.cnt;
 	for(long long k = gtid; k < L2; k += gstride) {
 		const int e0 = cov_off[k], e1 = cov_off[k + 1];
 		double sx = 0.0, sy = 0.0;
 		if(e1 > e0) {
-			const double id = sh.iT[box_deg(cnt, (int) k, L)];
 			for(int e = e0; e < e1; e += NB) {
 				int js[NB];
-				double rxv[NB], ryv[NB], pxv[NB], pyv[NB];
+				double rxv[NB], ryv[NB], qxv[NB], qyv[NB];
 #pragma unroll
 				for(int u = 0; u < NB; u++) js[u] = e + u < e1 ? cov_idx[e + u] : -1;
 #pragma unroll
@@ -444,28 +437,29 @@ __device__ __forceinline__ bool cg_phase_a_sites(const CGArgs &a, CGShared &sh, 
 					const int j = js[u];
 					const bool v = j >= 0;
 					rxv[u] = (v && ax) ? rx[j] : 0.0;
-					pxv[u] = (v && ax && !first) ? px[j] : 0.0;
+					qxv[u] = (v && ax && !first) ? qx[j] : 0.0;
 					ryv[u] = (v && ay) ? ry[j] : 0.0;
-					pyv[u] = (v && ay && !first) ? py[j] : 0.0;
+					qyv[u] = (v && ay && !first) ? qy[j] : 0.0;
 				}
 #pragma unroll
 				for(int u = 0; u < NB; u++) {
 					const int j = js[u];
 					if(j < 0) break;
 					if(ax) {
-						const double z = id * rxv[u];
-						const double p = first ? z : __fma_rn(bx, pxv[u], z);
-						px[j] = p;
-						sx += p;
+						const double q = first ? rxv[u] : __fma_rn(bx, qxv[u], rxv[u]);
+						qx[j] = q;
+						sx += q;
 					}
 					if(ay) {
-						const double z = id * ryv[u];
-						const double p = first ? z : __fma_rn(by, pyv[u], z);
-						py[j] = p;
-						sy += p;
+						const double q = first ? ryv[u] : __fma_rn(by, qyv[u], ryv[u]);
+						qy[j] = q;
+						sy += q;
 					}
 				}
 			}
+			const double id = sh.iT[box_deg(cnt, (int) k, L)];
+			sx *= id;
+			sy *= id;
 		}
 		if(ax) Pbx[k] = sx;
 		if(ay) Pby[k] = sy;
@@ -473,55 +467,56 @@ __device__ __forceinline__ bool cg_phase_a_sites(const CGArgs &a, CGShared &sh, 
 	return grid_reduce(a, sh, 0, nullptr);
 }
 
-// FP64 phase B by box site: the four-neighbour sum of P and the diagonal once
-// per site, then Ap and p.Ap for its unknowns.
+// Phase B by box site: the four-neighbour sum of P once per site, then Ap
+// and the site's sum of q Ap for its unknowns; p.Ap = sum_k (1/T) sum q Ap.
 template<int NB>
-__device__ __forceinline__ bool cg_phase_b_sites(const CGArgs &a, CGShared &sh, const CGVecs<double> &V) {
+__device__ __forceinline__ bool cg_phase_b_sites(const CGArgs &a, CGShared &sh, const CGVecs &V) {
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
 	const double neta = -a.eta * 1.0;
 	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
 	const long long gstride = (long long) gridDim.x * blockDim.x;
 	const int ax = sh.act[0], ay = sh.act[1];
-	const double *px = V.px, *py = V.py, *Pbx = V.Pbx, *Pby = V.Pby;
+	const double *qx = V.qx, *qy = V.qy, *Pbx = V.Pbx, *Pby = V.Pby;
 	double *apx = V.apx, *apy = V.apy;
 	const int *cov_idx = a.cov_idx, *cov_off = a.cov_off, *cnt = a.cnt;
 	double w0 = 0.0, w1 = 0.0;
 	for(long long k = gtid; k < L2; k += gstride) {
 		const int e0 = cov_off[k], e1 = cov_off[k + 1];
 		if(e1 == e0) continue;
-		const double d = sh.T[box_deg(cnt, (int) k, L)];
-		const double qx = ax ? neta * box_n4T<double>(Pbx, (int) k, L) : 0.0;
-		const double qy = ay ? neta * box_n4T<double>(Pby, (int) k, L) : 0.0;
+		const double nx = ax ? neta * box_n4T<double>(Pbx, (int) k, L) : 0.0;
+		const double ny = ay ? neta * box_n4T<double>(Pby, (int) k, L) : 0.0;
+		double sx = 0.0, sy = 0.0;
 		for(int e = e0; e < e1; e += NB) {
 			int js[NB];
-			double pxv[NB], pyv[NB];
+			double qxv[NB], qyv[NB];
 #pragma unroll
 			for(int u = 0; u < NB; u++) js[u] = e + u < e1 ? cov_idx[e + u] : -1;
 #pragma unroll
 			for(int u = 0; u < NB; u++) {
 				const int j = js[u];
-				pxv[u] = (j >= 0 && ax) ? px[j] : 0.0;
-				pyv[u] = (j >= 0 && ay) ? py[j] : 0.0;
+				qxv[u] = (j >= 0 && ax) ? qx[j] : 0.0;
+				qyv[u] = (j >= 0 && ay) ? qy[j] : 0.0;
 			}
 #pragma unroll
 			for(int u = 0; u < NB; u++) {
 				const int j = js[u];
 				if(j < 0) break;
 				if(ax) {
-					const double p = pxv[u];
-					const double ap = __fma_rn(d, p, qx);
+					const double ap = qxv[u] + nx;
 					apx[j] = ap;
-					w0 = __fma_rn(p, ap, w0);
+					sx = __fma_rn(qxv[u], ap, sx);
 				}
 				if(ay) {
-					const double p = pyv[u];
-					const double ap = __fma_rn(d, p, qy);
+					const double ap = qyv[u] + ny;
 					apy[j] = ap;
-					w1 = __fma_rn(p, ap, w1);
+					sy = __fma_rn(qyv[u], ap, sy);
 				}
 			}
 		}
+		const double id = sh.iT[box_deg(cnt, (int) k, L)];
+		w0 = __fma_rn(id, sx, w0);
+		w1 = __fma_rn(id, sy, w1);
 	}
 	double w[2] = {w0, w1};
 	warp_tree<double, 2>(w);
@@ -530,71 +525,90 @@ __device__ __forceinline__ bool cg_phase_b_sites(const CGArgs &a, CGShared &sh, 
 	return grid_reduce(a, sh, 2, v);
 }
 
-// Phase C: u += alpha p; r -= alpha Ap; |r|^2 and r.z into sh.tot[0..3];
-// the box sums are cleared for the next phase A.
-template<typename T>
-__device__ __forceinline__ bool cg_phase_c(const CGArgs &a, CGShared &sh, const CGVecs<T> &V) {
+// Phase C by box site: x += (alpha / T) q, r -= alpha Ap for the unknowns at
+// k and the site's sum of r^2, giving |r|^2 and r.z = sum_k (1/T) sum r^2
+// into sh.tot[0..3].
+template<int NB>
+__device__ __forceinline__ bool cg_phase_c_sites(const CGArgs &a, CGShared &sh, const CGVecs &V) {
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
-	const long long S = a.st->S;
 	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
 	const long long gstride = (long long) gridDim.x * blockDim.x;
 	const int ax = sh.act[0], ay = sh.act[1];
-	const T alx = (T) sh.alpha[0], aly = (T) sh.alpha[1];
-	const T *iTT = tab_iT<T>(sh);
-	const T *px = V.px, *py = V.py, *apx = V.apx, *apy = V.apy;
-	T *rx = V.rx, *ry = V.ry, *ux = V.ux, *uy = V.uy;
-	const int *mapg = a.mapg, *cnt = a.cnt;
-	T w[4] = {(T) 0, (T) 0, (T) 0, (T) 0};
-	for(long long j = gtid; j < S; j += gstride) {
-		const int k = mapg[j];
-		const T id = iTT[box_deg(cnt, k, L)];
-		if(ax) {
-			ux[j] = fmaT<T>(alx, px[j], ux[j]);
-			const T r = fmaT<T>(-alx, apx[j], rx[j]);
-			rx[j] = r;
-			w[0] = fmaT<T>(r, r, w[0]);
-			w[2] = fmaT<T>(r, id * r, w[2]);
+	const double alx = sh.alpha[0], aly = sh.alpha[1];
+	const double *qx = V.qx, *qy = V.qy, *apx = V.apx, *apy = V.apy;
+	double *rx = V.rx, *ry = V.ry, *ux = V.ux, *uy = V.uy;
+	const int *cov_idx = a.cov_idx, *cov_off = a.cov_off, *cnt = a.cnt;
+	double w[4] = {0.0, 0.0, 0.0, 0.0};
+	for(long long k = gtid; k < L2; k += gstride) {
+		const int e0 = cov_off[k], e1 = cov_off[k + 1];
+		if(e1 == e0) continue;
+		const double id = sh.iT[box_deg(cnt, (int) k, L)];
+		const double gx = alx * id, gy = aly * id;
+		double sx = 0.0, sy = 0.0;
+		for(int e = e0; e < e1; e += NB) {
+			int js[NB];
+			double qxv[NB], axv[NB], rxv[NB], uxv[NB], qyv[NB], ayv[NB], ryv[NB], uyv[NB];
+#pragma unroll
+			for(int u = 0; u < NB; u++) js[u] = e + u < e1 ? cov_idx[e + u] : -1;
+#pragma unroll
+			for(int u = 0; u < NB; u++) {
+				const int j = js[u];
+				const bool vx = j >= 0 && ax, vy = j >= 0 && ay;
+				qxv[u] = vx ? qx[j] : 0.0;
+				axv[u] = vx ? apx[j] : 0.0;
+				rxv[u] = vx ? rx[j] : 0.0;
+				uxv[u] = vx ? ux[j] : 0.0;
+				qyv[u] = vy ? qy[j] : 0.0;
+				ayv[u] = vy ? apy[j] : 0.0;
+				ryv[u] = vy ? ry[j] : 0.0;
+				uyv[u] = vy ? uy[j] : 0.0;
+			}
+#pragma unroll
+			for(int u = 0; u < NB; u++) {
+				const int j = js[u];
+				if(j < 0) break;
+				if(ax) {
+					ux[j] = __fma_rn(gx, qxv[u], uxv[u]);
+					const double r = __fma_rn(-alx, axv[u], rxv[u]);
+					rx[j] = r;
+					sx = __fma_rn(r, r, sx);
+				}
+				if(ay) {
+					uy[j] = __fma_rn(gy, qyv[u], uyv[u]);
+					const double r = __fma_rn(-aly, ayv[u], ryv[u]);
+					ry[j] = r;
+					sy = __fma_rn(r, r, sy);
+				}
+			}
 		}
-		if(ay) {
-			uy[j] = fmaT<T>(aly, py[j], uy[j]);
-			const T r = fmaT<T>(-aly, apy[j], ry[j]);
-			ry[j] = r;
-			w[1] = fmaT<T>(r, r, w[1]);
-			w[3] = fmaT<T>(r, id * r, w[3]);
-		}
+		w[0] += sx;
+		w[1] += sy;
+		w[2] = __fma_rn(id, sx, w[2]);
+		w[3] = __fma_rn(id, sy, w[3]);
 	}
-	double v[4] = {(double) w[0], (double) w[1], (double) w[2], (double) w[3]};
+	double v[4] = {w[0], w[1], w[2], w[3]};
 	block_sum<4>(v, sh.red);
 	return grid_reduce(a, sh, 4, v);
 }
 
 // Jacobi-preconditioned CG iterations from the state in sh (act, rz, thr) and
-// the residual in V.rx, V.ry: Eigen's loop, in FP64 (the plain solve and
-// the FP64 fallback of the mixed-precision refinement); every thread's
-// partial dot product is summed for the block and grid reductions.  Updates use fused multiply-adds (the solve is not bitwise
-// Eigen's in any case: its reductions run in a different order).
-template<typename T, int NB = 1>
-__device__ __forceinline__ bool cg_iterate(const CGArgs &a, CGShared &sh, const CGVecs<T> &V, long long max_it) {
-	const int L = a.L;
-	const long long L2 = (long long) L * L;
-	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-	const long long gstride = (long long) gridDim.x * blockDim.x;
+// the residual in V.rx, V.ry: Eigen's loop, in FP64 and on the scaled
+// direction q = T p (the plain solve and the FP64 fallback of the
+// mixed-precision refinement); every thread's partial dot products, in
+// box-site order, are summed for the block and grid reductions.
+template<int NB = 1>
+__device__ __forceinline__ bool cg_iterate(const CGArgs &a, CGShared &sh, const CGVecs &V, long long max_it) {
+	// phase A writes P at every site for each active component
 	if(threadIdx.x == 0) sh.first = 1;
-	for(long long k = gtid; k < L2; k += gstride) {
-		V.Pbx[k] = (T) 0;
-		V.Pby[k] = (T) 0;
-	}
-	if(!grid_reduce(a, sh, 0, nullptr)) return false;
+	__syncthreads();
 	long long sweep = 0;
 	while(sh.act[0] || sh.act[1]) {
-		if constexpr(sizeof(T) == sizeof(double)) {
-			if(a.harv_in && !a.mixed && sh.hm < a.harv_per_solve && sweep % a.harv_every == 0 &&
-			   sh.hbase + 2LL * (sh.hm + 1) <= a.harv_cap) {
-				if(!harvest_point(a, sh, V.ux, V.uy, V.rx, V.ry, sh.hm)) return false;
-				if(threadIdx.x == 0) sh.hm++;
-				__syncthreads();
-			}
+		if(a.harv_in && !a.mixed && sh.hm < a.harv_per_solve && sweep % a.harv_every == 0 &&
+		   sh.hbase + 2LL * (sh.hm + 1) <= a.harv_cap) {
+			if(!harvest_point(a, sh, V.ux, V.uy, V.rx, V.ry, sh.hm)) return false;
+			if(threadIdx.x == 0) sh.hm++;
+			__syncthreads();
 		}
 		sweep++;
 		const int ax = sh.act[0], ay = sh.act[1];
@@ -605,7 +619,8 @@ __device__ __forceinline__ bool cg_iterate(const CGArgs &a, CGShared &sh, const 
 			if(ay) sh.alpha[1] = sh.rz[1] / sh.tot[1];
 		}
 		__syncthreads();
-		if(!cg_phase_c<T>(a, sh, V)) return false;
+		// phase C loads twice the values per unknown: half the unknowns in flight
+		if(!cg_phase_c_sites<(NB > 1 ? NB / 2 : 1)>(a, sh, V)) return false;
 		if(threadIdx.x == 0) {
 			for(int c = 0; c < 2; c++) {
 				if(!sh.act[c]) continue;
@@ -1278,7 +1293,7 @@ __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcCtx &tc
 	const long long max_it = 2 * S;
 	int refinements = 0;
 	if constexpr(!LEARNED) {
-		if(!cg_iterate<double, NB>(a, sh, CGVecs<double>{a.rx, a.ry, a.px, a.py, a.apx, a.apy, a.Px, a.Py, a.vx, a.vy}, max_it)) return;
+		if(!cg_iterate<NB>(a, sh, CGVecs{a.rx, a.ry, a.px, a.py, a.apx, a.apy, a.Px, a.Py, a.vx, a.vy}, max_it)) return;
 		if(a.harv_in && sh.hm > 0 && !harvest_finish(a, sh, a.vx, a.vy)) return;
 	}
 	else {
@@ -1331,7 +1346,7 @@ __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcCtx &tc
 				}
 			}
 			__syncthreads();
-			if(!cg_iterate<double>(a, sh, CGVecs<double>{a.rx, a.ry, a.px, a.py, a.apx, a.apy, a.Px, a.Py, a.vx, a.vy}, max_it)) return;
+			if(!cg_iterate<1>(a, sh, CGVecs{a.rx, a.ry, a.px, a.py, a.apx, a.apy, a.Px, a.Py, a.vx, a.vy}, max_it)) return;
 		}
 	}
 	if(blockIdx.x == 0 && threadIdx.x == 0) {
