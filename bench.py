@@ -145,9 +145,12 @@ class ClockSampler:
 
 def cg_bytes_per_launch(S, L2, iters_per_launch, setup_reads=68.0):
     """Algorithmic bytes of one viscous-solve launch (both components):
-    setup S*68 B (b, x, r, map); per component-iteration S*78 B (p, r, x reads
-    and writes, cover indices, map) + L2*28 B (box sums of p)."""
-    return S * setup_reads + iters_per_launch * (S * 78.0 + L2 * 28.0)
+    setup S*68 B (b, x, r, map); per component-iteration the minimal fused
+    Jacobi-PCG, 11 FP64 vector passes = S*88 B (SpMV: read p, write Ap;
+    update: read x, r, p, Ap, write x, r; direction: read r, p, write p),
+    plus the box sums of p written and read (16 B) and the box count n(k)
+    (4 B) per box site = L2*20 B."""
+    return S * setup_reads + iters_per_launch * (S * 88.0 + L2 * 20.0)
 
 
 def fused_bytes_per_site(model):

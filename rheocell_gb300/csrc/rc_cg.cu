@@ -390,25 +390,31 @@ __device__ __forceinline__ T box_n4T(const T *P, int k, int L) {
 	return P[kd] + P[kl] + P[kr] + P[ku];
 }
 
-// Vectors of one FP64 CG run: residual r, scaled direction q = T p, A p, box
-// sums P of p, solution x.
+// Vectors of one FP64 CG run: residual r, scaled direction q = T p, box sums
+// P of p, solution x.
 struct CGVecs {
-	double *rx, *ry, *qx, *qy, *apx, *apy, *Pbx, *Pby, *ux, *uy;
+	double *rx, *ry, *qx, *qy, *Pbx, *Pby, *ux, *uy;
 };
 
 // The Jacobi preconditioner is constant on a box site (every unknown at k has
 // the diagonal T(k)), so the plain solve carries q = T p in place of Eigen's
 // direction p.  Eigen's p = z + beta p with z = r / T becomes q = r + beta q,
 // and every other 1/T factor is taken once per site instead of once per
-// unknown: P(k) = (1/T) sum q, Ap = q - eta N4(P), p.Ap = sum_k (1/T) sum q Ap,
-// x += (alpha / T) q, r.z = sum_k (1/T) sum r^2.  GB300 issues FP64 at a small
-// fraction of its FP32 rate and the solve is bound by that issue: this cuts
-// the FP64 operations per unknown and iteration from ten to seven.  The
-// iterates are Eigen's up to rounding (the solve is not bitwise Eigen's in any
-// case: its reductions run in a different order).
+// unknown.  With P(k) = sum of p over the unknowns at k:
+//   p.Ap = sum_k (1/T) sum q^2 - eta sum_k P(k) N4(P)(k)
+//   Ap = q - eta N4(P),  x += (alpha / T) q,  r.z = sum_k (1/T) sum r^2,
+// so no pass reads or writes an Ap vector: phase A forms q, P and the first
+// term of p.Ap; phase B is a pass over box sites only (the second term);
+// phase C forms Ap on the fly.  Per unknown and component-iteration that is
+// 64 B of vector traffic (r, q read and q written; q, r, x read and r, x
+// written) and seven FP64 operations -- GB300 issues FP64 at a small fraction
+// of its FP32 rate and the solve is bound by that issue and by HBM.  The
+// iterates are Eigen's up to rounding (the solve is not bitwise Eigen's in
+// any case: its reductions run in a different order).
 
 // Phase A by box site: thread k walks its cover list in order, updates q
-// there and stores P(k) (every site written, so P needs no clearing).
+// there, stores P(k) (every site written, so P needs no clearing) and sums
+// (1/T) sum q^2 into sh.tot[0..1].
 // NB: unknowns of a site whose loads are issued together (their indices
 // first, then their values), summed in the same order; 2 in the two-CTA
 // build, 4 where one CTA per SM leaves the registers for it.
@@ -423,10 +429,12 @@ __device__ __forceinline__ bool cg_phase_a_sites(const CGArgs &a, CGShared &sh, 
 	const double *rx = V.rx, *ry = V.ry;
 	double *qx = V.qx, *qy = V.qy, *Pbx = V.Pbx, *Pby = V.Pby;
 	const int *cov_idx = a.cov_idx, *cov_off = a.cov_off, *cnt = a.cnt;
+	double w0 = 0.0, w1 = 0.0;
 	for(long long k = gtid; k < L2; k += gstride) {
 		const int e0 = cov_off[k], e1 = cov_off[k + 1];
 		double sx = 0.0, sy = 0.0;
 		if(e1 > e0) {
+			double hx = 0.0, hy = 0.0;
 			for(int e = e0; e < e1; e += NB) {
 				int js[NB];
 				double rxv[NB], ryv[NB], qxv[NB], qyv[NB];
@@ -449,74 +457,24 @@ __device__ __forceinline__ bool cg_phase_a_sites(const CGArgs &a, CGShared &sh, 
 						const double q = first ? rxv[u] : __fma_rn(bx, qxv[u], rxv[u]);
 						qx[j] = q;
 						sx += q;
+						hx = __fma_rn(q, q, hx);
 					}
 					if(ay) {
 						const double q = first ? ryv[u] : __fma_rn(by, qyv[u], ryv[u]);
 						qy[j] = q;
 						sy += q;
+						hy = __fma_rn(q, q, hy);
 					}
 				}
 			}
 			const double id = sh.iT[box_deg(cnt, (int) k, L)];
 			sx *= id;
 			sy *= id;
+			w0 = __fma_rn(id, hx, w0);
+			w1 = __fma_rn(id, hy, w1);
 		}
 		if(ax) Pbx[k] = sx;
 		if(ay) Pby[k] = sy;
-	}
-	return grid_reduce(a, sh, 0, nullptr);
-}
-
-// Phase B by box site: the four-neighbour sum of P once per site, then Ap
-// and the site's sum of q Ap for its unknowns; p.Ap = sum_k (1/T) sum q Ap.
-template<int NB>
-__device__ __forceinline__ bool cg_phase_b_sites(const CGArgs &a, CGShared &sh, const CGVecs &V) {
-	const int L = a.L;
-	const long long L2 = (long long) L * L;
-	const double neta = -a.eta * 1.0;
-	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-	const long long gstride = (long long) gridDim.x * blockDim.x;
-	const int ax = sh.act[0], ay = sh.act[1];
-	const double *qx = V.qx, *qy = V.qy, *Pbx = V.Pbx, *Pby = V.Pby;
-	double *apx = V.apx, *apy = V.apy;
-	const int *cov_idx = a.cov_idx, *cov_off = a.cov_off, *cnt = a.cnt;
-	double w0 = 0.0, w1 = 0.0;
-	for(long long k = gtid; k < L2; k += gstride) {
-		const int e0 = cov_off[k], e1 = cov_off[k + 1];
-		if(e1 == e0) continue;
-		const double nx = ax ? neta * box_n4T<double>(Pbx, (int) k, L) : 0.0;
-		const double ny = ay ? neta * box_n4T<double>(Pby, (int) k, L) : 0.0;
-		double sx = 0.0, sy = 0.0;
-		for(int e = e0; e < e1; e += NB) {
-			int js[NB];
-			double qxv[NB], qyv[NB];
-#pragma unroll
-			for(int u = 0; u < NB; u++) js[u] = e + u < e1 ? cov_idx[e + u] : -1;
-#pragma unroll
-			for(int u = 0; u < NB; u++) {
-				const int j = js[u];
-				qxv[u] = (j >= 0 && ax) ? qx[j] : 0.0;
-				qyv[u] = (j >= 0 && ay) ? qy[j] : 0.0;
-			}
-#pragma unroll
-			for(int u = 0; u < NB; u++) {
-				const int j = js[u];
-				if(j < 0) break;
-				if(ax) {
-					const double ap = qxv[u] + nx;
-					apx[j] = ap;
-					sx = __fma_rn(qxv[u], ap, sx);
-				}
-				if(ay) {
-					const double ap = qyv[u] + ny;
-					apy[j] = ap;
-					sy = __fma_rn(qyv[u], ap, sy);
-				}
-			}
-		}
-		const double id = sh.iT[box_deg(cnt, (int) k, L)];
-		w0 = __fma_rn(id, sx, w0);
-		w1 = __fma_rn(id, sy, w1);
 	}
 	double w[2] = {w0, w1};
 	warp_tree<double, 2>(w);
@@ -525,18 +483,43 @@ __device__ __forceinline__ bool cg_phase_b_sites(const CGArgs &a, CGShared &sh, 
 	return grid_reduce(a, sh, 2, v);
 }
 
-// Phase C by box site: x += (alpha / T) q, r -= alpha Ap for the unknowns at
-// k and the site's sum of r^2, giving |r|^2 and r.z = sum_k (1/T) sum r^2
-// into sh.tot[0..3].
-template<int NB>
-__device__ __forceinline__ bool cg_phase_c_sites(const CGArgs &a, CGShared &sh, const CGVecs &V) {
+// Phase B over box sites: sum_k P(k) N4(P)(k) = 2 sum_k P(k) (P(k + x) +
+// P(k + y)) on the periodic box, into sh.tot[0..1].
+__device__ __forceinline__ bool cg_phase_b_sites(const CGArgs &a, CGShared &sh, const CGVecs &V) {
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
 	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
 	const long long gstride = (long long) gridDim.x * blockDim.x;
 	const int ax = sh.act[0], ay = sh.act[1];
+	const double *Pbx = V.Pbx, *Pby = V.Pby;
+	double w0 = 0.0, w1 = 0.0;
+	for(long long k = gtid; k < L2; k += gstride) {
+		const int x = (int) (k % L);
+		const long long kr = (x == L - 1) ? k - (L - 1) : k + 1;
+		const long long ku = (k >= L2 - L) ? k - (L2 - L) : k + L;
+		if(ax) w0 = __fma_rn(Pbx[k], Pbx[kr] + Pbx[ku], w0);
+		if(ay) w1 = __fma_rn(Pby[k], Pby[kr] + Pby[ku], w1);
+	}
+	double w[2] = {w0, w1};
+	warp_tree<double, 2>(w);
+	double v[2] = {w[0], w[1]};
+	block_sum_warps<2>(v, sh.red);
+	return grid_reduce(a, sh, 2, v);
+}
+
+// Phase C by box site: Ap = q - eta N4(P), x += (alpha / T) q, r -= alpha Ap
+// for the unknowns at k and the site's sum of r^2, giving |r|^2 and
+// r.z = sum_k (1/T) sum r^2 into sh.tot[0..3].
+template<int NB>
+__device__ __forceinline__ bool cg_phase_c_sites(const CGArgs &a, CGShared &sh, const CGVecs &V) {
+	const int L = a.L;
+	const long long L2 = (long long) L * L;
+	const double neta = -a.eta * 1.0;
+	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
+	const long long gstride = (long long) gridDim.x * blockDim.x;
+	const int ax = sh.act[0], ay = sh.act[1];
 	const double alx = sh.alpha[0], aly = sh.alpha[1];
-	const double *qx = V.qx, *qy = V.qy, *apx = V.apx, *apy = V.apy;
+	const double *qx = V.qx, *qy = V.qy, *Pbx = V.Pbx, *Pby = V.Pby;
 	double *rx = V.rx, *ry = V.ry, *ux = V.ux, *uy = V.uy;
 	const int *cov_idx = a.cov_idx, *cov_off = a.cov_off, *cnt = a.cnt;
 	double w[4] = {0.0, 0.0, 0.0, 0.0};
@@ -545,10 +528,12 @@ __device__ __forceinline__ bool cg_phase_c_sites(const CGArgs &a, CGShared &sh, 
 		if(e1 == e0) continue;
 		const double id = sh.iT[box_deg(cnt, (int) k, L)];
 		const double gx = alx * id, gy = aly * id;
+		const double nx = ax ? neta * box_n4T<double>(Pbx, (int) k, L) : 0.0;
+		const double ny = ay ? neta * box_n4T<double>(Pby, (int) k, L) : 0.0;
 		double sx = 0.0, sy = 0.0;
 		for(int e = e0; e < e1; e += NB) {
 			int js[NB];
-			double qxv[NB], axv[NB], rxv[NB], uxv[NB], qyv[NB], ayv[NB], ryv[NB], uyv[NB];
+			double qxv[NB], rxv[NB], uxv[NB], qyv[NB], ryv[NB], uyv[NB];
 #pragma unroll
 			for(int u = 0; u < NB; u++) js[u] = e + u < e1 ? cov_idx[e + u] : -1;
 #pragma unroll
@@ -556,11 +541,9 @@ __device__ __forceinline__ bool cg_phase_c_sites(const CGArgs &a, CGShared &sh, 
 				const int j = js[u];
 				const bool vx = j >= 0 && ax, vy = j >= 0 && ay;
 				qxv[u] = vx ? qx[j] : 0.0;
-				axv[u] = vx ? apx[j] : 0.0;
 				rxv[u] = vx ? rx[j] : 0.0;
 				uxv[u] = vx ? ux[j] : 0.0;
 				qyv[u] = vy ? qy[j] : 0.0;
-				ayv[u] = vy ? apy[j] : 0.0;
 				ryv[u] = vy ? ry[j] : 0.0;
 				uyv[u] = vy ? uy[j] : 0.0;
 			}
@@ -570,13 +553,13 @@ __device__ __forceinline__ bool cg_phase_c_sites(const CGArgs &a, CGShared &sh, 
 				if(j < 0) break;
 				if(ax) {
 					ux[j] = __fma_rn(gx, qxv[u], uxv[u]);
-					const double r = __fma_rn(-alx, axv[u], rxv[u]);
+					const double r = __fma_rn(-alx, qxv[u] + nx, rxv[u]);
 					rx[j] = r;
 					sx = __fma_rn(r, r, sx);
 				}
 				if(ay) {
 					uy[j] = __fma_rn(gy, qyv[u], uyv[u]);
-					const double r = __fma_rn(-aly, ayv[u], ryv[u]);
+					const double r = __fma_rn(-aly, qyv[u] + ny, ryv[u]);
 					ry[j] = r;
 					sy = __fma_rn(r, r, sy);
 				}
@@ -613,14 +596,20 @@ __device__ __forceinline__ bool cg_iterate(const CGArgs &a, CGShared &sh, const 
 		sweep++;
 		const int ax = sh.act[0], ay = sh.act[1];
 		if(!cg_phase_a_sites<NB>(a, sh, V)) return false;
-		if(!cg_phase_b_sites<NB>(a, sh, V)) return false;
 		if(threadIdx.x == 0) {
-			if(ax) sh.alpha[0] = sh.rz[0] / sh.tot[0];
-			if(ay) sh.alpha[1] = sh.rz[1] / sh.tot[1];
+			sh.pap[0] = sh.tot[0];
+			sh.pap[1] = sh.tot[1];
+		}
+		if(!cg_phase_b_sites(a, sh, V)) return false;
+		if(threadIdx.x == 0) {
+			const double neta2 = -2.0 * a.eta;
+			if(ax) sh.alpha[0] = sh.rz[0] / __fma_rn(neta2, sh.tot[0], sh.pap[0]);
+			if(ay) sh.alpha[1] = sh.rz[1] / __fma_rn(neta2, sh.tot[1], sh.pap[1]);
 		}
 		__syncthreads();
-		// phase C loads twice the values per unknown: half the unknowns in flight
-		if(!cg_phase_c_sites<(NB > 1 ? NB / 2 : 1)>(a, sh, V)) return false;
+		// phase C holds six values per unknown: the two-CTA build has the
+		// registers for one unknown in flight
+		if(!cg_phase_c_sites<(NB >= 4 ? NB : 1)>(a, sh, V)) return false;
 		if(threadIdx.x == 0) {
 			for(int c = 0; c < 2; c++) {
 				if(!sh.act[c]) continue;
@@ -1293,7 +1282,7 @@ __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcCtx &tc
 	const long long max_it = 2 * S;
 	int refinements = 0;
 	if constexpr(!LEARNED) {
-		if(!cg_iterate<NB>(a, sh, CGVecs{a.rx, a.ry, a.px, a.py, a.apx, a.apy, a.Px, a.Py, a.vx, a.vy}, max_it)) return;
+		if(!cg_iterate<NB>(a, sh, CGVecs{a.rx, a.ry, a.px, a.py, a.Px, a.Py, a.vx, a.vy}, max_it)) return;
 		if(a.harv_in && sh.hm > 0 && !harvest_finish(a, sh, a.vx, a.vy)) return;
 	}
 	else {
@@ -1346,7 +1335,7 @@ __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcCtx &tc
 				}
 			}
 			__syncthreads();
-			if(!cg_iterate<1>(a, sh, CGVecs{a.rx, a.ry, a.px, a.py, a.apx, a.apy, a.Px, a.Py, a.vx, a.vy}, max_it)) return;
+			if(!cg_iterate<1>(a, sh, CGVecs{a.rx, a.ry, a.px, a.py, a.Px, a.Py, a.vx, a.vy}, max_it)) return;
 		}
 	}
 	if(blockIdx.x == 0 && threadIdx.x == 0) {

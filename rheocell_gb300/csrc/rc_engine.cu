@@ -78,7 +78,7 @@ struct rc_engine {
 	CellSum *csum = nullptr;  // split mode (many cells): per-cell sums for the epilogue kernel
 	DevStatus *st = nullptr;
 	DevStatus *st_host = nullptr;
-	double *rx = nullptr, *ry = nullptr, *px = nullptr, *py = nullptr, *apx = nullptr, *apy = nullptr, *Px = nullptr, *Py = nullptr;
+	double *rx = nullptr, *ry = nullptr, *px = nullptr, *py = nullptr, *Px = nullptr, *Py = nullptr;
 	double *partials = nullptr, *scalars = nullptr;
 	unsigned *bar = nullptr;
 	float *rxf = nullptr, *ryf = nullptr, *pxf = nullptr, *pyf = nullptr, *apxf = nullptr, *apyf = nullptr;
@@ -306,8 +306,6 @@ static void solve(rc_engine *e, int phase) {
 	g.ry = e->ry;
 	g.px = e->px;
 	g.py = e->py;
-	g.apx = e->apx;
-	g.apy = e->apy;
 	g.apxf = e->apxf;
 	g.apyf = e->apyf;
 	g.Px = e->Px;
@@ -808,7 +806,7 @@ int rc_batch_create(const rc_params *params, int n_layers, const rc_box *boxes, 
 		if((rc = dalloc(e, &e->fx, cap)) || (rc = dalloc(e, &e->fy, cap)) || (rc = dalloc(e, &e->cover, L2 * STORE_MAX)) ||
 		   (rc = dalloc(e, &e->cov_off, L2 + 1)) || (rc = dalloc(e, &e->cov_idx, cap)) ||
 		   (rc = dalloc(e, &e->rx, cap)) || (rc = dalloc(e, &e->ry, cap)) || (rc = dalloc(e, &e->px, cap)) ||
-		   (rc = dalloc(e, &e->py, cap)) || (rc = dalloc(e, &e->apx, cap)) || (rc = dalloc(e, &e->apy, cap)) ||
+		   (rc = dalloc(e, &e->py, cap)) ||
 		   (rc = dalloc(e, &e->Px, L2)) || (rc = dalloc(e, &e->Py, L2)) ||
 		   (rc = dalloc(e, &e->partials, 8 * 4096)) || (rc = dalloc(e, &e->scalars, 64)) || (rc = dalloc(e, &e->bar, 4)))
 			return bail(rc);
@@ -1527,7 +1525,7 @@ constexpr size_t NA_OFF_SCALARS = NA_OFF_BAR + na_round(2 * sizeof(unsigned));
 constexpr size_t NA_OFF_PARTIALS = NA_OFF_SCALARS + na_round(64 * sizeof(double));
 constexpr size_t NA_OFF_VEC = NA_OFF_PARTIALS + na_round(8 * NA_MAX_BLOCKS * sizeof(double));
 constexpr size_t NA_VEC = na_round(NA_MAX_UNKNOWNS * sizeof(double));
-constexpr size_t NA_OFF_BOX = NA_OFF_VEC + 6 * NA_VEC;
+constexpr size_t NA_OFF_BOX = NA_OFF_VEC + 4 * NA_VEC;
 constexpr size_t NA_BOX = na_round(NA_MAX_BOX_SITES * sizeof(double));
 constexpr size_t NA_OFF_COV_OFF = NA_OFF_BOX + 2 * NA_BOX;
 constexpr size_t NA_OFF_COV_IDX = NA_OFF_COV_OFF + na_round((NA_MAX_BOX_SITES + 1) * sizeof(int));
@@ -1625,8 +1623,6 @@ int rc_viscous_resolve_noalloc(rc_engine *e, double *vx, double *vy, long long n
 	g.ry = vec + vs;
 	g.px = vec + 2 * vs;
 	g.py = vec + 3 * vs;
-	g.apx = vec + 4 * vs;
-	g.apy = vec + 5 * vs;
 	g.Px = (double *) (base + NA_OFF_BOX);
 	g.Py = g.Px + bs;
 	g.partials = (double *) (base + NA_OFF_PARTIALS);

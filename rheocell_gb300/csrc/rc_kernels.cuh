@@ -77,7 +77,7 @@ struct CGArgs {
 	int *cov_off, *cov_idx;  // CSR cover lists built by the solve
 	const double *fx, *fy;   // right-hand sides
 	double *vx, *vy;         // solution; warm start
-	double *rx, *ry, *px, *py, *apx, *apy;
+	double *rx, *ry, *px, *py;  // residual; scaled direction T p
 	double *Px, *Py;         // box-grid sums of p
 	double *partials;        // per-block partial sums
 	double *scalars;         // solver scalars (see rc_cg.cu)
