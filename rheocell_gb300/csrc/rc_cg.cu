@@ -50,6 +50,7 @@ struct CGShared {
 	double pap[2], scale[2];  // learned path: p.Ap of the sweep, residual scale
 	float Tf[CG_MAX_D + 1], iTf[CG_MAX_D + 1];  // FP32 copies of T, 1/T (learned path)
 	int act[2], it[2], first, zero[2];
+	int site_first, site_step, site_end;  // by-site phases: this block's box sites
 	int hbase, hm;            // harvesting: first slot of this solve, points taken
 	unsigned long long tmark; // diagnostic phase timers: last mark (block 0, thread 0)
 	unsigned epoch;           // grid barriers passed (the same count in every block)
@@ -412,6 +413,40 @@ struct CGVecs {
 // iterates are Eigen's up to rounding (the solve is not bitwise Eigen's in
 // any case: its reductions run in a different order).
 
+// First box site k in [0, L2] with cov_off[k] >= t (cov_off is
+// nondecreasing, cov_off[L2] = the number of cover entries >= t).
+__device__ __forceinline__ long long first_site_from(const int *cov_off, long long L2, long long t) {
+	long long lo = 0, hi = L2;
+	while(lo < hi) {
+		const long long mid = (lo + hi) >> 1;
+		if((long long) __ldcg(&cov_off[mid]) >= t) hi = mid;
+		else lo = mid + 1;
+	}
+	return lo;
+}
+
+// The box sites of this block in the by-site phases (thread 0 only): the
+// thread (or warp) at offset t of the block takes sites site_first + t,
+// + site_step, ... below site_end.  On boxes with fewer than four sites per
+// thread of the grid the block takes a contiguous run of sites holding an
+// equal share of the cover entries (the unknowns): a grid-stride split would
+// leave whole blocks (SMs) without sites there while others walk long cover
+// lists.  Larger boxes keep the grid-stride split, balanced by itself.
+__device__ __forceinline__ void block_site_range(const CGArgs &a, CGShared &sh) {
+	const long long L2 = (long long) a.L * a.L;
+	const long long nb = gridDim.x, b = blockIdx.x, threads = nb * blockDim.x;
+	if(L2 >= 4 * threads) {
+		sh.site_first = (int) (b * blockDim.x);
+		sh.site_step = (int) threads;
+		sh.site_end = (int) L2;
+		return;
+	}
+	const long long E = __ldcg(&a.cov_off[L2]);
+	sh.site_first = (int) first_site_from(a.cov_off, L2, E * b / nb);
+	sh.site_step = blockDim.x;
+	sh.site_end = (int) (b + 1 == nb ? L2 : first_site_from(a.cov_off, L2, E * (b + 1) / nb));
+}
+
 // Phase A by box site: thread k walks its cover list in order, updates q
 // there, stores P(k) (every site written, so P needs no clearing) and sums
 // (1/T) sum q^2 into sh.tot[0..1].
@@ -421,16 +456,13 @@ struct CGVecs {
 template<int NB>
 __device__ __forceinline__ bool cg_phase_a_sites(const CGArgs &a, CGShared &sh, const CGVecs &V) {
 	const int L = a.L;
-	const long long L2 = (long long) L * L;
-	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-	const long long gstride = (long long) gridDim.x * blockDim.x;
 	const int ax = sh.act[0], ay = sh.act[1], first = sh.first;
 	const double bx = sh.beta[0], by = sh.beta[1];
 	const double *rx = V.rx, *ry = V.ry;
 	double *qx = V.qx, *qy = V.qy, *Pbx = V.Pbx, *Pby = V.Pby;
 	const int *cov_idx = a.cov_idx, *cov_off = a.cov_off, *cnt = a.cnt;
 	double w0 = 0.0, w1 = 0.0;
-	for(long long k = gtid; k < L2; k += gstride) {
+	for(long long k = sh.site_first + threadIdx.x; k < sh.site_end; k += sh.site_step) {
 		const int e0 = cov_off[k], e1 = cov_off[k + 1];
 		double sx = 0.0, sy = 0.0;
 		if(e1 > e0) {
@@ -513,17 +545,14 @@ __device__ __forceinline__ bool cg_phase_b_sites(const CGArgs &a, CGShared &sh, 
 template<int NB>
 __device__ __forceinline__ bool cg_phase_c_sites(const CGArgs &a, CGShared &sh, const CGVecs &V) {
 	const int L = a.L;
-	const long long L2 = (long long) L * L;
 	const double neta = -a.eta * 1.0;
-	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
-	const long long gstride = (long long) gridDim.x * blockDim.x;
 	const int ax = sh.act[0], ay = sh.act[1];
 	const double alx = sh.alpha[0], aly = sh.alpha[1];
 	const double *qx = V.qx, *qy = V.qy, *Pbx = V.Pbx, *Pby = V.Pby;
 	double *rx = V.rx, *ry = V.ry, *ux = V.ux, *uy = V.uy;
 	const int *cov_idx = a.cov_idx, *cov_off = a.cov_off, *cnt = a.cnt;
 	double w[4] = {0.0, 0.0, 0.0, 0.0};
-	for(long long k = gtid; k < L2; k += gstride) {
+	for(long long k = sh.site_first + threadIdx.x; k < sh.site_end; k += sh.site_step) {
 		const int e0 = cov_off[k], e1 = cov_off[k + 1];
 		if(e1 == e0) continue;
 		const double id = sh.iT[box_deg(cnt, (int) k, L)];
@@ -583,7 +612,10 @@ __device__ __forceinline__ bool cg_phase_c_sites(const CGArgs &a, CGShared &sh, 
 template<int NB = 1>
 __device__ __forceinline__ bool cg_iterate(const CGArgs &a, CGShared &sh, const CGVecs &V, long long max_it) {
 	// phase A writes P at every site for each active component
-	if(threadIdx.x == 0) sh.first = 1;
+	if(threadIdx.x == 0) {
+		block_site_range(a, sh);
+		sh.first = 1;
+	}
 	__syncthreads();
 	long long sweep = 0;
 	while(sh.act[0] || sh.act[1]) {
@@ -894,8 +926,6 @@ __device__ __noinline__ bool fcg_phase_e(const CGArgs &a, CGShared &sh, bool fir
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
 	const int lane = threadIdx.x & 31;
-	const long long gwarp = (blockIdx.x * (long long) blockDim.x + threadIdx.x) >> 5;
-	const long long nwarps = ((long long) gridDim.x * blockDim.x) >> 5;
 	const int ax = sh.act[0], ay = sh.act[1];
 	const float es0 = (float) (a.eta * sh.scale[0]), es1 = (float) (a.eta * sh.scale[1]);
 	const bool net = a.unet_params != nullptr;  // without a network: z = r / T (Jacobi)
@@ -903,13 +933,15 @@ __device__ __noinline__ bool fcg_phase_e(const CGArgs &a, CGShared &sh, bool fir
 	const float *rx = a.rxf, *ry = a.ryf, *apx = a.apxf, *apy = a.apyf;
 	float *zx = a.zxf, *zy = a.zyf;
 	const int *cov_off = a.cov_off;
-	const int Etot = __ldcg(&cov_off[L2]);
+	const int Eend = __ldcg(&cov_off[sh.site_end]);
 	float *accx = wacc, *accy = wacc + blockDim.x;
 	float w[4] = {0.f, 0.f, 0.f, 0.f};
-	for(long long g = gwarp; g * 32 < L2; g += nwarps) {
-		const long long k = g * 32 + lane;
-		const bool kv = k < L2;
-		const int e0 = kv ? cov_off[k] : Etot, e1 = kv ? cov_off[k + 1] : Etot;
+	// warps take runs of 32 of the block's sites; lanes past the last site
+	// hold the empty entry range at Eend
+	for(long long k0 = sh.site_first + (threadIdx.x & ~31); k0 < sh.site_end; k0 += sh.site_step) {
+		const long long k = k0 + lane;
+		const bool kv = k < sh.site_end;
+		const int e0 = kv ? cov_off[k] : Eend, e1 = kv ? cov_off[k + 1] : Eend;
 		float id = 0.f, nvx = 0.f, nvy = 0.f;
 		if(e1 > e0) {
 			id = sh.iTf[box_deg(a.cnt, (int) k, L)];
@@ -984,23 +1016,22 @@ __device__ __noinline__ bool fcg_phase_e(const CGArgs &a, CGShared &sh, bool fir
 __device__ __noinline__ bool fcg_phase_ab(const CGArgs &a, CGShared &sh, bool first, const float *Pox, const float *Poy,
                                           float *Pnx, float *Pny, float *wacc) {
 	const int L = a.L;
-	const long long L2 = (long long) L * L;
 	const int lane = threadIdx.x & 31;
-	const long long gwarp = (blockIdx.x * (long long) blockDim.x + threadIdx.x) >> 5;
-	const long long nwarps = ((long long) gridDim.x * blockDim.x) >> 5;
 	const int ax = sh.act[0], ay = sh.act[1];
 	const float bx = (float) sh.beta[0], by = (float) sh.beta[1];
 	const float neta = (float) (-a.eta * 1.0);
 	const float *zx = a.zxf, *zy = a.zyf, *Zx = a.Zxf, *Zy = a.Zyf;
 	float *px = a.pxf, *py = a.pyf, *apx = a.apxf, *apy = a.apyf;
 	const int *cov_off = a.cov_off;
-	const int Etot = __ldcg(&cov_off[L2]);
+	const int Eend = __ldcg(&cov_off[sh.site_end]);
 	float *accx = wacc, *accy = wacc + blockDim.x;
 	float w[2] = {0.f, 0.f};
-	for(long long g = gwarp; g * 32 < L2; g += nwarps) {
-		const long long k = g * 32 + lane;
-		const bool kv = k < L2;
-		const int e0 = kv ? cov_off[k] : Etot, e1 = kv ? cov_off[k + 1] : Etot;
+	// warps take runs of 32 of the block's sites; lanes past the last site
+	// hold the empty entry range at Eend
+	for(long long k0 = sh.site_first + (threadIdx.x & ~31); k0 < sh.site_end; k0 += sh.site_step) {
+		const long long k = k0 + lane;
+		const bool kv = k < sh.site_end;
+		const int e0 = kv ? cov_off[k] : Eend, e1 = kv ? cov_off[k + 1] : Eend;
 		float d = 0.f, qx = 0.f, qy = 0.f;
 		if(e1 > e0) {
 			d = sh.Tf[box_deg(a.cnt, (int) k, L)];
@@ -1079,21 +1110,21 @@ __device__ __noinline__ bool fcg_phase_c(const CGArgs &a, CGShared &sh, float *w
 	const int L = a.L;
 	const long long L2 = (long long) L * L;
 	const int lane = threadIdx.x & 31;
-	const long long gwarp = (blockIdx.x * (long long) blockDim.x + threadIdx.x) >> 5;
-	const long long nwarps = ((long long) gridDim.x * blockDim.x) >> 5;
 	const int ax = sh.act[0], ay = sh.act[1];
 	const float alx = (float) sh.alpha[0], aly = (float) sh.alpha[1];
 	const float *px = a.pxf, *py = a.pyf, *apx = a.apxf, *apy = a.apyf;
 	float *ex = a.exf, *ey = a.eyf, *rx = a.rxf, *ry = a.ryf, *x0 = a.unet.x0;
 	const bool net = a.unet_params != nullptr;
 	const int *cov_off = a.cov_off;
-	const int Etot = __ldcg(&cov_off[L2]);
+	const int Eend = __ldcg(&cov_off[sh.site_end]);
 	float *accx = wacc, *accy = wacc + blockDim.x;
 	float w[2] = {0.f, 0.f};
-	for(long long g = gwarp; g * 32 < L2; g += nwarps) {
-		const long long k = g * 32 + lane;
-		const bool kv = k < L2;
-		const int e0 = kv ? cov_off[k] : Etot, e1 = kv ? cov_off[k + 1] : Etot;
+	// warps take runs of 32 of the block's sites; lanes past the last site
+	// hold the empty entry range at Eend
+	for(long long k0 = sh.site_first + (threadIdx.x & ~31); k0 < sh.site_end; k0 += sh.site_step) {
+		const long long k = k0 + lane;
+		const bool kv = k < sh.site_end;
+		const int e0 = kv ? cov_off[k] : Eend, e1 = kv ? cov_off[k + 1] : Eend;
 		const float id = (e1 > e0) ? sh.iTf[box_deg(a.cnt, (int) k, L)] : 0.f;
 		accx[threadIdx.x] = 0.f;
 		accy[threadIdx.x] = 0.f;
@@ -1178,6 +1209,7 @@ __device__ __noinline__ bool fcg_iterate(const CGArgs &a, CGShared &sh, TcCtx &t
 	}
 	if(threadIdx.x == 0) {
 		for(int c = 0; c < 2; c++) sh.scale[c] = sqrt(sh.rn2[c] / (double) S);
+		block_site_range(a, sh);
 	}
 	__syncthreads();
 	pmark(a, sh, PH_INIT);
