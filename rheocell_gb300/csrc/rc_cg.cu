@@ -243,7 +243,11 @@ enum { RES_FP64 = 0, RES_FLOAT_COVER = 1 };
 // add_e: first x += e, the FP32 correction of the last refinement sweep
 // (exf/eyf, in cover order; RES_FLOAT_COVER only), fused into the pass that
 // forms the box sums of x.
-template<int fmode>
+// NB: unknowns of a site whose index and value loads are issued together
+// (one dependent load chain per NB unknowns instead of per unknown); the
+// arithmetic runs unknown by unknown in cover order whatever NB is, so the
+// result does not depend on it.
+template<int fmode, int NB = 1>
 __device__ __forceinline__ bool true_residual(const CGArgs &a, CGShared &sh, bool x_zero, bool want_b = true, bool want_rz = true,
                                               bool add_e = false) {
 	const int L = a.L;
@@ -257,17 +261,36 @@ __device__ __forceinline__ bool true_residual(const CGArgs &a, CGShared &sh, boo
 			const int e0 = cov_off[k], e1 = cov_off[k + 1];
 			double sx = 0.0, sy = 0.0;
 #pragma unroll 1
-			for(int e = e0; e < e1; e++) {
-				const int j = cov_idx[e];
-				double ux = a.vx[j], uy = a.vy[j];
-				if(fmode == RES_FLOAT_COVER && add_e) {
-					ux += (double) a.exf[e];
-					uy += (double) a.eyf[e];
-					a.vx[j] = ux;
-					a.vy[j] = uy;
+			for(int e = e0; e < e1; e += NB) {
+				int js[NB];
+				double uxv[NB], uyv[NB];
+				float exv[NB], eyv[NB];
+#pragma unroll
+				for(int u = 0; u < NB; u++) js[u] = e + u < e1 ? cov_idx[e + u] : -1;
+#pragma unroll
+				for(int u = 0; u < NB; u++) {
+					const int j = js[u];
+					uxv[u] = j >= 0 ? a.vx[j] : 0.0;
+					uyv[u] = j >= 0 ? a.vy[j] : 0.0;
+					if(fmode == RES_FLOAT_COVER && add_e) {
+						exv[u] = j >= 0 ? a.exf[e + u] : 0.0f;
+						eyv[u] = j >= 0 ? a.eyf[e + u] : 0.0f;
+					}
 				}
-				sx += ux;
-				sy += uy;
+#pragma unroll
+				for(int u = 0; u < NB; u++) {
+					const int j = js[u];
+					if(j < 0) break;
+					double ux = uxv[u], uy = uyv[u];
+					if(fmode == RES_FLOAT_COVER && add_e) {
+						ux += (double) exv[u];
+						uy += (double) eyv[u];
+						a.vx[j] = ux;
+						a.vy[j] = uy;
+					}
+					sx += ux;
+					sy += uy;
+				}
 			}
 			a.Px[k] = sx;
 			a.Py[k] = sy;
@@ -285,46 +308,63 @@ __device__ __forceinline__ bool true_residual(const CGArgs &a, CGShared &sh, boo
 			const double qx = x_zero ? 0.0 : neta * box_n4(a.Px, (int) k, L);
 			const double qy = x_zero ? 0.0 : neta * box_n4(a.Py, (int) k, L);
 #pragma unroll 1
-			for(int e = e0; e < e1; e++) {
-				const int j = cov_idx[e];
-				const double bx = a.fx[j], by = a.fy[j];
-				double rx, ry;
-				if(x_zero) {
-					rx = bx - 0.0;
-					ry = by - 0.0;
+			for(int e0b = e0; e0b < e1; e0b += NB) {
+				int js[NB];
+				double bxv[NB], byv[NB], uxv[NB], uyv[NB];
+#pragma unroll
+				for(int u = 0; u < NB; u++) js[u] = e0b + u < e1 ? cov_idx[e0b + u] : -1;
+#pragma unroll
+				for(int u = 0; u < NB; u++) {
+					const int j = js[u];
+					bxv[u] = j >= 0 ? a.fx[j] : 0.0;
+					byv[u] = j >= 0 ? a.fy[j] : 0.0;
+					uxv[u] = (j >= 0 && !x_zero) ? a.vx[j] : 0.0;
+					uyv[u] = (j >= 0 && !x_zero) ? a.vy[j] : 0.0;
 				}
-				else {
-					rx = bx - __fma_rn(T, a.vx[j], qx);
-					ry = by - __fma_rn(T, a.vy[j], qy);
-				}
-				if(fmode != RES_FLOAT_COVER) {
-					// the learned path never reads the FP64 residual (its FP64
-					// fallback recomputes it)
-					a.rx[j] = rx;
-					a.ry[j] = ry;
-				}
-				if(want_b) {
-					v[0] = __fma_rn(bx, bx, v[0]);
-					v[1] = __fma_rn(by, by, v[1]);
-				}
-				v[2] = __fma_rn(rx, rx, v[2]);
-				v[3] = __fma_rn(ry, ry, v[3]);
-				if(fmode != RES_FP64) {
-					const float fx = (float) rx, fy = (float) ry;
-					a.rxf[e] = fx;
-					a.ryf[e] = fy;
-					a.exf[e] = 0.0f;
-					a.eyf[e] = 0.0f;
-					if(want_rz) {
-						v[4] += (double) fx * (iT * (double) fx);
-						v[5] += (double) fy * (iT * (double) fy);
+#pragma unroll
+				for(int u = 0; u < NB; u++) {
+					const int j = js[u];
+					if(j < 0) break;
+					const int e = e0b + u;
+					const double bx = bxv[u], by = byv[u];
+					double rx, ry;
+					if(x_zero) {
+						rx = bx - 0.0;
+						ry = by - 0.0;
 					}
-					Rx += fx * iTf;
-					Ry += fy * iTf;
-				}
-				else if(want_rz) {
-					v[4] += rx * (iT * rx);
-					v[5] += ry * (iT * ry);
+					else {
+						rx = bx - __fma_rn(T, uxv[u], qx);
+						ry = by - __fma_rn(T, uyv[u], qy);
+					}
+					if(fmode != RES_FLOAT_COVER) {
+						// the learned path never reads the FP64 residual (its FP64
+						// fallback recomputes it)
+						a.rx[j] = rx;
+						a.ry[j] = ry;
+					}
+					if(want_b) {
+						v[0] = __fma_rn(bx, bx, v[0]);
+						v[1] = __fma_rn(by, by, v[1]);
+					}
+					v[2] = __fma_rn(rx, rx, v[2]);
+					v[3] = __fma_rn(ry, ry, v[3]);
+					if(fmode != RES_FP64) {
+						const float fx = (float) rx, fy = (float) ry;
+						a.rxf[e] = fx;
+						a.ryf[e] = fy;
+						a.exf[e] = 0.0f;
+						a.eyf[e] = 0.0f;
+						if(want_rz) {
+							v[4] += (double) fx * (iT * (double) fx);
+							v[5] += (double) fy * (iT * (double) fy);
+						}
+						Rx += fx * iTf;
+						Ry += fy * iTf;
+					}
+					else if(want_rz) {
+						v[4] += rx * (iT * rx);
+						v[5] += ry * (iT * ry);
+					}
 				}
 			}
 		}
@@ -1283,10 +1323,10 @@ __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcCtx &tc
 	// the flexible-CG kernel runs every mixed-precision solve (with or
 	// without a network); the plain kernel only FP64 ones
 	if constexpr(LEARNED) {
-		if(!true_residual<RES_FLOAT_COVER>(a, sh, cold != 0, true, false)) return;
+		if(!true_residual<RES_FLOAT_COVER, 4>(a, sh, cold != 0, true, false)) return;
 	}
 	else {
-		if(!true_residual<RES_FP64>(a, sh, cold != 0)) return;
+		if(!true_residual<RES_FP64, (NB >= 4 ? NB : 1)>(a, sh, cold != 0)) return;
 	}
 	pmark(a, sh, PH_START);
 	if(threadIdx.x == 0) {
@@ -1340,7 +1380,7 @@ __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcCtx &tc
 			if(!fcg_iterate(a, sh, tc, max_it < 1000 ? max_it : 1000)) return;
 			refinements++;
 			// x += e and r = b - A x
-			if(!true_residual<RES_FLOAT_COVER>(a, sh, false, false, false, true)) return;
+			if(!true_residual<RES_FLOAT_COVER, 4>(a, sh, false, false, false, true)) return;
 			if(threadIdx.x == 0) {
 				for(int c = 0; c < 2; c++) {
 					sh.rn2[c] = sh.tot[2 + c];
@@ -1356,7 +1396,7 @@ __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcCtx &tc
 		}
 		if(s_fallback || sh.act[0] || sh.act[1]) {
 			// plain FP64 CG from the current x (the residual is in rx, ry)
-			if(!true_residual<RES_FP64>(a, sh, false, false, true)) return;
+			if(!true_residual<RES_FP64, 4>(a, sh, false, false, true)) return;
 			if(threadIdx.x == 0) {
 				for(int c = 0; c < 2; c++) {
 					sh.rn2[c] = sh.tot[2 + c];

@@ -639,12 +639,20 @@ static __device__ __noinline__ void out_range(const bf16 *t0, const float *w, fl
 		const int n = (int) (p / ((long long) L * L));
 		const int r = (int) (p - (long long) n * L * L);
 		const int i = r / L, j = r - (r / L) * L;
-		float acc = w[9 * 16];
-#pragma unroll 3
+		// the nine taps' loads are issued together (one load round trip per
+		// pixel), then the FMAs run in tap and channel order
+		uint4 q0[9], q1[9];
+#pragma unroll
 		for(int t = 0; t < 9; t++) {
 			const int ii = wrap(i + t / 3 - 1, L), jj = wrap(j + t % 3 - 1, L);
 			const uint4 *q = reinterpret_cast<const uint4 *>(t0 + ((size_t) (n * L + ii) * L + jj) * 16);
-			const uint4 u0 = q[0], u1 = q[1];
+			q0[t] = q[0];
+			q1[t] = q[1];
+		}
+		float acc = w[9 * 16];
+#pragma unroll
+		for(int t = 0; t < 9; t++) {
+			const uint4 u0 = q0[t], u1 = q1[t];
 			const uint32_t u[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
 			const float *wt = w + t * 16;
 #pragma unroll
