@@ -27,7 +27,8 @@ from tests.common import (build_inputs, case_from_monolayer, case_from_texts, co
 
 pytestmark = pytest.mark.gpu
 
-ALL = ["polar_dry", "polar_noise", "nematic", "simple", "polar41", "resize", "wet", "wetpolar", "wet_equil", "ch_polar", "ch_nematic", "ch_wet"]
+ALL = ["polar_dry", "polar_noise", "nematic", "simple", "polar41", "resize", "wet", "wetpolar", "wet_equil", "ch_polar",
+       "ch_nematic", "ch_wet", "polar_beta", "wetpolar_beta"]
 EQ = {"wet_equil": 3}
 TOL = 1e-10
 
