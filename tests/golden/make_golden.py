@@ -60,6 +60,10 @@ CASES = {
     "polar_beta": (dict(L=48, n=9, seed=24, **SMALL), dict(DRY_POLAR_S, beta=0.5, J_Q=0.5, zetaQ_inter=0.3, omega=0.004),
                    [0, 1, 5], 34, 0),
     "wetpolar_beta": (dict(L=36, n=4, seed=25, **SMALL), dict(WETPOLAR_S, beta=0.3, omega=0.004), [0, 1, 4], 35, 0),
+    # past the viscous solve's cold restarts: one solve per force evaluation,
+    # a cold start every 100 warm solves (wetmodel) or every 10 (wetpolarmodel)
+    "wet_restart": (dict(L=36, n=4, seed=26, **SMALL), WET_S, [0, 1, 52], 36, 0),
+    "wetpolar_restart": (dict(L=36, n=4, seed=27, **SMALL), WETPOLAR_S, [0, 1, 7], 37, 0),
 }
 
 
