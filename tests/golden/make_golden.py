@@ -56,6 +56,8 @@ CASES = {
     "ch_nematic": (dict(L=48, n=9, seed=22, types=[0, 1, 1, 0, 1, 1, 0, 1, 1], **SMALL),
                    dict(NEMATIC_S, sim_type="FD_CH", dt=0.01), [0, 1, 5], 32, 0),
     "ch_wet": (dict(L=36, n=4, seed=23, **SMALL), dict(WET_S, sim_type="FD_CH", dt=0.01), [0, 1, 3], 33, 0),
+    "ch_simple": (dict(L=36, n=4, seed=28, **SMALL), dict(SIMPLE_S, sim_type="FD_CH", dt=0.01), [0, 1, 5], 38, 0),
+    "ch_wetpolar": (dict(L=36, n=4, seed=29, **SMALL), dict(WETPOLAR_S, sim_type="FD_CH", dt=0.01), [0, 1, 3], 39, 0),
     # the polar model's perimeter term (beta != 0) with adhesion, dry and wet
     "polar_beta": (dict(L=48, n=9, seed=24, **SMALL), dict(DRY_POLAR_S, beta=0.5, J_Q=0.5, zetaQ_inter=0.3, omega=0.004),
                    [0, 1, 5], 34, 0),

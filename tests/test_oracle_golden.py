@@ -13,8 +13,9 @@ import pytest
 from oracle import oracle as orc
 from tests.common import GOLDEN, build_inputs, case_from_texts, compare_to_golden, golden, run
 
-DRY = ["polar_dry", "polar_noise", "nematic", "simple", "polar41", "resize", "ch_polar", "ch_nematic", "polar_beta"]
-WET = ["wet", "wetpolar", "wet_equil", "ch_wet", "wetpolar_beta", "wet_restart", "wetpolar_restart"]
+DRY = ["polar_dry", "polar_noise", "nematic", "simple", "polar41", "resize", "ch_polar", "ch_nematic", "polar_beta", "ch_simple"]
+WET = ["wet", "wetpolar", "wet_equil", "ch_wet", "wetpolar_beta", "wet_restart", "wetpolar_restart",
+       "ch_wetpolar"]
 EQ = {"wet_equil": 3}
 
 
