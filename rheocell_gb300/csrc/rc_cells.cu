@@ -882,7 +882,6 @@ __global__ void __launch_bounds__(BLOCK) cell_kernel_f32(const CellArgs a) {
 	for(int i = 0; i < 12; i++) af[i] = 0.f;
 	int imin[2] = {lx, ly};
 	float area_s = 0.f, area_c = 0.f;
-	const PhaseParams &pu = a.pu;
 	const float J0 = kc[K_J0], hdt = kc[K_HDT];
 	const bool conserved = P.conserved != 0;
 	const float zs = kc[K_ZS], alpha = kc[K_ALPHA], lam = lambda;
@@ -1332,14 +1331,12 @@ void launch_bins(CellDev *cells, const LayerDev *layers, int N, int *bin_count, 
 // kernels return at once when nothing was resized.
 __global__ void repack_scan_kernel(CellDev *cells, int N, DevStatus *st, int *new_start, long long cap) {
 	if(st->resized == 0) return;
-	__shared__ long long s_sum;
 	if(threadIdx.x == 0) {
 		long long acc = 0;
 		for(int i = 0; i < N; i++) {
 			new_start[i] = (int) acc;
 			acc += cells[i].n;
 		}
-		s_sum = acc;
 		st->S = acc;
 		if(acc > cap) {
 			atomicOr(&st->err, ERR_CAPACITY);
