@@ -257,7 +257,7 @@ int rc_set_stream(rc_engine *e, void *cuda_stream);
  * force evaluation (both components, from a cold start, plain FP64 CG at the
  * engine's tolerance) into vx and vy, device arrays of n = rc_site_count(e)
  * doubles in the order of rc_download_phi, without allocating any memory:
- * the solver's work arrays live in one fixed device area of about 2.2 MB per
+ * the solver's work arrays live in one fixed device area of about 1.8 MB per
  * device, so the state must have at most RC_NOALLOC_MAX_UNKNOWNS unknowns
  * and a box of at most RC_NOALLOC_MAX_BOX_SITES sites (RC_ERR_CAPACITY
  * otherwise, nothing launched).  For hosts that may not allocate device

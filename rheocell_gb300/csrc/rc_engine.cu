@@ -1531,9 +1531,10 @@ constexpr size_t NA_OFF_COV_OFF = NA_OFF_BOX + 2 * NA_BOX;
 constexpr size_t NA_OFF_COV_IDX = NA_OFF_COV_OFF + na_round((NA_MAX_BOX_SITES + 1) * sizeof(int));
 constexpr size_t NA_BYTES = NA_OFF_COV_IDX + na_round(NA_MAX_UNKNOWNS * sizeof(int));
 
-// The fixed solver area (about 2.2 MB): status, barrier words, reduction
-// slots, six work vectors, two box-grid sums and the CSR cover lists, laid
-// out at the offsets above.  One area per device, shared by every caller.
+// The fixed solver area (about 1.8 MB): status, barrier words, reduction
+// slots, four work vectors (residual and scaled direction of both
+// components), two box-grid sums and the CSR cover lists, laid out at the
+// offsets above.  One area per device, shared by every caller.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
 
 // Device address of the area, looked up once per device.
