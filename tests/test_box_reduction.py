@@ -1,0 +1,98 @@
+"""The box-grid reduction behind the learned preconditioner, checked on the
+CPU with the operator of the wet models' viscous system.
+
+The reference assembles, per velocity component, the SPD matrix over the
+stacked patch sites (WetModel.cpp:279-347):
+
+    (A v)_j = (xi + eta D_j) v_j - eta sum_{k' in N4(k_j)} sum_{i covers k'} v_i,
+    D_j = sum_{k' in N4(k_j)} n(k'),
+
+with k_j the box site of patch site j and n(k) the number of patches covering
+box site k.  Every unknown at one box site k has the same diagonal T(k), so
+A v = r reduces exactly to the box-grid system
+
+    V - eta W (N4 V) = R,   R[k] = sum_{j at k} r_j / T(k),   W[k] = n(k) / T(k),
+
+for the box sums V = S v, after which v_j = (r_j + eta (N4 V)[k_j]) / T(k_j).
+The learned solve's network approximates R -> V; this file checks that the
+reduction itself is exact, so the preconditioner's only error is the
+network's."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle import oracle as orc
+from rheocell_gb300 import generator as g
+from tests.common import case_from_monolayer, run
+
+sp = pytest.importorskip("scipy.sparse")
+spla = pytest.importorskip("scipy.sparse.linalg")
+
+
+def _n4(F, L):
+    G = F.reshape(L, L)
+    return (np.roll(G, 1, 0) + np.roll(G, -1, 0) + np.roll(G, 1, 1) + np.roll(G, -1, 1)).ravel()
+
+
+def _n4_matrix(L):
+    idx = np.arange(L * L).reshape(L, L)
+    rows, cols = [], []
+    for sh, ax in ((1, 0), (-1, 0), (1, 1), (-1, 1)):
+        rows.append(idx.ravel())
+        cols.append(np.roll(idx, sh, ax).ravel())
+    r, c = np.concatenate(rows), np.concatenate(cols)
+    return sp.csr_matrix((np.ones(r.size), (r, c)), shape=(L * L, L * L))
+
+
+@pytest.fixture(scope="module")
+def system():
+    m = g.make_monolayer(48, 9, seed=41, R=5, lam=1.5, patch=27)
+    keys, m2 = case_from_monolayer(m, dict(g.WET_NEMATIC, R=5, **{"lambda": 1.5}), seed=42)
+    sim, states = run(orc.OracleSim, keys, m2, [0])
+    sim.close()
+    k = np.asarray(states[0]["box_index"], dtype=np.int64)
+    L = m2.L
+    xi, eta = float(keys["friction"]), float(keys["friction_cell"])
+    n = np.bincount(k, minlength=L * L).astype(float)
+    T = xi + eta * _n4(n, L)
+
+    def apply_a(v):
+        return T[k] * v - eta * _n4(np.bincount(k, weights=v, minlength=L * L), L)[k]
+
+    return dict(k=k, L=L, xi=xi, eta=eta, n=n, T=T, A=apply_a)
+
+
+def test_operator_is_symmetric_positive_definite(system):
+    rng = np.random.default_rng(1)
+    A = system["A"]
+    u, v = rng.normal(size=(2, system["k"].size))
+    assert abs(u @ A(v) - v @ A(u)) <= 1e-12 * abs(u @ A(v))
+    for _ in range(4):
+        w = rng.normal(size=system["k"].size)
+        assert w @ A(w) > 0
+
+
+def test_box_reduction_solves_the_patch_system_exactly(system):
+    k, L, eta, n, T, A = (system[x] for x in ("k", "L", "eta", "n", "T", "A"))
+    rng = np.random.default_rng(2)
+    r = rng.normal(size=k.size)
+    R = np.bincount(k, weights=r / T[k], minlength=L * L)
+    W = n / T
+    M = sp.identity(L * L, format="csr") - eta * sp.diags(W) @ _n4_matrix(L)
+    V = spla.spsolve(M.tocsc(), R)
+    v = (r + eta * _n4(V, L)[k]) / T[k]
+    assert np.max(np.abs(A(v) - r)) <= 1e-11 * np.max(np.abs(r))
+    assert np.allclose(np.bincount(k, weights=v, minlength=L * L), V, rtol=0, atol=1e-11 * np.max(np.abs(V)))
+
+
+def test_box_system_is_screened(system):
+    """On a confluent monolayer the coupling eta W N4 of the box system has
+    spectral radius below one: the system is a screened Poisson problem
+    (Jacobi on it converges), whose inverse is short-ranged -- what a
+    three-level network with 3x3 convolutions can represent."""
+    L, eta, n, T = (system[x] for x in ("L", "eta", "n", "T"))
+    W = n / T
+    B = eta * sp.diags(W) @ _n4_matrix(L)
+    rho = abs(spla.eigs(B, k=1, which="LM", return_eigenvectors=False)[0])
+    assert rho < 1.0
