@@ -15,6 +15,7 @@ reference sources).
 """
 from __future__ import annotations
 
+import hashlib
 import json
 import os
 import shutil
@@ -67,6 +68,63 @@ CASES = {
     "wet_restart": (dict(L=36, n=4, seed=26, **SMALL), WET_S, [0, 1, 52], 36, 0),
     "wetpolar_restart": (dict(L=36, n=4, seed=27, **SMALL), WETPOLAR_S, [0, 1, 7], 37, 0),
 }
+
+
+# Full-size cases stored compactly: the project generator regenerates the
+# configuration (its text is checked against the recorded SHA-256), per-cell
+# scalars are stored as they are, and per-site arrays as SHA-256 digests of
+# their bytes -- the dry oracle must reproduce them bit for bit -- with their
+# sums of squares to size a mismatch.
+# name: (monolayer kwargs, params, dump steps, seed)
+HASHED = {
+    # the 140x140 / 100-cell dry polar workload on 41x41 patches, over 100 steps
+    "dry140_100": (dict(L=140, n=100, seed=1), g.DRY_POLAR, [0, 1, 10, 100], 1),
+}
+
+
+def sha256_of(a, dtype) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a, dtype=dtype).tobytes()).hexdigest()
+
+
+def conf_text(m) -> str:
+    d = tempfile.mkdtemp(prefix="rc_golden_")
+    try:
+        g.write_conf(os.path.join(d, "start_conf.dat"), m)
+        return open(os.path.join(d, "start_conf.dat")).read()
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+
+
+def record_hashed(name):
+    mkw, params, steps, seed = HASHED[name]
+    m = monolayer(mkw)
+    d = tempfile.mkdtemp(prefix="rc_golden_")
+    try:
+        g.write_case(d, m, params, steps=max(steps), seed=seed)
+        recs = refdump.run_reference(d, steps, flavour="exact")
+        conf = open(os.path.join(d, "start_conf.dat")).read()
+        topo = open(os.path.join(d, "topology.top")).read()
+        inp = open(os.path.join(d, "input")).read()
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    assert conf == conf_text(monolayer(mkw))
+    out = {"monolayer": np.array(json.dumps(mkw)), "conf_sha256": np.array(hashlib.sha256(conf.encode()).hexdigest()),
+           "topology": np.array(topo), "input": np.array(inp),
+           "steps": np.array([r["step"] for r in recs], dtype=np.int64)}
+    for r in recs:
+        s = r["step"]
+        for k in refdump.CELL_I32 + refdump.CELL_F64:
+            out["s%d_%s" % (s, k)] = r[k]
+        if s > 0:
+            out["s%d_phi_sha256" % s] = np.array(sha256_of(r["phi"], "<f8"))
+            out["s%d_phi_sumsq" % s] = np.array(float(np.sum(r["phi"] ** 2)))
+    last = recs[-1]
+    for k in ("vx", "vy", "mu"):
+        out["last_%s_sha256" % k] = np.array(sha256_of(last[k], "<f8"))
+        out["last_%s_sumsq" % k] = np.array(float(np.sum(last[k] ** 2)))
+    out["last_map_sha256"] = np.array(sha256_of(last["map"], "<i8"))
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    return recs
 
 
 def monolayer(kw):
@@ -166,6 +224,12 @@ def main():
     if not refdump.have_reference("exact"):
         subprocess.check_call(["make", "-C", os.path.join(ROOT, "oracle"), "-j8"])
     only = sys.argv[1:]  # optional: record only these cases
+    for name in HASHED:
+        if only and name not in only:
+            continue
+        recs = record_hashed(name)
+        print("%-12s steps %s  cells %d  %.0f KB" % (name, [r["step"] for r in recs], recs[0]["N"],
+                                                  os.path.getsize(os.path.join(HERE, name + ".npz")) / 1024))
     for name in CASES:
         if only and name not in only:
             continue

@@ -6,6 +6,8 @@ products and operator rows in a different order than the reference's Eigen
 (shim) CG, so they are held to 1e-12 relative."""
 import json
 import os
+import shutil
+import tempfile
 
 import numpy as np
 import pytest
@@ -63,3 +65,48 @@ def test_overlap_error_like_reference():
     p, cells = build_inputs(keys, m2)
     with pytest.raises(RuntimeError, match="overlap"):
         orc.OracleSim(p, m2.L, cells)
+
+
+# full-size cases whose per-site arrays are stored as digests (make_golden.HASHED)
+HASHED = ["dry140_100"]
+
+
+@pytest.mark.parametrize("name", HASHED)
+def test_oracle_matches_reference_bitwise_full_size(name):
+    import hashlib
+
+    from rheocell_gb300 import generator as g
+    from tests.common import CELL_KEYS
+    gd = golden(name)
+    mkw = json.loads(str(gd["monolayer"]))
+    m = g.make_monolayer(mkw.pop("L"), mkw.pop("n"), mkw.pop("seed"), **mkw)
+    d = tempfile.mkdtemp(prefix="rc_case_")
+    try:
+        g.write_conf(os.path.join(d, "start_conf.dat"), m)
+        conf = open(os.path.join(d, "start_conf.dat")).read()
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    # the generator still writes the configuration the reference ran on
+    assert hashlib.sha256(conf.encode()).hexdigest() == str(gd["conf_sha256"])
+    keys, m2 = case_from_texts(str(gd["input"]), conf, str(gd["topology"]))
+    steps = [int(s) for s in gd["steps"]]
+    _, states = run(orc.OracleSim, keys, m2, steps)
+
+    def digest(a, dtype):
+        return hashlib.sha256(np.ascontiguousarray(a, dtype=dtype).tobytes()).hexdigest()
+
+    bad = {}
+    for s in steps:
+        st = states[s]
+        for k, sk in CELL_KEYS.items():
+            if not np.array_equal(np.asarray(st[sk]), gd["s%d_%s" % (s, k)]):
+                bad[(s, k)] = float(np.max(np.abs(np.asarray(st[sk], float) - gd["s%d_%s" % (s, k)])))
+        if s > 0 and digest(st["phi"], "<f8") != str(gd["s%d_phi_sha256" % s]):
+            bad[(s, "phi")] = (float(np.sum(st["phi"] ** 2)), float(gd["s%d_phi_sumsq" % s]))
+    last = states[steps[-1]]
+    for k in ("vx", "vy", "mu"):
+        if digest(last[k], "<f8") != str(gd["last_%s_sha256" % k]):
+            bad[("last", k)] = (float(np.sum(last[k] ** 2)), float(gd["last_%s_sumsq" % k]))
+    if digest(last["box_index"], "<i8") != str(gd["last_map_sha256"]):
+        bad[("last", "map")] = "differs"
+    assert not bad, bad
