@@ -148,7 +148,7 @@ typedef struct rc_step_stats {
 
 typedef struct rc_engine rc_engine;
 
-/* Version of this ABI (RC_ABI_VERSION). */
+/* Version of this ABI (RC_ABI_VERSION).  No counterpart in the reference. */
 int rc_abi_version(void);
 
 /*
@@ -169,11 +169,15 @@ int rc_create(const rc_params *params, const rc_box *box, int n_cells,
  * layers share `params`.  Batches are provided for dry evaluations
  * (friction_cell = 0 in both phases); downloads and uploads address the cells
  * in the same layer-major order.  A monolayer simulation is a batch of one.
+ * No counterpart in the reference, which runs one monolayer per process
+ * (src/rheoCell.cpp:13-29); each layer here is what one such process reads
+ * (SimBackend::read_next_configuration, src/Backends/SimBackend.cpp:220-314).
  */
 int rc_batch_create(const rc_params *params, int n_layers, const rc_box *boxes, const int *n_cells_per_layer,
                     const rc_cell_host *cells, const unsigned long long *rng_states, int device, rc_engine **out);
 
-/* Number of monolayers the engine advances. */
+/* Number of monolayers the engine advances.  No counterpart in the reference
+ * (one monolayer per process there). */
 int rc_layer_count(const rc_engine *e);
 
 /*
@@ -188,12 +192,16 @@ int rc_step(rc_engine *e, int n_steps, rc_step_stats *stats);
  * Errors raised on the device are reported by the next rc_wait.  Patch sizes
  * are not re-examined between the steps of one call, so a patch that grows
  * past the engine's current shared-memory sizing is reported as
- * RC_ERR_CAPACITY; rc_step does that check every 16 steps.
+ * RC_ERR_CAPACITY; rc_step does that check every 16 steps.  The same steps
+ * as rc_step (FD_CPUBackend::sim_step, src/Backends/FD_CPUBackend.cpp:134-160);
+ * the reference has no asynchronous form.
  */
 int rc_step_async(rc_engine *e, int n_steps);
 
 /* Wait for enqueued work; report device errors and the statistics
- * accumulated since the last rc_wait / rc_step (stats may be NULL). */
+ * accumulated since the last rc_wait / rc_step (stats may be NULL).  No
+ * counterpart in the reference, whose sim_step returns when the step is done
+ * (src/Managers/SimManager.cpp:148-159). */
 int rc_wait(rc_engine *e, rc_step_stats *stats);
 
 /*
@@ -202,7 +210,8 @@ int rc_wait(rc_engine *e, rc_step_stats *stats);
  */
 int rc_set_phase(rc_engine *e, int active);
 
-/* Number of cells and, if the pointers are non-NULL, each patch's size. */
+/* Number of cells and, if the pointers are non-NULL, each patch's size:
+ * BaseField::LsubX / LsubY (src/Fields/BaseField.h:198-199). */
 int rc_get_sizes(const rc_engine *e, int *n_cells, int *lsub_x, int *lsub_y);
 
 /*
@@ -249,7 +258,8 @@ int rc_upload_phi(rc_engine *e, const double *phi, long long n);
 int rc_set_timing(rc_engine *e, int enable);
 int rc_timers(rc_engine *e, double *ms, long long *launches, int reset);
 
-/* Issue the engine's work on this cudaStream_t (NULL: the engine's own). */
+/* Issue the engine's work on this cudaStream_t (NULL: the engine's own).
+ * No counterpart in the reference (CPU only). */
 int rc_set_stream(rc_engine *e, void *cuda_stream);
 
 /*
@@ -309,8 +319,13 @@ int rc_set_cell_threads(rc_engine *e, int threads);
 
 /* rc_unet_forward_tc: the network's forward pass as the solve runs it
  * (BF16 activations, tensor-core layers, FP32 first and last layers);
- * input [batch][L][L][2], output [batch][L][L]. */
+ * input [batch][L][L][2], output [batch][L][L].  No counterpart in the
+ * reference (the learned preconditioner is this engine's own). */
 int rc_unet_forward_tc(int L, int batch, const double *params, const double *input, double *output, int device);
+/* rc_unet_loss_grad: one training pass of the network (FP32 forward,
+ * relative-L2 loss against target [batch][L][L], backward): the loss, the
+ * gradient of all RC_UNET_PARAMS parameters and the output.  No counterpart
+ * in the reference. */
 int rc_unet_loss_grad(int L, int batch, const double *params, const double *input, const double *target,
                       double *loss, double *grad, double *output, int device);
 
@@ -383,7 +398,7 @@ int rc_set_solver(rc_engine *e, int solver);
  * gather, first layer, tensor-core layers at levels 0, 1, 2, last layer,
  * preconditioned residual, flexible-CG phases A, B, C, everything else,
  * then (within the tensor-core layers) weight staging, operand staging,
- * MMA issue and completion, epilogue.
+ * MMA issue and completion, epilogue.  No counterpart in the reference.
  */
 int rc_solver_profile(rc_engine *e, int enable, double *ms, int n);
 
@@ -413,12 +428,19 @@ int rc_observe_field(rc_engine *e, int kind, int layer, int only_type, int size_
                      double *coarse_x, double *coarse_y);
 int rc_observe_cells(rc_engine *e, double *cell_obs, double *layer_obs);
 
-/* Sites (sum of LsubX*LsubY) in the current configuration. */
+/* Sites (sum of LsubX*LsubY) in the current configuration: the reference's
+ * stacked unknown count size_rows (src/Interactions/WetModel.cpp:203-209). */
 long long rc_site_count(const rc_engine *e);
 
-/* Message of the last failure on this engine (or of the last failed create). */
+/* Message of the last failure on this engine (or of the last failed create):
+ * the text the reference's RCexception carries to main
+ * (src/rheoCell.cpp:40-43). */
 const char *rc_last_error(const rc_engine *e);
 
+/* Release the engine's device memory, stream and graphs: the backend's
+ * destruction (SimBackend::~SimBackend, src/Backends/SimBackend.cpp:37-39;
+ * FD_CPUBackend::~FD_CPUBackend, src/Backends/FD_CPUBackend.cpp:9).  NULL is
+ * a no-op. */
 void rc_destroy(rc_engine *e);
 
 #ifdef __cplusplus
