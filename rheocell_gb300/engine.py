@@ -188,7 +188,8 @@ class Engine:
 
     def set_params(self, p: np.ndarray) -> None:
         p = np.ascontiguousarray(p, dtype=np.float64)
-        assert p.size == abi.RC_UNET_PARAMS
+        if p.size != abi.RC_UNET_PARAMS:
+            raise ValueError("the network has %d parameters, got %d" % (abi.RC_UNET_PARAMS, p.size))
         self._check(self._lib.rc_learned_set_params(self.h, p.ctypes.data_as(abi.DP)), "rc_learned_set_params")
 
     # --- tile-shape autotuning of the FP32 cell kernel ----------------------------
