@@ -95,3 +95,28 @@ def test_read_input(tmp_path):
     p.write_text("a = 1 # c\n# full\nb=  x y \n a = 2\n")
     k = host.read_input(str(p), {"c": 3})
     assert k == {"a": "2", "b": "x y", "c": "3"}
+
+
+def test_bench_workloads_start_within_the_overlap_limit():
+    """Every bench workload's initial condition keeps at most 20 patches on a
+    box site: the wet models abort beyond that (store_max_size,
+    WetModel.cpp:58, :475-480), and the 123 % area fraction of the wet
+    configurations is well inside it (mean coverage n P^2 / L^2 = 10.26)."""
+    import bench
+    from rheocell_gb300 import generator as gen
+
+    def coverage(m):
+        L = m.L
+        cnt = np.zeros(L * L, np.int64)
+        for c in m.cells:
+            cx, cy = c.corner % L, c.corner // L
+            idx = (((cy + np.arange(c.ly)) % L)[:, None] * L + ((cx + np.arange(c.lx)) % L)[None, :]).ravel()
+            cnt += np.bincount(idx, minlength=L * L)
+        return cnt
+
+    for L, n in ((140, 100), (256, 400), (512, 1600), (1024, 6400)):
+        cnt = coverage(gen.make_monolayer(L, n, seed=1))
+        assert cnt.max() <= 20
+        assert cnt.sum() == n * 41 * 41
+    for L, n, seed in bench.ensemble_members():
+        assert coverage(gen.make_monolayer(L, n, seed=seed)).max() <= 20
