@@ -96,3 +96,60 @@ def test_box_system_is_screened(system):
     B = eta * sp.diags(W) @ _n4_matrix(L)
     rho = abs(spla.eigs(B, k=1, which="LM", return_eigenvectors=False)[0])
     assert rho < 1.0
+
+
+def test_scaled_direction_cg_follows_jacobi_cg(system):
+    """The plain FP64 device solve carries q = T p in place of the Jacobi-CG
+    direction p (T is constant on a box site) and forms p.Ap from box sums:
+    p.Ap = sum_k (1/T) sum q^2 - eta sum_k P(k) N4(P)(k) with P = S p, Ap =
+    q - eta N4(P), x += (alpha / T) q, r.z = sum (1/T) r^2, q = r + beta q.
+    Restated here next to Eigen's Jacobi-CG recurrence (the reference's
+    solver, WetModel.cpp:361-376): the iterates agree to rounding."""
+    k, L, eta, T, A = (system[x] for x in ("k", "L", "eta", "T", "A"))
+    Tj = T[k]
+    rng = np.random.default_rng(3)
+    b = rng.normal(size=k.size)
+
+    # Eigen's ConjugateGradient with the diagonal preconditioner, from x = 0
+    x1 = np.zeros_like(b)
+    r = b - A(x1)
+    p = r / Tj
+    rz = r @ p
+    xs1 = []
+    for _ in range(25):
+        Ap = A(p)
+        alpha = rz / (p @ Ap)
+        x1 += alpha * p
+        r -= alpha * Ap
+        z = r / Tj
+        rz_new = r @ z
+        p = z + (rz_new / rz) * p
+        rz = rz_new
+        xs1.append(x1.copy())
+
+    # the device's form: scaled direction, box sums, no Ap vector
+    x2 = np.zeros_like(b)
+    r = b.copy()
+    q = np.zeros_like(b)
+    rz = np.sum(r * r / Tj)
+    beta = 0.0
+    xs2 = []
+    for it in range(25):
+        q = r + beta * q if it else r.copy()                      # phase A
+        P = np.bincount(k, weights=q, minlength=L * L) / T
+        w = np.sum(q * q / Tj)
+        G = P.reshape(L, L)                                       # phase B
+        s = np.sum(G * (np.roll(G, -1, 0) + np.roll(G, -1, 1)))
+        alpha = rz / (w - 2 * eta * s)
+        Ap = q - eta * _n4(P, L)[k]                               # phase C
+        x2 += (alpha / Tj) * q
+        r -= alpha * Ap
+        rz_new = np.sum(r * r / Tj)
+        beta = rz_new / rz
+        rz = rz_new
+        xs2.append(x2.copy())
+
+    for a, c in zip(xs1, xs2):
+        assert np.max(np.abs(a - c)) <= 1e-12 * np.max(np.abs(a))
+    # and it converges on this operator (a random right-hand side, from zero)
+    assert np.linalg.norm(b - A(xs2[-1])) < 1e-4 * np.linalg.norm(b)
