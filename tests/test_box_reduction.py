@@ -153,3 +153,64 @@ def test_scaled_direction_cg_follows_jacobi_cg(system):
         assert np.max(np.abs(a - c)) <= 1e-12 * np.max(np.abs(a))
     # and it converges on this operator (a random right-hand side, from zero)
     assert np.linalg.norm(b - A(xs2[-1])) < 1e-4 * np.linalg.norm(b)
+
+
+def _fcg(A, b, precond, iters):
+    """Flexible CG (Notay's FCG(1)) as the learned solve's inner iterations
+    run it: beta = -z.Ap_old / p_old.Ap_old, alpha = r.z / p.Ap."""
+    x = np.zeros_like(b)
+    r = b.copy()
+    p = Ap = None
+    xs, res = [], []
+    for _ in range(iters):
+        z = precond(r)
+        rz = r @ z
+        if p is None:
+            p = z.copy()
+        else:
+            p = z + (-(z @ Ap) / pap) * p
+        Ap = A(p)
+        pap = p @ Ap
+        alpha = rz / pap
+        x += alpha * p
+        r -= alpha * Ap
+        xs.append(x.copy())
+        res.append(np.linalg.norm(r) / np.linalg.norm(b))
+    return xs, res
+
+
+def test_flexible_cg_with_jacobi_is_jacobi_cg_and_exact_box_solve_converges_at_once(system):
+    """With a fixed SPD preconditioner FCG(1) is preconditioned CG: with
+    z = r / T its iterates are Jacobi CG's (the mixed-precision solve's inner
+    iterations without a network).  With the exact box-grid solve as the
+    preconditioner (what the network approximates) one iteration reaches
+    rounding level."""
+    k, L, eta, n, T, A = (system[x] for x in ("k", "L", "eta", "n", "T", "A"))
+    Tj = T[k]
+    b = np.random.default_rng(4).normal(size=k.size)
+
+    xs_f, _ = _fcg(A, b, lambda r: r / Tj, 20)
+    x = np.zeros_like(b)
+    r = b.copy()
+    p = r / Tj
+    rz = r @ p
+    for it in range(20):
+        Ap = A(p)
+        alpha = rz / (p @ Ap)
+        x += alpha * p
+        r -= alpha * Ap
+        z = r / Tj
+        rz_new = r @ z
+        p = z + (rz_new / rz) * p
+        rz = rz_new
+        assert np.max(np.abs(xs_f[it] - x)) <= 1e-9 * np.max(np.abs(x))
+
+    M = (sp.identity(L * L, format="csr") - eta * sp.diags(n / T) @ _n4_matrix(L)).tocsc()
+    lu = spla.splu(M)
+
+    def box_solve(r):
+        V = lu.solve(np.bincount(k, weights=r / Tj, minlength=L * L))
+        return (r + eta * _n4(V, L)[k]) / Tj
+
+    _, res = _fcg(A, b, box_solve, 1)
+    assert res[0] < 1e-12
