@@ -214,3 +214,45 @@ def test_flexible_cg_with_jacobi_is_jacobi_cg_and_exact_box_solve_converges_at_o
 
     _, res = _fcg(A, b, box_solve, 1)
     assert res[0] < 1e-12
+
+
+def test_fp32_inner_iterations_in_fp64_refinement_reach_the_fp64_tolerance(system):
+    """The mixed-precision solve: FCG(1) in FP32 on the correction A e = r
+    stopped at 1e-4 of |r|, then x += e and the true residual in FP64, until
+    |r| < 1e-8 |b| (the reference's CGtolerance).  Restated in numpy with
+    float32 inner arithmetic, it reaches the FP64 tolerance in a few sweeps
+    although FP32 alone cannot resolve 1e-8."""
+    k, L, eta, T, A = (system[x] for x in ("k", "L", "eta", "T", "A"))
+    Tj = T[k]
+    f32 = np.float32
+    b = np.random.default_rng(5).normal(size=k.size)
+
+    def a32(v):
+        Tj32 = Tj.astype(f32)
+        P = np.bincount(k, weights=v, minlength=L * L).astype(f32)
+        return (Tj32 * v - f32(eta) * _n4(P, L)[k].astype(f32)).astype(f32)
+
+    x = np.zeros_like(b)
+    r = b - A(x)
+    sweeps = 0
+    while np.linalg.norm(r) >= 1e-8 * np.linalg.norm(b):
+        sweeps += 1
+        assert sweeps <= 6
+        rf = r.astype(f32)
+        goal = f32(1e-4) * np.linalg.norm(rf)
+        e = np.zeros_like(rf)
+        p = Ap = None
+        for _ in range(500):
+            z = (rf / Tj.astype(f32)).astype(f32)
+            rz = rf @ z
+            p = z.copy() if p is None else (z + (-(z @ Ap) / pap) * p).astype(f32)
+            Ap = a32(p)
+            pap = p @ Ap
+            alpha = rz / pap
+            e = (e + alpha * p).astype(f32)
+            rf = (rf - alpha * Ap).astype(f32)
+            if np.linalg.norm(rf) < goal:
+                break
+        x += e.astype(np.float64)
+        r = b - A(x)
+    assert 2 <= sweeps <= 4
