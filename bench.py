@@ -208,6 +208,7 @@ def prepare_learned(args, eng, lib):
     eng.set_solver(abi.RC_SOLVER_LEARNED)
     solve_stage(eng, lib, 1, flush)
     learned_ms, learned_it, learned_res = solve_stage(eng, lib, k, flush)
+    accuracy = velocity_error(eng)
     # per-phase breakdown of the learned solve (device clock, one block)
     phases = None
     if args.solver_phases:
@@ -225,7 +226,29 @@ def prepare_learned(args, eng, lib):
                                   "speedup": plain_ms / learned_ms if learned_ms > 0 else None},
             "iterations_per_solve": {"plain_fp64_cg": plain_it, "learned_fcg_inner": learned_it},
             "max_rel_residual": {"plain_fp64_cg": plain_res, "learned_fcg": learned_res},
-            "steps_each": k, "phases_ms_per_step": phases}
+            "steps_each": k, "phases_ms_per_step": phases,
+            "velocity_rel_err_vs_fp64": accuracy}
+
+
+def velocity_error(eng):
+    """The last evaluation's viscous system solved again from a cold start
+    by the plain FP64 CG and by the learned flexible CG (rc_viscous_resolve,
+    device arrays, engine state untouched): max |v_learned - v_fp64| /
+    max |v_fp64| per component, with both solves' iterations and residuals."""
+    import torch
+    from rheocell_gb300 import abi
+    S = eng.site_count()
+    v = [torch.zeros(S, dtype=torch.float64, device="cuda") for _ in range(4)]
+    torch.cuda.synchronize()
+    sp = eng.resolve(abi.RC_SOLVER_PLAIN, v[0].data_ptr(), v[1].data_ptr())
+    sl = eng.resolve(abi.RC_SOLVER_LEARNED, v[2].data_ptr(), v[3].data_ptr())
+    err = [float((v[2 + c] - v[c]).abs().max() / v[c].abs().max().clamp_min(1e-300)) for c in range(2)]
+    return {"vx": err[0], "vy": err[1], "max": max(err),
+            "how": "same right-hand side (last evaluation of the timed run), cold-start solves, "
+                   "plain FP64 CG vs learned flexible CG, device velocities of all %d unknowns" % S,
+            "plain_fp64": {"iterations": sp.cg_iterations, "max_rel_residual": sp.cg_max_rel_residual},
+            "learned": {"inner_iterations": sl.cg_iterations, "refinements": sl.refinements,
+                        "fallbacks": sl.fallbacks, "max_rel_residual": sl.cg_max_rel_residual}}
 
 
 def make_engine(name, prec, dev):

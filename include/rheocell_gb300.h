@@ -144,6 +144,9 @@ typedef struct rc_step_stats {
 	int resized_cells;       /* patches that changed size                     */
 	int refinements;         /* mixed precision: outer refinement sweeps      */
 	long long kernel_launches; /* engine kernels launched by the call         */
+	int fallbacks;           /* mixed/learned solves whose refinement stalled
+	                            and that the plain FP64 CG finished           */
+	int reserved;
 } rc_step_stats;
 
 typedef struct rc_engine rc_engine;
@@ -272,12 +275,16 @@ int rc_set_stream(rc_engine *e, void *cuda_stream);
  * and a box of at most RC_NOALLOC_MAX_BOX_SITES sites (RC_ERR_CAPACITY
  * otherwise, nothing launched).  For hosts that may not allocate device
  * memory inside their time loop.  The first call on a device looks the area
- * up (cudaGetSymbolAddress); make that call before any stream capture.  The
- * area is shared: calls on one device must not overlap in time (from any
+ * up (cudaGetSymbolAddress); with CUDA's lazy module loading (the default)
+ * that lookup may load the library's device code and with it the area, i.e.
+ * the first call per device can allocate: make it during set-up, before the
+ * time loop and before any stream capture.  Later calls allocate nothing.
+ * The area is shared: calls on one device must not overlap in time (from any
  * engine or stream), or they race.  Runs on the engine's stream and returns
- * when the solve is done; `iterations` (may be NULL) receives the CG
- * iterations of both components.  RC_ERR_UNSUPPORTED if the last evaluation
- * had no viscous solve.
+ * when the solve is done; it does not wait for work the caller has pending
+ * on vx and vy in other streams (finish or order that first).  `iterations`
+ * (may be NULL) receives the CG iterations of both components.
+ * RC_ERR_UNSUPPORTED if the last evaluation had no viscous solve.
  */
 #define RC_NOALLOC_MAX_UNKNOWNS 32768
 #define RC_NOALLOC_MAX_BOX_SITES 16384
@@ -389,6 +396,44 @@ int rc_learned_train(rc_engine *e, const rc_train_options *options, rc_train_rep
 int rc_learned_get_params(rc_engine *e, double *params);
 int rc_learned_set_params(rc_engine *e, const double *params);
 int rc_set_solver(rc_engine *e, int solver);
+
+/*
+ * rc_viscous_resolve: run the viscous solve of the last force evaluation
+ * again, from a cold start, with `solver` (RC_SOLVER_PLAIN: the engine's
+ * precision -- FP64 CG for RC_PRECISION_DOUBLE; or a learned solver, which
+ * needs parameters) into vx and vy, device arrays of n = rc_site_count(e)
+ * doubles in the order of rc_download_phi.  The engine's velocities,
+ * warm-start schedule and counters are unchanged, so solvers can be compared
+ * on one right-hand side without advancing the simulation.  `stats` (may be
+ * NULL) receives the solve's counters.  RC_ERR_UNSUPPORTED if the last
+ * evaluation had no viscous solve.  Synchronises.  No counterpart in the
+ * reference (the closest is calling Eigen's solve() twice,
+ * WetModel.cpp:364-375).
+ */
+int rc_viscous_resolve(rc_engine *e, int solver, double *vx, double *vy, long long n, rc_step_stats *stats);
+
+/*
+ * rc_set_cg_limits: cap every viscous solve at max_iterations iterations
+ * per component (0: Eigen's default, twice the number of unknowns,
+ * WetModel.cpp:361-376 with Eigen's ConjugateGradient defaults).  With
+ * fail_on_no_convergence != 0, a solve that stops at the cap with its
+ * residual above the tolerance makes rc_step fail with RC_ERR_CG (the
+ * reference, like Eigen, carries on silently; it never reads
+ * solverCG.info()).
+ */
+int rc_set_cg_limits(rc_engine *e, long long max_iterations, int fail_on_no_convergence);
+
+/*
+ * Test hook of the solve's failure detection (no counterpart in the
+ * reference).  spin_limit: polls of a grid-barrier wait before it gives up
+ * (0: the default, about 1-2 s).  unreachable != 0 makes the first grid
+ * barrier of every later solve wait for one arrival more than the grid has
+ * blocks, which never comes: every block gives up after spin_limit polls,
+ * the kernel returns, and rc_step fails with RC_ERR_CG ("grid barrier timed
+ * out") with the CUDA context intact.  The engine's state is then undefined;
+ * destroy it.
+ */
+int rc_test_barrier_timeout(rc_engine *e, long long spin_limit, int unreachable);
 
 /*
  * Diagnostic timers of the learned solve, read on the device clock by one

@@ -85,17 +85,20 @@ static void dump_state(FILE *f, long long step) {
 }
 
 int main(int argc, char *argv[]) {
-	if(argc < 5) {
+	const std::string mode = argc > 1 ? argv[1] : "";
+	if(argc < (mode == "time" ? 4 : 5)) {
 		fprintf(stderr, "usage: %s dump <out> <steps,csv> <input> [k=v...] | time <n> <input> [k=v...]\n", argv[0]);
 		return 2;
 	}
-	const std::string mode = argv[1];
 	try {
 		Logger::init();
 		TimingManager::init();
 
+		// the parser takes (program, input file, key=value ...): the argument
+		// before the input file stands in for the program name
+		const int skip = mode == "time" ? 2 : 3;
 		input_file input(true);
-		input.init_from_command_line_args(argc - 3, argv + 3);
+		input.init_from_command_line_args(argc - skip, argv + skip);
 
 		long long steps = 0, eq_steps = 0;
 		int seed = 1;

@@ -95,6 +95,7 @@ class RcStepStats(C.Structure):
         ("steps_done", C.c_longlong), ("cg_solves", C.c_int), ("cg_iterations", C.c_int),
         ("cg_max_iterations", C.c_int), ("cg_max_rel_residual", C.c_double),
         ("resized_cells", C.c_int), ("refinements", C.c_int), ("kernel_launches", C.c_longlong),
+        ("fallbacks", C.c_int), ("reserved", C.c_int),
     ]
 
 
@@ -183,6 +184,12 @@ def declare(lib: C.CDLL, prefix: str) -> C.CDLL:
         lib.rc_unet_loss_grad.restype = C.c_int
         lib.rc_viscous_resolve_noalloc.argtypes = [vp, vp, vp, C.c_longlong, C.POINTER(C.c_int)]
         lib.rc_viscous_resolve_noalloc.restype = C.c_int
+        lib.rc_viscous_resolve.argtypes = [vp, C.c_int, vp, vp, C.c_longlong, C.POINTER(RcStepStats)]
+        lib.rc_viscous_resolve.restype = C.c_int
+        lib.rc_set_cg_limits.argtypes = [vp, C.c_longlong, C.c_int]
+        lib.rc_set_cg_limits.restype = C.c_int
+        lib.rc_test_barrier_timeout.argtypes = [vp, C.c_longlong, C.c_int]
+        lib.rc_test_barrier_timeout.restype = C.c_int
         lib.rc_autotune.argtypes = [vp, C.c_int, C.POINTER(RcAutotuneReport)]
         lib.rc_autotune.restype = C.c_int
         lib.rc_set_cell_threads.argtypes = [vp, C.c_int]
@@ -200,7 +207,8 @@ def declare(lib: C.CDLL, prefix: str) -> C.CDLL:
 # Every symbol the header declares (checked by the CPU test suite).
 EXPORTED = ["rc_abi_version", "rc_create", "rc_batch_create", "rc_layer_count", "rc_viscous_resolve_noalloc", "rc_unet_loss_grad", "rc_unet_forward_tc",
             "rc_learned_harvest", "rc_learned_harvested", "rc_learned_train", "rc_learned_get_params",
-            "rc_learned_set_params", "rc_set_solver", "rc_solver_profile",
+            "rc_learned_set_params", "rc_set_solver", "rc_solver_profile", "rc_viscous_resolve",
+            "rc_set_cg_limits", "rc_test_barrier_timeout",
             "rc_observe_field", "rc_observe_cells", "rc_autotune", "rc_set_cell_threads", "rc_step", "rc_step_async", "rc_wait", "rc_set_phase",
             "rc_get_sizes", "rc_download", "rc_upload", "rc_download_phi", "rc_upload_phi", "rc_set_stream",
             "rc_set_timing", "rc_timers", "rc_site_count", "rc_last_error", "rc_destroy"]

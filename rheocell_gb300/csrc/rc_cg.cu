@@ -73,7 +73,8 @@ __device__ __forceinline__ bool grid_reduce(const CGArgs &a, CGShared &sh, int n
 		const unsigned e = sh.epoch;
 		double *part = a.partials + (size_t) (e & 1u) * 8 * nb;
 		for(int i = 0; i < nv; i++) part[(size_t) i * nb + blockIdx.x] = v[i];
-		const unsigned target = (e + 1u) * nb;
+		const unsigned target = (e + 1u) * nb + (e == 0u ? (unsigned) a.barrier_extra : 0u);
+		const long long limit = a.spin_limit > 0 ? a.spin_limit : BARRIER_SPIN_LIMIT;
 		__threadfence();
 		atomicAdd(&a.bar[0], 1u);
 		long long spins = 0;
@@ -81,7 +82,7 @@ __device__ __forceinline__ bool grid_reduce(const CGArgs &a, CGShared &sh, int n
 		while(true) {
 			asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(c) : "l"(a.bar) : "memory");
 			if((int) (c - target) >= 0) break;
-			if(++spins > BARRIER_SPIN_LIMIT) {
+			if(++spins > limit) {
 				atomicOr(&a.st->err, ERR_BARRIER);
 				sh.fail = 1;
 				break;
@@ -688,6 +689,13 @@ __device__ __forceinline__ bool cg_iterate(const CGArgs &a, CGShared &sh, const 
 				sh.rn2[c] = sh.tot[c];
 				if(sh.rn2[c] < sh.thr[c]) {
 					sh.act[c] = 0;
+					continue;
+				}
+				// a NaN/Inf right-hand side: stop now (Eigen would run to its
+				// iteration cap, twice the unknowns) and report it
+				if(!isfinite(sh.rn2[c])) {
+					sh.act[c] = 0;
+					atomicOr(&a.st->err, ERR_NONFINITE);
 					continue;
 				}
 				const double rz_new = sh.tot[2 + c];
@@ -1351,8 +1359,8 @@ __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcCtx &tc
 			if(sh.zero[1]) a.vy[j] = 0.0;
 		}
 	}
-	const long long max_it = 2 * S;
-	int refinements = 0;
+	const long long max_it = a.max_iters > 0 ? a.max_iters : 2 * S;
+	int refinements = 0, fell_back = 0;
 	if constexpr(!LEARNED) {
 		if(!cg_iterate<NB>(a, sh, CGVecs{a.rx, a.ry, a.px, a.py, a.Px, a.Py, a.vx, a.vy}, max_it)) return;
 		if(a.harv_in && sh.hm > 0 && !harvest_finish(a, sh, a.vx, a.vy)) return;
@@ -1396,6 +1404,7 @@ __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcCtx &tc
 		}
 		if(s_fallback || sh.act[0] || sh.act[1]) {
 			// plain FP64 CG from the current x (the residual is in rx, ry)
+			fell_back = 1;
 			if(!true_residual<RES_FP64, 4>(a, sh, false, false, true)) return;
 			if(threadIdx.x == 0) {
 				for(int c = 0; c < 2; c++) {
@@ -1416,9 +1425,15 @@ __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcCtx &tc
 		st->cg_iters += sh.it[0] + sh.it[1];
 		st->cg_max_iters = max(st->cg_max_iters, max(sh.it[0], sh.it[1]));
 		st->refinements += refinements;
+		st->fallbacks += fell_back;
 		for(int c = 0; c < 2; c++) {
 			const double rel = sh.bn2[c] > 0 ? sqrt(sh.rn2[c] / sh.bn2[c]) : 0.0;
 			st->cg_max_rel = fmax(st->cg_max_rel, rel);
+			// stopped at the cap (or on a non-finite residual) above the
+			// tolerance; sh.thr is the FP64 goal here on every path (the
+			// mixed sweeps leave a looser inner threshold only when they
+			// reached the goal)
+			if(a.fail_noconv && !sh.zero[c] && !(sh.rn2[c] < sh.thr[c])) atomicOr(&st->err, ERR_NOCONV);
 		}
 		if(cold) st->restart = 0;
 		else st->restart += 1;

@@ -39,6 +39,7 @@ enum ErrBits {
 	ERR_BARRIER = 16,   // a grid barrier timed out
 	ERR_TYPE = 32,      // activenematic type other than 0/1
 	ERR_MMA = 64,       // a tensor-core completion wait timed out
+	ERR_NOCONV = 128,   // a viscous solve stopped at its iteration cap above the tolerance
 };
 
 // Phase-dependent parameters (see rc_params in the C header).
@@ -92,6 +93,8 @@ struct DevStatus {
 	int cg_iters;
 	int cg_max_iters;
 	int refinements;
+	int fallbacks;    // mixed/learned solves finished by the plain FP64 CG
+	int pad_fb;
 	double cg_max_rel;
 	int resized_total;
 	int overflow_used;

@@ -128,6 +128,12 @@ struct rc_engine {
 	bool phase_on = false;
 	double *obs_buf = nullptr;               // diagnostic observables scratch
 	size_t obs_cap = 0;
+	// viscous solve limits (rc_set_cg_limits) and the barrier test hook
+	long long cg_max_iters = 0;
+	int cg_fail_noconv = 0;
+	long long spin_limit = 0;
+	int barrier_extra = 0;
+	DevStatus *st_save = nullptr;            // rc_viscous_resolve: the engine's status kept aside
 };
 
 static cudaEvent_t get_event(rc_engine *e) {
@@ -289,8 +295,10 @@ static void gather(rc_engine *e, const double *phi, int phase) {
 	e->launches += b.bookkeeping ? 2 : 1;
 }
 
-static void solve(rc_engine *e, int phase) {
-	CGArgs g;
+// Arguments of the viscous solve of the evaluation at `phase` with `solver`
+// into (vx, vy); returns the grid size.  harvest: record training samples
+// when the engine collects them (plain FP64 solves only).
+static int solve_args(rc_engine *e, int phase, int solver, bool harvest, double *vx, double *vy, CGArgs &g) {
 	memset(&g, 0, sizeof(g));
 	g.cells = e->cells;
 	g.mapg = e->mapg;
@@ -300,8 +308,8 @@ static void solve(rc_engine *e, int phase) {
 	g.cov_idx = e->cov_idx;
 	g.fx = e->fx;
 	g.fy = e->fy;
-	g.vx = e->vx;
-	g.vy = e->vy;
+	g.vx = vx;
+	g.vy = vy;
 	g.rx = e->rx;
 	g.ry = e->ry;
 	g.px = e->px;
@@ -329,8 +337,12 @@ static void solve(rc_engine *e, int phase) {
 	g.Pyf = e->Pyf;
 	g.exf = e->exf;
 	g.eyf = e->eyf;
+	g.max_iters = e->cg_max_iters;
+	g.fail_noconv = e->cg_fail_noconv;
+	g.spin_limit = e->spin_limit;
+	g.barrier_extra = e->barrier_extra;
 	int blocks = e->cg_blocks;
-	if(g.mixed && e->solver == RC_SOLVER_PLAIN) {
+	if(g.mixed && solver == RC_SOLVER_PLAIN) {
 		// mixed precision: Jacobi-preconditioned flexible CG in cover order
 		g.fcg = 1;
 		g.zxf = e->zxf;
@@ -341,12 +353,12 @@ static void solve(rc_engine *e, int phase) {
 		g.Pyf2 = e->Pyf2;
 		blocks = e->cg_blocks_learned;
 	}
-	if(e->solver == RC_SOLVER_LEARNED || e->solver == RC_SOLVER_LEARNED_FP32) {
+	if(solver == RC_SOLVER_LEARNED || solver == RC_SOLVER_LEARNED_FP32) {
 		g.mixed = 1;
 		g.fcg = 1;
 		g.unet_params = e->unet_params;
 		g.unet = e->unet;
-		g.unet_tc = e->solver == RC_SOLVER_LEARNED;
+		g.unet_tc = solver == RC_SOLVER_LEARNED;
 		g.phase_ns = e->phase_on ? e->phase_ns : nullptr;
 		g.unet_bf = e->unet_bf;
 		g.unet_wpack = e->unet_pack;
@@ -358,7 +370,7 @@ static void solve(rc_engine *e, int phase) {
 		g.Pyf2 = e->Pyf2;
 		blocks = e->cg_blocks_learned;
 	}
-	else if(e->harv_cap > 0 && e->harv_collect && !g.mixed) {
+	else if(harvest && e->harv_cap > 0 && e->harv_collect && !g.mixed) {
 		g.harv_in = e->harv_in;
 		g.harv_tgt = e->harv_tgt;
 		g.harv_s = e->harv_s;
@@ -367,6 +379,12 @@ static void solve(rc_engine *e, int phase) {
 		g.harv_every = e->harv_every;
 		g.harv_per_solve = e->harv_per_solve;
 	}
+	return blocks;
+}
+
+static void solve(rc_engine *e, int phase) {
+	CGArgs g;
+	const int blocks = solve_args(e, phase, e->solver, true, e->vx, e->vy, g);
 	StageMark sm(e, RC_TIMER_SOLVE);
 	cudaMemsetAsync(e->bar, 0, sizeof(unsigned) * 4, e->stream);  // the barrier counter starts at zero
 	const cudaError_t c = launch_cg(g, blocks, e->stream);
@@ -569,6 +587,7 @@ static int check_status(rc_engine *e, rc_step_stats *stats) {
 		stats->cg_max_iterations = std::max(stats->cg_max_iterations, h.cg_max_iters);
 		stats->cg_max_rel_residual = std::max(stats->cg_max_rel_residual, h.cg_max_rel);
 		stats->refinements += h.refinements;
+		stats->fallbacks += h.fallbacks;
 		stats->resized_cells += h.resized_total;
 		stats->kernel_launches += e->launches;
 	}
@@ -586,6 +605,9 @@ static int check_status(rc_engine *e, rc_step_stats *stats) {
 		if(h.err & ERR_BARRIER) return set_err(e, RC_ERR_CG, "viscous solve: grid barrier timed out");
 		if(h.err & ERR_TYPE) return set_err(e, RC_ERR_INVALID, "Too many field types (cell %d)", h.err_where);
 		if(h.err & ERR_MMA) return set_err(e, RC_ERR_CG, "viscous solve: tensor-core completion wait timed out");
+		if(h.err & ERR_NOCONV)
+			return set_err(e, RC_ERR_CG, "viscous solve: tolerance not reached within the iteration cap (%lld)",
+			               e->cg_max_iters);
 		return set_err(e, RC_ERR_INVALID, "device error 0x%x", h.err);
 	}
 	return RC_OK;
@@ -798,7 +820,7 @@ int rc_batch_create(const rc_params *params, int n_layers, const rc_box *boxes, 
 	   (rc = dalloc(e, &e->tab_cosf, (size_t) table_base(MAX_TABLE_SIDE + 1))) ||
 	   (n_cells >= SPLIT_FINISH_CELLS && (rc = dalloc(e, &e->csum, (size_t) n_cells))) ||
 	   (rc = dalloc(e, &e->tab_sinf, (size_t) table_base(MAX_TABLE_SIDE + 1))) ||
-	   (rc = dalloc(e, &e->st, 1)) ||
+	   (rc = dalloc(e, &e->st, 1)) || (rc = dalloc(e, &e->st_save, 1)) ||
 	   (rc = dalloc(e, &e->scratch_phi, cap + (size_t) n_cells / 2 + 8)) ||
 	   (rc = dalloc(e, &e->rep, e->rep_on ? cap : 1)) || (rc = dalloc(e, &e->scratch_rep, e->rep_on ? cap : 1)))
 		return bail(rc);
@@ -1378,17 +1400,17 @@ int rc_learned_set_params(rc_engine *e, const double *params) {
 	return RC_OK;
 }
 
-int rc_set_solver(rc_engine *e, int solver) {
-	if(!e) return RC_ERR_INVALID;
+}  // extern "C"
+
+// Work arrays of `solver` (allocated on first use; the stream must be idle).
+static int prepare_solver(rc_engine *e, int solver, const char *who) {
 	if(solver != RC_SOLVER_PLAIN && solver != RC_SOLVER_LEARNED && solver != RC_SOLVER_LEARNED_FP32)
-		return set_err(e, RC_ERR_INVALID, "rc_set_solver: unknown solver %d", solver);
-	CUDA_TRY(e, cudaSetDevice(e->device));
-	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+		return set_err(e, RC_ERR_INVALID, "%s: unknown solver %d", who, solver);
 	if(solver != RC_SOLVER_PLAIN) {
-		if(!is_wet_engine(e)) return set_err(e, RC_ERR_UNSUPPORTED, "rc_set_solver: the engine has no viscous solve");
+		if(!is_wet_engine(e)) return set_err(e, RC_ERR_UNSUPPORTED, "%s: the engine has no viscous solve", who);
 		if(e->L % 4 != 0 || e->L < 8)
-			return set_err(e, RC_ERR_UNSUPPORTED, "rc_set_solver: box side %d is not a multiple of 4", e->L);
-		if(!e->unet_params) return set_err(e, RC_ERR_INVALID, "rc_set_solver: no network parameters (train or set them first)");
+			return set_err(e, RC_ERR_UNSUPPORTED, "%s: box side %d is not a multiple of 4", who, e->L);
+		if(!e->unet_params) return set_err(e, RC_ERR_INVALID, "%s: no network parameters (train or set them first)", who);
 		const size_t cap = (size_t) e->S_cap, L2 = (size_t) e->L * e->L;
 		int rc;
 		if(!e->rxf) {
@@ -1426,8 +1448,103 @@ int rc_set_solver(rc_engine *e, int solver) {
 		}
 		if(!e->cg_blocks_learned) e->cg_blocks_learned = cg_grid_blocks(e->device, true, (long long) e->L * e->L);
 	}
+	return RC_OK;
+}
+
+extern "C" {
+
+int rc_set_solver(rc_engine *e, int solver) {
+	if(!e) return RC_ERR_INVALID;
+	CUDA_TRY(e, cudaSetDevice(e->device));
+	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+	const int rc = prepare_solver(e, solver, "rc_set_solver");
+	if(rc) return rc;
 	if(solver != e->solver) drop_graphs(e);
 	e->solver = solver;
+	return RC_OK;
+}
+
+int rc_set_cg_limits(rc_engine *e, long long max_iterations, int fail_on_no_convergence) {
+	if(!e) return RC_ERR_INVALID;
+	if(max_iterations < 0) return set_err(e, RC_ERR_INVALID, "rc_set_cg_limits: max_iterations %lld < 0", max_iterations);
+	CUDA_TRY(e, cudaSetDevice(e->device));
+	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+	drop_graphs(e);
+	e->cg_max_iters = max_iterations;
+	e->cg_fail_noconv = fail_on_no_convergence != 0;
+	return RC_OK;
+}
+
+int rc_test_barrier_timeout(rc_engine *e, long long spin_limit, int unreachable) {
+	if(!e) return RC_ERR_INVALID;
+	if(spin_limit < 0) return set_err(e, RC_ERR_INVALID, "rc_test_barrier_timeout: spin_limit %lld < 0", spin_limit);
+	CUDA_TRY(e, cudaSetDevice(e->device));
+	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+	drop_graphs(e);
+	e->spin_limit = spin_limit;
+	e->barrier_extra = unreachable ? 1 : 0;
+	return RC_OK;
+}
+
+}  // extern "C"
+
+// A re-solve starts cold with zeroed counters and no error; S and the rest of
+// the record are the engine's (kept aside and put back after the solve).
+__global__ void resolve_status_kernel(DevStatus *st) {
+	if(threadIdx.x == 0 && blockIdx.x == 0) {
+		st->err = 0;
+		st->cg_cold = 1;
+		st->cg_solves = st->cg_iters = st->cg_max_iters = st->refinements = st->fallbacks = 0;
+		st->cg_max_rel = 0.0;
+	}
+}
+
+extern "C" {
+
+/*
+ * rc_viscous_resolve: the viscous solve of the last force evaluation run
+ * again from a cold start with `solver` into caller-owned device arrays; the
+ * engine's own velocities, warm-start schedule and counters are left as they
+ * were.  It compares solvers on one right-hand side (the learned flexible CG
+ * against the plain FP64 CG) without advancing the simulation.  No
+ * counterpart in the reference.
+ */
+int rc_viscous_resolve(rc_engine *e, int solver, double *vx, double *vy, long long n, rc_step_stats *stats) {
+	if(!e) return RC_ERR_INVALID;
+	if(!vx || !vy) return set_err(e, RC_ERR_INVALID, "rc_viscous_resolve: NULL output array");
+	if(n != e->S) return set_err(e, RC_ERR_INVALID, "rc_viscous_resolve: n = %lld but the state has %lld unknowns", n, e->S);
+	if(e->pending || !wet_phase(e, e->eval_phase))
+		return set_err(e, RC_ERR_UNSUPPORTED, "rc_viscous_resolve: the last evaluation had no viscous solve");
+	CUDA_TRY(e, cudaSetDevice(e->device));
+	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+	int rc = prepare_solver(e, solver, "rc_viscous_resolve");
+	if(rc) return rc;
+	CUDA_TRY(e, cudaMemcpyAsync(e->st_save, e->st, sizeof(DevStatus), cudaMemcpyDeviceToDevice, e->stream));
+	resolve_status_kernel<<<1, 32, 0, e->stream>>>(e->st);
+	CUDA_TRY(e, cudaGetLastError());
+	CUDA_TRY(e, cudaMemsetAsync(e->bar, 0, sizeof(unsigned) * 4, e->stream));
+	CGArgs g;
+	const int blocks = solve_args(e, e->eval_phase, solver, false, vx, vy, g);
+	g.phase_ns = nullptr;
+	CUDA_TRY(e, launch_cg(g, blocks, e->stream));
+	DevStatus h;
+	CUDA_TRY(e, cudaMemcpyAsync(&h, e->st, sizeof(h), cudaMemcpyDeviceToHost, e->stream));
+	CUDA_TRY(e, cudaMemcpyAsync(e->st, e->st_save, sizeof(DevStatus), cudaMemcpyDeviceToDevice, e->stream));
+	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+	if(stats) {
+		memset(stats, 0, sizeof(*stats));
+		stats->cg_solves = h.cg_solves;
+		stats->cg_iterations = h.cg_iters;
+		stats->cg_max_iterations = h.cg_max_iters;
+		stats->cg_max_rel_residual = h.cg_max_rel;
+		stats->refinements = h.refinements;
+		stats->fallbacks = h.fallbacks;
+		stats->kernel_launches = 2;
+	}
+	if(h.err & ERR_BARRIER) return set_err(e, RC_ERR_CG, "rc_viscous_resolve: grid barrier timed out");
+	if(h.err & ERR_MMA) return set_err(e, RC_ERR_CG, "rc_viscous_resolve: tensor-core completion wait timed out");
+	if(h.err & ERR_NOCONV) return set_err(e, RC_ERR_CG, "rc_viscous_resolve: tolerance not reached within the iteration cap");
+	if(h.err) return set_err(e, RC_ERR_INVALID, "rc_viscous_resolve: device error 0x%x", h.err);
 	return RC_OK;
 }
 

@@ -108,6 +108,17 @@ struct CGArgs {
 	float *harv_in, *harv_tgt, *harv_s;
 	int *harv_count;
 	int harv_cap, harv_every, harv_per_solve;
+	// iteration cap per component (0: Eigen's default of twice the unknowns);
+	// fail_noconv: a solve that stops at the cap above its tolerance sets
+	// ERR_NOCONV (Eigen reports that only through info(), which the
+	// reference does not read)
+	long long max_iters;
+	int fail_noconv;
+	// grid-barrier polls before a wait gives up (0: the default, about 1-2 s);
+	// barrier_extra: arrivals the first barrier waits for beyond the grid's
+	// blocks -- a test hook that makes the wait run out (nothing arrives)
+	int barrier_extra;
+	long long spin_limit;
 };
 
 cudaError_t configure_kernels();

@@ -181,6 +181,19 @@ class Engine:
     def set_solver(self, solver: int) -> None:
         self._check(self._lib.rc_set_solver(self.h, solver), "rc_set_solver")
 
+    def resolve(self, solver: int, vx_ptr: int, vy_ptr: int) -> abi.RcStepStats:
+        """Re-run the last evaluation's viscous solve from a cold start with
+        `solver` into device arrays (pointers) of site_count() doubles; the
+        engine's own state is unchanged (rc_viscous_resolve)."""
+        st = abi.RcStepStats()
+        self._check(self._lib.rc_viscous_resolve(self.h, solver, C.c_void_p(vx_ptr), C.c_void_p(vy_ptr),
+                                                 self.site_count(), C.byref(st)), "rc_viscous_resolve")
+        return st
+
+    def set_cg_limits(self, max_iterations: int, fail_on_no_convergence: bool) -> None:
+        self._check(self._lib.rc_set_cg_limits(self.h, max_iterations, int(fail_on_no_convergence)),
+                    "rc_set_cg_limits")
+
     def get_params(self) -> np.ndarray:
         p = np.zeros(abi.RC_UNET_PARAMS)
         self._check(self._lib.rc_learned_get_params(self.h, p.ctypes.data_as(abi.DP)), "rc_learned_get_params")

@@ -152,8 +152,13 @@ def read_conf(path: str) -> Monolayer:
             tok = line.split()
             if not tok:
                 continue
+            if len(tok) < 11:
+                raise ValueError("configuration line %d: %d values, a patch header needs 11" % (len(cells) + 3, len(tok)))
             lx, ly = int(tok[0]), int(tok[1])
             n = lx * ly
+            if len(tok) < 11 + 2 * n:
+                raise ValueError("configuration line %d too short: %d values for a %dx%d patch (%d needed)"
+                                 % (len(cells) + 3, len(tok), lx, ly, 11 + 2 * n))
             vals = np.array(tok[11:11 + 2 * n], dtype=np.float64)
             cells.append(Cell(lx=lx, ly=ly, com=(float(tok[2]), float(tok[3])),
                               offset=(int(tok[4]), int(tok[5])), corner=int(tok[6]),

@@ -116,3 +116,55 @@ def compare_to_golden(gd, states: Dict[int, Dict[str, np.ndarray]], skip=(), abs
             errs[("last", k)] = rel_err(last[sk], gd["last_" + k])
     errs[("last", "map")] = 0.0 if np.array_equal(last["box_index"], gd["last_map"]) else float("inf")
     return errs
+
+
+def full_size_case(gd):
+    """(keys, monolayer) of a full-size golden case whose configuration is not
+    stored: it is regenerated from the recorded generator arguments and
+    checked against the SHA-256 of the file the reference ran on."""
+    import hashlib
+    import json
+    import shutil
+    mkw = json.loads(str(gd["monolayer"]))
+    m = g.make_monolayer(mkw.pop("L"), mkw.pop("n"), mkw.pop("seed"), **mkw)
+    d = tempfile.mkdtemp(prefix="rc_case_")
+    try:
+        g.write_conf(os.path.join(d, "start_conf.dat"), m)
+        conf = open(os.path.join(d, "start_conf.dat")).read()
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    assert hashlib.sha256(conf.encode()).hexdigest() == str(gd["conf_sha256"])
+    return case_from_texts(str(gd["input"]), conf, str(gd["topology"]))
+
+
+def sampled_errors(gd, states):
+    """Errors of a run against a full-size golden stored at sampled sites
+    (tests/golden/make_golden.py SAMPLED): per-cell scalars in full, per-site
+    arrays at the 8192 sites numpy seed 0 draws, and their sums of squares;
+    the box map by digest.  Max relative error per quantity (inf: unequal
+    integers)."""
+    import hashlib
+
+    def sample(a):
+        a = np.asarray(a)
+        return a[np.sort(np.random.default_rng(0).choice(a.size, size=min(8192, a.size), replace=False))]
+
+    errs = {}
+    steps = [int(s) for s in gd["steps"]]
+    for s in steps:
+        st = states[s]
+        for k, sk in CELL_KEYS.items():
+            if k in INT_KEYS:
+                errs[(s, k)] = 0.0 if np.array_equal(st[sk], gd["s%d_%s" % (s, k)]) else float("inf")
+            else:
+                errs[(s, k)] = rel_err(st[sk], gd["s%d_%s" % (s, k)])
+        if s > 0:
+            errs[(s, "phi")] = rel_err(sample(st["phi"]), gd["s%d_phi_sample" % s])
+            errs[(s, "phi_sumsq")] = rel_err(np.sum(np.asarray(st["phi"]) ** 2), gd["s%d_phi_sumsq" % s])
+    last = states[steps[-1]]
+    for k in ("vx", "vy", "mu"):
+        errs[("last", k)] = rel_err(sample(last[k]), gd["last_%s_sample" % k])
+        errs[("last", k + "_sumsq")] = rel_err(np.sum(np.asarray(last[k]) ** 2), gd["last_%s_sumsq" % k])
+    digest = hashlib.sha256(np.ascontiguousarray(last["box_index"], dtype="<i8").tobytes()).hexdigest()
+    errs[("last", "map")] = 0.0 if digest == str(gd["last_map_sha256"]) else float("inf")
+    return errs

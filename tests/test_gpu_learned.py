@@ -118,3 +118,74 @@ def test_learned_solve_with_strip_layers_matches_fp64_oracle(trained):
     for k in ("vx", "vy", "phi", "area", "com_x"):
         assert rel_err(got[k], want[k]) < 1e-7, k
     e.close()
+
+
+def test_stalled_refinement_falls_back_to_fp64(trained):
+    """A network that points the wrong way (negated parameters): the
+    refinement sweeps stop reducing the residual, the plain FP64 CG takes
+    over (counted in rc_step_stats.fallbacks), and the solve still meets the
+    FP64 stopping rule with velocities within 1e-7 of the FP64 oracle."""
+    keys, m, e64, _, _ = trained
+    params = -e64.get_params()
+    p, cells = build_inputs(keys, m)
+    e = engine.Engine(p, m.L, cells)
+    e.set_phase(1)
+    e.step(WARM)
+    e.set_params(params)
+    e.set_solver(abi.RC_SOLVER_LEARNED)
+    st = e.step(2)
+    print("negated network:", st.cg_iterations, st.refinements, st.fallbacks, st.cg_max_rel_residual)
+    assert st.fallbacks > 0
+    assert st.cg_max_rel_residual < 1e-8
+    got = e.state()
+    p, cells = build_inputs(keys, m)
+    o = orc.OracleSim(p, m.L, cells)
+    o.set_phase(1)
+    o.step(WARM + 2)
+    want = o.state()
+    for k in ("vx", "vy", "phi"):
+        assert rel_err(got[k], want[k]) < 1e-7, k
+    e.close()
+
+
+@pytest.mark.parametrize("L", [512, 800])
+def test_learned_solve_on_large_boxes(trained, L):
+    """The learned solve on the benchmark box sides with few cells: 512^2
+    runs every network level on the strip tensor-core layers (512, 256, 128),
+    800^2 the gathered layers and the grid-stride split of the box sites.
+    The same right-hand side solved by the learned flexible CG and by the
+    plain FP64 CG (rc_viscous_resolve) agrees within 1e-7, and after steps
+    with the learned solver the state is within 1e-7 of the FP64 oracle."""
+    import torch
+    from tests.test_gpu_large_box import cluster_case
+    _, _, e64, _, _ = trained
+    params = e64.get_params()
+    keys, m = cluster_case(L, "wetmodel")
+    warm, steps = 3, 2
+    p, cells = build_inputs(keys, m)
+    e = engine.Engine(p, m.L, cells)
+    e.set_phase(1)
+    e.step(warm)
+    e.set_params(params)
+    S = e.site_count()
+    v = [torch.zeros(S, dtype=torch.float64, device="cuda") for _ in range(4)]
+    torch.cuda.synchronize()
+    sp = e.resolve(abi.RC_SOLVER_PLAIN, v[0].data_ptr(), v[1].data_ptr())
+    sl = e.resolve(abi.RC_SOLVER_LEARNED, v[2].data_ptr(), v[3].data_ptr())
+    print("L=%d plain %d it, learned %d inner it (%d refinements)" % (L, sp.cg_iterations, sl.cg_iterations,
+                                                                         sl.refinements))
+    assert sp.cg_max_rel_residual < 1e-8 and sl.cg_max_rel_residual < 1e-8
+    for a, b in ((v[2], v[0]), (v[3], v[1])):
+        assert rel_err(a.cpu().numpy(), b.cpu().numpy()) < 1e-7
+    e.set_solver(abi.RC_SOLVER_LEARNED)
+    st = e.step(steps)
+    assert st.cg_max_rel_residual < 1e-8
+    got = e.state()
+    e.close()
+    p, cells = build_inputs(keys, m)
+    o = orc.OracleSim(p, m.L, cells)
+    o.set_phase(1)
+    o.step(warm + steps)
+    want = o.state()
+    for k in ("vx", "vy", "phi", "area", "com_x"):
+        assert rel_err(got[k], want[k]) < 1e-7, k

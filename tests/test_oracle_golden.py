@@ -75,20 +75,10 @@ HASHED = ["dry140_100"]
 def test_oracle_matches_reference_bitwise_full_size(name):
     import hashlib
 
-    from rheocell_gb300 import generator as g
-    from tests.common import CELL_KEYS
+    from tests.common import CELL_KEYS, full_size_case
     gd = golden(name)
-    mkw = json.loads(str(gd["monolayer"]))
-    m = g.make_monolayer(mkw.pop("L"), mkw.pop("n"), mkw.pop("seed"), **mkw)
-    d = tempfile.mkdtemp(prefix="rc_case_")
-    try:
-        g.write_conf(os.path.join(d, "start_conf.dat"), m)
-        conf = open(os.path.join(d, "start_conf.dat")).read()
-    finally:
-        shutil.rmtree(d, ignore_errors=True)
     # the generator still writes the configuration the reference ran on
-    assert hashlib.sha256(conf.encode()).hexdigest() == str(gd["conf_sha256"])
-    keys, m2 = case_from_texts(str(gd["input"]), conf, str(gd["topology"]))
+    keys, m2 = full_size_case(gd)
     steps = [int(s) for s in gd["steps"]]
     _, states = run(orc.OracleSim, keys, m2, steps)
 
@@ -118,44 +108,10 @@ SAMPLED = ["wet256"]
 
 @pytest.mark.parametrize("name", SAMPLED)
 def test_oracle_matches_reference_wet_full_size(name):
-    import hashlib
-
-    from rheocell_gb300 import generator as g
-    from tests.common import CELL_KEYS, rel_err
+    from tests.common import full_size_case, sampled_errors
     gd = golden(name)
-    mkw = json.loads(str(gd["monolayer"]))
-    m = g.make_monolayer(mkw.pop("L"), mkw.pop("n"), mkw.pop("seed"), **mkw)
-    d = tempfile.mkdtemp(prefix="rc_case_")
-    try:
-        g.write_conf(os.path.join(d, "start_conf.dat"), m)
-        conf = open(os.path.join(d, "start_conf.dat")).read()
-    finally:
-        shutil.rmtree(d, ignore_errors=True)
-    assert hashlib.sha256(conf.encode()).hexdigest() == str(gd["conf_sha256"])
-    keys, m2 = case_from_texts(str(gd["input"]), conf, str(gd["topology"]))
-    steps = [int(s) for s in gd["steps"]]
-    _, states = run(orc.OracleSim, keys, m2, steps)
-
-    def sample(a):
-        a = np.asarray(a)
-        return a[np.sort(np.random.default_rng(0).choice(a.size, size=min(8192, a.size), replace=False))]
-
-    errs = {}
-    for s in steps:
-        st = states[s]
-        for k, sk in CELL_KEYS.items():
-            if k in ("lx", "ly", "offx", "offy", "corner"):
-                errs[(s, k)] = 0.0 if np.array_equal(st[sk], gd["s%d_%s" % (s, k)]) else float("inf")
-            else:
-                errs[(s, k)] = rel_err(st[sk], gd["s%d_%s" % (s, k)])
-        if s > 0:
-            errs[(s, "phi")] = rel_err(sample(st["phi"]), gd["s%d_phi_sample" % s])
-            errs[(s, "phi_sumsq")] = rel_err(np.sum(np.asarray(st["phi"]) ** 2), gd["s%d_phi_sumsq" % s])
-    last = states[steps[-1]]
-    for k in ("vx", "vy", "mu"):
-        errs[("last", k)] = rel_err(sample(last[k]), gd["last_%s_sample" % k])
-        errs[("last", k + "_sumsq")] = rel_err(np.sum(np.asarray(last[k]) ** 2), gd["last_%s_sumsq" % k])
-    digest = hashlib.sha256(np.ascontiguousarray(last["box_index"], dtype="<i8").tobytes()).hexdigest()
-    errs[("last", "map")] = 0.0 if digest == str(gd["last_map_sha256"]) else float("inf")
+    keys, m2 = full_size_case(gd)
+    _, states = run(orc.OracleSim, keys, m2, [int(s) for s in gd["steps"]])
+    errs = sampled_errors(gd, states)
     bad = {k: v for k, v in errs.items() if v > 1e-12}
     assert not bad, bad

@@ -47,6 +47,10 @@ def test_noalloc_resolve_matches_engine_twice():
     vx = torch.full((S,), 7.0, dtype=torch.float64, device="cuda")
     vy = torch.full((S,), -7.0, dtype=torch.float64, device="cuda")
     for _ in range(2):
+        # the fills run on torch's stream and the solve on the engine's:
+        # finish them first (the entry point does not wait for the caller's
+        # pending work on its arrays)
+        torch.cuda.synchronize()
         rc, it = _resolve(e, vx, vy)
         assert rc == 0, e._lib.rc_last_error(e.h).decode()
         assert it > 0
