@@ -6,13 +6,15 @@ turn the unmodified reference's output into numpy arrays.
 from __future__ import annotations
 
 import os
+import platform
 import subprocess
 from typing import Dict, List
 
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_DIR = os.path.join(HERE, "_ref")
+# binaries of the out-of-tree reference build for this machine (oracle/Makefile)
+REF_DIR = os.path.join(HERE, "_ref", platform.machine())
 
 CELL_I32 = ["lx", "ly", "offx", "offy", "corner", "type"]
 CELL_F64 = ["comx", "comy", "unrapx", "unrapy", "q00", "q01", "thetaq", "nemqx", "nemqy",
