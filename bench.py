@@ -1,16 +1,26 @@
 #!/usr/bin/env python3
 """Benchmark of the GB300 multi-phase-field time step.
 
-Default workload (the configuration the headline metric is quoted on): the wet
-multi-phase-field monolayer, periodic 256x256 box, 400 cells of radius 8 on
-41x41 patches, wetmodel (Brinkman viscous solve, xi = eta = 1, CG rtol 1e-8),
-FP64, seeded synthetic initial condition (jittered triangular lattice, tanh
-interfaces) -- synthetic data with the workload's shapes, no dataset exists.
-A "step" is one FD_CPUBackend::sim_step (Heun predictor + corrector, two
-force evaluations, four viscous solves).
+Default workload (the largest single-GPU configuration of the headline
+metric, which names the learned-vs-plain solve): the wet multi-phase-field
+monolayer on a periodic 1024x1024 box, 6400 cells of radius 8 on 41x41
+patches, wetmodel (nematic activity, Brinkman viscous solve xi = eta = 1,
+rtol 1e-8), FP64 fields, the viscous solve by the learned flexible CG (FP32
+inner iterations with the U-Net preconditioner on the tensor cores, FP64
+refinement and plain FP64 CG fallback).  Set-up, outside the timed region:
+training samples harvested from the plain FP64 solve of the 256x256 /
+400-cell monolayer of the same physics (160 steps), the network trained on
+the GPU (30 epochs), its parameters moved to the 1024^2 engine; then the
+solve stage timed with the plain FP64 CG and with the learned solver on the
+same states, and the velocity difference of the two solves of one
+right-hand side.  Seeded synthetic initial condition (jittered triangular
+lattice, tanh interfaces) -- synthetic data with the workload's shapes, no
+dataset exists.  A "step" is one FD_CPUBackend::sim_step (Heun predictor +
+corrector, two force evaluations, four viscous solves).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--workload wet256|wet512|wet1024|dry140|ensemble64] [--precision double|mixed]
+                  [--workload wet1024|wet512|wet256|dry140|ensemble64]
+                  [--precision double|mixed|float] [--solver learned|plain]
 
 Prints one JSON line (rank 0).  `value` is site-updates/s over all ranks with
 the state resident on the device, timed with CUDA events per step on the
@@ -72,7 +82,6 @@ def ensemble_members(count=64, seed=64, R=8.0):
 def make_case(w):
     """[(keys, monolayer)] of the workload's members (one for a single box)."""
     from rheocell_gb300 import generator as g
-    from tests.common import case_from_monolayer
     if "members" in w:
         out = []
         for L, n, seed in w["members"]:
@@ -82,7 +91,7 @@ def make_case(w):
             out.append((keys, m))
         return out
     m = g.make_monolayer(w["L"], w["n"], seed=w["seed"])
-    keys, m2 = case_from_monolayer(m, w["params"], seed=w["seed"])
+    keys, m2 = g.case_keys(m, w["params"], seed=w["seed"])
     return [(keys, m2)]
 
 
@@ -191,7 +200,8 @@ def prepare_learned(args, eng, lib):
     # samples come from this monolayer's own plain solve, or from a smaller
     # monolayer of the same physics (--train-workload): the network is
     # convolutional, so parameters trained there apply at any box side
-    src = eng if not args.train_workload else make_engine(args.train_workload, abi.RC_PRECISION_DOUBLE, eng.device)
+    own = not args.train_workload or args.train_workload == args.workload
+    src = eng if own else make_engine(args.train_workload, abi.RC_PRECISION_DOUBLE, eng.device)
     src.harvest(capacity=args.harvest_capacity, every=3, per_solve=6)
     t0 = time.perf_counter()
     src.step(args.harvest_steps)
@@ -253,10 +263,9 @@ def velocity_error(eng):
 
 def make_engine(name, prec, dev):
     """A single-monolayer engine of workload `name` on device `dev`, in phase 1."""
-    from rheocell_gb300 import engine
-    from tests.common import build_inputs
+    from rheocell_gb300 import engine, host
     (keys, m), = make_case(workload(name))
-    p, cells = build_inputs(keys, m, precision=prec)
+    p, cells = host.engine_inputs(keys, m, precision=prec)
     e = engine.Engine(p, m.L, cells, device=dev)
     e.set_phase(1)
     return e
@@ -264,8 +273,7 @@ def make_engine(name, prec, dev):
 
 def run_gb300(args, rank, world):
     import torch
-    from rheocell_gb300 import abi, engine
-    from tests.common import build_inputs
+    from rheocell_gb300 import abi, engine, host
 
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
@@ -273,7 +281,7 @@ def run_gb300(args, rank, world):
     members = make_case(w)
     prec = {"double": abi.RC_PRECISION_DOUBLE, "mixed": abi.RC_PRECISION_MIXED,
             "float": abi.RC_PRECISION_FLOAT}[args.precision]
-    built = [build_inputs(keys, m, precision=prec) for keys, m in members]
+    built = [host.engine_inputs(keys, m, precision=prec) for keys, m in members]
     stream = torch.cuda.Stream(dev)  # a real stream: the engine's graphs cannot capture on the legacy one
     torch.cuda.set_stream(stream)
     if len(members) == 1:
@@ -398,10 +406,8 @@ def run_gb300(args, rank, world):
         "dtype": {"double": "f64", "mixed": "f64 fields, f32 solve inner iterations",
                   "float": "f32 site arithmetic, f64 field storage and cell-area integrals"}[args.precision],
         "data": "synthetic (seeded jittered lattice, tanh interfaces)",
-        "config": {"workload": w["name"], "L": [m.L for _, m in members] if len(members) > 1 else members[0][1].L,
-                   "monolayers": len(members), "cells": n_cells, "sites": S, "precision": args.precision,
-                   "parallelism": "replicas" if world > 1 else "single GPU",
-                   "l2": "flushed (256 MiB write) before every timed step"},
+        "config": dict(arm_config(args, w, members), parallelism="replicas" if world > 1 else "single GPU",
+                       l2="flushed (256 MiB write) before every timed step"),
         "cg": {"solves": st.cg_solves, "iterations": st.cg_iterations, "max_iterations": st.cg_max_iterations,
                "max_rel_residual": st.cg_max_rel_residual,
                "ms_per_step": tms[3] / prof_steps if tn[3] else 0.0},
@@ -425,71 +431,77 @@ def run_gb300(args, rank, world):
                            "chosen": tuned["chosen"]}
     if learned is not None:
         out["learned_pcg"] = learned
-        out["config"]["solver"] = "learned flexible CG (FP32 inner, FP64 refinement)"
         out["dtype"] = "f64 fields, f32 solve inner iterations, learned preconditioner"
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, w, members)
+        if out["cpu_baseline"]["kind"] == "reference" and len(members) == 1:
+            # the restatement beside it: how far the port's speed is from the reference's
+            out["cpu_baseline_port"] = cpu_baseline(args, w, members, kind="port")
     return out
 
 
-def cpu_baseline(args, w, members, budget_s=25.0, max_steps=None):
-    """The CPU restatement (oracle/, serial FP64, the reference's algorithm)
-    on the same workload, timed on this host for a bounded sample: main-loop
-    steps of the single box, or for an ensemble one step of each member in
-    turn (creation untimed) until the budget is spent."""
-    from oracle import oracle as orc
-    from tests.common import build_inputs
-    orc.build()
-    sites = 0
-    el = 0.0
-    steps = 0
-    if len(members) == 1:
-        keys, m = members[0]
-        p, cells = build_inputs(keys, m)
-        sim = orc.OracleSim(p, m.L, cells)
-        sim.set_phase(1)
-        t0 = time.perf_counter()
-        while True:
-            sim.step(1)
-            steps += 1
-            el = time.perf_counter() - t0
-            if el >= budget_s or (max_steps and steps >= max_steps):
-                break
-            if el / steps * (steps + 1) > budget_s * 1.5:
-                break
-        sites = m.sites * steps
-        sim.close()
-        sample = "%d main-loop step(s) of the same workload, %.1f s wall" % (steps, el)
-    else:
-        # independent members spread over the host cores (spawned workers),
-        # each timing its own main-loop steps; aggregate = sum over workers of
-        # work / step time (all workers run concurrently)
-        import multiprocessing as mp
-        cores = max(1, min(os.cpu_count() or 1, len(members)))
-        per_member = budget_s * cores / len(members)
-        groups = [[] for _ in range(cores)]
-        for i, (keys, m) in enumerate(members):
-            groups[i % cores].append((keys, m, per_member))
-        with mp.get_context("spawn").Pool(cores) as pool:
-            res = pool.map(_ensemble_worker, groups)
-        value = sum(w / t for w, t, _ in res if t > 0)
-        steps = sum(n for _, _, n in res)
-        el = max(t for _, t, _ in res)
-        sample = ("%d main-loop steps over the %d members (>= 1 each, about %.1f s per member), %d worker "
-                  "processes, %.1f s of stepping per worker" % (steps, len(members), per_member, cores, el))
-        return {"value": value, "unit": "site-updates/s", "cores": cores, "kind": "port", "sample": sample}
-    return {"value": sites / el, "unit": "site-updates/s", "cores": 1, "kind": "port", "sample": sample}
+# A 1024^2 or 512^2 main-loop step of the CPU codes takes minutes (the
+# reference's alone about a quarter of an hour at 1024^2 on one core), so
+# their bounded sample is the 256^2 / 400-cell monolayer of the same physics
+# (area fraction, R, xi, eta, activity).  Its solves need fewer iterations
+# (about 48 against 65 per solve on the device), so the CPU rate measured
+# there is an upper bound on the CPU rate at the larger box.
+SAMPLE_OF = {"wet1024": "wet256", "wet512": "wet256"}
 
 
-def _ensemble_worker(group):
-    """Step each (keys, monolayer, seconds) of a group with the oracle;
-    returns (site-updates, stepping seconds, steps)."""
+def reference_driver():
+    """The reference built out of tree with its own Release flags
+    (oracle/_ref/<machine>/ref_driver_fast), or None."""
+    import platform
+    path = os.path.join(ROOT, "oracle", "_ref", platform.machine(), "ref_driver_fast")
+    return path if os.access(path, os.X_OK) else None
+
+
+def _time_reference_case(exe, keys, m, steps):
+    """Wall-clock seconds of `steps` main-loop steps of the reference on one
+    monolayer (its driver's std::chrono around the loop; set-up untimed)."""
+    import shutil
+    import tempfile
+    from rheocell_gb300 import generator as g
+    d = tempfile.mkdtemp(prefix="rc_refcase_")
+    try:
+        g.write_case(d, m, keys, steps=steps, seed=int(keys.get("seed", 1)))
+        res = subprocess.run([exe, "time", str(steps), "input"], cwd=d, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError("reference driver failed: %s" % res.stderr[-1000:])
+        line = [ln for ln in res.stdout.splitlines() if ln.startswith("{")][-1]
+        return float(json.loads(line)["seconds"])
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+
+
+def _reference_worker(group):
+    """Reference steps of each (exe, keys, monolayer, seconds) of a group:
+    one step to size the sample, then as many as fit the member's share.
+    Returns (site-updates, stepping seconds, steps)."""
+    work, el, n = 0.0, 0.0, 0
+    for exe, keys, m, budget in group:
+        t1 = _time_reference_case(exe, keys, m, 1)
+        k = int(budget / t1) if t1 > 0 else 1
+        if k >= 2:
+            t = _time_reference_case(exe, keys, m, k)
+        else:
+            k, t = 1, t1
+        work += m.sites * k
+        el += t
+        n += k
+    return work, el, n
+
+
+def _port_worker(group):
+    """The CPU restatement (oracle/) on each (keys, monolayer, seconds) of a
+    group; returns (site-updates, stepping seconds, steps)."""
     sys.path.insert(0, ROOT)
     from oracle import oracle as orc
-    from tests.common import build_inputs
+    from rheocell_gb300 import host
     work, el, n = 0.0, 0.0, 0
     for keys, m, budget in group:
-        p, cells = build_inputs(keys, m)
+        p, cells = host.engine_inputs(keys, m)
         sim = orc.OracleSim(p, m.L, cells)
         sim.set_phase(1)
         t0 = time.perf_counter()
@@ -507,19 +519,60 @@ def _ensemble_worker(group):
     return work, el, n
 
 
+def cpu_baseline(args, w, members, budget_s=25.0, kind=None):
+    """A CPU implementation of the path timed on this host over a bounded
+    sample of the workload: the reference's own build (kind "reference",
+    oracle/_ref, the reference's Release flags) when it was built here, else
+    the CPU restatement (kind "port", oracle/, the reference's algorithm in
+    serial C).  One monolayer: main-loop steps on one core (the reference
+    steps serially); the 512^2 and 1024^2 boxes are sampled on the 256^2 box
+    of the same physics (SAMPLE_OF).  An ensemble: its independent members
+    spread over the host cores, aggregate = sum over workers of work / time."""
+    import multiprocessing as mp
+    exe = reference_driver()
+    if kind is None:
+        kind = "reference" if exe else "port"
+    if kind == "reference" and not exe:
+        raise RuntimeError("the reference build (oracle/_ref) is missing")
+    sample_name = SAMPLE_OF.get(args.workload)
+    sample_members = make_case(workload(sample_name)) if sample_name else members
+    what = ("the reference's own build (Release flags -O3 -ffast-math -march=native, Eigen CG through the "
+            "documented-semantics shim)" if kind == "reference" else "the CPU restatement (serial C)")
+    if len(sample_members) == 1:
+        keys, m = sample_members[0]
+        item = [(exe, keys, m, budget_s)] if kind == "reference" else [(keys, m, budget_s)]
+        work, el, steps = (_reference_worker if kind == "reference" else _port_worker)(item)
+        where = ("the %dx%d / %d-cell monolayer of the same physics (a %s step takes minutes on one core)"
+                 % (m.L, m.L, m.n, args.workload) if sample_name else "the same workload")
+        sample = "%s: %d main-loop step(s) of %s, %.1f s of stepping" % (what, steps, where, el)
+        return {"value": work / el, "unit": "site-updates/s", "cores": 1, "kind": kind, "sample": sample}
+    cores = max(1, min(os.cpu_count() or 1, len(sample_members)))
+    per_member = budget_s * cores / len(sample_members)
+    groups = [[] for _ in range(cores)]
+    for i, (keys, m) in enumerate(sample_members):
+        groups[i % cores].append((exe, keys, m, per_member) if kind == "reference" else (keys, m, per_member))
+    with mp.get_context("spawn").Pool(cores) as pool:
+        res = pool.map(_reference_worker if kind == "reference" else _port_worker, groups)
+    value = sum(wk / t for wk, t, _ in res if t > 0)
+    steps = sum(n for _, _, n in res)
+    el = max(t for _, t, _ in res)
+    sample = ("%s: %d main-loop steps over the %d members (>= 1 each, about %.1f s per member), %d worker "
+              "processes, %.1f s of stepping per worker" % (what, steps, len(sample_members), per_member, cores, el))
+    return {"value": value, "unit": "site-updates/s", "cores": cores, "kind": kind, "sample": sample}
+
+
 def run_reference(args, rank, world):
-    """Reference arm: the reference's CPU implementation of the path.  The
-    compiled reference (oracle/_ref) is an x86 build made where the reference
-    sources are; it does not exist on the GPU host, so this times the CPU
-    restatement (bit-identical to the reference on the dry models), which is
-    single-threaded as the reference's stepping is."""
+    """Reference arm: the reference's own CPU build of the path (oracle/_ref,
+    compiled on this host from the reference's sources with its Release
+    flags) on all the host cores the path can use -- one for a monolayer,
+    whose stepping is serial in the reference; the ensemble's members in
+    parallel -- over a bounded sample of the workload (cpu_baseline).  Falls
+    back to the CPU restatement where the reference could not be built."""
     if rank != 0:
         return None
     w = workload(args.workload)
     members = make_case(w)
-    kind = "port"
-    budget = 90.0
-    base = cpu_baseline(args, w, members, budget_s=budget, max_steps=max(1, args.steps))
+    base = cpu_baseline(args, w, members, budget_s=90.0)
     line = {
         "impl": "reference",
         "metric": METRIC,
@@ -533,13 +586,21 @@ def run_reference(args, rank, world):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded jittered lattice, tanh interfaces)",
-        "config": {"workload": w["name"], "L": [m.L for _, m in members] if len(members) > 1 else members[0][1].L,
-                   "monolayers": len(members), "cells": sum(m.n for _, m in members),
-                   "sites": sum(m.sites for _, m in members), "precision": "double"},
-        "cpu_baseline": dict(base, kind=kind),
+        "config": arm_config(args, w, members),
+        "cpu_baseline": base,
         "e2e": {"value": base["value"], "unit": "site-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     return line
+
+
+def arm_config(args, w, members):
+    """The `config` block both arms print for the workload."""
+    cfg = {"workload": w["name"], "L": [m.L for _, m in members] if len(members) > 1 else members[0][1].L,
+           "monolayers": len(members), "cells": sum(m.n for _, m in members),
+           "sites": sum(m.sites for _, m in members), "precision": args.precision}
+    if args.solver == "learned":
+        cfg["solver"] = "learned flexible CG (FP32 inner, FP64 refinement)"
+    return cfg
 
 
 def main():
@@ -548,21 +609,24 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="wet256", choices=["wet256", "wet512", "wet1024", "dry140", "ensemble64"])
+    ap.add_argument("--workload", default="wet1024", choices=["wet1024", "wet512", "wet256", "dry140", "ensemble64"])
     ap.add_argument("--precision", default="double", choices=["double", "mixed", "float"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--solver", default="plain", choices=["plain", "learned"])
-    ap.add_argument("--harvest-steps", type=int, default=40)
-    ap.add_argument("--harvest-capacity", type=int, default=2000)
-    ap.add_argument("--train-epochs", type=int, default=10)
+    ap.add_argument("--solver", default=None, choices=["plain", "learned"],
+                    help="viscous solver (default: learned for the wet workloads)")
+    ap.add_argument("--harvest-steps", type=int, default=160)
+    ap.add_argument("--harvest-capacity", type=int, default=4000)
+    ap.add_argument("--train-epochs", type=int, default=30)
     ap.add_argument("--solver-phases", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default cell tile (FP32 only)")
-    ap.add_argument("--train-workload", default=None, choices=["wet256", "wet512", "wet1024"],
-                    help="harvest and train on this monolayer instead of the timed one")
+    ap.add_argument("--train-workload", default="wet256", choices=["wet256", "wet512", "wet1024"],
+                    help="harvest and train on this monolayer (the network transfers to the timed one)")
     ap.add_argument("--train-max-samples", type=int, default=0, help="train on at most this many samples (0: all)")
     ap.add_argument("--train-lr", type=float, default=2e-3)
     ap.add_argument("--train-lr-final", type=float, default=0.05, help="final step size as a fraction of --train-lr")
     args = ap.parse_args()
+    if args.solver is None:
+        args.solver = "learned" if args.workload.startswith("wet") and args.precision != "float" else "plain"
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1:

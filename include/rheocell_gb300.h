@@ -176,6 +176,34 @@ int rc_create(const rc_params *params, const rc_box *box, int n_cells,
  * (src/rheoCell.cpp:13-29); each layer here is what one such process reads
  * (SimBackend::read_next_configuration, src/Backends/SimBackend.cpp:220-314).
  */
+/*
+ * rc_create with every patch's phi generated on the device instead of copied
+ * from host arrays (cells[i].phi is ignored and may be NULL; the other fields
+ * of cells[i] -- patch geometry, centre, Q, the drand48-drawn director --
+ * are taken as in rc_create).  It replaces, for a start from generated
+ * discs, the reference's confGenerator writing the configuration file and
+ * SimBackend::read_next_configuration parsing it back
+ * (src/Managers/GeneratorManager.cpp:130-158, src/Backends/SimBackend.cpp:220-314):
+ * at 1024^2 that file is about 0.4 GB of text.
+ *   RC_PROFILE_TANH: phi = (1 - tanh((d - radius) / width)) / 2, d the
+ *     distance of the box site from the cell's centre (com_x, com_y), nearest
+ *     periodic image;
+ *   RC_PROFILE_DISC: the reference's initial disc (MultiPhaseField::init,
+ *     src/Fields/MultiPhaseField.cpp:149-156): phi = 1 where
+ *     x^2 + y^2 < radius^2 + 0.5, x = LsubX/2 - (q mod LsubX),
+ *     y = LsubY/2 - q / LsubX, else 0 (confGenerator's files hold the same
+ *     values for radius = its init_radius).
+ */
+#define RC_PROFILE_TANH 0
+#define RC_PROFILE_DISC 1
+typedef struct rc_generate_spec {
+	int profile;     /* RC_PROFILE_TANH or RC_PROFILE_DISC */
+	double radius;   /* tanh: R; disc: the disc radius      */
+	double width;    /* tanh: interface width lambda        */
+} rc_generate_spec;
+int rc_create_generated(const rc_params *params, const rc_box *box, int n_cells, const rc_cell_host *cells,
+                        const rc_generate_spec *spec, int device, rc_engine **out);
+
 int rc_batch_create(const rc_params *params, int n_layers, const rc_box *boxes, const int *n_cells_per_layer,
                     const rc_cell_host *cells, const unsigned long long *rng_states, int device, rc_engine **out);
 
@@ -458,6 +486,23 @@ int rc_solver_profile(rc_engine *e, int enable, double *ms, int n);
  * type only_type; -1: all) in index order, into fx, fy (L*L each, row-major
  * box sites).  With size_grid > 0 also the coarse-grained fields
  * (VelocityField.cpp:105-121) into coarse_x, coarse_y (may be NULL).
+ * The force kinds are the box fields of ForceField / StressField::calc_field
+ * (src/Observables/ForceField.cpp:79-96, StressField.cpp:84-100) from the
+ * last force evaluation: RC_OBS_FORCE the total force, velocity times the
+ * friction (get_total_force_x/y); RC_OBS_FORCE_PASSIVE and
+ * RC_OBS_FORCE_ACTIVE the interaction's Fpassive / Factive split
+ * (e.g. WetModel.cpp:636-637,655-656); RC_OBS_PRESSURE the pressure
+ * Rep - CH - A (WetModel.cpp:605) in fx and the phi field in fy.  Their
+ * coarse fields are ForceField's window means (ForceField.cpp:141-160).
+ * The split is formed by evaluating the forces again at the current state,
+ * which leaves the simulation unchanged (FP64 engines only).
+ *
+ * rc_observe_stress: StressField's coarse stress of one of the force kinds
+ * (StressField.cpp:171-199): per box site, over the size_grid^2 periodic
+ * window, with e the unit vector from the window site to the centre,
+ * xx = sum fx ex / sg^2, yy = sum fy ey / sg^2,
+ * xy = sum (fx ey + fy ex) / (2 sg^2); for RC_OBS_PRESSURE xx and yy of the
+ * pressure field (xy is not formed and may be NULL).
  *
  * rc_observe_cells: per cell (6 doubles each, cell order): unwrapped centre
  * of mass x, y; area; elongation |S|; aspect ratio sqrt(s1/s2) - 1;
@@ -469,8 +514,14 @@ int rc_solver_profile(rc_engine *e, int enable, double *ms, int n);
 #define RC_OBS_VELOCITY 0
 #define RC_OBS_SHAPE 1
 #define RC_OBS_NEMATIC 2
+#define RC_OBS_FORCE 3
+#define RC_OBS_FORCE_PASSIVE 4
+#define RC_OBS_FORCE_ACTIVE 5
+#define RC_OBS_PRESSURE 6
 int rc_observe_field(rc_engine *e, int kind, int layer, int only_type, int size_grid, double *fx, double *fy,
                      double *coarse_x, double *coarse_y);
+int rc_observe_stress(rc_engine *e, int kind, int layer, int only_type, int size_grid, double *xx, double *yy,
+                      double *xy);
 int rc_observe_cells(rc_engine *e, double *cell_obs, double *layer_obs);
 
 /* Sites (sum of LsubX*LsubY) in the current configuration: the reference's

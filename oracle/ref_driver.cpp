@@ -13,6 +13,10 @@
 // Usage:
 //   ref_driver dump  <out.bin> <steps,csv> <input> [key=value ...]
 //   ref_driver time  <n_steps>             <input> [key=value ...]
+//   ref_driver observe <out.txt> <step>:<type>:<size_grid> <input> [key=value ...]
+//     after <step> main-loop steps, the output string of the reference's
+//     own field observable <type> (force_field or stress_field) with that
+//     size_grid, as its ObservableOutput would print it
 //
 // Dump record layout (little endian), one record per requested step (step 0 is
 // the state right after init and equilibration, before the main loop):
@@ -24,6 +28,8 @@
 //     double phi[subSize]; int32 map_sub_to_box[subSize];
 //     double vx[subSize], vy[subSize], freeEnergy[subSize], dx[subSize], dy[subSize]
 #include "defs.h"
+#include "Observables/ForceField.h"
+#include "Observables/StressField.h"
 #include "Backends/BackendFactory.h"
 #include "Backends/SimBackend.h"
 #include "Interactions/BaseInteraction.h"
@@ -120,6 +126,9 @@ int main(int argc, char *argv[]) {
 		else if(mode == "time") {
 			steps = std::atoll(argv[2]);
 		}
+		else if(mode == "observe") {
+			steps = std::atoll(argv[3]);
+		}
 		else {
 			throw RCexception("unknown mode %s", mode.c_str());
 		}
@@ -141,6 +150,26 @@ int main(int argc, char *argv[]) {
 		}
 		auto t1 = std::chrono::steady_clock::now();
 		if(out) fclose(out);
+		if(mode == "observe") {
+			// <step>:<type>:<size_grid>; the backend's fields hold the state
+			// and the forces of the last evaluation, as when SimBackend prints
+			std::string spec = argv[3];
+			const size_t c1 = spec.find(':'), c2 = spec.find(':', c1 + 1);
+			const std::string type = spec.substr(c1 + 1, c2 - c1 - 1);
+			input_file oi;
+			oi.init_from_string("type = " + type + "\nsize_grid = " + spec.substr(c2 + 1) + "\n");
+			std::shared_ptr<BaseObservable> obs;
+			if(type == "force_field") obs = std::make_shared<ForceField>();
+			else if(type == "stress_field") obs = std::make_shared<StressField>();
+			else throw RCexception("unknown observable %s", type.c_str());
+			obs->get_settings(oi, input);
+			obs->init();
+			FILE *o = fopen(argv[2], "w");
+			if(!o) throw RCexception("cannot open %s", argv[2]);
+			const std::string text = obs->get_output_string(steps);
+			fwrite(text.data(), 1, text.size(), o);
+			fclose(o);
+		}
 		if(mode == "time") {
 			double secs = std::chrono::duration<double>(t1 - t0).count();
 			printf("{\"steps\": %lld, \"seconds\": %.9f}\n", steps, secs);

@@ -26,6 +26,10 @@ RC_SOLVER_LEARNED_FP32 = 2
 RC_OBS_VELOCITY = 0
 RC_OBS_SHAPE = 1
 RC_OBS_NEMATIC = 2
+RC_OBS_FORCE = 3
+RC_OBS_FORCE_PASSIVE = 4
+RC_OBS_FORCE_ACTIVE = 5
+RC_OBS_PRESSURE = 6
 SOLVER_PHASES = ["fcg_setup", "first_layer", "tc_level0", "tc_level1", "tc_level2", "last_layer",
                  "fcg_z", "fcg_direction", "solve_start", "fcg_update", "other",
                  "tc_weights", "tc_staging", "tc_mma", "tc_epilogue"]
@@ -99,6 +103,13 @@ class RcStepStats(C.Structure):
     ]
 
 
+RC_PROFILE_TANH, RC_PROFILE_DISC = 0, 1
+
+
+class RcGenerateSpec(C.Structure):
+    _fields_ = [("profile", C.c_int), ("radius", C.c_double), ("width", C.c_double)]
+
+
 class RcAutotuneReport(C.Structure):
     _fields_ = [("candidates", C.c_int), ("threads", C.c_int * 4), ("ms_per_step", C.c_double * 4), ("chosen", C.c_int)]
 
@@ -158,6 +169,9 @@ def declare(lib: C.CDLL, prefix: str) -> C.CDLL:
         lib.rc_batch_create.argtypes = [C.POINTER(RcParams), C.c_int, C.POINTER(RcBox), C.POINTER(C.c_int),
                                         C.POINTER(RcCellHost), C.POINTER(C.c_ulonglong), C.c_int, C.POINTER(vp)]
         lib.rc_batch_create.restype = C.c_int
+        lib.rc_create_generated.argtypes = [C.POINTER(RcParams), C.POINTER(RcBox), C.c_int, C.POINTER(RcCellHost),
+                                            C.POINTER(RcGenerateSpec), C.c_int, C.POINTER(vp)]
+        lib.rc_create_generated.restype = C.c_int
         lib.rc_layer_count.argtypes = [vp]
         lib.rc_layer_count.restype = C.c_int
         lib.rc_learned_harvest.argtypes = [vp, C.c_int, C.c_int, C.c_int]
@@ -172,6 +186,8 @@ def declare(lib: C.CDLL, prefix: str) -> C.CDLL:
         lib.rc_learned_set_params.restype = C.c_int
         lib.rc_observe_field.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, DP, DP, DP, DP]
         lib.rc_observe_field.restype = C.c_int
+        lib.rc_observe_stress.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, DP, DP, DP]
+        lib.rc_observe_stress.restype = C.c_int
         lib.rc_observe_cells.argtypes = [vp, DP, DP]
         lib.rc_observe_cells.restype = C.c_int
         lib.rc_solver_profile.argtypes = [vp, C.c_int, DP, C.c_int]
@@ -205,11 +221,11 @@ def declare(lib: C.CDLL, prefix: str) -> C.CDLL:
 
 
 # Every symbol the header declares (checked by the CPU test suite).
-EXPORTED = ["rc_abi_version", "rc_create", "rc_batch_create", "rc_layer_count", "rc_viscous_resolve_noalloc", "rc_unet_loss_grad", "rc_unet_forward_tc",
+EXPORTED = ["rc_abi_version", "rc_create", "rc_create_generated", "rc_batch_create", "rc_layer_count", "rc_viscous_resolve_noalloc", "rc_unet_loss_grad", "rc_unet_forward_tc",
             "rc_learned_harvest", "rc_learned_harvested", "rc_learned_train", "rc_learned_get_params",
             "rc_learned_set_params", "rc_set_solver", "rc_solver_profile", "rc_viscous_resolve",
             "rc_set_cg_limits", "rc_test_barrier_timeout",
-            "rc_observe_field", "rc_observe_cells", "rc_autotune", "rc_set_cell_threads", "rc_step", "rc_step_async", "rc_wait", "rc_set_phase",
+            "rc_observe_field", "rc_observe_stress", "rc_observe_cells", "rc_autotune", "rc_set_cell_threads", "rc_step", "rc_step_async", "rc_wait", "rc_set_phase",
             "rc_get_sizes", "rc_download", "rc_upload", "rc_download_phi", "rc_upload_phi", "rc_set_stream",
             "rc_set_timing", "rc_timers", "rc_site_count", "rc_last_error", "rc_destroy"]
 

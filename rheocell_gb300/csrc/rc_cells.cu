@@ -386,6 +386,7 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 				const double A = A_c * phi;
 				const double Rep = Rep_c * phi * (p2 - phi * phi);
 				mu = CH + A + Rep + 0.;
+				if(a.fsplit) a.fsplit[4 * a.fsplit_stride + start + q] = 0.0;  // SimpleMultiField sets no pressure
 			}
 			else if(MODEL == M_NEMATIC) {
 				const double lap = pr + pu_ + pl + pd - 4. * phi;
@@ -399,6 +400,7 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 					V = V + (-4 * lambda * omega * sup * phi);
 				}
 				mu = V;
+				if(a.fsplit) a.fsplit[4 * a.fsplit_stride + start + q] = Rep - CH - A;  // ActiveNematic.cpp:225
 			}
 			else {
 				const double lap = pu_ + pd + pr + pl - 4 * phi;
@@ -411,6 +413,7 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 					const double sup = (ls - lsq) / sqrt(1 + (ls - lsq) * (ls - lsq));
 					V = V + (-4 * lambda * omega * sup * phi);
 				}
+				if(a.fsplit) a.fsplit[4 * a.fsplit_stride + start + q] = Rep - CH - A;  // WetModel.cpp:605, WetPolarModel.cpp:298
 				if(MODEL == M_POLAR) {
 					if(pe.beta != 0.0) {
 						const double p0 = 12.;
@@ -464,6 +467,8 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 			if(MODEL == M_SIMPLE) {
 				vx = 0.0;
 				vy = 0.0;
+				if(a.fsplit)
+					for(int f = 0; f < 4; f++) a.fsplit[f * a.fsplit_stride + start + q] = 0.0;
 			}
 			else if(MODEL == M_NEMATIC || MODEL == M_WET) {
 				const int k = box_site(c, x, y, L);
@@ -475,6 +480,13 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 				if(MODEL == M_NEMATIC) {
 					vx = div_rn(mu * dx + fsx * zs + fix * zi, fr, rfr);
 					vy = div_rn(mu * dy + fsy * zs + fiy * zi, fr, rfr);
+					if(a.fsplit) {  // ActiveNematic.cpp:239-240,249-250
+						double *fs = a.fsplit + start + q;
+						fs[0] = mu * dx;
+						fs[a.fsplit_stride] = mu * dy;
+						fs[2 * a.fsplit_stride] = zs * fsx + zi * fix;
+						fs[3 * a.fsplit_stride] = zs * fsy + zi * fiy;
+					}
 				}
 				else {
 					// Passive stress of WetModel.cpp:634-635 from neighbours' mu, f_d and gradients.
@@ -503,6 +515,13 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 					                   - 0.5 * ((dyr * fgxr_y) - (dyl * fgxl_y));
 					const double fx = fpx * alpha + fsx * zs + fix * zi;
 					const double fy = fpy * alpha + fsy * zs + fiy * zi;
+					if(a.fsplit) {  // WetModel.cpp:636-637,655-656
+						double *fs = a.fsplit + start + q;
+						fs[0] = fpx * alpha;
+						fs[a.fsplit_stride] = fpy * alpha;
+						fs[2 * a.fsplit_stride] = zs * fsx + zi * fix;
+						fs[3 * a.fsplit_stride] = zs * fsy + zi * fiy;
+					}
 					if(EVAL == EV_WET_RHS) {
 						a.fxg[start + q] = fx;
 						a.fyg[start + q] = fy;
@@ -527,6 +546,13 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 				const double fsy = lambda * (-dy * c.q01) * th * c.q01;
 				const double fx = fpx * alpha + fsx * zs;
 				const double fy = fpy * alpha + fsy * zs;
+				if(a.fsplit) {  // WetPolarModel.cpp:311-312,325-326
+					double *fs = a.fsplit + start + q;
+					fs[0] = fpx * alpha;
+					fs[a.fsplit_stride] = fpy * alpha;
+					fs[2 * a.fsplit_stride] = zs * fsx;
+					fs[3 * a.fsplit_stride] = zs * fsy;
+				}
 				acc[10] += fx * phi_e;
 				acc[11] += fy * phi_e;
 				if(EVAL == EV_WET_RHS) {

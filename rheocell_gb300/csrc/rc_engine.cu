@@ -128,6 +128,8 @@ struct rc_engine {
 	bool phase_on = false;
 	double *obs_buf = nullptr;               // diagnostic observables scratch
 	size_t obs_cap = 0;
+	double *split_buf = nullptr;             // force split of an observation: 5 x S_cap
+	CellDev *cells_save = nullptr;           // cell records kept aside while it is formed
 	// viscous solve limits (rc_set_cg_limits) and the barrier test hook
 	long long cg_max_iters = 0;
 	int cg_fail_noconv = 0;
@@ -671,15 +673,72 @@ extern "C" {
 
 int rc_abi_version(void) { return RC_ABI_VERSION; }
 
+}  // extern "C"
+
+// Fills each cell's patch with the generated profile (one block per cell):
+// RC_PROFILE_TANH: phi = (1 - tanh((d - radius) / width)) / 2, d the distance
+// from the box site to the cell's centre (nearest periodic image);
+// RC_PROFILE_DISC: the reference's initial disc (MultiPhaseField::init,
+// MultiPhaseField.cpp:149-156), phi = 1 where x^2 + y^2 < radius^2 + 0.5 with
+// x = LsubX/2 - (q mod LsubX), y = LsubY/2 - q / LsubX (integer division).
+__global__ void generate_phi_kernel(const CellDev *cells, double *phi, rc_generate_spec g, int L) {
+	const CellDev &c = cells[blockIdx.x];
+	double *out = phi + c.start;
+	for(int q = threadIdx.x; q < c.n; q += blockDim.x) {
+		const int sy = q / c.lx, sx = q - sy * c.lx;
+		double v;
+		if(g.profile == RC_PROFILE_DISC) {
+			const int x = c.lx / 2 - sx, y = c.ly / 2 - sy;
+			v = (double) (x * x + y * y) < g.radius * g.radius + 0.5 ? 1.0 : 0.0;
+		}
+		else {
+			const int k = box_site(c, sx, sy, L);
+			const int by = k / L, bx = k - by * L;
+			double dx = (double) bx - c.comx, dy = (double) by - c.comy;
+			dx -= L * rint(dx / L);
+			dy -= L * rint(dy / L);
+			const double d = sqrt(dx * dx + dy * dy);
+			v = 0.5 * (1.0 - tanh((d - g.radius) / g.width));
+		}
+		out[q] = v;
+	}
+}
+
+static int create_engine(const rc_params *params, int n_layers, const rc_box *boxes, const int *n_cells_per_layer,
+                         const rc_cell_host *cells, const unsigned long long *rng_states, int device, rc_engine **out,
+                         const rc_generate_spec *gen);
+
+extern "C" {
+
 int rc_create(const rc_params *params, const rc_box *box, int n_cells, const rc_cell_host *cells, int device,
               rc_engine **out) {
 	if(!params) return set_err(nullptr, RC_ERR_INVALID, "invalid arguments");
 	const unsigned long long rs = params->rng_state;
-	return rc_batch_create(params, 1, box, &n_cells, cells, &rs, device, out);
+	return create_engine(params, 1, box, &n_cells, cells, &rs, device, out, nullptr);
+}
+
+int rc_create_generated(const rc_params *params, const rc_box *box, int n_cells, const rc_cell_host *cells,
+                        const rc_generate_spec *spec, int device, rc_engine **out) {
+	if(out) *out = nullptr;
+	if(!params || !spec) return set_err(nullptr, RC_ERR_INVALID, "invalid arguments");
+	if(spec->profile != RC_PROFILE_TANH && spec->profile != RC_PROFILE_DISC)
+		return set_err(nullptr, RC_ERR_INVALID, "rc_create_generated: unknown profile %d", spec->profile);
+	if(!(spec->radius > 0.0) || (spec->profile == RC_PROFILE_TANH && !(spec->width > 0.0)))
+		return set_err(nullptr, RC_ERR_INVALID, "rc_create_generated: radius and width must be positive");
+	const unsigned long long rs = params->rng_state;
+	return create_engine(params, 1, box, &n_cells, cells, &rs, device, out, spec);
 }
 
 int rc_batch_create(const rc_params *params, int n_layers, const rc_box *boxes, const int *n_cells_per_layer,
                     const rc_cell_host *cells, const unsigned long long *rng_states, int device, rc_engine **out) {
+	return create_engine(params, n_layers, boxes, n_cells_per_layer, cells, rng_states, device, out, nullptr);
+}
+
+}  // extern "C"
+
+static int create_engine(const rc_params *params, int n_layers, const rc_box *boxes, const int *n_cells_per_layer,
+                         const rc_cell_host *cells, const unsigned long long *rng_states, int device, rc_engine **out,
+                         const rc_generate_spec *gen) {
 	if(!out) return set_err(nullptr, RC_ERR_INVALID, "out is NULL");
 	*out = nullptr;
 	if(!params || !boxes || !n_cells_per_layer || n_layers < 1)
@@ -733,7 +792,7 @@ int rc_batch_create(const rc_params *params, int n_layers, const rc_box *boxes, 
 			if(h.offset_x < 0 || h.offset_x >= h.lsub_x || h.offset_y < 0 || h.offset_y >= h.lsub_y)
 				return set_err(nullptr, RC_ERR_INVALID, "cell %d: offset out of range", i);
 			if(h.corner < 0 || h.corner >= L * L) return set_err(nullptr, RC_ERR_INVALID, "cell %d: corner out of box", i);
-			if(!h.phi) return set_err(nullptr, RC_ERR_INVALID, "cell %d: phi is NULL", i);
+			if(!h.phi && !gen) return set_err(nullptr, RC_ERR_INVALID, "cell %d: phi is NULL", i);
 			S += (long long) h.lsub_x * h.lsub_y;
 			max_n = std::max(max_n, h.lsub_x * h.lsub_y);
 		}
@@ -867,13 +926,13 @@ int rc_batch_create(const rc_params *params, int n_layers, const rc_box *boxes, 
 	// cells and fields
 	{
 		std::vector<CellDev> hc((size_t) std::max(n_cells, 1));
-		std::vector<double> phi((size_t) S);
+		std::vector<double> phi(gen ? 0 : (size_t) S);
 		long long start = 0;
 		for(int i = 0; i < n_cells; i++) {
 			int layer = 0;
 			while(layer + 1 < n_layers && i >= layers[(size_t) layer].cell_hi) layer++;
 			host_cell(cells[i], hc[i], (int) start, layer);
-			memcpy(&phi[(size_t) start], cells[i].phi, sizeof(double) * (size_t) hc[i].n);
+			if(!gen) memcpy(&phi[(size_t) start], cells[i].phi, sizeof(double) * (size_t) hc[i].n);
 			start += hc[i].n;
 		}
 		CUDA_TRY(e, cudaMemcpy(e->cells, hc.data(), sizeof(CellDev) * (size_t) std::max(n_cells, 1), cudaMemcpyHostToDevice));
@@ -885,7 +944,11 @@ int rc_batch_create(const rc_params *params, int n_layers, const rc_box *boxes, 
 				for(int b = 0; b < layers[(size_t) l].nbx * layers[(size_t) l].nby; b++) bl[(size_t) (layers[(size_t) l].bin_off + b)] = l;
 			CUDA_TRY(e, cudaMemcpy(e->bin_layer, bl.data(), sizeof(int) * (size_t) total_bins, cudaMemcpyHostToDevice));
 		}
-		if(S) CUDA_TRY(e, cudaMemcpy(e->phiA, phi.data(), sizeof(double) * (size_t) S, cudaMemcpyHostToDevice));
+		if(S && !gen) CUDA_TRY(e, cudaMemcpy(e->phiA, phi.data(), sizeof(double) * (size_t) S, cudaMemcpyHostToDevice));
+		if(S && gen) {
+			generate_phi_kernel<<<n_cells, 256, 0, e->stream>>>(e->cells, e->phiA, *gen, L);
+			CUDA_TRY(e, cudaGetLastError());
+		}
 		DevStatus h;
 		memset(&h, 0, sizeof(h));
 		h.S = S;
@@ -905,6 +968,8 @@ int rc_batch_create(const rc_params *params, int n_layers, const rc_box *boxes, 
 	*out = e;
 	return RC_OK;
 }
+
+extern "C" {
 
 int rc_step(rc_engine *e, int n_steps, rc_step_stats *stats) {
 	if(!e) return RC_ERR_INVALID;
@@ -1578,20 +1643,77 @@ static int obs_scratch(rc_engine *e, size_t n) {
 	return RC_OK;
 }
 
+// The last force evaluation formed again with its force split recorded in
+// split_buf (Fpassive x/y, Factive x/y, Pressure per site, stride S_cap), the
+// way the reference's interactions leave them in BaseField for its
+// ForceField and StressField observables.  The re-evaluation reads the
+// current phi and box sums and rewrites mu, gradients, the map and the
+// forces (or dry velocities) with the values they already hold; the polar
+// Repulsion accumulator is not advanced, and the cell records are put back,
+// so the engine's trajectory is unchanged.
+static int observe_split(rc_engine *e) {
+	if(e->hp.precision == RC_PRECISION_FLOAT)
+		return set_err(e, RC_ERR_UNSUPPORTED, "force observables are formed by the FP64 cell kernels only");
+	int rc;
+	if(!e->split_buf && (rc = dalloc(e, &e->split_buf, 5 * (size_t) e->S_cap))) return rc;
+	if(!e->cells_save && (rc = dalloc(e, &e->cells_save, (size_t) std::max(e->N, 1)))) return rc;
+	if(e->N == 0) return RC_OK;
+	CUDA_TRY(e, cudaMemcpyAsync(e->cells_save, e->cells, sizeof(CellDev) * (size_t) e->N, cudaMemcpyDeviceToDevice, e->stream));
+	CellArgs a = cell_args(e);
+	a.phi_eval = e->phiA;
+	a.pe = e->ph[e->eval_phase];
+	a.pu = e->ph[e->eval_phase];
+	a.accumulate_rep = 0;
+	a.fsplit = e->split_buf;
+	a.fsplit_stride = e->S_cap;
+	cell_launch(e, wet_phase(e, e->eval_phase) ? EV_WET_RHS : EV_STORE, UP_NONE, a, e->stream);
+	CUDA_TRY(e, cudaGetLastError());
+	CUDA_TRY(e, cudaMemcpyAsync(e->cells, e->cells_save, sizeof(CellDev) * (size_t) e->N, cudaMemcpyDeviceToDevice, e->stream));
+	return RC_OK;
+}
+
+// Box fields (f0, f1) of an observable kind into the scratch area.
+static int observe_box_fields(rc_engine *e, int kind, int layer, int only_type, double *f0, double *f1) {
+	const LayerDev &lay = e->layers_h[(size_t) layer];
+	if(kind <= RC_OBS_NEMATIC) {
+		materialise(e, 0);  // current velocities (dry models)
+		launch_obs_field(e->cells, e->layers, lay, e->bin_count, e->bin_cells, e->phiA, e->vx, e->vy, kind, layer,
+		                 only_type, f0, f1, e->stream);
+		return RC_OK;
+	}
+	int rc;
+	if((rc = observe_split(e))) return rc;
+	const double *sp = e->split_buf;
+	const size_t st = (size_t) e->S_cap;
+	if(kind == RC_OBS_FORCE) {
+		// get_total_force_x/y: the velocity times the interaction's friction
+		launch_obs_sites(e->cells, e->layers, lay, e->bin_count, e->bin_cells, e->phiA, e->vx, e->vy,
+		                 e->ph[e->phase].friction, layer, only_type, f0, f1, e->stream);
+	}
+	else if(kind == RC_OBS_FORCE_PASSIVE || kind == RC_OBS_FORCE_ACTIVE) {
+		const double *g = sp + (kind == RC_OBS_FORCE_PASSIVE ? 0 : 2) * st;
+		launch_obs_sites(e->cells, e->layers, lay, e->bin_count, e->bin_cells, e->phiA, g, g + st, 1.0, layer,
+		                 only_type, f0, f1, e->stream);
+	}
+	else {
+		launch_obs_sites(e->cells, e->layers, lay, e->bin_count, e->bin_cells, e->phiA, sp + 4 * st, nullptr, 1.0, layer,
+		                 only_type, f0, f1, e->stream);
+	}
+	return RC_OK;
+}
+
 int rc_observe_field(rc_engine *e, int kind, int layer, int only_type, int size_grid, double *fx, double *fy,
                      double *coarse_x, double *coarse_y) {
 	if(!e || !fx || !fy) return RC_ERR_INVALID;
-	if(kind < RC_OBS_VELOCITY || kind > RC_OBS_NEMATIC) return set_err(e, RC_ERR_INVALID, "rc_observe_field: kind %d", kind);
+	if(kind < RC_OBS_VELOCITY || kind > RC_OBS_PRESSURE) return set_err(e, RC_ERR_INVALID, "rc_observe_field: kind %d", kind);
 	if(layer < 0 || layer >= e->n_layers) return set_err(e, RC_ERR_INVALID, "rc_observe_field: layer %d", layer);
 	CUDA_TRY(e, cudaSetDevice(e->device));
 	const LayerDev &lay = e->layers_h[(size_t) layer];
 	const size_t L2 = (size_t) lay.L * lay.L;
 	int rc;
 	if((rc = obs_scratch(e, 4 * L2))) return rc;
-	materialise(e, 0);  // current velocities (dry models)
 	double *f0 = e->obs_buf, *f1 = f0 + L2, *c0 = f1 + L2, *c1 = c0 + L2;
-	launch_obs_field(e->cells, e->layers, lay, e->bin_count, e->bin_cells, e->phiA, e->vx, e->vy, kind, layer, only_type,
-	                 f0, f1, e->stream);
+	if((rc = observe_box_fields(e, kind, layer, only_type, f0, f1))) return rc;
 	if(size_grid > 0) {
 		launch_obs_coarse(f0, c0, lay.L, size_grid, e->stream);
 		launch_obs_coarse(f1, c1, lay.L, size_grid, e->stream);
@@ -1601,6 +1723,30 @@ int rc_observe_field(rc_engine *e, int kind, int layer, int only_type, int size_
 	CUDA_TRY(e, cudaMemcpyAsync(fy, f1, sizeof(double) * L2, cudaMemcpyDeviceToHost, e->stream));
 	if(size_grid > 0 && coarse_x) CUDA_TRY(e, cudaMemcpyAsync(coarse_x, c0, sizeof(double) * L2, cudaMemcpyDeviceToHost, e->stream));
 	if(size_grid > 0 && coarse_y) CUDA_TRY(e, cudaMemcpyAsync(coarse_y, c1, sizeof(double) * L2, cudaMemcpyDeviceToHost, e->stream));
+	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+	return RC_OK;
+}
+
+int rc_observe_stress(rc_engine *e, int kind, int layer, int only_type, int size_grid, double *xx, double *yy,
+                      double *xy) {
+	if(!e || !xx || !yy) return RC_ERR_INVALID;
+	if(kind < RC_OBS_FORCE || kind > RC_OBS_PRESSURE) return set_err(e, RC_ERR_INVALID, "rc_observe_stress: kind %d", kind);
+	if(layer < 0 || layer >= e->n_layers) return set_err(e, RC_ERR_INVALID, "rc_observe_stress: layer %d", layer);
+	if(size_grid < 1) return set_err(e, RC_ERR_INVALID, "rc_observe_stress: size_grid %d", size_grid);
+	CUDA_TRY(e, cudaSetDevice(e->device));
+	const LayerDev &lay = e->layers_h[(size_t) layer];
+	const size_t L2 = (size_t) lay.L * lay.L;
+	int rc;
+	if((rc = obs_scratch(e, 5 * L2))) return rc;
+	double *f0 = e->obs_buf, *f1 = f0 + L2, *o0 = f1 + L2, *o1 = o0 + L2, *o2 = o1 + L2;
+	if((rc = observe_box_fields(e, kind, layer, only_type, f0, f1))) return rc;
+	const bool pressure = kind == RC_OBS_PRESSURE;
+	// pressure: both components come from the pressure field (StressField.cpp:192-193)
+	launch_obs_stress(f0, pressure ? f0 : f1, o0, o1, pressure ? nullptr : o2, lay.L, size_grid, e->stream);
+	CUDA_TRY(e, cudaGetLastError());
+	CUDA_TRY(e, cudaMemcpyAsync(xx, o0, sizeof(double) * L2, cudaMemcpyDeviceToHost, e->stream));
+	CUDA_TRY(e, cudaMemcpyAsync(yy, o1, sizeof(double) * L2, cudaMemcpyDeviceToHost, e->stream));
+	if(xy && !pressure) CUDA_TRY(e, cudaMemcpyAsync(xy, o2, sizeof(double) * L2, cudaMemcpyDeviceToHost, e->stream));
 	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
 	return RC_OK;
 }

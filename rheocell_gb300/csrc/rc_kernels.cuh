@@ -49,6 +49,12 @@ struct CellArgs {
 	PhaseParams pu;        // parameters of the update (directed active forces)
 	int rep_on;            // track the polar Repulsion accumulator
 	int accumulate_rep;    // this evaluation adds to it (not a re-evaluation for download)
+	// force split of an observation (null otherwise): per site, at
+	// fsplit + f * fsplit_stride + start + q, f = 0..4: Fpassive_x, Fpassive_y,
+	// Factive_x, Factive_y, Pressure (BaseField members the reference's
+	// interactions fill, e.g. WetModel.cpp:605,636-637,655-656)
+	double *fsplit;
+	long long fsplit_stride;
 };
 
 struct BoxArgs {
@@ -141,6 +147,10 @@ void launch_obs_field(const CellDev *cells, const LayerDev *layers, const LayerD
                       const int *bin_cells, const double *phi, const double *vx, const double *vy, int kind, int layer,
                       int only_type, double *fx, double *fy, cudaStream_t s);
 void launch_obs_coarse(const double *f, double *out, int L, int sg, cudaStream_t s);
+void launch_obs_sites(const CellDev *cells, const LayerDev *layers, const LayerDev &lay_h, const int *bin_count,
+                      const int *bin_cells, const double *phi, const double *g0, const double *g1, double scale, int layer,
+                      int only_type, double *fx, double *fy, cudaStream_t s);
+void launch_obs_stress(const double *fx, const double *fy, double *xx, double *yy, double *xy, int L, int sg, cudaStream_t s);
 void launch_obs_cells(const CellDev *cells, const LayerDev *layers, int N, int n_layers, const double *dxg,
                       const double *dyg, double *cell_obs, double *layer_obs, cudaStream_t s);
 cudaError_t launch_cg(const CGArgs &a, int blocks, cudaStream_t s);

@@ -31,9 +31,15 @@ struct ObsArgs {
 	const double *phi, *vx, *vy;
 	int kind, layer, only_type;
 	double *fx, *fy;
+	double scale;  // OBS_SITES: per-site values are multiplied by it first
 };
 
-enum { OBS_VELOCITY = 0, OBS_SHAPE = 1, OBS_NEMATIC = 2 };
+// OBS_SITES: f0 += (vx[j] * scale) * phi, f1 += (vy[j] * scale) * phi, or
+// f1 += phi when vy is null -- ForceField / StressField::calc_field
+// (ForceField.cpp:79-96, StressField.cpp:84-100): total force (v times the
+// friction, get_total_force_x/y), passive and active forces, pressure with
+// the phi field.
+enum { OBS_VELOCITY = 0, OBS_SHAPE = 1, OBS_NEMATIC = 2, OBS_SITES = 3 };
 
 __global__ void __launch_bounds__(BIN_X *BIN_Y) obs_field_kernel(const ObsArgs a) {
 	__shared__ int s_ids[BIN_CAP];
@@ -92,6 +98,10 @@ __global__ void __launch_bounds__(BIN_X *BIN_Y) obs_field_kernel(const ObsArgs a
 			f0 += a.vx[j] * phi;
 			f1 += a.vy[j] * phi;
 		}
+		else if(a.kind == OBS_SITES) {
+			f0 += (a.vx[j] * a.scale) * phi;
+			f1 += a.vy ? (a.vy[j] * a.scale) * phi : phi;
+		}
 		else {
 			f0 += s_g0[i] * phi;
 			f1 += s_g1[i] * phi;
@@ -116,6 +126,40 @@ __global__ void obs_coarse_kernel(const double *f, double *out, int L, int sg) {
 			acc += f[xx + yy * L] / den;
 		}
 	out[site] = acc;
+}
+
+// StressField's coarse stress (StressField.cpp:171-199): per site, over the
+// size_grid^2 window in the reference's order (rows outer, columns inner),
+// with r the periodic offset of the window site from the centre and
+// e = -r / |r| (the centre itself skipped):
+//   xx += fx * ex / sg^2, yy += fy * ey / sg^2,
+//   xy += (fx * ey + fy * ex) / (2 sg^2)  (xy null: not formed).
+__global__ void obs_stress_kernel(const double *fx, const double *fy, double *xx, double *yy, double *xy, int L, int sg) {
+	const int site = blockIdx.x * blockDim.x + threadIdx.x;
+	if(site >= L * L) return;
+	const int i = site / L, j = site - (site / L) * L;
+	double axx = 0.0, ayy = 0.0, axy = 0.0;
+	for(int k = 0; k < sg; k++)
+		for(int l = 0; l < sg; l++) {
+			const int xx_ = (((j - sg / 2 + L) % L) + l) % L;
+			const int yy_ = (((i - sg / 2 + L) % L) + k) % L;
+			const int ss = xx_ + yy_ * L;
+			double rx = j - xx_, ry = i - yy_;
+			if(rx >= L / 2) rx -= L;
+			if(rx <= -L / 2) rx += L;
+			if(ry >= L / 2) ry -= L;
+			if(ry <= -L / 2) ry += L;
+			const double r = sqrt(rx * rx + ry * ry);
+			if(r != 0) {
+				const double ex = -rx / r, ey = -ry / r;
+				axx += (fx[ss] * ex) / (sg * sg);
+				ayy += (fy[ss] * ey) / (sg * sg);
+				if(xy) axy += ((fx[ss] * ey + fy[ss] * ex)) / (2 * sg * sg);
+			}
+		}
+	xx[site] = axx;
+	yy[site] = ayy;
+	if(xy) xy[site] = axy;
 }
 
 // Per-cell statistics (one CTA per cell): x, y, area, elongation, aspect, theta.
@@ -190,7 +234,32 @@ void launch_obs_field(const CellDev *cells, const LayerDev *layers, const LayerD
 	a.only_type = only_type;
 	a.fx = fx;
 	a.fy = fy;
+	a.scale = 1.0;
 	obs_field_kernel<<<lay_h.nbx * lay_h.nby, BIN_X * BIN_Y, 0, s>>>(a);
+}
+
+void launch_obs_sites(const CellDev *cells, const LayerDev *layers, const LayerDev &lay_h, const int *bin_count,
+                      const int *bin_cells, const double *phi, const double *g0, const double *g1, double scale, int layer,
+                      int only_type, double *fx, double *fy, cudaStream_t s) {
+	ObsArgs a;
+	a.cells = cells;
+	a.layers = layers;
+	a.bin_count = bin_count;
+	a.bin_cells = bin_cells;
+	a.phi = phi;
+	a.vx = g0;
+	a.vy = g1;
+	a.kind = OBS_SITES;
+	a.layer = layer;
+	a.only_type = only_type;
+	a.fx = fx;
+	a.fy = fy;
+	a.scale = scale;
+	obs_field_kernel<<<lay_h.nbx * lay_h.nby, BIN_X * BIN_Y, 0, s>>>(a);
+}
+
+void launch_obs_stress(const double *fx, const double *fy, double *xx, double *yy, double *xy, int L, int sg, cudaStream_t s) {
+	obs_stress_kernel<<<(L * L + 255) / 256, 256, 0, s>>>(fx, fy, xx, yy, xy, L, sg);
 }
 
 void launch_obs_coarse(const double *f, double *out, int L, int sg, cudaStream_t s) {

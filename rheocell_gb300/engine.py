@@ -67,6 +67,31 @@ class Engine:
         self.stats = abi.RcStepStats()
 
     @classmethod
+    def generated(cls, params: abi.RcParams, L: int, cells: HostCells, profile: int, radius: float,
+                  width: float = 1.0, device: int = 0) -> "Engine":
+        """A monolayer whose patches' phi is generated on the device
+        (rc_create_generated); `cells` gives the geometry, centres and Q
+        (their phi pointers are not read)."""
+        self = cls.__new__(cls)
+        self._lib = lib()
+        self.h = C.c_void_p()
+        spec = abi.RcGenerateSpec(profile, radius, width)
+        rc = self._lib.rc_create_generated(C.byref(params), C.byref(abi.RcBox(L, L)), cells.n, cells.arr,
+                                           C.byref(spec), device, C.byref(self.h))
+        if rc != 0:
+            msg = self._lib.rc_last_error(self.h).decode()
+            if self.h:
+                self._lib.rc_destroy(self.h)
+            self.h = None
+            raise EngineError(rc, msg)
+        self.n = cells.n
+        self.L = L
+        self.device = device
+        self.layer_sizes = [cells.n]
+        self.stats = abi.RcStepStats()
+        return self
+
+    @classmethod
     def batch(cls, params: abi.RcParams, layers, device: int = 0) -> "Engine":
         """An ensemble of independent monolayers advanced together
         (rc_batch_create).  `layers` is a list of (L, HostCells, rng_state);

@@ -215,3 +215,25 @@ def write_case(directory: str, m: Monolayer, params: Dict[str, object], steps: i
     inp = os.path.join(directory, "input")
     write_input(inp, params, steps, seed=seed, equilibration_steps=equilibration_steps, extra=extra)
     return inp
+
+
+def case_keys(m: Monolayer, params: Dict[str, object], seed: int = 1,
+              extra: Optional[Dict[str, object]] = None):
+    """(input keys, monolayer) of a run of `m` with interaction `params`: the
+    keys as strings with `seed` and the square box, and the monolayer as the
+    reference reads it back from its configuration file (15-digit text)."""
+    import shutil
+    import tempfile
+    keys = {k: str(v) for k, v in params.items()}
+    keys["seed"] = str(seed)
+    keys.setdefault("box", "square")
+    if extra:
+        keys.update({k: str(v) for k, v in extra.items()})
+    d = tempfile.mkdtemp(prefix="rc_case_")
+    try:
+        write_conf(os.path.join(d, "conf"), m)
+        m2 = read_conf(os.path.join(d, "conf"))
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    m2.types = list(m.types)
+    return keys, m2

@@ -232,3 +232,14 @@ def read_input(path: str, overrides: Optional[Dict[str, object]] = None) -> Dict
     for k, v in (overrides or {}).items():
         keys[k] = str(v)
     return keys
+
+
+def engine_inputs(keys: Dict[str, object], m: Monolayer,
+                  precision: int = abi.RC_PRECISION_DOUBLE) -> Tuple[abi.RcParams, HostCells]:
+    """rc_params and host cells of a monolayer as the reference's SimBackend
+    would set them up from `keys` (srand48(seed), then the configuration's
+    draws), with drand48's state handed to the device's noise stream."""
+    p = make_params(keys, precision=precision)
+    cells, rng = make_cells(m, keys, int(keys.get("seed", 1)))
+    attach_rng(p, rng)
+    return p, cells

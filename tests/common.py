@@ -32,25 +32,9 @@ def case_from_texts(input_text: str, conf_text: str, topo_text: str):
     return keys, m
 
 
-def build_inputs(keys, m, precision=abi.RC_PRECISION_DOUBLE):
-    p = host.make_params(keys, precision=precision)
-    cells, rng = host.make_cells(m, keys, int(keys.get("seed", 1)))
-    host.attach_rng(p, rng)
-    return p, cells
-
-
-def case_from_monolayer(m, params: Dict[str, object], seed: int = 1, extra=None):
-    keys = {k: str(v) for k, v in params.items()}
-    keys["seed"] = str(seed)
-    keys.setdefault("box", "square")
-    if extra:
-        keys.update({k: str(v) for k, v in extra.items()})
-    # round-trip through the text format so both sides see the file's values
-    d = tempfile.mkdtemp(prefix="rc_case_")
-    g.write_conf(os.path.join(d, "conf"), m)
-    m2 = g.read_conf(os.path.join(d, "conf"))
-    m2.types = list(m.types)
-    return keys, m2
+# case set-up shared with bench.py (rheocell_gb300.host / .generator)
+build_inputs = host.engine_inputs
+case_from_monolayer = g.case_keys
 
 
 def run(sim_factory, keys, m, steps: List[int], eq: int = 0, precision=abi.RC_PRECISION_DOUBLE):

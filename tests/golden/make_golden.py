@@ -10,8 +10,8 @@ its state dumps as compressed .npz files:
   * at the last recorded step also vx, vy, mu and the box map.
 
 Run from the repository root:  python tests/golden/make_golden.py
-(needs oracle/_ref, i.e. `make -C oracle`; only this container has the
-reference sources).
+(needs the reference built out of tree, `make -C oracle REF_SRC=<reference>/src`;
+only a machine with the reference's sources can run it).
 """
 from __future__ import annotations
 
@@ -269,6 +269,42 @@ def record_confgenerator():
     np.savez_compressed(os.path.join(HERE, "confgenerator.npz"), **out)
 
 
+# field observables of the reference (ForceField, StressField) after `step`
+# main-loop steps: name -> (monolayer kwargs, params, step, seed, size_grid)
+OBS_CASES = {
+    "obs_wet": (dict(L=36, n=4, seed=41, **SMALL), WET_S, 2, 51, 3),
+    "obs_wetpolar": (dict(L=36, n=4, seed=42, **SMALL), WETPOLAR_S, 2, 52, 3),
+    "obs_nematic": (dict(L=36, n=4, seed=43, types=[0, 1, 1, 0], **SMALL), NEMATIC_S, 2, 53, 4),
+    "obs_polar": (dict(L=36, n=4, seed=44, **SMALL), dict(DRY_POLAR_S, J_Q=0.3), 2, 54, 3),
+}
+
+
+def record_observables(name):
+    """The reference's own ForceField and StressField output strings (its
+    observable classes, driven by oracle/ref_driver.cpp's observe mode) as
+    number arrays after the two header lines."""
+    mkw, params, step, seed, sg = OBS_CASES[name]
+    m = monolayer(mkw)
+    d = tempfile.mkdtemp(prefix="rc_golden_")
+    out = {}
+    try:
+        g.write_case(d, m, params, steps=step, seed=seed)
+        for kind in ("force_field", "stress_field"):
+            res = subprocess.run([refdump.driver_path("exact"), "observe", kind + ".txt", "%d:%s:%d" % (step, kind, sg),
+                                  "input"], cwd=d, capture_output=True, text=True)
+            if res.returncode != 0:
+                raise RuntimeError(res.stderr[-2000:])
+            lines = open(os.path.join(d, kind + ".txt")).read().split("\n", 2)
+            out[kind] = np.array(lines[2].split(), dtype=np.float64)
+        for f, k in (("start_conf.dat", "conf"), ("topology.top", "topology"), ("input", "input")):
+            out[k] = np.array(open(os.path.join(d, f)).read())
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    out["step"] = np.array(step)
+    out["size_grid"] = np.array(sg)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+
+
 def main():
     if not refdump.have_reference("exact"):
         subprocess.check_call(["make", "-C", os.path.join(ROOT, "oracle"), "-j8"])
@@ -292,6 +328,11 @@ def main():
         sz = os.path.getsize(os.path.join(HERE, name + ".npz"))
         print("%-12s steps %s  cells %d  sizes %s  %.0f KB" % (name, [r["step"] for r in recs], recs[0]["N"],
                                                                 sorted(set(zip(recs[-1]["lx"], recs[-1]["ly"]))), sz / 1024))
+    for name in OBS_CASES:
+        if only and name not in only:
+            continue
+        record_observables(name)
+        print("%-12s %.0f KB" % (name, os.path.getsize(os.path.join(HERE, name + ".npz")) / 1024))
     if only:
         return
     print("overlap", record_overlap())
