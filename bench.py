@@ -200,19 +200,27 @@ def prepare_learned(args, eng, lib):
     # samples come from this monolayer's own plain solve, or from a smaller
     # monolayer of the same physics (--train-workload): the network is
     # convolutional, so parameters trained there apply at any box side
-    own = not args.train_workload or args.train_workload == args.workload
-    src = eng if own else make_engine(args.train_workload, abi.RC_PRECISION_DOUBLE, eng.device)
-    src.harvest(capacity=args.harvest_capacity, every=3, per_solve=6)
-    t0 = time.perf_counter()
-    src.step(args.harvest_steps)
-    harvest_s = time.perf_counter() - t0
-    n = src.harvested()
-    src.harvest(args.harvest_capacity, 3, 0)  # stop collecting, keep the samples
-    rep = src.train(epochs=args.train_epochs, batch=8, learning_rate=args.train_lr, seed=1,
-                    learning_rate_final=args.train_lr * args.train_lr_final, max_samples=args.train_max_samples)
-    if src is not eng:
-        eng.set_params(src.get_params())
-        src.close()
+    import numpy as np
+    if args.load_params:
+        # parameters of an earlier training (set-up shortcut for experiments)
+        eng.set_params(np.loadtxt(args.load_params))
+        harvest_s, n, rep = 0.0, 0, {"loaded_from": os.path.basename(args.load_params)}
+    else:
+        own = not args.train_workload or args.train_workload == args.workload
+        src = eng if own else make_engine(args.train_workload, abi.RC_PRECISION_DOUBLE, eng.device)
+        src.harvest(capacity=args.harvest_capacity, every=3, per_solve=6)
+        t0 = time.perf_counter()
+        src.step(args.harvest_steps)
+        harvest_s = time.perf_counter() - t0
+        n = src.harvested()
+        src.harvest(args.harvest_capacity, 3, 0)  # stop collecting, keep the samples
+        rep = src.train(epochs=args.train_epochs, batch=8, learning_rate=args.train_lr, seed=1,
+                        learning_rate_final=args.train_lr * args.train_lr_final, max_samples=args.train_max_samples)
+        if src is not eng:
+            eng.set_params(src.get_params())
+            src.close()
+    if args.save_params:
+        np.savetxt(args.save_params, eng.get_params(), fmt="%.17g")
     k = max(2, min(args.steps, 10))
     plain_ms, plain_it, plain_res = solve_stage(eng, lib, k, flush)
     eng.set_solver(abi.RC_SOLVER_LEARNED)
@@ -226,8 +234,9 @@ def prepare_learned(args, eng, lib):
         for _ in range(k):
             lib.rc_step_async(eng.h, 1)
         torch.cuda.synchronize()
-        ms = (C.c_double * 15)()
-        lib.rc_solver_profile(eng.h, 0, ms, 15)
+        nph = len(abi.SOLVER_PHASES)
+        ms = (C.c_double * nph)()
+        lib.rc_solver_profile(eng.h, 0, ms, nph)
         phases = {nm: round(ms[i] / k, 4) for i, nm in enumerate(abi.SOLVER_PHASES)}
     return {"harvest_steps": args.harvest_steps, "harvest_s": harvest_s, "samples": n,
             "trained_on": args.train_workload or args.workload,
@@ -622,6 +631,8 @@ def main():
     ap.add_argument("--train-workload", default="wet256", choices=["wet256", "wet512", "wet1024"],
                     help="harvest and train on this monolayer (the network transfers to the timed one)")
     ap.add_argument("--train-max-samples", type=int, default=0, help="train on at most this many samples (0: all)")
+    ap.add_argument("--save-params", default=None, help="write the trained network parameters to this file")
+    ap.add_argument("--load-params", default=None, help="use these network parameters instead of training")
     ap.add_argument("--train-lr", type=float, default=2e-3)
     ap.add_argument("--train-lr-final", type=float, default=0.05, help="final step size as a fraction of --train-lr")
     args = ap.parse_args()

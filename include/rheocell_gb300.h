@@ -471,7 +471,10 @@ int rc_test_barrier_timeout(rc_engine *e, long long spin_limit, int unreachable)
  * gather, first layer, tensor-core layers at levels 0, 1, 2, last layer,
  * preconditioned residual, flexible-CG phases A, B, C, everything else,
  * then (within the tensor-core layers) weight staging, operand staging,
- * MMA issue and completion, epilogue.  No counterpart in the reference.
+ * MMA issue and completion, epilogue as one write-out thread sees them, the
+ * MMA thread's waits (row staged, accumulator slot free) and issue, and one
+ * staging thread's waits (buffer free) and loads.  No counterpart in the
+ * reference.
  */
 int rc_solver_profile(rc_engine *e, int enable, double *ms, int n);
 
@@ -494,6 +497,12 @@ int rc_solver_profile(rc_engine *e, int enable, double *ms, int n);
  * (e.g. WetModel.cpp:636-637,655-656); RC_OBS_PRESSURE the pressure
  * Rep - CH - A (WetModel.cpp:605) in fx and the phi field in fy.  Their
  * coarse fields are ForceField's window means (ForceField.cpp:141-160).
+ * RC_OBS_THERMO, RC_OBS_THERMO_XY and RC_OBS_CHEMPOT2 are the unweighted box
+ * sums of ThermodynamicStressField::calc_field (ThermodynamicStressField.cpp:
+ * 75-99): xx and yy of f_d - mu phi + d phi g (g = 2 gamma lambda grad(phi)
+ * where the interaction sets it, WetModel.cpp:607-609, SimpleMultiField.cpp:
+ * 178-180), then xy = d_x phi g_y with the sum of mu, then the sums of mu^2
+ * and phi; their coarse fields are its window means (:131-150).
  * The split is formed by evaluating the forces again at the current state,
  * which leaves the simulation unchanged (FP64 engines only).
  *
@@ -518,6 +527,9 @@ int rc_solver_profile(rc_engine *e, int enable, double *ms, int n);
 #define RC_OBS_FORCE_PASSIVE 4
 #define RC_OBS_FORCE_ACTIVE 5
 #define RC_OBS_PRESSURE 6
+#define RC_OBS_THERMO 7      /* ThermodynamicStressField xx, yy */
+#define RC_OBS_THERMO_XY 8   /* ThermodynamicStressField xy, sum of mu */
+#define RC_OBS_CHEMPOT2 9    /* ThermodynamicStressField sum of mu^2, sum of phi */
 int rc_observe_field(rc_engine *e, int kind, int layer, int only_type, int size_grid, double *fx, double *fy,
                      double *coarse_x, double *coarse_y);
 int rc_observe_stress(rc_engine *e, int kind, int layer, int only_type, int size_grid, double *xx, double *yy,

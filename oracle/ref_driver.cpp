@@ -15,7 +15,8 @@
 //   ref_driver time  <n_steps>             <input> [key=value ...]
 //   ref_driver observe <out.txt> <step>:<type>:<size_grid> <input> [key=value ...]
 //     after <step> main-loop steps, the output string of the reference's
-//     own field observable <type> (force_field or stress_field) with that
+//     own field observable <type> (force_field, stress_field or
+//     thermodynamic_stress_field) with that
 //     size_grid, as its ObservableOutput would print it
 //
 // Dump record layout (little endian), one record per requested step (step 0 is
@@ -30,6 +31,7 @@
 #include "defs.h"
 #include "Observables/ForceField.h"
 #include "Observables/StressField.h"
+#include "Observables/ThermodynamicStressField.h"
 #include "Backends/BackendFactory.h"
 #include "Backends/SimBackend.h"
 #include "Interactions/BaseInteraction.h"
@@ -161,6 +163,7 @@ int main(int argc, char *argv[]) {
 			std::shared_ptr<BaseObservable> obs;
 			if(type == "force_field") obs = std::make_shared<ForceField>();
 			else if(type == "stress_field") obs = std::make_shared<StressField>();
+			else if(type == "thermodynamic_stress_field") obs = std::make_shared<ThermodynamicStressField>();
 			else throw RCexception("unknown observable %s", type.c_str());
 			obs->get_settings(oi, input);
 			obs->init();

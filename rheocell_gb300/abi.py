@@ -30,9 +30,13 @@ RC_OBS_FORCE = 3
 RC_OBS_FORCE_PASSIVE = 4
 RC_OBS_FORCE_ACTIVE = 5
 RC_OBS_PRESSURE = 6
+RC_OBS_THERMO = 7
+RC_OBS_THERMO_XY = 8
+RC_OBS_CHEMPOT2 = 9
 SOLVER_PHASES = ["fcg_setup", "first_layer", "tc_level0", "tc_level1", "tc_level2", "last_layer",
                  "fcg_z", "fcg_direction", "solve_start", "fcg_update", "other",
-                 "tc_weights", "tc_staging", "tc_mma", "tc_epilogue"]
+                 "tc_weights", "tc_staging", "tc_mma", "tc_epilogue",
+                 "tc_mma_warp_wait", "tc_mma_warp_issue", "tc_stage_wait", "tc_stage_load"]
 
 RC_SIMPLEFIELD = 0
 RC_ACTIVENEMATIC = 1

@@ -386,7 +386,14 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 				const double A = A_c * phi;
 				const double Rep = Rep_c * phi * (p2 - phi * phi);
 				mu = CH + A + Rep + 0.;
-				if(a.fsplit) a.fsplit[4 * a.fsplit_stride + start + q] = 0.0;  // SimpleMultiField sets no pressure
+				if(a.fsplit) {  // SimpleMultiField.cpp:158-181: pressure and free-energy density
+					a.fsplit[4 * a.fsplit_stride + start + q] = Rep - CH - A;
+					const double dx = .5 * (pr - pl), dy = .5 * (pu_ - pd);
+					const double CHd = (gamma / lambda) * 4 * phi * phi * (1 - phi) * (1 - phi) + gamma * lambda * (dx * dx + dy * dy);
+					const double Ad = -P.mu / P.a0 * phi * phi;
+					const double Repd = (P.kappa / lambda) * phi * phi * (p2 - phi * phi);
+					a.fsplit[5 * a.fsplit_stride + start + q] = CHd + Ad + Repd;
+				}
 			}
 			else if(MODEL == M_NEMATIC) {
 				const double lap = pr + pu_ + pl + pd - 4. * phi;
@@ -400,7 +407,10 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 					V = V + (-4 * lambda * omega * sup * phi);
 				}
 				mu = V;
-				if(a.fsplit) a.fsplit[4 * a.fsplit_stride + start + q] = Rep - CH - A;  // ActiveNematic.cpp:225
+				if(a.fsplit) {  // ActiveNematic.cpp:225; no free-energy density
+					a.fsplit[4 * a.fsplit_stride + start + q] = Rep - CH - A;
+					a.fsplit[5 * a.fsplit_stride + start + q] = 0.0;
+				}
 			}
 			else {
 				const double lap = pu_ + pd + pr + pl - 4 * phi;
@@ -430,7 +440,9 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 					const double Ad = Ad_c * phi * phi;
 					const double Repd = kl_c * phi * phi * (p2 - phi * phi);
 					saux[q] = CHd + Ad + Repd;
+					if(a.fsplit) a.fsplit[5 * a.fsplit_stride + start + q] = saux[q];  // WetModel.cpp:607
 				}
+				if(MODEL == M_POLAR && a.fsplit) a.fsplit[5 * a.fsplit_stride + start + q] = 0.0;
 				mu = V;
 			}
 			smu[q] = mu;

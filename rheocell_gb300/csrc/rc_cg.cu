@@ -929,7 +929,8 @@ __device__ __noinline__ bool precond_network(const CGArgs &a, CGShared &sh, TcCt
 // per-site sums are formed by a segmented scan in the chunk and added by the
 // tail lane to the owner's slot of a per-warp accumulator, chunk after chunk,
 // so all sums have a fixed order.
-constexpr int FCG_BATCH = 4;  // chunks whose loads are in flight together
+constexpr int FCG_BATCH = 4;  // chunks whose loads are in flight together (phase C: eight streams)
+constexpr int FCG_BATCH_EA = 8;  // the same for phases E and AB (four streams)
 
 struct SegLane {
 	int s;
@@ -984,27 +985,42 @@ __device__ __noinline__ bool fcg_phase_e(const CGArgs &a, CGShared &sh, bool fir
 	const int Eend = __ldcg(&cov_off[sh.site_end]);
 	float *accx = wacc, *accy = wacc + blockDim.x;
 	float w[4] = {0.f, 0.f, 0.f, 0.f};
+	// per-site values of a group of 32 sites, loaded one group ahead so that
+	// their round trips overlap the previous group's entries
+	int pe0 = Eend, pe1 = Eend, pdeg = 0;
+	float pvx = 0.f, pvy = 0.f;
+	auto prefetch = [&](long long kk) {
+		const bool v = kk < sh.site_end;
+		pe0 = v ? cov_off[kk] : Eend;
+		pe1 = v ? cov_off[kk + 1] : Eend;
+		pdeg = v ? box_deg(a.cnt, (int) kk, L) : 0;
+		pvx = (v && net && ax) ? box_n4T<float>(V, (int) kk, L) : 0.f;
+		pvy = (v && net && ay) ? box_n4T<float>(V + L2, (int) kk, L) : 0.f;
+	};
 	// warps take runs of 32 of the block's sites; lanes past the last site
 	// hold the empty entry range at Eend
-	for(long long k0 = sh.site_first + (threadIdx.x & ~31); k0 < sh.site_end; k0 += sh.site_step) {
+	const long long kfirst = sh.site_first + (threadIdx.x & ~31);
+	if(kfirst < sh.site_end) prefetch(kfirst + lane);
+	for(long long k0 = kfirst; k0 < sh.site_end; k0 += sh.site_step) {
 		const long long k = k0 + lane;
 		const bool kv = k < sh.site_end;
-		const int e0 = kv ? cov_off[k] : Eend, e1 = kv ? cov_off[k + 1] : Eend;
+		const int e0 = pe0, e1 = pe1;
 		float id = 0.f, nvx = 0.f, nvy = 0.f;
 		if(e1 > e0) {
-			id = sh.iTf[box_deg(a.cnt, (int) k, L)];
-			if(net && ax) nvx = es0 * box_n4T<float>(V, (int) k, L);
-			if(net && ay) nvy = es1 * box_n4T<float>(V + L2, (int) k, L);
+			id = sh.iTf[pdeg];
+			if(net && ax) nvx = es0 * pvx;
+			if(net && ay) nvy = es1 * pvy;
 		}
+		if(k0 + sh.site_step < sh.site_end) prefetch(k0 + sh.site_step + lane);
 		accx[threadIdx.x] = 0.f;
 		accy[threadIdx.x] = 0.f;
 		__syncwarp();
 		const int E0 = __shfl_sync(0xffffffffu, e0, 0), E1 = __shfl_sync(0xffffffffu, e1, 31);
 		// chunks in batches of FCG_BATCH: all loads of a batch are issued first
-		for(int c0 = E0; c0 < E1; c0 += 32 * FCG_BATCH) {
-			float r0[FCG_BATCH], q0[FCG_BATCH], r1[FCG_BATCH], q1[FCG_BATCH];
+		for(int c0 = E0; c0 < E1; c0 += 32 * FCG_BATCH_EA) {
+			float r0[FCG_BATCH_EA], q0[FCG_BATCH_EA], r1[FCG_BATCH_EA], q1[FCG_BATCH_EA];
 #pragma unroll
-			for(int u = 0; u < FCG_BATCH; u++) {
+			for(int u = 0; u < FCG_BATCH_EA; u++) {
 				const int e = c0 + 32 * u + lane;
 				const bool v = e < E1;
 				r0[u] = (v && ax) ? rx[e] : 0.f;
@@ -1013,7 +1029,7 @@ __device__ __noinline__ bool fcg_phase_e(const CGArgs &a, CGShared &sh, bool fir
 				q1[u] = (v && ay && !first) ? apy[e] : 0.f;
 			}
 #pragma unroll
-			for(int u = 0; u < FCG_BATCH; u++) {
+			for(int u = 0; u < FCG_BATCH_EA; u++) {
 				if(c0 + 32 * u >= E1) break;
 				const int e = c0 + 32 * u + lane;
 				const SegLane sg = seg_lane(e, E1, e0);
@@ -1074,28 +1090,43 @@ __device__ __noinline__ bool fcg_phase_ab(const CGArgs &a, CGShared &sh, bool fi
 	const int Eend = __ldcg(&cov_off[sh.site_end]);
 	float *accx = wacc, *accy = wacc + blockDim.x;
 	float w[2] = {0.f, 0.f};
+	// per-site values of a group of 32 sites, loaded one group ahead (their
+	// round trips overlap the previous group's entries)
+	int pe0 = Eend, pe1 = Eend, pdeg = 0;
+	float pzx = 0.f, pzy = 0.f, pox = 0.f, poy = 0.f;
+	auto prefetch = [&](long long kk) {
+		const bool v = kk < sh.site_end;
+		pe0 = v ? cov_off[kk] : Eend;
+		pe1 = v ? cov_off[kk + 1] : Eend;
+		pdeg = v ? box_deg(a.cnt, (int) kk, L) : 0;
+		pzx = (v && ax) ? box_n4T<float>(Zx, (int) kk, L) : 0.f;
+		pzy = (v && ay) ? box_n4T<float>(Zy, (int) kk, L) : 0.f;
+		pox = (v && ax && !first) ? box_n4T<float>(Pox, (int) kk, L) : 0.f;
+		poy = (v && ay && !first) ? box_n4T<float>(Poy, (int) kk, L) : 0.f;
+	};
 	// warps take runs of 32 of the block's sites; lanes past the last site
 	// hold the empty entry range at Eend
-	for(long long k0 = sh.site_first + (threadIdx.x & ~31); k0 < sh.site_end; k0 += sh.site_step) {
+	const long long kfirst = sh.site_first + (threadIdx.x & ~31);
+	if(kfirst < sh.site_end) prefetch(kfirst + lane);
+	for(long long k0 = kfirst; k0 < sh.site_end; k0 += sh.site_step) {
 		const long long k = k0 + lane;
 		const bool kv = k < sh.site_end;
-		const int e0 = kv ? cov_off[k] : Eend, e1 = kv ? cov_off[k + 1] : Eend;
+		const int e0 = pe0, e1 = pe1;
 		float d = 0.f, qx = 0.f, qy = 0.f;
 		if(e1 > e0) {
-			d = sh.Tf[box_deg(a.cnt, (int) k, L)];
-			if(ax) qx = neta * (first ? box_n4T<float>(Zx, (int) k, L)
-			                          : __fmaf_rn(bx, box_n4T<float>(Pox, (int) k, L), box_n4T<float>(Zx, (int) k, L)));
-			if(ay) qy = neta * (first ? box_n4T<float>(Zy, (int) k, L)
-			                          : __fmaf_rn(by, box_n4T<float>(Poy, (int) k, L), box_n4T<float>(Zy, (int) k, L)));
+			d = sh.Tf[pdeg];
+			if(ax) qx = neta * (first ? pzx : __fmaf_rn(bx, pox, pzx));
+			if(ay) qy = neta * (first ? pzy : __fmaf_rn(by, poy, pzy));
 		}
+		if(k0 + sh.site_step < sh.site_end) prefetch(k0 + sh.site_step + lane);
 		accx[threadIdx.x] = 0.f;
 		accy[threadIdx.x] = 0.f;
 		__syncwarp();
 		const int E0 = __shfl_sync(0xffffffffu, e0, 0), E1 = __shfl_sync(0xffffffffu, e1, 31);
-		for(int c0 = E0; c0 < E1; c0 += 32 * FCG_BATCH) {
-			float z0[FCG_BATCH], p0[FCG_BATCH], z1[FCG_BATCH], p1[FCG_BATCH];
+		for(int c0 = E0; c0 < E1; c0 += 32 * FCG_BATCH_EA) {
+			float z0[FCG_BATCH_EA], p0[FCG_BATCH_EA], z1[FCG_BATCH_EA], p1[FCG_BATCH_EA];
 #pragma unroll
-			for(int u = 0; u < FCG_BATCH; u++) {
+			for(int u = 0; u < FCG_BATCH_EA; u++) {
 				const int e = c0 + 32 * u + lane;
 				const bool v = e < E1;
 				z0[u] = (v && ax) ? zx[e] : 0.f;
@@ -1104,7 +1135,7 @@ __device__ __noinline__ bool fcg_phase_ab(const CGArgs &a, CGShared &sh, bool fi
 				p1[u] = (v && ay && !first) ? py[e] : 0.f;
 			}
 #pragma unroll
-			for(int u = 0; u < FCG_BATCH; u++) {
+			for(int u = 0; u < FCG_BATCH_EA; u++) {
 				if(c0 + 32 * u >= E1) break;
 				const int e = c0 + 32 * u + lane;
 				const SegLane sg = seg_lane(e, E1, e0);
@@ -1167,13 +1198,24 @@ __device__ __noinline__ bool fcg_phase_c(const CGArgs &a, CGShared &sh, float *w
 	const int Eend = __ldcg(&cov_off[sh.site_end]);
 	float *accx = wacc, *accy = wacc + blockDim.x;
 	float w[2] = {0.f, 0.f};
+	// per-site values of a group of 32 sites, loaded one group ahead
+	int pe0 = Eend, pe1 = Eend, pdeg = 0;
+	auto prefetch = [&](long long kk) {
+		const bool v = kk < sh.site_end;
+		pe0 = v ? cov_off[kk] : Eend;
+		pe1 = v ? cov_off[kk + 1] : Eend;
+		pdeg = v ? box_deg(a.cnt, (int) kk, L) : 0;
+	};
 	// warps take runs of 32 of the block's sites; lanes past the last site
 	// hold the empty entry range at Eend
-	for(long long k0 = sh.site_first + (threadIdx.x & ~31); k0 < sh.site_end; k0 += sh.site_step) {
+	const long long kfirst = sh.site_first + (threadIdx.x & ~31);
+	if(kfirst < sh.site_end) prefetch(kfirst + lane);
+	for(long long k0 = kfirst; k0 < sh.site_end; k0 += sh.site_step) {
 		const long long k = k0 + lane;
 		const bool kv = k < sh.site_end;
-		const int e0 = kv ? cov_off[k] : Eend, e1 = kv ? cov_off[k + 1] : Eend;
-		const float id = (e1 > e0) ? sh.iTf[box_deg(a.cnt, (int) k, L)] : 0.f;
+		const int e0 = pe0, e1 = pe1;
+		const float id = (e1 > e0) ? sh.iTf[pdeg] : 0.f;
+		if(k0 + sh.site_step < sh.site_end) prefetch(k0 + sh.site_step + lane);
 		accx[threadIdx.x] = 0.f;
 		accy[threadIdx.x] = 0.f;
 		__syncwarp();

@@ -128,7 +128,7 @@ struct rc_engine {
 	bool phase_on = false;
 	double *obs_buf = nullptr;               // diagnostic observables scratch
 	size_t obs_cap = 0;
-	double *split_buf = nullptr;             // force split of an observation: 5 x S_cap
+	double *split_buf = nullptr;             // force split and free-energy density of an observation: 6 x S_cap
 	CellDev *cells_save = nullptr;           // cell records kept aside while it is formed
 	// viscous solve limits (rc_set_cg_limits) and the barrier test hook
 	long long cg_max_iters = 0;
@@ -1655,7 +1655,7 @@ static int observe_split(rc_engine *e) {
 	if(e->hp.precision == RC_PRECISION_FLOAT)
 		return set_err(e, RC_ERR_UNSUPPORTED, "force observables are formed by the FP64 cell kernels only");
 	int rc;
-	if(!e->split_buf && (rc = dalloc(e, &e->split_buf, 5 * (size_t) e->S_cap))) return rc;
+	if(!e->split_buf && (rc = dalloc(e, &e->split_buf, 6 * (size_t) e->S_cap))) return rc;
 	if(!e->cells_save && (rc = dalloc(e, &e->cells_save, (size_t) std::max(e->N, 1)))) return rc;
 	if(e->N == 0) return RC_OK;
 	CUDA_TRY(e, cudaMemcpyAsync(e->cells_save, e->cells, sizeof(CellDev) * (size_t) e->N, cudaMemcpyDeviceToDevice, e->stream));
@@ -1695,9 +1695,16 @@ static int observe_box_fields(rc_engine *e, int kind, int layer, int only_type, 
 		launch_obs_sites(e->cells, e->layers, lay, e->bin_count, e->bin_cells, e->phiA, g, g + st, 1.0, layer,
 		                 only_type, f0, f1, e->stream);
 	}
-	else {
+	else if(kind == RC_OBS_PRESSURE) {
 		launch_obs_sites(e->cells, e->layers, lay, e->bin_count, e->bin_cells, e->phiA, sp + 4 * st, nullptr, 1.0, layer,
 		                 only_type, f0, f1, e->stream);
+	}
+	else {
+		// the free-energy density gradient 2 gamma lambda grad(phi) of the
+		// models that set it (WetModel.cpp:608-609, SimpleMultiField.cpp:179-180)
+		const double g2 = (e->P.model == M_WET || e->P.model == M_SIMPLE) ? 2 * e->P.gamma * e->P.lambda : 0.0;
+		launch_obs_thermo(e->cells, e->layers, lay, e->bin_count, e->bin_cells, e->phiA, sp + 5 * st, e->mu, e->dxg,
+		                  e->dyg, g2, kind - RC_OBS_THERMO, layer, only_type, f0, f1, e->stream);
 	}
 	return RC_OK;
 }
@@ -1705,7 +1712,7 @@ static int observe_box_fields(rc_engine *e, int kind, int layer, int only_type, 
 int rc_observe_field(rc_engine *e, int kind, int layer, int only_type, int size_grid, double *fx, double *fy,
                      double *coarse_x, double *coarse_y) {
 	if(!e || !fx || !fy) return RC_ERR_INVALID;
-	if(kind < RC_OBS_VELOCITY || kind > RC_OBS_PRESSURE) return set_err(e, RC_ERR_INVALID, "rc_observe_field: kind %d", kind);
+	if(kind < RC_OBS_VELOCITY || kind > RC_OBS_CHEMPOT2) return set_err(e, RC_ERR_INVALID, "rc_observe_field: kind %d", kind);
 	if(layer < 0 || layer >= e->n_layers) return set_err(e, RC_ERR_INVALID, "rc_observe_field: layer %d", layer);
 	CUDA_TRY(e, cudaSetDevice(e->device));
 	const LayerDev &lay = e->layers_h[(size_t) layer];

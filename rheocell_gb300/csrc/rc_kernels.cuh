@@ -150,6 +150,10 @@ void launch_obs_coarse(const double *f, double *out, int L, int sg, cudaStream_t
 void launch_obs_sites(const CellDev *cells, const LayerDev *layers, const LayerDev &lay_h, const int *bin_count,
                       const int *bin_cells, const double *phi, const double *g0, const double *g1, double scale, int layer,
                       int only_type, double *fx, double *fy, cudaStream_t s);
+void launch_obs_thermo(const CellDev *cells, const LayerDev *layers, const LayerDev &lay_h, const int *bin_count,
+                       const int *bin_cells, const double *phi, const double *fd, const double *mu, const double *dxg,
+                       const double *dyg, double g2, int sub, int layer, int only_type, double *fx, double *fy,
+                       cudaStream_t s);
 void launch_obs_stress(const double *fx, const double *fy, double *xx, double *yy, double *xy, int L, int sg, cudaStream_t s);
 void launch_obs_cells(const CellDev *cells, const LayerDev *layers, int N, int n_layers, const double *dxg,
                       const double *dyg, double *cell_obs, double *layer_obs, cudaStream_t s);

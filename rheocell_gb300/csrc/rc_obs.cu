@@ -31,7 +31,11 @@ struct ObsArgs {
 	const double *phi, *vx, *vy;
 	int kind, layer, only_type;
 	double *fx, *fy;
-	double scale;  // OBS_SITES: per-site values are multiplied by it first
+	double scale;  // OBS_SITES: per-site values are multiplied by it first; OBS_THERMO: 2 gamma lambda
+	// OBS_THERMO: free-energy density, chemical potential and gradients per
+	// site; sub 0: (xx, yy), 1: (xy, mu), 2: (mu^2, phi)
+	const double *fd, *mu, *dxg, *dyg;
+	int sub;
 };
 
 // OBS_SITES: f0 += (vx[j] * scale) * phi, f1 += (vy[j] * scale) * phi, or
@@ -39,7 +43,11 @@ struct ObsArgs {
 // (ForceField.cpp:79-96, StressField.cpp:84-100): total force (v times the
 // friction, get_total_force_x/y), passive and active forces, pressure with
 // the phi field.
-enum { OBS_VELOCITY = 0, OBS_SHAPE = 1, OBS_NEMATIC = 2, OBS_SITES = 3 };
+// OBS_THERMO: ThermodynamicStressField::calc_field (ThermodynamicStressField.cpp:75-99),
+// unweighted per-site sums: xx += f_d - mu phi + dx g_x, yy likewise with y,
+// xy += dx g_y, with g = 2 gamma lambda grad(phi) (WetModel.cpp:608-609;
+// zero for the models that do not set it), and the sums of mu, mu^2, phi.
+enum { OBS_VELOCITY = 0, OBS_SHAPE = 1, OBS_NEMATIC = 2, OBS_SITES = 3, OBS_THERMO = 4 };
 
 __global__ void __launch_bounds__(BIN_X *BIN_Y) obs_field_kernel(const ObsArgs a) {
 	__shared__ int s_ids[BIN_CAP];
@@ -101,6 +109,22 @@ __global__ void __launch_bounds__(BIN_X *BIN_Y) obs_field_kernel(const ObsArgs a
 		else if(a.kind == OBS_SITES) {
 			f0 += (a.vx[j] * a.scale) * phi;
 			f1 += a.vy ? (a.vy[j] * a.scale) * phi : phi;
+		}
+		else if(a.kind == OBS_THERMO) {
+			const double mu = a.mu[j], dx = a.dxg[j], dy = a.dyg[j];
+			const double gx = a.scale * dx, gy = a.scale * dy;
+			if(a.sub == 0) {
+				f0 += a.fd[j] - mu * phi + dx * gx;
+				f1 += a.fd[j] - mu * phi + dy * gy;
+			}
+			else if(a.sub == 1) {
+				f0 += dx * gy;
+				f1 += mu;
+			}
+			else {
+				f0 += mu * mu;
+				f1 += phi;
+			}
 		}
 		else {
 			f0 += s_g0[i] * phi;
@@ -222,6 +246,7 @@ void launch_obs_field(const CellDev *cells, const LayerDev *layers, const LayerD
                       const int *bin_cells, const double *phi, const double *vx, const double *vy, int kind, int layer,
                       int only_type, double *fx, double *fy, cudaStream_t s) {
 	ObsArgs a;
+	memset(&a, 0, sizeof(a));
 	a.cells = cells;
 	a.layers = layers;
 	a.bin_count = bin_count;
@@ -242,6 +267,7 @@ void launch_obs_sites(const CellDev *cells, const LayerDev *layers, const LayerD
                       const int *bin_cells, const double *phi, const double *g0, const double *g1, double scale, int layer,
                       int only_type, double *fx, double *fy, cudaStream_t s) {
 	ObsArgs a;
+	memset(&a, 0, sizeof(a));
 	a.cells = cells;
 	a.layers = layers;
 	a.bin_count = bin_count;
@@ -255,6 +281,31 @@ void launch_obs_sites(const CellDev *cells, const LayerDev *layers, const LayerD
 	a.fx = fx;
 	a.fy = fy;
 	a.scale = scale;
+	obs_field_kernel<<<lay_h.nbx * lay_h.nby, BIN_X * BIN_Y, 0, s>>>(a);
+}
+
+void launch_obs_thermo(const CellDev *cells, const LayerDev *layers, const LayerDev &lay_h, const int *bin_count,
+                       const int *bin_cells, const double *phi, const double *fd, const double *mu, const double *dxg,
+                       const double *dyg, double g2, int sub, int layer, int only_type, double *fx, double *fy,
+                       cudaStream_t s) {
+	ObsArgs a;
+	memset(&a, 0, sizeof(a));
+	a.cells = cells;
+	a.layers = layers;
+	a.bin_count = bin_count;
+	a.bin_cells = bin_cells;
+	a.phi = phi;
+	a.kind = OBS_THERMO;
+	a.layer = layer;
+	a.only_type = only_type;
+	a.fx = fx;
+	a.fy = fy;
+	a.scale = g2;
+	a.fd = fd;
+	a.mu = mu;
+	a.dxg = dxg;
+	a.dyg = dyg;
+	a.sub = sub;
 	obs_field_kernel<<<lay_h.nbx * lay_h.nby, BIN_X * BIN_Y, 0, s>>>(a);
 }
 

@@ -397,6 +397,7 @@ static __device__ __noinline__ bool tc_conv_strip(int l, const TcSrc &src, const
 			// row i - 4 has been written out (its slot is reused and the MMA
 			// mbarriers stay at most one phase ahead of their waiters)
 			if(lane == 0) {
+				TcTimer tmm(c.tns, 0);  // block 0's MMA thread: [4] waits for staged rows and free slots, [5] issue
 				for(int i = 0; i < nin; i++) {
 					bool ok = false;
 					for(long long t = 0; t < TC_WAIT_LIMIT; t++) {
@@ -406,6 +407,7 @@ static __device__ __noinline__ bool tc_conv_strip(int l, const TcSrc &src, const
 						}
 						if(*abort) break;
 					}
+					tmm.mark(4);
 					if(!ok) {
 						ctrl[2] = 1;
 						break;
@@ -427,6 +429,7 @@ static __device__ __noinline__ bool tc_conv_strip(int l, const TcSrc &src, const
 					}
 					tc_commit(&acc[(G + i) & 3]);
 					ctrl[3] = i + 1;
+					tmm.mark(5);
 				}
 			}
 			__syncwarp();
@@ -435,6 +438,7 @@ static __device__ __noinline__ bool tc_conv_strip(int l, const TcSrc &src, const
 			// staging warps: row r into buffer r % 3 once the MMAs of row r - 3
 			// (the buffer's previous row) are done
 			const int pt = threadIdx.x - 32, np = 224;
+			TcTimer tst(c.tns, 32);  // block 0's first staging thread: [6] waits for buffer reuse, [7] loading
 			for(int r = 0; r < nin; r++) {
 				bool ok = true;
 				if(r >= 3 && pt == 0) {
@@ -443,11 +447,13 @@ static __device__ __noinline__ bool tc_conv_strip(int l, const TcSrc &src, const
 					if(!ok) ctrl[2] = 1;
 				}
 				if(bar_named_or(1, np, !ok || *abort != 0)) break;
+				tst.mark(6);
 				tc_stage_strip_row(src, KC, n, wrap(y0 - 1 + r, L), x0, HW, L, Abuf + (r % 3) * KC * HW, w0s, pt, np);
 				cp_async_wait_all();
 				fence_async_smem();
 				bar_named(1, np);
 				if(pt == 0) st_release_s32(&ctrl[0], r + 1);
+				tst.mark(7);
 			}
 		}
 		else {
@@ -631,38 +637,61 @@ static __device__ __noinline__ void e0a_range(const float *x0, const float *w, b
 }
 
 // Last layer (16 -> 1, no activation) on the CUDA cores: BF16 input, FP32
-// output.  w: FP32 [9][16][1] then 1 bias (shared memory).
+// output.  w: FP32 [9][16][1] then 1 bias (shared memory).  A work item is
+// one column j of OUT_ROWS consecutive output rows of one sample; its input
+// rows are loaded once each (three pixels, j - 1 .. j + 1) and folded at
+// once into the outputs they feed: row r adds its dy = -1 taps to output
+// r + 1, its dy = 0 taps to r, its dy = +1 taps to r - 1.  Every output thus
+// receives its taps in the order dy, dx, channel, as a per-pixel loop would,
+// with (OUT_ROWS + 2) * 3 / OUT_ROWS pixel loads per output instead of nine;
+// consecutive threads take consecutive columns (coalesced).  L must be a
+// multiple of OUT_ROWS (the learned solver requires L % 4 == 0).
+constexpr int OUT_ROWS = 4;
 static __device__ __noinline__ void out_range(const bf16 *t0, const float *w, float *dst, int batch, int L, long long first,
                                           long long stride) {
-	const long long npix = (long long) batch * L * L;
-	for(long long p = first; p < npix; p += stride) {
-		const int n = (int) (p / ((long long) L * L));
-		const int r = (int) (p - (long long) n * L * L);
-		const int i = r / L, j = r - (r / L) * L;
-		// the nine taps' loads are issued together (one load round trip per
-		// pixel), then the FMAs run in tap and channel order
-		uint4 q0[9], q1[9];
+	const int nrb = L / OUT_ROWS;
+	const long long nitems = (long long) batch * nrb * L;
+	for(long long it = first; it < nitems; it += stride) {
+		const int j = (int) (it % L);
+		const long long rest = it / L;
+		const int rb = (int) (rest % nrb), n = (int) (rest / nrb);
+		const int i0 = rb * OUT_ROWS;
+		const int cols[3] = {wrap(j - 1, L), j, wrap(j + 1, L)};
+		float acc[OUT_ROWS];
 #pragma unroll
-		for(int t = 0; t < 9; t++) {
-			const int ii = wrap(i + t / 3 - 1, L), jj = wrap(j + t % 3 - 1, L);
-			const uint4 *q = reinterpret_cast<const uint4 *>(t0 + ((size_t) (n * L + ii) * L + jj) * 16);
-			q0[t] = q[0];
-			q1[t] = q[1];
-		}
-		float acc = w[9 * 16];
+		for(int o = 0; o < OUT_ROWS; o++) acc[o] = w[9 * 16];
 #pragma unroll
-		for(int t = 0; t < 9; t++) {
-			const uint4 u0 = q0[t], u1 = q1[t];
-			const uint32_t u[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
-			const float *wt = w + t * 16;
+		for(int r = -1; r <= OUT_ROWS; r++) {
+			uint4 px[3][2];
+			const uint4 *row = reinterpret_cast<const uint4 *>(t0 + (size_t) (n * L + wrap(i0 + r, L)) * L * 16);
 #pragma unroll
-			for(int e = 0; e < 8; e++) {
-				const float2 f = bf2f(u[e]);
-				acc = fmaf(f.x, wt[2 * e], acc);
-				acc = fmaf(f.y, wt[2 * e + 1], acc);
+			for(int d = 0; d < 3; d++) {
+				px[d][0] = row[cols[d] * 2];
+				px[d][1] = row[cols[d] * 2 + 1];
 			}
+			// tap rows ty = 0, 1, 2 (dy = ty - 1) feed output row r - ty + 1
+#pragma unroll
+			for(int ty = 0; ty < 3; ty++) {
+				const int o = r - ty + 1;
+				if(o < 0 || o >= OUT_ROWS) continue;
+#pragma unroll
+				for(int d = 0; d < 3; d++) {
+					const uint32_t u[8] = {px[d][0].x, px[d][0].y, px[d][0].z, px[d][0].w,
+					                       px[d][1].x, px[d][1].y, px[d][1].z, px[d][1].w};
+					const float *wt = w + (ty * 3 + d) * 16;
+#pragma unroll
+					for(int e = 0; e < 8; e++) {
+						const float2 f = bf2f(u[e]);
+						acc[o] = fmaf(f.x, wt[2 * e], acc[o]);
+						acc[o] = fmaf(f.y, wt[2 * e + 1], acc[o]);
+					}
+				}
+			}
+			if(r >= 1) dst[((size_t) n * L + i0 + r - 1) * L + j] = acc[r - 1];
+			// one input row in registers at a time: keep the next row's loads
+			// from being hoisted above this row's arithmetic
+			asm volatile("" ::: "memory");
 		}
-		dst[p] = acc;
 	}
 }
 

@@ -276,11 +276,12 @@ OBS_CASES = {
     "obs_wetpolar": (dict(L=36, n=4, seed=42, **SMALL), WETPOLAR_S, 2, 52, 3),
     "obs_nematic": (dict(L=36, n=4, seed=43, types=[0, 1, 1, 0], **SMALL), NEMATIC_S, 2, 53, 4),
     "obs_polar": (dict(L=36, n=4, seed=44, **SMALL), dict(DRY_POLAR_S, J_Q=0.3), 2, 54, 3),
+    "obs_simple": (dict(L=36, n=4, seed=45, **SMALL), SIMPLE_S, 2, 55, 3),
 }
 
 
 def record_observables(name):
-    """The reference's own ForceField and StressField output strings (its
+    """The reference's own ForceField, StressField and ThermodynamicStressField output strings (its
     observable classes, driven by oracle/ref_driver.cpp's observe mode) as
     number arrays after the two header lines."""
     mkw, params, step, seed, sg = OBS_CASES[name]
@@ -289,7 +290,7 @@ def record_observables(name):
     out = {}
     try:
         g.write_case(d, m, params, steps=step, seed=seed)
-        for kind in ("force_field", "stress_field"):
+        for kind in ("force_field", "stress_field", "thermodynamic_stress_field"):
             res = subprocess.run([refdump.driver_path("exact"), "observe", kind + ".txt", "%d:%s:%d" % (step, kind, sg),
                                   "input"], cwd=d, capture_output=True, text=True)
             if res.returncode != 0:

@@ -36,7 +36,7 @@ def test_generated_tanh_discs_match_host_patches(L, n):
     p2, cells2 = _cells(keys, m, True)
     b = engine.Engine.generated(p2, L, cells2, abi.RC_PROFILE_TANH, 8.0, 2.0)
     sa, sb = a.state(), b.state()
-    assert np.max(np.abs(sa["phi"] - sb["phi"])) <= 1e-15
+    assert np.max(np.abs(sa["phi"] - sb["phi"])) <= 1e-14  # CUDA tanh against glibc tanh: a few tens of ulps
     for k in ("area", "sum_f", "com_x", "com_y"):
         assert rel_err(sb[k], sa[k]) <= 1e-13, k
     a.set_phase(1)
