@@ -208,6 +208,7 @@ def prepare_learned(args, eng, lib):
     else:
         own = not args.train_workload or args.train_workload == args.workload
         src = eng if own else make_engine(args.train_workload, abi.RC_PRECISION_DOUBLE, eng.device)
+        src.set_solver(abi.RC_SOLVER_PLAIN_FP64)  # samples come from plain FP64 solves
         src.harvest(capacity=args.harvest_capacity, every=3, per_solve=6)
         t0 = time.perf_counter()
         src.step(args.harvest_steps)
@@ -222,6 +223,9 @@ def prepare_learned(args, eng, lib):
     if args.save_params:
         np.savetxt(args.save_params, eng.get_params(), fmt="%.17g")
     k = max(2, min(args.steps, 10))
+    # the plain FP64 device CG on the same states (whatever the engine's precision)
+    eng.set_solver(abi.RC_SOLVER_PLAIN_FP64)
+    solve_stage(eng, lib, 1, flush)
     plain_ms, plain_it, plain_res = solve_stage(eng, lib, k, flush)
     eng.set_solver(abi.RC_SOLVER_LEARNED)
     solve_stage(eng, lib, 1, flush)
@@ -259,7 +263,7 @@ def velocity_error(eng):
     S = eng.site_count()
     v = [torch.zeros(S, dtype=torch.float64, device="cuda") for _ in range(4)]
     torch.cuda.synchronize()
-    sp = eng.resolve(abi.RC_SOLVER_PLAIN, v[0].data_ptr(), v[1].data_ptr())
+    sp = eng.resolve(abi.RC_SOLVER_PLAIN_FP64, v[0].data_ptr(), v[1].data_ptr())
     sl = eng.resolve(abi.RC_SOLVER_LEARNED, v[2].data_ptr(), v[3].data_ptr())
     err = [float((v[2 + c] - v[c]).abs().max() / v[c].abs().max().clamp_min(1e-300)) for c in range(2)]
     return {"vx": err[0], "vy": err[1], "max": max(err),
@@ -637,7 +641,7 @@ def main():
     ap.add_argument("--train-lr-final", type=float, default=0.05, help="final step size as a fraction of --train-lr")
     args = ap.parse_args()
     if args.solver is None:
-        args.solver = "learned" if args.workload.startswith("wet") and args.precision != "float" else "plain"
+        args.solver = "learned" if args.workload.startswith("wet") else "plain"
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1:

@@ -57,8 +57,9 @@ typedef enum rc_precision {
 	RC_PRECISION_DOUBLE = 0, /* FP64 everywhere; the parity path                    */
 	RC_PRECISION_MIXED = 1,  /* FP64 fields; FP32 viscous-solve inner iterations,
 	                            FP64 dots and FP64 true-residual refinement        */
-	RC_PRECISION_FLOAT = 2   /* dry polar model: FP32 site arithmetic, FP64 field
-	                            storage and FP64 cell-area integrals               */
+	RC_PRECISION_FLOAT = 2   /* wetpolarmodel and wetmodel: FP32 site arithmetic,
+	                            FP64 field storage and FP64 cell-area integrals;
+	                            the viscous solve as RC_PRECISION_MIXED            */
 } rc_precision;
 
 /*
@@ -380,7 +381,8 @@ int rc_unet_loss_grad(int L, int batch, const double *params, const double *inpu
  * hands over to plain FP64 CG).
  *
  * rc_learned_harvest: collect training samples from the following plain
- * FP64 solves (RC_PRECISION_DOUBLE and RC_SOLVER_PLAIN): at sweeps 0,
+ * FP64 solves (RC_SOLVER_PLAIN with RC_PRECISION_DOUBLE, or
+ * RC_SOLVER_PLAIN_FP64): at sweeps 0,
  * every, 2*every, ... (at most per_solve points per solve) each velocity
  * component gives the pair (box residual, box error), until `capacity`
  * samples are stored.  capacity = 0 stops harvesting and frees the store;
@@ -388,13 +390,16 @@ int rc_unet_loss_grad(int L, int batch, const double *params, const double *inpu
  * rc_learned_harvested: samples stored so far (synchronises).
  * rc_learned_train: Adam on the stored samples (device forward and backward
  * kernels); the trained parameters become the engine's.
- * rc_set_solver: RC_SOLVER_PLAIN (default) or RC_SOLVER_LEARNED (needs
- * parameters, from training or rc_learned_set_params, and a box side that
- * is a multiple of 4).
+ * rc_set_solver: RC_SOLVER_PLAIN (default), RC_SOLVER_PLAIN_FP64 or
+ * RC_SOLVER_LEARNED (needs parameters, from training or
+ * rc_learned_set_params, and a box side that is a multiple of 4).
  */
 #define RC_SOLVER_PLAIN 0
 #define RC_SOLVER_LEARNED 1        /* network on the tensor cores (BF16 activations) */
 #define RC_SOLVER_LEARNED_FP32 2   /* the same network in FP32 on the CUDA cores     */
+#define RC_SOLVER_PLAIN_FP64 3     /* Eigen's Jacobi CG in FP64 whatever the engine's
+                                      precision (RC_SOLVER_PLAIN follows it: the
+                                      FP32 inner iterations for mixed and float) */
 
 typedef struct rc_train_options {
 	int epochs;                 /* passes over the training samples (<= 0: 8)         */
@@ -428,8 +433,9 @@ int rc_set_solver(rc_engine *e, int solver);
 /*
  * rc_viscous_resolve: run the viscous solve of the last force evaluation
  * again, from a cold start, with `solver` (RC_SOLVER_PLAIN: the engine's
- * precision -- FP64 CG for RC_PRECISION_DOUBLE; or a learned solver, which
- * needs parameters) into vx and vy, device arrays of n = rc_site_count(e)
+ * precision -- FP64 CG for RC_PRECISION_DOUBLE; RC_SOLVER_PLAIN_FP64: FP64 CG
+ * for any precision; or a learned solver, which needs parameters) into vx
+ * and vy, device arrays of n = rc_site_count(e)
  * doubles in the order of rc_download_phi.  The engine's velocities,
  * warm-start schedule and counters are unchanged, so solvers can be compared
  * on one right-hand side without advancing the simulation.  `stats` (may be

@@ -23,6 +23,7 @@ RC_UNET_PARAMS = 25937
 RC_SOLVER_PLAIN = 0
 RC_SOLVER_LEARNED = 1
 RC_SOLVER_LEARNED_FP32 = 2
+RC_SOLVER_PLAIN_FP64 = 3
 RC_OBS_VELOCITY = 0
 RC_OBS_SHAPE = 1
 RC_OBS_NEMATIC = 2

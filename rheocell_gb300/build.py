@@ -3,7 +3,8 @@
 Compiles every translation unit under csrc/ for sm_103a with nvcc (in
 parallel), links librheocell_gb300.so with the CUDA runtime statically, and
 never touches site-packages.  FP64 kernels are compiled without FMA
-contraction so that single evaluations match the reference's arithmetic.
+contraction so that single evaluations match the reference's arithmetic;
+the FP32-only units (FMA_UNITS) keep it.
 """
 from __future__ import annotations
 
@@ -23,8 +24,16 @@ GEN = os.path.join(BUILD, "confgenerator")
 HOST_SRC = os.path.join(HERE, "host", "rheocell.cpp")
 GEN_SRC = os.path.join(HERE, "host", "confgenerator.cpp")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
-                     "-Xptxas", "-O3"]
+NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-Xptxas", "-O3"]
+# Translation units whose FP32 arithmetic is not held to the reference bit for
+# bit (FP32 cell kernels, network training) keep FMA contraction; every other
+# unit -- the FP64 kernels, box sums, solves and observables -- is compiled
+# without it, as the reference's exact build evaluates its expressions.
+FMA_UNITS = ("rc_cells_f32.cu", "rc_unet.cu")
+
+
+def unit_flags(src: str):
+    return NVCC_FLAGS + ["--fmad=" + ("true" if os.path.basename(src) in FMA_UNITS else "false")]
 
 
 def nvcc() -> str:
@@ -61,7 +70,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-        cmd = [nv] + NVCC_FLAGS + ["-c", src, "-o", obj]
+        cmd = [nv] + unit_flags(src) + ["-c", src, "-o", obj]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -69,7 +78,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
             raise RuntimeError("nvcc failed on %s:\n%s%s" % (src, r.stdout, r.stderr))
         return obj
 
-    with cf.ThreadPoolExecutor(max_workers=min(8, len(sources()) or 1)) as ex:
+    with cf.ThreadPoolExecutor(max_workers=min(os.cpu_count() or 8, len(sources()) or 1)) as ex:
         objs = list(ex.map(compile_one, sources()))
     tmp = LIB + ".tmp"
     cmd = [nv] + ARCH + ["-shared", "-o", tmp] + objs + ["-cudart", "static"]

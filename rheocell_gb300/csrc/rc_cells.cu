@@ -25,19 +25,9 @@
 // library is compiled without FMA contraction, so a single evaluation is
 // bit-identical to the reference's exact build; per-cell sums use a fixed
 // tree instead of the reference's sequential loop (last-bit differences).
-#include "rc_kernels.cuh"
-
-#include <math.h>
+#include "rc_cell_dev.cuh"
 
 namespace rc {
-
-#define RC_PI_F 3.141592653589793238462643f
-
-enum { EVB = 0 };
-
-__device__ inline int box_el(int site, int dx, int dy, int L) {
-	return wrapi(site % L + dx, L) + wrapi(site / L + dy, L) * L;
-}
 
 // Correctly rounded x / b from rb = RN(1/b): q = RN(x rb), the exact
 // remainder x - q b by FMA, and one correction q + rem rb (Markstein's
@@ -51,237 +41,6 @@ __device__ __forceinline__ double div_rn(double x, double b, double rb) {
 	return __fma_rn(rem, rb, q);
 }
 
-struct Nb {
-	int r, l, u, d;
-};
-
-__device__ inline Nb patch_nb(int q, int x, int y, int lx, int ly) {
-	Nb nb;
-	nb.r = (x == lx - 1) ? q - (lx - 1) : q + 1;
-	nb.l = (x == 0) ? q + (lx - 1) : q - 1;
-	nb.u = (y == ly - 1) ? q - (ly - 1) * lx : q + lx;
-	nb.d = (y == 0) ? q + (ly - 1) * lx : q - lx;
-	return nb;
-}
-
-struct BoxNb {
-	int r, l, u, d;
-};
-
-__device__ inline BoxNb box_nb(int k, int L) {
-	const int x = k % L, y = k / L;
-	BoxNb b;
-	b.r = (x == L - 1) ? k - (L - 1) : k + 1;
-	b.l = (x == 0) ? k + (L - 1) : k - 1;
-	b.u = (y == L - 1) ? k - (L - 1) * L : k + L;
-	b.d = (y == 0) ? k + (L - 1) * L : k - L;
-	return b;
-}
-
-// Appends cell ci to the bins its patch rectangle overlaps (periodic).
-__device__ void append_bins(const CellDev &c, int ci, const LayerDev &ly, int *bin_count_all, int *bin_cells_all,
-                            DevStatus *st) {
-	const int L = ly.L, nbx = ly.nbx;
-	int *bin_count = bin_count_all + ly.bin_off;
-	int *bin_cells = bin_cells_all + (size_t) ly.bin_off * BIN_CAP;
-	// patch sides are <= MAX_TABLE_SIDE (128): at most 5 x-bins and 17 y-bins
-	int bxs[8], bys[24];
-	int nbxs = 0, nbys = 0;
-	{
-		int x = c.corner % L, rem = c.lx;
-		while(rem > 0 && nbxs < 8) {
-			const int b = x / BIN_X;
-			int end = min((b + 1) * BIN_X, L);
-			int run = min(rem, end - x);
-			bool seen = false;
-			for(int i = 0; i < nbxs; i++) seen |= (bxs[i] == b);
-			if(!seen) bxs[nbxs++] = b;
-			rem -= run;
-			x += run;
-			if(x >= L) x = 0;
-		}
-	}
-	{
-		int y = c.corner / L, rem = c.ly;
-		while(rem > 0 && nbys < 24) {
-			const int b = y / BIN_Y;
-			int end = min((b + 1) * BIN_Y, L);
-			int run = min(rem, end - y);
-			bool seen = false;
-			for(int i = 0; i < nbys; i++) seen |= (bys[i] == b);
-			if(!seen) bys[nbys++] = b;
-			rem -= run;
-			y += run;
-			if(y >= L) y = 0;
-		}
-	}
-	for(int j = 0; j < nbys; j++)
-		for(int i = 0; i < nbxs; i++) {
-			const int b = bxs[i] + bys[j] * nbx;
-			const int slot = atomicAdd(&bin_count[b], 1);
-			if(slot < BIN_CAP) bin_cells[(size_t) b * BIN_CAP + slot] = ci;
-			else atomicOr(&st->err, ERR_BIN);
-		}
-}
-
-// set_positions (Fields/MultiPhaseField.cpp:223-310).  The resize branch only
-// records the new geometry; the field copy runs in the repack kernels.
-__device__ void set_positions_dev(CellDev &c, const DevParams &P, int L, DevStatus *st, int ci) {
-	const int border = P.border;
-	if(c.xl >= border && c.yb >= border) {
-		const int site = box_el(c.corner, (int) c.comx, (int) c.comy, L);
-		c.comy = (int) (site / L) + (c.comy - (int) c.comy);
-		c.comx = (int) (site - (int) (site / L) * L) + (c.comx - (int) c.comx);
-		const double cox = c.corner % L, coy = c.corner / L;
-		const int ncorner = box_el(site, (int) -c.lx / 2, (int) -c.ly / 2, L);
-		const double cnx = ncorner % L, cny = ncorner / L;
-		const double d0 = cnx - cox - rint((cnx - cox) / L) * L;
-		const double d1 = cny - coy - rint((cny - coy) / L) * L;
-		c.unrapx += d0;
-		c.unrapy += d1;
-		c.offx = (int) (c.offx + c.lx - d0) % c.lx;
-		c.offy = (int) (c.offy + c.ly - d1) % c.ly;
-		c.corner = ncorner;
-		c.resized = 0;
-		return;
-	}
-	const int nlx = c.lx - (2 * c.xl) + (2 * border);
-	const int nly = c.ly - (2 * c.yb) + (2 * border);
-	if(nlx <= 0 || nly <= 0 || nlx > L || nly > L || nlx > MAX_TABLE_SIDE || nly > MAX_TABLE_SIDE ||
-	   nlx * nly > MAX_PATCH_SITES) {
-		atomicOr(&st->err, ERR_CAPACITY);
-		st->err_where = ci;
-		c.resized = 0;
-		return;
-	}
-	const int ncorner = box_el(c.corner, -(-(2 * c.xl) + (2 * border)) / 2, -(-(2 * c.yb) + (2 * border)) / 2, L);
-	c.old_lx = c.lx;
-	c.old_ly = c.ly;
-	c.old_offx = c.offx;
-	c.old_offy = c.offy;
-	c.old_corner = c.corner;
-	{
-		const double ox = c.corner % L, oy = c.corner / L;
-		const double nx = ncorner % L, ny = ncorner / L;
-		c.unrapx += nx - ox - rint((nx - ox) / L) * L;
-		c.unrapy += ny - oy - rint((ny - oy) / L) * L;
-	}
-	c.lx = nlx;
-	c.ly = nly;
-	c.n = nlx * nly;
-	c.corner = ncorner;
-	c.offx = c.offy = 0;
-	const int site = box_el(c.corner, c.lx / 2, c.ly / 2, L);
-	c.comy = (int) (site / L);
-	c.comx = (int) (site - (int) (site / L) * L);
-	c.resized = 1;
-	atomicAdd(&st->resized, 1);
-	atomicAdd(&st->resized_total, 1);
-}
-
-__device__ void directed_forces_dev(CellDev &c, const DevParams &P, const PhaseParams &pu, int store, DevStatus *st,
-                                    int ci) {
-	const double dt = P.dt, JQ = pu.JQ;
-	if(P.model == M_POLAR) {
-		if(store) c.thq_old = c.thq + sqrt(dt) * pu.zi * c.gauss;
-		const double f0 = c.trx, f1 = c.try_;
-		c.thq = c.thq_old - dt * JQ * (atan2(f0 * c.q01 - f1 * c.q00, f0 * c.q00 + f1 * c.q01));
-		c.q00 = cos(c.thq);
-		c.q01 = sin(c.thq);
-	}
-	else if(P.model == M_WET) {
-		const double smod = sqrt(c.s00 * c.s00 + c.s01 * c.s01);
-		if(store) {
-			c.nq_oldx = c.nqx;
-			c.nq_oldy = c.nqy;
-		}
-		if(smod > 0.00000001) {
-			const double t = 0.5 * atan2(c.s01, c.s00);
-			const double d0 = cos(t), d1 = sin(t);
-			const double sgn = (d0 * c.nqx + d1 * c.nqy > 0.0) ? 1.0 : -1.0;
-			c.nqx = c.nq_oldx + dt * JQ * (sgn * d0 - c.nqx);
-			c.nqy = c.nq_oldy + dt * JQ * (sgn * d1 - c.nqy);
-			c.q00 = 0.5 * (c.nqx * c.nqx - c.nqy * c.nqy);
-			c.q01 = c.nqx * c.nqy;
-		}
-	}
-	else if(P.model == M_NEMATIC) {
-		if(store) {
-			c.nq_oldx = c.nqx;
-			c.nq_oldy = c.nqy;
-		}
-		if(c.type == 0) {
-			c.nqx = c.nq_oldx;
-			c.nqy = c.nq_oldy;
-		}
-		else if(c.type == 1) {
-			const double t = 0.5 * atan2(c.s01, c.s00);
-			const double d0 = cos(t), d1 = sin(t);
-			const double sgn = (d0 * c.nqx + d1 * c.nqy > 0.0) ? 1.0 : -1.0;
-			c.nqx = c.nq_oldx + dt * JQ * (sgn * d0 - c.nqx);
-			c.nqy = c.nq_oldy + dt * JQ * (sgn * d1 - c.nqy);
-			c.q00 = 0.5 * (c.nqx * c.nqx - c.nqy * c.nqy);
-			c.q01 = c.nqx * c.nqy;
-		}
-		else {
-			atomicOr(&st->err, ERR_TYPE);
-			st->err_where = ci;
-		}
-	}
-}
-
-// Per-cell epilogue of an evaluation / update (one thread): cell outputs,
-// area, centre of mass, set_positions, the per-cell scalar dynamics and the
-// bins of the next gather.  Shared by the FP64 and FP32 cell kernels.
-template<int MODEL, int EVAL, int UPD>
-__device__ __forceinline__ void cell_finish(CellDev &c, const double (&acc)[12], const int (&imin)[2], double perim,
-                                            const CellArgs &a, const LayerDev &lay, int ci) {
-	const DevParams &P = a.P;
-	const PhaseParams &pu = a.pu;
-	const int lx = c.lx, ly = c.ly, L = lay.L;
-	(void) lx;
-	(void) ly;
-	if(EVAL != EV_NONE) {
-		// per-cell outputs of the evaluation (perimeter, force totals)
-		c.perim = (MODEL == M_POLAR) ? perim : 0.0;
-		if(MODEL == M_POLAR) {
-			c.trx = acc[8];
-			c.try_ = acc[9];
-			c.tfx = acc[10];
-			c.tfy = acc[11];
-		}
-		else {
-			c.trx = c.try_ = c.tfx = c.tfy = 0.0;
-		}
-	}
-	if(UPD != UP_NONE) {
-		if(UPD == UP_PRED) {
-			c.com_oldx = c.comx;
-			c.com_oldy = c.comy;
-			c.area_old = c.area;
-			c.sumf_old = c.sumf;
-		}
-		c.area = acc[0];
-		c.sumf = acc[1];
-		c.s00 = acc[6];
-		c.s01 = acc[7];
-		c.perim = 0.0;
-		c.xl = (UPD == UP_CORR) ? imin[0] : lx;
-		c.yb = (UPD == UP_CORR) ? imin[1] : ly;
-		c.comx = c.lx * (atan2(-acc[3] / c.sumf, -acc[2] / c.sumf) + RC_PI_F) / (2 * RC_PI_F);
-		c.comy = c.ly * (atan2(-acc[5] / c.sumf, -acc[4] / c.sumf) + RC_PI_F) / (2 * RC_PI_F);
-		if(!isfinite(c.area) || !isfinite(c.sumf) || !isfinite(c.comx) || !isfinite(c.comy)) {
-			atomicOr(&a.st->err, ERR_NONFINITE);
-			a.st->err_where = ci;
-		}
-		if(UPD == UP_CORR) set_positions_dev(c, P, L, a.st, ci);
-		directed_forces_dev(c, P, pu, UPD == UP_PRED, a.st, ci);
-		if(UPD == UP_CORR) {
-			append_bins(c, ci, lay, a.bin_count, a.bin_cells, a.st);
-			atomicMax(&a.st->max_n, c.n);
-		}
-	}
-}
 
 // Forces of one site from the shared-memory patch (stage 2 of the evaluation)
 // and the update of that site.  Kept as one templated kernel so that the fused
@@ -736,384 +495,6 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 	}
 }
 
-// ---------------------------------------------------------------- FP32 ---
-// Double-float accumulation of x*x: (s, c) holds the running sum with its
-// error term (exact product by FMA, Knuth's TwoSum), close to FP64 accuracy
-// with FP32 arithmetic only.
-__device__ __forceinline__ void acc_square(float x, float &s, float &c) {
-	const float p = x * x;
-	const float ep = __fmaf_rn(x, x, -p);
-	const float t = s + p;
-	const float bp = t - s;
-	const float err = (s - (t - bp)) + (p - bp);
-	s = t;
-	c += err + ep;
-}
-
-// The dry polar model (wetpolarmodel with friction_cell = 0, the
-// ensemble's model) with FP32 site arithmetic: the patch, chemical
-// potential, forces and the update in FP32 (shared memory in FP32, fields
-// stored in FP64); the area integral sum(phi^2) that drives the area
-// constraint accumulates in double-float (near FP64), the other per-cell
-// sums from FP32 per-thread partials in FP64.  Same stages, expressions and per-cell
-// epilogue as cell_kernel<M_POLAR, ...>; not bitwise the reference.
-// Patch coordinates of q = threadIdx.x, threadIdx.x + blockDim.x, ... without
-// a per-site division: the stride's row and column steps are fixed per cell.
-struct PatchWalk {
-	int q, x, y, sx, sy, lx;
-	__device__ __forceinline__ PatchWalk(int lx_) : lx(lx_) {
-		q = threadIdx.x;
-		y = q / lx;
-		x = q - y * lx;
-		sy = (int) blockDim.x / lx;
-		sx = (int) blockDim.x - sy * lx;
-	}
-	__device__ __forceinline__ void next() {
-		q += blockDim.x;
-		x += sx;
-		y += sy;
-		if(x >= lx) {
-			x -= lx;
-			y += 1;
-		}
-	}
-};
-
-template<int EVAL, int UPD, int BLOCK>
-__global__ void __launch_bounds__(BLOCK) cell_kernel_f32(const CellArgs a) {
-	extern __shared__ __align__(16) unsigned char smem_raw[];
-	__shared__ CellDev c;
-	__shared__ double red[12 * (BLOCK / 32 + 1)];
-	__shared__ int ired[2 * (BLOCK / 32)];
-	const int ci = blockIdx.x;
-	{
-		const int *src = reinterpret_cast<const int *>(&a.cells[ci]);
-		int *dst = reinterpret_cast<int *>(&c);
-		for(int i = threadIdx.x; i < (int) (sizeof(CellDev) / 4); i += blockDim.x) dst[i] = src[i];
-	}
-	__syncthreads();
-	const LayerDev lay = a.layers[c.layer];
-	const int n = c.n, lx = c.lx, ly = c.ly, L = lay.L, start = c.start;
-	const double *phi2 = a.phi2 + lay.box_off;
-	const int cx0 = c.corner % L, cy0 = c.corner / L;
-	// box site of patch site (x, y): GetSubIndex without divisions
-	auto site_of = [&](int x, int y) {
-		int px = x + c.offx;
-		if(px >= lx) px -= lx;
-		int py = y + c.offy;
-		if(py >= ly) py -= ly;
-		int bx = cx0 + px;
-		if(bx >= L) bx -= L;
-		int by = cy0 + py;
-		if(by >= L) by -= L;
-		return bx + by * L;
-	};
-	if(n > a.smem_n) {
-		if(threadIdx.x == 0) {
-			atomicOr(&a.st->err, ERR_CAPACITY);
-			a.st->err_where = ci;
-		}
-		return;
-	}
-	float *sphi = reinterpret_cast<float *>(smem_raw);
-	float *smu = sphi + a.smem_n;
-	float *saux = smu + a.smem_n;
-	const DevParams &P = a.P;
-	const PhaseParams &pe = a.pe;
-	// Per-cell constants, formed once by thread 0: on GB300 an FP64 warp
-	// instruction (a division is ~10 of them) costs tens of issue cycles, too
-	// many to repeat in every thread.
-	enum { K_GAMMA, K_LAMBDA, K_OMEGA, K_RLAMBDA, K_AC, K_REPC, K_J0, K_HDT, K_ZS, K_ALPHA, K_RFR, K_Q00, K_Q01, K_BETA,
-	       K_HAS_BETA, K_HAS_OMEGA, K_N };
-	__shared__ float kc[K_N];
-	__shared__ double s_perim;
-	if(threadIdx.x == 0) {
-		kc[K_GAMMA] = (float) P.gamma;
-		kc[K_LAMBDA] = (float) P.lambda;
-		kc[K_OMEGA] = (float) P.omega;
-		kc[K_RLAMBDA] = (float) (1.0 / P.lambda);
-		kc[K_AC] = (float) (-4 * (P.mu / P.a0) * (1 - c.area / P.a0));
-		kc[K_REPC] = (float) (4 * (P.kappa / P.lambda));
-		kc[K_J0] = (float) P.J0;
-		kc[K_HDT] = (float) (P.dt * .5);
-		kc[K_ZS] = (float) pe.zs;
-		kc[K_ALPHA] = (float) P.passive_alpha;
-		kc[K_RFR] = (float) (1.0 / pe.friction);
-		kc[K_Q00] = (float) c.q00;
-		kc[K_Q01] = (float) c.q01;
-		kc[K_HAS_BETA] = pe.beta != 0.0 ? 1.f : 0.f;
-		kc[K_HAS_OMEGA] = P.omega != 0.0 ? 1.f : 0.f;
-	}
-	__syncthreads();
-	const float gamma = kc[K_GAMMA], lambda = kc[K_LAMBDA], omega = kc[K_OMEGA];
-	const float rlambda = kc[K_RLAMBDA], two_lambda = 2.f * lambda;
-	const float A_c = kc[K_AC], Rep_c = kc[K_REPC];
-	double perim = 0.0;
-	const bool has_beta = kc[K_HAS_BETA] != 0.f, has_omega = kc[K_HAS_OMEGA] != 0.f;
-	if(EVAL != EV_NONE) {
-		for(int q = threadIdx.x; q < n; q += blockDim.x) sphi[q] = d2f_int(a.phi_eval[start + q]);
-		__syncthreads();
-		if(has_beta) {
-			float pp = 0.f;
-			for(PatchWalk w(lx); w.q < n; w.next()) {
-				const int q = w.q, x = w.x, y = w.y;
-				const Nb nb = patch_nb(q, x, y, lx, ly);
-				const float dx = .5f * (sphi[nb.r] - sphi[nb.l]);
-				const float dy = .5f * (sphi[nb.u] - sphi[nb.d]);
-				pp += dx * dx + dy * dy;
-			}
-#pragma unroll
-			for(int o = 16; o > 0; o >>= 1) pp += __shfl_down_sync(0xffffffffu, pp, o);
-			__shared__ float s_pp[BLOCK / 32];
-			if((threadIdx.x & 31) == 0) s_pp[threadIdx.x >> 5] = pp;
-			__syncthreads();
-			if(threadIdx.x == 0) {
-				double t = 0.0;
-				for(int w = 0; w < (int) (blockDim.x >> 5); w++) t += (double) s_pp[w];
-				s_perim = t;
-				kc[K_BETA] = (float) (4 * (pe.beta / 12.) * (1 - t / 12.));
-			}
-			__syncthreads();
-			perim = s_perim;
-		}
-		const float beta_t = has_beta ? kc[K_BETA] : 0.f;
-		for(PatchWalk w(lx); w.q < n; w.next()) {
-			const int q = w.q, x = w.x, y = w.y;
-			const Nb nb = patch_nb(q, x, y, lx, ly);
-			const float phi = sphi[q];
-			const float pr = sphi[nb.r], pl = sphi[nb.l], pu_ = sphi[nb.u], pd = sphi[nb.d];
-			const int k = site_of(x, y);
-			const float p2 = d2f_int(phi2[k]);
-			const float lap = pu_ + pd + pr + pl - 4.f * phi;
-			const float CH = gamma * (8.f * phi * (1.f - phi) * (1.f - 2.f * phi) * rlambda - two_lambda * lap);
-			const float Rep = Rep_c * phi * (p2 - phi * phi);
-			float V = CH + A_c * phi + Rep;
-			if(has_omega) {
-				const BoxNb kb = box_nb(k, L);
-				const float ls = (float) (phi2[kb.r] + phi2[kb.u] + phi2[kb.l] + phi2[kb.d] - 4. * phi2[k]);
-				const float dx = .5f * (pr - pl), dy = .5f * (pu_ - pd);
-				const float lsq = 2.f * phi * lap + 2.f * (dx * dx + dy * dy);
-				const float sup = (ls - lsq) * rsqrtf(1.f + (ls - lsq) * (ls - lsq));
-				V = V + (-4.f * lambda * omega * sup * phi);
-			}
-			if(has_beta) V = V + beta_t * lap;
-			if(EVAL == EV_STORE) {
-				a.mu[start + q] = f2d_int(V);
-				a.dxg[start + q] = f2d_int(.5f * (pr - pl));
-				a.dyg[start + q] = f2d_int(.5f * (pu_ - pd));
-				a.mapg[start + q] = k;
-			}
-			if(a.rep_on) {
-				const float r = d2f_int(a.rep[start + q]) + Rep;
-				if(a.accumulate_rep) a.rep[start + q] = f2d_int(r);
-				saux[q] = r;
-			}
-			smu[q] = V;
-		}
-		__syncthreads();
-	}
-	double acc[12];
-#pragma unroll
-	for(int i = 0; i < 12; i++) acc[i] = 0.0;
-	float af[12];
-#pragma unroll
-	for(int i = 0; i < 12; i++) af[i] = 0.f;
-	int imin[2] = {lx, ly};
-	float area_s = 0.f, area_c = 0.f;
-	const float J0 = kc[K_J0], hdt = kc[K_HDT];
-	const bool conserved = P.conserved != 0;
-	const float zs = kc[K_ZS], alpha = kc[K_ALPHA], lam = lambda;
-	const float rfr = kc[K_RFR];
-	const int tb = table_base(lx), tby = table_base(ly);
-	const float q00 = kc[K_Q00], q01 = kc[K_Q01];
-	for(PatchWalk w(lx); w.q < n; w.next()) {
-		const int q = w.q, x = w.x, y = w.y;
-		float mu, vx, vy, dx, dy, phi_e = 0.f;
-		if(EVAL != EV_NONE) {
-			const Nb nb = patch_nb(q, x, y, lx, ly);
-			phi_e = sphi[q];
-			dx = .5f * (sphi[nb.r] - sphi[nb.l]);
-			dy = .5f * (sphi[nb.u] - sphi[nb.d]);
-			mu = smu[q];
-			const float fpx = -.5f * (smu[nb.r] - smu[nb.l]);
-			const float fpy = -.5f * (smu[nb.u] - smu[nb.d]);
-			if(a.rep_on) {
-				af[8] += -.5f * (saux[nb.r] - saux[nb.l]) * phi_e;
-				af[9] += -.5f * (saux[nb.u] - saux[nb.d]) * phi_e;
-			}
-			const float sx = -dx * q00, sy = -dy * q01;
-			const float fsx = sx < 0.f ? 0.f : lam * sx * q00;
-			const float fsy = sy < 0.f ? 0.f : lam * sy * q01;
-			const float fx = fpx * alpha + fsx * zs;
-			const float fy = fpy * alpha + fsy * zs;
-			af[10] += fx * phi_e;
-			af[11] += fy * phi_e;
-			vx = fx * rfr;
-			vy = fy * rfr;
-			if(EVAL == EV_STORE) {
-				a.vxg[start + q] = f2d_int(vx);
-				a.vyg[start + q] = f2d_int(vy);
-			}
-		}
-		else {
-			mu = d2f_int(a.mu[start + q]);
-			vx = d2f_int(a.vxg[start + q]);
-			vy = d2f_int(a.vyg[start + q]);
-			dx = d2f_int(a.dxg[start + q]);
-			dy = d2f_int(a.dyg[start + q]);
-		}
-		if(UPD == UP_NONE) continue;
-		float dphi;
-		if(conserved) {
-			// FD_CH (FD_CHBackend.cpp:63-68); the polar model keeps every
-			// neighbour's freeEnergy through the loop (WetPolarModel.cpp:130)
-			const Nb nb = patch_nb(q, x, y, lx, ly);
-			auto fe = [&](int s_) {
-				return (EVAL != EV_NONE) ? smu[s_] : d2f_int(a.mu[start + s_]);
-			};
-			const float lmu = fe(nb.r) + fe(nb.u) + fe(nb.l) + fe(nb.d) - 4.f * mu;
-			dphi = J0 * lmu - vx * dx - vy * dy;
-		}
-		else
-			dphi = -J0 * mu - vx * dx - vy * dy;
-		float phi_new;
-		if(UPD == UP_PRED) {
-			const float phi_old = (EVAL != EV_NONE) ? phi_e : d2f_int(a.phi_eval[start + q]);
-			a.dphi_old[start + q] = f2d_int(dphi);
-			phi_new = phi_old + hdt * (dphi + dphi);
-		}
-		else {
-			phi_new = d2f_int(a.phi_old[start + q]) + hdt * (dphi + d2f_int(a.dphi_old[start + q]));
-		}
-		a.phi_out[start + q] = f2d_int(phi_new);
-		acc_square(phi_new, area_s, area_c);
-		af[1] += phi_new;
-		int lxx = x + c.offx;
-		if(lxx >= lx) lxx -= lx;
-		int lyy = y + c.offy;
-		if(lyy >= ly) lyy -= ly;
-		af[2] += phi_new * a.tab_cosf[tb + lxx];
-		af[3] += phi_new * a.tab_sinf[tb + lxx];
-		af[4] += phi_new * a.tab_cosf[tby + lyy];
-		af[5] += phi_new * a.tab_sinf[tby + lyy];
-		if(UPD == UP_CORR && phi_new < 0.09f && phi_new > 0.01f) {
-			imin[0] = min(imin[0], lxx);
-			imin[1] = min(imin[1], lyy);
-		}
-		af[6] += -.5f * (dx * dx - dy * dy);
-		af[7] += -dx * dy;
-	}
-	if(a.split) {
-		// per-warp partials for the epilogue kernel: FP32 warp trees, the area
-		// as a double-float pair, converted once per warp
-		const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-		for(int o = 16; o > 0; o >>= 1) {
-			const float s2 = __shfl_down_sync(0xffffffffu, area_s, o);
-			const float c2 = __shfl_down_sync(0xffffffffu, area_c, o);
-			const float t = area_s + s2, bp = t - area_s;
-			area_c += ((area_s - (t - bp)) + (s2 - bp)) + c2;
-			area_s = t;
-#pragma unroll
-			for(int i = 1; i < 12; i++) af[i] += __shfl_down_sync(0xffffffffu, af[i], o);
-		}
-		if(UPD == UP_CORR) block_min<2>(imin, ired);
-		CellSum &o = a.csum[ci];
-		if(lane == 0) {
-			o.area[warp] = (double) area_s + (double) area_c;
-#pragma unroll
-			for(int i = 1; i < 12; i++) o.part[warp][i] = af[i];
-		}
-		if(threadIdx.x == 0) {
-			o.imin[0] = imin[0];
-			o.imin[1] = imin[1];
-			o.nw = BLOCK / 32;
-			o.perim = perim;
-		}
-		return;
-	}
-	acc[0] = (double) area_s + (double) area_c;
-	// per-cell sums: warp trees in FP32 (the area term in FP64), then the
-	// warps' partial sums in FP64 by one warp; the totals are needed by thread 0 only
-	{
-		const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-		for(int o = 16; o > 0; o >>= 1) {
-			acc[0] += __shfl_down_sync(0xffffffffu, acc[0], o);
-#pragma unroll
-			for(int i = 1; i < 12; i++) af[i] += __shfl_down_sync(0xffffffffu, af[i], o);
-		}
-		if(lane == 0) {
-			red[warp] = acc[0];
-#pragma unroll
-			for(int i = 1; i < 12; i++) red[i * nw + warp] = (double) af[i];
-		}
-		__syncthreads();
-		if(warp == 0) {
-#pragma unroll
-			for(int i = 0; i < 12; i++) {
-				double t = lane < nw ? red[i * nw + lane] : 0.0;
-#pragma unroll
-				for(int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-				acc[i] = t;
-			}
-		}
-	}
-	if(UPD == UP_CORR) block_min<2>(imin, ired);
-	if(threadIdx.x == 0) cell_finish<M_POLAR, EVAL, UPD>(c, acc, imin, perim, a, lay, ci);
-	__syncthreads();
-	{
-		const int *src = reinterpret_cast<const int *>(&c);
-		int *dst = reinterpret_cast<int *>(&a.cells[ci]);
-		for(int i = threadIdx.x; i < (int) (sizeof(CellDev) / 4); i += blockDim.x) dst[i] = src[i];
-	}
-}
-
-template<int BLOCK>
-static bool launch_f32_block(int eval, int upd, const CellArgs &a, cudaStream_t s) {
-	const size_t smem = sizeof(float) * 3 * (size_t) a.smem_n;
-	if(eval == EV_LOCAL && upd == UP_PRED) cell_kernel_f32<EV_LOCAL, UP_PRED, BLOCK><<<a.N, BLOCK, smem, s>>>(a);
-	else if(eval == EV_LOCAL && upd == UP_CORR) cell_kernel_f32<EV_LOCAL, UP_CORR, BLOCK><<<a.N, BLOCK, smem, s>>>(a);
-	else if(eval == EV_NONE && upd == UP_PRED) cell_kernel_f32<EV_NONE, UP_PRED, BLOCK><<<a.N, BLOCK, smem, s>>>(a);
-	else if(eval == EV_STORE && upd == UP_NONE) cell_kernel_f32<EV_STORE, UP_NONE, BLOCK><<<a.N, BLOCK, smem, s>>>(a);
-	else return false;
-	return true;
-}
-
-bool launch_cell_kernel_f32(int eval, int upd, const CellArgs &a, cudaStream_t s, int block) {
-	if(a.N <= 0) return true;
-	if(block == 128) return launch_f32_block<128>(eval, upd, a, s);
-	if(block == 512) return launch_f32_block<512>(eval, upd, a, s);
-	return launch_f32_block<256>(eval, upd, a, s);
-}
-
-template<int BLOCK>
-static cudaError_t configure_f32_block() {
-	cudaError_t e = cudaSuccess, c;
-	const int mx = 200 * 1024;
-	if((c = cudaFuncSetAttribute(cell_kernel_f32<EV_LOCAL, UP_PRED, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx)) !=
-	   cudaSuccess)
-		e = c;
-	if((c = cudaFuncSetAttribute(cell_kernel_f32<EV_LOCAL, UP_CORR, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx)) !=
-	   cudaSuccess)
-		e = c;
-	if((c = cudaFuncSetAttribute(cell_kernel_f32<EV_NONE, UP_PRED, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx)) !=
-	   cudaSuccess)
-		e = c;
-	if((c = cudaFuncSetAttribute(cell_kernel_f32<EV_STORE, UP_NONE, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx)) !=
-	   cudaSuccess)
-		e = c;
-	return e;
-}
-
-static cudaError_t configure_f32() {
-	cudaError_t e = cudaSuccess, c;
-	if((c = configure_f32_block<128>()) != cudaSuccess) e = c;
-	if((c = configure_f32_block<256>()) != cudaSuccess) e = c;
-	if((c = configure_f32_block<512>()) != cudaSuccess) e = c;
-	return e;
-}
-
 // Split mode: the per-cell epilogue with one thread per cell, so that 32
 // cells share every FP64 instruction of the centre-of-mass, re-centering and
 // per-cell dynamics code (the same cell_finish the fused kernels run).
@@ -1160,11 +541,8 @@ static void launch_finish_m(int eval, int upd, const CellArgs &a, cudaStream_t s
 void launch_cell_finish(int model, int eval, int upd, bool f32, const CellArgs &a, cudaStream_t s) {
 	if(a.N <= 0) return;
 	if(f32) {
-		const int g = (a.N + 127) / 128;
-		if(eval == EV_LOCAL && upd == UP_PRED) cell_finish_kernel<M_POLAR, EV_LOCAL, UP_PRED, true><<<g, 128, 0, s>>>(a);
-		else if(eval == EV_LOCAL && upd == UP_CORR) cell_finish_kernel<M_POLAR, EV_LOCAL, UP_CORR, true><<<g, 128, 0, s>>>(a);
-		else if(eval == EV_STORE && upd == UP_NONE) cell_finish_kernel<M_POLAR, EV_STORE, UP_NONE, true><<<g, 128, 0, s>>>(a);
-		else cell_finish_kernel<M_POLAR, EV_NONE, UP_PRED, true><<<g, 128, 0, s>>>(a);
+		if(model == M_POLAR) launch_finish_m<M_POLAR, true>(eval, upd, a, s);
+		else launch_finish_m<M_WET, true>(eval, upd, a, s);
 		return;
 	}
 	switch(model) {
@@ -1331,7 +709,7 @@ cudaError_t configure_kernels() {
 	if((c = configure_m<M_NEMATIC>()) != cudaSuccess) e = c;
 	if((c = configure_m<M_POLAR>()) != cudaSuccess) e = c;
 	if((c = configure_m<M_WET>()) != cudaSuccess) e = c;
-	if((c = configure_f32()) != cudaSuccess) e = c;
+	if((c = configure_kernels_f32()) != cudaSuccess) e = c;
 	unsigned long long A[2 * CELL_THREADS + 1], Cc[2 * CELL_THREADS + 1];
 	const unsigned long long a = 0x5DEECE66DULL, cc = 0xBULL, M = (1ULL << 48) - 1;
 	A[0] = 1;

@@ -251,14 +251,15 @@ static CellArgs cell_args(rc_engine *e) {
 }
 
 // Cell kernel launch: the FP32 variant where the engine runs
-// RC_PRECISION_FLOAT and one exists for (eval, upd), else FP64; in split
+// RC_PRECISION_FLOAT (polar and wet nematic models), else FP64; in split
 // mode (many cells) followed by the per-cell epilogue kernel.  Returns the
 // number of kernels launched.
 static int cell_launch(rc_engine *e, int eval, int upd, const CellArgs &a0, cudaStream_t s) {
 	CellArgs a = a0;
 	a.split = e->csum != nullptr;
 	a.csum = e->csum;
-	const bool f32 = e->hp.precision == RC_PRECISION_FLOAT && launch_cell_kernel_f32(eval, upd, a, s, e->f32_block);
+	const bool f32 =
+	    e->hp.precision == RC_PRECISION_FLOAT && launch_cell_kernel_f32(e->P.model, eval, upd, a, s, e->f32_block);
 	if(!f32) launch_cell_kernel(e->P.model, eval, upd, a, s);
 	if(!a.split) return 1;
 	launch_cell_finish(e->P.model, eval, upd, f32, a, s);
@@ -329,7 +330,8 @@ static int solve_args(rc_engine *e, int phase, int solver, bool harvest, double 
 	g.xi = e->ph[phase].friction;
 	g.eta = e->ph[phase].friction_cell;
 	g.tol = e->hp.cg_tolerance > 0 ? e->hp.cg_tolerance : 2.220446049250313e-16;
-	g.mixed = e->hp.precision == RC_PRECISION_MIXED;
+	// FP32 engines solve in mixed precision (FP32 inner iterations, FP64 refinement)
+	g.mixed = e->hp.precision == RC_PRECISION_MIXED || e->hp.precision == RC_PRECISION_FLOAT;
 	g.inner_tol = 1e-4;
 	g.rxf = e->rxf;
 	g.ryf = e->ryf;
@@ -344,6 +346,7 @@ static int solve_args(rc_engine *e, int phase, int solver, bool harvest, double 
 	g.spin_limit = e->spin_limit;
 	g.barrier_extra = e->barrier_extra;
 	int blocks = e->cg_blocks;
+	if(solver == RC_SOLVER_PLAIN_FP64) g.mixed = 0;  // Eigen's Jacobi CG in FP64 whatever the precision
 	if(g.mixed && solver == RC_SOLVER_PLAIN) {
 		// mixed precision: Jacobi-preconditioned flexible CG in cover order
 		g.fcg = 1;
@@ -751,8 +754,8 @@ static int create_engine(const rc_params *params, int n_layers, const rc_box *bo
 		return set_err(nullptr, RC_ERR_INVALID, "unknown precision %d", params->precision);
 	const bool any_wet = (params->model == RC_WETMODEL || params->model == RC_WETPOLARMODEL) &&
 	                     (params->friction_cell[0] != 0.0 || params->friction_cell[1] != 0.0);
-	if(params->precision == RC_PRECISION_FLOAT && (params->model != RC_WETPOLARMODEL || any_wet))
-		return set_err(nullptr, RC_ERR_UNSUPPORTED, "FP32 fields are provided for the dry polar model only");
+	if(params->precision == RC_PRECISION_FLOAT && params->model != RC_WETPOLARMODEL && params->model != RC_WETMODEL)
+		return set_err(nullptr, RC_ERR_UNSUPPORTED, "FP32 site arithmetic is provided for wetpolarmodel and wetmodel only");
 	if(n_layers > 1 && any_wet)
 		return set_err(nullptr, RC_ERR_UNSUPPORTED, "batches of monolayers are provided for dry evaluations only");
 	std::vector<LayerDev> layers((size_t) n_layers);
@@ -891,7 +894,7 @@ static int create_engine(const rc_params *params, int n_layers, const rc_box *bo
 		   (rc = dalloc(e, &e->Px, L2)) || (rc = dalloc(e, &e->Py, L2)) ||
 		   (rc = dalloc(e, &e->partials, 8 * 4096)) || (rc = dalloc(e, &e->scalars, 64)) || (rc = dalloc(e, &e->bar, 4)))
 			return bail(rc);
-		if(params->precision == RC_PRECISION_MIXED) {
+		if(params->precision == RC_PRECISION_MIXED || params->precision == RC_PRECISION_FLOAT) {
 			// FP32 inner iterations: the flexible CG in cover order, Jacobi-preconditioned
 			if((rc = dalloc(e, &e->rxf, cap)) || (rc = dalloc(e, &e->ryf, cap)) || (rc = dalloc(e, &e->pxf, cap)) ||
 			   (rc = dalloc(e, &e->pyf, cap)) || (rc = dalloc(e, &e->exf, cap)) || (rc = dalloc(e, &e->eyf, cap)) ||
@@ -1469,9 +1472,12 @@ int rc_learned_set_params(rc_engine *e, const double *params) {
 
 // Work arrays of `solver` (allocated on first use; the stream must be idle).
 static int prepare_solver(rc_engine *e, int solver, const char *who) {
-	if(solver != RC_SOLVER_PLAIN && solver != RC_SOLVER_LEARNED && solver != RC_SOLVER_LEARNED_FP32)
+	if(solver != RC_SOLVER_PLAIN && solver != RC_SOLVER_LEARNED && solver != RC_SOLVER_LEARNED_FP32 &&
+	   solver != RC_SOLVER_PLAIN_FP64)
 		return set_err(e, RC_ERR_INVALID, "%s: unknown solver %d", who, solver);
-	if(solver != RC_SOLVER_PLAIN) {
+	if(solver == RC_SOLVER_PLAIN_FP64 && !is_wet_engine(e))
+		return set_err(e, RC_ERR_UNSUPPORTED, "%s: the engine has no viscous solve", who);
+	if(solver == RC_SOLVER_LEARNED || solver == RC_SOLVER_LEARNED_FP32) {
 		if(!is_wet_engine(e)) return set_err(e, RC_ERR_UNSUPPORTED, "%s: the engine has no viscous solve", who);
 		if(e->L % 4 != 0 || e->L < 8)
 			return set_err(e, RC_ERR_UNSUPPORTED, "%s: box side %d is not a multiple of 4", who, e->L);

@@ -129,9 +129,11 @@ struct CGArgs {
 
 cudaError_t configure_kernels();
 void launch_cell_kernel(int model, int eval, int upd, const CellArgs &a, cudaStream_t s);
-// FP32 site arithmetic for the dry polar model; false if (eval, upd) has no FP32 variant
-// block: threads per cell (CELL_F32_BLOCKS); false if (eval, upd, block) has no kernel
-bool launch_cell_kernel_f32(int eval, int upd, const CellArgs &a, cudaStream_t s, int block);
+// FP32 site arithmetic (rc_cells_f32.cu) for the polar and wet nematic
+// models; block: threads per cell (CELL_F32_BLOCKS); false if the model has
+// no FP32 kernel
+bool launch_cell_kernel_f32(int model, int eval, int upd, const CellArgs &a, cudaStream_t s, int block);
+cudaError_t configure_kernels_f32();
 // split mode: the per-cell epilogue, one thread per cell (f32: after the FP32 kernel)
 void launch_cell_finish(int model, int eval, int upd, bool f32, const CellArgs &a, cudaStream_t s);
 size_t cell_smem_bytes(int model, int smem_n);

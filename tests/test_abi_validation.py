@@ -52,11 +52,12 @@ def test_create_rejects_bad_parameters(lib):
     bad.anchoring = 1
     assert _create(lib, bad, L, cells)[0] == abi.RC_ERR_UNSUPPORTED
 
-    # FP32 fields exist for the dry polar model only; this is the wet model
+    # FP32 site arithmetic exists for wetpolarmodel and wetmodel; not for activenematic
     bad = abi.RcParams.from_buffer_copy(p)
     bad.precision = abi.RC_PRECISION_FLOAT
+    bad.model = abi.RC_ACTIVENEMATIC
     rc, msg = _create(lib, bad, L, cells)
-    assert rc == abi.RC_ERR_UNSUPPORTED and "dry polar" in msg
+    assert rc == abi.RC_ERR_UNSUPPORTED and "wetpolarmodel and wetmodel only" in msg
 
 
 def test_create_rejects_bad_box_and_cells(lib):

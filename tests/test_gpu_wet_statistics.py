@@ -1,5 +1,6 @@
-"""Ensemble statistics of long wet runs: the mixed-precision solve and the
-learned solve against the plain FP64 path.
+"""Ensemble statistics of long wet runs: the mixed-precision solve, the
+learned solve and FP32 site arithmetic (with either solve) against the plain
+FP64 path.
 
 Active wet monolayers are chaotic, so trajectories from the same start
 separate once rounding differences grow; the runs are compared by their
@@ -92,6 +93,21 @@ def test_learned_solver_statistics_within_one_percent(wet256, solver):
     e.step(WARM)
     e.set_params(params)
     e.set_solver(solver)
+    got = statistics(e, m.L)
+    assert e.stats.cg_max_rel_residual < 1e-8
+    _check(got, base)
+
+
+@pytest.mark.parametrize("solver", [abi.RC_SOLVER_PLAIN, abi.RC_SOLVER_LEARNED])
+def test_fp32_fields_statistics_within_one_percent(wet256, solver):
+    """FP32 site arithmetic (RC_PRECISION_FLOAT) with the mixed-precision
+    solve, plain (Jacobi inner iterations) or learned."""
+    keys, m, params, base = wet256
+    e = _engine(keys, m, abi.RC_PRECISION_FLOAT)
+    e.step(WARM)
+    if solver != abi.RC_SOLVER_PLAIN:
+        e.set_params(params)
+        e.set_solver(solver)
     got = statistics(e, m.L)
     assert e.stats.cg_max_rel_residual < 1e-8
     _check(got, base)
