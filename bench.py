@@ -253,6 +253,28 @@ def prepare_learned(args, eng, lib):
             "velocity_rel_err_vs_fp64": accuracy}
 
 
+def field_errors(args, eng_device=0, steps=20):
+    """Error of every reported field against the FP64 engine: the training
+    workload (256^2, same physics) run from the same start in FP64 and in
+    the benchmarked precision for `steps` steps; max |a - b| / max |b|."""
+    from rheocell_gb300 import abi
+    name = args.train_workload or "wet256"
+    prec = {"mixed": abi.RC_PRECISION_MIXED, "float": abi.RC_PRECISION_FLOAT}[args.precision]
+    a = make_engine(name, abi.RC_PRECISION_DOUBLE, eng_device)
+    b = make_engine(name, prec, eng_device)
+    a.step(steps)
+    b.step(steps)
+    sa, sb = a.state(), b.state()
+    a.close()
+    b.close()
+    out = {"workload": workload(name)["name"], "steps": steps,
+           "how": "FP64 engine vs this precision from the same start, plain solves, max |a-b| / max |a|"}
+    for k in ("phi", "vx", "vy", "mu", "area", "sum_f", "com_x", "com_y"):
+        den = max(float(abs(sa[k]).max()), 1e-300)
+        out[k] = float(abs(sb[k] - sa[k]).max()) / den
+    return out
+
+
 def velocity_error(eng):
     """The last evaluation's viscous system solved again from a cold start
     by the plain FP64 CG and by the learned flexible CG (rc_viscous_resolve,
@@ -442,9 +464,28 @@ def run_gb300(args, rank, world):
         out["config"]["cell_tile_threads"] = tuned["chosen"]
         out["autotune"] = {"candidates_ms_per_step": {str(t): round(ms, 4) for t, ms in tuned["candidates"]},
                            "chosen": tuned["chosen"]}
+    # the phi update (the per-cell update kernels) against its roofline, by
+    # the minimal wet-stage bytes per site (predictor: read phi, vx, vy,
+    # write phi*, dphi = 40 B; corrector: read phi*, phi^n, dphi, vx, vy,
+    # write phi = 48 B; FP64 storage) and by the bytes the kernels move
+    # (they also read the force evaluation's mu and gradients: 64 B)
+    iu = names.index("update")
+    if tn[iu] and args.workload.startswith("wet"):
+        upd_s = tms[iu] / tn[iu] / 1e3
+        out["phi_update"] = {
+            "launch_ms": upd_s * 1e3, "launches": int(tn[iu]),
+            "achieved_gbs": 44.0 * S / upd_s / 1e9, "frac": 44.0 * S / upd_s / 1e9 / peak,
+            "algorithmic_bytes_per_site": 44.0, "moved_bytes_per_site": 64.0,
+            "moved_gbs": 64.0 * S / upd_s / 1e9, "moved_frac": 64.0 * S / upd_s / 1e9 / peak,
+            "peak": peak, "unit": "GB/s"}
     if learned is not None:
         out["learned_pcg"] = learned
-        out["dtype"] = "f64 fields, f32 solve inner iterations, learned preconditioner"
+        out["dtype"] = {"double": "f64 fields, f32 solve inner iterations, bf16 learned preconditioner",
+                        "mixed": "f64 fields, f32 solve inner iterations, bf16 learned preconditioner",
+                        "float": "f32 site arithmetic (f64 field storage and cell-area integrals), f32 solve "
+                                 "inner iterations with f64 refinement, bf16 learned preconditioner"}[args.precision]
+    if args.precision != "double" and args.workload.startswith("wet"):
+        out["field_error_vs_fp64"] = field_errors(args, eng_device=dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, w, members)
         if out["cpu_baseline"]["kind"] == "reference" and len(members) == 1:
@@ -623,7 +664,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="wet1024", choices=["wet1024", "wet512", "wet256", "dry140", "ensemble64"])
-    ap.add_argument("--precision", default="double", choices=["double", "mixed", "float"])
+    ap.add_argument("--precision", default=None, choices=["double", "mixed", "float"],
+                    help="default: float (FP32 site arithmetic) for the wet workloads, double otherwise")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--solver", default=None, choices=["plain", "learned"],
                     help="viscous solver (default: learned for the wet workloads)")
@@ -640,6 +682,8 @@ def main():
     ap.add_argument("--train-lr", type=float, default=2e-3)
     ap.add_argument("--train-lr-final", type=float, default=0.05, help="final step size as a fraction of --train-lr")
     args = ap.parse_args()
+    if args.precision is None:
+        args.precision = "float" if args.workload.startswith("wet") else "double"
     if args.solver is None:
         args.solver = "learned" if args.workload.startswith("wet") else "plain"
     world = int(os.environ.get("WORLD_SIZE", "1"))

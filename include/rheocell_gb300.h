@@ -80,7 +80,7 @@ typedef struct rc_params {
 	double passive_alpha;  /* wet models                                        */
 	double cg_tolerance;   /* CGtolerance; <= 0 means Eigen's default (epsilon) */
 	int cg_restart_every;  /* warm solves between cold restarts: 100 (wetmodel), 10 (wetpolarmodel) */
-	int anchoring;         /* reserved; must be 0 (walls are out of scope)      */
+	int anchoring;         /* reserved; must be 0 (update_anchoring is not provided) */
 	double friction[2];    /* xi                                               */
 	double friction_cell[2]; /* eta; 0 selects the dry path v = f / xi         */
 	double zetaQ_self[2];
@@ -95,10 +95,29 @@ typedef struct rc_params {
 	/* 1: conserved dynamics of sim_type = FD_CH (src/Backends/FD_CHBackend.cpp:44-118),
 	 * d(phi)/dt = J0 lap(mu) - v.grad(phi); 0: FD_CPU, d(phi)/dt = -J0 mu - v.grad(phi) */
 	int conserved;
+	/* wall_slip (src/Interactions/BaseInteraction.cpp:10,23; 0.5 unless set):
+	 * a box site whose wall value is below it is open; used only with walls */
+	double wall_slip;
 } rc_params;
 
+/*
+ * The simulation box: a periodic square of Lx x Ly sites (Lx == Ly;
+ * src/Boxes/SquareBox.cpp).  `walls` (NULL: none) holds Lx*Ly values of the
+ * box's getWalls(k) for the square wall boxes (box = square with type =
+ * square_walls, circle_walls or triangle_walls: SquareWalls.cpp:23-55,
+ * CircleWalls.cpp:23-45, TriangleWalls.cpp:24-60), copied at create.  With
+ * walls, the stencils, the adhesion term and the forces of the wetmodel,
+ * wetpolarmodel and simplemultifield interactions take the reference's wall
+ * branches (BaseInteraction.h:196-263, WetModel.cpp:531-536,664-690,
+ * WetPolarModel.cpp:267-272,329-337); activenematic ignores walls, as the
+ * reference's does.  A viscous solve with walls is not provided
+ * (RC_ERR_UNSUPPORTED): the reference's wall rows make its assembled matrix
+ * unsymmetric (WetModel.cpp:295-335), and its upper-triangle CG then
+ * depends on the order of the unknowns.
+ */
 typedef struct rc_box {
-	int Lx, Ly;            /* periodic square box (src/Boxes/SquareBox.cpp) */
+	int Lx, Ly;
+	const double *walls;
 } rc_box;
 
 /*

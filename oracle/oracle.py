@@ -48,10 +48,11 @@ def lib() -> C.CDLL:
 class OracleSim:
     """Same surface as rheocell_gb300.engine.Engine, on the CPU restatement."""
 
-    def __init__(self, params: abi.RcParams, L: int, cells: HostCells):
+    def __init__(self, params: abi.RcParams, L: int, cells: HostCells, walls=None):
         self._lib = lib()
         self.h = C.c_void_p()
-        box = abi.RcBox(L, L)
+        walls = None if walls is None else np.ascontiguousarray(walls, dtype=np.float64)
+        box = abi.make_box(L, walls)
         rc = self._lib.orc_create(C.byref(params), C.byref(box), cells.n, cells.arr, C.byref(self.h))
         if rc != 0:
             msg = self._lib.orc_last_error(self.h).decode()

@@ -72,6 +72,7 @@ struct orc_sim {
 	double next_g;
 	char err[512];
 	rc_step_stats st;
+	double *walls;  /* box->getWalls(k), NULL for the periodic square box */
 };
 
 static int fail(orc_sim *s, int code, const char *fmt, ...) {
@@ -141,6 +142,45 @@ static inline int sub_index(const orc_sim *s, const ocell *c, int q) {
 	return box_el(s, c->corner, (lxs + c->off[0]) % c->lx, (lys + c->off[1]) % c->ly);
 }
 
+/* ------------------------------------------------------------- walls --- */
+/* A box site is open when it has no walls or its wall value is below
+ * wall_slip (BaseInteraction.h:196-263 tests getWalls(k) < wall_slip). */
+static inline int open_site(const orc_sim *s, int k) { return !s->walls || s->walls[k] < s->P.wall_slip; }
+
+/* BaseInteraction::derivX, derivY and Laplacian (BaseInteraction.h:196-263)
+ * at patch site q of cell c covering box site k: the central differences
+ * and the five-point Laplacian, with the reference's one-sided forms where
+ * a box neighbour of k is a wall site. */
+static void wall_stencils(const orc_sim *s, const ocell *c, int q, int k, double *dx, double *dy, double *lap) {
+	const double phi = c->phi[q];
+	const double r = c->phi[patch_nb(c, q, 5)], l = c->phi[patch_nb(c, q, 3)];
+	const double u = c->phi[patch_nb(c, q, 7)], d = c->phi[patch_nb(c, q, 1)];
+	const int R = open_site(s, box_nb(s, k, 5)), Lf = open_site(s, box_nb(s, k, 3));
+	const int U = open_site(s, box_nb(s, k, 7)), D = open_site(s, box_nb(s, k, 1));
+	*dx = (R && Lf) ? .5 * (r - l) : 0.;
+	*dy = (U && D) ? .5 * (u - d) : 0.;
+	if(!lap) return;
+	if(U && D) {
+		if(R && Lf) *lap = u + d + r + l - 4 * phi;
+		else if(R) *lap = u + d + 2 * r - 4 * phi;
+		else if(Lf) *lap = u + d + 2 * l - 4 * phi;
+		else *lap = u + d - 2 * phi;
+	}
+	else if(U) {
+		if(R && Lf) *lap = 2 * u + r + l - 4 * phi;
+		else if(R) *lap = 2 * u + 2 * r - 4 * phi;
+		else if(Lf) *lap = 2 * u + 2 * l - 4 * phi;
+		else *lap = 2 * u - 2 * phi;
+	}
+	else if(D) {
+		if(R && Lf) *lap = 2 * d + r + l - 4 * phi;
+		else if(R) *lap = 2 * d + 2 * r - 4 * phi;
+		else if(Lf) *lap = 2 * d + 2 * l - 4 * phi;
+		else *lap = 2 * d - 2 * phi;
+	}
+	else *lap = 0.;
+}
+
 static void make_tables(ocell *c) {
 	c->ctx = (double *) realloc(c->ctx, sizeof(double) * (size_t) c->lx);
 	c->stx = (double *) realloc(c->stx, sizeof(double) * (size_t) c->lx);
@@ -200,6 +240,10 @@ static void init_field_properties(orc_sim *s) {
 			c->fed[q] = 0.;
 			double dx = .5 * (c->phi[patch_nb(c, q, 5)] - c->phi[patch_nb(c, q, 3)]);
 			double dy = .5 * (c->phi[patch_nb(c, q, 7)] - c->phi[patch_nb(c, q, 1)]);
+			/* derivX/derivY (SimpleMultiField.cpp:97-98, WetModel.cpp:154-155,
+			 * WetPolarModel.cpp:119-120); ActiveNematic.cpp:127-128 keeps the
+			 * plain differences */
+			if(s->walls && s->P.model != RC_ACTIVENEMATIC) wall_stencils(s, c, q, sub_index(s, c, q), &dx, &dy, NULL);
 			c->dx[q] = dx;
 			c->dy[q] = dy;
 			c->s00 += -0.5 * (dx * dx - dy * dy);
@@ -252,6 +296,7 @@ static int global_sums(orc_sim *s) {
 			c->dx[q] = .5 * (r - l);
 			c->dy[q] = .5 * (u - d);
 			if(model != RC_SIMPLEFIELD) c->lap[q] = u + d + r + l - 4 * phi;
+			if(s->walls) wall_stencils(s, c, q, k, &c->dx[q], &c->dy[q], &c->lap[q]);
 			if(model == RC_WETPOLARMODEL) c->perim += c->dx[q] * c->dx[q] + c->dy[q] * c->dy[q];
 			c->tfx = c->tfy = c->trx = c->try_ = 0.;
 			c->mu[q] = 0.;
@@ -271,6 +316,12 @@ static int global_sums(orc_sim *s) {
 static inline double lap_square(const orc_sim *s, int k) {
 	return s->phi2[box_nb(s, k, 5)] + s->phi2[box_nb(s, k, 7)] + s->phi2[box_nb(s, k, 3)] + s->phi2[box_nb(s, k, 1)] - 4. * s->phi2[k];
 }
+/* the wet and polar models' laplacianSquare at a wall site keeps the x terms
+ * (WetModel.cpp:531-536, WetPolarModel.cpp:267-272) */
+static inline double lap_square_walls(const orc_sim *s, int k) {
+	if(open_site(s, k)) return lap_square(s, k);
+	return s->phi2[box_nb(s, k, 5)] + s->phi2[box_nb(s, k, 3)] - 2. * s->phi2[k];
+}
 
 static void f_interaction(orc_sim *s) {
 	const int model = s->P.model;
@@ -282,7 +333,11 @@ static void f_interaction(orc_sim *s) {
 			const int k = c->map[q];
 			const double phi = c->phi[q];
 			if(model == RC_SIMPLEFIELD) {
-				const double lap = c->phi[patch_nb(c, q, 7)] + c->phi[patch_nb(c, q, 1)] + c->phi[patch_nb(c, q, 5)] + c->phi[patch_nb(c, q, 3)] - 4 * phi;
+				double lap = c->phi[patch_nb(c, q, 7)] + c->phi[patch_nb(c, q, 1)] + c->phi[patch_nb(c, q, 5)] + c->phi[patch_nb(c, q, 3)] - 4 * phi;
+				if(s->walls) {
+					double dxw, dyw;
+					wall_stencils(s, c, q, k, &dxw, &dyw, &lap);
+				}
 				const double CH = gamma * (8 * phi * (1 - phi) * (1 - 2 * phi) / lambda - 2 * lambda * lap);
 				const double A = -4 * mu / a0 * (1 - c->area / a0) * phi;
 				const double Rep = 4 * kappa / lambda * phi * (s->phi2[k] - phi * phi);
@@ -309,7 +364,7 @@ static void f_interaction(orc_sim *s) {
 			}
 			else {
 				const double lap = c->lap[q];
-				const double ls = lap_square(s, k);
+				const double ls = lap_square_walls(s, k);
 				const double CH = gamma * (8 * phi * (1 - phi) * (1 - 2 * phi) / lambda - 2 * lambda * lap);
 				const double A = -4 * (mu / a0) * (1 - c->area / a0) * phi;
 				const double Rep = 4 * (kappa / lambda) * phi * (s->phi2[k] - phi * phi);
@@ -373,8 +428,10 @@ static void internal_forces(orc_sim *s) {
 				const double fsy = lambda * (-dy * c->q01) * th * c->q01;
 				fx = fpx * alpha + fsx * zs;
 				fy = fpy * alpha + fsy * zs;
-				c->tfx += fx * phi;
-				c->tfy += fy * phi;
+				if(open_site(s, k)) {
+					c->tfx += fx * phi;
+					c->tfy += fy * phi;
+				}
 			}
 			else { /* RC_WETMODEL */
 				const int kr = box_nb(s, k, 5), kl = box_nb(s, k, 3), ku = box_nb(s, k, 7), kd = box_nb(s, k, 1);
@@ -387,6 +444,7 @@ static void internal_forces(orc_sim *s) {
 				fx = fpx * alpha + fsx * zs + fix * zi;
 				fy = fpy * alpha + fsy * zs + fiy * zi;
 			}
+			if(!open_site(s, k)) fx = fy = 0.; /* WetModel.cpp:686-689, WetPolarModel.cpp:334-337 */
 			s->vfx[g] = fx;
 			s->vfy[g] = fy;
 			if(dry) {
@@ -751,6 +809,14 @@ int orc_create(const rc_params *params, const rc_box *box, int n_cells, const rc
 	if(params->model < RC_SIMPLEFIELD || params->model > RC_WETMODEL) return fail(s, RC_ERR_INVALID, "unknown model %d", params->model);
 	s->L = box->Lx;
 	s->N = n_cells;
+	if(box->walls) {
+		const int wet = (params->model == RC_WETMODEL || params->model == RC_WETPOLARMODEL) &&
+		                (params->friction_cell[0] != 0.0 || params->friction_cell[1] != 0.0);
+		if(wet) return fail(s, RC_ERR_UNSUPPORTED, "walls with a viscous solve are not provided");
+		s->walls = (double *) malloc(sizeof(double) * (size_t) s->L * (size_t) s->L);
+		if(!s->walls) return fail(s, RC_ERR_OOM, "out of memory");
+		memcpy(s->walls, box->walls, sizeof(double) * (size_t) s->L * (size_t) s->L);
+	}
 	s->rng = params->rng_state & 0xFFFFFFFFFFFFULL;
 	s->has_g = params->rng_has_cached;
 	s->next_g = params->rng_cached;
@@ -904,6 +970,7 @@ void orc_destroy(orc_sim *s) {
 		free(c->map);
 	}
 	free(s->c);
+	free(s->walls);
 	free(s->phi2);
 	free(s->sq00);
 	free(s->sq01);

@@ -73,12 +73,21 @@ class RcParams(C.Structure):
         ("friction", D2), ("friction_cell", D2), ("zetaQ_self", D2), ("zetaQ_inter", D2),
         ("J_Q", D2), ("beta", D2),
         ("rng_state", C.c_ulonglong), ("rng_has_cached", C.c_int), ("rng_cached", C.c_double),
-        ("conserved", C.c_int),
+        ("conserved", C.c_int), ("wall_slip", C.c_double),
     ]
 
 
 class RcBox(C.Structure):
-    _fields_ = [("Lx", C.c_int), ("Ly", C.c_int)]
+    _fields_ = [("Lx", C.c_int), ("Ly", C.c_int), ("walls", C.POINTER(C.c_double))]
+
+
+def make_box(L: int, walls=None) -> RcBox:
+    """An rc_box of side L; `walls` (L*L float64 values or None) must stay
+    alive until the call that reads the box returns."""
+    b = RcBox(L, L)
+    if walls is not None:
+        b.walls = walls.ctypes.data_as(C.POINTER(C.c_double))
+    return b
 
 
 DP = C.POINTER(C.c_double)

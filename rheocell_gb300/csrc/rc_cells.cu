@@ -41,6 +41,42 @@ __device__ __forceinline__ double div_rn(double x, double b, double rb) {
 	return __fma_rn(rem, rb, q);
 }
 
+// Wall boxes.  A box site is open when its wall value is below wall_slip
+// (BaseInteraction.h:196-263 test getWalls(k) < wall_slip); open_nb packs
+// the four box neighbours of k: bit 0 right, 1 left, 2 up, 3 down.
+__device__ __forceinline__ int open_nb(const double *walls, double slip, int k, int L) {
+	const BoxNb b = box_nb(k, L);
+	return (walls[b.r] < slip ? 1 : 0) | (walls[b.l] < slip ? 2 : 0) | (walls[b.u] < slip ? 4 : 0) |
+	       (walls[b.d] < slip ? 8 : 0);
+}
+
+// BaseInteraction::derivX, derivY and Laplacian (BaseInteraction.h:196-263)
+// of the shared patch at q, whose covering box site has open neighbours f:
+// the central differences vanish across a wall, and the Laplacian doubles
+// the open side of a direction that has one wall (the reference's branch
+// order and expressions, for bitwise equal results).
+__device__ __forceinline__ void wall_stencil(const double *sphi, const Nb &nb, int q, int f, double &dx, double &dy,
+                                             double &lap) {
+	const double phi = sphi[q], r = sphi[nb.r], l = sphi[nb.l], u = sphi[nb.u], d = sphi[nb.d];
+	const bool R = f & 1, Lf = f & 2, U = f & 4, D = f & 8;
+	dx = (R && Lf) ? .5 * (r - l) : 0.;
+	dy = (U && D) ? .5 * (u - d) : 0.;
+	if(U && D) {
+		if(R && Lf) lap = u + d + r + l - 4 * phi;
+		else if(R) lap = u + d + 2 * r - 4 * phi;
+		else if(Lf) lap = u + d + 2 * l - 4 * phi;
+		else lap = u + d - 2 * phi;
+	}
+	else if(U || D) {
+		const double v = U ? u : d;
+		if(R && Lf) lap = 2 * v + r + l - 4 * phi;
+		else if(R) lap = 2 * v + 2 * r - 4 * phi;
+		else if(Lf) lap = 2 * v + 2 * l - 4 * phi;
+		else lap = 2 * v - 2 * phi;
+	}
+	else lap = 0.;
+}
+
 
 // Forces of one site from the shared-memory patch (stage 2 of the evaluation)
 // and the update of that site.  Kept as one templated kernel so that the fused
@@ -64,6 +100,8 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 	const double *phi2 = a.phi2 + lay.box_off;
 	const double *sq00 = a.sq00 + lay.box_off;
 	const double *sq01 = a.sq01 + lay.box_off;
+	const double *walls = a.walls ? a.walls + lay.box_off : nullptr;  // wall boxes (null: periodic)
+	const double slip = a.P.wall_slip;
 	if(n > a.smem_n) {
 		if(threadIdx.x == 0) {
 			atomicOr(&a.st->err, ERR_CAPACITY);
@@ -117,8 +155,12 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 			for(int q = threadIdx.x; q < n; q += blockDim.x) {
 				const int y = q / lx, x = q - y * lx;
 				const Nb nb = patch_nb(q, x, y, lx, ly);
-				const double dx = .5 * (sphi[nb.r] - sphi[nb.l]);
-				const double dy = .5 * (sphi[nb.u] - sphi[nb.d]);
+				double dx = .5 * (sphi[nb.r] - sphi[nb.l]);
+				double dy = .5 * (sphi[nb.u] - sphi[nb.d]);
+				if(walls) {
+					double lw;
+					wall_stencil(sphi, nb, q, open_nb(walls, slip, box_site(c, x, y, L), L), dx, dy, lw);
+				}
 				v[0] += dx * dx + dy * dy;
 			}
 			block_sum<1>(v, red);
@@ -130,24 +172,31 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 			const Nb nb = patch_nb(q, x, y, lx, ly);
 			const double phi = sphi[q];
 			const double pr = sphi[nb.r], pl = sphi[nb.l], pu_ = sphi[nb.u], pd = sphi[nb.d];
-			const double dx = .5 * (pr - pl), dy = .5 * (pu_ - pd);
+			double dx = .5 * (pr - pl), dy = .5 * (pu_ - pd);
 			const int k = box_site(c, x, y, L);
 			const double p2 = phi2[k];
+			// wall boxes: the stencils of every model but activenematic, whose
+			// own plain differences ignore walls (ActiveNematic.cpp:176-230)
+			double lapw = 0.0;
+			const bool walled = MODEL != M_NEMATIC && walls != nullptr;
+			if(walled) wall_stencil(sphi, nb, q, open_nb(walls, slip, k, L), dx, dy, lapw);
 			double ls = 0.0;
 			if(omega != 0.0 && MODEL != M_SIMPLE) {
 				const BoxNb kb = box_nb(k, L);
-				ls = phi2[kb.r] + phi2[kb.u] + phi2[kb.l] + phi2[kb.d] - 4. * p2;
+				// at a wall site the polar and wet models keep the x terms
+				// (WetModel.cpp:531-536, WetPolarModel.cpp:267-272)
+				if(walled && !(walls[k] < slip)) ls = phi2[kb.r] + phi2[kb.l] - 2. * p2;
+				else ls = phi2[kb.r] + phi2[kb.u] + phi2[kb.l] + phi2[kb.d] - 4. * p2;
 			}
 			double mu = 0.0;
 			if(MODEL == M_SIMPLE) {
-				const double lap = pu_ + pd + pr + pl - 4 * phi;
+				const double lap = walled ? lapw : pu_ + pd + pr + pl - 4 * phi;
 				const double CH = gamma * (div_rn(8 * phi * (1 - phi) * (1 - 2 * phi), lambda, rlambda) - two_lambda * lap);
 				const double A = A_c * phi;
 				const double Rep = Rep_c * phi * (p2 - phi * phi);
 				mu = CH + A + Rep + 0.;
 				if(a.fsplit) {  // SimpleMultiField.cpp:158-181: pressure and free-energy density
 					a.fsplit[4 * a.fsplit_stride + start + q] = Rep - CH - A;
-					const double dx = .5 * (pr - pl), dy = .5 * (pu_ - pd);
 					const double CHd = (gamma / lambda) * 4 * phi * phi * (1 - phi) * (1 - phi) + gamma * lambda * (dx * dx + dy * dy);
 					const double Ad = -P.mu / P.a0 * phi * phi;
 					const double Repd = (P.kappa / lambda) * phi * phi * (p2 - phi * phi);
@@ -172,7 +221,7 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 				}
 			}
 			else {
-				const double lap = pu_ + pd + pr + pl - 4 * phi;
+				const double lap = walled ? lapw : pu_ + pd + pr + pl - 4 * phi;
 				const double CH = gamma * (div_rn(8 * phi * (1 - phi) * (1 - 2 * phi), lambda, rlambda) - two_lambda * lap);
 				const double A = A_c * phi;
 				const double Rep = Rep_c * phi * (p2 - phi * phi);
@@ -234,6 +283,16 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 			phi_e = sphi[q];
 			dx = .5 * (sphi[nb.r] - sphi[nb.l]);
 			dy = .5 * (sphi[nb.u] - sphi[nb.d]);
+			// wall boxes: stored gradients (not activenematic's), and the polar
+			// and wet forces vanish on wall sites (WetPolarModel.cpp:329-337,
+			// WetModel.cpp:664-690)
+			bool open_q = true;
+			if(MODEL != M_NEMATIC && walls != nullptr) {
+				const int kq = box_site(c, x, y, L);
+				double lw;
+				wall_stencil(sphi, nb, q, open_nb(walls, slip, kq, L), dx, dy, lw);
+				open_q = walls[kq] < slip;
+			}
 			mu = smu[q];
 			if(MODEL == M_SIMPLE) {
 				vx = 0.0;
@@ -262,12 +321,16 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 				else {
 					// Passive stress of WetModel.cpp:634-635 from neighbours' mu, f_d and gradients.
 					const double g2 = 2 * gamma * lambda;
+					// the neighbours' stored gradients, with the wall branches of
+					// their own box sites
 					auto grad_x = [&](int s, int sx, int sy) {
 						const Nb b = patch_nb(s, sx, sy, lx, ly);
+						if(walls != nullptr && (open_nb(walls, slip, box_site(c, sx, sy, L), L) & 3) != 3) return 0.;
 						return .5 * (sphi[b.r] - sphi[b.l]);
 					};
 					auto grad_y = [&](int s, int sx, int sy) {
 						const Nb b = patch_nb(s, sx, sy, lx, ly);
+						if(walls != nullptr && (open_nb(walls, slip, box_site(c, sx, sy, L), L) & 12) != 12) return 0.;
 						return .5 * (sphi[b.u] - sphi[b.d]);
 					};
 					const int xr = (x == lx - 1) ? 0 : x + 1, xl_ = (x == 0) ? lx - 1 : x - 1;
@@ -284,8 +347,8 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 					                   - 0.5 * ((dxu * fgyu_x) - (dxd * fgyd_x));
 					const double fpy = -0.5 * ((saux[nb2.u] - smu[nb2.u] * sphi[nb2.u] + dyu * fgyu) - (saux[nb2.d] - smu[nb2.d] * sphi[nb2.d] + dyd * fgyd))
 					                   - 0.5 * ((dyr * fgxr_y) - (dyl * fgxl_y));
-					const double fx = fpx * alpha + fsx * zs + fix * zi;
-					const double fy = fpy * alpha + fsy * zs + fiy * zi;
+					const double fx = open_q ? fpx * alpha + fsx * zs + fix * zi : 0.;
+					const double fy = open_q ? fpy * alpha + fsy * zs + fiy * zi : 0.;
 					if(a.fsplit) {  // WetModel.cpp:636-637,655-656
 						double *fs = a.fsplit + start + q;
 						fs[0] = fpx * alpha;
@@ -315,8 +378,8 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 				const double fsx = lambda * (-dx * c.q00) * th * c.q00;
 				th = (-dy * c.q01) < 0 ? 0.0 : 1.0;
 				const double fsy = lambda * (-dy * c.q01) * th * c.q01;
-				const double fx = fpx * alpha + fsx * zs;
-				const double fy = fpy * alpha + fsy * zs;
+				const double fx = open_q ? fpx * alpha + fsx * zs : 0.;
+				const double fy = open_q ? fpy * alpha + fsy * zs : 0.;
 				if(a.fsplit) {  // WetPolarModel.cpp:311-312,325-326
 					double *fs = a.fsplit + start + q;
 					fs[0] = fpx * alpha;
@@ -324,8 +387,10 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 					fs[2 * a.fsplit_stride] = zs * fsx;
 					fs[3 * a.fsplit_stride] = zs * fsy;
 				}
-				acc[10] += fx * phi_e;
-				acc[11] += fy * phi_e;
+				if(open_q) {
+					acc[10] += fx * phi_e;
+					acc[11] += fy * phi_e;
+				}
 				if(EVAL == EV_WET_RHS) {
 					a.fxg[start + q] = fx;
 					a.fyg[start + q] = fy;
@@ -420,6 +485,10 @@ __global__ void __launch_bounds__(CELL_THREADS) cell_kernel(const CellArgs a) {
 				const Nb nb = patch_nb(q, x, y, lx, ly);
 				dx = .5 * (sphi[nb.r] - sphi[nb.l]);
 				dy = .5 * (sphi[nb.u] - sphi[nb.d]);
+				if(MODEL == M_WET && walls != nullptr) {
+					double lw;
+					wall_stencil(sphi, nb, q, open_nb(walls, slip, box_site(c, x, y, L), L), dx, dy, lw);
+				}
 			}
 			else {
 				dx = a.dxg[start + q];

@@ -50,6 +50,7 @@ struct PhaseParams {
 struct DevParams {
 	int model, L, border, conserved;  // conserved: FD_CH dynamics
 	double dt, J0, gamma, lambda, omega, mu, kappa, passive_alpha, a0, cg_tol;
+	double wall_slip;  // open box sites have a wall value below it (wall boxes only)
 };
 
 struct CellDev {

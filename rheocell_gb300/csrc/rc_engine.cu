@@ -71,6 +71,7 @@ struct rc_engine {
 	double *vx = nullptr, *vy = nullptr, *fx = nullptr, *fy = nullptr, *rep = nullptr;
 	int *mapg = nullptr;
 	double *phi2 = nullptr, *sq00 = nullptr, *sq01 = nullptr;
+	double *walls = nullptr;  // getWalls(k) per box site of every layer; null: periodic boxes
 	int *cnt = nullptr, *cover = nullptr, *cov_off = nullptr, *cov_idx = nullptr;
 	int *bin_count = nullptr, *bin_cells = nullptr;
 	double *tab_cos = nullptr, *tab_sin = nullptr;
@@ -232,6 +233,7 @@ static CellArgs cell_args(rc_engine *e) {
 	a.mapg = e->mapg;
 	a.rep = e->rep;
 	a.phi2 = e->phi2;
+	a.walls = e->walls;
 	a.sq00 = e->sq00;
 	a.sq01 = e->sq01;
 	a.tab_cos = e->tab_cos;
@@ -758,6 +760,14 @@ static int create_engine(const rc_params *params, int n_layers, const rc_box *bo
 		return set_err(nullptr, RC_ERR_UNSUPPORTED, "FP32 site arithmetic is provided for wetpolarmodel and wetmodel only");
 	if(n_layers > 1 && any_wet)
 		return set_err(nullptr, RC_ERR_UNSUPPORTED, "batches of monolayers are provided for dry evaluations only");
+	bool has_walls = false;
+	for(int l = 0; l < n_layers; l++) has_walls |= boxes[l].walls != nullptr;
+	if(has_walls && any_wet)
+		return set_err(nullptr, RC_ERR_UNSUPPORTED,
+		               "walls with a viscous solve are not provided (the reference's wall rows make the assembled "
+		               "matrix unsymmetric; its upper-triangle CG then depends on the order of the unknowns)");
+	if(has_walls && params->precision == RC_PRECISION_FLOAT)
+		return set_err(nullptr, RC_ERR_UNSUPPORTED, "walls are provided by the FP64 cell kernels only");
 	std::vector<LayerDev> layers((size_t) n_layers);
 	int n_cells = 0, total_bins = 0;
 	long long total_box = 0;
@@ -854,6 +864,7 @@ static int create_engine(const rc_params *params, int n_layers, const rc_box *bo
 		P.a0 = (double) a0;
 	}
 	P.cg_tol = params->cg_tolerance;
+	P.wall_slip = params->wall_slip;
 	for(int k = 0; k < 2; k++) {
 		e->ph[k].friction = params->friction[k];
 		e->ph[k].friction_cell = params->friction_cell[k];
@@ -886,6 +897,17 @@ static int create_engine(const rc_params *params, int n_layers, const rc_box *bo
 	   (rc = dalloc(e, &e->scratch_phi, cap + (size_t) n_cells / 2 + 8)) ||
 	   (rc = dalloc(e, &e->rep, e->rep_on ? cap : 1)) || (rc = dalloc(e, &e->scratch_rep, e->rep_on ? cap : 1)))
 		return bail(rc);
+	if(has_walls) {
+		// the boxes' wall values (layers without walls stay zero)
+		if((rc = dalloc(e, &e->walls, (size_t) total_box))) return bail(rc);
+		for(int l = 0; l < n_layers; l++) {
+			if(!boxes[l].walls) continue;
+			const LayerDev &ly = layers[(size_t) l];
+			const cudaError_t c = cudaMemcpy(e->walls + ly.box_off, boxes[l].walls, sizeof(double) * (size_t) ly.L * ly.L,
+			                                 cudaMemcpyHostToDevice);
+			if(c != cudaSuccess) return bail(set_err(e, RC_ERR_CUDA, "walls upload failed: %s", cudaGetErrorString(c)));
+		}
+	}
 	if(wet) {
 		if((rc = dalloc(e, &e->fx, cap)) || (rc = dalloc(e, &e->fy, cap)) || (rc = dalloc(e, &e->cover, L2 * STORE_MAX)) ||
 		   (rc = dalloc(e, &e->cov_off, L2 + 1)) || (rc = dalloc(e, &e->cov_idx, cap)) ||

@@ -37,6 +37,7 @@ struct CellArgs {
 	int *mapg;
 	double *rep;
 	const double *phi2, *sq00, *sq01;
+	const double *walls;     // wall values per box site (getWalls), null for periodic boxes
 	const double *tab_cos, *tab_sin;
 	const float *tab_cosf, *tab_sinf;  // the same tables rounded to FP32 (FP32 kernels)
 	CellSum *csum;                     // split mode: sums for the epilogue kernel

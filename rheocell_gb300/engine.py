@@ -49,10 +49,11 @@ SITE_FIELDS = ("phi", "vx", "vy", "mu", "dx", "dy", "box_index")
 class Engine:
     """One monolayer on one GPU (rc_create / rc_step / rc_download ...)."""
 
-    def __init__(self, params: abi.RcParams, L: int, cells: HostCells, device: int = 0):
+    def __init__(self, params: abi.RcParams, L: int, cells: HostCells, device: int = 0, walls=None):
         self._lib = lib()
         self.h = C.c_void_p()
-        box = abi.RcBox(L, L)
+        walls = None if walls is None else np.ascontiguousarray(walls, dtype=np.float64)
+        box = abi.make_box(L, walls)
         rc = self._lib.rc_create(C.byref(params), C.byref(box), cells.n, cells.arr, device, C.byref(self.h))
         if rc != 0:
             msg = self._lib.rc_last_error(self.h).decode()

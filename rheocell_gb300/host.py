@@ -94,9 +94,7 @@ def make_params(keys: Dict[str, object], precision: int = abi.RC_PRECISION_DOUBL
     if name not in abi.MODEL_NAMES:
         raise ValueError("interaction_type '%s' is not provided by the GB300 engine" % name)
     if str(keys.get("box", "square")).strip() != "square":
-        raise ValueError("only the periodic square box is provided")
-    if "wall_slip" in keys and float(keys["wall_slip"]) <= 0:
-        raise ValueError("wall_slip <= 0 selects wall stencils, which are not provided")
+        raise ValueError("only the square boxes are provided (box = square, with or without walls)")
     if int(float(keys.get("external_forces", 0))) != 0:
         raise ValueError("external forces are not provided")
     if int(float(keys.get("anchoring", 0))) != 0:
@@ -121,6 +119,7 @@ def make_params(keys: Dict[str, object], precision: int = abi.RC_PRECISION_DOUBL
     p.cg_tolerance = _num(keys, "CGtolerance", 0.0001) if name in ("wetmodel", "wetpolarmodel") else 0.0
     p.cg_restart_every = 10 if name == "wetpolarmodel" else 100
     p.anchoring = 0
+    p.wall_slip = _num(keys, "wall_slip", 0.5)  # BaseInteraction.cpp:10,23
     if name == "simplefield":
         p.friction = abi.D2(1.0, 1.0)
         p.friction_cell = abi.D2(0, 0)
@@ -232,6 +231,54 @@ def read_input(path: str, overrides: Optional[Dict[str, object]] = None) -> Dict
     for k, v in (overrides or {}).items():
         keys[k] = str(v)
     return keys
+
+
+WALL_TYPES = ("square_walls", "circle_walls", "triangle_walls")
+
+
+def box_walls(keys: Dict[str, object], L: int) -> Optional[np.ndarray]:
+    """getWalls(k) of the box the reference's BoxFactory makes from `keys`
+    (src/Boxes/BoxFactory.cpp:13-27), as L*L doubles, or None for the periodic
+    SquareBox.  The masks restate SquareWalls::init (SquareWalls.cpp:23-55),
+    CircleWalls::init (CircleWalls.cpp:23-45) and TriangleWalls::init
+    (TriangleWalls.cpp:24-60) with their integer and double arithmetic.  A
+    SquareBox with wall_slip <= 0 has every site closed (getWalls = 0 is not
+    below it), which an all-zero mask reproduces."""
+    import math
+    kind = str(keys.get("type", "none")).strip()
+    if kind not in WALL_TYPES:
+        if "wall_slip" in keys and float(keys["wall_slip"]) <= 0:
+            return np.zeros(L * L)
+        return None
+    if "lambda_wall" not in keys:
+        raise ValueError("box type %s needs lambda_wall" % kind)
+    lw = float(keys["lambda_wall"])
+    w = np.zeros((L, L))  # [y][x]
+    if kind == "square_walls":
+        for y in range(L):
+            for x in range(L):
+                if x < lw - 1 or x > L - lw or y < lw or y > L - lw:
+                    w[y, x] = 1.0
+    elif kind == "circle_walls":
+        h = L // 2
+        for y in range(L):
+            for x in range(L):
+                dist = h - math.sqrt(float((h - x) * (h - x) + (h - y) * (h - y)))
+                w[y, x] = 1.0 if (dist <= 0 or dist < lw) else 0.0
+    else:
+        w[:, :] = 1.0
+        side = int(L - lw * 2)
+        height = int(round(side * math.sqrt(3.0) / 2.0))
+        center = L // 2
+        top = L // 2 - height // 2
+        for row in range(height):
+            half = int((side / 2.0) * (1.0 - float(row) / height))
+            y = top + row
+            if 0 <= y < L:
+                for x in range(center - half, min(center + half, L - 1) + 1):
+                    if x >= 0:
+                        w[y, x] = 0.0
+    return w.reshape(-1)
 
 
 def engine_inputs(keys: Dict[str, object], m: Monolayer,

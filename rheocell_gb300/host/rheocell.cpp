@@ -141,7 +141,11 @@ public:
 			throw RCexception("cell_tile must be 128, 256 or 512");
 		if(inp.str("box", "square") != "square") throw RCexception("only the periodic square box is provided");
 		if(inp.integer("external_forces", 0) != 0) throw RCexception("external forces are not provided");
-		if(inp.has("wall_slip") && inp.num("wall_slip") <= 0) throw RCexception("wall stencils are not provided");
+		// wall boxes run through the library (rc_box.walls) from the reference's
+		// own rheoCell with backend = CUDA; this driver runs the periodic box
+		if(inp.str("type", "none").find("walls") != std::string::npos || (inp.has("wall_slip") && inp.num("wall_slip") <= 0))
+			throw RCexception("wall boxes are run by the reference's rheoCell with backend = CUDA, not by this driver");
+		params_.wall_slip = inp.has("wall_slip") ? inp.num("wall_slip") : 0.5;
 		if(inp.boolean("anchoring")) throw RCexception("anchoring is not provided");
 
 		interaction_ = inp.str("interaction_type", "", true);

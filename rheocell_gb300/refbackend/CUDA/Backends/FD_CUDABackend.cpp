@@ -75,7 +75,9 @@ void FD_CUDABackend::get_settings(input_file &inp) {
 	if(lees_edwards) throw RCexception("GB300 engine: Lees-Edwards boundaries are not provided");
 	std::string box_type("square");
 	getInputString(&inp, "box", box_type, 0);
-	if(box_type != "square") throw RCexception("GB300 engine: box '%s' is not provided (periodic square box only)", box_type.c_str());
+	if(box_type != "square")
+		throw RCexception("GB300 engine: box '%s' is not provided (square boxes, with or without walls, only)", box_type.c_str());
+	params_.wall_slip = number_or(inp, "wall_slip", 0.5);  // BaseInteraction.cpp:10,23
 	bool ext = false;
 	getInputBool(&inp, "external_forces", &ext, 0);
 	if(ext) throw RCexception("GB300 engine: external forces are not provided");
@@ -169,7 +171,16 @@ void FD_CUDABackend::init() {
 	params_.rng_has_cached = 0;
 	params_.rng_cached = 0.0;
 
-	rc_box b = {box->getXsize(), box->getYsize()};
+	rc_box b = {box->getXsize(), box->getYsize(), nullptr};
+	// the box's wall values (SquareWalls, CircleWalls, TriangleWalls; zero for
+	// the periodic SquareBox, whose sites are all open unless wall_slip <= 0)
+	std::vector<double> walls((size_t) b.Lx * (size_t) b.Ly);
+	bool any_wall = params_.wall_slip <= 0.0;
+	for(size_t k = 0; k < walls.size(); k++) {
+		walls[k] = (double) box->getWalls((int) k);
+		any_wall |= walls[k] != 0.0;
+	}
+	if(any_wall) b.walls = walls.data();
 	// the first force evaluation of FD_CPUBackend::init (FD_CPUBackend.cpp:19-42)
 	// runs inside rc_create
 	const int rc = rc_create(&params_, &b, (int) cells.size(), cells.data(), device_, &engine_);

@@ -41,7 +41,8 @@ def run(sim_factory, keys, m, steps: List[int], eq: int = 0, precision=abi.RC_PR
     """Run equilibration (phase 0), switch to phase 1, and return the states at
     the requested main-loop steps (0 = before the first main step)."""
     p, cells = build_inputs(keys, m, precision)
-    sim = sim_factory(p, m.L, cells)
+    walls = host.box_walls(keys, m.L)
+    sim = sim_factory(p, m.L, cells) if walls is None else sim_factory(p, m.L, cells, walls=walls)
     for _ in range(eq):
         sim.step(1)
     sim.set_phase(1)

@@ -67,6 +67,18 @@ CASES = {
     # a cold start every 100 warm solves (wetmodel) or every 10 (wetpolarmodel)
     "wet_restart": (dict(L=36, n=4, seed=26, **SMALL), WET_S, [0, 1, 52], 36, 0),
     "wetpolar_restart": (dict(L=36, n=4, seed=27, **SMALL), WETPOLAR_S, [0, 1, 7], 37, 0),
+    # wall boxes (box = square with type = square_walls / circle_walls /
+    # triangle_walls): the wall branches of the stencils, adhesion and forces
+    "walls_polar": (dict(L=48, n=9, seed=41, **SMALL),
+                    dict(DRY_POLAR_S, type="square_walls", lambda_wall=4, beta=0.5, J_Q=0.5, zetaQ_inter=0.3,
+                         omega=0.004), [0, 1, 5], 51, 0),
+    "walls_simple": (dict(L=36, n=4, seed=42, **SMALL), dict(SIMPLE_S, type="circle_walls", lambda_wall=3),
+                     [0, 1, 5], 52, 0),
+    "walls_wetdry": (dict(L=48, n=9, seed=43, **SMALL), dict(WET_S, friction_cell=0, type="triangle_walls", lambda_wall=3),
+                     [0, 1, 5], 53, 0),
+    "walls_ch_polar": (dict(L=36, n=4, seed=44, **SMALL),
+                       dict(DRY_POLAR_S, sim_type="FD_CH", dt=0.01, type="square_walls", lambda_wall=3, wall_slip=0.7),
+                       [0, 1, 5], 54, 0),
 }
 
 

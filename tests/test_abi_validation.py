@@ -60,6 +60,23 @@ def test_create_rejects_bad_parameters(lib):
     assert rc == abi.RC_ERR_UNSUPPORTED and "wetpolarmodel and wetmodel only" in msg
 
 
+def test_create_rejects_walls_it_does_not_provide(lib):
+    # walls with a viscous solve, and walls on FP32 engines: rejected before any CUDA call
+    import numpy as np
+    p, L, cells = _inputs()  # the wet nematic model with friction_cell = 1
+    walls = np.zeros(L * L)
+    walls[:L] = 1.0
+    h = C.c_void_p()
+    rc = lib.rc_create(C.byref(p), C.byref(abi.make_box(L, walls)), cells.n, cells.arr, 0, C.byref(h))
+    assert rc == abi.RC_ERR_UNSUPPORTED and not h
+    assert "walls with a viscous solve" in lib.rc_last_error(None).decode()
+    dry = abi.RcParams.from_buffer_copy(p)
+    dry.friction_cell = abi.D2(0.0, 0.0)
+    dry.precision = abi.RC_PRECISION_FLOAT
+    rc = lib.rc_create(C.byref(dry), C.byref(abi.make_box(L, walls)), cells.n, cells.arr, 0, C.byref(h))
+    assert rc == abi.RC_ERR_UNSUPPORTED and "FP64 cell kernels only" in lib.rc_last_error(None).decode()
+
+
 def test_create_rejects_bad_box_and_cells(lib):
     p, L, cells = _inputs()
     rc, msg = _create(lib, p, L, cells, Ly=L + 1)

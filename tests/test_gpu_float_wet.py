@@ -10,7 +10,13 @@ after the first step (the forces are the right-hand side of the solve, so
 the velocities carry the FP32 force error) and after 20 steps.  The error
 bounds are stated per field below; they are the FP32 rounding of O(1)
 quantities (phi, box sums of phi^2 and phi Q) through a few dozen
-operations, grown over the steps by the dynamics."""
+operations, grown over the steps by the dynamics.  The first-step check
+runs with the director dynamics off (J_Q = 0): the tanh discs of the start
+are nearly round, so the direction of their shape tensor -- which turns
+each wetmodel cell's director when J_Q != 0 -- is set by rounding and
+differs between any two orders of summation (the reference's exact and
+-ffast-math builds included); with J_Q = 0.1 that alone moves phi by
+~2.5e-5 in the first step, and the 20-step bound covers it."""
 from __future__ import annotations
 
 import numpy as np
@@ -29,9 +35,9 @@ FIRST_STEP_TOL = {"phi": 1e-5, "vx": 2e-5, "vy": 2e-5, "mu": 1e-5, "dx": 1e-5, "
 AFTER_20_TOL = {"phi": 1e-4, "vx": 1e-3, "vy": 1e-3, "area": 1e-5, "com_x": 1e-5, "com_y": 1e-5}
 
 
-def _pair(model, L=64, n=16, seed=4):
+def _pair(model, L=64, n=16, seed=4, **extra):
     m = g.make_monolayer(L, n, seed=seed)
-    keys, m2 = case_from_monolayer(m, MODELS[model], seed=seed)
+    keys, m2 = case_from_monolayer(m, dict(MODELS[model], **extra), seed=seed)
     out = []
     for prec in (abi.RC_PRECISION_DOUBLE, abi.RC_PRECISION_FLOAT):
         p, cells = build_inputs(keys, m2, precision=prec)
@@ -43,7 +49,7 @@ def _pair(model, L=64, n=16, seed=4):
 
 @pytest.mark.parametrize("model", sorted(MODELS))
 def test_first_step_close_to_fp64(model):
-    a, b = _pair(model)
+    a, b = _pair(model, J_Q=0)
     a.step(1)
     b.step(1)
     sa, sb = a.state(), b.state()

@@ -28,7 +28,8 @@ from tests.common import (build_inputs, case_from_monolayer, case_from_texts, co
 pytestmark = pytest.mark.gpu
 
 ALL = ["polar_dry", "polar_noise", "nematic", "simple", "polar41", "resize", "wet", "wetpolar", "wet_equil", "ch_polar",
-       "ch_nematic", "ch_wet", "polar_beta", "wetpolar_beta"]
+       "ch_nematic", "ch_wet", "polar_beta", "wetpolar_beta", "walls_polar", "walls_simple", "walls_wetdry",
+       "walls_ch_polar"]
 EQ = {"wet_equil": 3}
 TOL = 1e-10
 
@@ -190,3 +191,25 @@ def test_first_evaluation_bitwise(model):
     b = orc.OracleSim(p, m2.L, cells).state()
     for k in ("mu", "vx", "vy", "box_index", "area", "sum_f"):
         assert np.array_equal(a[k], b[k]), (k, rel_err(a[k], b[k]))
+
+
+WALL_BOXES = [dict(type="square_walls", lambda_wall=6), dict(type="circle_walls", lambda_wall=4),
+              dict(type="triangle_walls", lambda_wall=5)]
+
+
+@pytest.mark.parametrize("box", range(len(WALL_BOXES)))
+@pytest.mark.parametrize("model", ["wetpolarmodel", "simplefield", "wetmodel"])
+def test_walls_vs_oracle(model, box):
+    """Wall boxes on 41x41 patches over 20 steps (the oracle itself is bit
+    for bit the reference's exact build on the wall goldens)."""
+    m = g.make_monolayer(96, 16, seed=5)
+    params = dict(g.DRY_POLAR, interaction_type=model, zetaQ_inter=0.05, J_Q=0.2, omega=0.004, beta=0.2,
+                  friction_cell=0, **WALL_BOXES[box])
+    keys, m2 = case_from_monolayer(m, params, seed=5)
+    _, a = run(engine.Engine, keys, m2, [1, 20])
+    _, b = run(orc.OracleSim, keys, m2, [1, 20])
+    for s_ in (1, 20):
+        assert np.array_equal(a[s_]["box_index"], b[s_]["box_index"])
+        for k in ("phi", "vx", "vy", "area", "com_x", "com_y", "dx", "dy", "mu"):
+            err = rel_err(a[s_][k], b[s_][k])
+            assert err <= TOL, (s_, k, err)

@@ -49,9 +49,26 @@ def test_params_reject_unprovided():
     with pytest.raises(ValueError):
         host.make_params(dict(base, box="channel"))
     with pytest.raises(ValueError):
-        host.make_params(dict(base, wall_slip=0))
+        host.make_params(dict(base, box="orthogonal", type="channel_walls"))
+    with pytest.raises(ValueError):
+        host.box_walls(dict(base, type="square_walls"), 64)  # lambda_wall is required
     with pytest.raises(ValueError):
         host.make_params({k: v for k, v in base.items() if k != "friction_cell"})
+
+
+def test_wall_masks():
+    # SquareWalls: x < lambda-1 or x > L-lambda, y < lambda or y > L-lambda
+    w = host.box_walls(dict(type="square_walls", lambda_wall=3), 16).reshape(16, 16)
+    assert w[:, 0].all() and w[:, 1].all() and not w[5, 2] and w[5, 14] and not w[5, 13]
+    assert w[0].all() and w[2].all() and not w[3, 5] and w[14, 5] and not w[13, 5]
+    # CircleWalls: centre open, corners closed; TriangleWalls: a closed border
+    c = host.box_walls(dict(type="circle_walls", lambda_wall=2), 32).reshape(32, 32)
+    assert c[0, 0] == 1 and c[16, 16] == 0 and c[16, 1] == 1
+    t = host.box_walls(dict(type="triangle_walls", lambda_wall=4), 64).reshape(64, 64)
+    assert t[0].all() and t[:, 0].all() and not t[32, 32]
+    # no walls: None; wall_slip <= 0 on the periodic box closes every site
+    assert host.box_walls({}, 8) is None
+    assert not host.box_walls(dict(wall_slip=0), 8).any()
 
 
 def test_nemq_seeding_order():

@@ -15,7 +15,8 @@ import pytest
 from oracle import oracle as orc
 from tests.common import GOLDEN, build_inputs, case_from_texts, compare_to_golden, golden, run
 
-DRY = ["polar_dry", "polar_noise", "nematic", "simple", "polar41", "resize", "ch_polar", "ch_nematic", "polar_beta", "ch_simple"]
+DRY = ["polar_dry", "polar_noise", "nematic", "simple", "polar41", "resize", "ch_polar", "ch_nematic", "polar_beta", "ch_simple",
+       "walls_polar", "walls_simple", "walls_wetdry", "walls_ch_polar"]
 WET = ["wet", "wetpolar", "wet_equil", "ch_wet", "wetpolar_beta", "wet_restart", "wetpolar_restart",
        "ch_wetpolar"]
 EQ = {"wet_equil": 3}
@@ -115,3 +116,17 @@ def test_oracle_matches_reference_wet_full_size(name):
     errs = sampled_errors(gd, states)
     bad = {k: v for k, v in errs.items() if v > 1e-12}
     assert not bad, bad
+
+
+@pytest.mark.parametrize("name", ["walls_polar", "walls_simple", "walls_wetdry"])
+def test_wall_cases_differ_from_the_periodic_box(name):
+    """The wall goldens exercise the wall branches: the same start without
+    the walls gives a different phi after the first step."""
+    from rheocell_gb300 import host
+    from tests.common import rel_err
+    gd = golden(name)
+    keys, m = case_from_texts(str(gd["input"]), str(gd["conf"]), str(gd["topology"]))
+    assert host.box_walls(keys, m.L) is not None
+    plain = {k: v for k, v in keys.items() if k not in ("type", "lambda_wall")}
+    _, a = run(orc.OracleSim, plain, m, [1])
+    assert rel_err(a[1]["phi"], gd["s1_phi"]) > 1e-6
