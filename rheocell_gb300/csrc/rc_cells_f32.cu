@@ -213,7 +213,74 @@ __global__ void __launch_bounds__(BLOCK) cell_kernel_f32(const CellArgs a) {
 	const float rfr = kc[K_RFR];
 	const int tb = table_base(lx), tby = table_base(ly);
 	const float q00 = kc[K_Q00], q01 = kc[K_Q01];
+	// The update of a site (first_step) from its dphi inputs; shared by the
+	// batched update-only loop and the evaluate-and-update loop below.
+	auto update_site = [&](int q, int x, int y, float dphi, float phi_pre, float dphi_prev) {
+		float phi_new;
+		if(UPD == UP_PRED) {
+			a.dphi_old[start + q] = f2d_int(dphi);
+			phi_new = phi_pre + hdt * (dphi + dphi);
+		}
+		else {
+			phi_new = phi_pre + hdt * (dphi + dphi_prev);
+		}
+		a.phi_out[start + q] = f2d_int(phi_new);
+		acc_square(phi_new, area_s, area_c);
+		af[1] += phi_new;
+		int lxx = x + c.offx;
+		if(lxx >= lx) lxx -= lx;
+		int lyy = y + c.offy;
+		if(lyy >= ly) lyy -= ly;
+		af[2] += phi_new * a.tab_cosf[tb + lxx];
+		af[3] += phi_new * a.tab_sinf[tb + lxx];
+		af[4] += phi_new * a.tab_cosf[tby + lyy];
+		af[5] += phi_new * a.tab_sinf[tby + lyy];
+		if(UPD == UP_CORR && phi_new < 0.09f && phi_new > 0.01f) {
+			imin[0] = min(imin[0], lxx);
+			imin[1] = min(imin[1], lyy);
+		}
+	};
+	if(EVAL == EV_NONE && UPD != UP_NONE && !conserved) {
+		// Update only (the wet models' predictor and corrector): every input
+		// is a stream from global memory, so the loads of UB sites are issued
+		// together ahead of their arithmetic (streaming loads: each value is
+		// read once; phi_old may be the array being written, site by site).
+		constexpr int UB = 2;
+		PatchWalk w(lx);
+		while(w.q < n) {
+			int qq[UB], xx[UB], yy[UB];
+#pragma unroll
+			for(int u = 0; u < UB; u++) {
+				qq[u] = w.q;
+				xx[u] = w.x;
+				yy[u] = w.y;
+				w.next();
+			}
+			double gm[UB], gvx[UB], gvy[UB], gdx[UB], gdy[UB], gp[UB], gd[UB];
+#pragma unroll
+			for(int u = 0; u < UB; u++) {
+				const long long i = start + (qq[u] < n ? qq[u] : 0);
+				gm[u] = __ldcs(&a.mu[i]);
+				gvx[u] = __ldcs(&a.vxg[i]);
+				gvy[u] = __ldcs(&a.vyg[i]);
+				gdx[u] = __ldcs(&a.dxg[i]);
+				gdy[u] = __ldcs(&a.dyg[i]);
+				gp[u] = __ldcs(UPD == UP_PRED ? &a.phi_eval[i] : &a.phi_old[i]);
+				gd[u] = UPD == UP_CORR ? __ldcs(&a.dphi_old[i]) : 0.0;
+			}
+#pragma unroll
+			for(int u = 0; u < UB; u++) {
+				if(qq[u] >= n) break;
+				const float dx = d2f_int(gdx[u]), dy = d2f_int(gdy[u]);
+				const float dphi = -J0 * d2f_int(gm[u]) - d2f_int(gvx[u]) * dx - d2f_int(gvy[u]) * dy;
+				update_site(qq[u], xx[u], yy[u], dphi, d2f_int(gp[u]), d2f_int(gd[u]));
+				af[6] += -.5f * (dx * dx - dy * dy);
+				af[7] += -dx * dy;
+			}
+		}
+	}
 	// Stage 2: forces (calc_internal_forces) and the update (first_step).
+	if(EVAL != EV_NONE || UPD == UP_NONE || conserved)
 	for(PatchWalk w(lx); w.q < n; w.next()) {
 		const int q = w.q, x = w.x, y = w.y;
 		float mu = 0.f, vx = 0.f, vy = 0.f, dx, dy, phi_e = 0.f;
@@ -297,30 +364,8 @@ __global__ void __launch_bounds__(BLOCK) cell_kernel_f32(const CellArgs a) {
 		}
 		else
 			dphi = -J0 * mu - vx * dx - vy * dy;
-		float phi_new;
-		if(UPD == UP_PRED) {
-			const float phi_old = (EVAL != EV_NONE) ? phi_e : d2f_int(a.phi_eval[start + q]);
-			a.dphi_old[start + q] = f2d_int(dphi);
-			phi_new = phi_old + hdt * (dphi + dphi);
-		}
-		else {
-			phi_new = d2f_int(a.phi_old[start + q]) + hdt * (dphi + d2f_int(a.dphi_old[start + q]));
-		}
-		a.phi_out[start + q] = f2d_int(phi_new);
-		acc_square(phi_new, area_s, area_c);
-		af[1] += phi_new;
-		int lxx = x + c.offx;
-		if(lxx >= lx) lxx -= lx;
-		int lyy = y + c.offy;
-		if(lyy >= ly) lyy -= ly;
-		af[2] += phi_new * a.tab_cosf[tb + lxx];
-		af[3] += phi_new * a.tab_sinf[tb + lxx];
-		af[4] += phi_new * a.tab_cosf[tby + lyy];
-		af[5] += phi_new * a.tab_sinf[tby + lyy];
-		if(UPD == UP_CORR && phi_new < 0.09f && phi_new > 0.01f) {
-			imin[0] = min(imin[0], lxx);
-			imin[1] = min(imin[1], lyy);
-		}
+		if(UPD == UP_PRED) update_site(q, x, y, dphi, (EVAL != EV_NONE) ? phi_e : d2f_int(a.phi_eval[start + q]), 0.f);
+		else update_site(q, x, y, dphi, d2f_int(a.phi_old[start + q]), d2f_int(a.dphi_old[start + q]));
 		af[6] += -.5f * (dx * dx - dy * dy);
 		af[7] += -dx * dy;
 	}

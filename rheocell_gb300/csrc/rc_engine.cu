@@ -651,11 +651,20 @@ static void host_cell(const rc_cell_host &h, CellDev &c, int start, int layer = 
 // bit-identical: area = sum phi^2 and sumF = sum phi of the loaded field
 // (SimBackend.cpp:289-296) and the shape tensor of begin_energy_computation()
 // (e.g. WetModel.cpp:126-164; only visible in a download before the first step).
-__global__ void init_sums_kernel(CellDev *cells, const double *phi, int N) {
+// walls (null: periodic boxes): the wet, polar and simple models' initial
+// gradients take derivX/derivY's wall branches (SimpleMultiField.cpp:97-98,
+// WetModel.cpp:154-155, WetPolarModel.cpp:119-120; ActiveNematic.cpp:127-128
+// keeps the plain differences)
+__global__ void init_sums_kernel(CellDev *cells, const LayerDev *layers, const double *phi, int N, const double *walls,
+                                 double slip) {
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if(i >= N) return;
 	CellDev &c = cells[i];
 	const int lx = c.lx, ly = c.ly, n = c.n, st = c.start;
+	const LayerDev &lay = layers[c.layer];
+	const int L = lay.L;
+	const double *wl = walls ? walls + lay.box_off : nullptr;
+	auto open = [&](int k) { return wl[k] < slip; };
 	double area = 0, sumf = 0, s00 = 0, s01 = 0;
 	for(int q = 0; q < n; q++) {
 		const double p = phi[st + q];
@@ -664,7 +673,14 @@ __global__ void init_sums_kernel(CellDev *cells, const double *phi, int N) {
 		const int y = q / lx, x = q - y * lx;
 		const int r = (x == lx - 1) ? q - (lx - 1) : q + 1, l = (x == 0) ? q + (lx - 1) : q - 1;
 		const int u = (y == ly - 1) ? q - (ly - 1) * lx : q + lx, d = (y == 0) ? q + (ly - 1) * lx : q - lx;
-		const double dx = .5 * (phi[st + r] - phi[st + l]), dy = .5 * (phi[st + u] - phi[st + d]);
+		double dx = .5 * (phi[st + r] - phi[st + l]), dy = .5 * (phi[st + u] - phi[st + d]);
+		if(wl) {
+			const int k = box_site(c, x, y, L), kx = k % L, ky = k / L;
+			const int kr = ky * L + (kx == L - 1 ? 0 : kx + 1), kl = ky * L + (kx == 0 ? L - 1 : kx - 1);
+			const int ku = (ky == L - 1 ? 0 : ky + 1) * L + kx, kd = (ky == 0 ? L - 1 : ky - 1) * L + kx;
+			if(!(open(kr) && open(kl))) dx = 0.;
+			if(!(open(ku) && open(kd))) dy = 0.;
+		}
 		s00 += -0.5 * (dx * dx - dy * dy);
 		s01 += -dx * dy;
 	}
@@ -984,7 +1000,8 @@ static int create_engine(const rc_params *params, int n_layers, const rc_box *bo
 	}
 	if((rc = choose_smem(e))) return bail(rc);
 	if(n_cells > 0) {
-		init_sums_kernel<<<(n_cells + 63) / 64, 64, 0, e->stream>>>(e->cells, e->phiA, n_cells);
+		init_sums_kernel<<<(n_cells + 63) / 64, 64, 0, e->stream>>>(
+		    e->cells, e->layers, e->phiA, n_cells, P.model == M_NEMATIC ? nullptr : e->walls, P.wall_slip);
 		launch_bins(e->cells, e->layers, n_cells, e->bin_count, e->bin_cells, total_bins, e->st, e->stream);
 		// FD_CPUBackend::init: first force evaluation with the phase-0 parameters
 		evaluate_end(e, e->phiA, 0);

@@ -11,12 +11,15 @@ the velocities carry the FP32 force error) and after 20 steps.  The error
 bounds are stated per field below; they are the FP32 rounding of O(1)
 quantities (phi, box sums of phi^2 and phi Q) through a few dozen
 operations, grown over the steps by the dynamics.  The first-step check
-runs with the director dynamics off (J_Q = 0): the tanh discs of the start
-are nearly round, so the direction of their shape tensor -- which turns
-each wetmodel cell's director when J_Q != 0 -- is set by rounding and
-differs between any two orders of summation (the reference's exact and
--ffast-math builds included); with J_Q = 0.1 that alone moves phi by
-~2.5e-5 in the first step, and the 20-step bound covers it."""
+runs the wetmodel without self-propulsion (zetaQ_self = 0): the tanh discs
+of the start are nearly round, and the reference updates a cell's Q only
+when |S| > 1e-8 (WetModel.cpp:697-747); for such cells |S| is ~1e-8, below
+what FP32 gradients resolve (~1e-7, the same order as the reference's own
+-ffast-math build differs from its exact build), so FP32 and FP64 can take
+different branches for a cell in the first predictor, and the self-active
+force of the next evaluation differs by O(dt zetaQ_self).  That shifts phi
+once by ~2.5e-5 (~2e-4 on a dry monolayer, where v = f / xi); the 20-step
+bound covers it."""
 from __future__ import annotations
 
 import numpy as np
@@ -49,7 +52,7 @@ def _pair(model, L=64, n=16, seed=4, **extra):
 
 @pytest.mark.parametrize("model", sorted(MODELS))
 def test_first_step_close_to_fp64(model):
-    a, b = _pair(model, J_Q=0)
+    a, b = _pair(model, J_Q=0, zetaQ_self=0) if model == "wetmodel" else _pair(model)
     a.step(1)
     b.step(1)
     sa, sb = a.state(), b.state()
