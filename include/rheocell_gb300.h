@@ -477,6 +477,15 @@ int rc_viscous_resolve(rc_engine *e, int solver, double *vx, double *vy, long lo
 int rc_set_cg_limits(rc_engine *e, long long max_iterations, int fail_on_no_convergence);
 
 /*
+ * rc_set_cg_tolerance: the relative residual at which every following
+ * viscous solve stops (the CGtolerance key, WetModel.cpp:59-60; 0: Eigen's
+ * default, machine epsilon).  Lets a host solve one right-hand side to a
+ * much tighter tolerance (with rc_viscous_resolve) as the reference
+ * solution other solves are measured against.
+ */
+int rc_set_cg_tolerance(rc_engine *e, double tolerance);
+
+/*
  * Test hook of the solve's failure detection (no counterpart in the
  * reference).  spin_limit: polls of a grid-barrier wait before it gives up
  * (0: the default, about 1-2 s).  unreachable != 0 makes the first grid

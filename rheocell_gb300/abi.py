@@ -218,6 +218,8 @@ def declare(lib: C.CDLL, prefix: str) -> C.CDLL:
         lib.rc_viscous_resolve.restype = C.c_int
         lib.rc_set_cg_limits.argtypes = [vp, C.c_longlong, C.c_int]
         lib.rc_set_cg_limits.restype = C.c_int
+        lib.rc_set_cg_tolerance.argtypes = [vp, C.c_double]
+        lib.rc_set_cg_tolerance.restype = C.c_int
         lib.rc_test_barrier_timeout.argtypes = [vp, C.c_longlong, C.c_int]
         lib.rc_test_barrier_timeout.restype = C.c_int
         lib.rc_autotune.argtypes = [vp, C.c_int, C.POINTER(RcAutotuneReport)]
@@ -238,7 +240,7 @@ def declare(lib: C.CDLL, prefix: str) -> C.CDLL:
 EXPORTED = ["rc_abi_version", "rc_create", "rc_create_generated", "rc_batch_create", "rc_layer_count", "rc_viscous_resolve_noalloc", "rc_unet_loss_grad", "rc_unet_forward_tc",
             "rc_learned_harvest", "rc_learned_harvested", "rc_learned_train", "rc_learned_get_params",
             "rc_learned_set_params", "rc_set_solver", "rc_solver_profile", "rc_viscous_resolve",
-            "rc_set_cg_limits", "rc_test_barrier_timeout",
+            "rc_set_cg_limits", "rc_set_cg_tolerance", "rc_test_barrier_timeout",
             "rc_observe_field", "rc_observe_stress", "rc_observe_cells", "rc_autotune", "rc_set_cell_threads", "rc_step", "rc_step_async", "rc_wait", "rc_set_phase",
             "rc_get_sizes", "rc_download", "rc_upload", "rc_download_phi", "rc_upload_phi", "rc_set_stream",
             "rc_set_timing", "rc_timers", "rc_site_count", "rc_last_error", "rc_destroy"]

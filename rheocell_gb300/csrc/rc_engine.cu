@@ -1585,6 +1585,17 @@ int rc_set_cg_limits(rc_engine *e, long long max_iterations, int fail_on_no_conv
 	return RC_OK;
 }
 
+int rc_set_cg_tolerance(rc_engine *e, double tolerance) {
+	if(!e) return RC_ERR_INVALID;
+	if(!(tolerance >= 0.0) || !std::isfinite(tolerance))
+		return set_err(e, RC_ERR_INVALID, "rc_set_cg_tolerance: tolerance %g is not a finite value >= 0", tolerance);
+	CUDA_TRY(e, cudaSetDevice(e->device));
+	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+	drop_graphs(e);
+	e->hp.cg_tolerance = tolerance;
+	return RC_OK;
+}
+
 int rc_test_barrier_timeout(rc_engine *e, long long spin_limit, int unreachable) {
 	if(!e) return RC_ERR_INVALID;
 	if(spin_limit < 0) return set_err(e, RC_ERR_INVALID, "rc_test_barrier_timeout: spin_limit %lld < 0", spin_limit);

@@ -220,6 +220,9 @@ class Engine:
         self._check(self._lib.rc_set_cg_limits(self.h, max_iterations, int(fail_on_no_convergence)),
                     "rc_set_cg_limits")
 
+    def set_cg_tolerance(self, tolerance: float) -> None:
+        self._check(self._lib.rc_set_cg_tolerance(self.h, tolerance), "rc_set_cg_tolerance")
+
     def get_params(self) -> np.ndarray:
         p = np.zeros(abi.RC_UNET_PARAMS)
         self._check(self._lib.rc_learned_get_params(self.h, p.ctypes.data_as(abi.DP)), "rc_learned_get_params")
