@@ -484,11 +484,13 @@ def run_gb300(args, rank, world):
     iu = names.index("update")
     if tn[iu] and args.workload.startswith("wet"):
         upd_s = tms[iu] / tn[iu] / 1e3
+        # FP32 engines keep mu and the gradients in FP32 (12 B of the reads instead of 24)
+        moved = 52.0 if args.precision == "float" else 64.0
         out["phi_update"] = {
             "launch_ms": upd_s * 1e3, "launches": int(tn[iu]),
             "achieved_gbs": 44.0 * S / upd_s / 1e9, "frac": 44.0 * S / upd_s / 1e9 / peak,
-            "algorithmic_bytes_per_site": 44.0, "moved_bytes_per_site": 64.0,
-            "moved_gbs": 64.0 * S / upd_s / 1e9, "moved_frac": 64.0 * S / upd_s / 1e9 / peak,
+            "algorithmic_bytes_per_site": 44.0, "moved_bytes_per_site": moved,
+            "moved_gbs": moved * S / upd_s / 1e9, "moved_frac": moved * S / upd_s / 1e9 / peak,
             "peak": peak, "unit": "GB/s"}
     if learned is not None:
         out["learned_pcg"] = learned

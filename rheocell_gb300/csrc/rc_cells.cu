@@ -793,6 +793,22 @@ cudaError_t configure_kernels() {
 }
 
 // ----------------------------------------------------------------- bins ---
+__global__ void widen3_kernel(const float *a, const float *b, const float *c, double *x, double *y, double *z,
+                              long long n) {
+	for(long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+		x[i] = (double) a[i];
+		y[i] = (double) b[i];
+		z[i] = (double) c[i];
+	}
+}
+
+void launch_widen3(const float *a, const float *b, const float *c, double *x, double *y, double *z, long long n,
+                   cudaStream_t s) {
+	if(n <= 0) return;
+	const long long blocks = std::min<long long>((n + 255) / 256, 152LL * 16);
+	widen3_kernel<<<(int) blocks, 256, 0, s>>>(a, b, c, x, y, z, n);
+}
+
 __global__ void bins_kernel(const CellDev *cells, const LayerDev *layers, int N, int *bin_count, int *bin_cells,
                             DevStatus *st) {
 	const int ci = blockIdx.x * blockDim.x + threadIdx.x;

@@ -8,10 +8,14 @@
 //   f_interaction (chemical potential) WetPolarModel.cpp:262-301, WetModel.cpp:487-613
 //   calc_internal_forces ............. WetPolarModel.cpp:304-339, WetModel.cpp:616-694
 //
+// The force evaluation's mu and gradients, which only the FP32 update reads,
+// are kept in FP32 arrays (muf, dxf, dyf): 12 B per site instead of 24, and
+// no conversions on either side; downloads and observables widen them.
+//
 // Precision pattern: the patch, chemical potential, stresses, forces and the
-// Heun update run in FP32 (shared memory in FP32); fields stay stored in FP64
-// (the box gather, the viscous solve and every download read them unchanged),
-// converted on the integer pipes (on GB300 the conversion instructions issue
+// Heun update run in FP32 (shared memory in FP32); phi, the velocities and
+// the right-hand side stay stored in FP64 (the box gather and the viscous
+// solve read them unchanged), converted on the integer pipes (on GB300 the conversion instructions issue
 // on the narrow FP64 pipe).  The area integral sum(phi^2) that drives the
 // area constraint accumulates in double-float (near FP64); the other per-cell
 // sums come from FP32 per-thread partials combined in FP64.  This
@@ -176,9 +180,9 @@ __global__ void __launch_bounds__(BLOCK) cell_kernel_f32(const CellArgs a) {
 			}
 			if(MODEL == M_POLAR && has_beta) V = V + beta_t * lap;
 			if(EVAL == EV_STORE || EVAL == EV_WET_RHS) {
-				a.mu[start + q] = f2d_int(V);
-				a.dxg[start + q] = f2d_int(dx);
-				a.dyg[start + q] = f2d_int(dy);
+				a.muf[start + q] = V;
+				a.dxf[start + q] = dx;
+				a.dyf[start + q] = dy;
 				a.mapg[start + q] = k;
 			}
 			if(MODEL == M_POLAR) {
@@ -256,23 +260,24 @@ __global__ void __launch_bounds__(BLOCK) cell_kernel_f32(const CellArgs a) {
 				yy[u] = w.y;
 				w.next();
 			}
-			double gm[UB], gvx[UB], gvy[UB], gdx[UB], gdy[UB], gp[UB], gd[UB];
+			float gm[UB], gdx[UB], gdy[UB];
+			double gvx[UB], gvy[UB], gp[UB], gd[UB];
 #pragma unroll
 			for(int u = 0; u < UB; u++) {
 				const long long i = start + (qq[u] < n ? qq[u] : 0);
-				gm[u] = __ldcs(&a.mu[i]);
+				gm[u] = __ldcs(&a.muf[i]);
 				gvx[u] = __ldcs(&a.vxg[i]);
 				gvy[u] = __ldcs(&a.vyg[i]);
-				gdx[u] = __ldcs(&a.dxg[i]);
-				gdy[u] = __ldcs(&a.dyg[i]);
+				gdx[u] = __ldcs(&a.dxf[i]);
+				gdy[u] = __ldcs(&a.dyf[i]);
 				gp[u] = __ldcs(UPD == UP_PRED ? &a.phi_eval[i] : &a.phi_old[i]);
 				gd[u] = UPD == UP_CORR ? __ldcs(&a.dphi_old[i]) : 0.0;
 			}
 #pragma unroll
 			for(int u = 0; u < UB; u++) {
 				if(qq[u] >= n) break;
-				const float dx = d2f_int(gdx[u]), dy = d2f_int(gdy[u]);
-				const float dphi = -J0 * d2f_int(gm[u]) - d2f_int(gvx[u]) * dx - d2f_int(gvy[u]) * dy;
+				const float dx = gdx[u], dy = gdy[u];
+				const float dphi = -J0 * gm[u] - d2f_int(gvx[u]) * dx - d2f_int(gvy[u]) * dy;
 				update_site(qq[u], xx[u], yy[u], dphi, d2f_int(gp[u]), d2f_int(gd[u]));
 				af[6] += -.5f * (dx * dx - dy * dy);
 				af[7] += -dx * dy;
@@ -342,11 +347,11 @@ __global__ void __launch_bounds__(BLOCK) cell_kernel_f32(const CellArgs a) {
 			}
 		}
 		else {
-			mu = d2f_int(a.mu[start + q]);
+			mu = a.muf[start + q];
 			vx = d2f_int(a.vxg[start + q]);
 			vy = d2f_int(a.vyg[start + q]);
-			dx = d2f_int(a.dxg[start + q]);
-			dy = d2f_int(a.dyg[start + q]);
+			dx = a.dxf[start + q];
+			dy = a.dyf[start + q];
 		}
 		if(UPD == UP_NONE) continue;
 		float dphi;
@@ -356,7 +361,7 @@ __global__ void __launch_bounds__(BLOCK) cell_kernel_f32(const CellArgs a) {
 			// WetModel.cpp:167)
 			const Nb nb = patch_nb(q, x, y, lx, ly);
 			auto fe = [&](int s_) {
-				if(EVAL == EV_NONE) return d2f_int(a.mu[start + s_]);
+				if(EVAL == EV_NONE) return a.muf[start + s_];
 				return MODEL == M_POLAR ? smu[s_] : smw[s_];
 			};
 			const float lmu = fe(nb.r) + fe(nb.u) + fe(nb.l) + fe(nb.d) - 4.f * mu;

@@ -72,6 +72,7 @@ struct rc_engine {
 	int *mapg = nullptr;
 	double *phi2 = nullptr, *sq00 = nullptr, *sq01 = nullptr;
 	double *walls = nullptr;  // getWalls(k) per box site of every layer; null: periodic boxes
+	float *muf = nullptr, *dxf = nullptr, *dyf = nullptr;  // FP32 engines: mu and gradients in FP32
 	int *cnt = nullptr, *cover = nullptr, *cov_off = nullptr, *cov_idx = nullptr;
 	int *bin_count = nullptr, *bin_cells = nullptr;
 	double *tab_cos = nullptr, *tab_sin = nullptr;
@@ -226,6 +227,9 @@ static CellArgs cell_args(rc_engine *e) {
 	a.mu = e->mu;
 	a.dxg = e->dxg;
 	a.dyg = e->dyg;
+	a.muf = e->muf;
+	a.dxf = e->dxf;
+	a.dyf = e->dyf;
 	a.vxg = e->vx;
 	a.vyg = e->vy;
 	a.fxg = e->fx;
@@ -913,6 +917,9 @@ static int create_engine(const rc_params *params, int n_layers, const rc_box *bo
 	   (rc = dalloc(e, &e->scratch_phi, cap + (size_t) n_cells / 2 + 8)) ||
 	   (rc = dalloc(e, &e->rep, e->rep_on ? cap : 1)) || (rc = dalloc(e, &e->scratch_rep, e->rep_on ? cap : 1)))
 		return bail(rc);
+	if(params->precision == RC_PRECISION_FLOAT &&
+	   ((rc = dalloc(e, &e->muf, cap)) || (rc = dalloc(e, &e->dxf, cap)) || (rc = dalloc(e, &e->dyf, cap))))
+		return bail(rc);
 	if(has_walls) {
 		// the boxes' wall values (layers without walls stay zero)
 		if((rc = dalloc(e, &e->walls, (size_t) total_box))) return bail(rc);
@@ -1147,10 +1154,17 @@ int rc_get_sizes(const rc_engine *e, int *n_cells, int *lsub_x, int *lsub_y) {
 	return RC_OK;
 }
 
+// FP32 engines keep mu and the gradients in FP32: widen them into the FP64
+// arrays that downloads and observables read.
+static void widen_fields(rc_engine *e) {
+	if(e->muf) launch_widen3(e->muf, e->dxf, e->dyf, e->mu, e->dxg, e->dyg, e->S_cap, e->stream);
+}
+
 int rc_download(rc_engine *e, rc_cell_host *cells, unsigned mask) {
 	if(!e || (!cells && e->N > 0)) return RC_ERR_INVALID;
 	CUDA_TRY(e, cudaSetDevice(e->device));
 	materialise(e, 0);
+	if(mask & (RC_FIELD_MU | RC_FIELD_GRAD)) widen_fields(e);
 	std::vector<CellDev> hc((size_t) std::max(e->N, 1));
 	CUDA_TRY(e, cudaMemcpyAsync(hc.data(), e->cells, sizeof(CellDev) * (size_t) std::max(e->N, 1), cudaMemcpyDeviceToHost, e->stream));
 	CUDA_TRY(e, cudaStreamSynchronize(e->stream));
@@ -1821,6 +1835,7 @@ int rc_observe_cells(rc_engine *e, double *cell_obs, double *layer_obs) {
 	int rc;
 	if((rc = obs_scratch(e, 6 * nc + 4 * nl))) return rc;
 	materialise(e, 0);  // current gradients (dry models)
+	widen_fields(e);
 	double *co = e->obs_buf, *lo = co + 6 * nc;
 	launch_obs_cells(e->cells, e->layers, e->N, e->n_layers, e->dxg, e->dyg, co, lo, e->stream);
 	CUDA_TRY(e, cudaGetLastError());

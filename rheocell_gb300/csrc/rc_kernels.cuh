@@ -34,6 +34,9 @@ struct CellArgs {
 	double *phi_out;         // PRED: phi*; CORR: phi^{n+1}
 	double *dphi_old;
 	double *mu, *dxg, *dyg, *vxg, *vyg, *fxg, *fyg;
+	// FP32 engines: the force evaluation's mu and gradients in FP32 (they feed
+	// only the FP32 update; downloads and observables widen them into mu, dxg, dyg)
+	float *muf, *dxf, *dyf;
 	int *mapg;
 	double *rep;
 	const double *phi2, *sq00, *sq01;
@@ -140,6 +143,9 @@ void launch_cell_finish(int model, int eval, int upd, bool f32, const CellArgs &
 size_t cell_smem_bytes(int model, int smem_n);
 int cell_smem_arrays(int model);
 void launch_rng(CellDev *cells, LayerDev *layers, int n_layers, DevStatus *st, cudaStream_t s);
+// out_k[i] = in_k[i] for three float arrays of n elements (FP32 engines' mu and gradients)
+void launch_widen3(const float *a, const float *b, const float *c, double *x, double *y, double *z, long long n,
+                   cudaStream_t s);
 void launch_bins(CellDev *cells, const LayerDev *layers, int N, int *bin_count, int *bin_cells, int total_bins,
                  DevStatus *st, cudaStream_t s);
 void launch_repack(CellArgs a, double *scratch_phi, double *scratch_rep, long long cap, cudaStream_t s);
