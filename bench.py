@@ -683,8 +683,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--solver", default=None, choices=["plain", "learned"],
                     help="viscous solver (default: learned for the wet workloads)")
-    ap.add_argument("--harvest-steps", type=int, default=160)
-    ap.add_argument("--harvest-capacity", type=int, default=4000)
+    ap.add_argument("--harvest-steps", type=int, default=320)
+    ap.add_argument("--harvest-capacity", type=int, default=8000)
     ap.add_argument("--train-epochs", type=int, default=30)
     ap.add_argument("--solver-phases", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default cell tile (FP32 only)")

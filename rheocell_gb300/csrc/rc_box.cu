@@ -109,7 +109,8 @@ __global__ void __launch_bounds__(BIN_X *BIN_Y) box_gather_kernel(const BoxArgs 
 			q1 += phi * s_q01[i];
 		}
 		if(a.want_cover) {
-			if(n < STORE_MAX) a.cover[(size_t) n * L2 + k] = j;
+			// a member's cover lists are [slot][its L x L sites] from STORE_MAX * box_off
+			if(n < STORE_MAX) a.cover[(size_t) STORE_MAX * lay.box_off + (size_t) n * L2 + kl] = j;
 			else {
 				atomicOr(&a.st->err, ERR_OVERLAP);
 				a.st->err_where = k;
@@ -143,10 +144,36 @@ __global__ void bookkeeping_kernel(DevStatus *st, int restart_every, int solve_f
 	if(solve_follows) st->cg_cold = (st->S_rows != rows_old) ? 1 : 0;
 }
 
+// The same bookkeeping for every member of a wet ensemble, one thread per
+// member: a member's unknowns are its cells' sites.
+__global__ void bookkeeping_layers_kernel(const CellDev *cells, const LayerDev *layers, int n_layers, LayerSolve *ls,
+                                          int restart_every, int solve_follows) {
+	const int l = blockIdx.x * blockDim.x + threadIdx.x;
+	if(l >= n_layers) return;
+	const LayerDev &ly = layers[l];
+	const long long S = ly.cell_hi > ly.cell_lo
+	                        ? (long long) cells[ly.cell_hi - 1].start + cells[ly.cell_hi - 1].n - cells[ly.cell_lo].start
+	                        : 0;
+	LayerSolve &b = ls[l];
+	long long rows_old;
+	if(b.restart < restart_every) rows_old = b.S_rows;
+	else {
+		rows_old = 0;
+		b.restart = 0;
+	}
+	b.S_rows = S;
+	if(solve_follows) b.cg_cold = (b.S_rows != rows_old) ? 1 : 0;
+}
+
 void launch_box_gather(const BoxArgs &a, cudaStream_t s) {
 	if(a.f32) box_gather_kernel<true><<<a.total_bins, BIN_X * BIN_Y, 0, s>>>(a);
 	else box_gather_kernel<false><<<a.total_bins, BIN_X * BIN_Y, 0, s>>>(a);
-	if(a.bookkeeping) bookkeeping_kernel<<<1, 1, 0, s>>>(a.st, a.restart_every, a.solve_follows);
+	if(a.bookkeeping) {
+		if(a.lsolve)
+			bookkeeping_layers_kernel<<<(a.n_layers + 127) / 128, 128, 0, s>>>(a.cells, a.layers, a.n_layers, a.lsolve,
+			                                                                   a.restart_every, a.solve_follows);
+		else bookkeeping_kernel<<<1, 1, 0, s>>>(a.st, a.restart_every, a.solve_follows);
+	}
 }
 
 }  // namespace rc

@@ -52,6 +52,8 @@ struct CGShared {
 	int act[2], it[2], first, zero[2];
 	int site_first, site_step, site_end;  // by-site phases: this block's box sites
 	int hbase, hm;            // harvesting: first slot of this solve, points taken
+	long long jlo, S;         // this solve's unknowns [jlo, jlo + S) (a member's, for ensembles)
+	int cold;                 // cold start
 	unsigned long long tmark; // diagnostic phase timers: last mark (block 0, thread 0)
 	unsigned epoch;           // grid barriers passed (the same count in every block)
 	int fail;                 // a barrier wait ran out (sticky)
@@ -742,7 +744,7 @@ __device__ __forceinline__ bool harvest_point(const CGArgs &a, CGShared &sh, con
 	}
 	if(blockIdx.x == 0 && threadIdx.x < 2) {
 		const int c = threadIdx.x;
-		a.harv_s[q0 + c] = sh.act[c] ? (float) sqrt(sh.rn2[c] / (double) a.st->S) : 0.f;
+		a.harv_s[q0 + c] = sh.act[c] ? (float) sqrt(sh.rn2[c] / (double) sh.S) : 0.f;
 	}
 	if(!grid_reduce(a, sh, 0, nullptr)) return false;
 	const long long E = __ldcg(&a.cov_off[L2]);
@@ -1292,7 +1294,7 @@ __device__ __noinline__ bool fcg_phase_c(const CGArgs &a, CGShared &sh, float *w
 // the network input x0 as true_residual(RES_FLOAT_COVER) leaves them.  Stops
 // a component at |r|^2 < thr.
 __device__ __noinline__ bool fcg_iterate(const CGArgs &a, CGShared &sh, TcCtx &tc, long long max_it) {
-	const long long S = a.st->S;
+	const long long S = sh.S;
 	for(int d = threadIdx.x; d <= CG_MAX_D; d += blockDim.x) {
 		sh.Tf[d] = (float) sh.T[d];
 		sh.iTf[d] = (float) sh.iT[d];
@@ -1349,9 +1351,26 @@ __device__ __noinline__ bool fcg_iterate(const CGArgs &a, CGShared &sh, TcCtx &t
 
 template<bool LEARNED, int NB>
 __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcCtx &tc) {
-	const long long S = a.st->S;
-	const int cold = a.st->cg_cold;
 	const double eta = a.eta;
+	if(threadIdx.x == 0) {
+		if(a.layer >= 0) {
+			// a member of an ensemble: its cells' sites are contiguous
+			const LayerDev &ly = a.layers[a.layer];
+			const CellDev &c0 = a.cells[ly.cell_lo];
+			const CellDev &c1 = a.cells[ly.cell_hi - 1];
+			sh.jlo = ly.cell_hi > ly.cell_lo ? c0.start : 0;
+			sh.S = ly.cell_hi > ly.cell_lo ? (long long) c1.start + c1.n - c0.start : 0;
+			sh.cold = a.lsolve[a.layer].cg_cold;
+		}
+		else {
+			sh.jlo = 0;
+			sh.S = a.st->S;
+			sh.cold = a.st->cg_cold;
+		}
+	}
+	__syncthreads();
+	const long long S = sh.S, jlo = sh.jlo;
+	const int cold = sh.cold;
 	const long long gtid = blockIdx.x * (long long) blockDim.x + threadIdx.x;
 	const long long gstride = (long long) gridDim.x * blockDim.x;
 	if(threadIdx.x == 0) {
@@ -1364,7 +1383,7 @@ __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcCtx &tc
 	}
 	__syncthreads();
 	if(cold) {
-		for(long long j = gtid; j < S; j += gstride) {
+		for(long long j = jlo + gtid; j < jlo + S; j += gstride) {
 			a.vx[j] = 0.0;
 			a.vy[j] = 0.0;
 		}
@@ -1396,7 +1415,7 @@ __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcCtx &tc
 	}
 	__syncthreads();
 	if(sh.zero[0] || sh.zero[1]) {
-		for(long long j = gtid; j < S; j += gstride) {
+		for(long long j = jlo + gtid; j < jlo + S; j += gstride) {
 			if(sh.zero[0]) a.vx[j] = 0.0;
 			if(sh.zero[1]) a.vy[j] = 0.0;
 		}
@@ -1477,8 +1496,9 @@ __device__ __forceinline__ void cg_body(const CGArgs &a, CGShared &sh, TcCtx &tc
 			// reached the goal)
 			if(a.fail_noconv && !sh.zero[c] && !(sh.rn2[c] < sh.thr[c])) atomicOr(&st->err, ERR_NOCONV);
 		}
-		if(cold) st->restart = 0;
-		else st->restart += 1;
+		int &restart = a.layer >= 0 ? a.lsolve[a.layer].restart : st->restart;
+		if(cold) restart = 0;
+		else restart += 1;
 	}
 }
 

@@ -105,6 +105,15 @@ struct DevStatus {
 	double rng_cached;
 };
 
+// Solver bookkeeping of one member of a wet ensemble (the single-monolayer
+// engine keeps it in DevStatus): size_rows, restart_solver and the cold-start
+// flag of its next solve (WetModel.cpp:195-209).
+struct LayerSolve {
+	long long S_rows;
+	int restart;
+	int cg_cold;
+};
+
 __host__ __device__ inline int wrapi(int v, int L) {
 	v %= L;
 	return v < 0 ? v + L : v;

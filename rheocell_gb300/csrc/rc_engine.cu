@@ -73,6 +73,8 @@ struct rc_engine {
 	double *phi2 = nullptr, *sq00 = nullptr, *sq01 = nullptr;
 	double *walls = nullptr;  // getWalls(k) per box site of every layer; null: periodic boxes
 	float *muf = nullptr, *dxf = nullptr, *dyf = nullptr;  // FP32 engines: mu and gradients in FP32
+	LayerSolve *lsolve = nullptr;  // wet ensembles: each member's solver bookkeeping
+	std::vector<int> layer_blocks[2];  // wet ensembles: solve grid per member (plain FP64, flexible CG)
 	int *cnt = nullptr, *cover = nullptr, *cov_off = nullptr, *cov_idx = nullptr;
 	int *bin_count = nullptr, *bin_cells = nullptr;
 	double *tab_cos = nullptr, *tab_sin = nullptr;
@@ -299,6 +301,7 @@ static void gather(rc_engine *e, const double *phi, int phase) {
 	b.solve_follows = wet_phase(e, phase);
 	b.st = e->st;
 	b.L = e->L;
+	b.lsolve = e->n_layers > 1 ? e->lsolve : nullptr;
 	StageMark sm(e, RC_TIMER_GATHER);
 	launch_box_gather(b, e->stream);
 	e->launches += b.bookkeeping ? 2 : 1;
@@ -309,6 +312,9 @@ static void gather(rc_engine *e, const double *phi, int phase) {
 // when the engine collects them (plain FP64 solves only).
 static int solve_args(rc_engine *e, int phase, int solver, bool harvest, double *vx, double *vy, CGArgs &g) {
 	memset(&g, 0, sizeof(g));
+	g.layer = -1;  // the single monolayer (solve() sets each member of an ensemble)
+	g.layers = e->layers;
+	g.lsolve = e->lsolve;
 	g.cells = e->cells;
 	g.mapg = e->mapg;
 	g.cnt = e->cnt;
@@ -397,10 +403,29 @@ static void solve(rc_engine *e, int phase) {
 	CGArgs g;
 	const int blocks = solve_args(e, phase, e->solver, true, e->vx, e->vy, g);
 	StageMark sm(e, RC_TIMER_SOLVE);
-	cudaMemsetAsync(e->bar, 0, sizeof(unsigned) * 4, e->stream);  // the barrier counter starts at zero
-	const cudaError_t c = launch_cg(g, blocks, e->stream);
-	e->launches += 1;
-	if(c != cudaSuccess && e->launch_error.empty()) e->launch_error = cudaGetErrorString(c);
+	if(e->n_layers == 1) {
+		cudaMemsetAsync(e->bar, 0, sizeof(unsigned) * 4, e->stream);  // the barrier counter starts at zero
+		const cudaError_t c = launch_cg(g, blocks, e->stream);
+		e->launches += 1;
+		if(c != cudaSuccess && e->launch_error.empty()) e->launch_error = cudaGetErrorString(c);
+		return;
+	}
+	// an ensemble: each member's system in turn, on its own box, with the grid
+	// a monolayer of its size would get (the same launches as the member alone)
+	const bool mixed = g.fcg != 0;
+	for(int l = 0; l < e->n_layers; l++) {
+		const LayerDev &ly = e->layers_h[(size_t) l];
+		CGArgs m = g;
+		m.layer = l;
+		m.L = ly.L;
+		m.cnt = e->cnt + ly.box_off;
+		m.cover = e->cover + (size_t) STORE_MAX * ly.box_off;
+		const int b = e->layer_blocks[mixed ? 1 : 0][(size_t) l];
+		cudaMemsetAsync(e->bar, 0, sizeof(unsigned) * 4, e->stream);
+		const cudaError_t c = launch_cg(m, b, e->stream);
+		e->launches += 1;
+		if(c != cudaSuccess && e->launch_error.empty()) e->launch_error = cudaGetErrorString(c);
+	}
 }
 
 // Forces (and the viscous solve) at phi^n for the current phase, run at its
@@ -778,8 +803,6 @@ static int create_engine(const rc_params *params, int n_layers, const rc_box *bo
 	                     (params->friction_cell[0] != 0.0 || params->friction_cell[1] != 0.0);
 	if(params->precision == RC_PRECISION_FLOAT && params->model != RC_WETPOLARMODEL && params->model != RC_WETMODEL)
 		return set_err(nullptr, RC_ERR_UNSUPPORTED, "FP32 site arithmetic is provided for wetpolarmodel and wetmodel only");
-	if(n_layers > 1 && any_wet)
-		return set_err(nullptr, RC_ERR_UNSUPPORTED, "batches of monolayers are provided for dry evaluations only");
 	bool has_walls = false;
 	for(int l = 0; l < n_layers; l++) has_walls |= boxes[l].walls != nullptr;
 	if(has_walls && any_wet)
@@ -951,6 +974,16 @@ static int create_engine(const rc_params *params, int n_layers, const rc_box *bo
 			e->cg_blocks_learned = cg_grid_blocks(device, true, (long long) L * L);
 		}
 		e->cg_blocks = cg_grid_blocks(device, false, (long long) L * L);
+		// an ensemble's members keep their own solver bookkeeping (size_rows,
+		// restart counter, cold-start flag), zeroed like DevStatus's
+		if(n_layers > 1) {
+			if((rc = dalloc(e, &e->lsolve, (size_t) n_layers))) return bail(rc);
+			for(int l = 0; l < n_layers; l++) {
+				const long long sites = (long long) layers[(size_t) l].L * layers[(size_t) l].L;
+				e->layer_blocks[0].push_back(cg_grid_blocks(device, false, sites));
+				e->layer_blocks[1].push_back(cg_grid_blocks(device, true, sites));
+			}
+		}
 	}
 	if(cudaMallocHost(&e->st_host, sizeof(DevStatus)) != cudaSuccess) return bail(set_err(e, RC_ERR_OOM, "pinned alloc failed"));
 
@@ -1303,6 +1336,7 @@ static bool is_wet_engine(const rc_engine *e) { return e->fx != nullptr; }
 int rc_learned_harvest(rc_engine *e, int capacity, int every, int per_solve) {
 	if(!e) return RC_ERR_INVALID;
 	if(!is_wet_engine(e)) return set_err(e, RC_ERR_UNSUPPORTED, "rc_learned_harvest: the engine has no viscous solve");
+	if(e->n_layers > 1) return set_err(e, RC_ERR_UNSUPPORTED, "rc_learned_harvest: not provided for ensembles");
 	if(per_solve == 0 && capacity > 0) {
 		// stop collecting, keep the stored samples
 		CUDA_TRY(e, cudaSetDevice(e->device));
@@ -1530,6 +1564,8 @@ static int prepare_solver(rc_engine *e, int solver, const char *who) {
 		return set_err(e, RC_ERR_INVALID, "%s: unknown solver %d", who, solver);
 	if(solver == RC_SOLVER_PLAIN_FP64 && !is_wet_engine(e))
 		return set_err(e, RC_ERR_UNSUPPORTED, "%s: the engine has no viscous solve", who);
+	if(solver != RC_SOLVER_PLAIN && e->n_layers > 1)
+		return set_err(e, RC_ERR_UNSUPPORTED, "%s: ensembles solve each member with the engine's plain solver only", who);
 	if(solver == RC_SOLVER_LEARNED || solver == RC_SOLVER_LEARNED_FP32) {
 		if(!is_wet_engine(e)) return set_err(e, RC_ERR_UNSUPPORTED, "%s: the engine has no viscous solve", who);
 		if(e->L % 4 != 0 || e->L < 8)
@@ -1648,6 +1684,7 @@ int rc_viscous_resolve(rc_engine *e, int solver, double *vx, double *vy, long lo
 	if(!e) return RC_ERR_INVALID;
 	if(!vx || !vy) return set_err(e, RC_ERR_INVALID, "rc_viscous_resolve: NULL output array");
 	if(n != e->S) return set_err(e, RC_ERR_INVALID, "rc_viscous_resolve: n = %lld but the state has %lld unknowns", n, e->S);
+	if(e->n_layers > 1) return set_err(e, RC_ERR_UNSUPPORTED, "rc_viscous_resolve: not provided for ensembles");
 	if(e->pending || !wet_phase(e, e->eval_phase))
 		return set_err(e, RC_ERR_UNSUPPORTED, "rc_viscous_resolve: the last evaluation had no viscous solve");
 	CUDA_TRY(e, cudaSetDevice(e->device));
@@ -1912,6 +1949,7 @@ extern "C" {
  */
 int rc_viscous_resolve_noalloc(rc_engine *e, double *vx, double *vy, long long n, int *iterations) {
 	if(!e) return RC_ERR_INVALID;
+	if(e->n_layers > 1) return set_err(e, RC_ERR_UNSUPPORTED, "rc_viscous_resolve_noalloc: not provided for ensembles");
 	if(!vx || !vy) return set_err(e, RC_ERR_INVALID, "rc_viscous_resolve_noalloc: NULL output array");
 	if(n != e->S)
 		return set_err(e, RC_ERR_INVALID, "rc_viscous_resolve_noalloc: n = %lld but the state has %lld unknowns", n, e->S);
@@ -1951,6 +1989,7 @@ int rc_viscous_resolve_noalloc(rc_engine *e, double *vx, double *vy, long long n
 	CUDA_TRY(e, cudaGetLastError());
 	CGArgs g;
 	memset(&g, 0, sizeof(g));
+	g.layer = -1;  // the single monolayer
 	g.cells = e->cells;
 	g.mapg = e->mapg;
 	g.cnt = e->cnt;

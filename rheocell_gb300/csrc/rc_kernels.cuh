@@ -78,6 +78,7 @@ struct BoxArgs {
 	int solve_follows;     // a viscous solve follows this evaluation
 	DevStatus *st;
 	int L;
+	LayerSolve *lsolve;    // wet ensembles: per-member bookkeeping (null: DevStatus)
 };
 
 struct CGArgs {
@@ -129,6 +130,12 @@ struct CGArgs {
 	// blocks -- a test hook that makes the wait run out (nothing arrives)
 	int barrier_extra;
 	long long spin_limit;
+	// ensembles: the member whose system this launch solves (-1: the single
+	// monolayer); its box arrays (cnt, cover) and L are the member's, its
+	// unknowns the contiguous run of its cells' sites, its bookkeeping lsolve[layer]
+	int layer;
+	const LayerDev *layers;
+	LayerSolve *lsolve;
 };
 
 cudaError_t configure_kernels();

@@ -110,14 +110,17 @@ def test_create_rejects_bad_box_and_cells(lib):
         c0.lsub_x, c0.offset_x, c0.corner, c0.phi = saved
 
 
-def test_batches_of_wet_monolayers_are_rejected(lib):
+def test_batches_of_wet_monolayers_with_walls_are_rejected(lib):
+    import numpy as np
     p, L, cells = _inputs()
-    boxes = (abi.RcBox * 2)(abi.RcBox(L, L), abi.RcBox(L, L))
+    walls = np.zeros(L * L)
+    walls[:L] = 1.0
+    boxes = (abi.RcBox * 2)(abi.make_box(L, walls), abi.RcBox(L, L))
     counts = (C.c_int * 2)(cells.n, 0)
     h = C.c_void_p()
     rc = lib.rc_batch_create(C.byref(p), 2, boxes, counts, cells.arr, None, 0, C.byref(h))
     assert rc == abi.RC_ERR_UNSUPPORTED and not h
-    assert "dry evaluations only" in lib.rc_last_error(None).decode()
+    assert "walls with a viscous solve" in lib.rc_last_error(None).decode()
 
 
 def test_null_handle_is_invalid(lib):
