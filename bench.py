@@ -474,7 +474,7 @@ def run_gb300(args, rank, world):
         out["config"]["sites_after"] = S_after
     if tuned is not None:
         out["config"]["cell_tile_threads"] = tuned["chosen"]
-        out["autotune"] = {"candidates_ms_per_step": {str(t): round(ms, 4) for t, ms in tuned["candidates"]},
+        out["autotune"] = {"cell_kernels_ms_per_step": {str(t): round(ms, 4) for t, ms in tuned["candidates"]},
                            "chosen": tuned["chosen"]}
     # the phi update (the per-cell update kernels) against its roofline, by
     # the minimal wet-stage bytes per site (predictor: read phi, vx, vy,

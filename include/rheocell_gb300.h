@@ -356,7 +356,9 @@ int rc_viscous_resolve_noalloc(rc_engine *e, double *vx, double *vy, long long n
  * FD_CPUBackend.cpp:44-120).  Each cell patch is swept by one CTA in tiles of
  * `threads` patch sites; rc_autotune times every candidate tile (128, 256,
  * 512 sites) over `steps_per_candidate` steps of this engine's own workload
- * (one untimed step first) and keeps the fastest.  The simulation advances by
+ * (one untimed step first) by the stage timers of the cell kernels (updates
+ * and force evaluations; ms_per_step reports their time per step) and keeps
+ * the fastest.  The simulation advances by
  * 3 x (steps_per_candidate + 1) steps.  The FP32 results of different tiles
  * differ by rounding only (their per-warp partial sums are grouped
  * differently).  FP64 engines keep one tile (their summation order is part of

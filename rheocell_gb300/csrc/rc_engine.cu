@@ -1119,27 +1119,26 @@ int rc_autotune(rc_engine *e, int steps_per_candidate, rc_autotune_report *repor
 		return RC_OK;
 	}
 	CUDA_TRY(e, cudaSetDevice(e->device));
-	cudaEvent_t t0, t1;
-	CUDA_TRY(e, cudaEventCreate(&t0));
-	CUDA_TRY(e, cudaEventCreate(&t1));
+	// each candidate is timed by the stage timers of the launches the tile
+	// changes (the cell kernels: updates and force evaluations), so that the
+	// viscous solve's run-to-run spread does not decide the tile
+	const bool was_timing = e->timing;
 	int rc = RC_OK, best = -1;
 	for(int b : CELL_F32_BLOCKS) {
 		if((rc = rc_set_cell_threads(e, b))) break;
-		if((rc = rc_step(e, 1, nullptr))) break;  // captures this tile's step graph
-		cudaEventRecord(t0, e->stream);
-		if((rc = rc_step_async(e, steps_per_candidate))) break;
-		cudaEventRecord(t1, e->stream);
-		cudaEventSynchronize(t1);
-		if((rc = rc_wait(e, nullptr))) break;
-		float ms = 0.f;
-		cudaEventElapsedTime(&ms, t0, t1);
+		if((rc = rc_step(e, 1, nullptr))) break;  // one untimed step with this tile
+		e->timing = true;
+		if((rc = rc_timers(e, nullptr, nullptr, 1))) break;
+		if((rc = rc_step(e, steps_per_candidate, nullptr))) break;
+		double ms[RC_NUM_TIMERS];
+		if((rc = rc_timers(e, ms, nullptr, 1))) break;
+		e->timing = was_timing;
 		r.threads[r.candidates] = b;
-		r.ms_per_step[r.candidates] = (double) ms / steps_per_candidate;
+		r.ms_per_step[r.candidates] = (ms[RC_TIMER_UPDATE] + ms[RC_TIMER_FORCES]) / steps_per_candidate;
 		if(best < 0 || r.ms_per_step[r.candidates] < r.ms_per_step[best]) best = r.candidates;
 		r.candidates++;
 	}
-	cudaEventDestroy(t0);
-	cudaEventDestroy(t1);
+	e->timing = was_timing;
 	if(rc) return rc;
 	if((rc = rc_set_cell_threads(e, r.threads[best]))) return rc;
 	r.chosen = e->f32_block;
