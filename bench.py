@@ -162,6 +162,24 @@ def cg_bytes_per_launch(S, L2, iters_per_launch, setup_reads=68.0):
     return S * setup_reads + iters_per_launch * (S * 88.0 + L2 * 20.0)
 
 
+# BF16 activation bytes of one network application per finest-grid pixel and
+# velocity component: every layer reads its input and writes its output once
+# (the first layer's FP32 input, the pooled and upsampled inputs at their own
+# resolution, the last layer's FP32 output), summed over the three levels
+NET_BYTES_PER_PIXEL = 348.0
+
+
+def learned_bytes_per_launch(S, L2, inner_per_launch, refinements_per_launch):
+    """Algorithmic bytes of one learned-solve launch (both components):
+    setup S*68 B; per inner iteration and component the flexible CG's
+    minimal FP32 vector passes (11 x 4 B per unknown) and the network
+    application (NET_BYTES_PER_PIXEL per box pixel); per refinement sweep
+    and component the FP64 true residual (read b, x, e, write x, r: 40 B per
+    unknown)."""
+    return (S * 68.0 + inner_per_launch * (S * 44.0 + L2 * NET_BYTES_PER_PIXEL)
+            + refinements_per_launch * 2 * S * 40.0)
+
+
 def fused_bytes_per_site(model):
     """Algorithmic HBM bytes per site of the dry fused predictor+corrector pair:
     predictor reads phi^n, writes phi*, dphi^n (24 B); corrector reads phi*,
@@ -420,7 +438,15 @@ def run_gb300(args, rank, world):
     peak, peak_kind = measured_peaks()
     dom = max(range(6), key=lambda i: tms[i])
     dom_avg_s = tms[dom] / max(tn[dom], 1) / 1e3
-    if names[dom] == "solve":
+    if names[dom] == "solve" and args.solver == "learned":
+        it_per_launch = st2.cg_iterations / max(tn[dom], 1)
+        ref_per_launch = st2.refinements / max(tn[dom], 1)
+        bytes_launch = learned_bytes_per_launch(S, L2, it_per_launch, ref_per_launch)
+        unit_desc = ("learned solve: %.1f inner component-iterations and %.1f refinement sweeps per launch "
+                     "(FP32 flexible CG, BF16 network, FP64 residuals); binding limit: grid barriers and the "
+                     "network's row pipeline, not DRAM or the tensor pipe (profiles/cg_kernel_learned_wet512.md)"
+                     % (it_per_launch, ref_per_launch))
+    elif names[dom] == "solve":
         it_per_launch = st2.cg_iterations / max(tn[dom], 1)
         bytes_launch = cg_bytes_per_launch(S, L2, it_per_launch)
         unit_desc = "viscous solve: %.1f component-iterations per launch" % it_per_launch
