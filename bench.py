@@ -67,6 +67,11 @@ def workload(name):
         return dict(name="ensemble of 64 dry polar monolayers, box side uniform in 96-256 (numpy seed 64), "
                          "N = round(0.75 L^2 / (pi 8^2)) cells each, R=8, 41x41 patches, seeds 1000-1063, FP64",
                     members=ensemble_members(), params=g.DRY_POLAR, seed=1000)
+    if name == "ensemble64wet":
+        return dict(name="ensemble of 64 wet monolayers (wetmodel, xi=eta=1, CG rtol 1e-8), box side uniform in "
+                         "96-256 (numpy seed 64), N = round(0.75 L^2 / (pi 8^2)) cells each, R=8, 41x41 patches, "
+                         "seeds 1000-1063; each member's viscous system solved on its own box",
+                    members=ensemble_members(), params=g.WET_NEMATIC, seed=1000)
     raise SystemExit("unknown workload %s" % name)
 
 
@@ -703,7 +708,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="wet1024", choices=["wet1024", "wet512", "wet256", "dry140", "ensemble64"])
+    ap.add_argument("--workload", default="wet1024",
+                    choices=["wet1024", "wet512", "wet256", "dry140", "ensemble64", "ensemble64wet"])
     ap.add_argument("--precision", default=None, choices=["double", "mixed", "float"],
                     help="default: float (FP32 site arithmetic) for the wet workloads, double otherwise")
     ap.add_argument("--no-cpu-baseline", action="store_true")
