@@ -206,8 +206,8 @@ def solve_stage(eng, lib, steps, flush):
         lib.rc_step_async(eng.h, 1)
     torch.cuda.synchronize()
     lib.rc_wait(eng.h, C.byref(st))
-    tms = (C.c_double * 6)()
-    tn = (C.c_longlong * 6)()
+    tms = (C.c_double * abi.NUM_TIMERS)()
+    tn = (C.c_longlong * abi.NUM_TIMERS)()
     lib.rc_timers(eng.h, tms, tn, 1)
     lib.rc_set_timing(eng.h, 0)
     return tms[3] / steps, st.cg_iterations / max(st.cg_solves, 1), st.cg_max_rel_residual
@@ -410,8 +410,8 @@ def run_gb300(args, rank, world):
         lib.rc_step_async(eng.h, 1)
     torch.cuda.synchronize()
     lib.rc_wait(eng.h, C.byref(st2))
-    tms = (C.c_double * 6)()
-    tn = (C.c_longlong * 6)()
+    tms = (C.c_double * abi.NUM_TIMERS)()
+    tn = (C.c_longlong * abi.NUM_TIMERS)()
     lib.rc_timers(eng.h, tms, tn, 1)
     lib.rc_set_timing(eng.h, 0)
     if world > 1:
@@ -439,9 +439,9 @@ def run_gb300(args, rank, world):
     total_sites = S * args.steps * world
     value = total_sites / (ms / 1e3)
     names = abi.TIMER_NAMES
-    stage = {names[i]: {"ms": round(tms[i], 3), "launches": int(tn[i])} for i in range(6) if tn[i]}
+    stage = {names[i]: {"ms": round(tms[i], 3), "launches": int(tn[i])} for i in range(abi.NUM_TIMERS) if tn[i]}
     peak, peak_kind = measured_peaks()
-    dom = max(range(6), key=lambda i: tms[i])
+    dom = max(range(abi.NUM_TIMERS), key=lambda i: tms[i])
     dom_avg_s = tms[dom] / max(tn[dom], 1) / 1e3
     if names[dom] == "solve" and args.solver == "learned":
         it_per_launch = st2.cg_iterations / max(tn[dom], 1)
@@ -507,21 +507,29 @@ def run_gb300(args, rank, world):
         out["config"]["cell_tile_threads"] = tuned["chosen"]
         out["autotune"] = {"cell_kernels_ms_per_step": {str(t): round(ms, 4) for t, ms in tuned["candidates"]},
                            "chosen": tuned["chosen"]}
-    # the phi update (the per-cell update kernels) against its roofline, by
-    # the minimal wet-stage bytes per site (predictor: read phi, vx, vy,
-    # write phi*, dphi = 40 B; corrector: read phi*, phi^n, dphi, vx, vy,
-    # write phi = 48 B; FP64 storage) and by the bytes the kernels move
-    # (they also read the force evaluation's mu and gradients: 64 B)
+    # the phi update (the per-cell update kernel alone; its per-cell epilogue
+    # is timed apart) against its roofline.  Algorithmic bytes per site =
+    # the update's inputs and outputs as the engine stores them: phi and the
+    # solve's velocities in FP64, the force evaluation's mu and gradient
+    # (FP32 engines: FP32, 12 B; FP64 engines: 24 B), dphi^n (FP32 engines:
+    # FP32).  Predictor: read phi, vx, vy, mu, d_x phi, d_y phi, write phi*,
+    # dphi; corrector: read phi^n, dphi, vx, vy, mu, d_x phi, d_y phi, write
+    # phi^{n+1}: 48 B each on FP32 engines (64 B on FP64 engines).  Beside it,
+    # the analysis formula of the update (reads phi* in the corrector, leaves
+    # out mu and the gradient): 36 + 44 B (FP32 dphi), 40 + 48 B (FP64).
     iu = names.index("update")
     if tn[iu] and args.workload.startswith("wet"):
         upd_s = tms[iu] / tn[iu] / 1e3
-        # FP32 engines keep mu and the gradients in FP32 (12 B of the reads instead of 24)
-        moved = 52.0 if args.precision == "float" else 64.0
+        alg = 48.0 if args.precision == "float" else 64.0
+        formula = 40.0 if args.precision == "float" else 44.0
+        ie = names.index("epilogue")
         out["phi_update"] = {
+            "kernel": "cell_update_bulk" if args.precision == "float" else "cell_kernel",
             "launch_ms": upd_s * 1e3, "launches": int(tn[iu]),
-            "achieved_gbs": 44.0 * S / upd_s / 1e9, "frac": 44.0 * S / upd_s / 1e9 / peak,
-            "algorithmic_bytes_per_site": 44.0, "moved_bytes_per_site": moved,
-            "moved_gbs": moved * S / upd_s / 1e9, "moved_frac": moved * S / upd_s / 1e9 / peak,
+            "achieved_gbs": alg * S / upd_s / 1e9, "frac": alg * S / upd_s / 1e9 / peak,
+            "algorithmic_bytes_per_site": alg,
+            "formula_bytes_per_site": formula, "formula_frac": formula * S / upd_s / 1e9 / peak,
+            "epilogue_ms": tms[ie] / tn[ie] if tn[ie] else None,
             "peak": peak, "unit": "GB/s"}
     if learned is not None:
         out["learned_pcg"] = learned

@@ -305,7 +305,9 @@ int rc_upload_phi(rc_engine *e, const double *phi, long long n);
 #define RC_TIMER_SOLVE  3   /* viscous solve                                  */
 #define RC_TIMER_REPACK 4   /* patch resize repack                            */
 #define RC_TIMER_RNG    5   /* polar noise stream                             */
-#define RC_NUM_TIMERS   6
+#define RC_TIMER_EPILOGUE 6 /* per-cell epilogue kernel of a split update:
+                               cell sums, positions, directed forces        */
+#define RC_NUM_TIMERS   7
 int rc_set_timing(rc_engine *e, int enable);
 int rc_timers(rc_engine *e, double *ms, long long *launches, int reset);
 

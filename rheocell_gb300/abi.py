@@ -245,4 +245,5 @@ EXPORTED = ["rc_abi_version", "rc_create", "rc_create_generated", "rc_batch_crea
             "rc_get_sizes", "rc_download", "rc_upload", "rc_download_phi", "rc_upload_phi", "rc_set_stream",
             "rc_set_timing", "rc_timers", "rc_site_count", "rc_last_error", "rc_destroy"]
 
-TIMER_NAMES = ["update", "gather", "forces", "solve", "repack", "rng"]
+TIMER_NAMES = ["update", "gather", "forces", "solve", "repack", "rng", "epilogue"]
+NUM_TIMERS = len(TIMER_NAMES)

@@ -32,6 +32,7 @@
 // the same terms as the reference's expression, grouped per site: stage 1
 // forms the three stress components once per site in shared memory.
 #include "rc_cell_dev.cuh"
+#include "rc_tc.cuh"
 
 namespace rc {
 
@@ -222,7 +223,7 @@ __global__ void __launch_bounds__(BLOCK) cell_kernel_f32(const CellArgs a) {
 	auto update_site = [&](int q, int x, int y, float dphi, float phi_pre, float dphi_prev) {
 		float phi_new;
 		if(UPD == UP_PRED) {
-			a.dphi_old[start + q] = f2d_int(dphi);
+			a.dphif[start + q] = dphi;
 			phi_new = phi_pre + hdt * (dphi + dphi);
 		}
 		else {
@@ -261,7 +262,8 @@ __global__ void __launch_bounds__(BLOCK) cell_kernel_f32(const CellArgs a) {
 				w.next();
 			}
 			float gm[UB], gdx[UB], gdy[UB];
-			double gvx[UB], gvy[UB], gp[UB], gd[UB];
+			double gvx[UB], gvy[UB], gp[UB];
+			float gd[UB];
 #pragma unroll
 			for(int u = 0; u < UB; u++) {
 				const long long i = start + (qq[u] < n ? qq[u] : 0);
@@ -271,14 +273,14 @@ __global__ void __launch_bounds__(BLOCK) cell_kernel_f32(const CellArgs a) {
 				gdx[u] = __ldcs(&a.dxf[i]);
 				gdy[u] = __ldcs(&a.dyf[i]);
 				gp[u] = __ldcs(UPD == UP_PRED ? &a.phi_eval[i] : &a.phi_old[i]);
-				gd[u] = UPD == UP_CORR ? __ldcs(&a.dphi_old[i]) : 0.0;
+				gd[u] = UPD == UP_CORR ? __ldcs(&a.dphif[i]) : 0.f;
 			}
 #pragma unroll
 			for(int u = 0; u < UB; u++) {
 				if(qq[u] >= n) break;
 				const float dx = gdx[u], dy = gdy[u];
 				const float dphi = -J0 * gm[u] - d2f_int(gvx[u]) * dx - d2f_int(gvy[u]) * dy;
-				update_site(qq[u], xx[u], yy[u], dphi, d2f_int(gp[u]), d2f_int(gd[u]));
+				update_site(qq[u], xx[u], yy[u], dphi, d2f_int(gp[u]), gd[u]);
 				af[6] += -.5f * (dx * dx - dy * dy);
 				af[7] += -dx * dy;
 			}
@@ -370,7 +372,7 @@ __global__ void __launch_bounds__(BLOCK) cell_kernel_f32(const CellArgs a) {
 		else
 			dphi = -J0 * mu - vx * dx - vy * dy;
 		if(UPD == UP_PRED) update_site(q, x, y, dphi, (EVAL != EV_NONE) ? phi_e : d2f_int(a.phi_eval[start + q]), 0.f);
-		else update_site(q, x, y, dphi, d2f_int(a.phi_old[start + q]), d2f_int(a.dphi_old[start + q]));
+		else update_site(q, x, y, dphi, d2f_int(a.phi_old[start + q]), a.dphif[start + q]);
 		af[6] += -.5f * (dx * dx - dy * dy);
 		af[7] += -dx * dy;
 	}
@@ -439,6 +441,358 @@ __global__ void __launch_bounds__(BLOCK) cell_kernel_f32(const CellArgs a) {
 	}
 }
 
+// The wet models' update alone, after the viscous solve (first_step,
+// FD_CPUBackend.cpp:44-120): dphi = -J0 mu - v . grad phi from the last
+// evaluation's mu and gradient, phi* = phi + dt dphi (predictor) or
+// phi^{n+1} = phi^n + dt/2 (dphi + dphi^n) (corrector), and the per-cell
+// sums of the new phi.  A pure stream over the patch: no per-cell set-up
+// beyond the patch's trig rows, staged in shared memory already rotated by
+// the patch offset (one 8-byte shared load per axis and site, no wrap); the
+// loads of UB sites are issued together at fixed offsets from one address;
+// the double -> float conversions are the short integer form (d2f_fast).
+// Per-warp partial sums go to the epilogue kernel (cell_finish_kernel),
+// which the engine runs after every FP32 wet update.
+template<int UPD, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) cell_update_f32(const CellArgs a) {
+	constexpr int UB = 2;
+	__shared__ float2 trow[2 * MAX_TABLE_SIDE];  // (cos, sin): patch columns, then rows at trow + lx
+	const int ci = blockIdx.x;
+	const CellDev *cp = a.cells + ci;
+	const int lx = cp->lx, ly = cp->ly, n = cp->n;
+	const long long start = cp->start;
+	{
+		const int offx = cp->offx, offy = cp->offy, tb = table_base(lx), tby = table_base(ly);
+		for(int i = threadIdx.x; i < lx + ly; i += BLOCK) {
+			int t;
+			if(i < lx) {
+				int j = i + offx;
+				if(j >= lx) j -= lx;
+				t = tb + j;
+			}
+			else {
+				int j = i - lx + offy;
+				if(j >= ly) j -= ly;
+				t = tby + j;
+			}
+			trow[i] = make_float2(a.tab_cosf[t], a.tab_sinf[t]);
+		}
+	}
+	const float J0 = d2f_int(a.P.J0), hdt = .5f * d2f_int(a.P.dt);
+	const float *mu = a.muf + start, *gx = a.dxf + start, *gy = a.dyf + start;
+	const double *ux = a.vxg + start, *uy = a.vyg + start;
+	const double *pin = (UPD == UP_PRED ? a.phi_eval : a.phi_old) + start;
+	float *dold = a.dphif + start;
+	double *pout = a.phi_out + start;
+	float sm[8];
+#pragma unroll
+	for(int i = 0; i < 8; i++) sm[i] = 0.f;
+	float area_s = 0.f, area_c = 0.f;
+	int imx = lx, imy = ly;
+	const int sy = BLOCK / lx, sx = BLOCK - sy * lx;
+	int q = threadIdx.x, y = q / lx, x = q - y * lx;
+	__syncthreads();
+	for(; q < n; q += UB * BLOCK) {
+		int xx[UB], yy[UB];
+#pragma unroll
+		for(int u = 0; u < UB; u++) {
+			xx[u] = x;
+			yy[u] = y;
+			x += sx;
+			y += sy;
+			if(x >= lx) {
+				x -= lx;
+				y += 1;
+			}
+		}
+		float m[UB], dx[UB], dy[UB];
+		double vx[UB], vy[UB], p[UB];
+		float d[UB];
+#pragma unroll
+		for(int u = 0; u < UB; u++) {
+			const bool ok = q + u * BLOCK < n;
+			m[u] = ok ? __ldcs(mu + q + u * BLOCK) : 0.f;
+			dx[u] = ok ? __ldcs(gx + q + u * BLOCK) : 0.f;
+			dy[u] = ok ? __ldcs(gy + q + u * BLOCK) : 0.f;
+			vx[u] = ok ? __ldcs(ux + q + u * BLOCK) : 0.0;
+			vy[u] = ok ? __ldcs(uy + q + u * BLOCK) : 0.0;
+			p[u] = ok ? __ldcs(pin + q + u * BLOCK) : 0.0;
+			d[u] = (UPD == UP_CORR && ok) ? __ldcs(dold + q + u * BLOCK) : 0.f;
+		}
+#pragma unroll
+		for(int u = 0; u < UB; u++) {
+			if(q + u * BLOCK >= n) break;
+			const float dphi = -J0 * m[u] - d2f_fast(vx[u]) * dx[u] - d2f_fast(vy[u]) * dy[u];
+			float pn;
+			if(UPD == UP_PRED) {
+				dold[q + u * BLOCK] = dphi;
+				pn = d2f_fast(p[u]) + hdt * (dphi + dphi);
+			}
+			else {
+				pn = d2f_fast(p[u]) + hdt * (dphi + d[u]);
+			}
+			pout[q + u * BLOCK] = f2d_int(pn);
+			acc_square(pn, area_s, area_c);
+			sm[1] += pn;
+			const float2 cx = trow[xx[u]], cy = trow[lx + yy[u]];
+			sm[2] += pn * cx.x;
+			sm[3] += pn * cx.y;
+			sm[4] += pn * cy.x;
+			sm[5] += pn * cy.y;
+			if(UPD == UP_CORR && pn < 0.09f && pn > 0.01f) {
+				int lxx = xx[u] + cp->offx, lyy = yy[u] + cp->offy;
+				if(lxx >= lx) lxx -= lx;
+				if(lyy >= ly) lyy -= ly;
+				imx = min(imx, lxx);
+				imy = min(imy, lyy);
+			}
+			sm[6] += -.5f * (dx[u] * dx[u] - dy[u] * dy[u]);
+			sm[7] += -dx[u] * dy[u];
+		}
+	}
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+	for(int o = 16; o > 0; o >>= 1) {
+		const float s2 = __shfl_down_sync(0xffffffffu, area_s, o);
+		const float c2 = __shfl_down_sync(0xffffffffu, area_c, o);
+		add_df(area_s, area_c, s2, c2);
+#pragma unroll
+		for(int i = 1; i < 8; i++) sm[i] += __shfl_down_sync(0xffffffffu, sm[i], o);
+	}
+	CellSum &o = a.csum[ci];
+	if(lane == 0) {
+		o.area[warp] = (double) area_s + (double) area_c;
+#pragma unroll
+		for(int i = 1; i < 8; i++) o.part[warp][i] = sm[i];
+#pragma unroll
+		for(int i = 8; i < 12; i++) o.part[warp][i] = 0.f;
+	}
+	if(UPD == UP_CORR) {
+		__shared__ int ired[2 * (BLOCK / 32)];
+		int im[2] = {imx, imy};
+		block_min<2>(im, ired);
+		imx = im[0];
+		imy = im[1];
+	}
+	if(threadIdx.x == 0) {
+		o.imin[0] = imx;
+		o.imin[1] = imy;
+		o.nw = BLOCK / 32;
+		o.perim = 0.0;
+	}
+}
+
+// The same update with its inputs staged by the Tensor Memory Accelerator:
+// thread 0 moves each chunk of CH sites of every input array into shared
+// memory with one bulk copy per array (cp.async.bulk, completion counted in
+// bytes on the stage's mbarrier), NST chunks ahead of the threads, so the
+// bytes in flight no longer depend on how many loads each thread keeps
+// outstanding.  The copies move 16-byte aligned windows around the chunk
+// (up to 3 floats or 1 double of slack at each end; the engine pads the
+// arrays by 8 elements so a window never leaves its allocation); values in
+// the slack belong to neighbouring sites and are never used.  In the
+// corrector phi^n is read and phi^{n+1} written in place: a site's new
+// value is written only after its chunk has landed, and a window's slack
+// value of a site being written elsewhere is not read.  Every completion
+// wait is bounded (ERR_COPY).
+constexpr long long UPD_WAIT_LIMIT = 1LL << 22;  // mbarrier polls
+
+template<int UPD>
+struct UpdStage {
+	static constexpr int NF = UPD == UP_CORR ? 4 : 3;  // FP32 inputs: mu, d_x phi, d_y phi [, dphi^n]
+};
+
+template<int UPD, int BLOCK, int CH, int NST>
+__global__ void __launch_bounds__(BLOCK) cell_update_bulk(const CellArgs a) {
+	static_assert(CH % BLOCK == 0, "a chunk is a whole number of thread strides");
+	constexpr int NF = UpdStage<UPD>::NF;
+	constexpr int FW = CH + 8, DW = CH + 4;  // window capacities (floats, doubles)
+	constexpr int STAGE = NF * FW * 4 + 3 * DW * 8;
+	static_assert((FW * 4) % 16 == 0 && (DW * 8) % 16 == 0 && STAGE % 16 == 0, "16-byte aligned windows");
+	extern __shared__ __align__(16) unsigned char stage_mem[];
+	__shared__ float2 trow[2 * MAX_TABLE_SIDE];
+	__shared__ __align__(8) uint64_t full[NST];
+	const int ci = blockIdx.x;
+	const CellDev *cp = a.cells + ci;
+	const int lx = cp->lx, ly = cp->ly, n = cp->n;
+	const long long start = cp->start;
+	const int nch = (n + CH - 1) / CH;
+	const double *pin = UPD == UP_PRED ? a.phi_eval : a.phi_old;
+	// chunk c into stage s: the float windows, then vx, vy, phi
+	auto issue = [&](int c, int s) {
+		const long long i0 = start + (long long) c * CH;
+		const int cnt = min(CH, n - c * CH);
+		const long long fa = i0 & ~3LL, fe = (i0 + cnt + 3) & ~3LL;
+		const long long da = i0 & ~1LL, de = (i0 + cnt + 1) & ~1LL;
+		const uint32_t fb = (uint32_t) (fe - fa) * 4u, db = (uint32_t) (de - da) * 8u;
+		unsigned char *base = stage_mem + (size_t) s * STAGE;
+		mbar_expect_tx(&full[s], NF * fb + 3 * db);
+		bulk_g2s(base, a.muf + fa, fb, &full[s]);
+		bulk_g2s(base + FW * 4, a.dxf + fa, fb, &full[s]);
+		bulk_g2s(base + 2 * FW * 4, a.dyf + fa, fb, &full[s]);
+		if(UPD == UP_CORR) bulk_g2s(base + 3 * FW * 4, a.dphif + fa, fb, &full[s]);
+		bulk_g2s(base + NF * FW * 4, a.vxg + da, db, &full[s]);
+		bulk_g2s(base + NF * FW * 4 + DW * 8, a.vyg + da, db, &full[s]);
+		bulk_g2s(base + NF * FW * 4 + 2 * DW * 8, pin + da, db, &full[s]);
+	};
+	if(threadIdx.x == 0) {
+		for(int s = 0; s < NST; s++) mbar_init(&full[s], 1);
+		for(int c = 0; c < min(NST, nch); c++) issue(c, c);
+	}
+	{
+		const int offx = cp->offx, offy = cp->offy, tb = table_base(lx), tby = table_base(ly);
+		for(int i = threadIdx.x; i < lx + ly; i += BLOCK) {
+			int t;
+			if(i < lx) {
+				int j = i + offx;
+				if(j >= lx) j -= lx;
+				t = tb + j;
+			}
+			else {
+				int j = i - lx + offy;
+				if(j >= ly) j -= ly;
+				t = tby + j;
+			}
+			trow[i] = make_float2(a.tab_cosf[t], a.tab_sinf[t]);
+		}
+	}
+	const float J0 = d2f_int(a.P.J0), hdt = .5f * d2f_int(a.P.dt);
+	float *dold = a.dphif + start;
+	double *pout = a.phi_out + start;
+	float sm[8];
+#pragma unroll
+	for(int i = 0; i < 8; i++) sm[i] = 0.f;
+	float area_s = 0.f, area_c = 0.f;
+	int imx = lx, imy = ly;
+	const int sy = BLOCK / lx, sx = BLOCK - sy * lx;
+	int y = (int) threadIdx.x / lx, x = (int) threadIdx.x - y * lx;
+	bool ok = true;
+	__syncthreads();  // barriers initialised, trig rows staged
+	int c_stop = nch;  // first chunk not consumed
+	for(int c = 0; c < nch; c++) {
+		const int s = c % NST;
+		// every thread acquires the stage itself; a timeout anywhere stops all
+		const bool got = mbar_wait(&full[s], (uint32_t) ((c / NST) & 1), UPD_WAIT_LIMIT);
+		if(__syncthreads_or(!got)) {
+			ok = false;
+			c_stop = c;
+			break;
+		}
+		const long long i0 = start + (long long) c * CH;
+		const unsigned char *base = stage_mem + (size_t) s * STAGE;
+		const float *smu = reinterpret_cast<const float *>(base) + (i0 & 3);
+		const float *sdx = smu + FW, *sdy = smu + 2 * FW, *sdp = smu + 3 * FW;
+		const double *svx = reinterpret_cast<const double *>(base + NF * FW * 4) + (i0 & 1);
+		const double *svy = svx + DW, *sph = svx + 2 * DW;
+#pragma unroll
+		for(int u = 0; u < CH / BLOCK; u++) {
+			const int j = (int) threadIdx.x + u * BLOCK, q = c * CH + j;
+			if(q < n) {
+				const float dx = sdx[j], dy = sdy[j];
+				const float dphi = -J0 * smu[j] - d2f_fast(svx[j]) * dx - d2f_fast(svy[j]) * dy;
+				float pn;
+				if(UPD == UP_PRED) {
+					dold[q] = dphi;
+					pn = d2f_fast(sph[j]) + hdt * (dphi + dphi);
+				}
+				else {
+					pn = d2f_fast(sph[j]) + hdt * (dphi + sdp[j]);
+				}
+				pout[q] = f2d_int(pn);
+				acc_square(pn, area_s, area_c);
+				sm[1] += pn;
+				const float2 cx = trow[x], cy = trow[lx + y];
+				sm[2] += pn * cx.x;
+				sm[3] += pn * cx.y;
+				sm[4] += pn * cy.x;
+				sm[5] += pn * cy.y;
+				if(UPD == UP_CORR && pn < 0.09f && pn > 0.01f) {
+					int lxx = x + cp->offx, lyy = y + cp->offy;
+					if(lxx >= lx) lxx -= lx;
+					if(lyy >= ly) lyy -= ly;
+					imx = min(imx, lxx);
+					imy = min(imy, lyy);
+				}
+				sm[6] += -.5f * (dx * dx - dy * dy);
+				sm[7] += -dx * dy;
+			}
+			x += sx;
+			y += sy;
+			if(x >= lx) {
+				x -= lx;
+				y += 1;
+			}
+		}
+		__syncthreads();  // stage s read by every thread: refill it
+		if(threadIdx.x == 0 && c + NST < nch) issue(c + NST, s);
+	}
+	if(!ok) {
+		// a completion wait ran out: report, then let the copies still in
+		// flight land (bounded) before the shared memory is released
+		if(threadIdx.x == 0) {
+			atomicOr(&a.st->err, ERR_COPY);
+			a.st->err_where = ci;
+			for(int c = c_stop; c < min(nch, c_stop + NST); c++)
+				mbar_wait(&full[c % NST], (uint32_t) ((c / NST) & 1), UPD_WAIT_LIMIT);
+		}
+		return;
+	}
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+	for(int o = 16; o > 0; o >>= 1) {
+		const float s2 = __shfl_down_sync(0xffffffffu, area_s, o);
+		const float c2 = __shfl_down_sync(0xffffffffu, area_c, o);
+		add_df(area_s, area_c, s2, c2);
+#pragma unroll
+		for(int i = 1; i < 8; i++) sm[i] += __shfl_down_sync(0xffffffffu, sm[i], o);
+	}
+	CellSum &o = a.csum[ci];
+	if(lane == 0) {
+		o.area[warp] = (double) area_s + (double) area_c;
+#pragma unroll
+		for(int i = 1; i < 8; i++) o.part[warp][i] = sm[i];
+#pragma unroll
+		for(int i = 8; i < 12; i++) o.part[warp][i] = 0.f;
+	}
+	if(UPD == UP_CORR) {
+		__shared__ int ired[2 * (BLOCK / 32)];
+		int im[2] = {imx, imy};
+		block_min<2>(im, ired);
+		imx = im[0];
+		imy = im[1];
+	}
+	if(threadIdx.x == 0) {
+		o.imin[0] = imx;
+		o.imin[1] = imy;
+		o.nw = BLOCK / 32;
+		o.perim = 0.0;
+	}
+}
+
+constexpr int UPD_BULK_BLOCK = 128, UPD_BULK_CH = 512, UPD_BULK_NST = 2;
+
+template<int UPD>
+constexpr size_t upd_bulk_smem() {
+	return (size_t) UPD_BULK_NST *
+	       (UpdStage<UPD>::NF * (UPD_BULK_CH + 8) * 4 + 3 * (UPD_BULK_CH + 4) * 8);
+}
+
+template<int BLOCK>
+static void launch_update_f32_b(int upd, const CellArgs &a, cudaStream_t s) {
+	// the bulk-copy form needs 16-byte aligned array bases (engine allocations are)
+	const bool aligned = ((reinterpret_cast<uintptr_t>(a.muf) | reinterpret_cast<uintptr_t>(a.dxf) |
+	                       reinterpret_cast<uintptr_t>(a.dyf) | reinterpret_cast<uintptr_t>(a.dphif) |
+	                       reinterpret_cast<uintptr_t>(a.vxg) | reinterpret_cast<uintptr_t>(a.vyg) |
+	                       reinterpret_cast<uintptr_t>(upd == UP_PRED ? a.phi_eval : a.phi_old)) & 15u) == 0;
+	if(aligned) {
+		constexpr int B = UPD_BULK_BLOCK, CH = UPD_BULK_CH, NST = UPD_BULK_NST;
+		if(upd == UP_PRED) cell_update_bulk<UP_PRED, B, CH, NST><<<a.N, B, upd_bulk_smem<UP_PRED>(), s>>>(a);
+		else cell_update_bulk<UP_CORR, B, CH, NST><<<a.N, B, upd_bulk_smem<UP_CORR>(), s>>>(a);
+		return;
+	}
+	if(upd == UP_PRED) cell_update_f32<UP_PRED, BLOCK><<<a.N, BLOCK, 0, s>>>(a);
+	else cell_update_f32<UP_CORR, BLOCK><<<a.N, BLOCK, 0, s>>>(a);
+}
+
 // (eval, upd) pairs with an FP32 kernel, for every model and tile
 #define RC_F32_MODES(X)      \
 	X(EV_LOCAL, UP_PRED)     \
@@ -469,6 +823,13 @@ static bool launch_f32_m(int eval, int upd, const CellArgs &a, cudaStream_t s, i
 }
 
 bool launch_cell_kernel_f32(int model, int eval, int upd, const CellArgs &a, cudaStream_t s, int block) {
+	if((model == M_POLAR || model == M_WET) && eval == EV_NONE && upd != UP_NONE && a.split && !a.P.conserved) {
+		if(a.N <= 0) return true;
+		if(block == 128) launch_update_f32_b<128>(upd, a, s);
+		else if(block == 512) launch_update_f32_b<512>(upd, a, s);
+		else launch_update_f32_b<256>(upd, a, s);
+		return true;
+	}
 	if(model == M_POLAR) {
 		if(a.N <= 0) return true;
 		return launch_f32_m<M_POLAR>(eval, upd, a, s, block);

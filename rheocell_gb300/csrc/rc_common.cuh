@@ -40,6 +40,7 @@ enum ErrBits {
 	ERR_TYPE = 32,      // activenematic type other than 0/1
 	ERR_MMA = 64,       // a tensor-core completion wait timed out
 	ERR_NOCONV = 128,   // a viscous solve stopped at its iteration cap above the tolerance
+	ERR_COPY = 256,     // a bulk-copy completion wait timed out
 };
 
 // Phase-dependent parameters (see rc_params in the C header).
@@ -206,6 +207,22 @@ __device__ __forceinline__ float d2f_int(double v) {
 	bits += m;
 	if(r > 0x10000000u || (r == 0x10000000u && (m & 1u))) bits += 1u;  // carries into the exponent
 	return __uint_as_float(bits);
+}
+
+// The short form for streams: one funnel shift takes the low 9 exponent bits
+// and the top 23 mantissa bits together, a subtraction of 384 << 23 rebiases
+// the exponent modulo 2^9 (exact for every FP32 normal), and the first
+// dropped bit is added (round to nearest, ties away from zero: differs from
+// d2f_int on exact ties only).  Below the FP32 normal range -> signed zero;
+// beyond the FP32 range, infinities and NaN -> NaN, so a non-finite input
+// stays non-finite.
+__device__ __forceinline__ float d2f_fast(double v) {
+	const unsigned hi = (unsigned) __double2hiint(v), lo = (unsigned) __double2loint(v);
+	const unsigned mag = hi & 0x7FFFFFFFu, sign = hi ^ mag;
+	unsigned b = __funnelshift_l(lo, hi, 3) - (384u << 23) + ((lo >> 28) & 1u);
+	b = mag < (897u << 20) ? 0u : b;
+	b = mag >= (1151u << 20) ? 0x7FC00000u : b;
+	return __uint_as_float(b | sign);
 }
 
 __device__ __forceinline__ double f2d_int(float v) {

@@ -41,6 +41,8 @@ using namespace rc;
 
 // From this many cells on, the per-cell epilogue runs as its own kernel with
 // one thread per cell (its FP64 code then shares instructions across cells).
+// FP32 engines with a viscous solve always run it: their update-only kernel
+// (cell_update_f32) writes per-warp partial sums only.
 constexpr int SPLIT_FINISH_CELLS = 256;
 
 struct rc_engine {
@@ -158,14 +160,17 @@ struct StageMark {
 	rc_engine *e;
 	rc_engine::Mark m;
 	StageMark(rc_engine *e_, int stage) : e(e_) {
-		if(!e->timing) return;
+		if(!e->timing || stage < 0) {
+			m.a = nullptr;
+			return;
+		}
 		m.stage = stage;
 		m.a = get_event(e);
 		m.b = get_event(e);
 		cudaEventRecord(m.a, e->stream);
 	}
 	~StageMark() {
-		if(!e->timing) return;
+		if(!e->timing || !m.a) return;
 		cudaEventRecord(m.b, e->stream);
 		e->marks.push_back(m);
 	}
@@ -232,6 +237,7 @@ static CellArgs cell_args(rc_engine *e) {
 	a.muf = e->muf;
 	a.dxf = e->dxf;
 	a.dyf = e->dyf;
+	a.dphif = reinterpret_cast<float *>(e->dphi_old);  // FP32 engines keep dphi^n in FP32
 	a.vxg = e->vx;
 	a.vyg = e->vy;
 	a.fxg = e->fx;
@@ -260,16 +266,21 @@ static CellArgs cell_args(rc_engine *e) {
 
 // Cell kernel launch: the FP32 variant where the engine runs
 // RC_PRECISION_FLOAT (polar and wet nematic models), else FP64; in split
-// mode (many cells) followed by the per-cell epilogue kernel.  Returns the
-// number of kernels launched.
-static int cell_launch(rc_engine *e, int eval, int upd, const CellArgs &a0, cudaStream_t s) {
+// mode (many cells) followed by the per-cell epilogue kernel.  With a stage
+// (RC_TIMER_*), the cell kernel alone is timed under it and the epilogue
+// under RC_TIMER_EPILOGUE.  Returns the number of kernels launched.
+static int cell_launch(rc_engine *e, int eval, int upd, const CellArgs &a0, cudaStream_t s, int stage = -1) {
 	CellArgs a = a0;
 	a.split = e->csum != nullptr;
 	a.csum = e->csum;
-	const bool f32 =
-	    e->hp.precision == RC_PRECISION_FLOAT && launch_cell_kernel_f32(e->P.model, eval, upd, a, s, e->f32_block);
-	if(!f32) launch_cell_kernel(e->P.model, eval, upd, a, s);
+	bool f32;
+	{
+		StageMark sm(e, stage);
+		f32 = e->hp.precision == RC_PRECISION_FLOAT && launch_cell_kernel_f32(e->P.model, eval, upd, a, s, e->f32_block);
+		if(!f32) launch_cell_kernel(e->P.model, eval, upd, a, s);
+	}
 	if(!a.split) return 1;
+	StageMark sm(e, stage >= 0 ? RC_TIMER_EPILOGUE : -1);
 	launch_cell_finish(e->P.model, eval, upd, f32, a, s);
 	return 2;
 }
@@ -437,10 +448,7 @@ static void evaluate_end(rc_engine *e, const double *phi, int phase) {
 		a.phi_eval = phi;
 		a.pe = e->ph[phase];
 		a.pu = e->ph[phase];
-		{
-			StageMark sm(e, RC_TIMER_FORCES);
-			e->launches += cell_launch(e, EV_WET_RHS, UP_NONE, a, e->stream) - 1;
-		}
+		e->launches += cell_launch(e, EV_WET_RHS, UP_NONE, a, e->stream, RC_TIMER_FORCES) - 1;
 		e->launches += 1;
 		solve(e, phase);
 		e->pending = false;
@@ -463,16 +471,13 @@ static void one_step(rc_engine *e) {
 	a.phi_eval = e->phiA;
 	a.phi_out = e->phiB;
 	a.pu = e->ph[cur];
-	{
-		StageMark sm(e, RC_TIMER_UPDATE);
-		if(e->pending) {
-			a.pe = e->ph[e->eval_phase];
-			e->launches += cell_launch(e, EV_LOCAL, UP_PRED, a, s) - 1;
-		}
-		else {
-			a.pe = e->ph[cur];
-			e->launches += cell_launch(e, EV_NONE, UP_PRED, a, s) - 1;
-		}
+	if(e->pending) {
+		a.pe = e->ph[e->eval_phase];
+		e->launches += cell_launch(e, EV_LOCAL, UP_PRED, a, s, RC_TIMER_UPDATE) - 1;
+	}
+	else {
+		a.pe = e->ph[cur];
+		e->launches += cell_launch(e, EV_NONE, UP_PRED, a, s, RC_TIMER_UPDATE) - 1;
 	}
 	e->launches += 1;
 	gather(e, e->phiB, cur);
@@ -484,8 +489,7 @@ static void one_step(rc_engine *e) {
 	c.pu = e->ph[cur];
 	if(!wet_phase(e, cur)) {
 		c.phi_eval = e->phiB;
-		StageMark sm(e, RC_TIMER_UPDATE);
-		e->launches += cell_launch(e, EV_LOCAL, UP_CORR, c, s) - 1;
+		e->launches += cell_launch(e, EV_LOCAL, UP_CORR, c, s, RC_TIMER_UPDATE) - 1;
 		e->launches += 1;
 	}
 	else {
@@ -493,16 +497,10 @@ static void one_step(rc_engine *e) {
 		f.phi_eval = e->phiB;
 		f.pe = e->ph[cur];
 		f.pu = e->ph[cur];
-		{
-			StageMark sm(e, RC_TIMER_FORCES);
-			e->launches += cell_launch(e, EV_WET_RHS, UP_NONE, f, s) - 1;
-		}
+		e->launches += cell_launch(e, EV_WET_RHS, UP_NONE, f, s, RC_TIMER_FORCES) - 1;
 		solve(e, cur);
 		c.phi_eval = e->phiB;
-		{
-			StageMark sm(e, RC_TIMER_UPDATE);
-			e->launches += cell_launch(e, EV_NONE, UP_CORR, c, s) - 1;
-		}
+		e->launches += cell_launch(e, EV_NONE, UP_CORR, c, s, RC_TIMER_UPDATE) - 1;
 		e->launches += 2;
 	}
 	CellArgs r = cell_args(e);
@@ -641,6 +639,7 @@ static int check_status(rc_engine *e, rc_step_stats *stats) {
 		if(h.err & ERR_BARRIER) return set_err(e, RC_ERR_CG, "viscous solve: grid barrier timed out");
 		if(h.err & ERR_TYPE) return set_err(e, RC_ERR_INVALID, "Too many field types (cell %d)", h.err_where);
 		if(h.err & ERR_MMA) return set_err(e, RC_ERR_CG, "viscous solve: tensor-core completion wait timed out");
+		if(h.err & ERR_COPY) return set_err(e, RC_ERR_CUDA, "cell update: bulk-copy completion wait timed out (cell %d)", h.err_where);
 		if(h.err & ERR_NOCONV)
 			return set_err(e, RC_ERR_CG, "viscous solve: tolerance not reached within the iteration cap (%lld)",
 			               e->cg_max_iters);
@@ -921,11 +920,14 @@ static int create_engine(const rc_params *params, int n_layers, const rc_box *bo
 	e->nby = layers[0].nby;
 	const size_t L2 = (size_t) total_box;  // box arrays of all layers (one layer for the wet paths)
 	const size_t cap = (size_t) e->S_cap;
+	// the update's per-site inputs are read through 16-byte aligned windows
+	// (bulk copies) that may reach up to 8 bytes past the last site
+	const size_t capw = cap + 8;
 	const bool wet = (P.model == M_POLAR || P.model == M_WET);
 	if((rc = dalloc(e, &e->cells, (size_t) std::max(n_cells, 1))) ||
-	   (rc = dalloc(e, &e->phiA, cap)) || (rc = dalloc(e, &e->phiB, cap)) || (rc = dalloc(e, &e->dphi_old, cap)) ||
+	   (rc = dalloc(e, &e->phiA, capw)) || (rc = dalloc(e, &e->phiB, capw)) || (rc = dalloc(e, &e->dphi_old, capw)) ||
 	   (rc = dalloc(e, &e->mu, cap)) || (rc = dalloc(e, &e->dxg, cap)) || (rc = dalloc(e, &e->dyg, cap)) ||
-	   (rc = dalloc(e, &e->vx, cap)) || (rc = dalloc(e, &e->vy, cap)) || (rc = dalloc(e, &e->mapg, cap)) ||
+	   (rc = dalloc(e, &e->vx, capw)) || (rc = dalloc(e, &e->vy, capw)) || (rc = dalloc(e, &e->mapg, cap)) ||
 	   (rc = dalloc(e, &e->phi2, L2)) || (rc = dalloc(e, &e->sq00, L2)) || (rc = dalloc(e, &e->sq01, L2)) ||
 	   (rc = dalloc(e, &e->cnt, L2)) ||
 	   (rc = dalloc(e, &e->bin_count, (size_t) total_bins)) || (rc = dalloc(e, &e->bin_layer, (size_t) total_bins)) ||
@@ -934,14 +936,15 @@ static int create_engine(const rc_params *params, int n_layers, const rc_box *bo
 	   (rc = dalloc(e, &e->tab_cos, (size_t) table_base(MAX_TABLE_SIDE + 1))) ||
 	   (rc = dalloc(e, &e->tab_sin, (size_t) table_base(MAX_TABLE_SIDE + 1))) ||
 	   (rc = dalloc(e, &e->tab_cosf, (size_t) table_base(MAX_TABLE_SIDE + 1))) ||
-	   (n_cells >= SPLIT_FINISH_CELLS && (rc = dalloc(e, &e->csum, (size_t) n_cells))) ||
+	   ((n_cells >= SPLIT_FINISH_CELLS || (any_wet && params->precision == RC_PRECISION_FLOAT)) &&
+	    (rc = dalloc(e, &e->csum, (size_t) std::max(n_cells, 1)))) ||
 	   (rc = dalloc(e, &e->tab_sinf, (size_t) table_base(MAX_TABLE_SIDE + 1))) ||
 	   (rc = dalloc(e, &e->st, 1)) || (rc = dalloc(e, &e->st_save, 1)) ||
 	   (rc = dalloc(e, &e->scratch_phi, cap + (size_t) n_cells / 2 + 8)) ||
 	   (rc = dalloc(e, &e->rep, e->rep_on ? cap : 1)) || (rc = dalloc(e, &e->scratch_rep, e->rep_on ? cap : 1)))
 		return bail(rc);
 	if(params->precision == RC_PRECISION_FLOAT &&
-	   ((rc = dalloc(e, &e->muf, cap)) || (rc = dalloc(e, &e->dxf, cap)) || (rc = dalloc(e, &e->dyf, cap))))
+	   ((rc = dalloc(e, &e->muf, capw)) || (rc = dalloc(e, &e->dxf, capw)) || (rc = dalloc(e, &e->dyf, capw))))
 		return bail(rc);
 	if(has_walls) {
 		// the boxes' wall values (layers without walls stay zero)

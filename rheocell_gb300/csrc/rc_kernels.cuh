@@ -37,6 +37,7 @@ struct CellArgs {
 	// FP32 engines: the force evaluation's mu and gradients in FP32 (they feed
 	// only the FP32 update; downloads and observables widen them into mu, dxg, dyg)
 	float *muf, *dxf, *dyf;
+	float *dphif;  // FP32 kernels: dphi^n in FP32, in the dphi_old buffer
 	int *mapg;
 	double *rep;
 	const double *phi2, *sq00, *sq01;

@@ -82,6 +82,21 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity, long 
 	return false;
 }
 
+// One arrival that also announces `bytes` of asynchronous transfers the
+// current phase waits for.
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *mbar, uint32_t bytes) {
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes) : "memory");
+}
+
+// Bulk (untiled TMA) global -> shared copy completing on an mbarrier: both
+// addresses 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void *smem_dst, const void *gmem_src, uint32_t bytes, uint64_t *mbar) {
+	asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+	                 smem_u32(smem_dst)),
+	             "l"(gmem_src), "r"(bytes), "r"(smem_u32(mbar))
+	             : "memory");
+}
+
 // 16-byte asynchronous global -> shared copy; src_bytes = 0 writes zeros.
 __device__ __forceinline__ void cp_async16(void *smem_dst, const void *gmem_src, uint32_t src_bytes) {
 	asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(smem_dst)), "l"(gmem_src), "r"(src_bytes)
