@@ -318,9 +318,13 @@ def velocity_error(eng, tol=1e-8, tight=1e-12):
 
     def err(a, b):
         return float((a - b).abs().max() / b.abs().max().clamp_min(1e-300))
+    def err2(a, b):
+        return float((a - b).norm() / b.norm().clamp_min(1e-300))
     learned = [err(v[2 + c], v[4 + c]) for c in range(2)]
     plain = [err(v[c], v[4 + c]) for c in range(2)]
     return {"vx": learned[0], "vy": learned[1], "max": max(learned),
+            "norm": "max |v - v_oracle| / max |v_oracle| per component",
+            "l2_max": max(err2(v[2 + c], v[4 + c]) for c in range(2)),
             "plain_fp64_max": max(plain),
             "learned_vs_plain_max": max(err(v[2 + c], v[c]) for c in range(2)),
             "how": "same right-hand side (last evaluation of the timed run), cold-start solves of all %d unknowns; "
