@@ -226,7 +226,8 @@ def prepare_learned(args, eng, lib):
     import numpy as np
     if args.load_params:
         # parameters of an earlier training (set-up shortcut for experiments)
-        eng.set_params(np.loadtxt(args.load_params))
+        lp = args.load_params
+        eng.set_params(np.load(lp).astype(np.float64) if lp.endswith(".npy") else np.loadtxt(lp))
         harvest_s, n, rep = 0.0, 0, {"loaded_from": os.path.basename(args.load_params)}
     else:
         own = not args.train_workload or args.train_workload == args.workload

@@ -189,3 +189,38 @@ def test_learned_solve_on_large_boxes(trained, L):
     want = o.state()
     for k in ("vx", "vy", "phi", "area", "com_x"):
         assert rel_err(got[k], want[k]) < 1e-7, k
+
+
+def test_committed_network_on_the_training_monolayer():
+    """tests/golden/unet_wet256.npy holds the network the default bench line
+    trains (tests/golden/make_unet_params.py).  On the monolayer it was
+    trained on (wet 256^2, 400 cells, FP32 site arithmetic) the learned solve
+    of one right-hand side needs under a fifth of the Jacobi flexible CG's
+    inner iterations, converges to the learned solve's residual margin (0.2 of
+    the tolerance), and its velocities are within 1e-7 (max norm, relative to
+    the largest velocity) of the FP64 CG solved to 1e-12."""
+    import os
+    import torch
+    import bench
+    params = np.load(os.path.join(os.path.dirname(__file__), "golden", "unet_wet256.npy")).astype(np.float64)
+    e = bench.make_engine("wet256", abi.RC_PRECISION_FLOAT, 0)
+    e.set_params(params)
+    e.set_solver(abi.RC_SOLVER_LEARNED)
+    e.step(5)
+    S = e.site_count()
+    v = [torch.zeros(S, dtype=torch.float64, device="cuda") for _ in range(6)]
+    torch.cuda.synchronize()
+    e.set_cg_tolerance(1e-12)
+    e.resolve(abi.RC_SOLVER_PLAIN_FP64, v[4].data_ptr(), v[5].data_ptr())
+    e.set_cg_tolerance(1e-8)
+    sj = e.resolve(abi.RC_SOLVER_PLAIN, v[0].data_ptr(), v[1].data_ptr())
+    sl = e.resolve(abi.RC_SOLVER_LEARNED, v[2].data_ptr(), v[3].data_ptr())
+    print("Jacobi FCG %d it, learned %d inner it, residual %.2e" % (sj.cg_iterations, sl.cg_iterations,
+                                                                    sl.cg_max_rel_residual))
+    assert sl.fallbacks == 0
+    assert sl.cg_iterations * 5 < sj.cg_iterations
+    assert sl.cg_max_rel_residual < 0.2 * 1e-8
+    for c in range(2):
+        err = float((v[2 + c] - v[4 + c]).abs().max() / v[4 + c].abs().max())
+        assert err < 1e-7, err
+    e.close()
