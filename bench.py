@@ -353,7 +353,15 @@ def run_gb300(args, rank, world):
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     w = workload(args.workload)
-    members = make_case(w)
+    members = all_members = make_case(w)
+    sharded = world > 1 and len(members) > 1
+    if sharded:
+        # an ensemble is split into contiguous blocks of members, one per
+        # rank (no data-path collective); a single monolayer runs as replicas
+        from rheocell_gb300 import replicas
+        members = replicas.shard(members, rank, world)
+        if not members:
+            raise SystemExit("more ranks (%d) than ensemble members (%d)" % (world, len(all_members)))
     prec = {"double": abi.RC_PRECISION_DOUBLE, "mixed": abi.RC_PRECISION_MIXED,
             "float": abi.RC_PRECISION_FLOAT}[args.precision]
     built = [host.engine_inputs(keys, m, precision=prec) for keys, m in members]
@@ -419,11 +427,11 @@ def run_gb300(args, rank, world):
     tn = (C.c_longlong * abi.NUM_TIMERS)()
     lib.rc_timers(eng.h, tms, tn, 1)
     lib.rc_set_timing(eng.h, 0)
+    # max over ranks of the timed region, sum over ranks of the sites updated
+    from rheocell_gb300 import replicas
+    ms, total_sites = replicas.reduce_timing(ms, float(S * args.steps))
     if world > 1:
         import torch.distributed as dist
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
         dist.barrier()
 
     # end-to-end through the C ABI with host buffers
@@ -440,8 +448,8 @@ def run_gb300(args, rank, world):
     e2e_s = time.perf_counter() - t0
     S_after = eng.site_count()
     eng.close()
+    e2e_ms, e2e_sites = replicas.reduce_timing(e2e_s * 1e3, float(S * e2e_steps))
 
-    total_sites = S * args.steps * world
     value = total_sites / (ms / 1e3)
     names = abi.TIMER_NAMES
     stage = {names[i]: {"ms": round(tms[i], 3), "launches": int(tn[i])} for i in range(abi.NUM_TIMERS) if tn[i]}
@@ -484,12 +492,12 @@ def run_gb300(args, rank, world):
         "ms_per_step": ms / args.steps,
         "steps_per_s": args.steps / (ms / 1e3),
         "higher_is_better": True,
-        "scaling": "weak",
+        "scaling": "strong" if sharded else "weak",
         "vs_baseline": None,
         "dtype": {"double": "f64", "mixed": "f64 fields, f32 solve inner iterations",
                   "float": "f32 site arithmetic, f64 field storage and cell-area integrals"}[args.precision],
         "data": "synthetic (seeded jittered lattice, tanh interfaces)",
-        "config": dict(arm_config(args, w, members), parallelism="replicas" if world > 1 else "single GPU",
+        "config": dict(arm_config(args, w, all_members), parallelism=("ensemble sharded by member" if sharded else "replicas") if world > 1 else "single GPU",
                        l2="flushed (256 MiB write) before every timed step"),
         "cg": {"solves": st.cg_solves, "iterations": st.cg_iterations, "max_iterations": st.cg_max_iterations,
                "max_rel_residual": st.cg_max_rel_residual,
@@ -498,7 +506,7 @@ def run_gb300(args, rank, world):
         "stages_note": "per-stage CUDA-event totals over %d further steps (direct launches)" % prof_steps,
         "gpu_launches": int(st.kernel_launches),
         "clocks": clk,
-        "e2e": {"value": S * e2e_steps / e2e_s * world, "unit": "site-updates/s",
+        "e2e": {"value": e2e_sites / (e2e_ms / 1e3), "unit": "site-updates/s",
                 "h2d_bytes_per_step": 8 * S, "d2h_bytes_per_step": 8 * S,
                 "how": "rc_upload_phi (pinned) + rc_step(1) + rc_download_phi (pinned), wall clock, %d steps" % e2e_steps},
         "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -754,7 +762,11 @@ def main():
         out = run_reference(args, rank, world)
     else:
         from rheocell_gb300 import build
-        build.build()
+        if rank == 0:
+            build.build()  # in-tree; the other ranks wait for it
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
         out = run_gb300(args, rank, world)
     if rank == 0 and out is not None:
         print(json.dumps(out), flush=True)

@@ -517,6 +517,21 @@ int rc_test_barrier_timeout(rc_engine *e, long long spin_limit, int unreachable)
 int rc_solver_profile(rc_engine *e, int enable, double *ms, int n);
 
 /*
+ * Self-test of the engine's double <-> float conversions on the integer
+ * pipes (the FP32 cell kernels use them in place of the conversion
+ * instructions, which issue on the narrow FP64 pipe of GB300).  On device
+ * `device`, converts the n doubles of `in` (host array) by the exact form
+ * (round to nearest even; below the FP32 normal range to signed zero) into
+ * `exact`, by the short streaming form (round to nearest, ties away; below
+ * the normal range to signed zero; beyond the FP32 range, infinities and NaN
+ * to NaN) into `fast`, and by CUDA's __double2float_rn into `cuda_rn`, and
+ * widens cuda_rn back to double by the integer form into `widened` (host
+ * arrays of n).  No counterpart in the reference.
+ */
+int rc_selftest_conversions(const double *in, float *exact, float *fast, float *cuda_rn, double *widened, long long n,
+                            int device);
+
+/*
  * Diagnostic observables computed on the device from the current state.
  *
  * rc_observe_field: the box fields of the reference's field observables --

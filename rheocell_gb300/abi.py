@@ -230,6 +230,9 @@ def declare(lib: C.CDLL, prefix: str) -> C.CDLL:
         lib.rc_set_timing.restype = C.c_int
         lib.rc_timers.argtypes = [vp, DP, C.POINTER(C.c_longlong), C.c_int]
         lib.rc_timers.restype = C.c_int
+        FP = C.POINTER(C.c_float)
+        lib.rc_selftest_conversions.argtypes = [DP, FP, FP, FP, DP, C.c_longlong, C.c_int]
+        lib.rc_selftest_conversions.restype = C.c_int
     else:
         lib.orc_rng_state.argtypes = [vp]
         lib.orc_rng_state.restype = C.c_ulonglong
@@ -243,7 +246,8 @@ EXPORTED = ["rc_abi_version", "rc_create", "rc_create_generated", "rc_batch_crea
             "rc_set_cg_limits", "rc_set_cg_tolerance", "rc_test_barrier_timeout",
             "rc_observe_field", "rc_observe_stress", "rc_observe_cells", "rc_autotune", "rc_set_cell_threads", "rc_step", "rc_step_async", "rc_wait", "rc_set_phase",
             "rc_get_sizes", "rc_download", "rc_upload", "rc_download_phi", "rc_upload_phi", "rc_set_stream",
-            "rc_set_timing", "rc_timers", "rc_site_count", "rc_last_error", "rc_destroy"]
+            "rc_set_timing", "rc_timers", "rc_site_count", "rc_last_error", "rc_destroy",
+            "rc_selftest_conversions"]
 
 TIMER_NAMES = ["update", "gather", "forces", "solve", "repack", "rng", "epilogue"]
 NUM_TIMERS = len(TIMER_NAMES)

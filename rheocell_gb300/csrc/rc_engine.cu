@@ -2039,6 +2039,56 @@ int rc_viscous_resolve_noalloc(rc_engine *e, double *vx, double *vy, long long n
 	return RC_OK;
 }
 
+}  // extern "C"
+
+namespace rc {
+__global__ void conversion_selftest_kernel(const double *in, float *exact, float *fast, float *cuda_rn, double *widened,
+                                           long long n) {
+	for(long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < n; i += (long long) gridDim.x * blockDim.x) {
+		const double v = in[i];
+		exact[i] = d2f_int(v);
+		fast[i] = d2f_fast(v);
+		const float r = __double2float_rn(v);
+		cuda_rn[i] = r;
+		widened[i] = f2d_int(r);
+	}
+}
+}  // namespace rc
+
+extern "C" {
+
+int rc_selftest_conversions(const double *in, float *exact, float *fast, float *cuda_rn, double *widened, long long n,
+                            int device) {
+	if(!in || !exact || !fast || !cuda_rn || !widened || n <= 0)
+		return set_err(nullptr, RC_ERR_INVALID, "rc_selftest_conversions: invalid arguments");
+	if(cudaSetDevice(device) != cudaSuccess) return set_err(nullptr, RC_ERR_CUDA, "rc_selftest_conversions: no device %d", device);
+	double *din = nullptr, *dw = nullptr;
+	float *de = nullptr, *df = nullptr, *dc = nullptr;
+	const size_t nd = sizeof(double) * (size_t) n, nf = sizeof(float) * (size_t) n;
+	cudaError_t c = cudaMalloc(&din, nd);
+	if(c == cudaSuccess) c = cudaMalloc(&dw, nd);
+	if(c == cudaSuccess) c = cudaMalloc(&de, nf);
+	if(c == cudaSuccess) c = cudaMalloc(&df, nf);
+	if(c == cudaSuccess) c = cudaMalloc(&dc, nf);
+	if(c == cudaSuccess) c = cudaMemcpy(din, in, nd, cudaMemcpyHostToDevice);
+	if(c == cudaSuccess) {
+		const long long blocks = std::min<long long>((n + 255) / 256, 4096);
+		conversion_selftest_kernel<<<(unsigned) blocks, 256>>>(din, de, df, dc, dw, n);
+		c = cudaGetLastError();
+	}
+	if(c == cudaSuccess) c = cudaMemcpy(exact, de, nf, cudaMemcpyDeviceToHost);
+	if(c == cudaSuccess) c = cudaMemcpy(fast, df, nf, cudaMemcpyDeviceToHost);
+	if(c == cudaSuccess) c = cudaMemcpy(cuda_rn, dc, nf, cudaMemcpyDeviceToHost);
+	if(c == cudaSuccess) c = cudaMemcpy(widened, dw, nd, cudaMemcpyDeviceToHost);
+	cudaFree(din);
+	cudaFree(dw);
+	cudaFree(de);
+	cudaFree(df);
+	cudaFree(dc);
+	if(c != cudaSuccess) return set_err(nullptr, RC_ERR_CUDA, "rc_selftest_conversions: %s", cudaGetErrorString(c));
+	return RC_OK;
+}
+
 void rc_destroy(rc_engine *e) {
 	if(!e) return;
 	cudaSetDevice(e->device);
