@@ -245,49 +245,9 @@ __global__ void __launch_bounds__(BLOCK) cell_kernel_f32(const CellArgs a) {
 			imin[1] = min(imin[1], lyy);
 		}
 	};
-	if(EVAL == EV_NONE && UPD != UP_NONE && !conserved) {
-		// Update only (the wet models' predictor and corrector): every input
-		// is a stream from global memory, so the loads of UB sites are issued
-		// together ahead of their arithmetic (streaming loads: each value is
-		// read once; phi_old may be the array being written, site by site).
-		constexpr int UB = 2;
-		PatchWalk w(lx);
-		while(w.q < n) {
-			int qq[UB], xx[UB], yy[UB];
-#pragma unroll
-			for(int u = 0; u < UB; u++) {
-				qq[u] = w.q;
-				xx[u] = w.x;
-				yy[u] = w.y;
-				w.next();
-			}
-			float gm[UB], gdx[UB], gdy[UB];
-			double gvx[UB], gvy[UB], gp[UB];
-			float gd[UB];
-#pragma unroll
-			for(int u = 0; u < UB; u++) {
-				const long long i = start + (qq[u] < n ? qq[u] : 0);
-				gm[u] = __ldcs(&a.muf[i]);
-				gvx[u] = __ldcs(&a.vxg[i]);
-				gvy[u] = __ldcs(&a.vyg[i]);
-				gdx[u] = __ldcs(&a.dxf[i]);
-				gdy[u] = __ldcs(&a.dyf[i]);
-				gp[u] = __ldcs(UPD == UP_PRED ? &a.phi_eval[i] : &a.phi_old[i]);
-				gd[u] = UPD == UP_CORR ? __ldcs(&a.dphif[i]) : 0.f;
-			}
-#pragma unroll
-			for(int u = 0; u < UB; u++) {
-				if(qq[u] >= n) break;
-				const float dx = gdx[u], dy = gdy[u];
-				const float dphi = -J0 * gm[u] - d2f_int(gvx[u]) * dx - d2f_int(gvy[u]) * dy;
-				update_site(qq[u], xx[u], yy[u], dphi, d2f_int(gp[u]), gd[u]);
-				af[6] += -.5f * (dx * dx - dy * dy);
-				af[7] += -dx * dy;
-			}
-		}
-	}
 	// Stage 2: forces (calc_internal_forces) and the update (first_step).
-	if(EVAL != EV_NONE || UPD == UP_NONE || conserved)
+	// (The wet models' update alone after the solve is cell_update_bulk
+	// below; this kernel runs it only for conserved dynamics.)
 	for(PatchWalk w(lx); w.q < n; w.next()) {
 		const int q = w.q, x = w.x, y = w.y;
 		float mu = 0.f, vx = 0.f, vy = 0.f, dx, dy, phi_e = 0.f;
@@ -445,144 +405,9 @@ __global__ void __launch_bounds__(BLOCK) cell_kernel_f32(const CellArgs a) {
 // FD_CPUBackend.cpp:44-120): dphi = -J0 mu - v . grad phi from the last
 // evaluation's mu and gradient, phi* = phi + dt dphi (predictor) or
 // phi^{n+1} = phi^n + dt/2 (dphi + dphi^n) (corrector), and the per-cell
-// sums of the new phi.  A pure stream over the patch: no per-cell set-up
-// beyond the patch's trig rows, staged in shared memory already rotated by
-// the patch offset (one 8-byte shared load per axis and site, no wrap); the
-// loads of UB sites are issued together at fixed offsets from one address;
-// the double -> float conversions are the short integer form (d2f_fast).
-// Per-warp partial sums go to the epilogue kernel (cell_finish_kernel),
-// which the engine runs after every FP32 wet update.
-template<int UPD, int BLOCK>
-__global__ void __launch_bounds__(BLOCK) cell_update_f32(const CellArgs a) {
-	constexpr int UB = 2;
-	__shared__ float2 trow[2 * MAX_TABLE_SIDE];  // (cos, sin): patch columns, then rows at trow + lx
-	const int ci = blockIdx.x;
-	const CellDev *cp = a.cells + ci;
-	const int lx = cp->lx, ly = cp->ly, n = cp->n;
-	const long long start = cp->start;
-	{
-		const int offx = cp->offx, offy = cp->offy, tb = table_base(lx), tby = table_base(ly);
-		for(int i = threadIdx.x; i < lx + ly; i += BLOCK) {
-			int t;
-			if(i < lx) {
-				int j = i + offx;
-				if(j >= lx) j -= lx;
-				t = tb + j;
-			}
-			else {
-				int j = i - lx + offy;
-				if(j >= ly) j -= ly;
-				t = tby + j;
-			}
-			trow[i] = make_float2(a.tab_cosf[t], a.tab_sinf[t]);
-		}
-	}
-	const float J0 = d2f_int(a.P.J0), hdt = .5f * d2f_int(a.P.dt);
-	const float *mu = a.muf + start, *gx = a.dxf + start, *gy = a.dyf + start;
-	const double *ux = a.vxg + start, *uy = a.vyg + start;
-	const double *pin = (UPD == UP_PRED ? a.phi_eval : a.phi_old) + start;
-	float *dold = a.dphif + start;
-	double *pout = a.phi_out + start;
-	float sm[8];
-#pragma unroll
-	for(int i = 0; i < 8; i++) sm[i] = 0.f;
-	float area_s = 0.f, area_c = 0.f;
-	int imx = lx, imy = ly;
-	const int sy = BLOCK / lx, sx = BLOCK - sy * lx;
-	int q = threadIdx.x, y = q / lx, x = q - y * lx;
-	__syncthreads();
-	for(; q < n; q += UB * BLOCK) {
-		int xx[UB], yy[UB];
-#pragma unroll
-		for(int u = 0; u < UB; u++) {
-			xx[u] = x;
-			yy[u] = y;
-			x += sx;
-			y += sy;
-			if(x >= lx) {
-				x -= lx;
-				y += 1;
-			}
-		}
-		float m[UB], dx[UB], dy[UB];
-		double vx[UB], vy[UB], p[UB];
-		float d[UB];
-#pragma unroll
-		for(int u = 0; u < UB; u++) {
-			const bool ok = q + u * BLOCK < n;
-			m[u] = ok ? __ldcs(mu + q + u * BLOCK) : 0.f;
-			dx[u] = ok ? __ldcs(gx + q + u * BLOCK) : 0.f;
-			dy[u] = ok ? __ldcs(gy + q + u * BLOCK) : 0.f;
-			vx[u] = ok ? __ldcs(ux + q + u * BLOCK) : 0.0;
-			vy[u] = ok ? __ldcs(uy + q + u * BLOCK) : 0.0;
-			p[u] = ok ? __ldcs(pin + q + u * BLOCK) : 0.0;
-			d[u] = (UPD == UP_CORR && ok) ? __ldcs(dold + q + u * BLOCK) : 0.f;
-		}
-#pragma unroll
-		for(int u = 0; u < UB; u++) {
-			if(q + u * BLOCK >= n) break;
-			const float dphi = -J0 * m[u] - d2f_fast(vx[u]) * dx[u] - d2f_fast(vy[u]) * dy[u];
-			float pn;
-			if(UPD == UP_PRED) {
-				dold[q + u * BLOCK] = dphi;
-				pn = d2f_fast(p[u]) + hdt * (dphi + dphi);
-			}
-			else {
-				pn = d2f_fast(p[u]) + hdt * (dphi + d[u]);
-			}
-			pout[q + u * BLOCK] = f2d_int(pn);
-			acc_square(pn, area_s, area_c);
-			sm[1] += pn;
-			const float2 cx = trow[xx[u]], cy = trow[lx + yy[u]];
-			sm[2] += pn * cx.x;
-			sm[3] += pn * cx.y;
-			sm[4] += pn * cy.x;
-			sm[5] += pn * cy.y;
-			if(UPD == UP_CORR && pn < 0.09f && pn > 0.01f) {
-				int lxx = xx[u] + cp->offx, lyy = yy[u] + cp->offy;
-				if(lxx >= lx) lxx -= lx;
-				if(lyy >= ly) lyy -= ly;
-				imx = min(imx, lxx);
-				imy = min(imy, lyy);
-			}
-			sm[6] += -.5f * (dx[u] * dx[u] - dy[u] * dy[u]);
-			sm[7] += -dx[u] * dy[u];
-		}
-	}
-	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-	for(int o = 16; o > 0; o >>= 1) {
-		const float s2 = __shfl_down_sync(0xffffffffu, area_s, o);
-		const float c2 = __shfl_down_sync(0xffffffffu, area_c, o);
-		add_df(area_s, area_c, s2, c2);
-#pragma unroll
-		for(int i = 1; i < 8; i++) sm[i] += __shfl_down_sync(0xffffffffu, sm[i], o);
-	}
-	CellSum &o = a.csum[ci];
-	if(lane == 0) {
-		o.area[warp] = (double) area_s + (double) area_c;
-#pragma unroll
-		for(int i = 1; i < 8; i++) o.part[warp][i] = sm[i];
-#pragma unroll
-		for(int i = 8; i < 12; i++) o.part[warp][i] = 0.f;
-	}
-	if(UPD == UP_CORR) {
-		__shared__ int ired[2 * (BLOCK / 32)];
-		int im[2] = {imx, imy};
-		block_min<2>(im, ired);
-		imx = im[0];
-		imy = im[1];
-	}
-	if(threadIdx.x == 0) {
-		o.imin[0] = imx;
-		o.imin[1] = imy;
-		o.nw = BLOCK / 32;
-		o.perim = 0.0;
-	}
-}
-
-// The same update with its inputs staged by the Tensor Memory Accelerator:
-// thread 0 moves each chunk of CH sites of every input array into shared
+// sums of the new phi, one CTA per cell.  The inputs are staged by the
+// Tensor Memory Accelerator: thread 0 moves each chunk of CH sites of every
+// input array into shared
 // memory with one bulk copy per array (cp.async.bulk, completion counted in
 // bytes on the stage's mbarrier), NST chunks ahead of the threads, so the
 // bytes in flight no longer depend on how many loads each thread keeps
@@ -776,21 +601,12 @@ constexpr size_t upd_bulk_smem() {
 	       (UpdStage<UPD>::NF * (UPD_BULK_CH + 8) * 4 + 3 * (UPD_BULK_CH + 4) * 8);
 }
 
-template<int BLOCK>
-static void launch_update_f32_b(int upd, const CellArgs &a, cudaStream_t s) {
-	// the bulk-copy form needs 16-byte aligned array bases (engine allocations are)
-	const bool aligned = ((reinterpret_cast<uintptr_t>(a.muf) | reinterpret_cast<uintptr_t>(a.dxf) |
-	                       reinterpret_cast<uintptr_t>(a.dyf) | reinterpret_cast<uintptr_t>(a.dphif) |
-	                       reinterpret_cast<uintptr_t>(a.vxg) | reinterpret_cast<uintptr_t>(a.vyg) |
-	                       reinterpret_cast<uintptr_t>(upd == UP_PRED ? a.phi_eval : a.phi_old)) & 15u) == 0;
-	if(aligned) {
-		constexpr int B = UPD_BULK_BLOCK, CH = UPD_BULK_CH, NST = UPD_BULK_NST;
-		if(upd == UP_PRED) cell_update_bulk<UP_PRED, B, CH, NST><<<a.N, B, upd_bulk_smem<UP_PRED>(), s>>>(a);
-		else cell_update_bulk<UP_CORR, B, CH, NST><<<a.N, B, upd_bulk_smem<UP_CORR>(), s>>>(a);
-		return;
-	}
-	if(upd == UP_PRED) cell_update_f32<UP_PRED, BLOCK><<<a.N, BLOCK, 0, s>>>(a);
-	else cell_update_f32<UP_CORR, BLOCK><<<a.N, BLOCK, 0, s>>>(a);
+// The update's inputs are engine allocations (cudaMalloc: 256-byte aligned),
+// as the bulk copies need.
+static void launch_update_bulk(int upd, const CellArgs &a, cudaStream_t s) {
+	constexpr int B = UPD_BULK_BLOCK, CH = UPD_BULK_CH, NST = UPD_BULK_NST;
+	if(upd == UP_PRED) cell_update_bulk<UP_PRED, B, CH, NST><<<a.N, B, upd_bulk_smem<UP_PRED>(), s>>>(a);
+	else cell_update_bulk<UP_CORR, B, CH, NST><<<a.N, B, upd_bulk_smem<UP_CORR>(), s>>>(a);
 }
 
 // (eval, upd) pairs with an FP32 kernel, for every model and tile
@@ -824,10 +640,7 @@ static bool launch_f32_m(int eval, int upd, const CellArgs &a, cudaStream_t s, i
 
 bool launch_cell_kernel_f32(int model, int eval, int upd, const CellArgs &a, cudaStream_t s, int block) {
 	if((model == M_POLAR || model == M_WET) && eval == EV_NONE && upd != UP_NONE && a.split && !a.P.conserved) {
-		if(a.N <= 0) return true;
-		if(block == 128) launch_update_f32_b<128>(upd, a, s);
-		else if(block == 512) launch_update_f32_b<512>(upd, a, s);
-		else launch_update_f32_b<256>(upd, a, s);
+		if(a.N > 0) launch_update_bulk(upd, a, s);
 		return true;
 	}
 	if(model == M_POLAR) {
