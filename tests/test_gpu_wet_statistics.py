@@ -8,8 +8,9 @@ statistics instead -- mean cell speed (unwrapped centre-of-mass
 displacement per unit time), the area distribution (mean and standard
 deviation over cells) and the shape index (mean elongation |S| and mean
 aspect ratio of the cells' shape tensors, rc_observe_cells) -- time-averaged
-over 2000 steps of the 256^2 / 400-cell wetmodel monolayer after 100 steps of
-transient, each within 1% of the plain FP64 run's."""
+over 2000 steps of the 256^2 / 400-cell wetmodel monolayer, and over 1000
+steps of the 1024^2 / 6400-cell one, after 100 steps of transient, each
+within 1% of the plain FP64 run's."""
 from __future__ import annotations
 
 import numpy as np
@@ -110,4 +111,30 @@ def test_fp32_fields_statistics_within_one_percent(wet256, solver):
         e.set_solver(solver)
     got = statistics(e, m.L)
     assert e.stats.cg_max_rel_residual < 1e-8
+    _check(got, base)
+
+
+def test_learned_fp32_statistics_at_1024_within_one_percent():
+    """The benchmark spec's configuration, judged the same way: the wet 1024^2 /
+    6400-cell monolayer (the bench's default line) with FP32 site arithmetic
+    and the learned solve (the network the bench trains at 256^2, committed
+    as tests/golden/unet_wet256.npy) against the plain FP64 run from the same
+    start, statistics over 1000 steps after 100 of transient."""
+    import os
+    import bench
+    params = np.load(os.path.join(os.path.dirname(__file__), "golden", "unet_wet256.npy")).astype(np.float64)
+    w = bench.workload("wet1024")
+    (keys, m), = bench.make_case(w)
+    ref = bench.make_engine("wet1024", abi.RC_PRECISION_DOUBLE, 0)
+    ref.set_solver(abi.RC_SOLVER_PLAIN_FP64)
+    ref.step(WARM)
+    base = statistics(ref, m.L, steps=1000)
+    ref.close()
+    e = bench.make_engine("wet1024", abi.RC_PRECISION_FLOAT, 0)
+    e.set_params(params)
+    e.set_solver(abi.RC_SOLVER_LEARNED)
+    e.step(WARM)
+    got = statistics(e, m.L, steps=1000)
+    assert e.stats.cg_max_rel_residual < 1e-8
+    e.close()
     _check(got, base)
