@@ -405,20 +405,26 @@ __global__ void __launch_bounds__(BLOCK) cell_kernel_f32(const CellArgs a) {
 // FD_CPUBackend.cpp:44-120): dphi = -J0 mu - v . grad phi from the last
 // evaluation's mu and gradient, phi* = phi + dt dphi (predictor) or
 // phi^{n+1} = phi^n + dt/2 (dphi + dphi^n) (corrector), and the per-cell
-// sums of the new phi, one CTA per cell.  The inputs are staged by the
-// Tensor Memory Accelerator: thread 0 moves each chunk of CH sites of every
-// input array into shared
-// memory with one bulk copy per array (cp.async.bulk, completion counted in
-// bytes on the stage's mbarrier), NST chunks ahead of the threads, so the
-// bytes in flight no longer depend on how many loads each thread keeps
-// outstanding.  The copies move 16-byte aligned windows around the chunk
-// (up to 3 floats or 1 double of slack at each end; the engine pads the
-// arrays by 8 elements so a window never leaves its allocation); values in
-// the slack belong to neighbouring sites and are never used.  In the
-// corrector phi^n is read and phi^{n+1} written in place: a site's new
-// value is written only after its chunk has landed, and a window's slack
-// value of a site being written elsewhere is not read.  Every completion
-// wait is bounded (ERR_COPY).
+// sums of the new phi, one CTA per cell.
+//
+// A pure stream, staged by the Tensor Memory Accelerator: thread 0 moves
+// each chunk of CH sites of every input array into shared memory with one
+// bulk copy per array (cp.async.bulk, completion counted in bytes on the
+// stage's mbarrier), NST chunks ahead of the threads, so the bytes in flight
+// do not depend on how many loads each thread keeps outstanding.  The copies
+// move 16-byte aligned windows around the chunk (up to 3 floats or 1 double
+// of slack at each end; the engine pads the arrays by 8 elements so that a
+// window never leaves its allocation); values in the slack belong to
+// neighbouring sites and are never used.  In the corrector phi^n is read and
+// phi^{n+1} written in place: a site's new value is written only after its
+// chunk has landed, and no site's value is read from another chunk's
+// window.  Every completion wait is bounded (ERR_COPY).
+//
+// Per site: no set-up beyond the patch's trig rows (centre-of-mass sums),
+// staged once per cell already rotated by the patch offset; the double ->
+// float conversions in the short integer form (d2f_fast); the area sum in
+// double-float.  Per-warp partial sums go to the epilogue kernel
+// (cell_finish_kernel), which every FP32 wet engine runs.
 constexpr long long UPD_WAIT_LIMIT = 1LL << 22;  // mbarrier polls
 
 template<int UPD>
