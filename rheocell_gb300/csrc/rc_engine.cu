@@ -2061,7 +2061,9 @@ int rc_selftest_conversions(const double *in, float *exact, float *fast, float *
                             int device) {
 	if(!in || !exact || !fast || !cuda_rn || !widened || n <= 0)
 		return set_err(nullptr, RC_ERR_INVALID, "rc_selftest_conversions: invalid arguments");
-	if(cudaSetDevice(device) != cudaSuccess) return set_err(nullptr, RC_ERR_CUDA, "rc_selftest_conversions: no device %d", device);
+	int prev = 0;
+	if(cudaGetDevice(&prev) != cudaSuccess || cudaSetDevice(device) != cudaSuccess)
+		return set_err(nullptr, RC_ERR_CUDA, "rc_selftest_conversions: no device %d", device);
 	double *din = nullptr, *dw = nullptr;
 	float *de = nullptr, *df = nullptr, *dc = nullptr;
 	const size_t nd = sizeof(double) * (size_t) n, nf = sizeof(float) * (size_t) n;
@@ -2085,6 +2087,7 @@ int rc_selftest_conversions(const double *in, float *exact, float *fast, float *
 	cudaFree(de);
 	cudaFree(df);
 	cudaFree(dc);
+	cudaSetDevice(prev);  // the caller's current device is left as it was
 	if(c != cudaSuccess) return set_err(nullptr, RC_ERR_CUDA, "rc_selftest_conversions: %s", cudaGetErrorString(c));
 	return RC_OK;
 }
